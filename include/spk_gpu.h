@@ -1,0 +1,162 @@
+/*
+ * spk_gpu.h - C ABI of the GB300 (sm_103a) numeric engine for the Sparspak
+ * LU SparseSolver.
+ *
+ * The host keeps ordering, elimination tree and symbolic factorisation (see
+ * spk_host.h) and hands the resulting supernodal structure to this library,
+ * which owns all numeric work on one GPU: value assembly (_inmatrix!), the
+ * supernodal LU with in-block partial pivoting (_lufactor!), the triangular
+ * solves (_lulsolve!/_luusolve!), a residual and iterative refinement.
+ * There is no CPU fallback: without a usable CUDA device every call fails.
+ *
+ * Conventions
+ *  - Structure arrays are int64 and use the reference's layout; index_base
+ *    says whether their values are 1-based (the reference's) or 0-based.
+ *  - Every function returns SPK_OK (0) or a negative SPK_E* code, never
+ *    throws across the ABI, and leaves a message for spk_last_error().
+ *  - A handle is used by one host thread at a time.  Work is issued on the
+ *    handle's stream (spk_set_stream); functions that return results to the
+ *    host synchronise that stream before returning.
+ *  - `where` arguments: SPK_HOST for host memory, SPK_DEVICE for device
+ *    memory of the handle's device.
+ */
+#ifndef SPK_GPU_H
+#define SPK_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPK_OK 0
+#define SPK_EARG (-1)      /* invalid argument                                    */
+#define SPK_ECUDA (-2)     /* CUDA runtime error (no device, launch failure, ...)  */
+#define SPK_ENOMEM (-3)    /* device or host allocation failed                     */
+#define SPK_ESEQ (-4)      /* call out of sequence (e.g. solve before factor)      */
+#define SPK_ESTRUCT (-5)   /* structure inconsistent, or A has an entry with no
+                              slot in the factor ("No space for matrix element")   */
+#define SPK_ESINGULAR (-6) /* a diagonal block had an exactly zero pivot           */
+#define SPK_ENOCONV (-7)   /* refinement did not reach the requested tolerance     */
+
+#define SPK_HOST 0
+#define SPK_DEVICE 1
+
+#define SPK_FP64 0         /* factor, solve and residual in double                */
+#define SPK_FP32 1         /* factor and solve in float; residual and correction
+                              in double (mixed form for spk_refine)               */
+
+typedef struct spk_handle spk_handle;
+
+/*
+ * Create a handle for one supernodal structure and copy it to the device.
+ * Replaces the allocation of lnz/unz/ipiv at the end of _symbolicfactor!
+ * (src/SparseMethod/SpkSparseBase.jl:236-248) and precomputes, once per
+ * structure, what _lufactor! rebuilds on every call: the relative index
+ * maps of _ldindx!/_igathr! (src/SparseSpdMethod/SpkSpdMMOps.jl:70-102) and
+ * the order of supernode updates (the link lists of
+ * src/SparseMethod/SpkLUFactor.jl:89-228), as an elimination-tree level
+ * schedule.  Arrays: xsuper[nsuper+1], snode[n], xlindx[nsuper+1],
+ * lindx[xlindx[nsuper+1]-1], xlnz[n+1], xunz[n+1] (reference meaning).
+ * Supernodes may be at most 64 columns wide (with maxblocksize 30 the
+ * reference's splitting rule yields pieces of up to 46 columns).
+ */
+int spk_create(int64_t n, int64_t nsuper, const int64_t* xsuper, const int64_t* snode,
+               const int64_t* xlindx, const int64_t* lindx, const int64_t* xlnz,
+               const int64_t* xunz, int index_base, spk_handle** out);
+
+/* Issue all further work of this handle on `stream` (a cudaStream_t, or
+ * NULL for the handle's own stream). */
+int spk_set_stream(spk_handle* h, void* stream);
+
+/*
+ * Fix the sparsity pattern of A (CSC: colptr[ncols+1], rowval[nnz]) and the
+ * permutation (rperm[new] = old, rinvp[old] = new; rows and columns are
+ * permuted alike, as in the reference).  Builds the value -> factor-slot map
+ * that _inmatrix! finds by linear search for every entry
+ * (src/SparseCSCInterface/SparseCSCInterface.jl:101-169 and
+ * src/SparseMethod/SpkSparseBase.jl:302-372), and the row-ordered copy of
+ * the pattern used by the residual.  Fails with SPK_ESTRUCT, naming the
+ * entry, when an entry of A has no slot in the factor.
+ */
+int spk_set_pattern(spk_handle* h, int64_t ncols, const int64_t* colptr, const int64_t* rowval,
+                    const int64_t* rperm, const int64_t* rinvp, int index_base);
+
+/*
+ * Load the values of A (nzval[nnz], in the CSC order given to
+ * spk_set_pattern) into the factor storage of the given precision: zero
+ * the storage, then scatter-add each value into its slot.  Replaces the body
+ * of _inmatrix!.  Also keeps an FP64 copy of A on the device for spk_refine.
+ */
+int spk_load_values(spk_handle* h, const double* nzval, int where, int precision);
+
+/*
+ * Numeric LU factorisation in place, in the given precision.  Replaces
+ * _lufactor! (src/SparseMethod/SpkLUFactor.jl:60-255) as called by _factor!
+ * (src/SparseMethod/SpkSparseBase.jl:378-391): the same supernode partition,
+ * in-block partial pivoting with the first strict maximum as pivot
+ * (src/Utilities/GenericBlasLapackFragments.jl:56-100) and the same pivots.
+ * *first_singular (may be NULL) receives 0, or the 1-based index of the
+ * first supernode whose diagonal block had an exactly zero pivot, in which
+ * case the call returns SPK_ESINGULAR (the reference only reports the last
+ * supernode's status, SpkLUFactor.jl:230-233).
+ */
+int spk_factor(spk_handle* h, int precision, int64_t* first_singular);
+
+/*
+ * Solve A X = B for nrhs right-hand sides stored column-major with leading
+ * dimension ldb, in original (unpermuted) order, overwritten by X.  Uses the
+ * factor of the given precision.  Replaces _triangularsolve!
+ * (src/SparseMethod/SpkSparseBase.jl:400-416) = permute, _lulsolve!,
+ * _luusolve! (src/SparseMethod/SpkLUFactor.jl:269-377), unpermute; the
+ * reference solves one vector per call.
+ */
+int spk_solve(spk_handle* h, double* b, int64_t nrhs, int64_t ldb, int where, int precision);
+
+/*
+ * Iterative refinement: x := solve(b) with the factor of `precision`, then
+ * repeat r = b - A x (FP64), x += solve(r) until max_j ||r_j||_2/||b_j||_2
+ * <= tol or max_iter corrections were applied.  b and x are n x nrhs,
+ * column-major, leading dimension ld, original order.  Reports the number
+ * of corrections and the final relative residual.  Returns SPK_ENOCONV if
+ * tol was not reached.  Modelled on the reference's commented-out
+ * refinement (src/SparseSpdMethod/SpkSparseSpdSolver.jl:267-343).
+ */
+int spk_refine(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where,
+               int precision, double tol, int max_iter, int* iters, double* relres);
+
+/*
+ * Relative residual max_j ||b_j - A x_j||_2 / ||b_j||_2 in FP64 for the
+ * current A (the reference's analogue is computeresidual,
+ * src/Problem/SpkProblem.jl:448-496).
+ */
+int spk_residual(spk_handle* h, const double* b, const double* x, int64_t nrhs, int64_t ld,
+                 int where, double* relres);
+
+/*
+ * Copy the factor of the given precision back in the reference's layout:
+ * lnz[xlnz[n+1]-1], unz[xunz[n+1]-1] and ipiv[n] (1-based, local to each
+ * supernode's diagonal block), exactly as _SparseBase holds them after
+ * factor! (src/SparseMethod/SpkSparseBase.jl:99-125).  Before spk_factor
+ * (after spk_load_values) it returns the assembled A, with ipiv all zero, as
+ * after inmatrix!.  Any pointer may be NULL.
+ */
+int spk_get_factors(spk_handle* h, int precision, double* lnz, double* unz, int64_t* ipiv);
+
+/* Statistics of the structure: fronts (merged chains of supernodes), levels of
+ * the schedule, factor entries, and the LU flop count sum_j (c_j-1)+2(c_j-1)^2. */
+int spk_stats(spk_handle* h, int64_t* nfronts, int64_t* nlevels, int64_t* factor_entries,
+              double* lu_flops);
+
+/* Text of the last error on this handle (never NULL); with h == NULL, the
+ * reason the last spk_create on this thread failed. */
+const char* spk_last_error(spk_handle* h);
+
+/* Release the handle and its device memory. */
+void spk_destroy(spk_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPK_GPU_H */

@@ -1,0 +1,932 @@
+// C-ABI of the GB300 supernodal LU engine: structure analysis, the level
+// schedule and the entry points of include/spk_gpu.h.  The kernels live in
+// spk_kernels.cuh; their storage layout is described there.
+
+#include "../../include/spk_gpu.h"
+#include "spk_kernels.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+using spk::ll;
+typedef int64_t i64;
+
+namespace {
+
+struct LaunchRec {
+    i64 off = 0;      // into sched_ids; prefix array at off + index_of_launch
+    i64 poff = 0;     // into sched_prefix
+    int count = 0;
+    int tiles = 0;
+};
+
+struct LevelPlan {
+    LaunchRec getrf0, schur, bwdu;
+    std::vector<LaunchRec> panel, trail, fwd, bwd;
+};
+
+struct HFront {
+    i64 f;
+    int nf, m, piece0, npieces, parent, level;
+    i64 loff, uoff, rows_off, runid_off;
+    int run0, nruns;
+};
+
+template <typename T>
+struct Storage {
+    T* d = nullptr;
+    bool loaded = false;    // values assembled since the last factor
+    bool factored = false;
+};
+
+}  // namespace
+
+struct spk_handle {
+    i64 n = 0, nsuper = 0;
+    std::vector<int> xs;            // 0-based first column per supernode [nsuper+1]
+    std::vector<int> lindx0;        // 0-based rows
+    std::vector<i64> xlindx0;       // 0-based offsets [nsuper+1]
+    std::vector<i64> xlnz0, xunz0;  // reference layout, 0-based offsets [n+1]
+    std::vector<HFront> fronts;
+    std::vector<int> col_front;     // column -> front
+    std::vector<int> rows;          // concatenated R_F
+    std::vector<int> runid, run_tgt, run_start;
+    std::vector<ll> run_rel;
+    std::vector<int> rel;
+    std::vector<LevelPlan> levels;
+    std::vector<int> sched_ids, sched_prefix;
+    i64 fsize = 0;
+    int wmax = 1;             // widest supernode
+    double lu_flops = 0.0;
+
+    // device structure
+    spk::DFront* d_fronts = nullptr;
+    int *d_xs = nullptr, *d_rows = nullptr, *d_runid = nullptr, *d_run_tgt = nullptr, *d_run_start = nullptr,
+        *d_rel = nullptr;
+    ll* d_run_rel = nullptr;
+    int *d_sched_ids = nullptr, *d_sched_prefix = nullptr;
+    int* d_ipiv = nullptr;
+    int* d_info = nullptr;
+    spk::Sched sched{};
+
+    // pattern and values
+    bool have_pattern = false, have_values = false;
+    i64 nnz = 0;
+    std::vector<int> rperm0, rinvp0;
+    ll* d_slot = nullptr;
+    double* d_aval = nullptr;
+    int *d_rowptr = nullptr, *d_col = nullptr;
+    ll* d_src = nullptr;
+    int *d_rperm = nullptr, *d_rinvp = nullptr;
+
+    Storage<double> s64;
+    Storage<float> s32;
+
+    // solve work space (sized for MAXRHS right-hand sides)
+    void *d_wb = nullptr, *d_wy = nullptr, *d_wx = nullptr;   // factor precision
+    double *d_rhs = nullptr, *d_x = nullptr, *d_r = nullptr;  // FP64, n*cap
+    double* d_sums = nullptr;
+    i64 rhs_cap = 0;
+
+    cudaStream_t own = nullptr, stream = nullptr;
+    int device = -1;
+    std::string err;
+};
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+static thread_local std::string g_create_err;
+
+static int set_err(spk_handle* h, int code, const std::string& msg) {
+    if (h) h->err = msg;
+    return code;
+}
+
+#define CU(h, call)                                                                                   \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                        \
+            return set_err(h, e_ == cudaErrorMemoryAllocation ? SPK_ENOMEM : SPK_ECUDA,               \
+                           std::string(#call) + ": " + cudaGetErrorString(e_));                       \
+    } while (0)
+
+template <typename T>
+static int upload(spk_handle* h, T** dst, const std::vector<T>& src) {
+    size_t bytes = sizeof(T) * std::max<size_t>(src.size(), 1);
+    CU(h, cudaMalloc((void**)dst, bytes));
+    if (!src.empty()) CU(h, cudaMemcpy(*dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice));
+    return SPK_OK;
+}
+
+static spk::Launch launch_of(const spk_handle* h, const LaunchRec& r) {
+    spk::Launch L;
+    L.front_ids = h->d_sched_ids + r.off;
+    L.prefix = h->d_sched_prefix + r.poff;
+    L.count = r.count;
+    return L;
+}
+
+// ---------------------------------------------------------------------------
+// structure analysis
+// ---------------------------------------------------------------------------
+static int analyse(spk_handle* h, const int64_t* xsuper, const int64_t* snode, const int64_t* xlindx,
+                   const int64_t* lindx, const int64_t* xlnz, const int64_t* xunz, int base) {
+    const i64 n = h->n, ns = h->nsuper;
+    h->xs.resize(ns + 1);
+    for (i64 s = 0; s <= ns; ++s) h->xs[s] = (int)(xsuper[s] - base);
+    if (h->xs[0] != 0 || h->xs[ns] != n) return set_err(h, SPK_ESTRUCT, "xsuper does not span 1..n");
+    for (i64 s = 0; s < ns; ++s) {
+        int w = h->xs[s + 1] - h->xs[s];
+        if (w <= 0) return set_err(h, SPK_ESTRUCT, "xsuper is not increasing");
+        if (w > spk::MAXW) return set_err(h, SPK_EARG, "supernodes wider than 64 columns are not supported");
+        h->wmax = std::max(h->wmax, w);
+    }
+    for (i64 j = 0; j < n; ++j) {
+        i64 s = snode[j] - base;
+        if (s < 0 || s >= ns || j < h->xs[s] || j >= h->xs[s + 1]) return set_err(h, SPK_ESTRUCT, "snode inconsistent with xsuper");
+    }
+    h->xlindx0.resize(ns + 1);
+    for (i64 s = 0; s <= ns; ++s) h->xlindx0[s] = xlindx[s] - base;
+    const i64 nsub = h->xlindx0[ns];
+    h->lindx0.resize(nsub);
+    for (i64 k = 0; k < nsub; ++k) {
+        i64 r = lindx[k] - base;
+        if (r < 0 || r >= n) return set_err(h, SPK_ESTRUCT, "lindx entry out of range");
+        h->lindx0[k] = (int)r;
+    }
+    h->xlnz0.resize(n + 1);
+    h->xunz0.resize(n + 1);
+    for (i64 j = 0; j <= n; ++j) { h->xlnz0[j] = xlnz[j] - base; h->xunz0[j] = xunz[j] - base; }
+    // each supernode: rows start with its own columns, ascending; rectangular storage
+    for (i64 s = 0; s < ns; ++s) {
+        int f = h->xs[s], w = h->xs[s + 1] - f;
+        i64 a = h->xlindx0[s], len = h->xlindx0[s + 1] - a;
+        if (len < w) return set_err(h, SPK_ESTRUCT, "supernode has fewer rows than columns");
+        for (int k = 0; k < w; ++k)
+            if (h->lindx0[a + k] != f + k) return set_err(h, SPK_ESTRUCT, "lindx does not start with the supernode's columns");
+        for (i64 k = 1; k < len; ++k)
+            if (h->lindx0[a + k] <= h->lindx0[a + k - 1]) return set_err(h, SPK_ESTRUCT, "lindx not ascending");
+        for (int k = 0; k < w; ++k) {
+            if (h->xlnz0[f + k + 1] - h->xlnz0[f + k] != len) return set_err(h, SPK_ESTRUCT, "xlnz inconsistent with lindx");
+            if (h->xunz0[f + k + 1] - h->xunz0[f + k] != len - w) return set_err(h, SPK_ESTRUCT, "xunz inconsistent with lindx");
+        }
+    }
+    // LU flop count from column counts (every column of a supernode of length
+    // len at offset k has c = len - k nonzeros in L)
+    double fl = 0.0;
+    for (i64 s = 0; s < ns; ++s) {
+        int w = h->xs[s + 1] - h->xs[s];
+        i64 len = h->xlindx0[s + 1] - h->xlindx0[s];
+        for (int k = 0; k < w; ++k) {
+            double c1 = (double)(len - k - 1);
+            fl += c1 + 2.0 * c1 * c1;
+        }
+    }
+    h->lu_flops = fl;
+
+    // fronts: maximal chains s, s+1, ... whose structures nest exactly
+    h->col_front.assign(n, -1);
+    h->fronts.clear();
+    for (i64 s = 0; s < ns;) {
+        i64 e = s;
+        while (e + 1 < ns) {
+            int w = h->xs[e + 1] - h->xs[e];
+            i64 a = h->xlindx0[e], len = h->xlindx0[e + 1] - a;
+            i64 a2 = h->xlindx0[e + 1], len2 = h->xlindx0[e + 2] - a2;
+            if (len - w != len2 || len2 == 0) break;
+            bool same = true;
+            for (i64 k = 0; k < len2; ++k)
+                if (h->lindx0[a + w + k] != h->lindx0[a2 + k]) { same = false; break; }
+            if (!same) break;
+            ++e;
+        }
+        HFront F{};
+        F.f = h->xs[s];
+        F.nf = h->xs[e + 1] - h->xs[s];
+        i64 a = h->xlindx0[e], len = h->xlindx0[e + 1] - a;
+        int we = h->xs[e + 1] - h->xs[e];
+        F.m = (int)(len - we);
+        F.piece0 = (int)s;
+        F.npieces = (int)(e - s + 1);
+        F.rows_off = (i64)h->rows.size();
+        for (i64 k = 0; k < F.m; ++k) h->rows.push_back(h->lindx0[a + we + k]);
+        F.parent = -1;
+        F.level = 0;
+        int id = (int)h->fronts.size();
+        for (i64 j = F.f; j < F.f + F.nf; ++j) h->col_front[j] = id;
+        h->fronts.push_back(F);
+        s = e + 1;
+    }
+    const int nfr = (int)h->fronts.size();
+    i64 off = 0;
+    for (int i = 0; i < nfr; ++i) {
+        HFront& F = h->fronts[i];
+        if (F.m > 0) {
+            int r0 = h->rows[F.rows_off];
+            if (r0 < F.f + F.nf) return set_err(h, SPK_ESTRUCT, "off-diagonal row inside its own front");
+            F.parent = h->col_front[r0];
+        }
+        F.loff = off;
+        off += (i64)(F.nf + F.m) * F.nf;
+        F.uoff = off;
+        off += (i64)F.m * F.nf;
+    }
+    h->fsize = off;
+    for (int i = 0; i < nfr; ++i)
+        if (h->fronts[i].parent >= 0)
+            h->fronts[h->fronts[i].parent].level =
+                std::max(h->fronts[h->fronts[i].parent].level, h->fronts[i].level + 1);
+    // runs and relative positions
+    h->runid.clear();
+    h->run_tgt.clear();
+    h->run_start.clear();
+    h->run_rel.clear();
+    h->rel.clear();
+    for (int i = 0; i < nfr; ++i) {
+        HFront& F = h->fronts[i];
+        F.runid_off = (i64)h->runid.size();
+        F.run0 = (int)h->run_tgt.size();
+        F.nruns = 0;
+        const int* R = h->rows.data() + F.rows_off;
+        int x = 0;
+        while (x < F.m) {
+            int g = h->col_front[R[x]];
+            const HFront& G = h->fronts[g];
+            int run = (int)h->run_tgt.size();
+            h->run_tgt.push_back(g);
+            h->run_start.push_back(x);
+            h->run_rel.push_back((ll)h->rel.size());
+            ++F.nruns;
+            const int* RG = h->rows.data() + G.rows_off;
+            int q = 0;
+            for (int y = x; y < F.m; ++y) {
+                int row = R[y];
+                int pos;
+                if (row < G.f) return set_err(h, SPK_ESTRUCT, "update row precedes its target front");
+                if (row < G.f + G.nf) pos = (int)(row - G.f);
+                else {
+                    while (q < G.m && RG[q] < row) ++q;
+                    if (q >= G.m || RG[q] != row)
+                        return set_err(h, SPK_ESTRUCT, "supernodal structure is not closed under elimination");
+                    pos = G.nf + q;
+                }
+                h->rel.push_back(pos);
+            }
+            int y = x;
+            while (y < F.m && R[y] < G.f + G.nf) { h->runid.push_back(run); ++y; }
+            x = y;
+        }
+    }
+    return SPK_OK;
+}
+
+static void add_launch(spk_handle* h, LaunchRec& rec, const std::vector<int>& ids, const std::vector<int>& tiles) {
+    rec.off = (i64)h->sched_ids.size();
+    rec.poff = (i64)h->sched_prefix.size();
+    rec.count = 0;
+    int acc = 0;
+    for (size_t k = 0; k < ids.size(); ++k) {
+        if (tiles[k] <= 0) continue;
+        h->sched_ids.push_back(ids[k]);
+        h->sched_prefix.push_back(acc);
+        acc += tiles[k];
+        ++rec.count;
+    }
+    h->sched_prefix.push_back(acc);
+    rec.tiles = acc;
+}
+
+static void build_schedule(spk_handle* h) {
+    using spk::cdiv;
+    int nlev = 0;
+    for (auto& F : h->fronts) nlev = std::max(nlev, F.level + 1);
+    std::vector<std::vector<int>> at(nlev);
+    for (int i = 0; i < (int)h->fronts.size(); ++i) at[h->fronts[i].level].push_back(i);
+    h->levels.assign(nlev, LevelPlan());
+    h->sched_ids.clear();
+    h->sched_prefix.clear();
+    for (int l = 0; l < nlev; ++l) {
+        LevelPlan& P = h->levels[l];
+        const std::vector<int>& ids = at[l];
+        int maxp = 0;
+        for (int id : ids) maxp = std::max(maxp, h->fronts[id].npieces);
+        std::vector<int> t(ids.size());
+        for (size_t k = 0; k < ids.size(); ++k) t[k] = 1;
+        add_launch(h, P.getrf0, ids, t);
+        P.panel.resize(maxp);
+        P.trail.resize(maxp);
+        P.fwd.resize(maxp);
+        P.bwd.resize(maxp);
+        for (int s = 0; s < maxp; ++s) {
+            std::vector<int> tp(ids.size()), tt(ids.size()), tf(ids.size()), tb(ids.size());
+            for (size_t k = 0; k < ids.size(); ++k) {
+                const HFront& F = h->fronts[ids[k]];
+                if (s >= F.npieces) { tp[k] = tt[k] = tf[k] = tb[k] = 0; continue; }
+                int p = F.piece0 + s;
+                int p1 = h->xs[p + 1] - (int)F.f;
+                int ld = F.nf + F.m;
+                tp[k] = cdiv(ld - p1, spk::TP) + cdiv(F.nf - p1, spk::TP) + cdiv(F.m, spk::TP);
+                tt[k] = cdiv(ld - p1, spk::TT) * cdiv(F.nf - p1, spk::TT) + cdiv(F.nf - p1, spk::TT) * cdiv(F.m, spk::TT);
+                tf[k] = std::max(1, cdiv(ld - p1, spk::TS));
+                int q = F.piece0 + F.npieces - 1 - s;
+                int q0 = h->xs[q] - (int)F.f;
+                tb[k] = std::max(1, cdiv(q0, spk::TS));
+            }
+            add_launch(h, P.panel[s], ids, tp);
+            add_launch(h, P.trail[s], ids, tt);
+            add_launch(h, P.fwd[s], ids, tf);
+            add_launch(h, P.bwd[s], ids, tb);
+        }
+        std::vector<int> tsch(ids.size()), tbu(ids.size());
+        for (size_t k = 0; k < ids.size(); ++k) {
+            const HFront& F = h->fronts[ids[k]];
+            tsch[k] = F.m > 0 ? cdiv(F.m, spk::TT) * cdiv(F.m, spk::TT) : 0;
+            tbu[k] = F.m > 0 ? cdiv(F.nf, spk::TS / 32) : 0;
+        }
+        add_launch(h, P.schur, ids, tsch);
+        add_launch(h, P.bwdu, ids, tbu);
+    }
+}
+
+static int upload_structure(spk_handle* h) {
+    std::vector<spk::DFront> df(h->fronts.size());
+    for (size_t i = 0; i < h->fronts.size(); ++i) {
+        const HFront& F = h->fronts[i];
+        spk::DFront& d = df[i];
+        d.loff = F.loff;
+        d.uoff = F.uoff;
+        d.rows_off = F.rows_off;
+        d.runid_off = F.runid_off;
+        d.f = (int)F.f;
+        d.nf = F.nf;
+        d.m = F.m;
+        d.ld = F.nf + F.m;
+        d.piece0 = F.piece0;
+        d.npieces = F.npieces;
+        d.run0 = F.run0;
+        d.pad = 0;
+    }
+    int rc;
+    if ((rc = upload(h, &h->d_fronts, df))) return rc;
+    if ((rc = upload(h, &h->d_xs, h->xs))) return rc;
+    if ((rc = upload(h, &h->d_rows, h->rows))) return rc;
+    if ((rc = upload(h, &h->d_runid, h->runid))) return rc;
+    if ((rc = upload(h, &h->d_run_tgt, h->run_tgt))) return rc;
+    if ((rc = upload(h, &h->d_run_start, h->run_start))) return rc;
+    if ((rc = upload(h, &h->d_run_rel, h->run_rel))) return rc;
+    if ((rc = upload(h, &h->d_rel, h->rel))) return rc;
+    if ((rc = upload(h, &h->d_sched_ids, h->sched_ids))) return rc;
+    if ((rc = upload(h, &h->d_sched_prefix, h->sched_prefix))) return rc;
+    CU(h, cudaMalloc((void**)&h->d_ipiv, sizeof(int) * std::max<i64>(h->n, 1)));
+    CU(h, cudaMalloc((void**)&h->d_info, sizeof(int)));
+    h->sched.fronts = h->d_fronts;
+    h->sched.xsuper = h->d_xs;
+    h->sched.rows = h->d_rows;
+    h->sched.runid = h->d_runid;
+    h->sched.run_tgt = h->d_run_tgt;
+    h->sched.run_start = h->d_run_start;
+    h->sched.run_rel = h->d_run_rel;
+    h->sched.rel = h->d_rel;
+    return SPK_OK;
+}
+
+template <typename T>
+static Storage<T>& storage(spk_handle* h);
+template <>
+Storage<double>& storage<double>(spk_handle* h) { return h->s64; }
+template <>
+Storage<float>& storage<float>(spk_handle* h) { return h->s32; }
+
+template <typename T>
+static int ensure_storage(spk_handle* h) {
+    Storage<T>& S = storage<T>(h);
+    if (!S.d) CU(h, cudaMalloc((void**)&S.d, sizeof(T) * std::max<i64>(h->fsize, 1)));
+    return SPK_OK;
+}
+
+static int ensure_rhs(spk_handle* h, i64 nrhs) {
+    if (nrhs <= h->rhs_cap) return SPK_OK;
+    cudaFree(h->d_wb); cudaFree(h->d_wy); cudaFree(h->d_wx);
+    cudaFree(h->d_rhs); cudaFree(h->d_x); cudaFree(h->d_r); cudaFree(h->d_sums);
+    h->d_wb = h->d_wy = h->d_wx = nullptr;
+    h->d_rhs = h->d_x = h->d_r = h->d_sums = nullptr;
+    h->rhs_cap = 0;
+    const i64 chunk = std::min<i64>(nrhs, spk::MAXRHS);
+    const size_t wbytes = sizeof(double) * (size_t)h->n * (size_t)chunk;
+    const size_t bytes = sizeof(double) * (size_t)h->n * (size_t)nrhs;
+    CU(h, cudaMalloc(&h->d_wb, wbytes));
+    CU(h, cudaMalloc(&h->d_wy, wbytes));
+    CU(h, cudaMalloc(&h->d_wx, wbytes));
+    CU(h, cudaMalloc((void**)&h->d_rhs, bytes));
+    CU(h, cudaMalloc((void**)&h->d_x, bytes));
+    CU(h, cudaMalloc((void**)&h->d_r, bytes));
+    CU(h, cudaMalloc((void**)&h->d_sums, sizeof(double) * 2 * (size_t)nrhs));
+    h->rhs_cap = nrhs;
+    return SPK_OK;
+}
+
+// ---------------------------------------------------------------------------
+// numeric phases
+// ---------------------------------------------------------------------------
+template <typename T>
+static int run_factor(spk_handle* h) {
+    Storage<T>& S = storage<T>(h);
+    T* fac = S.d;
+    const int big = INT_MAX;
+    const size_t panel_smem = sizeof(T) * (size_t)(h->wmax * h->wmax + h->wmax * spk::TP) + sizeof(int) * spk::MAXW;
+    CU(h, cudaFuncSetAttribute(spk::k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem));
+    CU(h, cudaMemcpyAsync(h->d_info, &big, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    for (const LevelPlan& P : h->levels) {
+        if (P.getrf0.tiles > 0)
+            spk::k_getrf_first<T><<<P.getrf0.tiles, 128, 0, h->stream>>>(fac, h->d_ipiv, h->d_info, h->sched,
+                                                                            launch_of(h, P.getrf0));
+        for (size_t s = 0; s < P.panel.size(); ++s) {
+            if (P.panel[s].tiles > 0)
+                spk::k_panel<T><<<P.panel[s].tiles, spk::TP, panel_smem, h->stream>>>(
+                    fac, h->d_ipiv, h->sched, launch_of(h, P.panel[s]), (int)s, h->wmax);
+            if (P.trail[s].tiles > 0)
+                spk::k_trail<T><<<P.trail[s].tiles, 256, 0, h->stream>>>(fac, h->d_ipiv, h->d_info, h->sched,
+                                                                           launch_of(h, P.trail[s]), (int)s);
+        }
+        if (P.schur.tiles > 0)
+            spk::k_schur<T><<<P.schur.tiles, 256, 0, h->stream>>>(fac, h->sched, launch_of(h, P.schur));
+    }
+    CU(h, cudaGetLastError());
+    return SPK_OK;
+}
+
+// Solve in place on the permuted work vectors: wb (rhs, consumed) -> wx.
+template <typename T>
+static int run_solve_permuted(spk_handle* h, int nrhs) {
+    const T* fac = storage<T>(h).d;
+    T* b = (T*)h->d_wb;
+    T* y = (T*)h->d_wy;
+    T* x = (T*)h->d_wx;
+    const int n = (int)h->n;
+    for (const LevelPlan& P : h->levels)
+        for (size_t s = 0; s < P.fwd.size(); ++s)
+            if (P.fwd[s].tiles > 0)
+                spk::k_fwd<T><<<P.fwd[s].tiles, spk::TS, 0, h->stream>>>(fac, h->d_ipiv, b, y, n, nrhs, h->sched,
+                                                                          launch_of(h, P.fwd[s]), (int)s);
+    for (size_t l = h->levels.size(); l-- > 0;) {
+        const LevelPlan& P = h->levels[l];
+        if (P.bwdu.tiles > 0)
+            spk::k_bwd_u12<T><<<P.bwdu.tiles, spk::TS, 0, h->stream>>>(fac, y, x, n, nrhs, h->sched,
+                                                                        launch_of(h, P.bwdu));
+        for (size_t s = 0; s < P.bwd.size(); ++s)
+            if (P.bwd[s].tiles > 0)
+                spk::k_bwd<T><<<P.bwd[s].tiles, spk::TS, 0, h->stream>>>(fac, y, x, n, nrhs, h->sched,
+                                                                          launch_of(h, P.bwd[s]), (int)s);
+    }
+    CU(h, cudaGetLastError());
+    return SPK_OK;
+}
+
+// x(:, 0:nrhs) (=|+=) A^{-1} rhs(:, 0:nrhs), both device FP64, original order.
+template <typename T>
+static int solve_device(spk_handle* h, const double* rhs, i64 ldr, double* x, i64 ldx, i64 nrhs, int accumulate) {
+    const int n = (int)h->n;
+    for (i64 c0 = 0; c0 < nrhs; c0 += spk::MAXRHS) {
+        int nc = (int)std::min<i64>(spk::MAXRHS, nrhs - c0);
+        ll tot = (ll)n * nc;
+        int blocks = (int)((tot + 255) / 256);
+        spk::k_permute<double, T><<<blocks, 256, 0, h->stream>>>(rhs + c0 * ldr, ldr, (T*)h->d_wb, n, h->d_rperm, n, nc);
+        int rc = run_solve_permuted<T>(h, nc);
+        if (rc) return rc;
+        spk::k_unpermute<T><<<blocks, 256, 0, h->stream>>>((const T*)h->d_wx, n, x + c0 * ldx, ldx, h->d_rinvp, n, nc,
+                                                           accumulate);
+    }
+    CU(h, cudaGetLastError());
+    return SPK_OK;
+}
+
+static int residual_device(spk_handle* h, const double* b, i64 ldb, const double* x, i64 ldx, i64 nrhs,
+                           double* relres) {
+    const int n = (int)h->n;
+    CU(h, cudaMemsetAsync(h->d_sums, 0, sizeof(double) * 2 * (size_t)nrhs, h->stream));
+    dim3 grid((n + 255) / 256, (unsigned)nrhs);
+    spk::k_residual<<<grid, 256, 0, h->stream>>>(h->d_aval, h->d_rowptr, h->d_col, h->d_src, x, ldx, b, ldb, h->d_r, n,
+                                                 (int)nrhs, h->d_sums);
+    CU(h, cudaGetLastError());
+    std::vector<double> sums(2 * nrhs);
+    CU(h, cudaMemcpyAsync(sums.data(), h->d_sums, sizeof(double) * 2 * nrhs, cudaMemcpyDeviceToHost, h->stream));
+    CU(h, cudaStreamSynchronize(h->stream));
+    double worst = 0.0;
+    for (i64 j = 0; j < nrhs; ++j) {
+        double nb = std::sqrt(sums[2 * j + 1]), nr = std::sqrt(sums[2 * j]);
+        double rel = nb > 0.0 ? nr / nb : nr;
+        if (!(rel <= worst)) worst = rel;   // NaN propagates
+    }
+    *relres = worst;
+    return SPK_OK;
+}
+
+static int check_h(spk_handle* h) {
+    if (!h) return SPK_EARG;
+    if (h->device >= 0) {
+        cudaError_t e = cudaSetDevice(h->device);
+        if (e != cudaSuccess) return set_err(h, SPK_ECUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    }
+    return SPK_OK;
+}
+
+static bool valid_precision(int p) { return p == SPK_FP64 || p == SPK_FP32; }
+
+template <typename T>
+static int load_into(spk_handle* h) {
+    int rc = ensure_storage<T>(h);
+    if (rc) return rc;
+    Storage<T>& S = storage<T>(h);
+    CU(h, cudaMemsetAsync(S.d, 0, sizeof(T) * (size_t)h->fsize, h->stream));
+    if (h->nnz > 0) {
+        int blocks = (int)std::min<i64>((h->nnz + 255) / 256, 152 * 16);
+        spk::k_scatter_values<T><<<blocks, 256, 0, h->stream>>>(h->d_aval, h->d_slot, S.d, h->nnz);
+    }
+    CU(h, cudaGetLastError());
+    S.loaded = true;
+    S.factored = false;
+    return SPK_OK;
+}
+
+template <typename T>
+static int fetch_factor(spk_handle* h, std::vector<double>& out) {
+    std::vector<T> tmp(h->fsize);
+    CU(h, cudaMemcpyAsync(tmp.data(), storage<T>(h).d, sizeof(T) * h->fsize, cudaMemcpyDeviceToHost, h->stream));
+    CU(h, cudaStreamSynchronize(h->stream));
+    out.assign(tmp.begin(), tmp.end());
+    return SPK_OK;
+}
+
+static bool factored(spk_handle* h, int precision) {
+    return precision == SPK_FP64 ? h->s64.factored : h->s32.factored;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int spk_create(int64_t n, int64_t nsuper, const int64_t* xsuper, const int64_t* snode, const int64_t* xlindx,
+               const int64_t* lindx, const int64_t* xlnz, const int64_t* xunz, int index_base, spk_handle** out) {
+    if (!out) return SPK_EARG;
+    *out = nullptr;
+    g_create_err = "spk_create: bad arguments";
+    if (n <= 0 || nsuper <= 0 || nsuper > n || n > INT_MAX || !xsuper || !snode || !xlindx || !lindx || !xlnz ||
+        !xunz || (index_base != 0 && index_base != 1))
+        return SPK_EARG;
+    spk_handle* h = nullptr;
+    try {
+        h = new spk_handle();
+    } catch (const std::bad_alloc&) {
+        return SPK_ENOMEM;
+    }
+    h->n = n;
+    h->nsuper = nsuper;
+    int rc;
+    try {
+        rc = analyse(h, xsuper, snode, xlindx, lindx, xlnz, xunz, index_base);
+        if (rc == SPK_OK) build_schedule(h);
+    } catch (const std::bad_alloc&) {
+        rc = set_err(h, SPK_ENOMEM, "host allocation failed while analysing the structure");
+    }
+    if (rc == SPK_OK) {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) rc = set_err(h, SPK_ECUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+        else {
+            h->device = dev;
+            e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking);
+            if (e != cudaSuccess) rc = set_err(h, SPK_ECUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+            h->stream = h->own;
+        }
+    }
+    if (rc == SPK_OK) rc = upload_structure(h);
+    if (rc != SPK_OK) {
+        g_create_err = h->err;
+        spk_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return SPK_OK;
+}
+
+int spk_set_stream(spk_handle* h, void* stream) {
+    int rc = check_h(h);
+    if (rc) return rc;
+    h->stream = stream ? (cudaStream_t)stream : h->own;
+    return SPK_OK;
+}
+
+int spk_set_pattern(spk_handle* h, int64_t ncols, const int64_t* colptr, const int64_t* rowval, const int64_t* rperm,
+                    const int64_t* rinvp, int index_base) {
+    int rc = check_h(h);
+    if (rc) return rc;
+    const i64 n = h->n;
+    if (ncols != n || !colptr || !rowval || !rperm || !rinvp || (index_base != 0 && index_base != 1))
+        return set_err(h, SPK_EARG, "spk_set_pattern: bad arguments");
+    const int b = index_base;
+    h->rperm0.resize(n);
+    h->rinvp0.resize(n);
+    for (i64 i = 0; i < n; ++i) {
+        i64 p = rperm[i] - b, q = rinvp[i] - b;
+        if (p < 0 || p >= n || q < 0 || q >= n) return set_err(h, SPK_EARG, "spk_set_pattern: permutation out of range");
+        h->rperm0[i] = (int)p;
+        h->rinvp0[i] = (int)q;
+    }
+    for (i64 i = 0; i < n; ++i)
+        if (h->rinvp0[h->rperm0[i]] != i) return set_err(h, SPK_EARG, "spk_set_pattern: rperm and rinvp are not inverse");
+    const i64 nnz = colptr[n] - colptr[0];
+    if (nnz < 0) return set_err(h, SPK_EARG, "spk_set_pattern: bad colptr");
+    std::vector<ll> slot(nnz);
+    std::vector<int> rowcount(n + 1, 0);
+    for (i64 j = 0; j < n; ++j) {
+        for (i64 k = colptr[j] - b; k < colptr[j + 1] - b; ++k) {
+            i64 i = rowval[k] - b;
+            if (i < 0 || i >= n) return set_err(h, SPK_EARG, "spk_set_pattern: row index out of range");
+            rowcount[i + 1]++;
+            const int inew = h->rinvp0[i], jnew = h->rinvp0[j];
+            const HFront& F = h->fronts[h->col_front[jnew]];
+            ll s = -1;
+            if (inew >= F.f && inew < F.f + F.nf) {
+                s = F.loff + (ll)(jnew - F.f) * (F.nf + F.m) + (inew - F.f);
+            } else if (inew > jnew) {
+                const int* R = h->rows.data() + F.rows_off;
+                const int* q = std::lower_bound(R, R + F.m, inew);
+                if (q != R + F.m && *q == inew) s = F.loff + (ll)(jnew - F.f) * (F.nf + F.m) + F.nf + (q - R);
+            } else {
+                const HFront& G = h->fronts[h->col_front[inew]];
+                const int* R = h->rows.data() + G.rows_off;
+                const int* q = std::lower_bound(R, R + G.m, jnew);
+                if (q != R + G.m && *q == jnew) s = G.uoff + (ll)(inew - G.f) * G.m + (q - R);
+            }
+            if (s < 0) {
+                char buf[160];
+                std::snprintf(buf, sizeof buf, "No space for matrix element (%lld, %lld).", (long long)inew + 1,
+                              (long long)jnew + 1);
+                return set_err(h, SPK_ESTRUCT, buf);
+            }
+            slot[k - (colptr[0] - b)] = s;
+        }
+    }
+    // row-ordered pattern for the residual
+    for (i64 i = 0; i < n; ++i) rowcount[i + 1] += rowcount[i];
+    std::vector<int> rowptr(rowcount), col(nnz);
+    std::vector<ll> src(nnz);
+    {
+        std::vector<int> next(rowcount.begin(), rowcount.end() - 1);
+        for (i64 j = 0; j < n; ++j)
+            for (i64 k = colptr[j] - b; k < colptr[j + 1] - b; ++k) {
+                i64 i = rowval[k] - b;
+                int at = next[i]++;
+                col[at] = (int)j;
+                src[at] = k - (colptr[0] - b);
+            }
+    }
+    cudaFree(h->d_slot); cudaFree(h->d_aval); cudaFree(h->d_rowptr); cudaFree(h->d_col); cudaFree(h->d_src);
+    cudaFree(h->d_rperm); cudaFree(h->d_rinvp);
+    h->d_slot = nullptr; h->d_aval = nullptr; h->d_rowptr = h->d_col = nullptr; h->d_src = nullptr;
+    h->d_rperm = h->d_rinvp = nullptr;
+    if ((rc = upload(h, &h->d_slot, slot))) return rc;
+    if ((rc = upload(h, &h->d_rowptr, rowptr))) return rc;
+    if ((rc = upload(h, &h->d_col, col))) return rc;
+    if ((rc = upload(h, &h->d_src, src))) return rc;
+    if ((rc = upload(h, &h->d_rperm, h->rperm0))) return rc;
+    if ((rc = upload(h, &h->d_rinvp, h->rinvp0))) return rc;
+    CU(h, cudaMalloc((void**)&h->d_aval, sizeof(double) * std::max<i64>(nnz, 1)));
+    h->nnz = nnz;
+    h->have_pattern = true;
+    h->have_values = false;
+    h->s64.loaded = h->s64.factored = false;
+    h->s32.loaded = h->s32.factored = false;
+    return SPK_OK;
+}
+
+
+int spk_load_values(spk_handle* h, const double* nzval, int where, int precision) {
+    int rc = check_h(h);
+    if (rc) return rc;
+    if (!h->have_pattern) return set_err(h, SPK_ESEQ, "Sequence error. Pattern not set yet.");
+    if ((!nzval && h->nnz > 0) || (where != SPK_HOST && where != SPK_DEVICE) || !valid_precision(precision))
+        return set_err(h, SPK_EARG, "spk_load_values: bad arguments");
+    if (h->nnz > 0)
+        CU(h, cudaMemcpyAsync(h->d_aval, nzval, sizeof(double) * (size_t)h->nnz,
+                              where == SPK_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, h->stream));
+    h->have_values = true;
+    // a new A invalidates both factors
+    h->s64.loaded = h->s64.factored = false;
+    h->s32.loaded = h->s32.factored = false;
+    rc = precision == SPK_FP64 ? load_into<double>(h) : load_into<float>(h);
+    if (rc) return rc;
+    if (where == SPK_HOST) CU(h, cudaStreamSynchronize(h->stream));
+    return SPK_OK;
+}
+
+int spk_factor(spk_handle* h, int precision, int64_t* first_singular) {
+    int rc = check_h(h);
+    if (rc) return rc;
+    if (first_singular) *first_singular = 0;
+    if (!valid_precision(precision)) return set_err(h, SPK_EARG, "spk_factor: bad precision");
+    if (!h->have_values) return set_err(h, SPK_ESEQ, "Sequence error. Matrix input not done yet.");
+    if (precision == SPK_FP64) {
+        if (!h->s64.loaded && (rc = load_into<double>(h))) return rc;
+        if ((rc = run_factor<double>(h))) return rc;
+    } else {
+        if (!h->s32.loaded && (rc = load_into<float>(h))) return rc;
+        if ((rc = run_factor<float>(h))) return rc;
+    }
+    int info = INT_MAX;
+    CU(h, cudaMemcpyAsync(&info, h->d_info, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CU(h, cudaStreamSynchronize(h->stream));
+    if (precision == SPK_FP64) { h->s64.loaded = false; h->s64.factored = true; }
+    else { h->s32.loaded = false; h->s32.factored = true; }
+    if (info != INT_MAX) {
+        if (first_singular) *first_singular = info;
+        char buf[128];
+        std::snprintf(buf, sizeof buf, "zero pivot in the diagonal block of supernode %d", info);
+        return set_err(h, SPK_ESINGULAR, buf);
+    }
+    return SPK_OK;
+}
+
+
+int spk_solve(spk_handle* h, double* b, int64_t nrhs, int64_t ldb, int where, int precision) {
+    int rc = check_h(h);
+    if (rc) return rc;
+    if (!valid_precision(precision) || nrhs < 0 || (nrhs > 0 && (!b || ldb < h->n)) ||
+        (where != SPK_HOST && where != SPK_DEVICE))
+        return set_err(h, SPK_EARG, "spk_solve: bad arguments");
+    if (!factored(h, precision)) return set_err(h, SPK_ESEQ, "Sequence error. Factorization not done yet.");
+    if (nrhs == 0) return SPK_OK;
+    if ((rc = ensure_rhs(h, nrhs))) return rc;
+    const i64 n = h->n;
+    double* src;
+    i64 ld;
+    if (where == SPK_HOST) {
+        CU(h, cudaMemcpy2DAsync(h->d_rhs, sizeof(double) * n, b, sizeof(double) * ldb, sizeof(double) * n, nrhs,
+                                cudaMemcpyHostToDevice, h->stream));
+        src = h->d_rhs;
+        ld = n;
+    } else {
+        src = b;
+        ld = ldb;
+    }
+    rc = precision == SPK_FP64 ? solve_device<double>(h, src, ld, h->d_x, n, nrhs, 0)
+                               : solve_device<float>(h, src, ld, h->d_x, n, nrhs, 0);
+    if (rc) return rc;
+    CU(h, cudaMemcpy2DAsync(b, sizeof(double) * ldb, h->d_x, sizeof(double) * n, sizeof(double) * n, nrhs,
+                            where == SPK_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, h->stream));
+    CU(h, cudaStreamSynchronize(h->stream));
+    return SPK_OK;
+}
+
+int spk_residual(spk_handle* h, const double* b, const double* x, int64_t nrhs, int64_t ld, int where,
+                 double* relres) {
+    int rc = check_h(h);
+    if (rc) return rc;
+    if (!relres || nrhs <= 0 || !b || !x || ld < h->n || (where != SPK_HOST && where != SPK_DEVICE))
+        return set_err(h, SPK_EARG, "spk_residual: bad arguments");
+    if (!h->have_values) return set_err(h, SPK_ESEQ, "Sequence error. Matrix input not done yet.");
+    if ((rc = ensure_rhs(h, nrhs))) return rc;
+    const i64 n = h->n;
+    const double *db = b, *dx = x;
+    i64 ldb = ld, ldx = ld;
+    if (where == SPK_HOST) {
+        CU(h, cudaMemcpy2DAsync(h->d_rhs, sizeof(double) * n, b, sizeof(double) * ld, sizeof(double) * n, nrhs,
+                                cudaMemcpyHostToDevice, h->stream));
+        CU(h, cudaMemcpy2DAsync(h->d_x, sizeof(double) * n, x, sizeof(double) * ld, sizeof(double) * n, nrhs,
+                                cudaMemcpyHostToDevice, h->stream));
+        db = h->d_rhs;
+        dx = h->d_x;
+        ldb = ldx = n;
+    }
+    return residual_device(h, db, ldb, dx, ldx, nrhs, relres);
+}
+
+int spk_refine(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where, int precision,
+               double tol, int max_iter, int* iters, double* relres) {
+    int rc = check_h(h);
+    if (rc) return rc;
+    if (iters) *iters = 0;
+    if (!valid_precision(precision) || nrhs <= 0 || !b || !x || ld < h->n || max_iter < 0 ||
+        (where != SPK_HOST && where != SPK_DEVICE))
+        return set_err(h, SPK_EARG, "spk_refine: bad arguments");
+    if (!factored(h, precision)) return set_err(h, SPK_ESEQ, "Sequence error. Factorization not done yet.");
+    if ((rc = ensure_rhs(h, nrhs))) return rc;
+    const i64 n = h->n;
+    const double* db;
+    double* dx;
+    i64 ldb, ldx;
+    if (where == SPK_HOST) {
+        CU(h, cudaMemcpy2DAsync(h->d_rhs, sizeof(double) * n, b, sizeof(double) * ld, sizeof(double) * n, nrhs,
+                                cudaMemcpyHostToDevice, h->stream));
+        db = h->d_rhs;
+        dx = h->d_x;
+        ldb = ldx = n;
+    } else {
+        db = b;
+        dx = x;
+        ldb = ldx = ld;
+    }
+    auto solve_into = [&](const double* rhs, i64 ldr, int acc) {
+        return precision == SPK_FP64 ? solve_device<double>(h, rhs, ldr, dx, ldx, nrhs, acc)
+                                     : solve_device<float>(h, rhs, ldr, dx, ldx, nrhs, acc);
+    };
+    if ((rc = solve_into(db, ldb, 0))) return rc;
+    double rel = 0.0;
+    int it = 0;
+    for (;;) {
+        if ((rc = residual_device(h, db, ldb, dx, ldx, nrhs, &rel))) return rc;
+        if (rel <= tol || it >= max_iter || rel != rel) break;
+        if ((rc = solve_into(h->d_r, n, 1))) return rc;
+        ++it;
+    }
+    if (where == SPK_HOST)
+        CU(h, cudaMemcpy2DAsync(x, sizeof(double) * ld, dx, sizeof(double) * n, sizeof(double) * n, nrhs,
+                                cudaMemcpyDeviceToHost, h->stream));
+    CU(h, cudaStreamSynchronize(h->stream));
+    if (iters) *iters = it;
+    if (relres) *relres = rel;
+    if (!(rel <= tol)) {
+        char buf[128];
+        std::snprintf(buf, sizeof buf, "refinement stopped at relative residual %.3e after %d corrections", rel, it);
+        return set_err(h, SPK_ENOCONV, buf);
+    }
+    return SPK_OK;
+}
+
+
+int spk_get_factors(spk_handle* h, int precision, double* lnz, double* unz, int64_t* ipiv) {
+    int rc = check_h(h);
+    if (rc) return rc;
+    if (!valid_precision(precision)) return set_err(h, SPK_EARG, "spk_get_factors: bad precision");
+    const bool done = factored(h, precision);
+    const bool loaded = precision == SPK_FP64 ? h->s64.loaded : h->s32.loaded;
+    if (!done && !loaded) return set_err(h, SPK_ESEQ, "Sequence error. Matrix input not done yet.");
+    std::vector<double> fac;
+    rc = precision == SPK_FP64 ? fetch_factor<double>(h, fac) : fetch_factor<float>(h, fac);
+    if (rc) return rc;
+    for (const HFront& F : h->fronts) {
+        const int ld = F.nf + F.m;
+        for (int s = F.piece0; s < F.piece0 + F.npieces; ++s) {
+            const int p0 = h->xs[s] - (int)F.f, w = h->xs[s + 1] - h->xs[s];
+            const i64 jlen = ld - p0;
+            const i64 lbase = h->xlnz0[h->xs[s]], ubase = h->xunz0[h->xs[s]];
+            for (int k = 0; k < w; ++k) {
+                if (lnz)
+                    for (i64 t = 0; t < jlen; ++t) lnz[lbase + k * jlen + t] = fac[F.loff + (i64)(p0 + k) * ld + p0 + t];
+                if (unz)
+                    for (i64 i = 0; i < jlen - w; ++i) {
+                        i64 c = p0 + w + i;
+                        unz[ubase + k * (jlen - w) + i] = c < F.nf ? fac[F.loff + c * ld + p0 + k]
+                                                                   : fac[F.uoff + (i64)(p0 + k) * F.m + (c - F.nf)];
+                    }
+            }
+        }
+    }
+    if (ipiv && !done) {
+        for (i64 j = 0; j < h->n; ++j) ipiv[j] = 0;   // as _inmatrix! leaves it
+    } else if (ipiv) {
+        std::vector<int> p(h->n);
+        CU(h, cudaMemcpyAsync(p.data(), h->d_ipiv, sizeof(int) * h->n, cudaMemcpyDeviceToHost, h->stream));
+        CU(h, cudaStreamSynchronize(h->stream));
+        for (i64 j = 0; j < h->n; ++j) ipiv[j] = p[j] + 1;
+    }
+    return SPK_OK;
+}
+
+int spk_stats(spk_handle* h, int64_t* nfronts, int64_t* nlevels, int64_t* factor_entries, double* lu_flops) {
+    if (!h) return SPK_EARG;
+    if (nfronts) *nfronts = (int64_t)h->fronts.size();
+    if (nlevels) *nlevels = (int64_t)h->levels.size();
+    if (factor_entries) *factor_entries = h->fsize;
+    if (lu_flops) *lu_flops = h->lu_flops;
+    return SPK_OK;
+}
+
+const char* spk_last_error(spk_handle* h) { return h ? h->err.c_str() : g_create_err.c_str(); }
+
+void spk_destroy(spk_handle* h) {
+    if (!h) return;
+    if (h->device >= 0) cudaSetDevice(h->device);
+    if (h->own) cudaStreamSynchronize(h->own);
+    void* ptrs[] = {h->d_fronts, h->d_xs, h->d_rows, h->d_runid, h->d_run_tgt, h->d_run_start, h->d_run_rel,
+                    h->d_rel, h->d_sched_ids, h->d_sched_prefix, h->d_ipiv, h->d_info, h->d_slot, h->d_aval,
+                    h->d_rowptr, h->d_col, h->d_src, h->d_rperm, h->d_rinvp, h->s64.d, h->s32.d, h->d_wb,
+                    h->d_wy, h->d_wx, h->d_rhs, h->d_x, h->d_r, h->d_sums};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (h->own) cudaStreamDestroy(h->own);
+    delete h;
+}
+
+}  // extern "C"

@@ -1,0 +1,96 @@
+"""ctypes bindings of the two native libraries.
+
+``host()`` returns the structure-phase library (CPU only), ``gpu()`` the
+numeric engine.  Both are built in-tree on first use.  The numeric engine has
+no CPU fallback: every numeric call goes to ``libspk_gpu.so`` and raises when
+the library or a CUDA device is unavailable.
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+
+import numpy as np
+
+from . import _build
+
+i64 = ctypes.c_int64
+P64 = ctypes.POINTER(ctypes.c_int64)
+PD = ctypes.POINTER(ctypes.c_double)
+VP = ctypes.c_void_p
+
+HOST_SYMBOLS = {
+    "spk_host_last_error": (ctypes.c_char_p, []),
+    "spk_graph_is_symmetric": (ctypes.c_int, [i64, P64, P64]),
+    "spk_graph_symmetrize": (ctypes.c_int, [i64, P64, P64, P64, P64, P64]),
+    "spk_order_mmd": (ctypes.c_int, [i64, P64, P64, P64, P64]),
+    "spk_order_nd_grid": (ctypes.c_int, [i64, i64, i64, i64, P64, P64, P64, P64]),
+    "spk_symbolic_create": (ctypes.c_int, [i64, P64, P64, P64, P64, i64, ctypes.POINTER(VP)]),
+    "spk_symbolic_sizes": (ctypes.c_int, [VP, P64, P64, P64, P64]),
+    "spk_symbolic_get": (ctypes.c_int, [VP, P64, P64, P64, P64, P64, P64, P64, P64, P64, P64]),
+    "spk_symbolic_destroy": (None, [VP]),
+}
+
+GPU_SYMBOLS = {
+    "spk_create": (ctypes.c_int, [i64, i64, P64, P64, P64, P64, P64, P64, ctypes.c_int, ctypes.POINTER(VP)]),
+    "spk_set_stream": (ctypes.c_int, [VP, VP]),
+    "spk_set_pattern": (ctypes.c_int, [VP, i64, P64, P64, P64, P64, ctypes.c_int]),
+    "spk_load_values": (ctypes.c_int, [VP, VP, ctypes.c_int, ctypes.c_int]),
+    "spk_factor": (ctypes.c_int, [VP, ctypes.c_int, P64]),
+    "spk_solve": (ctypes.c_int, [VP, VP, i64, i64, ctypes.c_int, ctypes.c_int]),
+    "spk_refine": (ctypes.c_int, [VP, VP, VP, i64, i64, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                  ctypes.c_int, ctypes.POINTER(ctypes.c_int), PD]),
+    "spk_residual": (ctypes.c_int, [VP, VP, VP, i64, i64, ctypes.c_int, PD]),
+    "spk_get_factors": (ctypes.c_int, [VP, ctypes.c_int, PD, PD, P64]),
+    "spk_stats": (ctypes.c_int, [VP, P64, P64, P64, PD]),
+    "spk_last_error": (ctypes.c_char_p, [VP]),
+    "spk_destroy": (None, [VP]),
+}
+
+SPK_OK, SPK_EARG, SPK_ECUDA, SPK_ENOMEM, SPK_ESEQ, SPK_ESTRUCT, SPK_ESINGULAR, SPK_ENOCONV = 0, -1, -2, -3, -4, -5, -6, -7
+SPK_HOST, SPK_DEVICE = 0, 1
+SPK_FP64, SPK_FP32 = 0, 1
+
+_lock = threading.Lock()
+_host = None
+_gpu = None
+
+
+def _bind(lib, table):
+    for name, (res, args) in table.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+def host():
+    global _host
+    with _lock:
+        if _host is None:
+            _build.build()
+            _host = _bind(ctypes.CDLL(_build.HOST_SO), HOST_SYMBOLS)
+    return _host
+
+
+def gpu():
+    global _gpu
+    with _lock:
+        if _gpu is None:
+            _build.build()
+            _gpu = _bind(ctypes.CDLL(_build.GPU_SO), GPU_SYMBOLS)
+    return _gpu
+
+
+def p64(a: np.ndarray):
+    assert a.dtype == np.int64 and a.flags.c_contiguous
+    return a.ctypes.data_as(P64)
+
+
+def pd(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(PD)
+
+
+def host_error() -> str:
+    return host().spk_host_last_error().decode()

@@ -1,0 +1,221 @@
+"""CUDA numeric phase vs the oracle, through the C ABI (libspk_gpu.so).
+
+Bar: identical pivot sequence; FP64 factors within 1e-12 (relative, max norm
+per array) of the oracle's; solutions within 1e-10 relative of the oracle's
+and relative residual <= 1e-12.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import oracle
+import sparspak as S
+from cases import m31_problem, problem_from_csc, sprand_spd_like, sprand_unsym, tridiag_csc, tridiag_problem
+from sparspak.problem import csc_arrays
+
+pytestmark = pytest.mark.gpu
+
+FACTOR_RTOL = 1e-12
+
+
+def run_both(p, orderfunction=None, precision="fp64"):
+    s = S.SparseSolver(p, precision=precision)
+    S.findorder_(s, orderfunction)
+    S.symbolicfactor_(s)
+    o = oracle.OracleLU(s.slvr)
+    o.inmatrix_csc(*S.sparse_solver._matrix_arrays(p))
+    o.factor()
+    S.inmatrix_(s)
+    S.factor_(s)
+    return s, o
+
+
+def rel(a, b):
+    scale = max(np.max(np.abs(b)), 1e-300) if b.size else 1.0
+    return float(np.max(np.abs(a - b)) / scale) if b.size else 0.0
+
+
+def check_factors(s, o, rtol=FACTOR_RTOL):
+    lnz, unz, ipiv = s.slvr.lnz, s.slvr.unz, s.slvr.ipiv
+    assert np.array_equal(ipiv, o.ipiv), "pivot sequence differs"
+    assert rel(lnz, o.lnz) <= rtol
+    assert rel(unz, o.unz[: unz.size]) <= rtol
+
+
+def test_golden_tridiag11(golden):
+    p = tridiag_problem(11)
+    s = S.SparseSolver(p)
+    S.findorder_(s)
+    S.symbolicfactor_(s)
+    S.inmatrix_(s)
+    # after inmatrix!: exact (msprs005)
+    assert s.slvr.lnz.tolist() == golden["tridiag11_inmatrix_lnz"]
+    assert s.slvr.unz.tolist() == golden["tridiag11_inmatrix_unz"]
+    S.factor_(s)
+    ref = np.array(golden["tridiag11_factor_lnz"])
+    assert np.max(np.abs(s.slvr.lnz - ref) / np.abs(ref)) < 1e-15
+    S.triangularsolve_(s)
+    A = S.outsparse(p).toarray()
+    xr = np.linalg.solve(A, p.rhs)
+    assert np.linalg.norm(p.x - xr) / np.linalg.norm(xr) < 1e-14
+
+
+@pytest.mark.parametrize("case", ["m31", "spd301", "spd357", "spd1357", "grid5x3", "tridiag1101"])
+def test_factor_and_solve_vs_oracle(case, golden):
+    if case == "m31":
+        p = m31_problem(golden)
+    elif case.startswith("spd"):
+        n = int(case[3:])
+        p = problem_from_csc(sprand_spd_like(n, n), np.arange(1, n + 1, dtype=np.float64))
+    elif case == "grid5x3":
+        p = S.makegridproblem(5, 3)
+        S.infullrhs_(p, np.arange(1, 16, dtype=np.float64))
+    else:
+        p = tridiag_problem(1101)
+    s, o = run_both(p)
+    check_factors(s, o)
+    S.triangularsolve_(s)
+    xo = o.solve(p.rhs[: p.nrows])
+    assert rel(p.x[: p.nrows], xo) < 1e-10
+    A = S.outsparse(p)
+    r = p.rhs[: p.nrows] - A @ p.x[: p.nrows]
+    assert np.linalg.norm(r) / np.linalg.norm(p.rhs[: p.nrows]) < 1e-12
+
+
+def test_small_literal_pivoting(golden):
+    for vals in golden["small4x4"]:
+        A = sp.csc_matrix(np.array(vals).reshape(4, 4))
+        p = problem_from_csc(A)
+        S.inbi_(p, 1, 1.0)
+        s, o = run_both(p)
+        check_factors(s, o)
+
+
+def test_random_unsymmetric_pivoting():
+    # test/test_structunsymm.jl:60-90 through both APIs: abs error < 1e-9, pivots equal to the oracle's
+    rng = np.random.default_rng(7)
+    for t in range(200):
+        A = sprand_unsym(4, 0.3, 1000 + t)
+        b = rng.random(4)
+        s, o = run_both(problem_from_csc(A, b))
+        check_factors(s, o)
+        x = S.ldiv(S.sparspaklu(A), b)
+        assert np.linalg.norm(x - np.linalg.solve(A.toarray(), b)) < 1e-9
+
+
+@pytest.mark.parametrize("shape,order", [((20, 20), "mmd"), ((20, 20), "nd"), ((10, 10, 10), "nd"),
+                                         ((9, 11, 7), "mmd")])
+def test_grid_laplacian(shape, order):
+    A = S.gallery.laplacian(shape)
+    of = None if order == "mmd" else S.nd_grid(*(shape + (1,) * (3 - len(shape))), leaf=16)
+    s, o = run_both(A, of)
+    check_factors(s, o)
+    b = S.gallery.random_rhs(A.shape[0], 3, seed=1)
+    x = b.copy(order="F")
+    S.triangularsolve_(s, x)
+    assert rel(x, o.solve(b)) < 1e-10
+
+
+def test_convection_diffusion_pivots_identity():
+    A = S.gallery.convection_diffusion(k=10)
+    s, o = run_both(A, S.nd_grid(10, 10, 10, leaf=16))
+    check_factors(s, o)
+    # an M-matrix: every in-block pivot is the diagonal (SURVEY N3 expectation)
+    b = s.slvr
+    ident = np.concatenate([np.arange(1, b.xsuper[k + 1] - b.xsuper[k] + 1) for k in range(b.nsuper)])
+    assert np.array_equal(b.ipiv, ident)
+
+
+def test_wide_supernodes():
+    # dense blocks give chains split 23/23/23/31 and long chains with a last piece > 32
+    rng = np.random.default_rng(5)
+    for n in (100, 400):
+        A = sp.csc_matrix(rng.standard_normal((n, n)) + n * np.eye(n))
+        s, o = run_both(A)
+        assert np.diff(s.slvr.xsuper).max() > 30
+        check_factors(s, o, 1e-11)
+
+
+def test_cscinterface_refactor():
+    # test/test_cscinterface.jl:127-199: sparspaklu, sparspaklu! with and without pattern change
+    n = 20
+    spm = sprand_spd_like(n, 11, diag=40.0)
+    ex = np.ones(n)
+    lu = S.sparspaklu(spm)
+    assert np.allclose(S.ldiv(lu, spm @ ex), ex)
+    spm2 = spm.copy()
+    spm2.data -= 0.1
+    S.sparspaklu_(lu, spm2)
+    assert np.allclose(S.ldiv(lu, spm2 @ ex), ex)
+    spm3 = sp.csc_matrix(spm2 + sp.random(n, n, density=1 / n, random_state=np.random.default_rng(2)))
+    with pytest.raises(S.ErrorException):
+        S.sparspaklu_(lu, spm3, allow_pattern_change=False)
+    S.sparspaklu_(lu, spm3)
+    assert np.allclose(S.ldiv(lu, spm3 @ ex), ex)
+    lu0 = S.sparspaklu(sp.csc_matrix((1, 1)), factorize=False)
+    S.sparspaklu_(lu0, spm3, allow_pattern_change=False)
+    assert np.allclose(S.ldiv(lu0, spm3 @ ex), ex)
+
+
+def test_solver_full_sequence_and_errors():
+    p = tridiag_problem(11)
+    s = S.SparseSolver(p)
+    with pytest.raises(S.ErrorException):
+        S.symbolicfactor_(s)
+    S.solve_(s)
+    A = S.outsparse(p).toarray()
+    assert np.linalg.norm(p.x - np.linalg.solve(A, p.rhs)) < 1e-12
+
+
+def test_singular_block_raises():
+    A = sp.csc_matrix(np.array([[1.0, 1.0, 0.0], [1.0, 1.0, 0.0], [0.0, 0.0, 2.0]]))
+    s = S.SparseSolver(A)
+    S.findorderperm_(s, [1, 2, 3])
+    S.symbolicfactor_(s)
+    S.inmatrix_(s)
+    with pytest.raises(S.ErrorException, match="supernode"):
+        S.factor_(s)
+
+
+def test_no_slot_for_entry():
+    # an entry outside the symbolic structure is reported like _inmatrix!'s "No space" error
+    A = tridiag_csc(6)
+    s = S.SparseSolver(A)
+    S.findorderperm_(s, np.arange(1, 7))
+    S.symbolicfactor_(s)
+    eng = S.sparse_solver._ensure_engine(s.slvr)
+    B = sp.csc_matrix(A + sp.csc_matrix(([1.0], ([5], [0])), shape=(6, 6)))
+    with pytest.raises(S.ErrorException, match="No space for matrix element"):
+        eng.set_pattern(B.indptr + 1, B.indices + 1, s.slvr.order.rperm, s.slvr.order.rinvp, index_base=1)
+
+
+def test_mixed_precision_refinement():
+    A = S.gallery.laplacian((12, 12, 12), shift=1e-3)
+    b = S.gallery.random_rhs(A.shape[0], 4, seed=2)
+    s = S.SparseSolver(A)
+    S.findorder_(s, S.nd_grid(12, 12, 12, leaf=16))
+    x, it, rr = S.refine_(s, b, precision="fp32", tol=1e-12)
+    assert rr <= 1e-12 and 1 <= it <= 10
+    r = b - A @ x
+    assert np.max(np.linalg.norm(r, axis=0) / np.linalg.norm(b, axis=0)) <= 1e-12
+    # FP32 factor entries agree with the FP64 oracle to FP32 accuracy
+    o = oracle.OracleLU(s.slvr)
+    o.inmatrix_csc(*S.sparse_solver._matrix_arrays(A))
+    o.factor()
+    assert rel(s.slvr.lnz, o.lnz) < 1e-4
+
+
+def test_device_resident_arrays():
+    torch = pytest.importorskip("torch")
+    A = S.gallery.laplacian((16, 16, 16), shift=1e-3)
+    s = S.SparseSolver(A)
+    S.findorder_(s, S.nd_grid(16, 16, 16))
+    S.symbolicfactor_(s)
+    S.inmatrix_(s)
+    S.factor_(s)
+    b = S.gallery.random_rhs(A.shape[0], 2, seed=3)
+    bt = torch.tensor(np.ascontiguousarray(b.T), device="cuda")
+    s.slvr.engine.solve(bt)
+    x = bt.cpu().numpy().T
+    r = b - A @ x
+    assert np.max(np.linalg.norm(r, axis=0) / np.linalg.norm(b, axis=0)) < 1e-12

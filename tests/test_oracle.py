@@ -1,0 +1,142 @@
+"""The oracle (C restatement of the reference's numeric phase) pinned against
+the reference's golden vectors and its end-to-end test tolerances (no GPU)."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import oracle
+import sparspak as S
+from cases import m31_problem, problem_from_csc, sprand_spd_like, sprand_unsym, tridiag_problem
+from sparspak.problem import csc_arrays
+
+
+def oracle_for(p, orderfunction=None):
+    s = S.SparseSolver(p)
+    S.findorder_(s, orderfunction)
+    S.symbolicfactor_(s)
+    o = oracle.OracleLU(s.slvr)
+    o.inmatrix_csc(*csc_arrays(p))
+    return s, o
+
+
+def test_inmatrix_golden(golden):
+    # msprs005, test/test_sparse_method.jl:172-175 (exact)
+    _, o = oracle_for(tridiag_problem(11))
+    assert o.lnz.tolist() == golden["tridiag11_inmatrix_lnz"]
+    assert o.unz.tolist() == golden["tridiag11_inmatrix_unz"]
+
+
+def test_factor_golden(golden):
+    # msprs006, test/test_sparse_method.jl:219-227 (the reference checks rtol 1e-6)
+    _, o = oracle_for(tridiag_problem(11))
+    assert o.factor() == 0
+    ref_l, ref_u = np.array(golden["tridiag11_factor_lnz"]), np.array(golden["tridiag11_factor_unz"])
+    assert np.max(np.abs(o.lnz - ref_l) / np.abs(ref_l)) < 1e-15
+    assert np.array_equal(o.unz, ref_u)
+
+
+def test_forward_solve_golden(golden):
+    # the permuted rhs before/after _lulsolve! quoted in test/test_sparse_method.jl:318-321
+    p = tridiag_problem(11)
+    s, o = oracle_for(p)
+    o.factor()
+    before = p.rhs[s.slvr.order.rperm - 1]
+    assert before.tolist() == golden["tridiag11_fwd_before"]
+    after = o.lulsolve(before)
+    assert np.max(np.abs(after - golden["tridiag11_fwd_after"])) < 1e-13
+
+
+def _solve_check(p, tol):
+    s, o = oracle_for(p)
+    o.factor()
+    x = o.solve(p.rhs[: p.nrows])
+    A = S.outsparse(p).toarray()
+    xr = np.linalg.solve(A, p.rhs[: p.nrows])
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < tol
+
+
+@pytest.mark.parametrize("n", [11, 1101, 11000])
+def test_tridiag_solve(n):
+    # msprs007-009
+    p = tridiag_problem(n)
+    s, o = oracle_for(p)
+    o.factor()
+    x = o.solve(p.rhs)
+    A = sp.csc_matrix(S.outsparse(p))
+    r = p.rhs - A @ x
+    assert np.linalg.norm(r) / np.linalg.norm(p.rhs) < 1e-14
+
+
+def test_m31(golden):
+    # msprs010
+    _solve_check(m31_problem(golden), 1e-12)
+
+
+@pytest.mark.parametrize("n,seed", [(301, 1), (357, 2), (1357, 3)])
+def test_sprand_spd_like(n, seed):
+    # msprs012, 015, 016
+    m = sprand_spd_like(n, seed)
+    _solve_check(problem_from_csc(m, np.arange(1, n + 1, dtype=np.float64)), 1e-12)
+
+
+def test_grid_problem():
+    # msprs017-018: makegridproblem(5, 3) with infullrhs! and makerhs!
+    p = S.makegridproblem(5, 3)
+    S.infullrhs_(p, np.arange(1, 16, dtype=np.float64))
+    _solve_check(p, 1e-12)
+    p = S.makegridproblem(5, 3)
+    S.makerhs_(p, None)
+    _solve_check(p, 1e-12)
+
+
+def test_small_literal_cases(golden):
+    # test/test_structunsymm.jl:25-57, test/test_small.jl:35-149
+    for vals in golden["small4x4"]:
+        A = np.array(vals).reshape(4, 4)
+        p = problem_from_csc(sp.csc_matrix(A))
+        S.inbi_(p, 1, 1.0)
+        _solve_check(p, 1e-12)
+
+
+def test_random_unsymmetric_pivoting():
+    # test/test_structunsymm.jl:60-90: 1000 x sprand(4,4,0.3)+I, abs error < 1e-9
+    rng = np.random.default_rng(0)
+    pivoted = 0
+    for t in range(1000):
+        A = sprand_unsym(4, 0.3, t)
+        b = rng.random(4)
+        s, o = oracle_for(problem_from_csc(A, b))
+        o.factor()
+        pivoted += int(np.any(o.ipiv != _identity_local(s.slvr)))
+        x = o.solve(b)
+        assert np.linalg.norm(x - np.linalg.solve(A.toarray(), b)) < 1e-9
+    assert pivoted > 0   # the cases exercise real in-block interchanges
+
+
+def _identity_local(b):
+    ip = np.zeros(b.n, dtype=np.int64)
+    for s in range(b.nsuper):
+        f, l = b.xsuper[s], b.xsuper[s + 1]
+        ip[f - 1:l - 1] = np.arange(1, l - f + 1)
+    return ip
+
+
+def test_singular_block_reported():
+    # a zero pivot: reference iflag -1 for the last block; the oracle also records the first
+    A = sp.csc_matrix(np.array([[0.0, 1.0], [1.0, 0.0]]))
+    p = problem_from_csc(A)
+    s = S.SparseSolver(p)
+    S.findorderperm_(s, [1, 2])
+    S.symbolicfactor_(s)
+    o = oracle.OracleLU(s.slvr)
+    o.inmatrix_csc(*csc_arrays(p))
+    o.factor()
+    assert o.first_singular == 0   # the 2x2 block pivots and is regular
+    B = sp.csc_matrix(np.array([[1.0, 1.0], [1.0, 1.0]]))
+    p = problem_from_csc(B)
+    s = S.SparseSolver(p)
+    S.findorderperm_(s, [1, 2])
+    S.symbolicfactor_(s)
+    o = oracle.OracleLU(s.slvr)
+    o.inmatrix_csc(*csc_arrays(p))
+    assert o.factor() == -1 and o.first_singular == 1
