@@ -1,0 +1,371 @@
+#!/usr/bin/env python
+"""Time to 1e-12 relative residual on the 64^3 shifted 3-D Laplacian.
+
+Workload: 7-point Dirichlet Laplacian on a 64 x 64 x 64 grid (n = 262,144)
+plus a diagonal shift of 1e-3, geometric nested-dissection ordering, four
+right-hand sides i.i.d. uniform[-1, 1] (numpy PCG64, seed 0).  Synthetic:
+the reference publishes no input for this configuration.
+
+A step is one complete time-to-solution pass of the numeric phase with the
+inputs already in HBM: value assembly (inmatrix), LU factorisation, solve
+and FP64 iterative refinement until max_j ||b_j - A x_j|| / ||b_j|| <= 1e-12.
+The headline `value` is the mixed form (FP32 factor and solves, FP64
+residual and correction); the plain FP64 form is timed beside it.  `e2e`
+repeats the mixed step through the public API with pinned host buffers,
+host<->device copies inside the timed region.  Ordering and symbolic
+factorisation are host work done once per pattern and reported apart.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "sparspak.jl_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "time to 1e-12 rel. residual, mixed vs FP64 on 1 GB300; factor GFLOP/s"
+TOL = 1e-12
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--grid", type=int, default=64)
+    ap.add_argument("--nrhs", type=int, default=4)
+    ap.add_argument("--sample-grid", type=int, default=32, help="grid of the CPU baseline's bounded sample")
+    return ap.parse_args()
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling (every 200 ms) during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-i", str(self.gpu), "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.p:
+            self.p.terminate()
+            self.p.wait(timeout=10)
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def workload(k, nrhs):
+    import sparspak as S
+
+    A = S.gallery.laplacian((k, k, k), shift=1e-3)
+    b = S.gallery.random_rhs(A.shape[0], nrhs, seed=0)
+    return A, np.asfortranarray(b.reshape(A.shape[0], nrhs))
+
+
+def symbolic(A, k):
+    import sparspak as S
+
+    s = S.SparseSolver(A)
+    t0 = time.perf_counter()
+    S.findorder_(s, S.nd_grid(k, k, k))
+    t1 = time.perf_counter()
+    S.symbolicfactor_(s)
+    t2 = time.perf_counter()
+    return s, {"order_s": t1 - t0, "symbolic_s": t2 - t1}
+
+
+def lu_flops(b):
+    w = np.diff(b.xsuper)
+    ln = np.diff(b.xlindx)
+    c = np.concatenate([ln[i] - np.arange(w[i]) for i in range(b.nsuper)]).astype(np.float64)
+    return float(np.sum((c - 1) + 2.0 * (c - 1) ** 2))
+
+
+def cpu_sample(k):
+    """The oracle (plain-C restatement of the reference's LU path, one thread) on the k^3 instance:
+    factor + one solve + residual.  Returns (factor flop rate, wall seconds, solve seconds per entry)."""
+    import oracle
+    import sparspak as S
+    from sparspak.sparse_solver import _matrix_arrays
+
+    A, b = workload(k, 1)
+    s, _ = symbolic(A, k)
+    o = oracle.OracleLU(s.slvr)
+    o.inmatrix_csc(*_matrix_arrays(A))
+    t0 = time.perf_counter()
+    o.factor()
+    t1 = time.perf_counter()
+    x = o.solve(b[:, 0])
+    t2 = time.perf_counter()
+    rr = np.linalg.norm(b[:, 0] - A @ x) / np.linalg.norm(b[:, 0])
+    nnz_lu = float(s.slvr.xlnz[-1] - 1 + s.slvr.xunz[-1] - 1)
+    return lu_flops(s.slvr) / (t1 - t0), t2 - t0, (t2 - t1) / nnz_lu, rr
+
+
+def cpu_baseline(args, F_full, nnz_full):
+    rate, wall, solve_per_entry, rr = cpu_sample(args.sample_grid)
+    est_ms = (F_full / rate + args.nrhs * solve_per_entry * nnz_full) * 1e3
+    return {"value": est_ms, "unit": "ms", "cores": 1, "kind": "port",
+            "sample": (f"oracle (C restatement of _inmatrix!/_lufactor!/_lulsolve!/_luusolve!, FP64, 1 thread) on the "
+                       f"{args.sample_grid}^3 instance of the same workload: factor at {rate / 1e9:.2f} GFLOP/s "
+                       f"({wall:.1f} s incl. one solve, rel. residual {rr:.1e}); value = 64^3 LU flops / that rate "
+                       f"+ {args.nrhs} solves scaled by nnz(L+U)"),
+            "factor_gflops": rate / 1e9}
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() and args.impl == "ours" else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def run_reference(args):
+    """--impl reference: the reference's algorithm on the host cores (the oracle port;
+    the Julia package cannot run here).  Each step is the bounded sample."""
+    ws, rank, _ = dist_setup(args)
+    if rank != 0:
+        return
+    A, _ = workload(args.grid, args.nrhs)
+    s, _ = symbolic(A, args.grid)
+    F = lu_flops(s.slvr)
+    nnz_full = float(s.slvr.xlnz[-1] - 1 + s.slvr.xunz[-1] - 1)
+    for _ in range(args.warmup):
+        cpu_sample(args.sample_grid)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        rate, wall, spe, rr = cpu_sample(args.sample_grid)
+        vals.append((F / rate + args.nrhs * spe * nnz_full) * 1e3)
+    wall = time.perf_counter() - t0
+    v = statistics.median(vals)
+    line = {"metric": METRIC, "value": v, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": wall * 1e3 / args.steps, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"laplace3d_{args.grid}^3_shift1e-3_nd_{args.nrhs}rhs", "n": A.shape[0],
+                       "nrhs": args.nrhs, "ordering": "nested dissection (grid)"},
+            "cpu_baseline": {"value": v, "unit": "ms", "cores": 1, "kind": "port",
+                             "sample": f"oracle on the {args.sample_grid}^3 instance per step, extrapolated by flops"},
+            "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+
+    import sparspak as S
+    from sparspak.sparse_solver import _ensure_engine, _matrix_arrays
+
+    ws, rank, local = dist_setup(args)
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    k, nrhs = args.grid, args.nrhs
+    A, b = workload(k, nrhs)
+    n = A.shape[0]
+    s, host_t = symbolic(A, k)
+    F = lu_flops(s.slvr)
+    eng = _ensure_engine(s.slvr)
+    colptr, rowval, nzval = _matrix_arrays(A)
+    t0 = time.perf_counter()
+    eng.set_pattern(colptr, rowval, s.slvr.order.rperm, s.slvr.order.rinvp, index_base=1)
+    host_t["pattern_s"] = time.perf_counter() - t0
+    stats = eng.stats()
+    stream = torch.cuda.Stream(dev)            # a real stream (the legacy default stream has handle 0)
+    torch.cuda.set_stream(stream)
+    eng.set_stream(stream.cuda_stream)
+
+    nz_d = torch.tensor(nzval, device=dev)
+    b_d = torch.tensor(np.ascontiguousarray(b.T), device=dev)       # (nrhs, n): rows are right-hand sides
+    x_d = torch.zeros_like(b_d)
+
+    def step(prec):
+        eng.load_values(nz_d, prec)
+        eng.factor(prec)
+        return eng.refine(b_d, x_d, prec, TOL, 30)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    def timed(fn, reps):
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = None
+        for _ in range(reps):
+            out = fn()
+        e1.record(stream)
+        barrier()
+        return e0.elapsed_time(e1) / reps, out
+
+    for _ in range(args.warmup):
+        step("fp32")
+    # which kernel class dominates the mixed step (one untimed step, every launch timed)
+    eng.profile(S._native.KERNEL_CLASSES)
+    eng.profile_reset()
+    step("fp32")
+    prof = eng.profile_read()
+    dom = max(prof, key=lambda c: prof[c]["ms"])
+    eng.profile([])
+    step("fp32")
+
+    # headline: launch sequences replayed as CUDA graphs, no per-kernel events
+    eng.profile_reset()
+    with Clocks(local) as clk:
+        ms_mixed, (it_mixed, rr_mixed) = timed(lambda: step("fp32"), args.steps)
+    clocks = clk.summary()
+    launches = sum(v["launches"] for v in eng.profile_read().values())
+    # live roofline: the same steps with CUDA events around every launch of the dominant class
+    eng.profile([dom])
+    eng.profile_reset()
+    ms_mixed_eager, _ = timed(lambda: step("fp32"), args.steps)
+    live = eng.profile_read()
+    eng.profile([])
+
+    # factor-only timings for GFLOP/s
+    eng.load_values(nz_d, "fp32")
+    ms_f32, _ = timed(lambda: (eng.load_values(nz_d, "fp32"), eng.factor("fp32")), args.steps)
+    for _ in range(args.warmup):
+        step("fp64")
+    ms_fp64, (it_fp64, rr_fp64) = timed(lambda: step("fp64"), args.steps)
+    ms_f64, _ = timed(lambda: (eng.load_values(nz_d, "fp64"), eng.factor("fp64")), max(1, args.steps // 2))
+    ms_asm32, _ = timed(lambda: eng.load_values(nz_d, "fp32"), args.steps)
+    ms_asm64, _ = timed(lambda: eng.load_values(nz_d, "fp64"), args.steps)
+
+    # e2e through the public API with pinned host buffers
+    nz_h = torch.tensor(nzval).pin_memory().numpy()
+    b_h = torch.tensor(b).pin_memory().numpy()
+    b_h = np.asfortranarray(b_h)
+    x_h = np.zeros_like(b_h, order="F")
+
+    def e2e():
+        eng.load_values(nz_h, "fp32")
+        eng.factor("fp32")
+        return eng.refine(b_h, x_h, "fp32", TOL, 30)
+
+    e2e()
+    ms_e2e, (it_e2e, rr_e2e) = timed(e2e, args.steps)
+    x_ref = x_d.cpu().numpy().T
+    rr_check = float(np.max(np.linalg.norm(b - A @ x_ref, axis=0) / np.linalg.norm(b, axis=0)))
+
+    # max over ranks
+    if ws > 1:
+        t = torch.tensor([ms_mixed, ms_fp64, ms_e2e], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_mixed, ms_fp64, ms_e2e = t.tolist()
+    if rank != 0:
+        return
+
+    pk, pk_kind = peaks()
+    d = live[dom]
+    per_launch_ms = d["ms"] / max(d["launches"], 1)
+    if dom in ("schur", "trail", "panel", "getrf"):
+        achieved = d["flops"] / (d["ms"] * 1e-3) / 1e12
+        roof = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops_sustained"], "unit": "TFLOP/s",
+                "peak_kind": f"{pk_kind} bf16 dense sustained (kernel timed inside a long step)"}
+    else:
+        achieved = d["bytes"] / (d["ms"] * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "peak_kind": f"{pk_kind} HBM copy bandwidth"}
+    roof.update({"frac": roof["achieved"] / roof["peak"], "traffic": None, "kernel": f"k_{dom}<float>",
+                 "launches": d["launches"], "ms_per_launch": per_launch_ms,
+                 "algorithmic_per_launch": (d["flops"] if roof["bound"] == "tensor" else d["bytes"]) / d["launches"]})
+    nnz_full = float(s.slvr.xlnz[-1] - 1 + s.slvr.xunz[-1] - 1)
+    cpu = cpu_baseline(args, F, nnz_full) if ws == 1 or rank == 0 else None
+    h2d = nzval.nbytes + b.nbytes
+    d2h = b.nbytes
+    line = {
+        "metric": METRIC, "value": ms_mixed, "unit": "ms", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_mixed, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 factor/solve + f64 residual/correction", "data": "synthetic",
+        "config": {"workload": f"laplace3d_{k}^3_shift1e-3_nd_{nrhs}rhs", "n": n, "nnz_A": int(A.nnz),
+                   "nrhs": nrhs, "ordering": "nested dissection (grid)", "maxblocksize": 30,
+                   "nnz_LU": int(nnz_full), "lu_flops": F, "fronts": stats["fronts"], "levels": stats["levels"],
+                   "l2": "inputs larger than L2 (factor %.2f GB)" % (nnz_full * 4 / 1e9), "parallelism": "replicas"},
+        "mixed": {"ms": ms_mixed, "ms_eager_profiled": ms_mixed_eager, "corrections": it_mixed, "relres": rr_mixed,
+                  "relres_host_check": rr_check,
+                  "factor_ms": ms_f32, "factor_gflops": F / (ms_f32 * 1e-3) / 1e9, "assembly_ms": ms_asm32},
+        "fp64": {"ms": ms_fp64, "corrections": it_fp64, "relres": rr_fp64, "factor_ms": ms_f64,
+                 "factor_gflops": F / (ms_f64 * 1e-3) / 1e9, "assembly_ms": ms_asm64},
+        "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
+        "host_once_per_pattern": host_t,
+        "profile_mixed_step": {c: {"ms": round(v["ms"], 4), "launches": v["launches"]} for c, v in prof.items()},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": {"value": ms_e2e, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "corrections": it_e2e, "relres": rr_e2e},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

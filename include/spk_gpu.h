@@ -148,6 +148,31 @@ int spk_get_factors(spk_handle* h, int precision, double* lnz, double* unz, int6
 int spk_stats(spk_handle* h, int64_t* nfronts, int64_t* nlevels, int64_t* factor_entries,
               double* lu_flops);
 
+/* Kernel classes for launch accounting and event timing. */
+#define SPK_K_ASSEMBLE 0   /* value scatter (_inmatrix!)                        */
+#define SPK_K_GETRF 1      /* first diagonal block of each front                */
+#define SPK_K_PANEL 2      /* panel triangular solves (_trsm!, _luswap!)         */
+#define SPK_K_TRAIL 3      /* rank-w update inside a front (+ next diagonal LU)  */
+#define SPK_K_SCHUR 4      /* front Schur complement + scatter-add (_gemm!, _assmb!) */
+#define SPK_K_FWD 5        /* forward substitution (_lulsolve!)                 */
+#define SPK_K_BWD 6        /* backward substitution (_luusolve!)                */
+#define SPK_K_PERMUTE 7    /* right-hand side permutation                       */
+#define SPK_K_RESIDUAL 8   /* r = b - A x                                       */
+#define SPK_K_COUNT 9
+
+/*
+ * Launch accounting (no counterpart in the reference, whose only timing is
+ * the tests' @time).  Every kernel launch of the handle is counted with its
+ * algorithmic flops and bytes; spk_profile(h, mask) additionally brackets
+ * each launch of the classes in `mask` (bit SPK_K_*) with CUDA events on the
+ * handle's stream.  spk_profile_read returns, for one class since the last
+ * spk_profile_reset: summed event time in ms (0 for untimed classes),
+ * launches, algorithmic flops and algorithmic bytes.
+ */
+int spk_profile(spk_handle* h, unsigned mask);
+int spk_profile_reset(spk_handle* h);
+int spk_profile_read(spk_handle* h, int kind, double* ms, int64_t* launches, double* flops, double* bytes);
+
 /* Text of the last error on this handle (never NULL); with h == NULL, the
  * reason the last spk_create on this thread failed. */
 const char* spk_last_error(spk_handle* h);

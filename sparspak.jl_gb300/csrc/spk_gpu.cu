@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <type_traits>
 #include <string>
 #include <vector>
 
@@ -23,10 +24,26 @@ typedef int64_t i64;
 namespace {
 
 struct LaunchRec {
-    i64 off = 0;      // into sched_ids; prefix array at off + index_of_launch
+    i64 off = 0;      // into sched_ids
     i64 poff = 0;     // into sched_prefix
     int count = 0;
     int tiles = 0;
+    double flops = 0.0;   // algorithmic flops of the launch (solves: per right-hand side)
+    double words = 0.0;   // algorithmic factor entries read or written (times sizeof(T) = bytes)
+};
+
+// A captured launch sequence and the accounting of one replay.
+struct GraphRec {
+    cudaGraphExec_t exec = nullptr;
+    double flops[SPK_K_COUNT] = {};
+    double bytes[SPK_K_COUNT] = {};
+    int64_t launches[SPK_K_COUNT] = {};
+};
+
+// One CUDA event pair per timed launch.
+struct Timed {
+    cudaEvent_t a, b;
+    int kind;
 };
 
 struct LevelPlan {
@@ -58,6 +75,7 @@ struct spk_handle {
     std::vector<i64> xlnz0, xunz0;  // reference layout, 0-based offsets [n+1]
     std::vector<HFront> fronts;
     std::vector<int> col_front;     // column -> front
+    std::vector<int> col_snode;     // column -> supernode (0-based)
     std::vector<int> rows;          // concatenated R_F
     std::vector<int> runid, run_tgt, run_start;
     std::vector<ll> run_rel;
@@ -66,6 +84,7 @@ struct spk_handle {
     std::vector<int> sched_ids, sched_prefix;
     i64 fsize = 0;
     int wmax = 1;             // widest supernode
+    double amalgamation = 0.1;  // allowed relative padding of a front
     double lu_flops = 0.0;
 
     // device structure
@@ -100,6 +119,20 @@ struct spk_handle {
     cudaStream_t own = nullptr, stream = nullptr;
     int device = -1;
     std::string err;
+
+    // launch accounting and optional per-class event timing
+    unsigned prof_mask = 0;
+    std::vector<Timed> pending;
+    std::vector<cudaEvent_t> event_pool;
+    double prof_ms[SPK_K_COUNT] = {};
+    double prof_flops[SPK_K_COUNT] = {};
+    double prof_bytes[SPK_K_COUNT] = {};
+    int64_t prof_launches[SPK_K_COUNT] = {};
+
+    // captured sequences: factor per precision, solve per precision x right-hand sides
+    bool use_graphs = true;
+    GraphRec g_factor[2];
+    GraphRec g_solve[2][spk::MAXRHS + 1];
 };
 
 // ---------------------------------------------------------------------------
@@ -136,6 +169,115 @@ static spk::Launch launch_of(const spk_handle* h, const LaunchRec& r) {
     return L;
 }
 
+static cudaEvent_t take_event(spk_handle* h) {
+    if (!h->event_pool.empty()) {
+        cudaEvent_t e = h->event_pool.back();
+        h->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Bracket one kernel launch: count it, add its algorithmic work, and when
+// its class is selected by spk_profile record an event pair around it.
+struct LaunchScope {
+    spk_handle* h;
+    int kind;
+    Timed t{};
+    bool timed;
+    LaunchScope(spk_handle* h_, int kind_, double flops, double bytes) : h(h_), kind(kind_) {
+        h->prof_launches[kind] += 1;
+        h->prof_flops[kind] += flops;
+        h->prof_bytes[kind] += bytes;
+        timed = (h->prof_mask >> kind) & 1u;
+        if (timed) {
+            t.a = take_event(h);
+            t.b = take_event(h);
+            t.kind = kind;
+            cudaEventRecord(t.a, h->stream);
+        }
+    }
+    ~LaunchScope() {
+        if (timed) {
+            cudaEventRecord(t.b, h->stream);
+            h->pending.push_back(t);
+        }
+    }
+};
+
+static void collect_events(spk_handle* h) {
+    for (Timed& t : h->pending) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(t.b) == cudaSuccess && cudaEventElapsedTime(&ms, t.a, t.b) == cudaSuccess)
+            h->prof_ms[t.kind] += ms;
+        h->event_pool.push_back(t.a);
+        h->event_pool.push_back(t.b);
+    }
+    h->pending.clear();
+}
+
+static void drop_graph(GraphRec& g) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = GraphRec();
+}
+
+static void drop_solve_graphs(spk_handle* h) {
+    for (int p = 0; p < 2; ++p)
+        for (int r = 0; r <= spk::MAXRHS; ++r) drop_graph(h->g_solve[p][r]);
+}
+
+// Run `body` (which issues launches on h->stream) through a CUDA graph: the
+// first call captures it on the handle's own stream, every call replays it
+// on h->stream.  With event timing requested the launches go out eagerly.
+template <typename Body>
+static int via_graph(spk_handle* h, GraphRec& g, Body body) {
+    if (h->prof_mask != 0 || !h->use_graphs) return body();
+    if (!g.exec) {
+        double f0[SPK_K_COUNT], b0[SPK_K_COUNT];
+        int64_t l0[SPK_K_COUNT];
+        for (int k = 0; k < SPK_K_COUNT; ++k) { f0[k] = h->prof_flops[k]; b0[k] = h->prof_bytes[k]; l0[k] = h->prof_launches[k]; }
+        cudaStream_t user = h->stream;
+        h->stream = h->own;
+        cudaError_t e = cudaStreamBeginCapture(h->own, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            h->stream = user;
+            return set_err(h, SPK_ECUDA, std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(e));
+        }
+        int rc = body();
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamEndCapture(h->own, &graph);
+        h->stream = user;
+        if (rc != SPK_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (e != cudaSuccess) return set_err(h, SPK_ECUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            g.exec = nullptr;
+            return set_err(h, SPK_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        }
+        for (int k = 0; k < SPK_K_COUNT; ++k) {
+            g.flops[k] = h->prof_flops[k] - f0[k];
+            g.bytes[k] = h->prof_bytes[k] - b0[k];
+            g.launches[k] = h->prof_launches[k] - l0[k];
+            h->prof_flops[k] = f0[k];
+            h->prof_bytes[k] = b0[k];
+            h->prof_launches[k] = l0[k];
+        }
+    }
+    CU(h, cudaGraphLaunch(g.exec, h->stream));
+    for (int k = 0; k < SPK_K_COUNT; ++k) {
+        h->prof_flops[k] += g.flops[k];
+        h->prof_bytes[k] += g.bytes[k];
+        h->prof_launches[k] += g.launches[k];
+    }
+    return SPK_OK;
+}
+
 // ---------------------------------------------------------------------------
 // structure analysis
 // ---------------------------------------------------------------------------
@@ -151,9 +293,11 @@ static int analyse(spk_handle* h, const int64_t* xsuper, const int64_t* snode, c
         if (w > spk::MAXW) return set_err(h, SPK_EARG, "supernodes wider than 64 columns are not supported");
         h->wmax = std::max(h->wmax, w);
     }
+    h->col_snode.resize(n);
     for (i64 j = 0; j < n; ++j) {
         i64 s = snode[j] - base;
         if (s < 0 || s >= ns || j < h->xs[s] || j >= h->xs[s + 1]) return set_err(h, SPK_ESTRUCT, "snode inconsistent with xsuper");
+        h->col_snode[j] = (int)s;
     }
     h->xlindx0.resize(ns + 1);
     for (i64 s = 0; s <= ns; ++s) h->xlindx0[s] = xlindx[s] - base;
@@ -194,20 +338,30 @@ static int analyse(spk_handle* h, const int64_t* xsuper, const int64_t* snode, c
     }
     h->lu_flops = fl;
 
-    // fronts: maximal chains s, s+1, ... whose structures nest exactly
+    // Fronts: maximal paths s, s+1, ..., e of the supernodal elimination tree
+    // (each supernode's parent is the next one) whose dense front storage
+    // (nf^2 + 2 nf m entries) exceeds the pieces' exact lnz+unz storage by at
+    // most the amalgamation allowance.  Exact fundamental chains need no
+    // padding; padded positions are structural zeros and stay exactly zero
+    // (every product that reaches them has a structurally zero factor).
     h->col_front.assign(n, -1);
     h->fronts.clear();
+    auto exact_entries = [&](i64 t) {
+        double w = h->xs[t + 1] - h->xs[t], len = (double)(h->xlindx0[t + 1] - h->xlindx0[t]);
+        return 2.0 * len * w - w * w;
+    };
     for (i64 s = 0; s < ns;) {
         i64 e = s;
+        double exact = exact_entries(s);
         while (e + 1 < ns) {
             int w = h->xs[e + 1] - h->xs[e];
             i64 a = h->xlindx0[e], len = h->xlindx0[e + 1] - a;
-            i64 a2 = h->xlindx0[e + 1], len2 = h->xlindx0[e + 2] - a2;
-            if (len - w != len2 || len2 == 0) break;
-            bool same = true;
-            for (i64 k = 0; k < len2; ++k)
-                if (h->lindx0[a + w + k] != h->lindx0[a2 + k]) { same = false; break; }
-            if (!same) break;
+            if (len == w || h->lindx0[a + w] != h->xs[e + 1]) break;   // parent is not the next supernode
+            double ex2 = exact + exact_entries(e + 1);
+            double nf = h->xs[e + 2] - h->xs[s];
+            double m = (double)(h->xlindx0[e + 2] - h->xlindx0[e + 1]) - (h->xs[e + 2] - h->xs[e + 1]);
+            if (nf * nf + 2.0 * nf * m > (1.0 + h->amalgamation) * ex2) break;
+            exact = ex2;
             ++e;
         }
         HFront F{};
@@ -276,9 +430,8 @@ static int analyse(spk_handle* h, const int64_t* xsuper, const int64_t* snode, c
                 if (row < G.f + G.nf) pos = (int)(row - G.f);
                 else {
                     while (q < G.m && RG[q] < row) ++q;
-                    if (q >= G.m || RG[q] != row)
-                        return set_err(h, SPK_ESTRUCT, "supernodal structure is not closed under elimination");
-                    pos = G.nf + q;
+                    // absent: the update there is an exact zero (padding of F), skipped
+                    pos = (q < G.m && RG[q] == row) ? G.nf + q : -1;
                 }
                 h->rel.push_back(pos);
             }
@@ -290,10 +443,12 @@ static int analyse(spk_handle* h, const int64_t* xsuper, const int64_t* snode, c
     return SPK_OK;
 }
 
-static void add_launch(spk_handle* h, LaunchRec& rec, const std::vector<int>& ids, const std::vector<int>& tiles) {
+static void add_launch(spk_handle* h, LaunchRec& rec, const std::vector<int>& ids, const std::vector<int>& tiles,
+                       const std::vector<double>& flops, const std::vector<double>& words) {
     rec.off = (i64)h->sched_ids.size();
     rec.poff = (i64)h->sched_prefix.size();
     rec.count = 0;
+    rec.flops = rec.words = 0.0;
     int acc = 0;
     for (size_t k = 0; k < ids.size(); ++k) {
         if (tiles[k] <= 0) continue;
@@ -301,6 +456,8 @@ static void add_launch(spk_handle* h, LaunchRec& rec, const std::vector<int>& id
         h->sched_prefix.push_back(acc);
         acc += tiles[k];
         ++rec.count;
+        rec.flops += flops[k];
+        rec.words += words[k];
     }
     h->sched_prefix.push_back(acc);
     rec.tiles = acc;
@@ -320,41 +477,71 @@ static void build_schedule(spk_handle* h) {
         const std::vector<int>& ids = at[l];
         int maxp = 0;
         for (int id : ids) maxp = std::max(maxp, h->fronts[id].npieces);
-        std::vector<int> t(ids.size());
-        for (size_t k = 0; k < ids.size(); ++k) t[k] = 1;
-        add_launch(h, P.getrf0, ids, t);
+        const size_t nid = ids.size();
+        std::vector<int> t(nid, 1);
+        std::vector<double> fl(nid), wd(nid);
+        for (size_t k = 0; k < nid; ++k) {
+            const HFront& F = h->fronts[ids[k]];
+            double w = h->xs[F.piece0 + 1] - h->xs[F.piece0];
+            fl[k] = 2.0 / 3.0 * w * w * w;
+            wd[k] = 2.0 * w * w;
+        }
+        add_launch(h, P.getrf0, ids, t, fl, wd);
         P.panel.resize(maxp);
         P.trail.resize(maxp);
         P.fwd.resize(maxp);
         P.bwd.resize(maxp);
         for (int s = 0; s < maxp; ++s) {
-            std::vector<int> tp(ids.size()), tt(ids.size()), tf(ids.size()), tb(ids.size());
-            for (size_t k = 0; k < ids.size(); ++k) {
+            std::vector<int> tp(nid), tt(nid), tf(nid), tb(nid);
+            std::vector<double> fp(nid), wp(nid), ft(nid), wt(nid), ff(nid), wf(nid), fb(nid), wb(nid);
+            for (size_t k = 0; k < nid; ++k) {
                 const HFront& F = h->fronts[ids[k]];
                 if (s >= F.npieces) { tp[k] = tt[k] = tf[k] = tb[k] = 0; continue; }
                 int p = F.piece0 + s;
                 int p1 = h->xs[p + 1] - (int)F.f;
+                double w = h->xs[p + 1] - h->xs[p];
                 int ld = F.nf + F.m;
                 tp[k] = cdiv(ld - p1, spk::TP) + cdiv(F.nf - p1, spk::TP) + cdiv(F.m, spk::TP);
                 tt[k] = cdiv(ld - p1, spk::TT) * cdiv(F.nf - p1, spk::TT) + cdiv(F.nf - p1, spk::TT) * cdiv(F.m, spk::TT);
                 tf[k] = std::max(1, cdiv(ld - p1, spk::TS));
+                double panel_vecs = (double)(ld - p1) + (double)(F.nf - p1) + F.m;
+                fp[k] = w * w * panel_vecs;
+                wp[k] = 2.0 * w * panel_vecs + w * w;
+                double area = (double)(ld - p1) * (F.nf - p1) + (double)(F.nf - p1) * F.m;
+                ft[k] = 2.0 * w * area;
+                wt[k] = 2.0 * area + w * panel_vecs;
+                if (s + 1 < F.npieces) {
+                    double w2 = h->xs[p + 2] - h->xs[p + 1];
+                    ft[k] += 2.0 / 3.0 * w2 * w2 * w2;
+                    wt[k] += 2.0 * w2 * w2;
+                }
+                ff[k] = w * w + 2.0 * w * (ld - p1);
+                wf[k] = w * w + w * (ld - p1);
                 int q = F.piece0 + F.npieces - 1 - s;
                 int q0 = h->xs[q] - (int)F.f;
+                double wq = h->xs[q + 1] - h->xs[q];
                 tb[k] = std::max(1, cdiv(q0, spk::TS));
+                fb[k] = wq * wq + 2.0 * wq * q0;
+                wb[k] = wq * wq + wq * q0;
             }
-            add_launch(h, P.panel[s], ids, tp);
-            add_launch(h, P.trail[s], ids, tt);
-            add_launch(h, P.fwd[s], ids, tf);
-            add_launch(h, P.bwd[s], ids, tb);
+            add_launch(h, P.panel[s], ids, tp, fp, wp);
+            add_launch(h, P.trail[s], ids, tt, ft, wt);
+            add_launch(h, P.fwd[s], ids, tf, ff, wf);
+            add_launch(h, P.bwd[s], ids, tb, fb, wb);
         }
-        std::vector<int> tsch(ids.size()), tbu(ids.size());
-        for (size_t k = 0; k < ids.size(); ++k) {
+        std::vector<int> tsch(nid), tbu(nid);
+        std::vector<double> fs(nid), ws(nid), fu(nid), wu(nid);
+        for (size_t k = 0; k < nid; ++k) {
             const HFront& F = h->fronts[ids[k]];
             tsch[k] = F.m > 0 ? cdiv(F.m, spk::TT) * cdiv(F.m, spk::TT) : 0;
             tbu[k] = F.m > 0 ? cdiv(F.nf, spk::TS / 32) : 0;
+            fs[k] = 2.0 * (double)F.m * F.m * F.nf;
+            ws[k] = 2.0 * (double)F.m * F.nf + 2.0 * (double)F.m * F.m;
+            fu[k] = 2.0 * (double)F.m * F.nf;
+            wu[k] = (double)F.m * F.nf;
         }
-        add_launch(h, P.schur, ids, tsch);
-        add_launch(h, P.bwdu, ids, tbu);
+        add_launch(h, P.schur, ids, tsch, fs, ws);
+        add_launch(h, P.bwdu, ids, tbu, fu, wu);
     }
 }
 
@@ -416,6 +603,7 @@ static int ensure_storage(spk_handle* h) {
 
 static int ensure_rhs(spk_handle* h, i64 nrhs) {
     if (nrhs <= h->rhs_cap) return SPK_OK;
+    drop_solve_graphs(h);
     cudaFree(h->d_wb); cudaFree(h->d_wy); cudaFree(h->d_wx);
     cudaFree(h->d_rhs); cudaFree(h->d_x); cudaFree(h->d_r); cudaFree(h->d_sums);
     h->d_wb = h->d_wy = h->d_wx = nullptr;
@@ -439,30 +627,47 @@ static int ensure_rhs(spk_handle* h, i64 nrhs) {
 // numeric phases
 // ---------------------------------------------------------------------------
 template <typename T>
-static int run_factor(spk_handle* h) {
-    Storage<T>& S = storage<T>(h);
-    T* fac = S.d;
-    const int big = INT_MAX;
-    const size_t panel_smem = sizeof(T) * (size_t)(h->wmax * h->wmax + h->wmax * spk::TP) + sizeof(int) * spk::MAXW;
-    CU(h, cudaFuncSetAttribute(spk::k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem));
-    CU(h, cudaMemcpyAsync(h->d_info, &big, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+static size_t panel_smem(const spk_handle* h) {
+    return sizeof(T) * (size_t)(h->wmax * h->wmax + h->wmax * spk::TP) + sizeof(int) * spk::MAXW;
+}
+
+template <typename T>
+static int factor_launches(spk_handle* h) {
+    T* fac = storage<T>(h).d;
+    const size_t psmem = panel_smem<T>(h);
     for (const LevelPlan& P : h->levels) {
-        if (P.getrf0.tiles > 0)
+        if (P.getrf0.tiles > 0) {
+            LaunchScope ls(h, SPK_K_GETRF, P.getrf0.flops, P.getrf0.words * sizeof(T));
             spk::k_getrf_first<T><<<P.getrf0.tiles, 128, 0, h->stream>>>(fac, h->d_ipiv, h->d_info, h->sched,
                                                                             launch_of(h, P.getrf0));
+        }
         for (size_t s = 0; s < P.panel.size(); ++s) {
-            if (P.panel[s].tiles > 0)
-                spk::k_panel<T><<<P.panel[s].tiles, spk::TP, panel_smem, h->stream>>>(
+            if (P.panel[s].tiles > 0) {
+                LaunchScope ls(h, SPK_K_PANEL, P.panel[s].flops, P.panel[s].words * sizeof(T));
+                spk::k_panel<T><<<P.panel[s].tiles, spk::TP, psmem, h->stream>>>(
                     fac, h->d_ipiv, h->sched, launch_of(h, P.panel[s]), (int)s, h->wmax);
-            if (P.trail[s].tiles > 0)
+            }
+            if (P.trail[s].tiles > 0) {
+                LaunchScope ls(h, SPK_K_TRAIL, P.trail[s].flops, P.trail[s].words * sizeof(T));
                 spk::k_trail<T><<<P.trail[s].tiles, 256, 0, h->stream>>>(fac, h->d_ipiv, h->d_info, h->sched,
                                                                            launch_of(h, P.trail[s]), (int)s);
+            }
         }
-        if (P.schur.tiles > 0)
+        if (P.schur.tiles > 0) {
+            LaunchScope ls(h, SPK_K_SCHUR, P.schur.flops, P.schur.words * sizeof(T));
             spk::k_schur<T><<<P.schur.tiles, 256, 0, h->stream>>>(fac, h->sched, launch_of(h, P.schur));
+        }
     }
     CU(h, cudaGetLastError());
     return SPK_OK;
+}
+
+template <typename T>
+static int run_factor(spk_handle* h) {
+    const int big = INT_MAX;
+    CU(h, cudaFuncSetAttribute(spk::k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem<T>(h)));
+    CU(h, cudaMemcpyAsync(h->d_info, &big, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    return via_graph(h, h->g_factor[std::is_same<T, float>::value ? 1 : 0], [&] { return factor_launches<T>(h); });
 }
 
 // Solve in place on the permuted work vectors: wb (rhs, consumed) -> wx.
@@ -475,18 +680,24 @@ static int run_solve_permuted(spk_handle* h, int nrhs) {
     const int n = (int)h->n;
     for (const LevelPlan& P : h->levels)
         for (size_t s = 0; s < P.fwd.size(); ++s)
-            if (P.fwd[s].tiles > 0)
+            if (P.fwd[s].tiles > 0) {
+                LaunchScope ls(h, SPK_K_FWD, P.fwd[s].flops * nrhs, P.fwd[s].words * sizeof(T));
                 spk::k_fwd<T><<<P.fwd[s].tiles, spk::TS, 0, h->stream>>>(fac, h->d_ipiv, b, y, n, nrhs, h->sched,
                                                                           launch_of(h, P.fwd[s]), (int)s);
+            }
     for (size_t l = h->levels.size(); l-- > 0;) {
         const LevelPlan& P = h->levels[l];
-        if (P.bwdu.tiles > 0)
+        if (P.bwdu.tiles > 0) {
+            LaunchScope ls(h, SPK_K_BWD, P.bwdu.flops * nrhs, P.bwdu.words * sizeof(T));
             spk::k_bwd_u12<T><<<P.bwdu.tiles, spk::TS, 0, h->stream>>>(fac, y, x, n, nrhs, h->sched,
                                                                         launch_of(h, P.bwdu));
+        }
         for (size_t s = 0; s < P.bwd.size(); ++s)
-            if (P.bwd[s].tiles > 0)
+            if (P.bwd[s].tiles > 0) {
+                LaunchScope ls(h, SPK_K_BWD, P.bwd[s].flops * nrhs, P.bwd[s].words * sizeof(T));
                 spk::k_bwd<T><<<P.bwd[s].tiles, spk::TS, 0, h->stream>>>(fac, y, x, n, nrhs, h->sched,
                                                                           launch_of(h, P.bwd[s]), (int)s);
+            }
     }
     CU(h, cudaGetLastError());
     return SPK_OK;
@@ -500,11 +711,19 @@ static int solve_device(spk_handle* h, const double* rhs, i64 ldr, double* x, i6
         int nc = (int)std::min<i64>(spk::MAXRHS, nrhs - c0);
         ll tot = (ll)n * nc;
         int blocks = (int)((tot + 255) / 256);
-        spk::k_permute<double, T><<<blocks, 256, 0, h->stream>>>(rhs + c0 * ldr, ldr, (T*)h->d_wb, n, h->d_rperm, n, nc);
-        int rc = run_solve_permuted<T>(h, nc);
+        {
+            LaunchScope ls(h, SPK_K_PERMUTE, 0.0, (double)tot * (8 + 4 + sizeof(T)));
+            spk::k_permute<double, T><<<blocks, 256, 0, h->stream>>>(rhs + c0 * ldr, ldr, (T*)h->d_wb, n, h->d_rperm,
+                                                                     n, nc);
+        }
+        int rc = via_graph(h, h->g_solve[std::is_same<T, float>::value ? 1 : 0][nc],
+                           [&] { return run_solve_permuted<T>(h, nc); });
         if (rc) return rc;
-        spk::k_unpermute<T><<<blocks, 256, 0, h->stream>>>((const T*)h->d_wx, n, x + c0 * ldx, ldx, h->d_rinvp, n, nc,
-                                                           accumulate);
+        {
+            LaunchScope ls(h, SPK_K_PERMUTE, 0.0, (double)tot * (8 * (accumulate ? 2 : 1) + 4 + sizeof(T)));
+            spk::k_unpermute<T><<<blocks, 256, 0, h->stream>>>((const T*)h->d_wx, n, x + c0 * ldx, ldx, h->d_rinvp, n,
+                                                               nc, accumulate);
+        }
     }
     CU(h, cudaGetLastError());
     return SPK_OK;
@@ -515,8 +734,12 @@ static int residual_device(spk_handle* h, const double* b, i64 ldb, const double
     const int n = (int)h->n;
     CU(h, cudaMemsetAsync(h->d_sums, 0, sizeof(double) * 2 * (size_t)nrhs, h->stream));
     dim3 grid((n + 255) / 256, (unsigned)nrhs);
-    spk::k_residual<<<grid, 256, 0, h->stream>>>(h->d_aval, h->d_rowptr, h->d_col, h->d_src, x, ldx, b, ldb, h->d_r, n,
-                                                 (int)nrhs, h->d_sums);
+    {
+        LaunchScope ls(h, SPK_K_RESIDUAL, 2.0 * h->nnz * nrhs, (double)h->nnz * (8 + 4 + 8) + 8.0 * h->nnz * nrhs +
+                                                                  24.0 * n * nrhs);
+        spk::k_residual<<<grid, 256, 0, h->stream>>>(h->d_aval, h->d_rowptr, h->d_col, h->d_src, x, ldx, b, ldb, h->d_r,
+                                                     n, (int)nrhs, h->d_sums);
+    }
     CU(h, cudaGetLastError());
     std::vector<double> sums(2 * nrhs);
     CU(h, cudaMemcpyAsync(sums.data(), h->d_sums, sizeof(double) * 2 * nrhs, cudaMemcpyDeviceToHost, h->stream));
@@ -550,6 +773,7 @@ static int load_into(spk_handle* h) {
     CU(h, cudaMemsetAsync(S.d, 0, sizeof(T) * (size_t)h->fsize, h->stream));
     if (h->nnz > 0) {
         int blocks = (int)std::min<i64>((h->nnz + 255) / 256, 152 * 16);
+        LaunchScope ls(h, SPK_K_ASSEMBLE, 0.0, (double)h->nnz * (8 + 8 + 2 * sizeof(T)));
         spk::k_scatter_values<T><<<blocks, 256, 0, h->stream>>>(h->d_aval, h->d_slot, S.d, h->nnz);
     }
     CU(h, cudaGetLastError());
@@ -569,6 +793,20 @@ static int fetch_factor(spk_handle* h, std::vector<double>& out) {
 
 static bool factored(spk_handle* h, int precision) {
     return precision == SPK_FP64 ? h->s64.factored : h->s32.factored;
+}
+
+// Does (i, j) (permuted, 0-based) belong to the reference's structure?  L
+// part (i >= first column of j's supernode): i in that supernode's rows;
+// otherwise U part: j in the off-diagonal rows of i's supernode.
+static bool in_structure(const spk_handle* h, int i, int j) {
+    const int sj = h->col_snode[j];
+    int s = (i >= h->xs[sj]) ? sj : h->col_snode[i];
+    int key = (i >= h->xs[sj]) ? i : j;
+    const int* a = h->lindx0.data() + h->xlindx0[s];
+    const int* b = h->lindx0.data() + h->xlindx0[s + 1];
+    if (s != sj) a += h->xs[s + 1] - h->xs[s];
+    const int* q = std::lower_bound(a, b, key);
+    return q != b && *q == key;
 }
 
 // ---------------------------------------------------------------------------
@@ -657,7 +895,9 @@ int spk_set_pattern(spk_handle* h, int64_t ncols, const int64_t* colptr, const i
             const int inew = h->rinvp0[i], jnew = h->rinvp0[j];
             const HFront& F = h->fronts[h->col_front[jnew]];
             ll s = -1;
-            if (inew >= F.f && inew < F.f + F.nf) {
+            if (!in_structure(h, inew, jnew)) {
+                s = -1;
+            } else if (inew >= F.f && inew < F.f + F.nf) {
                 s = F.loff + (ll)(jnew - F.f) * (F.nf + F.m) + (inew - F.f);
             } else if (inew > jnew) {
                 const int* R = h->rows.data() + F.rows_off;
@@ -877,17 +1117,26 @@ int spk_get_factors(spk_handle* h, int precision, double* lnz, double* unz, int6
     if (rc) return rc;
     for (const HFront& F : h->fronts) {
         const int ld = F.nf + F.m;
+        const int* R = h->rows.data() + F.rows_off;
+        std::vector<int> pos;
         for (int s = F.piece0; s < F.piece0 + F.npieces; ++s) {
             const int p0 = h->xs[s] - (int)F.f, w = h->xs[s + 1] - h->xs[s];
-            const i64 jlen = ld - p0;
+            const i64 a = h->xlindx0[s], jlen = h->xlindx0[s + 1] - a;
+            // position of each of the piece's rows in the (padded) front
+            pos.resize(jlen);
+            for (i64 t = 0; t < jlen; ++t) {
+                int row = h->lindx0[a + t];
+                pos[t] = row < F.f + F.nf ? (int)(row - F.f)
+                                          : F.nf + (int)(std::lower_bound(R, R + F.m, row) - R);
+            }
             const i64 lbase = h->xlnz0[h->xs[s]], ubase = h->xunz0[h->xs[s]];
             for (int k = 0; k < w; ++k) {
                 if (lnz)
-                    for (i64 t = 0; t < jlen; ++t) lnz[lbase + k * jlen + t] = fac[F.loff + (i64)(p0 + k) * ld + p0 + t];
+                    for (i64 t = 0; t < jlen; ++t) lnz[lbase + k * jlen + t] = fac[F.loff + (i64)(p0 + k) * ld + pos[t]];
                 if (unz)
                     for (i64 i = 0; i < jlen - w; ++i) {
-                        i64 c = p0 + w + i;
-                        unz[ubase + k * (jlen - w) + i] = c < F.nf ? fac[F.loff + c * ld + p0 + k]
+                        const int c = pos[w + i];
+                        unz[ubase + k * (jlen - w) + i] = c < F.nf ? fac[F.loff + (i64)c * ld + p0 + k]
                                                                    : fac[F.uoff + (i64)(p0 + k) * F.m + (c - F.nf)];
                     }
             }
@@ -913,6 +1162,36 @@ int spk_stats(spk_handle* h, int64_t* nfronts, int64_t* nlevels, int64_t* factor
     return SPK_OK;
 }
 
+int spk_profile(spk_handle* h, unsigned mask) {
+    int rc = check_h(h);
+    if (rc) return rc;
+    h->prof_mask = mask;
+    return SPK_OK;
+}
+
+int spk_profile_reset(spk_handle* h) {
+    int rc = check_h(h);
+    if (rc) return rc;
+    collect_events(h);
+    for (int k = 0; k < SPK_K_COUNT; ++k) {
+        h->prof_ms[k] = h->prof_flops[k] = h->prof_bytes[k] = 0.0;
+        h->prof_launches[k] = 0;
+    }
+    return SPK_OK;
+}
+
+int spk_profile_read(spk_handle* h, int kind, double* ms, int64_t* launches, double* flops, double* bytes) {
+    int rc = check_h(h);
+    if (rc) return rc;
+    if (kind < 0 || kind >= SPK_K_COUNT) return set_err(h, SPK_EARG, "spk_profile_read: bad kernel class");
+    collect_events(h);
+    if (ms) *ms = h->prof_ms[kind];
+    if (launches) *launches = h->prof_launches[kind];
+    if (flops) *flops = h->prof_flops[kind];
+    if (bytes) *bytes = h->prof_bytes[kind];
+    return SPK_OK;
+}
+
 const char* spk_last_error(spk_handle* h) { return h ? h->err.c_str() : g_create_err.c_str(); }
 
 void spk_destroy(spk_handle* h) {
@@ -925,6 +1204,11 @@ void spk_destroy(spk_handle* h) {
                     h->d_wy, h->d_wx, h->d_rhs, h->d_x, h->d_r, h->d_sums};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    collect_events(h);
+    for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
+    drop_graph(h->g_factor[0]);
+    drop_graph(h->g_factor[1]);
+    drop_solve_graphs(h);
     if (h->own) cudaStreamDestroy(h->own);
     delete h;
 }

@@ -1,15 +1,17 @@
 // Device kernels of the supernodal LU engine (sm_103a).
 //
-// Storage.  Consecutive supernodes that form one fundamental supernode (a
-// chain whose structures nest exactly) are grouped into a *front*.  A front
-// F owns columns f..f+nf-1 and has m off-diagonal rows R_F (global,
-// permuted, ascending).  Its part of the factor is
+// Storage.  Consecutive supernodes that form a path of the elimination tree
+// (each one's parent is the next) are grouped into a *front*, allowing a
+// little padding (structural zeros that stay exactly zero).  A front F owns
+// columns f..f+nf-1 and has m off-diagonal rows R_F (global, permuted,
+// ascending: the rows of its last supernode below the front).  Its part of
+// the factor is
 //   Lf: (nf+m) x nf column-major, ld = nf+m: rows 0..nf-1 are the front's own
 //       columns (unit-lower L11 below the diagonal, U11 on and above it),
 //       rows nf.. are L21;
 //   Uf: m x nf column-major (U12 transposed: column k holds U row f+k).
-// This is a permutation of the reference's lnz/unz storage with the same
-// number of entries (src/SparseMethod/SpkSparseBase.jl:253-284).
+// Without padding this is a permutation of the reference's lnz/unz storage
+// (src/SparseMethod/SpkSparseBase.jl:253-284); with padding it holds it.
 //
 // Pivoting.  Every supernode of the reference partition (a *piece* of a
 // front, at most 32 columns) factors its own diagonal block with row
@@ -431,6 +433,7 @@ __global__ void __launch_bounds__(256) k_schur(T* fac, Sched S, Launch L) {
             const DFront G = S.fronts[S.run_tgt[g]];
             const ll base = S.run_rel[g] - S.run_start[g];
             const int pr = S.rel[base + r], pc = S.rel[base + c];
+            if (pr < 0 || pc < 0) continue;     // exact zero: (r, c) is padding of F only
             ll addr;
             if (r >= c || pc < G.nf) addr = G.loff + (ll)pc * G.ld + pr;
             else addr = G.uoff + (ll)pr * G.m + (pc - G.nf);

@@ -43,12 +43,16 @@ GPU_SYMBOLS = {
     "spk_residual": (ctypes.c_int, [VP, VP, VP, i64, i64, ctypes.c_int, PD]),
     "spk_get_factors": (ctypes.c_int, [VP, ctypes.c_int, PD, PD, P64]),
     "spk_stats": (ctypes.c_int, [VP, P64, P64, P64, PD]),
+    "spk_profile": (ctypes.c_int, [VP, ctypes.c_uint]),
+    "spk_profile_reset": (ctypes.c_int, [VP]),
+    "spk_profile_read": (ctypes.c_int, [VP, ctypes.c_int, PD, P64, PD, PD]),
     "spk_last_error": (ctypes.c_char_p, [VP]),
     "spk_destroy": (None, [VP]),
 }
 
 SPK_OK, SPK_EARG, SPK_ECUDA, SPK_ENOMEM, SPK_ESEQ, SPK_ESTRUCT, SPK_ESINGULAR, SPK_ENOCONV = 0, -1, -2, -3, -4, -5, -6, -7
 SPK_HOST, SPK_DEVICE = 0, 1
+KERNEL_CLASSES = ["assemble", "getrf", "panel", "trail", "schur", "fwd", "bwd", "permute", "residual"]
 SPK_FP64, SPK_FP32 = 0, 1
 
 _lock = threading.Lock()

@@ -176,3 +176,25 @@ class NumericEngine:
         self._check(self._lib.spk_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(f)),
                     "spk_stats")
         return {"fronts": a.value, "levels": b.value, "factor_entries": c.value, "lu_flops": f.value}
+
+    # -- launch accounting ----------------------------------------------------
+    def profile(self, classes=()):
+        """Time the listed kernel classes (names of _native.KERNEL_CLASSES) with CUDA events."""
+        mask = 0
+        for c in classes:
+            mask |= 1 << N.KERNEL_CLASSES.index(c)
+        self._check(self._lib.spk_profile(self._h, mask), "spk_profile")
+
+    def profile_reset(self):
+        self._check(self._lib.spk_profile_reset(self._h), "spk_profile_reset")
+
+    def profile_read(self):
+        """{class: {ms, launches, flops, bytes}} since the last reset."""
+        out = {}
+        for k, name in enumerate(N.KERNEL_CLASSES):
+            ms, fl, by = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+            la = ctypes.c_int64()
+            self._check(self._lib.spk_profile_read(self._h, k, ctypes.byref(ms), ctypes.byref(la), ctypes.byref(fl),
+                                                   ctypes.byref(by)), "spk_profile_read")
+            out[name] = {"ms": ms.value, "launches": la.value, "flops": fl.value, "bytes": by.value}
+        return out
