@@ -46,9 +46,29 @@ struct Timed {
     int kind;
 };
 
+// Launches of one elimination-tree level: per block step t the block LU,
+// panel and trailing kernels; then the Schur complements; for the solves
+// the forward block steps, and backward the U12 product and block steps.
 struct LevelPlan {
-    LaunchRec getrf0, schur, bwdu;
-    std::vector<LaunchRec> panel, trail, fwd, bwd;
+    LaunchRec schur, bwdu;
+    std::vector<LaunchRec> blu, bpanel, btrail, fwd, bwd;
+};
+
+// Block partition and schedule for one precision (block width BlockMax<T>).
+struct Plan {
+    bool built = false;
+    int bmax = 0, bwmax = 1;
+    std::vector<int> blk_c0, blk_c1, blk_p0, blk_np;
+    std::vector<ll> blk_inv;
+    ll inv_size = 0;
+    std::vector<int> block0, nblocks;     // per front
+    std::vector<LevelPlan> levels;
+    std::vector<int> sched_ids, sched_prefix;
+    spk::DFront* d_fronts = nullptr;
+    int *d_blk_c0 = nullptr, *d_blk_c1 = nullptr, *d_blk_p0 = nullptr, *d_blk_np = nullptr;
+    ll* d_blk_inv = nullptr;
+    int *d_sched_ids = nullptr, *d_sched_prefix = nullptr;
+    spk::Sched sched{};
 };
 
 struct HFront {
@@ -61,6 +81,7 @@ struct HFront {
 template <typename T>
 struct Storage {
     T* d = nullptr;
+    T* inv = nullptr;       // Minv / Uinv of every block
     bool loaded = false;    // values assembled since the last factor
     bool factored = false;
 };
@@ -80,22 +101,19 @@ struct spk_handle {
     std::vector<int> runid, run_tgt, run_start;
     std::vector<ll> run_rel;
     std::vector<int> rel;
-    std::vector<LevelPlan> levels;
-    std::vector<int> sched_ids, sched_prefix;
+    Plan plan[2];                   // [0] FP64, [1] FP32
+    int nlevels = 0;
     i64 fsize = 0;
     int wmax = 1;             // widest supernode
     double amalgamation = 0.1;  // allowed relative padding of a front
     double lu_flops = 0.0;
 
-    // device structure
-    spk::DFront* d_fronts = nullptr;
+    // device structure shared by both plans
     int *d_xs = nullptr, *d_rows = nullptr, *d_runid = nullptr, *d_run_tgt = nullptr, *d_run_start = nullptr,
         *d_rel = nullptr;
     ll* d_run_rel = nullptr;
-    int *d_sched_ids = nullptr, *d_sched_prefix = nullptr;
     int* d_ipiv = nullptr;
     int* d_info = nullptr;
-    spk::Sched sched{};
 
     // pattern and values
     bool have_pattern = false, have_values = false;
@@ -161,13 +179,16 @@ static int upload(spk_handle* h, T** dst, const std::vector<T>& src) {
     return SPK_OK;
 }
 
-static spk::Launch launch_of(const spk_handle* h, const LaunchRec& r) {
+static spk::Launch launch_of(const Plan& P, const LaunchRec& r) {
     spk::Launch L;
-    L.front_ids = h->d_sched_ids + r.off;
-    L.prefix = h->d_sched_prefix + r.poff;
+    L.front_ids = P.d_sched_ids + r.off;
+    L.prefix = P.d_sched_prefix + r.poff;
     L.count = r.count;
     return L;
 }
+
+template <typename T>
+static constexpr int prec_index() { return std::is_same<T, float>::value ? 1 : 0; }
 
 static cudaEvent_t take_event(spk_handle* h) {
     if (!h->event_pool.empty()) {
@@ -400,6 +421,8 @@ static int analyse(spk_handle* h, const int64_t* xsuper, const int64_t* snode, c
         if (h->fronts[i].parent >= 0)
             h->fronts[h->fronts[i].parent].level =
                 std::max(h->fronts[h->fronts[i].parent].level, h->fronts[i].level + 1);
+    h->nlevels = 0;
+    for (int i = 0; i < nfr; ++i) h->nlevels = std::max(h->nlevels, h->fronts[i].level + 1);
     // runs and relative positions
     h->runid.clear();
     h->run_tgt.clear();
@@ -443,7 +466,7 @@ static int analyse(spk_handle* h, const int64_t* xsuper, const int64_t* snode, c
     return SPK_OK;
 }
 
-static void add_launch(spk_handle* h, LaunchRec& rec, const std::vector<int>& ids, const std::vector<int>& tiles,
+static void add_launch(Plan* h, LaunchRec& rec, const std::vector<int>& ids, const std::vector<int>& tiles,
                        const std::vector<double>& flops, const std::vector<double>& words) {
     rec.off = (i64)h->sched_ids.size();
     rec.poff = (i64)h->sched_prefix.size();
@@ -463,71 +486,89 @@ static void add_launch(spk_handle* h, LaunchRec& rec, const std::vector<int>& id
     rec.tiles = acc;
 }
 
-static void build_schedule(spk_handle* h) {
+// Group each front's pieces into blocks of at most `bmax` columns and lay
+// out the launches of every level.
+static void build_plan(const spk_handle* h, Plan& P, int bmax) {
     using spk::cdiv;
-    int nlev = 0;
-    for (auto& F : h->fronts) nlev = std::max(nlev, F.level + 1);
-    std::vector<std::vector<int>> at(nlev);
-    for (int i = 0; i < (int)h->fronts.size(); ++i) at[h->fronts[i].level].push_back(i);
-    h->levels.assign(nlev, LevelPlan());
-    h->sched_ids.clear();
-    h->sched_prefix.clear();
-    for (int l = 0; l < nlev; ++l) {
-        LevelPlan& P = h->levels[l];
-        const std::vector<int>& ids = at[l];
-        int maxp = 0;
-        for (int id : ids) maxp = std::max(maxp, h->fronts[id].npieces);
-        const size_t nid = ids.size();
-        std::vector<int> t(nid, 1);
-        std::vector<double> fl(nid), wd(nid);
-        for (size_t k = 0; k < nid; ++k) {
-            const HFront& F = h->fronts[ids[k]];
-            double w = h->xs[F.piece0 + 1] - h->xs[F.piece0];
-            fl[k] = 2.0 / 3.0 * w * w * w;
-            wd[k] = 2.0 * w * w;
+    P = Plan();
+    P.bmax = bmax;
+    const int nfr = (int)h->fronts.size();
+    P.block0.resize(nfr);
+    P.nblocks.resize(nfr);
+    ll inv = 0;
+    for (int i = 0; i < nfr; ++i) {
+        const HFront& F = h->fronts[i];
+        P.block0[i] = (int)P.blk_c0.size();
+        int s = F.piece0;
+        const int e = F.piece0 + F.npieces;
+        while (s < e) {
+            int t = s + 1;
+            while (t < e && h->xs[t + 1] - h->xs[s] <= bmax) ++t;
+            const int c0 = h->xs[s] - (int)F.f, c1 = h->xs[t] - (int)F.f, bw = c1 - c0;
+            P.blk_c0.push_back(c0);
+            P.blk_c1.push_back(c1);
+            P.blk_p0.push_back(s);
+            P.blk_np.push_back(t - s);
+            P.blk_inv.push_back(inv);
+            inv += 2 * (ll)bw * bw;
+            P.bwmax = std::max(P.bwmax, bw);
+            s = t;
         }
-        add_launch(h, P.getrf0, ids, t, fl, wd);
-        P.panel.resize(maxp);
-        P.trail.resize(maxp);
-        P.fwd.resize(maxp);
-        P.bwd.resize(maxp);
-        for (int s = 0; s < maxp; ++s) {
-            std::vector<int> tp(nid), tt(nid), tf(nid), tb(nid);
-            std::vector<double> fp(nid), wp(nid), ft(nid), wt(nid), ff(nid), wf(nid), fb(nid), wb(nid);
+        P.nblocks[i] = (int)P.blk_c0.size() - P.block0[i];
+    }
+    P.inv_size = inv;
+    const int nlev = h->nlevels;
+    std::vector<std::vector<int>> at(nlev);
+    for (int i = 0; i < nfr; ++i) at[h->fronts[i].level].push_back(i);
+    P.levels.assign(nlev, LevelPlan());
+    for (int l = 0; l < nlev; ++l) {
+        LevelPlan& L = P.levels[l];
+        const std::vector<int>& ids = at[l];
+        const size_t nid = ids.size();
+        int maxb = 0;
+        for (int id : ids) maxb = std::max(maxb, P.nblocks[id]);
+        L.blu.resize(maxb);
+        L.bpanel.resize(maxb);
+        L.btrail.resize(maxb);
+        L.fwd.resize(maxb);
+        L.bwd.resize(maxb);
+        for (int t = 0; t < maxb; ++t) {
+            std::vector<int> tl(nid), tp(nid), tt(nid), tf(nid), tb(nid);
+            std::vector<double> fl(nid), wl(nid), fp(nid), wp(nid), ft(nid), wt(nid), ff(nid), wf(nid), fb(nid), wb(nid);
             for (size_t k = 0; k < nid; ++k) {
                 const HFront& F = h->fronts[ids[k]];
-                if (s >= F.npieces) { tp[k] = tt[k] = tf[k] = tb[k] = 0; continue; }
-                int p = F.piece0 + s;
-                int p1 = h->xs[p + 1] - (int)F.f;
-                double w = h->xs[p + 1] - h->xs[p];
-                int ld = F.nf + F.m;
-                tp[k] = cdiv(ld - p1, spk::TP) + cdiv(F.nf - p1, spk::TP) + cdiv(F.m, spk::TP);
-                tt[k] = cdiv(ld - p1, spk::TT) * cdiv(F.nf - p1, spk::TT) + cdiv(F.nf - p1, spk::TT) * cdiv(F.m, spk::TT);
-                tf[k] = std::max(1, cdiv(ld - p1, spk::TS));
-                double panel_vecs = (double)(ld - p1) + (double)(F.nf - p1) + F.m;
-                fp[k] = w * w * panel_vecs;
-                wp[k] = 2.0 * w * panel_vecs + w * w;
-                double area = (double)(ld - p1) * (F.nf - p1) + (double)(F.nf - p1) * F.m;
-                ft[k] = 2.0 * w * area;
-                wt[k] = 2.0 * area + w * panel_vecs;
-                if (s + 1 < F.npieces) {
-                    double w2 = h->xs[p + 2] - h->xs[p + 1];
-                    ft[k] += 2.0 / 3.0 * w2 * w2 * w2;
-                    wt[k] += 2.0 * w2 * w2;
-                }
-                ff[k] = w * w + 2.0 * w * (ld - p1);
-                wf[k] = w * w + w * (ld - p1);
-                int q = F.piece0 + F.npieces - 1 - s;
-                int q0 = h->xs[q] - (int)F.f;
-                double wq = h->xs[q + 1] - h->xs[q];
-                tb[k] = std::max(1, cdiv(q0, spk::TS));
-                fb[k] = wq * wq + 2.0 * wq * q0;
-                wb[k] = wq * wq + wq * q0;
+                const int nb = P.nblocks[ids[k]];
+                if (t >= nb) { tl[k] = tp[k] = tt[k] = tf[k] = tb[k] = 0; continue; }
+                const int blk = P.block0[ids[k]] + t;
+                const int c0 = P.blk_c0[blk], c1 = P.blk_c1[blk];
+                const double bw = c1 - c0;
+                const int ld = F.nf + F.m;
+                tl[k] = 1;
+                fl[k] = 2.0 * bw * bw * bw;
+                wl[k] = 4.0 * bw * bw;
+                tp[k] = cdiv(ld - c1, 64) + cdiv(F.nf - c1, 64) + cdiv(F.m, 64);
+                const double rowsL = ld - c1, colsU = (double)(F.nf - c1) + F.m;
+                fp[k] = bw * bw * rowsL + 2.0 * bw * bw * colsU;
+                wp[k] = 2.0 * bw * (rowsL + colsU) + 2.0 * bw * bw;
+                tt[k] = cdiv(ld - c1, spk::TT) * cdiv(F.nf - c1, spk::TT) + cdiv(F.nf - c1, spk::TT) * cdiv(F.m, spk::TT);
+                const double area = (double)(ld - c1) * (F.nf - c1) + (double)(F.nf - c1) * F.m;
+                ft[k] = 2.0 * bw * area;
+                wt[k] = 2.0 * area + bw * (rowsL + colsU);
+                tf[k] = std::max(1, cdiv(ld - c1, spk::TS));
+                ff[k] = 2.0 * bw * bw + 2.0 * bw * rowsL;
+                wf[k] = bw * bw + bw * rowsL;
+                const int rb = P.block0[ids[k]] + nb - 1 - t;
+                const int r0 = P.blk_c0[rb];
+                const double rbw = P.blk_c1[rb] - r0;
+                tb[k] = std::max(1, cdiv(r0, spk::TS));
+                fb[k] = rbw * rbw + 2.0 * rbw * r0;
+                wb[k] = 0.5 * rbw * rbw + rbw * r0;
             }
-            add_launch(h, P.panel[s], ids, tp, fp, wp);
-            add_launch(h, P.trail[s], ids, tt, ft, wt);
-            add_launch(h, P.fwd[s], ids, tf, ff, wf);
-            add_launch(h, P.bwd[s], ids, tb, fb, wb);
+            add_launch(&P, L.blu[t], ids, tl, fl, wl);
+            add_launch(&P, L.bpanel[t], ids, tp, fp, wp);
+            add_launch(&P, L.btrail[t], ids, tt, ft, wt);
+            add_launch(&P, L.fwd[t], ids, tf, ff, wf);
+            add_launch(&P, L.bwd[t], ids, tb, fb, wb);
         }
         std::vector<int> tsch(nid), tbu(nid);
         std::vector<double> fs(nid), ws(nid), fu(nid), wu(nid);
@@ -540,12 +581,35 @@ static void build_schedule(spk_handle* h) {
             fu[k] = 2.0 * (double)F.m * F.nf;
             wu[k] = (double)F.m * F.nf;
         }
-        add_launch(h, P.schur, ids, tsch, fs, ws);
-        add_launch(h, P.bwdu, ids, tbu, fu, wu);
+        add_launch(&P, L.schur, ids, tsch, fs, ws);
+        add_launch(&P, L.bwdu, ids, tbu, fu, wu);
     }
 }
 
 static int upload_structure(spk_handle* h) {
+    int rc;
+    if ((rc = upload(h, &h->d_xs, h->xs))) return rc;
+    if ((rc = upload(h, &h->d_rows, h->rows))) return rc;
+    if ((rc = upload(h, &h->d_runid, h->runid))) return rc;
+    if ((rc = upload(h, &h->d_run_tgt, h->run_tgt))) return rc;
+    if ((rc = upload(h, &h->d_run_start, h->run_start))) return rc;
+    if ((rc = upload(h, &h->d_run_rel, h->run_rel))) return rc;
+    if ((rc = upload(h, &h->d_rel, h->rel))) return rc;
+    CU(h, cudaMalloc((void**)&h->d_ipiv, sizeof(int) * std::max<i64>(h->n, 1)));
+    CU(h, cudaMalloc((void**)&h->d_info, sizeof(int)));
+    return SPK_OK;
+}
+
+// Build (once) and upload the plan of precision T.
+template <typename T>
+static int ensure_plan(spk_handle* h) {
+    Plan& P = h->plan[prec_index<T>()];
+    if (P.built) return SPK_OK;
+    try {
+        build_plan(h, P, spk::BlockMax<T>::value);
+    } catch (const std::bad_alloc&) {
+        return set_err(h, SPK_ENOMEM, "host allocation failed while planning");
+    }
     std::vector<spk::DFront> df(h->fronts.size());
     for (size_t i = 0; i < h->fronts.size(); ++i) {
         const HFront& F = h->fronts[i];
@@ -561,30 +625,48 @@ static int upload_structure(spk_handle* h) {
         d.piece0 = F.piece0;
         d.npieces = F.npieces;
         d.run0 = F.run0;
+        d.block0 = P.block0[i];
+        d.nblocks = P.nblocks[i];
         d.pad = 0;
     }
     int rc;
-    if ((rc = upload(h, &h->d_fronts, df))) return rc;
-    if ((rc = upload(h, &h->d_xs, h->xs))) return rc;
-    if ((rc = upload(h, &h->d_rows, h->rows))) return rc;
-    if ((rc = upload(h, &h->d_runid, h->runid))) return rc;
-    if ((rc = upload(h, &h->d_run_tgt, h->run_tgt))) return rc;
-    if ((rc = upload(h, &h->d_run_start, h->run_start))) return rc;
-    if ((rc = upload(h, &h->d_run_rel, h->run_rel))) return rc;
-    if ((rc = upload(h, &h->d_rel, h->rel))) return rc;
-    if ((rc = upload(h, &h->d_sched_ids, h->sched_ids))) return rc;
-    if ((rc = upload(h, &h->d_sched_prefix, h->sched_prefix))) return rc;
-    CU(h, cudaMalloc((void**)&h->d_ipiv, sizeof(int) * std::max<i64>(h->n, 1)));
-    CU(h, cudaMalloc((void**)&h->d_info, sizeof(int)));
-    h->sched.fronts = h->d_fronts;
-    h->sched.xsuper = h->d_xs;
-    h->sched.rows = h->d_rows;
-    h->sched.runid = h->d_runid;
-    h->sched.run_tgt = h->d_run_tgt;
-    h->sched.run_start = h->d_run_start;
-    h->sched.run_rel = h->d_run_rel;
-    h->sched.rel = h->d_rel;
+    if ((rc = upload(h, &P.d_fronts, df))) return rc;
+    if ((rc = upload(h, &P.d_blk_c0, P.blk_c0))) return rc;
+    if ((rc = upload(h, &P.d_blk_c1, P.blk_c1))) return rc;
+    if ((rc = upload(h, &P.d_blk_p0, P.blk_p0))) return rc;
+    if ((rc = upload(h, &P.d_blk_np, P.blk_np))) return rc;
+    if ((rc = upload(h, &P.d_blk_inv, P.blk_inv))) return rc;
+    if ((rc = upload(h, &P.d_sched_ids, P.sched_ids))) return rc;
+    if ((rc = upload(h, &P.d_sched_prefix, P.sched_prefix))) return rc;
+    spk::Sched& S = P.sched;
+    S.fronts = P.d_fronts;
+    S.xsuper = h->d_xs;
+    S.rows = h->d_rows;
+    S.runid = h->d_runid;
+    S.run_tgt = h->d_run_tgt;
+    S.run_start = h->d_run_start;
+    S.run_rel = h->d_run_rel;
+    S.rel = h->d_rel;
+    S.blk_c0 = P.d_blk_c0;
+    S.blk_c1 = P.d_blk_c1;
+    S.blk_p0 = P.d_blk_p0;
+    S.blk_np = P.d_blk_np;
+    S.blk_inv = P.d_blk_inv;
+    const int bw = P.bwmax;
+    CU(h, cudaFuncSetAttribute(spk::k_block_lu<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(sizeof(T) * 3 * bw * (bw + 1) + sizeof(int) * 2 * (spk::BlockMax<T>::value + 1))));
+    CU(h, cudaFuncSetAttribute(spk::k_block_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(sizeof(T) * (64 + bw) * bw)));
+    P.built = true;
     return SPK_OK;
+}
+
+static void free_plan(Plan& P) {
+    void* ptrs[] = {P.d_fronts, P.d_blk_c0, P.d_blk_c1, P.d_blk_p0, P.d_blk_np, P.d_blk_inv, P.d_sched_ids,
+                    P.d_sched_prefix};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    P = Plan();
 }
 
 template <typename T>
@@ -596,8 +678,11 @@ Storage<float>& storage<float>(spk_handle* h) { return h->s32; }
 
 template <typename T>
 static int ensure_storage(spk_handle* h) {
+    int rc = ensure_plan<T>(h);
+    if (rc) return rc;
     Storage<T>& S = storage<T>(h);
     if (!S.d) CU(h, cudaMalloc((void**)&S.d, sizeof(T) * std::max<i64>(h->fsize, 1)));
+    if (!S.inv) CU(h, cudaMalloc((void**)&S.inv, sizeof(T) * std::max<ll>(h->plan[prec_index<T>()].inv_size, 1)));
     return SPK_OK;
 }
 
@@ -627,35 +712,35 @@ static int ensure_rhs(spk_handle* h, i64 nrhs) {
 // numeric phases
 // ---------------------------------------------------------------------------
 template <typename T>
-static size_t panel_smem(const spk_handle* h) {
-    return sizeof(T) * (size_t)(h->wmax * h->wmax + h->wmax * spk::TP) + sizeof(int) * spk::MAXW;
-}
-
-template <typename T>
 static int factor_launches(spk_handle* h) {
     T* fac = storage<T>(h).d;
-    const size_t psmem = panel_smem<T>(h);
-    for (const LevelPlan& P : h->levels) {
-        if (P.getrf0.tiles > 0) {
-            LaunchScope ls(h, SPK_K_GETRF, P.getrf0.flops, P.getrf0.words * sizeof(T));
-            spk::k_getrf_first<T><<<P.getrf0.tiles, 128, 0, h->stream>>>(fac, h->d_ipiv, h->d_info, h->sched,
-                                                                            launch_of(h, P.getrf0));
-        }
-        for (size_t s = 0; s < P.panel.size(); ++s) {
-            if (P.panel[s].tiles > 0) {
-                LaunchScope ls(h, SPK_K_PANEL, P.panel[s].flops, P.panel[s].words * sizeof(T));
-                spk::k_panel<T><<<P.panel[s].tiles, spk::TP, psmem, h->stream>>>(
-                    fac, h->d_ipiv, h->sched, launch_of(h, P.panel[s]), (int)s, h->wmax);
+    T* inv = storage<T>(h).inv;
+    const Plan& PL = h->plan[prec_index<T>()];
+    const spk::Sched& S = PL.sched;
+    const int bw = PL.bwmax;
+    const size_t lu_smem = sizeof(T) * 3 * bw * (bw + 1) + sizeof(int) * 2 * (spk::BlockMax<T>::value + 1);
+    const size_t panel_smem = sizeof(T) * (64 + bw) * bw;
+    for (const LevelPlan& P : PL.levels) {
+        for (size_t t = 0; t < P.blu.size(); ++t) {
+            if (P.blu[t].tiles > 0) {
+                LaunchScope ls(h, SPK_K_GETRF, P.blu[t].flops, P.blu[t].words * sizeof(T));
+                spk::k_block_lu<T><<<P.blu[t].tiles, 128, lu_smem, h->stream>>>(fac, h->d_ipiv, h->d_info, inv, S,
+                                                                                 launch_of(PL, P.blu[t]), (int)t, bw);
             }
-            if (P.trail[s].tiles > 0) {
-                LaunchScope ls(h, SPK_K_TRAIL, P.trail[s].flops, P.trail[s].words * sizeof(T));
-                spk::k_trail<T><<<P.trail[s].tiles, 256, 0, h->stream>>>(fac, h->d_ipiv, h->d_info, h->sched,
-                                                                           launch_of(h, P.trail[s]), (int)s);
+            if (P.bpanel[t].tiles > 0) {
+                LaunchScope ls(h, SPK_K_PANEL, P.bpanel[t].flops, P.bpanel[t].words * sizeof(T));
+                spk::k_block_panel<T><<<P.bpanel[t].tiles, 256, panel_smem, h->stream>>>(
+                    fac, inv, S, launch_of(PL, P.bpanel[t]), (int)t, bw);
+            }
+            if (P.btrail[t].tiles > 0) {
+                LaunchScope ls(h, SPK_K_TRAIL, P.btrail[t].flops, P.btrail[t].words * sizeof(T));
+                spk::k_block_trail<T><<<P.btrail[t].tiles, 256, 0, h->stream>>>(fac, S, launch_of(PL, P.btrail[t]),
+                                                                                 (int)t);
             }
         }
         if (P.schur.tiles > 0) {
             LaunchScope ls(h, SPK_K_SCHUR, P.schur.flops, P.schur.words * sizeof(T));
-            spk::k_schur<T><<<P.schur.tiles, 256, 0, h->stream>>>(fac, h->sched, launch_of(h, P.schur));
+            spk::k_schur<T><<<P.schur.tiles, 256, 0, h->stream>>>(fac, S, launch_of(PL, P.schur));
         }
     }
     CU(h, cudaGetLastError());
@@ -665,38 +750,39 @@ static int factor_launches(spk_handle* h) {
 template <typename T>
 static int run_factor(spk_handle* h) {
     const int big = INT_MAX;
-    CU(h, cudaFuncSetAttribute(spk::k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem<T>(h)));
     CU(h, cudaMemcpyAsync(h->d_info, &big, sizeof(int), cudaMemcpyHostToDevice, h->stream));
-    return via_graph(h, h->g_factor[std::is_same<T, float>::value ? 1 : 0], [&] { return factor_launches<T>(h); });
+    return via_graph(h, h->g_factor[prec_index<T>()], [&] { return factor_launches<T>(h); });
 }
 
 // Solve in place on the permuted work vectors: wb (rhs, consumed) -> wx.
 template <typename T>
 static int run_solve_permuted(spk_handle* h, int nrhs) {
     const T* fac = storage<T>(h).d;
+    const T* inv = storage<T>(h).inv;
+    const Plan& PL = h->plan[prec_index<T>()];
+    const spk::Sched& S = PL.sched;
     T* b = (T*)h->d_wb;
     T* y = (T*)h->d_wy;
     T* x = (T*)h->d_wx;
     const int n = (int)h->n;
-    for (const LevelPlan& P : h->levels)
-        for (size_t s = 0; s < P.fwd.size(); ++s)
-            if (P.fwd[s].tiles > 0) {
-                LaunchScope ls(h, SPK_K_FWD, P.fwd[s].flops * nrhs, P.fwd[s].words * sizeof(T));
-                spk::k_fwd<T><<<P.fwd[s].tiles, spk::TS, 0, h->stream>>>(fac, h->d_ipiv, b, y, n, nrhs, h->sched,
-                                                                          launch_of(h, P.fwd[s]), (int)s);
+    for (const LevelPlan& P : PL.levels)
+        for (size_t t = 0; t < P.fwd.size(); ++t)
+            if (P.fwd[t].tiles > 0) {
+                LaunchScope ls(h, SPK_K_FWD, P.fwd[t].flops * nrhs, P.fwd[t].words * sizeof(T));
+                spk::k_fwd<T><<<P.fwd[t].tiles, spk::TS, 0, h->stream>>>(fac, inv, b, y, n, nrhs, S,
+                                                                          launch_of(PL, P.fwd[t]), (int)t);
             }
-    for (size_t l = h->levels.size(); l-- > 0;) {
-        const LevelPlan& P = h->levels[l];
+    for (size_t l = PL.levels.size(); l-- > 0;) {
+        const LevelPlan& P = PL.levels[l];
         if (P.bwdu.tiles > 0) {
             LaunchScope ls(h, SPK_K_BWD, P.bwdu.flops * nrhs, P.bwdu.words * sizeof(T));
-            spk::k_bwd_u12<T><<<P.bwdu.tiles, spk::TS, 0, h->stream>>>(fac, y, x, n, nrhs, h->sched,
-                                                                        launch_of(h, P.bwdu));
+            spk::k_bwd_u12<T><<<P.bwdu.tiles, spk::TS, 0, h->stream>>>(fac, y, x, n, nrhs, S, launch_of(PL, P.bwdu));
         }
-        for (size_t s = 0; s < P.bwd.size(); ++s)
-            if (P.bwd[s].tiles > 0) {
-                LaunchScope ls(h, SPK_K_BWD, P.bwd[s].flops * nrhs, P.bwd[s].words * sizeof(T));
-                spk::k_bwd<T><<<P.bwd[s].tiles, spk::TS, 0, h->stream>>>(fac, y, x, n, nrhs, h->sched,
-                                                                          launch_of(h, P.bwd[s]), (int)s);
+        for (size_t t = 0; t < P.bwd.size(); ++t)
+            if (P.bwd[t].tiles > 0) {
+                LaunchScope ls(h, SPK_K_BWD, P.bwd[t].flops * nrhs, P.bwd[t].words * sizeof(T));
+                spk::k_bwd<T><<<P.bwd[t].tiles, spk::TS, 0, h->stream>>>(fac, inv, y, x, n, nrhs, S,
+                                                                          launch_of(PL, P.bwd[t]), (int)t);
             }
     }
     CU(h, cudaGetLastError());
@@ -716,7 +802,7 @@ static int solve_device(spk_handle* h, const double* rhs, i64 ldr, double* x, i6
             spk::k_permute<double, T><<<blocks, 256, 0, h->stream>>>(rhs + c0 * ldr, ldr, (T*)h->d_wb, n, h->d_rperm,
                                                                      n, nc);
         }
-        int rc = via_graph(h, h->g_solve[std::is_same<T, float>::value ? 1 : 0][nc],
+        int rc = via_graph(h, h->g_solve[prec_index<T>()][nc],
                            [&] { return run_solve_permuted<T>(h, nc); });
         if (rc) return rc;
         {
@@ -833,7 +919,7 @@ int spk_create(int64_t n, int64_t nsuper, const int64_t* xsuper, const int64_t* 
     int rc;
     try {
         rc = analyse(h, xsuper, snode, xlindx, lindx, xlnz, xunz, index_base);
-        if (rc == SPK_OK) build_schedule(h);
+
     } catch (const std::bad_alloc&) {
         rc = set_err(h, SPK_ENOMEM, "host allocation failed while analysing the structure");
     }
@@ -1156,7 +1242,7 @@ int spk_get_factors(spk_handle* h, int precision, double* lnz, double* unz, int6
 int spk_stats(spk_handle* h, int64_t* nfronts, int64_t* nlevels, int64_t* factor_entries, double* lu_flops) {
     if (!h) return SPK_EARG;
     if (nfronts) *nfronts = (int64_t)h->fronts.size();
-    if (nlevels) *nlevels = (int64_t)h->levels.size();
+    if (nlevels) *nlevels = (int64_t)h->nlevels;
     if (factor_entries) *factor_entries = h->fsize;
     if (lu_flops) *lu_flops = h->lu_flops;
     return SPK_OK;
@@ -1198,8 +1284,10 @@ void spk_destroy(spk_handle* h) {
     if (!h) return;
     if (h->device >= 0) cudaSetDevice(h->device);
     if (h->own) cudaStreamSynchronize(h->own);
-    void* ptrs[] = {h->d_fronts, h->d_xs, h->d_rows, h->d_runid, h->d_run_tgt, h->d_run_start, h->d_run_rel,
-                    h->d_rel, h->d_sched_ids, h->d_sched_prefix, h->d_ipiv, h->d_info, h->d_slot, h->d_aval,
+    free_plan(h->plan[0]);
+    free_plan(h->plan[1]);
+    void* ptrs[] = {h->d_xs, h->d_rows, h->d_runid, h->d_run_tgt, h->d_run_start, h->d_run_rel,
+                    h->d_rel, h->s64.inv, h->s32.inv, h->d_ipiv, h->d_info, h->d_slot, h->d_aval,
                     h->d_rowptr, h->d_col, h->d_src, h->d_rperm, h->d_rinvp, h->s64.d, h->s32.d, h->d_wb,
                     h->d_wy, h->d_wx, h->d_rhs, h->d_x, h->d_r, h->d_sums};
     for (void* p : ptrs)

@@ -45,6 +45,8 @@ struct DFront {
     int piece0;    // first supernode (0-based) of the front
     int npieces;
     int run0;      // first run of the front in run_*[]
+    int block0;    // first block of the front (in the plan's block arrays)
+    int nblocks;
     int pad;
 };
 
@@ -60,6 +62,11 @@ struct Sched {
     const int* run_start;  // first row (local to R_F) of each run
     const ll* run_rel;     // offset in rel[] of the run's first row
     const int* rel;
+    const int* blk_c0;     // front-local first column of each block
+    const int* blk_c1;     // front-local end column of each block
+    const int* blk_p0;     // first supernode (0-based) of each block
+    const int* blk_np;     // supernodes in the block
+    const ll* blk_inv;     // offset in inv[] of the block's Minv (then Uinv)
 };
 
 // One launch = a list of fronts and the prefix sum of their tile counts.
@@ -89,184 +96,193 @@ template <typename T> __device__ __forceinline__ T tabs(T x) { return x < T(0) ?
 constexpr int MAXW = 64;
 
 // ---------------------------------------------------------------------------
-// In-block partial pivoting LU of a w x w block held in shared memory
-// (column-major, leading dimension w, w <= MAXW).  Pivot = first row with the
-// strictly largest |a| (ggetrf!, src/Utilities/GenericBlasLapackFragments.jl:
-// 56-100): NaN never wins, except a NaN on the diagonal, which keeps k; a
-// zero pivot skips the interchange and the scaling and sets *sing.
-// piv[k] receives the 0-based local pivot row.
+// Blocks.  The pieces of a front are processed in *blocks* of consecutive
+// pieces (at most BlockMax<T> columns).  k_block_lu factors a block in
+// shared memory piece by piece with exactly the reference's in-block
+// pivoting (ggetrf! on the piece's diagonal block, _luswap! of the piece's U
+// rows, the two _trsm! panels), and also forms two explicit inverses:
+//   Uinv = U_BB^{-1}  (upper triangle of the factored block), and
+//   Minv = the block's forward operator: applying it to a vector performs,
+//          piece by piece, "subtract the earlier pieces' L columns, apply
+//          the piece's interchanges, unit-lower solve" - the reference's
+//          _lulsolve! steps restricted to the block.
+// The L panel below the block is then X * Uinv, the U panel to its right is
+// Minv * Y, and the block steps of both triangular solves are Minv * b and
+// Uinv * c: small dense products instead of serial substitutions.
 // ---------------------------------------------------------------------------
+template <typename T> struct BlockMax;
+template <> struct BlockMax<float> { static constexpr int value = 128; };
+template <> struct BlockMax<double> { static constexpr int value = 64; };
+
+// Factor the bw x bw block A (shared, column-major, leading dimension lda,
+// odd so that one-thread-per-column loops do not collide on banks).  Pieces
+// start at local columns q0[0] < q0[1] < ... < q0[np] = bw.  piv[c] receives
+// the 0-based pivot row of column c local to its piece; *sing is set on a
+// zero pivot.
 template <typename T>
-__device__ void block_getrf(T* A, int w, int* piv, int* sing) {
+__device__ void block_lu(T* A, int bw, int lda, const int* q0, int np, int* piv, int* sing) {
     const int tid = threadIdx.x, nt = blockDim.x;
-    for (int k = 0; k < w; ++k) {
-        if (tid < 32) {
-            double key = -1.0;
-            int idx = w;
-            for (int i = k + tid; i < w; i += 32) {   // first strict maximum among this lane's rows
-                double a = (double)tabs(A[k * w + i]);
-                double ki = (a != a) ? ((i == k) ? __longlong_as_double(0x7ff0000000000000LL) : -1.0) : a;
-                if (ki > key || idx == w) { key = ki; idx = i; }
-            }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                double k2 = __shfl_down_sync(0xffffffffu, key, off);
-                int i2 = __shfl_down_sync(0xffffffffu, idx, off);
-                if (k2 > key || (k2 == key && i2 < idx)) { key = k2; idx = i2; }
-            }
-            if (tid == 0) piv[k] = idx;
-        }
-        __syncthreads();
-        const int kp = piv[k];
-        const bool nz = A[k * w + kp] != T(0);
-        if (nz) {
-            if (kp != k)
-                for (int j = tid; j < w; j += nt) {
-                    T t = A[j * w + k];
-                    A[j * w + k] = A[j * w + kp];
-                    A[j * w + kp] = t;
+    for (int pc = 0; pc < np; ++pc) {
+        const int a = q0[pc], b = q0[pc + 1];
+        // ggetrf! on the piece's diagonal block: pivots among the piece's rows only
+        for (int k = a; k < b; ++k) {
+            if (tid < 32) {
+                double key = -1.0;
+                int idx = b;
+                for (int i = k + tid; i < b; i += 32) {
+                    double v = (double)tabs(A[k * lda + i]);
+                    double ki = (v != v) ? ((i == k) ? __longlong_as_double(0x7ff0000000000000LL) : -1.0) : v;
+                    if (ki > key || idx == b) { key = ki; idx = i; }
                 }
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    double k2 = __shfl_down_sync(0xffffffffu, key, off);
+                    int i2 = __shfl_down_sync(0xffffffffu, idx, off);
+                    if (k2 > key || (k2 == key && i2 < idx)) { key = k2; idx = i2; }
+                }
+                if (tid == 0) piv[k] = idx - a;
+            }
             __syncthreads();
-            const T inv = T(1) / A[k * w + k];
-            for (int i = k + 1 + tid; i < w; i += nt) A[k * w + i] *= inv;
-        } else if (tid == 0) {
-            *sing = 1;
+            const int kp = a + piv[k];
+            const bool nz = A[k * lda + kp] != T(0);
+            if (nz) {
+                if (kp != k)
+                    for (int j = a + tid; j < b; j += nt) {
+                        T t = A[j * lda + k];
+                        A[j * lda + k] = A[j * lda + kp];
+                        A[j * lda + kp] = t;
+                    }
+                __syncthreads();
+                const T inv = T(1) / A[k * lda + k];
+                for (int i = k + 1 + tid; i < b; i += nt) A[k * lda + i] *= inv;
+            } else if (tid == 0) {
+                *sing = 1;
+            }
+            __syncthreads();
+            const int r = b - k - 1;
+            for (int e = tid; e < r * r; e += nt) {
+                int i = k + 1 + e % r, j = k + 1 + e / r;
+                A[j * lda + i] -= A[k * lda + i] * A[j * lda + k];
+            }
+            __syncthreads();
+        }
+        if (b == bw) break;
+        // _luswap! of the piece's rows in the block columns to its right and the
+        // U panel solve (one thread per column), the L panel solve (one per row)
+        for (int j = b + tid; j < bw; j += nt) {
+            T* col = A + j * lda;
+            for (int k = a; k < b; ++k) {
+                int kp = a + piv[k];
+                if (kp != k) { T t = col[k]; col[k] = col[kp]; col[kp] = t; }
+            }
+            for (int k = a; k < b; ++k) {           // unit-lower solve (trsm 'r','l','t','u' on U')
+                T xk = col[k];
+                for (int i = k + 1; i < b; ++i) {
+                    T l = A[k * lda + i];
+                    if (l != T(0)) col[i] -= l * xk;
+                }
+            }
+        }
+        for (int i = b + tid; i < bw; i += nt) {   // X := X * inv(U_pp)  (trsm 'r','u','n','n')
+            for (int j = a; j < b; ++j) {
+                T sacc = A[j * lda + i];
+                for (int k = a; k < j; ++k) {
+                    T u = A[j * lda + k];
+                    if (u != T(0)) sacc -= u * A[k * lda + i];
+                }
+                A[j * lda + i] = sacc * (T(1) / A[j * lda + j]);
+            }
         }
         __syncthreads();
-        const int r = w - k - 1;
-        for (int e = tid; e < r * r; e += nt) {
-            int i = k + 1 + e % r, j = k + 1 + e / r;
-            A[j * w + i] -= A[k * w + i] * A[j * w + k];
+        const int r = bw - b, w = b - a;
+        for (int e = tid; e < r * r; e += nt) {   // block-local trailing update
+            int i = b + e % r, j = b + e / r;
+            T acc = T(0);
+            for (int k = 0; k < w; ++k) acc += A[(a + k) * lda + i] * A[j * lda + a + k];
+            A[j * lda + i] -= acc;
         }
         __syncthreads();
     }
 }
 
-// Factor the diagonal block of piece p of front F in place and record its
-// pivots (0-based local) in ipiv[column].  Used by k_getrf_first and by the
-// corner tile of k_trail.
+// One CTA per front: factor block `step` of the front, write it back with
+// its pivots, and store Minv and Uinv (each bw x bw, column-major) in inv[].
+// Dynamic shared memory: 3 * bwmax * (bwmax + 1) T's + 2 * (BlockMax + 1) ints.
 template <typename T>
-__device__ void factor_diag(T* fac, int* ipiv, int* info, const DFront& F, int p, int p0, int w, T* sD,
-                            int* spiv, int* ssing) {
-    const int tid = threadIdx.x, nt = blockDim.x;
-    if (tid == 0) *ssing = 0;
-    for (int e = tid; e < w * w; e += nt) {
-        int i = e % w, k = e / w;
-        sD[k * w + i] = fac[F.loff + (ll)(p0 + k) * F.ld + p0 + i];
-    }
-    __syncthreads();
-    block_getrf(sD, w, spiv, ssing);
-    for (int e = tid; e < w * w; e += nt) {
-        int i = e % w, k = e / w;
-        fac[F.loff + (ll)(p0 + k) * F.ld + p0 + i] = sD[k * w + i];
-    }
-    if (tid < w) ipiv[F.f + p0 + tid] = spiv[tid];
-    if (tid == 0 && *ssing) atomicMin(info, p + 1);
-}
-
-template <typename T>
-__global__ void __launch_bounds__(128) k_getrf_first(T* fac, int* ipiv, int* info, Sched S, Launch L) {
-    __shared__ T sD[MAXW * MAXW];
-    __shared__ int spiv[MAXW];
+__global__ void __launch_bounds__(128) k_block_lu(T* fac, int* ipiv, int* info, T* inv, Sched S, Launch L, int step,
+                                                   int bwmax) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lmax = bwmax + 1;
+    T* A = reinterpret_cast<T*>(smem_raw);
+    T* Mi = A + bwmax * lmax;       // row-major: (i, j) at i * lda + j, thread j owns column j
+    T* Ui = Mi + bwmax * lmax;
+    int* q0 = reinterpret_cast<int*>(Ui + bwmax * lmax);
+    int* piv = q0 + BlockMax<T>::value + 1;
     __shared__ int ssing;
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
-    const int p = F.piece0;
-    const int p0 = S.xsuper[p] - F.f, w = S.xsuper[p + 1] - S.xsuper[p];
-    factor_diag(fac, ipiv, info, F, p, p0, w, sD, spiv, &ssing);
-}
-
-// ---------------------------------------------------------------------------
-// Panel kernel for piece `step` of every front in the launch.  Tiles:
-//   [0, nL)          : 128 rows of the L panel, X := X * inv(U11) (trsm 'r','u','n','n')
-//   [nL, nL+nUa)     : 128 U columns inside the front (stored in Lf)
-//   [nL+nUa, ...)    : 128 U columns of U12 (stored in Uf)
-// U columns get the block's row interchanges (_luswap!) and then
-// X := inv(L11) X (the reference's trsm 'r','l','t','u' on U12').
-// ---------------------------------------------------------------------------
-constexpr int TP = 128;
-
-// Dynamic shared memory: (wmax^2 + wmax*TP) T's and MAXW ints, wmax the widest piece.
-template <typename T>
-__global__ void __launch_bounds__(TP) k_panel(T* fac, const int* ipiv, Sched S, Launch L, int step, int wmax) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sD = reinterpret_cast<T*>(smem_raw);
-    T* sX = sD + wmax * wmax;
-    int* spiv = reinterpret_cast<int*>(sX + wmax * TP);
-    int fid, tile;
-    locate(L, blockIdx.x, fid, tile);
-    const DFront F = S.fronts[fid];
-    const int p = F.piece0 + step;
-    const int p0 = S.xsuper[p] - F.f, p1 = S.xsuper[p + 1] - F.f, w = p1 - p0;
-    const int tid = threadIdx.x;
-    for (int e = tid; e < w * w; e += TP) {
-        int i = e % w, k = e / w;
-        sD[k * w + i] = fac[F.loff + (ll)(p0 + k) * F.ld + p0 + i];
+    const int blk = F.block0 + step;
+    const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
+    const int lda = bw | 1;
+    const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    if (tid == 0) ssing = 0;
+    for (int k = tid; k <= np; k += nt) q0[k] = S.xsuper[p0 + k] - F.f - c0;
+    for (int e = tid; e < bw * bw; e += nt) {
+        int i = e % bw, j = e / bw;
+        A[j * lda + i] = fac[F.loff + (ll)(c0 + j) * F.ld + c0 + i];
     }
-    if (tid < w) spiv[tid] = ipiv[F.f + p0 + tid];
-    const int nL = cdiv(F.ld - p1, TP), nUa = cdiv(F.nf - p1, TP);
-    if (tile < nL) {
-        const int r0 = p1 + tile * TP;
-        const int nr = min(TP, F.ld - r0);
-        for (int k = 0; k < w; ++k)
-            if (tid < nr) sX[k * TP + tid] = fac[F.loff + (ll)(p0 + k) * F.ld + r0 + tid];
-        __syncthreads();
-        if (tid < nr) {
-            for (int j = 0; j < w; ++j) {
-                T s = sX[j * TP + tid];
-                for (int k = 0; k < j; ++k) {
-                    T u = sD[j * w + k];
-                    if (u != T(0)) s -= u * sX[k * TP + tid];
-                }
-                sX[j * TP + tid] = s * (T(1) / sD[j * w + j]);
+    __syncthreads();
+    block_lu(A, bw, lda, q0, np, piv, &ssing);
+    for (int e = tid; e < bw * bw; e += nt) {
+        int i = e % bw, j = e / bw;
+        fac[F.loff + (ll)(c0 + j) * F.ld + c0 + i] = A[j * lda + i];
+    }
+    for (int c = tid; c < bw; c += nt) ipiv[F.f + c0 + c] = piv[c];
+    if (tid == 0 && ssing) {
+        for (int pc = 0; pc < np; ++pc) {   // first singular piece of the block
+            bool z = false;
+            for (int k = q0[pc]; k < q0[pc + 1]; ++k) z |= A[k * lda + k] == T(0);
+            if (z) { atomicMin(info, p0 + pc + 1); break; }
+        }
+    }
+    // column j of Minv and of Uinv, one thread per column
+    for (int j = tid; j < bw; j += nt) {
+        for (int i = 0; i < bw; ++i) Mi[i * lda + j] = T(i == j);
+        for (int pc = 0; pc < np; ++pc) {
+            const int a = q0[pc], b = q0[pc + 1];
+            for (int i = a; i < b; ++i) {             // earlier pieces' L columns
+                T acc = T(0);
+                for (int c = 0; c < a; ++c) acc += A[c * lda + i] * Mi[c * lda + j];
+                Mi[i * lda + j] -= acc;
+            }
+            for (int k = a; k < b; ++k) {             // the piece's interchanges (laswp)
+                int kp = a + piv[k];
+                if (kp != k) { T t = Mi[k * lda + j]; Mi[k * lda + j] = Mi[kp * lda + j]; Mi[kp * lda + j] = t; }
+            }
+            for (int k = a; k < b; ++k) {             // unit-lower solve (trsm 'l','l','n','u')
+                T vk = Mi[k * lda + j];
+                if (vk != T(0))
+                    for (int i = k + 1; i < b; ++i) Mi[i * lda + j] -= vk * A[k * lda + i];
             }
         }
-        __syncthreads();
-        for (int k = 0; k < w; ++k)
-            if (tid < nr) fac[F.loff + (ll)(p0 + k) * F.ld + r0 + tid] = sX[k * TP + tid];
-    } else {
-        const bool inner = tile < nL + nUa;
-        const int c0 = inner ? p1 + (tile - nL) * TP : (tile - nL - nUa) * TP;   // inner: front column; else U12 column
-        const int nc = inner ? min(TP, F.nf - c0) : min(TP, F.m - c0);
-        // cooperative load of the w x nc block into sX[k*TP + c]
-        if (inner) {
-            for (int e = tid; e < w * nc; e += TP) {
-                int k = e % w, c = e / w;
-                sX[k * TP + c] = fac[F.loff + (ll)(c0 + c) * F.ld + p0 + k];
-            }
-        } else {
-            for (int k = 0; k < w; ++k)
-                if (tid < nc) sX[k * TP + tid] = fac[F.uoff + (ll)(p0 + k) * F.m + c0 + tid];
-        }
-        __syncthreads();
-        if (tid < nc) {
-            for (int k = 0; k < w; ++k) {
-                int kp = spiv[k];
-                if (kp != k) {
-                    T t = sX[k * TP + tid];
-                    sX[k * TP + tid] = sX[kp * TP + tid];
-                    sX[kp * TP + tid] = t;
-                }
-            }
-            for (int k = 0; k < w; ++k) {
-                T xk = sX[k * TP + tid];
-                for (int j = k + 1; j < w; ++j) {
-                    T l = sD[k * w + j];
-                    if (l != T(0)) sX[j * TP + tid] -= l * xk;
-                }
+        for (int i = 0; i < bw; ++i) Ui[i * lda + j] = T(i == j);
+        for (int k = bw - 1; k >= 0; --k) {           // upper solve (trsm 'l','u','n','n')
+            T uk = Ui[k * lda + j];
+            if (uk != T(0)) {
+                uk /= A[k * lda + k];
+                Ui[k * lda + j] = uk;
+                for (int i = 0; i < k; ++i) Ui[i * lda + j] -= uk * A[k * lda + i];
             }
         }
-        __syncthreads();
-        if (inner) {
-            for (int e = tid; e < w * nc; e += TP) {
-                int k = e % w, c = e / w;
-                fac[F.loff + (ll)(c0 + c) * F.ld + p0 + k] = sX[k * TP + c];
-            }
-        } else {
-            for (int k = 0; k < w; ++k)
-                if (tid < nc) fac[F.uoff + (ll)(p0 + k) * F.m + c0 + tid] = sX[k * TP + tid];
-        }
+    }
+    __syncthreads();
+    T* out = inv + S.blk_inv[blk];
+    for (int e = tid; e < bw * bw; e += nt) {   // column-major out: (i, j) at j * bw + i
+        int i = e % bw, j = e / bw;
+        out[e] = Mi[i * lda + j];
+        out[bw * bw + e] = Ui[i * lda + j];
     }
 }
 
@@ -294,59 +310,118 @@ __device__ __forceinline__ void mma_tile(const T* sA, const T* sB, int kc, T acc
     }
 }
 
-// Trailing update after piece `step`: A[R, C] -= L[R, piece] * U[piece, C]
-// over the front minus its Schur-complement block.  L tiles: rows in
-// [p1, nf+m), columns in [p1, nf) (stored in Lf).  U tiles: rows in
-// [p1, nf), columns in U12 (stored in Uf).  The L tile at the corner then
-// factors the next piece's diagonal block.
+// Panels of block `step`: 64-row tiles of the L panel below the block
+// (X := X * Uinv) and 64-column tiles of the U panel to its right, inside the
+// front (stored in Lf) and in U12 (stored in Uf) (Y := Minv * Y).
+// Dynamic shared memory: (64 + bwmax) * bwmax T's.
 template <typename T>
-__global__ void __launch_bounds__(256) k_trail(T* fac, int* ipiv, int* info, Sched S, Launch L, int step) {
-    __shared__ T sAB[2 * KC * TT];     // also the MAXW x MAXW scratch of the corner factorisation
-    __shared__ int spiv[MAXW];
-    __shared__ int ssing;
-    T* sA = sAB;
-    T* sB = sAB + KC * TT;
+__global__ void __launch_bounds__(256) k_block_panel(T* fac, const T* inv, Sched S, Launch L, int step, int bwmax) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sX = reinterpret_cast<T*>(smem_raw);   // 64 x bw tile (k-major: sX[k*64 + i])
+    T* sI = sX + 64 * bwmax;                  // bw x bw inverse
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
-    const int p = F.piece0 + step;
-    const int p0 = S.xsuper[p] - F.f, p1 = S.xsuper[p + 1] - F.f, w = p1 - p0;
+    const int blk = F.block0 + step;
+    const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
     const int tid = threadIdx.x;
-    const int nrL = cdiv(F.ld - p1, TT), ncL = cdiv(F.nf - p1, TT);
-    const bool isL = tile < nrL * ncL;
-    int r0, c0, nr, nc;
-    if (isL) {
-        r0 = p1 + (tile % nrL) * TT;
-        c0 = p1 + (tile / nrL) * TT;
-        nr = min(TT, F.ld - r0);
-        nc = min(TT, F.nf - c0);
+    const int nL = cdiv(F.ld - c1, 64), nUa = cdiv(F.nf - c1, 64);
+    const T* Mi = inv + S.blk_inv[blk];
+    const T* Ui = Mi + bw * bw;
+    if (tile < nL) {
+        const int r0 = c1 + tile * 64, nr = min(64, F.ld - r0);
+        for (int e = tid; e < 64 * bw; e += 256) {
+            int i = e % 64, k = e / 64;
+            sX[k * 64 + i] = i < nr ? fac[F.loff + (ll)(c0 + k) * F.ld + r0 + i] : T(0);
+        }
+        for (int e = tid; e < bw * bw; e += 256) sI[e] = Ui[e];
+        __syncthreads();
+        const int i = tid & 63, jg = tid >> 6;
+        if (i < nr) {
+            for (int j = jg; j < bw; j += 4) {
+                T acc = T(0);
+                for (int k = 0; k <= j; ++k) acc += sX[k * 64 + i] * sI[j * bw + k];
+                fac[F.loff + (ll)(c0 + j) * F.ld + r0 + i] = acc;
+            }
+        }
     } else {
-        const int t2 = tile - nrL * ncL, nrU = cdiv(F.nf - p1, TT);
-        r0 = p1 + (t2 % nrU) * TT;
-        c0 = (t2 / nrU) * TT;            // U12 column index
+        const bool inner = tile < nL + nUa;
+        const int col0 = inner ? c1 + (tile - nL) * 64 : (tile - nL - nUa) * 64;
+        const int nc = inner ? min(64, F.nf - col0) : min(64, F.m - col0);
+        if (inner) {
+            for (int e = tid; e < bw * 64; e += 256) {
+                int k = e % bw, c = e / bw;
+                sX[k * 64 + c] = c < nc ? fac[F.loff + (ll)(col0 + c) * F.ld + c0 + k] : T(0);
+            }
+        } else {
+            for (int e = tid; e < bw * 64; e += 256) {
+                int c = e % 64, k = e / 64;
+                sX[k * 64 + c] = c < nc ? fac[F.uoff + (ll)(c0 + k) * F.m + col0 + c] : T(0);
+            }
+        }
+        for (int e = tid; e < bw * bw; e += 256) sI[e] = Mi[e];
+        __syncthreads();
+        const int c = tid & 63, ig = tid >> 6;
+        if (c < nc) {
+            for (int i = ig; i < bw; i += 4) {
+                T acc = T(0);
+                for (int k = 0; k < bw; ++k) acc += sI[k * bw + i] * sX[k * 64 + c];
+                if (inner) fac[F.loff + (ll)(col0 + c) * F.ld + c0 + i] = acc;
+                else fac[F.uoff + (ll)(c0 + i) * F.m + col0 + c] = acc;
+            }
+        }
+    }
+}
+
+// Trailing update after block `step`: A[R, C] -= L[R, block] * U[block, C]
+// over the front minus its Schur-complement block.  L tiles: rows in
+// [c1, nf+m), columns in [c1, nf) (stored in Lf).  U tiles: rows in [c1, nf),
+// columns in U12 (stored in Uf).
+template <typename T>
+__global__ void __launch_bounds__(256) k_block_trail(T* fac, Sched S, Launch L, int step) {
+    __shared__ T sA[KC * TT];
+    __shared__ T sB[KC * TT];
+    int fid, tile;
+    locate(L, blockIdx.x, fid, tile);
+    const DFront F = S.fronts[fid];
+    const int blk = F.block0 + step;
+    const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk];
+    const int tid = threadIdx.x;
+    const int nrL = cdiv(F.ld - c1, TT), ncL = cdiv(F.nf - c1, TT);
+    const bool isL = tile < nrL * ncL;
+    int r0, col0, nr, nc;
+    if (isL) {
+        r0 = c1 + (tile % nrL) * TT;
+        col0 = c1 + (tile / nrL) * TT;
+        nr = min(TT, F.ld - r0);
+        nc = min(TT, F.nf - col0);
+    } else {
+        const int t2 = tile - nrL * ncL, nrU = cdiv(F.nf - c1, TT);
+        r0 = c1 + (t2 % nrU) * TT;
+        col0 = (t2 / nrU) * TT;            // U12 column index
         nr = min(TT, F.nf - r0);
-        nc = min(TT, F.m - c0);
+        nc = min(TT, F.m - col0);
     }
     T acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
-    for (int k0 = 0; k0 < w; k0 += KC) {
-        const int kc = min(KC, w - k0);
+    for (int k0 = c0; k0 < c1; k0 += KC) {
+        const int kc = min(KC, c1 - k0);
         for (int e = tid; e < kc * TT; e += 256) {
             int i = e % TT, k = e / TT;
-            sA[k * TT + i] = (i < nr) ? fac[F.loff + (ll)(p0 + k0 + k) * F.ld + r0 + i] : T(0);
+            sA[k * TT + i] = (i < nr) ? fac[F.loff + (ll)(k0 + k) * F.ld + r0 + i] : T(0);
         }
         if (isL) {
             for (int e = tid; e < kc * TT; e += 256) {
                 int k = e % kc, j = e / kc;
-                sB[k * TT + j] = (j < nc) ? fac[F.loff + (ll)(c0 + j) * F.ld + p0 + k0 + k] : T(0);
+                sB[k * TT + j] = (j < nc) ? fac[F.loff + (ll)(col0 + j) * F.ld + k0 + k] : T(0);
             }
         } else {
             for (int e = tid; e < kc * TT; e += 256) {
                 int j = e % TT, k = e / TT;
-                sB[k * TT + j] = (j < nc) ? fac[F.uoff + (ll)(p0 + k0 + k) * F.m + c0 + j] : T(0);
+                sB[k * TT + j] = (j < nc) ? fac[F.uoff + (ll)(k0 + k) * F.m + col0 + j] : T(0);
             }
         }
         __syncthreads();
@@ -363,7 +438,7 @@ __global__ void __launch_bounds__(256) k_trail(T* fac, int* ipiv, int* info, Sch
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
                 int r = tx + 16 * a;
-                if (r < nr) fac[F.loff + (ll)(c0 + c) * F.ld + r0 + r] -= acc[a][b];
+                if (r < nr) fac[F.loff + (ll)(col0 + c) * F.ld + r0 + r] -= acc[a][b];
             }
         }
     } else {
@@ -374,15 +449,9 @@ __global__ void __launch_bounds__(256) k_trail(T* fac, int* ipiv, int* info, Sch
 #pragma unroll
             for (int b = 0; b < 4; ++b) {
                 int c = tx + 16 * b;
-                if (c < nc) fac[F.uoff + (ll)(r0 + r) * F.m + c0 + c] -= acc[a][b];
+                if (c < nc) fac[F.uoff + (ll)(r0 + r) * F.m + col0 + c] -= acc[a][b];
             }
         }
-    }
-    if (isL && tile == 0 && step + 1 < F.npieces) {
-        __syncthreads();
-        const int q = p + 1;
-        const int q0 = S.xsuper[q] - F.f, wq = S.xsuper[q + 1] - S.xsuper[q];
-        factor_diag(fac, ipiv, info, F, q, q0, wq, sAB, spiv, &ssing);
     }
 }
 
@@ -449,57 +518,54 @@ __global__ void __launch_bounds__(256) k_schur(T* fac, Sched S, Launch L) {
 constexpr int TS = 128;
 constexpr int MAXRHS = 16;
 
-// Forward step for piece `step`: interchanges (laswp), unit-lower solve of
-// the piece (the reference's _lulsolve!, SpkLUFactor.jl:297-321) and the
-// update of every row below it in the front; rows of R_F are updated with
-// atomics because sibling fronts share them.  b is the running right-hand
-// side, y receives the solved values of the piece.
+// Forward step for block `step`: y_B = Minv * b_B (the interchanges and
+// unit-lower solves of the block's pieces, the reference's _lulsolve! steps,
+// SpkLUFactor.jl:297-321), then every row below the block in the front is
+// updated; rows of R_F are updated with atomics because sibling fronts share
+// them.  b is the running right-hand side, y receives the block's values.
 template <typename T>
-__global__ void __launch_bounds__(TS) k_fwd(const T* fac, const int* ipiv, T* b, T* y, int n, int nrhs, Sched S,
+__global__ void __launch_bounds__(TS) k_fwd(const T* fac, const T* inv, T* b, T* y, int n, int nrhs, Sched S,
                                             Launch L, int step) {
-    __shared__ T sD[MAXW * MAXW];
-    __shared__ T sy[MAXW * MAXRHS];
+    constexpr int BM = BlockMax<T>::value;
+    __shared__ T sb[BM * MAXRHS];
+    __shared__ T sy[BM * MAXRHS];
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
-    const int p = F.piece0 + step;
-    const int p0 = S.xsuper[p] - F.f, p1 = S.xsuper[p + 1] - F.f, w = p1 - p0;
+    const int blk = F.block0 + step;
+    const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
+    const T* Mi = inv + S.blk_inv[blk];
     const int tid = threadIdx.x;
-    for (int e = tid; e < w * w; e += TS) {
-        int i = e % w, k = e / w;
-        sD[k * w + i] = fac[F.loff + (ll)(p0 + k) * F.ld + p0 + i];
-    }
-    for (int e = tid; e < w * nrhs; e += TS) {
-        int k = e % w, r = e / w;
-        sy[r * MAXW + k] = b[(ll)r * n + F.f + p0 + k];
+    for (int e = tid; e < bw * nrhs; e += TS) {
+        int k = e % bw, r = e / bw;
+        sb[r * BM + k] = b[(ll)r * n + F.f + c0 + k];
     }
     __syncthreads();
-    if (tid < nrhs) {
-        T* v = sy + tid * MAXW;
-        for (int k = 0; k < w; ++k) {
-            int kp = ipiv[F.f + p0 + k];
-            if (kp != k) { T t = v[k]; v[k] = v[kp]; v[kp] = t; }
-        }
-        for (int k = 0; k < w; ++k) {
-            T vk = v[k];
-            if (vk != T(0))
-                for (int i = k + 1; i < w; ++i) v[i] -= vk * sD[k * w + i];
+    for (int i = tid; i < bw; i += TS) {
+        for (int r = 0; r < nrhs; ++r) {
+            T acc = T(0);
+            for (int k = 0; k < bw; ++k) acc += Mi[(ll)k * bw + i] * sb[r * BM + k];
+            sy[r * BM + i] = acc;
         }
     }
     __syncthreads();
     if (tile == 0)
-        for (int e = tid; e < w * nrhs; e += TS) {
-            int k = e % w, r = e / w;
-            y[(ll)r * n + F.f + p0 + k] = sy[r * MAXW + k];
+        for (int e = tid; e < bw * nrhs; e += TS) {
+            int k = e % bw, r = e / bw;
+            y[(ll)r * n + F.f + c0 + k] = sy[r * BM + k];
         }
-    const int row = p1 + tile * TS + tid;
+    const int row = c1 + tile * TS + tid;
     if (row < F.ld) {
         const int grow = row < F.nf ? F.f + row : S.rows[F.rows_off + row - F.nf];
+        T acc[MAXRHS];
+        for (int r = 0; r < nrhs; ++r) acc[r] = T(0);
+        for (int k = 0; k < bw; ++k) {
+            const T l = fac[F.loff + (ll)(c0 + k) * F.ld + row];
+            for (int r = 0; r < nrhs; ++r) acc[r] += l * sy[r * BM + k];
+        }
         for (int r = 0; r < nrhs; ++r) {
-            T acc = T(0);
-            for (int k = 0; k < w; ++k) acc += sy[r * MAXW + k] * fac[F.loff + (ll)(p0 + k) * F.ld + row];
-            if (row < F.nf) b[(ll)r * n + grow] -= acc;
-            else atomicAdd(&b[(ll)r * n + grow], -acc);
+            if (row < F.nf) b[(ll)r * n + grow] -= acc[r];
+            else atomicAdd(&b[(ll)r * n + grow], -acc[r]);
         }
     }
 }
@@ -523,51 +589,49 @@ __global__ void __launch_bounds__(TS) k_bwd_u12(const T* fac, T* y, const T* x, 
     }
 }
 
-// Backward, part 2, for the piece `step`-th from the last: upper solve of
-// the piece (the reference's _luusolve!, SpkLUFactor.jl:350-375), then the
-// update of the front's rows above it.
+// Backward, part 2, for the block `step`-th from the last: x_B = Uinv * y_B
+// (the upper solves of the block's pieces, the reference's _luusolve!,
+// SpkLUFactor.jl:350-375), then the update of the front's rows above it.
 template <typename T>
-__global__ void __launch_bounds__(TS) k_bwd(const T* fac, T* y, T* x, int n, int nrhs, Sched S, Launch L, int step) {
-    __shared__ T sD[MAXW * MAXW];
-    __shared__ T sx[MAXW * MAXRHS];
+__global__ void __launch_bounds__(TS) k_bwd(const T* fac, const T* inv, T* y, T* x, int n, int nrhs, Sched S, Launch L,
+                                            int step) {
+    constexpr int BM = BlockMax<T>::value;
+    __shared__ T sc[BM * MAXRHS];
+    __shared__ T sx[BM * MAXRHS];
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
-    const int p = F.piece0 + F.npieces - 1 - step;
-    const int p0 = S.xsuper[p] - F.f, p1 = S.xsuper[p + 1] - F.f, w = p1 - p0;
+    const int blk = F.block0 + F.nblocks - 1 - step;
+    const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
+    const T* Ui = inv + S.blk_inv[blk] + (ll)bw * bw;
     const int tid = threadIdx.x;
-    for (int e = tid; e < w * w; e += TS) {
-        int i = e % w, k = e / w;
-        sD[k * w + i] = fac[F.loff + (ll)(p0 + k) * F.ld + p0 + i];
-    }
-    for (int e = tid; e < w * nrhs; e += TS) {
-        int k = e % w, r = e / w;
-        sx[r * MAXW + k] = y[(ll)r * n + F.f + p0 + k];
+    for (int e = tid; e < bw * nrhs; e += TS) {
+        int k = e % bw, r = e / bw;
+        sc[r * BM + k] = y[(ll)r * n + F.f + c0 + k];
     }
     __syncthreads();
-    if (tid < nrhs) {
-        T* v = sx + tid * MAXW;
-        for (int k = w - 1; k >= 0; --k) {
-            if (v[k] != T(0)) {
-                v[k] /= sD[k * w + k];
-                T vk = v[k];
-                for (int i = 0; i < k; ++i) v[i] -= vk * sD[k * w + i];
-            }
+    for (int i = tid; i < bw; i += TS) {
+        for (int r = 0; r < nrhs; ++r) {
+            T acc = T(0);
+            for (int k = i; k < bw; ++k) acc += Ui[(ll)k * bw + i] * sc[r * BM + k];
+            sx[r * BM + i] = acc;
         }
     }
     __syncthreads();
     if (tile == 0)
-        for (int e = tid; e < w * nrhs; e += TS) {
-            int k = e % w, r = e / w;
-            x[(ll)r * n + F.f + p0 + k] = sx[r * MAXW + k];
+        for (int e = tid; e < bw * nrhs; e += TS) {
+            int k = e % bw, r = e / bw;
+            x[(ll)r * n + F.f + c0 + k] = sx[r * BM + k];
         }
     const int row = tile * TS + tid;
-    if (row < p0) {
-        for (int r = 0; r < nrhs; ++r) {
-            T acc = T(0);
-            for (int k = 0; k < w; ++k) acc += fac[F.loff + (ll)(p0 + k) * F.ld + row] * sx[r * MAXW + k];
-            y[(ll)r * n + F.f + row] -= acc;
+    if (row < c0) {
+        T acc[MAXRHS];
+        for (int r = 0; r < nrhs; ++r) acc[r] = T(0);
+        for (int k = 0; k < bw; ++k) {
+            const T u = fac[F.loff + (ll)(c0 + k) * F.ld + row];
+            for (int r = 0; r < nrhs; ++r) acc[r] += u * sx[r * BM + k];
         }
+        for (int r = 0; r < nrhs; ++r) y[(ll)r * n + F.f + row] -= acc[r];
     }
 }
 
