@@ -724,7 +724,7 @@ static int factor_launches(spk_handle* h) {
         for (size_t t = 0; t < P.blu.size(); ++t) {
             if (P.blu[t].tiles > 0) {
                 LaunchScope ls(h, SPK_K_GETRF, P.blu[t].flops, P.blu[t].words * sizeof(T));
-                spk::k_block_lu<T><<<P.blu[t].tiles, 128, lu_smem, h->stream>>>(fac, h->d_ipiv, h->d_info, inv, S,
+                spk::k_block_lu<T><<<P.blu[t].tiles, 256, lu_smem, h->stream>>>(fac, h->d_ipiv, h->d_info, inv, S,
                                                                                  launch_of(PL, P.blu[t]), (int)t, bw);
             }
             if (P.bpanel[t].tiles > 0) {

@@ -209,7 +209,7 @@ __device__ void block_lu(T* A, int bw, int lda, const int* q0, int np, int* piv,
 // its pivots, and store Minv and Uinv (each bw x bw, column-major) in inv[].
 // Dynamic shared memory: 3 * bwmax * (bwmax + 1) T's + 2 * (BlockMax + 1) ints.
 template <typename T>
-__global__ void __launch_bounds__(128) k_block_lu(T* fac, int* ipiv, int* info, T* inv, Sched S, Launch L, int step,
+__global__ void __launch_bounds__(256) k_block_lu(T* fac, int* ipiv, int* info, T* inv, Sched S, Launch L, int step,
                                                    int bwmax) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lmax = bwmax + 1;
@@ -247,35 +247,47 @@ __global__ void __launch_bounds__(128) k_block_lu(T* fac, int* ipiv, int* info, 
             if (z) { atomicMin(info, p0 + pc + 1); break; }
         }
     }
-    // column j of Minv and of Uinv, one thread per column
-    for (int j = tid; j < bw; j += nt) {
-        for (int i = 0; i < bw; ++i) Mi[i * lda + j] = T(i == j);
-        for (int pc = 0; pc < np; ++pc) {
-            const int a = q0[pc], b = q0[pc + 1];
-            for (int i = a; i < b; ++i) {             // earlier pieces' L columns
-                T acc = T(0);
-                for (int c = 0; c < a; ++c) acc += A[c * lda + i] * Mi[c * lda + j];
-                Mi[i * lda + j] -= acc;
-            }
-            for (int k = a; k < b; ++k) {             // the piece's interchanges (laswp)
+    // Minv: the block's forward operator applied to the identity, as
+    // right-looking sweeps over the rows of Z (row-major, (i, j) at i * lda + j)
+    for (int e = tid; e < bw * bw; e += nt) {
+        int i = e / bw, j = e % bw;
+        Mi[i * lda + j] = T(i == j);
+    }
+    __syncthreads();
+    for (int pc = 0; pc < np; ++pc) {
+        const int a = q0[pc], b = q0[pc + 1];
+        for (int j = tid; j < bw; j += nt)             // the piece's interchanges (laswp), per column
+            for (int k = a; k < b; ++k) {
                 int kp = a + piv[k];
                 if (kp != k) { T t = Mi[k * lda + j]; Mi[k * lda + j] = Mi[kp * lda + j]; Mi[kp * lda + j] = t; }
             }
-            for (int k = a; k < b; ++k) {             // unit-lower solve (trsm 'l','l','n','u')
-                T vk = Mi[k * lda + j];
-                if (vk != T(0))
-                    for (int i = k + 1; i < b; ++i) Mi[i * lda + j] -= vk * A[k * lda + i];
+        __syncthreads();
+        for (int k = a; k < b; ++k) {                  // column k of L: rows below k, within the block
+            const int r = bw - k - 1;
+            for (int e = tid; e < r * bw; e += nt) {
+                int i = k + 1 + e / bw, j = e % bw;
+                T l = A[k * lda + i];
+                if (l != T(0)) Mi[i * lda + j] -= l * Mi[k * lda + j];
             }
+            __syncthreads();
         }
-        for (int i = 0; i < bw; ++i) Ui[i * lda + j] = T(i == j);
-        for (int k = bw - 1; k >= 0; --k) {           // upper solve (trsm 'l','u','n','n')
-            T uk = Ui[k * lda + j];
-            if (uk != T(0)) {
-                uk /= A[k * lda + k];
-                Ui[k * lda + j] = uk;
-                for (int i = 0; i < k; ++i) Ui[i * lda + j] -= uk * A[k * lda + i];
-            }
+    }
+    // Uinv = U^{-1} by backward sweeps (trsm 'l','u','n','n' on the identity)
+    for (int e = tid; e < bw * bw; e += nt) {
+        int i = e / bw, j = e % bw;
+        Ui[i * lda + j] = T(i == j);
+    }
+    __syncthreads();
+    for (int k = bw - 1; k >= 0; --k) {
+        const T d = A[k * lda + k];
+        for (int j = k + tid; j < bw; j += nt) Ui[k * lda + j] /= d;
+        __syncthreads();
+        const int cols = bw - k;
+        for (int e = tid; e < k * cols; e += nt) {
+            int i = e / cols, j = k + e % cols;
+            Ui[i * lda + j] -= A[k * lda + i] * Ui[k * lda + j];
         }
+        __syncthreads();
     }
     __syncthreads();
     T* out = inv + S.blk_inv[blk];
@@ -542,11 +554,18 @@ __global__ void __launch_bounds__(TS) k_fwd(const T* fac, const T* inv, T* b, T*
     }
     __syncthreads();
     for (int i = tid; i < bw; i += TS) {
-        for (int r = 0; r < nrhs; ++r) {
-            T acc = T(0);
-            for (int k = 0; k < bw; ++k) acc += Mi[(ll)k * bw + i] * sb[r * BM + k];
-            sy[r * BM + i] = acc;
+        T acc[MAXRHS];
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r) acc[r] = T(0);
+        for (int k = 0; k < bw; ++k) {
+            const T mk = Mi[(ll)k * bw + i];
+#pragma unroll
+            for (int r = 0; r < MAXRHS; ++r)
+                if (r < nrhs) acc[r] += mk * sb[r * BM + k];
         }
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r)
+            if (r < nrhs) sy[r * BM + i] = acc[r];
     }
     __syncthreads();
     if (tile == 0)
@@ -558,12 +577,19 @@ __global__ void __launch_bounds__(TS) k_fwd(const T* fac, const T* inv, T* b, T*
     if (row < F.ld) {
         const int grow = row < F.nf ? F.f + row : S.rows[F.rows_off + row - F.nf];
         T acc[MAXRHS];
-        for (int r = 0; r < nrhs; ++r) acc[r] = T(0);
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r) acc[r] = T(0);
+        const T* lcol = fac + F.loff + (ll)c0 * F.ld + row;
+#pragma unroll 4
         for (int k = 0; k < bw; ++k) {
-            const T l = fac[F.loff + (ll)(c0 + k) * F.ld + row];
-            for (int r = 0; r < nrhs; ++r) acc[r] += l * sy[r * BM + k];
+            const T l = lcol[(ll)k * F.ld];
+#pragma unroll
+            for (int r = 0; r < MAXRHS; ++r)
+                if (r < nrhs) acc[r] += l * sy[r * BM + k];
         }
-        for (int r = 0; r < nrhs; ++r) {
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r) {
+            if (r >= nrhs) break;
             if (row < F.nf) b[(ll)r * n + grow] -= acc[r];
             else atomicAdd(&b[(ll)r * n + grow], -acc[r]);
         }
@@ -611,11 +637,18 @@ __global__ void __launch_bounds__(TS) k_bwd(const T* fac, const T* inv, T* y, T*
     }
     __syncthreads();
     for (int i = tid; i < bw; i += TS) {
-        for (int r = 0; r < nrhs; ++r) {
-            T acc = T(0);
-            for (int k = i; k < bw; ++k) acc += Ui[(ll)k * bw + i] * sc[r * BM + k];
-            sx[r * BM + i] = acc;
+        T acc[MAXRHS];
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r) acc[r] = T(0);
+        for (int k = i; k < bw; ++k) {
+            const T uk = Ui[(ll)k * bw + i];
+#pragma unroll
+            for (int r = 0; r < MAXRHS; ++r)
+                if (r < nrhs) acc[r] += uk * sc[r * BM + k];
         }
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r)
+            if (r < nrhs) sx[r * BM + i] = acc[r];
     }
     __syncthreads();
     if (tile == 0)
@@ -626,12 +659,19 @@ __global__ void __launch_bounds__(TS) k_bwd(const T* fac, const T* inv, T* y, T*
     const int row = tile * TS + tid;
     if (row < c0) {
         T acc[MAXRHS];
-        for (int r = 0; r < nrhs; ++r) acc[r] = T(0);
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r) acc[r] = T(0);
+        const T* ucol = fac + F.loff + (ll)c0 * F.ld + row;
+#pragma unroll 4
         for (int k = 0; k < bw; ++k) {
-            const T u = fac[F.loff + (ll)(c0 + k) * F.ld + row];
-            for (int r = 0; r < nrhs; ++r) acc[r] += u * sx[r * BM + k];
+            const T u = ucol[(ll)k * F.ld];
+#pragma unroll
+            for (int r = 0; r < MAXRHS; ++r)
+                if (r < nrhs) acc[r] += u * sx[r * BM + k];
         }
-        for (int r = 0; r < nrhs; ++r) y[(ll)r * n + F.f + row] -= acc[r];
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r)
+            if (r < nrhs) y[(ll)r * n + F.f + row] -= acc[r];
     }
 }
 
