@@ -348,7 +348,9 @@ def run_ours(args):
                  "factor_gflops": F / (ms_f64 * 1e-3) / 1e9, "assembly_ms": ms_asm64},
         "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
         "host_once_per_pattern": host_t,
-        "profile_mixed_step": {c: {"ms": round(v["ms"], 4), "launches": v["launches"]} for c, v in prof.items()},
+        "profile_mixed_step": {c: {"ms": round(v["ms"], 4), "launches": v["launches"],
+                                   "gflops": round(v["flops"] / max(v["ms"], 1e-9) / 1e6, 1),
+                                   "gbs": round(v["bytes"] / max(v["ms"], 1e-9) / 1e6, 1)} for c, v in prof.items()},
         "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": {"value": ms_e2e, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),

@@ -30,6 +30,7 @@ struct LaunchRec {
     int tiles = 0;
     double flops = 0.0;   // algorithmic flops of the launch (solves: per right-hand side)
     double words = 0.0;   // algorithmic factor entries read or written (times sizeof(T) = bytes)
+    int bw = 1;           // widest block in the launch (sizes dynamic shared memory)
 };
 
 // A captured launch sequence and the accounting of one replay.
@@ -566,6 +567,13 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax) {
             }
             add_launch(&P, L.blu[t], ids, tl, fl, wl);
             add_launch(&P, L.bpanel[t], ids, tp, fp, wp);
+            int bwl = 1;
+            for (size_t k = 0; k < nid; ++k)
+                if (t < P.nblocks[ids[k]]) {
+                    const int blk = P.block0[ids[k]] + t;
+                    bwl = std::max(bwl, P.blk_c1[blk] - P.blk_c0[blk]);
+                }
+            L.blu[t].bw = L.bpanel[t].bw = bwl;
             add_launch(&P, L.btrail[t], ids, tt, ft, wt);
             add_launch(&P, L.fwd[t], ids, tf, ff, wf);
             add_launch(&P, L.bwd[t], ids, tb, fb, wb);
@@ -717,11 +725,11 @@ static int factor_launches(spk_handle* h) {
     T* inv = storage<T>(h).inv;
     const Plan& PL = h->plan[prec_index<T>()];
     const spk::Sched& S = PL.sched;
-    const int bw = PL.bwmax;
-    const size_t lu_smem = sizeof(T) * 3 * bw * (bw + 1) + sizeof(int) * 2 * (spk::BlockMax<T>::value + 1);
-    const size_t panel_smem = sizeof(T) * (64 + bw) * bw;
     for (const LevelPlan& P : PL.levels) {
         for (size_t t = 0; t < P.blu.size(); ++t) {
+            const int bw = P.blu[t].bw;
+            const size_t lu_smem = sizeof(T) * 3 * bw * (bw + 1) + sizeof(int) * 2 * (spk::BlockMax<T>::value + 1);
+            const size_t panel_smem = sizeof(T) * (64 + bw) * bw;
             if (P.blu[t].tiles > 0) {
                 LaunchScope ls(h, SPK_K_GETRF, P.blu[t].flops, P.blu[t].words * sizeof(T));
                 spk::k_block_lu<T><<<P.blu[t].tiles, 256, lu_smem, h->stream>>>(fac, h->d_ipiv, h->d_info, inv, S,
