@@ -511,7 +511,7 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax) {
             P.blk_p0.push_back(s);
             P.blk_np.push_back(t - s);
             P.blk_inv.push_back(inv);
-            inv += 2 * (ll)bw * bw;
+            for (int q = s; q < t; ++q) inv += 2 * (ll)(h->xs[q + 1] - h->xs[q]) * (h->xs[q + 1] - h->xs[q]);
             P.bwmax = std::max(P.bwmax, bw);
             s = t;
         }
@@ -662,9 +662,10 @@ static int ensure_plan(spk_handle* h) {
     S.blk_inv = P.d_blk_inv;
     const int bw = P.bwmax;
     CU(h, cudaFuncSetAttribute(spk::k_block_lu<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)(sizeof(T) * 3 * bw * (bw + 1) + sizeof(int) * 2 * (spk::BlockMax<T>::value + 1))));
+                               (int)(sizeof(T) * ((size_t)bw * (bw | 1) + 2 * (size_t)bw * spk::MAXW) +
+                                     sizeof(int) * 2 * (spk::BlockMax<T>::value + 1))));
     CU(h, cudaFuncSetAttribute(spk::k_block_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)(sizeof(T) * (64 + bw) * bw)));
+                               (int)(sizeof(T) * 64 * (size_t)bw)));
     P.built = true;
     return SPK_OK;
 }
@@ -728,8 +729,9 @@ static int factor_launches(spk_handle* h) {
     for (const LevelPlan& P : PL.levels) {
         for (size_t t = 0; t < P.blu.size(); ++t) {
             const int bw = P.blu[t].bw;
-            const size_t lu_smem = sizeof(T) * 3 * bw * (bw + 1) + sizeof(int) * 2 * (spk::BlockMax<T>::value + 1);
-            const size_t panel_smem = sizeof(T) * (64 + bw) * bw;
+            const size_t lu_smem = sizeof(T) * ((size_t)bw * (bw | 1) + 2 * (size_t)bw * spk::MAXW) +
+                                   sizeof(int) * 2 * (spk::BlockMax<T>::value + 1);
+            const size_t panel_smem = sizeof(T) * 64 * (size_t)bw;
             if (P.blu[t].tiles > 0) {
                 LaunchScope ls(h, SPK_K_GETRF, P.blu[t].flops, P.blu[t].words * sizeof(T));
                 spk::k_block_lu<T><<<P.blu[t].tiles, 256, lu_smem, h->stream>>>(fac, h->d_ipiv, h->d_info, inv, S,

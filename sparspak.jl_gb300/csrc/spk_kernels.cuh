@@ -99,124 +99,115 @@ constexpr int MAXW = 64;
 // Blocks.  The pieces of a front are processed in *blocks* of consecutive
 // pieces (at most BlockMax<T> columns).  k_block_lu factors a block in
 // shared memory piece by piece with exactly the reference's in-block
-// pivoting (ggetrf! on the piece's diagonal block, _luswap! of the piece's U
-// rows, the two _trsm! panels), and also forms two explicit inverses:
-//   Uinv = U_BB^{-1}  (upper triangle of the factored block), and
-//   Minv = the block's forward operator: applying it to a vector performs,
-//          piece by piece, "subtract the earlier pieces' L columns, apply
-//          the piece's interchanges, unit-lower solve" - the reference's
-//          _lulsolve! steps restricted to the block.
-// The L panel below the block is then X * Uinv, the U panel to its right is
-// Minv * Y, and the block steps of both triangular solves are Minv * b and
-// Uinv * c: small dense products instead of serial substitutions.
+// pivoting: ggetrf! on the piece's diagonal block (one warp), _luswap! of
+// the piece's U rows and the two _trsm! panels inside the block, and the
+// block-local trailing update.  For every piece p it also stores two w x w
+// matrices in inv[] (at 2 * sum of the earlier pieces' w^2):
+//   Ui_p = U_pp^{-1}            and   Li_p = L_pp^{-1} P_p
+// (P_p the piece's interchanges), so that the L panel below a piece is
+// X * Ui_p, the U panel to its right Li_p * Y, and the triangular-solve
+// steps of the piece Li_p * b and Ui_p * c: small dense products.
 // ---------------------------------------------------------------------------
 template <typename T> struct BlockMax;
 template <> struct BlockMax<float> { static constexpr int value = 128; };
 template <> struct BlockMax<double> { static constexpr int value = 64; };
 
-// Factor the bw x bw block A (shared, column-major, leading dimension lda,
-// odd so that one-thread-per-column loops do not collide on banks).  Pieces
-// start at local columns q0[0] < q0[1] < ... < q0[np] = bw.  piv[c] receives
-// the 0-based pivot row of column c local to its piece; *sing is set on a
-// zero pivot.
+// ggetrf! of the w x w diagonal block of a piece (w <= 64), by one warp:
+// A points at the block's first entry, column-major with leading dimension
+// lda.  piv[k] = 0-based local pivot row; returns true on a zero pivot.
 template <typename T>
-__device__ void block_lu(T* A, int bw, int lda, const int* q0, int np, int* piv, int* sing) {
-    const int tid = threadIdx.x, nt = blockDim.x;
-    for (int pc = 0; pc < np; ++pc) {
-        const int a = q0[pc], b = q0[pc + 1];
-        // ggetrf! on the piece's diagonal block: pivots among the piece's rows only
-        for (int k = a; k < b; ++k) {
-            if (tid < 32) {
-                double key = -1.0;
-                int idx = b;
-                for (int i = k + tid; i < b; i += 32) {
-                    double v = (double)tabs(A[k * lda + i]);
-                    double ki = (v != v) ? ((i == k) ? __longlong_as_double(0x7ff0000000000000LL) : -1.0) : v;
-                    if (ki > key || idx == b) { key = ki; idx = i; }
-                }
+__device__ bool warp_getrf(T* A, int lda, int w, int* piv) {
+    const int lane = threadIdx.x & 31;
+    bool sing = false;
+    for (int k = 0; k < w; ++k) {
+        double key = -1.0;
+        int idx = w;
+        for (int i = k + lane; i < w; i += 32) {
+            double v = (double)tabs(A[k * lda + i]);
+            double ki = (v != v) ? ((i == k) ? __longlong_as_double(0x7ff0000000000000LL) : -1.0) : v;
+            if (ki > key || idx == w) { key = ki; idx = i; }
+        }
 #pragma unroll
-                for (int off = 16; off > 0; off >>= 1) {
-                    double k2 = __shfl_down_sync(0xffffffffu, key, off);
-                    int i2 = __shfl_down_sync(0xffffffffu, idx, off);
-                    if (k2 > key || (k2 == key && i2 < idx)) { key = k2; idx = i2; }
+        for (int off = 16; off > 0; off >>= 1) {
+            double k2 = __shfl_xor_sync(0xffffffffu, key, off);
+            int i2 = __shfl_xor_sync(0xffffffffu, idx, off);
+            if (k2 > key || (k2 == key && i2 < idx)) { key = k2; idx = i2; }
+        }
+        const int kp = idx;
+        if (lane == 0) piv[k] = kp;
+        const T pv = A[k * lda + kp];
+        __syncwarp();
+        if (pv != T(0)) {
+            if (kp != k)
+                for (int j = lane; j < w; j += 32) {
+                    T t = A[j * lda + k];
+                    A[j * lda + k] = A[j * lda + kp];
+                    A[j * lda + kp] = t;
                 }
-                if (tid == 0) piv[k] = idx - a;
-            }
-            __syncthreads();
-            const int kp = a + piv[k];
-            const bool nz = A[k * lda + kp] != T(0);
-            if (nz) {
-                if (kp != k)
-                    for (int j = a + tid; j < b; j += nt) {
-                        T t = A[j * lda + k];
-                        A[j * lda + k] = A[j * lda + kp];
-                        A[j * lda + kp] = t;
-                    }
-                __syncthreads();
-                const T inv = T(1) / A[k * lda + k];
-                for (int i = k + 1 + tid; i < b; i += nt) A[k * lda + i] *= inv;
-            } else if (tid == 0) {
-                *sing = 1;
-            }
-            __syncthreads();
-            const int r = b - k - 1;
-            for (int e = tid; e < r * r; e += nt) {
-                int i = k + 1 + e % r, j = k + 1 + e / r;
-                A[j * lda + i] -= A[k * lda + i] * A[j * lda + k];
-            }
-            __syncthreads();
+            __syncwarp();
+            const T inv = T(1) / A[k * lda + k];
+            for (int i = k + 1 + lane; i < w; i += 32) A[k * lda + i] *= inv;
+        } else {
+            sing = true;
         }
-        if (b == bw) break;
-        // _luswap! of the piece's rows in the block columns to its right and the
-        // U panel solve (one thread per column), the L panel solve (one per row)
-        for (int j = b + tid; j < bw; j += nt) {
-            T* col = A + j * lda;
-            for (int k = a; k < b; ++k) {
-                int kp = a + piv[k];
-                if (kp != k) { T t = col[k]; col[k] = col[kp]; col[kp] = t; }
-            }
-            for (int k = a; k < b; ++k) {           // unit-lower solve (trsm 'r','l','t','u' on U')
-                T xk = col[k];
-                for (int i = k + 1; i < b; ++i) {
-                    T l = A[k * lda + i];
-                    if (l != T(0)) col[i] -= l * xk;
+        __syncwarp();
+        for (int i = k + 1 + lane; i < w; i += 32) {
+            const T lik = A[k * lda + i];
+            for (int j = k + 1; j < w; ++j) A[j * lda + i] -= lik * A[j * lda + k];
+        }
+        __syncwarp();
+    }
+    return sing;
+}
+
+// Inverses of a factored piece: Ui = U^{-1} (upper solve on the identity,
+// as trsm 'l','u','n','n') and Li = L^{-1} P (laswp then unit-lower solve on
+// the identity, as _lulsolve!), each w x w column-major (ld w), one lane per
+// column.  Warp 0 of the caller forms Ui, warp 1 forms Li.
+template <typename T>
+__device__ void piece_inverses(const T* A, int lda, int w, const int* piv, T* Ui, T* Li) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 0) {
+        for (int j = lane; j < w; j += 32) {
+            T* u = Ui + j * w;
+            for (int i = 0; i < w; ++i) u[i] = T(i == j);
+            for (int k = j; k >= 0; --k) {
+                T uk = u[k];
+                if (uk != T(0)) {
+                    uk /= A[k * lda + k];
+                    u[k] = uk;
+                    for (int i = 0; i < k; ++i) u[i] -= uk * A[k * lda + i];
                 }
             }
         }
-        for (int i = b + tid; i < bw; i += nt) {   // X := X * inv(U_pp)  (trsm 'r','u','n','n')
-            for (int j = a; j < b; ++j) {
-                T sacc = A[j * lda + i];
-                for (int k = a; k < j; ++k) {
-                    T u = A[j * lda + k];
-                    if (u != T(0)) sacc -= u * A[k * lda + i];
-                }
-                A[j * lda + i] = sacc * (T(1) / A[j * lda + j]);
+    } else if (warp == 1) {
+        for (int j = lane; j < w; j += 32) {
+            T* v = Li + j * w;
+            for (int i = 0; i < w; ++i) v[i] = T(i == j);
+            for (int k = 0; k < w; ++k) {
+                int kp = piv[k];
+                if (kp != k) { T t = v[k]; v[k] = v[kp]; v[kp] = t; }
+            }
+            for (int k = 0; k < w; ++k) {
+                T vk = v[k];
+                if (vk != T(0))
+                    for (int i = k + 1; i < w; ++i) v[i] -= vk * A[k * lda + i];
             }
         }
-        __syncthreads();
-        const int r = bw - b, w = b - a;
-        for (int e = tid; e < r * r; e += nt) {   // block-local trailing update
-            int i = b + e % r, j = b + e / r;
-            T acc = T(0);
-            for (int k = 0; k < w; ++k) acc += A[(a + k) * lda + i] * A[j * lda + a + k];
-            A[j * lda + i] -= acc;
-        }
-        __syncthreads();
     }
 }
 
-// One CTA per front: factor block `step` of the front, write it back with
-// its pivots, and store Minv and Uinv (each bw x bw, column-major) in inv[].
-// Dynamic shared memory: 3 * bwmax * (bwmax + 1) T's + 2 * (BlockMax + 1) ints.
+// One CTA (256 threads) per front: factor block `step` of the front in shared
+// memory, write it back with its pivots and the pieces' inverses.
+// Dynamic shared memory: bwmax * (bwmax | 1) + 2 * bwmax * MAXW T's, and
+// 2 * (BlockMax + 1) ints.
 template <typename T>
 __global__ void __launch_bounds__(256) k_block_lu(T* fac, int* ipiv, int* info, T* inv, Sched S, Launch L, int step,
                                                    int bwmax) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int lmax = bwmax + 1;
     T* A = reinterpret_cast<T*>(smem_raw);
-    T* Mi = A + bwmax * lmax;       // row-major: (i, j) at i * lda + j, thread j owns column j
-    T* Ui = Mi + bwmax * lmax;
-    int* q0 = reinterpret_cast<int*>(Ui + bwmax * lmax);
+    T* W = A + bwmax * (bwmax | 1);                 // the pieces' inverses, packed as in inv[]
+    int* q0 = reinterpret_cast<int*>(W + 2 * bwmax * MAXW);
     int* piv = q0 + BlockMax<T>::value + 1;
     __shared__ int ssing;
     int fid, tile;
@@ -226,75 +217,72 @@ __global__ void __launch_bounds__(256) k_block_lu(T* fac, int* ipiv, int* info, 
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
     const int lda = bw | 1;
     const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
-    const int tid = threadIdx.x, nt = blockDim.x;
+    const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
     if (tid == 0) ssing = 0;
     for (int k = tid; k <= np; k += nt) q0[k] = S.xsuper[p0 + k] - F.f - c0;
-    for (int e = tid; e < bw * bw; e += nt) {
-        int i = e % bw, j = e / bw;
-        A[j * lda + i] = fac[F.loff + (ll)(c0 + j) * F.ld + c0 + i];
-    }
+    for (int j = warp; j < bw; j += nw)
+        for (int i = lane; i < bw; i += 32) A[j * lda + i] = fac[F.loff + (ll)(c0 + j) * F.ld + c0 + i];
     __syncthreads();
-    block_lu(A, bw, lda, q0, np, piv, &ssing);
-    for (int e = tid; e < bw * bw; e += nt) {
-        int i = e % bw, j = e / bw;
-        fac[F.loff + (ll)(c0 + j) * F.ld + c0 + i] = A[j * lda + i];
+    int woff = 0;
+    for (int pc = 0; pc < np; ++pc) {
+        const int a = q0[pc], b = q0[pc + 1], w = b - a;
+        T* Ui = W + woff;
+        T* Li = Ui + w * w;
+        if (warp == 0) {
+            if (warp_getrf(A + a * lda + a, lda, w, piv + a)) ssing = 1;
+        }
+        __syncthreads();
+        piece_inverses(A + a * lda + a, lda, w, piv + a, Ui, Li);
+        __syncthreads();
+        if (b < bw) {
+            // U panel to the right inside the block: Y := Li * Y (interchanges + unit-lower
+            // solve); L panel below: X := X * Ui.  Both read the pre-solve values, so
+            // go through registers column by column / row by row.
+            for (int j = b + warp; j < bw; j += nw) {
+                T yv[2];
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const int i = lane + 32 * q;
+                    T acc = T(0);
+                    if (i < w)
+                        for (int k = 0; k < w; ++k) acc += Li[k * w + i] * A[j * lda + a + k];
+                    yv[q] = acc;
+                }
+                __syncwarp();
+#pragma unroll
+                for (int q = 0; q < 2; ++q)
+                    if (lane + 32 * q < w) A[j * lda + a + lane + 32 * q] = yv[q];
+            }
+            for (int i = b + tid; i < bw; i += nt) {
+                for (int j = w - 1; j >= 0; --j) {     // output column j needs inputs 0..j only
+                    T acc = T(0);
+                    for (int k = 0; k <= j; ++k) acc += A[(a + k) * lda + i] * Ui[j * w + k];
+                    A[(a + j) * lda + i] = acc;
+                }
+            }
+            __syncthreads();
+            for (int j = b + warp; j < bw; j += nw) {   // block-local trailing update
+                for (int i = b + lane; i < bw; i += 32) {
+                    T acc = T(0);
+                    for (int k = 0; k < w; ++k) acc += A[(a + k) * lda + i] * A[j * lda + a + k];
+                    A[j * lda + i] -= acc;
+                }
+            }
+            __syncthreads();
+        }
+        woff += 2 * w * w;
     }
+    for (int j = warp; j < bw; j += nw)
+        for (int i = lane; i < bw; i += 32) fac[F.loff + (ll)(c0 + j) * F.ld + c0 + i] = A[j * lda + i];
     for (int c = tid; c < bw; c += nt) ipiv[F.f + c0 + c] = piv[c];
+    T* out = inv + S.blk_inv[blk];
+    for (int e = tid; e < woff; e += nt) out[e] = W[e];
     if (tid == 0 && ssing) {
         for (int pc = 0; pc < np; ++pc) {   // first singular piece of the block
             bool z = false;
             for (int k = q0[pc]; k < q0[pc + 1]; ++k) z |= A[k * lda + k] == T(0);
             if (z) { atomicMin(info, p0 + pc + 1); break; }
         }
-    }
-    // Minv: the block's forward operator applied to the identity, as
-    // right-looking sweeps over the rows of Z (row-major, (i, j) at i * lda + j)
-    for (int e = tid; e < bw * bw; e += nt) {
-        int i = e / bw, j = e % bw;
-        Mi[i * lda + j] = T(i == j);
-    }
-    __syncthreads();
-    for (int pc = 0; pc < np; ++pc) {
-        const int a = q0[pc], b = q0[pc + 1];
-        for (int j = tid; j < bw; j += nt)             // the piece's interchanges (laswp), per column
-            for (int k = a; k < b; ++k) {
-                int kp = a + piv[k];
-                if (kp != k) { T t = Mi[k * lda + j]; Mi[k * lda + j] = Mi[kp * lda + j]; Mi[kp * lda + j] = t; }
-            }
-        __syncthreads();
-        for (int k = a; k < b; ++k) {                  // column k of L: rows below k, within the block
-            const int r = bw - k - 1;
-            for (int e = tid; e < r * bw; e += nt) {
-                int i = k + 1 + e / bw, j = e % bw;
-                T l = A[k * lda + i];
-                if (l != T(0)) Mi[i * lda + j] -= l * Mi[k * lda + j];
-            }
-            __syncthreads();
-        }
-    }
-    // Uinv = U^{-1} by backward sweeps (trsm 'l','u','n','n' on the identity)
-    for (int e = tid; e < bw * bw; e += nt) {
-        int i = e / bw, j = e % bw;
-        Ui[i * lda + j] = T(i == j);
-    }
-    __syncthreads();
-    for (int k = bw - 1; k >= 0; --k) {
-        const T d = A[k * lda + k];
-        for (int j = k + tid; j < bw; j += nt) Ui[k * lda + j] /= d;
-        __syncthreads();
-        const int cols = bw - k;
-        for (int e = tid; e < k * cols; e += nt) {
-            int i = e / cols, j = k + e % cols;
-            Ui[i * lda + j] -= A[k * lda + i] * Ui[k * lda + j];
-        }
-        __syncthreads();
-    }
-    __syncthreads();
-    T* out = inv + S.blk_inv[blk];
-    for (int e = tid; e < bw * bw; e += nt) {   // column-major out: (i, j) at j * bw + i
-        int i = e % bw, j = e / bw;
-        out[e] = Mi[i * lda + j];
-        out[bw * bw + e] = Ui[i * lda + j];
     }
 }
 
@@ -322,39 +310,67 @@ __device__ __forceinline__ void mma_tile(const T* sA, const T* sB, int kc, T acc
     }
 }
 
-// Panels of block `step`: 64-row tiles of the L panel below the block
-// (X := X * Uinv) and 64-column tiles of the U panel to its right, inside the
-// front (stored in Lf) and in U12 (stored in Uf) (Y := Minv * Y).
-// Dynamic shared memory: (64 + bwmax) * bwmax T's.
+// Panels of block `step`: 64-row tiles of the L panel below the block and
+// 64-column tiles of the U panel to its right (inside the front, stored in
+// Lf, and in U12, stored in Uf).  Piece by piece: an L row gets
+//   X_p := (X_p - X_<p U_<p,p) Ui_p,
+// a U column gets
+//   Y_p := Li_p (Y_p - L_p,<p Y_<p),
+// the reference's two _trsm! panels (after _luswap!) for every piece of the
+// block.  Block entries and inverses are read through the cache.
+// Dynamic shared memory: 64 * bwmax T's.
 template <typename T>
 __global__ void __launch_bounds__(256) k_block_panel(T* fac, const T* inv, Sched S, Launch L, int step, int bwmax) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sX = reinterpret_cast<T*>(smem_raw);   // 64 x bw tile (k-major: sX[k*64 + i])
-    T* sI = sX + 64 * bwmax;                  // bw x bw inverse
+    T* sX = reinterpret_cast<T*>(smem_raw);   // sX[k * 64 + t], k < bw, t < 64
+    __shared__ int q0[BlockMax<T>::value + 1];
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
     const int blk = F.block0 + step;
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
-    const int tid = threadIdx.x;
+    const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
+    const int tid = threadIdx.x, t = tid & 63, g = tid >> 6;
     const int nL = cdiv(F.ld - c1, 64), nUa = cdiv(F.nf - c1, 64);
-    const T* Mi = inv + S.blk_inv[blk];
-    const T* Ui = Mi + bw * bw;
+    const T* blockA = fac + F.loff + (ll)c0 * F.ld + c0;   // (i, j) of the block at j * ld + i
+    const T* W = inv + S.blk_inv[blk];
+    for (int k = tid; k <= np; k += 256) q0[k] = S.xsuper[p0 + k] - F.f - c0;
     if (tile < nL) {
         const int r0 = c1 + tile * 64, nr = min(64, F.ld - r0);
         for (int e = tid; e < 64 * bw; e += 256) {
-            int i = e % 64, k = e / 64;
+            int i = e & 63, k = e >> 6;
             sX[k * 64 + i] = i < nr ? fac[F.loff + (ll)(c0 + k) * F.ld + r0 + i] : T(0);
         }
-        for (int e = tid; e < bw * bw; e += 256) sI[e] = Ui[e];
         __syncthreads();
-        const int i = tid & 63, jg = tid >> 6;
-        if (i < nr) {
-            for (int j = jg; j < bw; j += 4) {
+        int woff = 0;
+        for (int pc = 0; pc < np; ++pc) {
+            const int a = q0[pc], b = q0[pc + 1], w = b - a;
+            const T* Ui = W + woff;
+            for (int j = a + g; j < b; j += 4) {       // X_p -= X_<p U_<p,p
                 T acc = T(0);
-                for (int k = 0; k <= j; ++k) acc += sX[k * 64 + i] * sI[j * bw + k];
-                fac[F.loff + (ll)(c0 + j) * F.ld + r0 + i] = acc;
+                for (int k = 0; k < a; ++k) acc += sX[k * 64 + t] * blockA[(ll)j * F.ld + k];
+                sX[j * 64 + t] -= acc;
             }
+            __syncthreads();
+            T out[16];                                  // X_p := X_p Ui_p, columns a+g+4q
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const int j = g + 4 * q;
+                T acc = T(0);
+                if (j < w)
+                    for (int k = 0; k <= j; ++k) acc += sX[(a + k) * 64 + t] * Ui[j * w + k];
+                out[q] = acc;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int q = 0; q < 16; ++q)
+                if (g + 4 * q < w) sX[(a + g + 4 * q) * 64 + t] = out[q];
+            __syncthreads();
+            woff += 2 * w * w;
+        }
+        for (int e = tid; e < 64 * bw; e += 256) {
+            int i = e & 63, k = e >> 6;
+            if (i < nr) fac[F.loff + (ll)(c0 + k) * F.ld + r0 + i] = sX[k * 64 + i];
         }
     } else {
         const bool inner = tile < nL + nUa;
@@ -367,19 +383,46 @@ __global__ void __launch_bounds__(256) k_block_panel(T* fac, const T* inv, Sched
             }
         } else {
             for (int e = tid; e < bw * 64; e += 256) {
-                int c = e % 64, k = e / 64;
+                int c = e & 63, k = e >> 6;
                 sX[k * 64 + c] = c < nc ? fac[F.uoff + (ll)(c0 + k) * F.m + col0 + c] : T(0);
             }
         }
-        for (int e = tid; e < bw * bw; e += 256) sI[e] = Mi[e];
         __syncthreads();
-        const int c = tid & 63, ig = tid >> 6;
-        if (c < nc) {
-            for (int i = ig; i < bw; i += 4) {
+        int woff = 0;
+        for (int pc = 0; pc < np; ++pc) {
+            const int a = q0[pc], b = q0[pc + 1], w = b - a;
+            const T* Li = W + woff + w * w;
+            for (int i = a + g; i < b; i += 4) {       // Y_p -= L_p,<p Y_<p
                 T acc = T(0);
-                for (int k = 0; k < bw; ++k) acc += sI[k * bw + i] * sX[k * 64 + c];
-                if (inner) fac[F.loff + (ll)(col0 + c) * F.ld + c0 + i] = acc;
-                else fac[F.uoff + (ll)(c0 + i) * F.m + col0 + c] = acc;
+                for (int k = 0; k < a; ++k) acc += blockA[(ll)k * F.ld + i] * sX[k * 64 + t];
+                sX[i * 64 + t] -= acc;
+            }
+            __syncthreads();
+            T out[16];                                  // Y_p := Li_p Y_p, rows a+g+4q
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const int i = g + 4 * q;
+                T acc = T(0);
+                if (i < w)
+                    for (int k = 0; k < w; ++k) acc += Li[k * w + i] * sX[(a + k) * 64 + t];
+                out[q] = acc;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int q = 0; q < 16; ++q)
+                if (g + 4 * q < w) sX[(a + g + 4 * q) * 64 + t] = out[q];
+            __syncthreads();
+            woff += 2 * w * w;
+        }
+        if (inner) {
+            for (int e = tid; e < bw * 64; e += 256) {
+                int k = e % bw, c = e / bw;
+                if (c < nc) fac[F.loff + (ll)(col0 + c) * F.ld + c0 + k] = sX[k * 64 + c];
+            }
+        } else {
+            for (int e = tid; e < bw * 64; e += 256) {
+                int c = e & 63, k = e >> 6;
+                if (c < nc) fac[F.uoff + (ll)(c0 + k) * F.m + col0 + c] = sX[k * 64 + c];
             }
         }
     }
@@ -530,8 +573,8 @@ __global__ void __launch_bounds__(256) k_schur(T* fac, Sched S, Launch L) {
 constexpr int TS = 128;
 constexpr int MAXRHS = 16;
 
-// Forward step for block `step`: y_B = Minv * b_B (the interchanges and
-// unit-lower solves of the block's pieces, the reference's _lulsolve! steps,
+// Forward step for block `step`: piece by piece y_p = Li_p (b_p - L_p,<p y_<p)
+// (the interchanges and unit-lower solves of the reference's _lulsolve!,
 // SpkLUFactor.jl:297-321), then every row below the block in the front is
 // updated; rows of R_F are updated with atomics because sibling fronts share
 // them.  b is the running right-hand side, y receives the block's values.
@@ -539,35 +582,44 @@ template <typename T>
 __global__ void __launch_bounds__(TS) k_fwd(const T* fac, const T* inv, T* b, T* y, int n, int nrhs, Sched S,
                                             Launch L, int step) {
     constexpr int BM = BlockMax<T>::value;
-    __shared__ T sb[BM * MAXRHS];
     __shared__ T sy[BM * MAXRHS];
+    __shared__ T st[BM * MAXRHS];
+    __shared__ int q0[BM + 1];
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
     const int blk = F.block0 + step;
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
-    const T* Mi = inv + S.blk_inv[blk];
+    const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
+    const T* blockA = fac + F.loff + (ll)c0 * F.ld + c0;
+    const T* W = inv + S.blk_inv[blk];
     const int tid = threadIdx.x;
+    for (int k = tid; k <= np; k += TS) q0[k] = S.xsuper[p0 + k] - F.f - c0;
     for (int e = tid; e < bw * nrhs; e += TS) {
         int k = e % bw, r = e / bw;
-        sb[r * BM + k] = b[(ll)r * n + F.f + c0 + k];
+        sy[r * BM + k] = b[(ll)r * n + F.f + c0 + k];
     }
     __syncthreads();
-    for (int i = tid; i < bw; i += TS) {
-        T acc[MAXRHS];
-#pragma unroll
-        for (int r = 0; r < MAXRHS; ++r) acc[r] = T(0);
-        for (int k = 0; k < bw; ++k) {
-            const T mk = Mi[(ll)k * bw + i];
-#pragma unroll
-            for (int r = 0; r < MAXRHS; ++r)
-                if (r < nrhs) acc[r] += mk * sb[r * BM + k];
+    int woff = 0;
+    for (int pc = 0; pc < np; ++pc) {
+        const int a = q0[pc], bb = q0[pc + 1], w = bb - a;
+        const T* Li = W + woff + w * w;
+        for (int e = tid; e < w * nrhs; e += TS) {
+            int i = a + e % w, r = e / w;
+            T acc = sy[r * BM + i];
+            for (int k = 0; k < a; ++k) acc -= blockA[(ll)k * F.ld + i] * sy[r * BM + k];
+            st[r * BM + i] = acc;
         }
-#pragma unroll
-        for (int r = 0; r < MAXRHS; ++r)
-            if (r < nrhs) sy[r * BM + i] = acc[r];
+        __syncthreads();
+        for (int e = tid; e < w * nrhs; e += TS) {
+            int i = e % w, r = e / w;
+            T acc = T(0);
+            for (int k = 0; k < w; ++k) acc += Li[k * w + i] * st[r * BM + a + k];
+            sy[r * BM + a + i] = acc;
+        }
+        __syncthreads();
+        woff += 2 * w * w;
     }
-    __syncthreads();
     if (tile == 0)
         for (int e = tid; e < bw * nrhs; e += TS) {
             int k = e % bw, r = e / bw;
@@ -615,42 +667,60 @@ __global__ void __launch_bounds__(TS) k_bwd_u12(const T* fac, T* y, const T* x, 
     }
 }
 
-// Backward, part 2, for the block `step`-th from the last: x_B = Uinv * y_B
-// (the upper solves of the block's pieces, the reference's _luusolve!,
-// SpkLUFactor.jl:350-375), then the update of the front's rows above it.
+// Backward, part 2, for the block `step`-th from the last: piece by piece
+// from the last, x_p = Ui_p (c_p - U_p,>p x_>p) (the reference's upper
+// solves, _luusolve!, SpkLUFactor.jl:350-375), then the update of the
+// front's rows above the block.
 template <typename T>
 __global__ void __launch_bounds__(TS) k_bwd(const T* fac, const T* inv, T* y, T* x, int n, int nrhs, Sched S, Launch L,
                                             int step) {
     constexpr int BM = BlockMax<T>::value;
-    __shared__ T sc[BM * MAXRHS];
     __shared__ T sx[BM * MAXRHS];
+    __shared__ T st[BM * MAXRHS];
+    __shared__ int q0[BM + 1];
+    __shared__ int wo[BM + 1];
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
     const int blk = F.block0 + F.nblocks - 1 - step;
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
-    const T* Ui = inv + S.blk_inv[blk] + (ll)bw * bw;
+    const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
+    const T* blockA = fac + F.loff + (ll)c0 * F.ld + c0;
+    const T* W = inv + S.blk_inv[blk];
     const int tid = threadIdx.x;
+    for (int k = tid; k <= np; k += TS) q0[k] = S.xsuper[p0 + k] - F.f - c0;
+    __syncthreads();
+    if (tid == 0) {
+        int o = 0;
+        for (int pc = 0; pc < np; ++pc) {
+            wo[pc] = o;
+            const int w = q0[pc + 1] - q0[pc];
+            o += 2 * w * w;
+        }
+    }
     for (int e = tid; e < bw * nrhs; e += TS) {
         int k = e % bw, r = e / bw;
-        sc[r * BM + k] = y[(ll)r * n + F.f + c0 + k];
+        sx[r * BM + k] = y[(ll)r * n + F.f + c0 + k];
     }
     __syncthreads();
-    for (int i = tid; i < bw; i += TS) {
-        T acc[MAXRHS];
-#pragma unroll
-        for (int r = 0; r < MAXRHS; ++r) acc[r] = T(0);
-        for (int k = i; k < bw; ++k) {
-            const T uk = Ui[(ll)k * bw + i];
-#pragma unroll
-            for (int r = 0; r < MAXRHS; ++r)
-                if (r < nrhs) acc[r] += uk * sc[r * BM + k];
+    for (int pc = np - 1; pc >= 0; --pc) {
+        const int a = q0[pc], bb = q0[pc + 1], w = bb - a;
+        const T* Ui = W + wo[pc];
+        for (int e = tid; e < w * nrhs; e += TS) {
+            int i = a + e % w, r = e / w;
+            T acc = sx[r * BM + i];
+            for (int k = bb; k < bw; ++k) acc -= blockA[(ll)k * F.ld + i] * sx[r * BM + k];
+            st[r * BM + i] = acc;
         }
-#pragma unroll
-        for (int r = 0; r < MAXRHS; ++r)
-            if (r < nrhs) sx[r * BM + i] = acc[r];
+        __syncthreads();
+        for (int e = tid; e < w * nrhs; e += TS) {
+            int i = e % w, r = e / w;
+            T acc = T(0);
+            for (int k = i; k < w; ++k) acc += Ui[k * w + i] * st[r * BM + a + k];
+            sx[r * BM + a + i] = acc;
+        }
+        __syncthreads();
     }
-    __syncthreads();
     if (tile == 0)
         for (int e = tid; e < bw * nrhs; e += TS) {
             int k = e % bw, r = e / bw;
