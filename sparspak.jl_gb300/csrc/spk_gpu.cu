@@ -60,14 +60,20 @@ struct Plan {
     bool built = false;
     int bmax = 0, bwmax = 1;
     std::vector<int> blk_c0, blk_c1, blk_p0, blk_np;
-    std::vector<ll> blk_inv;
-    ll inv_size = 0;
+    std::vector<ll> blk_inv, blk_inv2;
+    std::vector<int> blk_front;
+    std::vector<int> inv_ids;             // block ids grouped by width class
+    int inv_off[5] = {0, 0, 0, 0, 0};     // class c: inv_ids[inv_off[c] .. inv_off[c+1])
+    ll inv_size = 0, inv2_size = 0;
     std::vector<int> block0, nblocks;     // per front
     std::vector<LevelPlan> levels;
     std::vector<int> sched_ids, sched_prefix;
     spk::DFront* d_fronts = nullptr;
     int *d_blk_c0 = nullptr, *d_blk_c1 = nullptr, *d_blk_p0 = nullptr, *d_blk_np = nullptr;
     ll* d_blk_inv = nullptr;
+    ll* d_blk_inv2 = nullptr;
+    int* d_blk_front = nullptr;
+    int* d_inv_ids = nullptr;
     int *d_sched_ids = nullptr, *d_sched_prefix = nullptr;
     spk::Sched sched{};
 };
@@ -82,7 +88,8 @@ struct HFront {
 template <typename T>
 struct Storage {
     T* d = nullptr;
-    T* inv = nullptr;       // Minv / Uinv of every block
+    T* inv = nullptr;       // the pieces' inverses
+    T* inv2 = nullptr;      // whole-block forward / backward operators
     bool loaded = false;    // values assembled since the last factor
     bool factored = false;
 };
@@ -511,6 +518,9 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax) {
             P.blk_p0.push_back(s);
             P.blk_np.push_back(t - s);
             P.blk_inv.push_back(inv);
+            P.blk_inv2.push_back(P.inv2_size);
+            P.inv2_size += 2 * (ll)bw * bw;
+            P.blk_front.push_back(i);
             for (int q = s; q < t; ++q) inv += 2 * (ll)(h->xs[q + 1] - h->xs[q]) * (h->xs[q + 1] - h->xs[q]);
             P.bwmax = std::max(P.bwmax, bw);
             s = t;
@@ -518,6 +528,17 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax) {
         P.nblocks[i] = (int)P.blk_c0.size() - P.block0[i];
     }
     P.inv_size = inv;
+    {
+        const int lim[4] = {16, 32, 64, 128};
+        for (int c = 0; c < 4; ++c) {
+            P.inv_off[c] = (int)P.inv_ids.size();
+            for (int b = 0; b < (int)P.blk_c0.size(); ++b) {
+                const int bw = P.blk_c1[b] - P.blk_c0[b];
+                if (bw <= lim[c] && (c == 0 || bw > lim[c - 1])) P.inv_ids.push_back(b);
+            }
+        }
+        P.inv_off[4] = (int)P.inv_ids.size();
+    }
     const int nlev = h->nlevels;
     std::vector<std::vector<int>> at(nlev);
     for (int i = 0; i < nfr; ++i) at[h->fronts[i].level].push_back(i);
@@ -644,6 +665,9 @@ static int ensure_plan(spk_handle* h) {
     if ((rc = upload(h, &P.d_blk_p0, P.blk_p0))) return rc;
     if ((rc = upload(h, &P.d_blk_np, P.blk_np))) return rc;
     if ((rc = upload(h, &P.d_blk_inv, P.blk_inv))) return rc;
+    if ((rc = upload(h, &P.d_blk_inv2, P.blk_inv2))) return rc;
+    if ((rc = upload(h, &P.d_blk_front, P.blk_front))) return rc;
+    if ((rc = upload(h, &P.d_inv_ids, P.inv_ids))) return rc;
     if ((rc = upload(h, &P.d_sched_ids, P.sched_ids))) return rc;
     if ((rc = upload(h, &P.d_sched_prefix, P.sched_prefix))) return rc;
     spk::Sched& S = P.sched;
@@ -660,19 +684,22 @@ static int ensure_plan(spk_handle* h) {
     S.blk_p0 = P.d_blk_p0;
     S.blk_np = P.d_blk_np;
     S.blk_inv = P.d_blk_inv;
+    S.blk_inv2 = P.d_blk_inv2;
     const int bw = P.bwmax;
     CU(h, cudaFuncSetAttribute(spk::k_block_lu<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)(sizeof(T) * ((size_t)bw * (bw | 1) + 2 * (size_t)bw * spk::MAXW) +
                                      sizeof(int) * 2 * (spk::BlockMax<T>::value + 1))));
     CU(h, cudaFuncSetAttribute(spk::k_block_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)(sizeof(T) * 64 * (size_t)bw)));
+    CU(h, cudaFuncSetAttribute(spk::k_block_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(sizeof(T) * 3 * (size_t)bw * (bw | 1))));
     P.built = true;
     return SPK_OK;
 }
 
 static void free_plan(Plan& P) {
-    void* ptrs[] = {P.d_fronts, P.d_blk_c0, P.d_blk_c1, P.d_blk_p0, P.d_blk_np, P.d_blk_inv, P.d_sched_ids,
-                    P.d_sched_prefix};
+    void* ptrs[] = {P.d_fronts, P.d_blk_c0, P.d_blk_c1, P.d_blk_p0, P.d_blk_np, P.d_blk_inv, P.d_blk_inv2,
+                    P.d_blk_front, P.d_inv_ids, P.d_sched_ids, P.d_sched_prefix};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     P = Plan();
@@ -692,6 +719,7 @@ static int ensure_storage(spk_handle* h) {
     Storage<T>& S = storage<T>(h);
     if (!S.d) CU(h, cudaMalloc((void**)&S.d, sizeof(T) * std::max<i64>(h->fsize, 1)));
     if (!S.inv) CU(h, cudaMalloc((void**)&S.inv, sizeof(T) * std::max<ll>(h->plan[prec_index<T>()].inv_size, 1)));
+    if (!S.inv2) CU(h, cudaMalloc((void**)&S.inv2, sizeof(T) * std::max<ll>(h->plan[prec_index<T>()].inv2_size, 1)));
     return SPK_OK;
 }
 
@@ -753,6 +781,15 @@ static int factor_launches(spk_handle* h) {
             spk::k_schur<T><<<P.schur.tiles, 256, 0, h->stream>>>(fac, S, launch_of(PL, P.schur));
         }
     }
+    const int lim[4] = {16, 32, 64, 128};
+    for (int c = 0; c < 4; ++c) {
+        const int cnt = PL.inv_off[c + 1] - PL.inv_off[c];
+        if (cnt <= 0) continue;
+        const int bw = std::min(lim[c], PL.bwmax);
+        LaunchScope ls(h, SPK_K_GETRF, 0.0, 0.0);
+        spk::k_block_inv<T><<<cnt, 256, sizeof(T) * 3 * (size_t)bw * (bw | 1), h->stream>>>(
+            fac, inv, storage<T>(h).inv2, S, PL.d_blk_front, PL.d_inv_ids + PL.inv_off[c], bw);
+    }
     CU(h, cudaGetLastError());
     return SPK_OK;
 }
@@ -768,7 +805,7 @@ static int run_factor(spk_handle* h) {
 template <typename T>
 static int run_solve_permuted(spk_handle* h, int nrhs) {
     const T* fac = storage<T>(h).d;
-    const T* inv = storage<T>(h).inv;
+    const T* inv = storage<T>(h).inv2;
     const Plan& PL = h->plan[prec_index<T>()];
     const spk::Sched& S = PL.sched;
     T* b = (T*)h->d_wb;
@@ -1297,7 +1334,7 @@ void spk_destroy(spk_handle* h) {
     free_plan(h->plan[0]);
     free_plan(h->plan[1]);
     void* ptrs[] = {h->d_xs, h->d_rows, h->d_runid, h->d_run_tgt, h->d_run_start, h->d_run_rel,
-                    h->d_rel, h->s64.inv, h->s32.inv, h->d_ipiv, h->d_info, h->d_slot, h->d_aval,
+                    h->d_rel, h->s64.inv, h->s32.inv, h->s64.inv2, h->s32.inv2, h->d_ipiv, h->d_info, h->d_slot, h->d_aval,
                     h->d_rowptr, h->d_col, h->d_src, h->d_rperm, h->d_rinvp, h->s64.d, h->s32.d, h->d_wb,
                     h->d_wy, h->d_wx, h->d_rhs, h->d_x, h->d_r, h->d_sums};
     for (void* p : ptrs)

@@ -66,7 +66,8 @@ struct Sched {
     const int* blk_c1;     // front-local end column of each block
     const int* blk_p0;     // first supernode (0-based) of each block
     const int* blk_np;     // supernodes in the block
-    const ll* blk_inv;     // offset in inv[] of the block's Minv (then Uinv)
+    const ll* blk_inv;     // offset in inv[] of the pieces' inverses
+    const ll* blk_inv2;    // offset in inv2[] of the block's Minv (then Uinv), bw x bw each
 };
 
 // One launch = a list of fronts and the prefix sum of their tile counts.
@@ -284,6 +285,97 @@ __global__ void __launch_bounds__(256) k_block_lu(T* fac, int* ipiv, int* info, 
             if (z) { atomicMin(info, p0 + pc + 1); break; }
         }
     }
+}
+
+// After the factorisation, one CTA per block (all blocks of all fronts in
+// one launch) turns the pieces' inverses into whole-block operators:
+//   Minv rows of piece q = Li_q (E_q - L_q,<q Minv_<q)     (forward, pieces in order)
+//   Uinv rows of piece p = Ui_p (E_p - U_p,>p Uinv_>p)     (backward, pieces reversed)
+// so that a triangular-solve step of the block is one product, Minv * b or
+// Uinv * c.  Both are written column-major (bw x bw) to inv2[].
+// Dynamic shared memory: 3 * bwmax * (bwmax | 1) T's.
+template <typename T>
+__global__ void __launch_bounds__(256) k_block_inv(const T* fac, const T* inv, T* inv2, Sched S, const int* blk_front,
+                                                    const int* blk_ids, int bwmax) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int q0[BlockMax<T>::value + 1];
+    __shared__ int wo[BlockMax<T>::value + 1];
+    const int blk = blk_ids[blockIdx.x];
+    const DFront F = S.fronts[blk_front[blk]];
+    const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0, lda = bw | 1;
+    const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
+    T* A = reinterpret_cast<T*>(smem_raw);        // block, column-major
+    T* M = A + bwmax * (bwmax | 1);               // Minv, row-major (i, j) at i * lda + j
+    T* U = M + bwmax * (bwmax | 1);               // Uinv, row-major
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nw = blockDim.x >> 5;
+    for (int k = tid; k <= np; k += blockDim.x) q0[k] = S.xsuper[p0 + k] - F.f - c0;
+    for (int j = warp; j < bw; j += nw)
+        for (int i = lane; i < bw; i += 32) A[j * lda + i] = fac[F.loff + (ll)(c0 + j) * F.ld + c0 + i];
+    __syncthreads();
+    if (tid == 0) {
+        int o = 0;
+        for (int pc = 0; pc < np; ++pc) {
+            wo[pc] = o;
+            const int w = q0[pc + 1] - q0[pc];
+            o += 2 * w * w;
+        }
+    }
+    __syncthreads();
+    const T* W = inv + S.blk_inv[blk];
+    for (int pc = 0; pc < np; ++pc) {               // forward operator
+        const int a = q0[pc], b = q0[pc + 1], w = b - a;
+        const T* Li = W + wo[pc] + w * w;
+        for (int i = a + warp; i < b; i += nw)      // T = E_q - L_q,<q Minv_<q  (into M rows of q)
+            for (int j = lane; j < bw; j += 32) {
+                T acc = T(i == j);
+                for (int k = 0; k < a; ++k) acc -= A[k * lda + i] * M[k * lda + j];
+                M[i * lda + j] = acc;
+            }
+        __syncthreads();
+        for (int j = tid; j < bw; j += blockDim.x) {   // rows of q := Li_q T, one thread per column
+            T t[64];
+#pragma unroll
+            for (int k = 0; k < 64; ++k) t[k] = k < w ? M[(a + k) * lda + j] : T(0);
+            for (int i = 0; i < w; ++i) {
+                T acc = T(0);
+#pragma unroll
+                for (int k = 0; k < 64; ++k)
+                    if (k < w) acc += Li[k * w + i] * t[k];
+                M[(a + i) * lda + j] = acc;
+            }
+        }
+        __syncthreads();
+    }
+    for (int pc = np - 1; pc >= 0; --pc) {          // backward operator
+        const int a = q0[pc], b = q0[pc + 1], w = b - a;
+        const T* Ui = W + wo[pc];
+        for (int i = a + warp; i < b; i += nw)      // T = E_p - U_p,>p Uinv_>p
+            for (int j = lane; j < bw; j += 32) {
+                T acc = T(i == j);
+                for (int k = b; k < bw; ++k) acc -= A[k * lda + i] * U[k * lda + j];
+                U[i * lda + j] = acc;
+            }
+        __syncthreads();
+        for (int j = tid; j < bw; j += blockDim.x) {
+            T t[64];
+#pragma unroll
+            for (int k = 0; k < 64; ++k) t[k] = k < w ? U[(a + k) * lda + j] : T(0);
+            for (int i = 0; i < w; ++i) {
+                T acc = T(0);
+#pragma unroll
+                for (int k = 0; k < 64; ++k)
+                    if (k >= i && k < w) acc += Ui[k * w + i] * t[k];
+                U[(a + i) * lda + j] = acc;
+            }
+        }
+        __syncthreads();
+    }
+    T* out = inv2 + S.blk_inv2[blk];
+    for (int j = warp; j < bw; j += nw)
+        for (int i = lane; i < bw; i += 32) {
+            out[(ll)j * bw + i] = M[i * lda + j];
+            out[(ll)bw * bw + (ll)j * bw + i] = U[i * lda + j];
+        }
 }
 
 // ---------------------------------------------------------------------------
@@ -573,53 +665,45 @@ __global__ void __launch_bounds__(256) k_schur(T* fac, Sched S, Launch L) {
 constexpr int TS = 128;
 constexpr int MAXRHS = 16;
 
-// Forward step for block `step`: piece by piece y_p = Li_p (b_p - L_p,<p y_<p)
-// (the interchanges and unit-lower solves of the reference's _lulsolve!,
+// Forward step for block `step`: y_B = Minv b_B (the interchanges and
+// unit-lower solves of the block's pieces, the reference's _lulsolve!,
 // SpkLUFactor.jl:297-321), then every row below the block in the front is
 // updated; rows of R_F are updated with atomics because sibling fronts share
 // them.  b is the running right-hand side, y receives the block's values.
 template <typename T>
-__global__ void __launch_bounds__(TS) k_fwd(const T* fac, const T* inv, T* b, T* y, int n, int nrhs, Sched S,
+__global__ void __launch_bounds__(TS) k_fwd(const T* fac, const T* inv2, T* b, T* y, int n, int nrhs, Sched S,
                                             Launch L, int step) {
     constexpr int BM = BlockMax<T>::value;
+    __shared__ T sb[BM * MAXRHS];
     __shared__ T sy[BM * MAXRHS];
-    __shared__ T st[BM * MAXRHS];
-    __shared__ int q0[BM + 1];
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
     const int blk = F.block0 + step;
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
-    const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
-    const T* blockA = fac + F.loff + (ll)c0 * F.ld + c0;
-    const T* W = inv + S.blk_inv[blk];
+    const T* Mi = inv2 + S.blk_inv2[blk];
     const int tid = threadIdx.x;
-    for (int k = tid; k <= np; k += TS) q0[k] = S.xsuper[p0 + k] - F.f - c0;
     for (int e = tid; e < bw * nrhs; e += TS) {
         int k = e % bw, r = e / bw;
-        sy[r * BM + k] = b[(ll)r * n + F.f + c0 + k];
+        sb[r * BM + k] = b[(ll)r * n + F.f + c0 + k];
     }
     __syncthreads();
-    int woff = 0;
-    for (int pc = 0; pc < np; ++pc) {
-        const int a = q0[pc], bb = q0[pc + 1], w = bb - a;
-        const T* Li = W + woff + w * w;
-        for (int e = tid; e < w * nrhs; e += TS) {
-            int i = a + e % w, r = e / w;
-            T acc = sy[r * BM + i];
-            for (int k = 0; k < a; ++k) acc -= blockA[(ll)k * F.ld + i] * sy[r * BM + k];
-            st[r * BM + i] = acc;
+    for (int i = tid; i < bw; i += TS) {
+        T acc[MAXRHS];
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r) acc[r] = T(0);
+#pragma unroll 4
+        for (int k = 0; k < bw; ++k) {
+            const T mk = Mi[(ll)k * bw + i];
+#pragma unroll
+            for (int r = 0; r < MAXRHS; ++r)
+                if (r < nrhs) acc[r] += mk * sb[r * BM + k];
         }
-        __syncthreads();
-        for (int e = tid; e < w * nrhs; e += TS) {
-            int i = e % w, r = e / w;
-            T acc = T(0);
-            for (int k = 0; k < w; ++k) acc += Li[k * w + i] * st[r * BM + a + k];
-            sy[r * BM + a + i] = acc;
-        }
-        __syncthreads();
-        woff += 2 * w * w;
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r)
+            if (r < nrhs) sy[r * BM + i] = acc[r];
     }
+    __syncthreads();
     if (tile == 0)
         for (int e = tid; e < bw * nrhs; e += TS) {
             int k = e % bw, r = e / bw;
@@ -667,60 +751,43 @@ __global__ void __launch_bounds__(TS) k_bwd_u12(const T* fac, T* y, const T* x, 
     }
 }
 
-// Backward, part 2, for the block `step`-th from the last: piece by piece
-// from the last, x_p = Ui_p (c_p - U_p,>p x_>p) (the reference's upper
-// solves, _luusolve!, SpkLUFactor.jl:350-375), then the update of the
-// front's rows above the block.
+// Backward, part 2, for the block `step`-th from the last: x_B = Uinv c_B
+// (the upper solves of the block's pieces, the reference's _luusolve!,
+// SpkLUFactor.jl:350-375), then the update of the front's rows above it.
 template <typename T>
-__global__ void __launch_bounds__(TS) k_bwd(const T* fac, const T* inv, T* y, T* x, int n, int nrhs, Sched S, Launch L,
-                                            int step) {
+__global__ void __launch_bounds__(TS) k_bwd(const T* fac, const T* inv2, T* y, T* x, int n, int nrhs, Sched S,
+                                            Launch L, int step) {
     constexpr int BM = BlockMax<T>::value;
+    __shared__ T sc[BM * MAXRHS];
     __shared__ T sx[BM * MAXRHS];
-    __shared__ T st[BM * MAXRHS];
-    __shared__ int q0[BM + 1];
-    __shared__ int wo[BM + 1];
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
     const int blk = F.block0 + F.nblocks - 1 - step;
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
-    const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
-    const T* blockA = fac + F.loff + (ll)c0 * F.ld + c0;
-    const T* W = inv + S.blk_inv[blk];
+    const T* Ui = inv2 + S.blk_inv2[blk] + (ll)bw * bw;
     const int tid = threadIdx.x;
-    for (int k = tid; k <= np; k += TS) q0[k] = S.xsuper[p0 + k] - F.f - c0;
-    __syncthreads();
-    if (tid == 0) {
-        int o = 0;
-        for (int pc = 0; pc < np; ++pc) {
-            wo[pc] = o;
-            const int w = q0[pc + 1] - q0[pc];
-            o += 2 * w * w;
-        }
-    }
     for (int e = tid; e < bw * nrhs; e += TS) {
         int k = e % bw, r = e / bw;
-        sx[r * BM + k] = y[(ll)r * n + F.f + c0 + k];
+        sc[r * BM + k] = y[(ll)r * n + F.f + c0 + k];
     }
     __syncthreads();
-    for (int pc = np - 1; pc >= 0; --pc) {
-        const int a = q0[pc], bb = q0[pc + 1], w = bb - a;
-        const T* Ui = W + wo[pc];
-        for (int e = tid; e < w * nrhs; e += TS) {
-            int i = a + e % w, r = e / w;
-            T acc = sx[r * BM + i];
-            for (int k = bb; k < bw; ++k) acc -= blockA[(ll)k * F.ld + i] * sx[r * BM + k];
-            st[r * BM + i] = acc;
+    for (int i = tid; i < bw; i += TS) {
+        T acc[MAXRHS];
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r) acc[r] = T(0);
+#pragma unroll 4
+        for (int k = i; k < bw; ++k) {
+            const T uk = Ui[(ll)k * bw + i];
+#pragma unroll
+            for (int r = 0; r < MAXRHS; ++r)
+                if (r < nrhs) acc[r] += uk * sc[r * BM + k];
         }
-        __syncthreads();
-        for (int e = tid; e < w * nrhs; e += TS) {
-            int i = e % w, r = e / w;
-            T acc = T(0);
-            for (int k = i; k < w; ++k) acc += Ui[k * w + i] * st[r * BM + a + k];
-            sx[r * BM + a + i] = acc;
-        }
-        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r)
+            if (r < nrhs) sx[r * BM + i] = acc[r];
     }
+    __syncthreads();
     if (tile == 0)
         for (int e = tid; e < bw * nrhs; e += TS) {
             int k = e % bw, r = e / bw;
