@@ -48,6 +48,9 @@ def parse():
     ap.add_argument("--grid", type=int, default=64)
     ap.add_argument("--nrhs", type=int, default=4)
     ap.add_argument("--sample-grid", type=int, default=32, help="grid of the CPU baseline's bounded sample")
+    ap.add_argument("--one-step", action="store_true",
+                    help="profiling aid: one warm-up step, then exactly one mixed step, no other work")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"], help="precision of --one-step")
     return ap.parse_args()
 
 
@@ -257,6 +260,15 @@ def run_ours(args):
         barrier()
         return e0.elapsed_time(e1) / reps, out
 
+    if args.one_step:
+        step(args.precision)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        it, rr = step(args.precision)
+        torch.cuda.synchronize(dev)
+        print(json.dumps({"one_step_ms": (time.perf_counter() - t0) * 1e3, "precision": args.precision,
+                          "corrections": it, "relres": rr, "grid": k}))
+        return
     for _ in range(args.warmup):
         step("fp32")
     # which kernel class dominates the mixed step (one untimed step, every launch timed)
