@@ -576,13 +576,13 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax) {
                 const double area = (double)(ld - c1) * (F.nf - c1) + (double)(F.nf - c1) * F.m;
                 ft[k] = 2.0 * bw * area;
                 wt[k] = 2.0 * area + bw * (rowsL + colsU);
-                tf[k] = std::max(1, cdiv(ld - c1, spk::TS));
+                tf[k] = std::max(1, cdiv(ld - c1, spk::TS)) * cdiv(c1 - c0, spk::SC);
                 ff[k] = 2.0 * bw * bw + 2.0 * bw * rowsL;
                 wf[k] = bw * bw + bw * rowsL;
                 const int rb = P.block0[ids[k]] + nb - 1 - t;
                 const int r0 = P.blk_c0[rb];
                 const double rbw = P.blk_c1[rb] - r0;
-                tb[k] = std::max(1, cdiv(r0, spk::TS));
+                tb[k] = std::max(1, cdiv(r0, spk::TS)) * cdiv((int)rbw, spk::SC);
                 fb[k] = rbw * rbw + 2.0 * rbw * r0;
                 wb[k] = 0.5 * rbw * rbw + rbw * r0;
             }

@@ -665,22 +665,28 @@ __global__ void __launch_bounds__(256) k_schur(T* fac, Sched S, Launch L) {
 constexpr int TS = 128;
 constexpr int MAXRHS = 16;
 
-// Forward step for block `step`: y_B = Minv b_B (the interchanges and
-// unit-lower solves of the block's pieces, the reference's _lulsolve!,
-// SpkLUFactor.jl:297-321), then every row below the block in the front is
-// updated; rows of R_F are updated with atomics because sibling fronts share
-// them.  b is the running right-hand side, y receives the block's values.
+// Forward step for block `step`, tiled as (128 rows below the block) x (32
+// columns of the block): a tile computes its 32 values of y_B = Minv b_B
+// (the interchanges and unit-lower solves of the block's pieces, the
+// reference's _lulsolve!, SpkLUFactor.jl:297-321), the first row tile stores
+// them, and every tile subtracts L[rows, chunk] y_chunk from its rows with
+// atomics (column chunks and sibling fronts share rows).  b is the running
+// right-hand side, y receives the block's values.
+constexpr int SC = 32;   // block columns per solve tile
 template <typename T>
 __global__ void __launch_bounds__(TS) k_fwd(const T* fac, const T* inv2, T* b, T* y, int n, int nrhs, Sched S,
                                             Launch L, int step) {
     constexpr int BM = BlockMax<T>::value;
     __shared__ T sb[BM * MAXRHS];
-    __shared__ T sy[BM * MAXRHS];
+    __shared__ T sp[4 * SC * MAXRHS];
+    __shared__ T sy[SC * MAXRHS];
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
     const int blk = F.block0 + step;
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
+    const int ncc = cdiv(bw, SC), cc = tile % ncc, rt = tile / ncc;
+    const int j0 = cc * SC, nj = min(SC, bw - j0);
     const T* Mi = inv2 + S.blk_inv2[blk];
     const int tid = threadIdx.x;
     for (int e = tid; e < bw * nrhs; e += TS) {
@@ -688,46 +694,50 @@ __global__ void __launch_bounds__(TS) k_fwd(const T* fac, const T* inv2, T* b, T
         sb[r * BM + k] = b[(ll)r * n + F.f + c0 + k];
     }
     __syncthreads();
-    for (int i = tid; i < bw; i += TS) {
+    {   // y_chunk = Minv[j0:j0+nj, :] b_B : 32 columns x 4 partial sums over k
+        const int j = tid & 31, kq = tid >> 5;
         T acc[MAXRHS];
 #pragma unroll
         for (int r = 0; r < MAXRHS; ++r) acc[r] = T(0);
-#pragma unroll 4
-        for (int k = 0; k < bw; ++k) {
-            const T mk = Mi[(ll)k * bw + i];
+        if (j < nj) {
+#pragma unroll 8
+            for (int k = kq; k < bw; k += 4) {
+                const T mk = Mi[(ll)k * bw + j0 + j];
 #pragma unroll
-            for (int r = 0; r < MAXRHS; ++r)
-                if (r < nrhs) acc[r] += mk * sb[r * BM + k];
+                for (int r = 0; r < MAXRHS; ++r)
+                    if (r < nrhs) acc[r] += mk * sb[r * BM + k];
+            }
         }
 #pragma unroll
         for (int r = 0; r < MAXRHS; ++r)
-            if (r < nrhs) sy[r * BM + i] = acc[r];
+            if (r < nrhs) sp[(kq * MAXRHS + r) * SC + j] = acc[r];
     }
     __syncthreads();
-    if (tile == 0)
-        for (int e = tid; e < bw * nrhs; e += TS) {
-            int k = e % bw, r = e / bw;
-            y[(ll)r * n + F.f + c0 + k] = sy[r * BM + k];
+    for (int e = tid; e < SC * nrhs; e += TS) {
+        int j = e % SC, r = e / SC;
+        sy[r * SC + j] = sp[(0 * MAXRHS + r) * SC + j] + sp[(1 * MAXRHS + r) * SC + j] +
+                         sp[(2 * MAXRHS + r) * SC + j] + sp[(3 * MAXRHS + r) * SC + j];
+    }
+    __syncthreads();
+    if (rt == 0)
+        for (int e = tid; e < nj * nrhs; e += TS) {
+            int j = e % nj, r = e / nj;
+            y[(ll)r * n + F.f + c0 + j0 + j] = sy[r * SC + j];
         }
-    const int row = c1 + tile * TS + tid;
+    const int row = c1 + rt * TS + tid;
     if (row < F.ld) {
         const int grow = row < F.nf ? F.f + row : S.rows[F.rows_off + row - F.nf];
-        T acc[MAXRHS];
+        T lv[SC];
+        const T* lcol = fac + F.loff + (ll)(c0 + j0) * F.ld + row;
 #pragma unroll
-        for (int r = 0; r < MAXRHS; ++r) acc[r] = T(0);
-        const T* lcol = fac + F.loff + (ll)c0 * F.ld + row;
-#pragma unroll 4
-        for (int k = 0; k < bw; ++k) {
-            const T l = lcol[(ll)k * F.ld];
-#pragma unroll
-            for (int r = 0; r < MAXRHS; ++r)
-                if (r < nrhs) acc[r] += l * sy[r * BM + k];
-        }
+        for (int j = 0; j < SC; ++j) lv[j] = j < nj ? lcol[(ll)j * F.ld] : T(0);
 #pragma unroll
         for (int r = 0; r < MAXRHS; ++r) {
             if (r >= nrhs) break;
-            if (row < F.nf) b[(ll)r * n + grow] -= acc[r];
-            else atomicAdd(&b[(ll)r * n + grow], -acc[r]);
+            T acc = T(0);
+#pragma unroll
+            for (int j = 0; j < SC; ++j) acc += lv[j] * sy[r * SC + j];
+            atomicAdd(&b[(ll)r * n + grow], -acc);
         }
     }
 }
@@ -743,6 +753,7 @@ __global__ void __launch_bounds__(TS) k_bwd_u12(const T* fac, T* y, const T* x, 
     if (i >= F.nf) return;
     for (int r = 0; r < nrhs; ++r) {
         T acc = T(0);
+#pragma unroll 8
         for (int c = lane; c < F.m; c += 32)
             acc += fac[F.uoff + (ll)i * F.m + c] * x[(ll)r * n + S.rows[F.rows_off + c]];
 #pragma unroll
@@ -751,20 +762,25 @@ __global__ void __launch_bounds__(TS) k_bwd_u12(const T* fac, T* y, const T* x, 
     }
 }
 
-// Backward, part 2, for the block `step`-th from the last: x_B = Uinv c_B
+// Backward, part 2, for the block `step`-th from the last, tiled as (128
+// rows above the block) x (32 block columns): x_chunk = Uinv[chunk, :] c_B
 // (the upper solves of the block's pieces, the reference's _luusolve!,
-// SpkLUFactor.jl:350-375), then the update of the front's rows above it.
+// SpkLUFactor.jl:350-375), stored by the first row tile, then the rows
+// above get U[rows, chunk] x_chunk subtracted (atomics across chunks).
 template <typename T>
 __global__ void __launch_bounds__(TS) k_bwd(const T* fac, const T* inv2, T* y, T* x, int n, int nrhs, Sched S,
                                             Launch L, int step) {
     constexpr int BM = BlockMax<T>::value;
     __shared__ T sc[BM * MAXRHS];
-    __shared__ T sx[BM * MAXRHS];
+    __shared__ T sp[4 * SC * MAXRHS];
+    __shared__ T sx[SC * MAXRHS];
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
     const int blk = F.block0 + F.nblocks - 1 - step;
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
+    const int ncc = cdiv(bw, SC), cc = tile % ncc, rt = tile / ncc;
+    const int j0 = cc * SC, nj = min(SC, bw - j0);
     const T* Ui = inv2 + S.blk_inv2[blk] + (ll)bw * bw;
     const int tid = threadIdx.x;
     for (int e = tid; e < bw * nrhs; e += TS) {
@@ -772,43 +788,51 @@ __global__ void __launch_bounds__(TS) k_bwd(const T* fac, const T* inv2, T* y, T
         sc[r * BM + k] = y[(ll)r * n + F.f + c0 + k];
     }
     __syncthreads();
-    for (int i = tid; i < bw; i += TS) {
+    {   // x_chunk = Uinv[j0:j0+nj, :] c_B (upper: k >= j)
+        const int j = tid & 31, kq = tid >> 5;
         T acc[MAXRHS];
 #pragma unroll
         for (int r = 0; r < MAXRHS; ++r) acc[r] = T(0);
-#pragma unroll 4
-        for (int k = i; k < bw; ++k) {
-            const T uk = Ui[(ll)k * bw + i];
+        if (j < nj) {
+            const int kstart = j0 + j;
+#pragma unroll 8
+            for (int k = kstart + kq; k < bw; k += 4) {
+                const T uk = Ui[(ll)k * bw + j0 + j];
 #pragma unroll
-            for (int r = 0; r < MAXRHS; ++r)
-                if (r < nrhs) acc[r] += uk * sc[r * BM + k];
+                for (int r = 0; r < MAXRHS; ++r)
+                    if (r < nrhs) acc[r] += uk * sc[r * BM + k];
+            }
         }
 #pragma unroll
         for (int r = 0; r < MAXRHS; ++r)
-            if (r < nrhs) sx[r * BM + i] = acc[r];
+            if (r < nrhs) sp[(kq * MAXRHS + r) * SC + j] = acc[r];
     }
     __syncthreads();
-    if (tile == 0)
-        for (int e = tid; e < bw * nrhs; e += TS) {
-            int k = e % bw, r = e / bw;
-            x[(ll)r * n + F.f + c0 + k] = sx[r * BM + k];
+    for (int e = tid; e < SC * nrhs; e += TS) {
+        int j = e % SC, r = e / SC;
+        sx[r * SC + j] = sp[(0 * MAXRHS + r) * SC + j] + sp[(1 * MAXRHS + r) * SC + j] +
+                         sp[(2 * MAXRHS + r) * SC + j] + sp[(3 * MAXRHS + r) * SC + j];
+    }
+    __syncthreads();
+    if (rt == 0)
+        for (int e = tid; e < nj * nrhs; e += TS) {
+            int j = e % nj, r = e / nj;
+            x[(ll)r * n + F.f + c0 + j0 + j] = sx[r * SC + j];
         }
-    const int row = tile * TS + tid;
+    const int row = rt * TS + tid;
     if (row < c0) {
-        T acc[MAXRHS];
+        T uv[SC];
+        const T* ucol = fac + F.loff + (ll)(c0 + j0) * F.ld + row;
 #pragma unroll
-        for (int r = 0; r < MAXRHS; ++r) acc[r] = T(0);
-        const T* ucol = fac + F.loff + (ll)c0 * F.ld + row;
-#pragma unroll 4
-        for (int k = 0; k < bw; ++k) {
-            const T u = ucol[(ll)k * F.ld];
+        for (int j = 0; j < SC; ++j) uv[j] = j < nj ? ucol[(ll)j * F.ld] : T(0);
 #pragma unroll
-            for (int r = 0; r < MAXRHS; ++r)
-                if (r < nrhs) acc[r] += u * sx[r * BM + k];
+        for (int r = 0; r < MAXRHS; ++r) {
+            if (r >= nrhs) break;
+            T acc = T(0);
+#pragma unroll
+            for (int j = 0; j < SC; ++j) acc += uv[j] * sx[r * SC + j];
+            atomicAdd(&y[(ll)r * n + F.f + row], -acc);
         }
-#pragma unroll
-        for (int r = 0; r < MAXRHS; ++r)
-            if (r < nrhs) y[(ll)r * n + F.f + row] -= acc[r];
     }
 }
 
