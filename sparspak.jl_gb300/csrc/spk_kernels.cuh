@@ -198,6 +198,115 @@ __device__ void piece_inverses(const T* A, int lda, int w, const int* piv, T* Ui
     }
 }
 
+// A piece of at most 32 columns factored and inverted by one warp in
+// registers, lane i holding row i of the w x w diagonal block:
+// ggetrf! (first strict maximum, interchanges of whole rows, scaling,
+// rank-1 updates), then Ui = U^{-1} (trsm 'l','u','n','n' on the identity)
+// and Li = L^{-1} P (laswp then trsm 'l','l','n','u' on the identity), lane j
+// forming column j of each.  A is read and written back; piv[k] is local.
+template <typename T>
+__device__ bool warp_piece32(T* A, int lda, int w, int* piv, T* Ui, T* Li) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    T r[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) r[j] = (lane < w && j < w) ? A[j * lda + lane] : T(0);
+    bool sing = false;
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+        if (k < w) {
+            const bool cand = lane >= k && lane < w;
+            const double v = (double)tabs(r[k]);
+            double key = cand ? ((v != v) ? (lane == k ? __longlong_as_double(0x7ff0000000000000LL) : -1.0) : v) : -2.0;
+            int idx = cand ? lane : 64;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const double k2 = __shfl_xor_sync(FULL, key, off);
+                const int i2 = __shfl_xor_sync(FULL, idx, off);
+                if (k2 > key || (k2 == key && i2 < idx)) { key = k2; idx = i2; }
+            }
+            const int kp = idx;
+            if (lane == 0) piv[k] = kp;
+            const T pv = __shfl_sync(FULL, r[k], kp);
+            if (pv != T(0)) {
+                if (kp != k) {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        const T vk = __shfl_sync(FULL, r[j], k), vp = __shfl_sync(FULL, r[j], kp);
+                        if (lane == k) r[j] = vp;
+                        else if (lane == kp) r[j] = vk;
+                    }
+                }
+                const T inv = T(1) / pv;
+                if (lane > k && lane < w) r[k] *= inv;
+            } else {
+                sing = true;
+            }
+#pragma unroll
+            for (int j = k + 1; j < 32; ++j) {
+                const T u = __shfl_sync(FULL, r[j], k);
+                if (lane > k && lane < w) r[j] -= r[k] * u;
+            }
+        }
+    }
+    if (lane < w) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            if (j < w) A[j * lda + lane] = r[j];
+    }
+    __syncwarp();
+    T x[32];
+    // Ui, column j = lane
+#pragma unroll
+    for (int i = 0; i < 32; ++i) x[i] = T(i == lane);
+#pragma unroll
+    for (int k = 31; k >= 0; --k) {
+        if (k < w) {
+            const T ukk = __shfl_sync(FULL, r[k], k);
+            T xk = x[k];
+            const bool nz = xk != T(0);
+            if (nz) { xk /= ukk; x[k] = xk; }
+#pragma unroll
+            for (int i = 0; i < k; ++i) {
+                const T uik = __shfl_sync(FULL, r[k], i);
+                if (nz) x[i] -= xk * uik;
+            }
+        }
+    }
+    if (lane < w) {
+#pragma unroll
+        for (int i = 0; i < 32; ++i)
+            if (i < w) Ui[lane * w + i] = x[i];
+    }
+    // Li, column j = lane: the interchanges move e_j to e_pos
+    int pos = lane;
+    for (int k = 0; k < w; ++k) {
+        const int kp = piv[k];
+        if (pos == k) pos = kp;
+        else if (pos == kp) pos = k;
+    }
+#pragma unroll
+    for (int i = 0; i < 32; ++i) x[i] = T(i == pos);
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+        if (k < w) {
+            const T xk = x[k];
+            const bool nz = xk != T(0);
+#pragma unroll
+            for (int i = k + 1; i < 32; ++i) {
+                const T lik = __shfl_sync(FULL, r[k], i);
+                if (nz && i < w) x[i] -= xk * lik;
+            }
+        }
+    }
+    if (lane < w) {
+#pragma unroll
+        for (int i = 0; i < 32; ++i)
+            if (i < w) Li[lane * w + i] = x[i];
+    }
+    return sing;
+}
+
 // One CTA (256 threads) per front: factor block `step` of the front in shared
 // memory, write it back with its pivots and the pieces' inverses.
 // Dynamic shared memory: bwmax * (bwmax | 1) + 2 * bwmax * MAXW T's, and
@@ -221,20 +330,30 @@ __global__ void __launch_bounds__(256) k_block_lu(T* fac, int* ipiv, int* info, 
     const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
     if (tid == 0) ssing = 0;
     for (int k = tid; k <= np; k += nt) q0[k] = S.xsuper[p0 + k] - F.f - c0;
-    for (int j = warp; j < bw; j += nw)
-        for (int i = lane; i < bw; i += 32) A[j * lda + i] = fac[F.loff + (ll)(c0 + j) * F.ld + c0 + i];
+#pragma unroll 4
+    for (int j = warp; j < bw; j += nw) {
+        const T* src = fac + F.loff + (ll)(c0 + j) * F.ld + c0;
+#pragma unroll
+        for (int q = 0; q < BlockMax<T>::value / 32; ++q) {
+            const int i = lane + 32 * q;
+            if (i < bw) A[j * lda + i] = src[i];
+        }
+    }
     __syncthreads();
     int woff = 0;
     for (int pc = 0; pc < np; ++pc) {
         const int a = q0[pc], b = q0[pc + 1], w = b - a;
         T* Ui = W + woff;
         T* Li = Ui + w * w;
-        if (warp == 0) {
-            if (warp_getrf(A + a * lda + a, lda, w, piv + a)) ssing = 1;
+        if (w <= 32) {
+            if (warp == 0 && warp_piece32(A + a * lda + a, lda, w, piv + a, Ui, Li)) ssing = 1;
+            __syncthreads();
+        } else {
+            if (warp == 0 && warp_getrf(A + a * lda + a, lda, w, piv + a)) ssing = 1;
+            __syncthreads();
+            piece_inverses(A + a * lda + a, lda, w, piv + a, Ui, Li);
+            __syncthreads();
         }
-        __syncthreads();
-        piece_inverses(A + a * lda + a, lda, w, piv + a, Ui, Li);
-        __syncthreads();
         if (b < bw) {
             // U panel to the right inside the block: Y := Li * Y (interchanges + unit-lower
             // solve); L panel below: X := X * Ui.  Both read the pre-solve values, so
