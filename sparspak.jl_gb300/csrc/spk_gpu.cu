@@ -762,8 +762,12 @@ static int factor_launches(spk_handle* h) {
             const size_t panel_smem = sizeof(T) * 64 * (size_t)bw;
             if (P.blu[t].tiles > 0) {
                 LaunchScope ls(h, SPK_K_GETRF, P.blu[t].flops, P.blu[t].words * sizeof(T));
-                spk::k_block_lu<T><<<P.blu[t].tiles, 256, lu_smem, h->stream>>>(fac, h->d_ipiv, h->d_info, inv, S,
-                                                                                 launch_of(PL, P.blu[t]), (int)t, bw);
+                if (bw <= 32)
+                    spk::k_block_lu_small<T><<<(P.blu[t].count + 3) / 4, 128, 0, h->stream>>>(
+                        fac, h->d_ipiv, h->d_info, inv, S, launch_of(PL, P.blu[t]), (int)t);
+                else
+                    spk::k_block_lu<T><<<P.blu[t].tiles, 256, lu_smem, h->stream>>>(
+                        fac, h->d_ipiv, h->d_info, inv, S, launch_of(PL, P.blu[t]), (int)t, bw);
             }
             if (P.bpanel[t].tiles > 0) {
                 LaunchScope ls(h, SPK_K_PANEL, P.bpanel[t].flops, P.bpanel[t].words * sizeof(T));

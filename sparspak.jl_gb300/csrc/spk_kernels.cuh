@@ -198,14 +198,39 @@ __device__ void piece_inverses(const T* A, int lda, int w, const int* piv, T* Ui
     }
 }
 
-// A piece of at most 32 columns factored and inverted by one warp in
-// registers, lane i holding row i of the w x w diagonal block:
-// ggetrf! (first strict maximum, interchanges of whole rows, scaling,
-// rank-1 updates), then Ui = U^{-1} (trsm 'l','u','n','n' on the identity)
-// and Li = L^{-1} P (laswp then trsm 'l','l','n','u' on the identity), lane j
-// forming column j of each.  A is read and written back; piv[k] is local.
+// Order-preserving pivot key of |x| for a candidate row (larger key = larger
+// |x|, all candidates above non-candidates), with the ggetrf! rules: a NaN
+// never wins, except on the diagonal row k, where nothing can displace it.
+__device__ __forceinline__ unsigned long long pivot_key(float x, bool cand, bool diag) {
+    if (!cand) return 0ull;
+    unsigned b = __float_as_uint(x) & 0x7fffffffu;
+    if (b > 0x7f800000u) return diag ? ~0ull : 1ull;   // NaN
+    return (unsigned long long)b + 2ull;
+}
+__device__ __forceinline__ unsigned long long pivot_key(double x, bool cand, bool diag) {
+    if (!cand) return 0ull;
+    unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+    if (b > 0x7ff0000000000000ull) return diag ? ~0ull : 1ull;
+    return b + 2ull;
+}
+
+// First lane holding the largest key (the reference's first strict maximum).
+__device__ __forceinline__ int warp_first_max(unsigned long long key) {
+    const unsigned FULL = 0xffffffffu;
+    const unsigned hi = (unsigned)(key >> 32), lo = (unsigned)key;
+    const unsigned mh = __reduce_max_sync(FULL, hi);
+    const unsigned ml = __reduce_max_sync(FULL, hi == mh ? lo : 0u);
+    const unsigned ballot = __ballot_sync(FULL, hi == mh && lo == ml);
+    return __ffs(ballot) - 1;
+}
+
+// ggetrf! of a piece of at most 32 columns by one warp, lane i holding row
+// i in registers: first strict maximum as pivot, interchange of whole rows,
+// scaling, rank-1 update.  The broadcasts of a pivot row are issued before
+// the FMAs that use them.  A (w x w, column-major, leading dimension lda)
+// is read and written back; piv[k] receives the local pivot row.
 template <typename T>
-__device__ bool warp_piece32(T* A, int lda, int w, int* piv, T* Ui, T* Li) {
+__device__ bool warp_getrf32(T* A, int lda, int w, int* piv) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     T r[32];
@@ -215,26 +240,18 @@ __device__ bool warp_piece32(T* A, int lda, int w, int* piv, T* Ui, T* Li) {
 #pragma unroll
     for (int k = 0; k < 32; ++k) {
         if (k < w) {
-            const bool cand = lane >= k && lane < w;
-            const double v = (double)tabs(r[k]);
-            double key = cand ? ((v != v) ? (lane == k ? __longlong_as_double(0x7ff0000000000000LL) : -1.0) : v) : -2.0;
-            int idx = cand ? lane : 64;
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                const double k2 = __shfl_xor_sync(FULL, key, off);
-                const int i2 = __shfl_xor_sync(FULL, idx, off);
-                if (k2 > key || (k2 == key && i2 < idx)) { key = k2; idx = i2; }
-            }
-            const int kp = idx;
+            const int kp = warp_first_max(pivot_key(r[k], lane >= k && lane < w, lane == k));
             if (lane == 0) piv[k] = kp;
             const T pv = __shfl_sync(FULL, r[k], kp);
             if (pv != T(0)) {
                 if (kp != k) {
+                    T vk[32], vp[32];
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) { vk[j] = __shfl_sync(FULL, r[j], k); vp[j] = __shfl_sync(FULL, r[j], kp); }
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
-                        const T vk = __shfl_sync(FULL, r[j], k), vp = __shfl_sync(FULL, r[j], kp);
-                        if (lane == k) r[j] = vp;
-                        else if (lane == kp) r[j] = vk;
+                        if (lane == k) r[j] = vp[j];
+                        else if (lane == kp) r[j] = vk[j];
                     }
                 }
                 const T inv = T(1) / pv;
@@ -242,10 +259,12 @@ __device__ bool warp_piece32(T* A, int lda, int w, int* piv, T* Ui, T* Li) {
             } else {
                 sing = true;
             }
+            T u[32];
 #pragma unroll
-            for (int j = k + 1; j < 32; ++j) {
-                const T u = __shfl_sync(FULL, r[j], k);
-                if (lane > k && lane < w) r[j] -= r[k] * u;
+            for (int j = k + 1; j < 32; ++j) u[j] = __shfl_sync(FULL, r[j], k);
+            if (lane > k && lane < w) {
+#pragma unroll
+                for (int j = k + 1; j < 32; ++j) r[j] -= r[k] * u[j];
             }
         }
     }
@@ -254,22 +273,34 @@ __device__ bool warp_piece32(T* A, int lda, int w, int* piv, T* Ui, T* Li) {
         for (int j = 0; j < 32; ++j)
             if (j < w) A[j * lda + lane] = r[j];
     }
-    __syncwarp();
+    return sing;
+}
+
+// Ui = U^{-1} of a factored piece (w <= 32) by one warp: trsm 'l','u','n','n'
+// on the identity, lane j forming column j; row k of U broadcast from
+// registers loaded from A.
+template <typename T>
+__device__ void warp_inv_upper32(const T* A, int lda, int w, T* Ui) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    T r[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) r[j] = (lane < w && j < w) ? A[j * lda + lane] : T(0);
     T x[32];
-    // Ui, column j = lane
 #pragma unroll
     for (int i = 0; i < 32; ++i) x[i] = T(i == lane);
 #pragma unroll
     for (int k = 31; k >= 0; --k) {
         if (k < w) {
-            const T ukk = __shfl_sync(FULL, r[k], k);
-            T xk = x[k];
-            const bool nz = xk != T(0);
-            if (nz) { xk /= ukk; x[k] = xk; }
+            T uk[32];
 #pragma unroll
-            for (int i = 0; i < k; ++i) {
-                const T uik = __shfl_sync(FULL, r[k], i);
-                if (nz) x[i] -= xk * uik;
+            for (int i = 0; i <= k; ++i) uk[i] = __shfl_sync(FULL, r[k], i);   // column k of U
+            T xk = x[k];
+            if (xk != T(0)) {
+                xk /= uk[k];
+                x[k] = xk;
+#pragma unroll
+                for (int i = 0; i < k; ++i) x[i] -= xk * uk[i];
             }
         }
     }
@@ -278,24 +309,36 @@ __device__ bool warp_piece32(T* A, int lda, int w, int* piv, T* Ui, T* Li) {
         for (int i = 0; i < 32; ++i)
             if (i < w) Ui[lane * w + i] = x[i];
     }
-    // Li, column j = lane: the interchanges move e_j to e_pos
+}
+
+// Li = L^{-1} P of a factored piece (w <= 32) by one warp: laswp then trsm
+// 'l','l','n','u' on the identity, lane j forming column j.
+template <typename T>
+__device__ void warp_inv_lower32(const T* A, int lda, int w, const int* piv, T* Li) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    T r[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) r[j] = (lane < w && j < w) ? A[j * lda + lane] : T(0);
     int pos = lane;
     for (int k = 0; k < w; ++k) {
         const int kp = piv[k];
         if (pos == k) pos = kp;
         else if (pos == kp) pos = k;
     }
+    T x[32];
 #pragma unroll
     for (int i = 0; i < 32; ++i) x[i] = T(i == pos);
 #pragma unroll
     for (int k = 0; k < 32; ++k) {
         if (k < w) {
-            const T xk = x[k];
-            const bool nz = xk != T(0);
+            T lk[32];
 #pragma unroll
-            for (int i = k + 1; i < 32; ++i) {
-                const T lik = __shfl_sync(FULL, r[k], i);
-                if (nz && i < w) x[i] -= xk * lik;
+            for (int i = k + 1; i < 32; ++i) lk[i] = __shfl_sync(FULL, r[k], i);   // column k of L
+            const T xk = x[k];
+            if (xk != T(0)) {
+#pragma unroll
+                for (int i = k + 1; i < 32; ++i) x[i] -= xk * lk[i];
             }
         }
     }
@@ -304,7 +347,111 @@ __device__ bool warp_piece32(T* A, int lda, int w, int* piv, T* Ui, T* Li) {
         for (int i = 0; i < 32; ++i)
             if (i < w) Li[lane * w + i] = x[i];
     }
+}
+
+// A whole block of at most 32 columns factored by one warp in registers
+// (lane i holds row i) as one right-looking sweep over its columns.  For
+// column k in piece [a, b): the pivot is the first strict maximum among rows
+// [k, b) (ggetrf!), the interchange moves whole rows over columns [a, bw)
+// (the piece's own columns, then _luswap! of its U rows), column k is scaled
+// below the diagonal (ggetrf! scaling for rows in the piece, the L-panel
+// trsm 'r','u','n','n' for rows below it) and the rank-1 update covers rows
+// and columns after k (ggetrf!, the U-panel trsm 'r','l','t','u' and the
+// block-local update).  Columns left of the piece are never interchanged.
+template <typename T>
+__device__ bool warp_block_lu32(T* A, int lda, int bw, const int* q0, int np, int* piv) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    T r[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) r[j] = (lane < bw && j < bw) ? A[j * lda + lane] : T(0);
+    bool sing = false;
+    int pc = 0;
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+        if (k < bw) {
+            while (q0[pc + 1] <= k) ++pc;
+            const int a = q0[pc], b = q0[pc + 1];
+            const int kp = warp_first_max(pivot_key(r[k], lane >= k && lane < b, lane == k));
+            if (lane == 0) piv[k] = kp - a;
+            const T pv = __shfl_sync(FULL, r[k], kp);
+            if (pv != T(0)) {
+                if (kp != k) {
+                    T vk[32], vp[32];
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) { vk[j] = __shfl_sync(FULL, r[j], k); vp[j] = __shfl_sync(FULL, r[j], kp); }
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        if (j >= a) {
+                            if (lane == k) r[j] = vp[j];
+                            else if (lane == kp) r[j] = vk[j];
+                        }
+                    }
+                }
+                const T inv = T(1) / pv;
+                if (lane > k && lane < bw) r[k] *= inv;
+            } else {
+                sing = true;
+            }
+            T u[32];
+#pragma unroll
+            for (int j = k + 1; j < 32; ++j) u[j] = __shfl_sync(FULL, r[j], k);
+            if (lane > k && lane < bw) {
+#pragma unroll
+                for (int j = k + 1; j < 32; ++j) r[j] -= r[k] * u[j];
+            }
+        }
+    }
+    if (lane < bw) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            if (j < bw) A[j * lda + lane] = r[j];
+    }
+    __syncwarp();
     return sing;
+}
+
+// Blocks of at most 32 columns: one warp per block, four blocks per CTA (the
+// launch holds one block per front).  Same outputs as k_block_lu.
+template <typename T>
+__global__ void __launch_bounds__(128) k_block_lu_small(T* fac, int* ipiv, int* info, T* inv, Sched S, Launch L,
+                                                         int step) {
+    __shared__ T sA[4][32 * 33];
+    __shared__ int sq[4][33];
+    __shared__ int spiv[4][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int idx = blockIdx.x * 4 + warp;
+    if (idx >= L.count) return;
+    const DFront F = S.fronts[L.front_ids[idx]];
+    const int blk = F.block0 + step;
+    const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0, lda = 33;
+    const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
+    T* A = sA[warp];
+    int* q0 = sq[warp];
+    int* piv = spiv[warp];
+    for (int k = lane; k <= np; k += 32) q0[k] = S.xsuper[p0 + k] - F.f - c0;
+    for (int j = 0; j < bw; ++j)
+        if (lane < bw) A[j * lda + lane] = fac[F.loff + (ll)(c0 + j) * F.ld + c0 + lane];
+    __syncwarp();
+    const bool sing = warp_block_lu32(A, lda, bw, q0, np, piv);
+    for (int j = 0; j < bw; ++j)
+        if (lane < bw) fac[F.loff + (ll)(c0 + j) * F.ld + c0 + lane] = A[j * lda + lane];
+    if (lane < bw) ipiv[F.f + c0 + lane] = piv[lane];
+    T* out = inv + S.blk_inv[blk];
+    int woff = 0;
+    for (int pc = 0; pc < np; ++pc) {
+        const int a = q0[pc], w = q0[pc + 1] - a;
+        warp_inv_upper32(A + a * lda + a, lda, w, out + woff);
+        warp_inv_lower32(A + a * lda + a, lda, w, piv + a, out + woff + w * w);
+        woff += 2 * w * w;
+    }
+    if (lane == 0 && sing) {   // sing is uniform across the warp
+        for (int pc = 0; pc < np; ++pc) {
+            bool z = false;
+            for (int k = q0[pc]; k < q0[pc + 1]; ++k) z |= A[k * lda + k] == T(0);
+            if (z) { atomicMin(info, p0 + pc + 1); break; }
+        }
+    }
 }
 
 // One CTA (256 threads) per front: factor block `step` of the front in shared
@@ -320,6 +467,7 @@ __global__ void __launch_bounds__(256) k_block_lu(T* fac, int* ipiv, int* info, 
     int* q0 = reinterpret_cast<int*>(W + 2 * bwmax * MAXW);
     int* piv = q0 + BlockMax<T>::value + 1;
     __shared__ int ssing;
+    __shared__ int src[32];
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
@@ -346,49 +494,114 @@ __global__ void __launch_bounds__(256) k_block_lu(T* fac, int* ipiv, int* info, 
         T* Ui = W + woff;
         T* Li = Ui + w * w;
         if (w <= 32) {
-            if (warp == 0 && warp_piece32(A + a * lda + a, lda, w, piv + a, Ui, Li)) ssing = 1;
+            if (warp == 0 && warp_getrf32(A + a * lda + a, lda, w, piv + a)) ssing = 1;
             __syncthreads();
+            if (tid == 0) {                          // the piece's interchanges as a gather map
+                for (int k = 0; k < w; ++k) src[k] = k;
+                for (int k = 0; k < w; ++k) {
+                    const int kp = piv[a + k];
+                    const int t0 = src[k];
+                    src[k] = src[kp];
+                    src[kp] = t0;
+                }
+            }
+            __syncthreads();
+            if (warp == 0) {
+                warp_inv_upper32(A + a * lda + a, lda, w, Ui);
+            } else if (warp == 1) {
+                warp_inv_lower32(A + a * lda + a, lda, w, piv + a, Li);
+            } else if (b < bw) {
+                // warps 2..: U panel to the right inside the block (one thread per
+                // column: _luswap! as a gather, then the unit-lower solve) and L
+                // panel below (one thread per row: X := X * inv(U_pp)), in registers
+                const int ncol = bw - b, nrow = bw - b;
+                for (int t = tid - 64; t < ncol + nrow; t += nt - 64) {
+                    if (t < ncol) {
+                        T* col = A + (b + t) * lda + a;
+                        T y[32];
+#pragma unroll
+                        for (int k = 0; k < 32; ++k) y[k] = k < w ? col[src[k]] : T(0);
+#pragma unroll
+                        for (int k = 0; k < 32; ++k) {
+                            if (k < w) {
+                                const T yk = y[k];
+#pragma unroll
+                                for (int i = k + 1; i < 32; ++i)
+                                    if (i < w) y[i] -= A[(a + k) * lda + a + i] * yk;
+                            }
+                        }
+#pragma unroll
+                        for (int k = 0; k < 32; ++k)
+                            if (k < w) col[k] = y[k];
+                    } else {
+                        const int i = b + (t - ncol);
+                        T x[32];
+#pragma unroll
+                        for (int k = 0; k < 32; ++k) x[k] = k < w ? A[(a + k) * lda + i] : T(0);
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            if (j < w) {
+                                T acc = x[j];
+#pragma unroll
+                                for (int k = 0; k < j; ++k) acc -= A[(a + j) * lda + a + k] * x[k];
+                                x[j] = acc * (T(1) / A[(a + j) * lda + a + j]);
+                            }
+                        }
+#pragma unroll
+                        for (int k = 0; k < 32; ++k)
+                            if (k < w) A[(a + k) * lda + i] = x[k];
+                    }
+                }
+            }
+            __syncthreads();
+            if (b < bw) {
+                for (int j = b + warp; j < bw; j += nw) {   // block-local trailing update
+                    for (int i = b + lane; i < bw; i += 32) {
+                        T acc = T(0);
+                        for (int k = 0; k < w; ++k) acc += A[(a + k) * lda + i] * A[j * lda + a + k];
+                        A[j * lda + i] -= acc;
+                    }
+                }
+                __syncthreads();
+            }
         } else {
             if (warp == 0 && warp_getrf(A + a * lda + a, lda, w, piv + a)) ssing = 1;
             __syncthreads();
             piece_inverses(A + a * lda + a, lda, w, piv + a, Ui, Li);
             __syncthreads();
-        }
-        if (b < bw) {
-            // U panel to the right inside the block: Y := Li * Y (interchanges + unit-lower
-            // solve); L panel below: X := X * Ui.  Both read the pre-solve values, so
-            // go through registers column by column / row by row.
-            for (int j = b + warp; j < bw; j += nw) {
-                T yv[2];
+            if (b < bw) {
+                for (int j = b + warp; j < bw; j += nw) {
+                    T yv[2];
 #pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    const int i = lane + 32 * q;
-                    T acc = T(0);
-                    if (i < w)
-                        for (int k = 0; k < w; ++k) acc += Li[k * w + i] * A[j * lda + a + k];
-                    yv[q] = acc;
-                }
-                __syncwarp();
+                    for (int q = 0; q < 2; ++q) {
+                        const int i = lane + 32 * q;
+                        T acc = T(0);
+                        if (i < w)
+                            for (int k = 0; k < w; ++k) acc += Li[k * w + i] * A[j * lda + a + k];
+                        yv[q] = acc;
+                    }
+                    __syncwarp();
 #pragma unroll
-                for (int q = 0; q < 2; ++q)
-                    if (lane + 32 * q < w) A[j * lda + a + lane + 32 * q] = yv[q];
-            }
-            for (int i = b + tid; i < bw; i += nt) {
-                for (int j = w - 1; j >= 0; --j) {     // output column j needs inputs 0..j only
-                    T acc = T(0);
-                    for (int k = 0; k <= j; ++k) acc += A[(a + k) * lda + i] * Ui[j * w + k];
-                    A[(a + j) * lda + i] = acc;
+                    for (int q = 0; q < 2; ++q)
+                        if (lane + 32 * q < w) A[j * lda + a + lane + 32 * q] = yv[q];
                 }
-            }
-            __syncthreads();
-            for (int j = b + warp; j < bw; j += nw) {   // block-local trailing update
-                for (int i = b + lane; i < bw; i += 32) {
-                    T acc = T(0);
-                    for (int k = 0; k < w; ++k) acc += A[(a + k) * lda + i] * A[j * lda + a + k];
-                    A[j * lda + i] -= acc;
+                for (int i = b + tid; i < bw; i += nt) {
+                    for (int j = w - 1; j >= 0; --j) {
+                        T acc = T(0);
+                        for (int k = 0; k <= j; ++k) acc += A[(a + k) * lda + i] * Ui[j * w + k];
+                        A[(a + j) * lda + i] = acc;
+                    }
                 }
+                __syncthreads();
+                for (int j = b + warp; j < bw; j += nw) {
+                    for (int i = b + lane; i < bw; i += 32) {
+                        T acc = T(0);
+                        for (int k = 0; k < w; ++k) acc += A[(a + k) * lda + i] * A[j * lda + a + k];
+                        A[j * lda + i] -= acc;
+                    }
+                }
+                __syncthreads();
             }
-            __syncthreads();
         }
         woff += 2 * w * w;
     }
