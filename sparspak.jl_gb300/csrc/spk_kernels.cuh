@@ -224,50 +224,82 @@ __device__ __forceinline__ int warp_first_max(unsigned long long key) {
     return __ffs(ballot) - 1;
 }
 
+// r[k] for a runtime k without indexing a register array dynamically.
+template <typename T>
+__device__ __forceinline__ T pick32(const T (&r)[32], int k) {
+    T v = r[0];
+#pragma unroll
+    for (int j = 1; j < 32; ++j)
+        if (j == k) v = r[j];
+    return v;
+}
+
+// One right-looking LU sweep over the columns [0, ncols) of a register block
+// held one row per lane (rows/columns below 32).  For column k in piece
+// [a, b): pivot = first strict maximum among rows [k, b) (ggetrf!), whole
+// rows interchanged over columns [a, 32) (the piece's columns, then
+// _luswap! of its U rows), column k scaled below the diagonal (ggetrf!
+// scaling, and the L-panel trsm 'r','u','n','n' for rows past the piece),
+// rank-1 update of rows and columns after k (ggetrf!, the U-panel trsm
+// 'r','l','t','u' and the block-local update).  `nrows` rows take part.
+template <typename T>
+__device__ bool warp_lu_sweep(T (&r)[32], int nrows, int ncols, const int* q0, int* piv) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    bool sing = false;
+    int pc = 0;
+#pragma unroll 1
+    for (int k = 0; k < ncols; ++k) {
+        while (q0[pc + 1] <= k) ++pc;
+        const int a = q0[pc], b = q0[pc + 1];
+        const T rk0 = pick32(r, k);
+        const int kp = warp_first_max(pivot_key(rk0, lane >= k && lane < b, lane == k));
+        if (lane == 0) piv[k] = kp - a;
+        const T pv = __shfl_sync(FULL, rk0, kp);
+        if (pv != T(0)) {
+            if (kp != k) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const T vk = __shfl_sync(FULL, r[j], k), vp = __shfl_sync(FULL, r[j], kp);
+                    if (j >= a) {
+                        if (lane == k) r[j] = vp;
+                        else if (lane == kp) r[j] = vk;
+                    }
+                }
+            }
+            const T inv = T(1) / pv;
+            if (lane > k && lane < nrows) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    if (j == k) r[j] *= inv;
+            }
+        } else {
+            sing = true;
+        }
+        const T lk = pick32(r, k);
+        T u[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) u[j] = __shfl_sync(FULL, r[j], k);
+        if (lane > k && lane < nrows) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                if (j > k) r[j] -= lk * u[j];
+        }
+    }
+    return sing;
+}
+
 // ggetrf! of a piece of at most 32 columns by one warp, lane i holding row
-// i in registers: first strict maximum as pivot, interchange of whole rows,
-// scaling, rank-1 update.  The broadcasts of a pivot row are issued before
-// the FMAs that use them.  A (w x w, column-major, leading dimension lda)
-// is read and written back; piv[k] receives the local pivot row.
+// i in registers; A (w x w, column-major, leading dimension lda) is read and
+// written back; piv[k] receives the local pivot row.
 template <typename T>
 __device__ bool warp_getrf32(T* A, int lda, int w, int* piv) {
-    const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     T r[32];
 #pragma unroll
     for (int j = 0; j < 32; ++j) r[j] = (lane < w && j < w) ? A[j * lda + lane] : T(0);
-    bool sing = false;
-#pragma unroll
-    for (int k = 0; k < 32; ++k) {
-        if (k < w) {
-            const int kp = warp_first_max(pivot_key(r[k], lane >= k && lane < w, lane == k));
-            if (lane == 0) piv[k] = kp;
-            const T pv = __shfl_sync(FULL, r[k], kp);
-            if (pv != T(0)) {
-                if (kp != k) {
-                    T vk[32], vp[32];
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) { vk[j] = __shfl_sync(FULL, r[j], k); vp[j] = __shfl_sync(FULL, r[j], kp); }
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        if (lane == k) r[j] = vp[j];
-                        else if (lane == kp) r[j] = vk[j];
-                    }
-                }
-                const T inv = T(1) / pv;
-                if (lane > k && lane < w) r[k] *= inv;
-            } else {
-                sing = true;
-            }
-            T u[32];
-#pragma unroll
-            for (int j = k + 1; j < 32; ++j) u[j] = __shfl_sync(FULL, r[j], k);
-            if (lane > k && lane < w) {
-#pragma unroll
-                for (int j = k + 1; j < 32; ++j) r[j] -= r[k] * u[j];
-            }
-        }
-    }
+    const int q0[2] = {0, w};
+    const bool sing = warp_lu_sweep(r, w, w, q0, piv);
     if (lane < w) {
 #pragma unroll
         for (int j = 0; j < 32; ++j)
@@ -277,8 +309,7 @@ __device__ bool warp_getrf32(T* A, int lda, int w, int* piv) {
 }
 
 // Ui = U^{-1} of a factored piece (w <= 32) by one warp: trsm 'l','u','n','n'
-// on the identity, lane j forming column j; row k of U broadcast from
-// registers loaded from A.
+// on the identity, lane j forming column j.
 template <typename T>
 __device__ void warp_inv_upper32(const T* A, int lda, int w, T* Ui) {
     const unsigned FULL = 0xffffffffu;
@@ -289,18 +320,19 @@ __device__ void warp_inv_upper32(const T* A, int lda, int w, T* Ui) {
     T x[32];
 #pragma unroll
     for (int i = 0; i < 32; ++i) x[i] = T(i == lane);
+#pragma unroll 1
+    for (int k = w - 1; k >= 0; --k) {
+        const T rk = pick32(r, k);
+        T uk[32];
 #pragma unroll
-    for (int k = 31; k >= 0; --k) {
-        if (k < w) {
-            T uk[32];
+        for (int i = 0; i < 32; ++i) uk[i] = __shfl_sync(FULL, rk, i);   // column k of U
+        T xk = pick32(x, k);
+        if (xk != T(0)) {
+            xk /= pick32(uk, k);
 #pragma unroll
-            for (int i = 0; i <= k; ++i) uk[i] = __shfl_sync(FULL, r[k], i);   // column k of U
-            T xk = x[k];
-            if (xk != T(0)) {
-                xk /= uk[k];
-                x[k] = xk;
-#pragma unroll
-                for (int i = 0; i < k; ++i) x[i] -= xk * uk[i];
+            for (int i = 0; i < 32; ++i) {
+                if (i == k) x[i] = xk;
+                else if (i < k) x[i] -= xk * uk[i];
             }
         }
     }
@@ -329,17 +361,17 @@ __device__ void warp_inv_lower32(const T* A, int lda, int w, const int* piv, T* 
     T x[32];
 #pragma unroll
     for (int i = 0; i < 32; ++i) x[i] = T(i == pos);
+#pragma unroll 1
+    for (int k = 0; k < w; ++k) {
+        const T rk = pick32(r, k);
+        T lk[32];
 #pragma unroll
-    for (int k = 0; k < 32; ++k) {
-        if (k < w) {
-            T lk[32];
+        for (int i = 0; i < 32; ++i) lk[i] = __shfl_sync(FULL, rk, i);   // column k of L
+        const T xk = pick32(x, k);
+        if (xk != T(0)) {
 #pragma unroll
-            for (int i = k + 1; i < 32; ++i) lk[i] = __shfl_sync(FULL, r[k], i);   // column k of L
-            const T xk = x[k];
-            if (xk != T(0)) {
-#pragma unroll
-                for (int i = k + 1; i < 32; ++i) x[i] -= xk * lk[i];
-            }
+            for (int i = 0; i < 32; ++i)
+                if (i > k && i < w) x[i] -= xk * lk[i];
         }
     }
     if (lane < w) {
@@ -360,48 +392,12 @@ __device__ void warp_inv_lower32(const T* A, int lda, int w, const int* piv, T* 
 // block-local update).  Columns left of the piece are never interchanged.
 template <typename T>
 __device__ bool warp_block_lu32(T* A, int lda, int bw, const int* q0, int np, int* piv) {
-    const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
+    (void)np;
     T r[32];
 #pragma unroll
     for (int j = 0; j < 32; ++j) r[j] = (lane < bw && j < bw) ? A[j * lda + lane] : T(0);
-    bool sing = false;
-    int pc = 0;
-#pragma unroll
-    for (int k = 0; k < 32; ++k) {
-        if (k < bw) {
-            while (q0[pc + 1] <= k) ++pc;
-            const int a = q0[pc], b = q0[pc + 1];
-            const int kp = warp_first_max(pivot_key(r[k], lane >= k && lane < b, lane == k));
-            if (lane == 0) piv[k] = kp - a;
-            const T pv = __shfl_sync(FULL, r[k], kp);
-            if (pv != T(0)) {
-                if (kp != k) {
-                    T vk[32], vp[32];
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) { vk[j] = __shfl_sync(FULL, r[j], k); vp[j] = __shfl_sync(FULL, r[j], kp); }
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        if (j >= a) {
-                            if (lane == k) r[j] = vp[j];
-                            else if (lane == kp) r[j] = vk[j];
-                        }
-                    }
-                }
-                const T inv = T(1) / pv;
-                if (lane > k && lane < bw) r[k] *= inv;
-            } else {
-                sing = true;
-            }
-            T u[32];
-#pragma unroll
-            for (int j = k + 1; j < 32; ++j) u[j] = __shfl_sync(FULL, r[j], k);
-            if (lane > k && lane < bw) {
-#pragma unroll
-                for (int j = k + 1; j < 32; ++j) r[j] -= r[k] * u[j];
-            }
-        }
-    }
+    const bool sing = warp_lu_sweep(r, bw, bw, q0, piv);
     if (lane < bw) {
 #pragma unroll
         for (int j = 0; j < 32; ++j)
@@ -521,14 +517,13 @@ __global__ void __launch_bounds__(256) k_block_lu(T* fac, int* ipiv, int* info, 
                         T y[32];
 #pragma unroll
                         for (int k = 0; k < 32; ++k) y[k] = k < w ? col[src[k]] : T(0);
+#pragma unroll 1
+                        for (int k = 0; k < w; ++k) {
+                            const T yk = pick32(y, k);
+                            const T* lcol = A + (a + k) * lda + a;
 #pragma unroll
-                        for (int k = 0; k < 32; ++k) {
-                            if (k < w) {
-                                const T yk = y[k];
-#pragma unroll
-                                for (int i = k + 1; i < 32; ++i)
-                                    if (i < w) y[i] -= A[(a + k) * lda + a + i] * yk;
-                            }
+                            for (int i = 0; i < 32; ++i)
+                                if (i > k && i < w) y[i] -= lcol[i] * yk;
                         }
 #pragma unroll
                         for (int k = 0; k < 32; ++k)
@@ -538,14 +533,17 @@ __global__ void __launch_bounds__(256) k_block_lu(T* fac, int* ipiv, int* info, 
                         T x[32];
 #pragma unroll
                         for (int k = 0; k < 32; ++k) x[k] = k < w ? A[(a + k) * lda + i] : T(0);
+#pragma unroll 1
+                        for (int j = 0; j < w; ++j) {
+                            const T* ucol = A + (a + j) * lda + a;
+                            T acc = pick32(x, j);
 #pragma unroll
-                        for (int j = 0; j < 32; ++j) {
-                            if (j < w) {
-                                T acc = x[j];
+                            for (int k = 0; k < 32; ++k)
+                                if (k < j) acc -= ucol[k] * x[k];
+                            acc *= T(1) / ucol[j];
 #pragma unroll
-                                for (int k = 0; k < j; ++k) acc -= A[(a + j) * lda + a + k] * x[k];
-                                x[j] = acc * (T(1) / A[(a + j) * lda + a + j]);
-                            }
+                            for (int k = 0; k < 32; ++k)
+                                if (k == j) x[k] = acc;
                         }
 #pragma unroll
                         for (int k = 0; k < 32; ++k)
