@@ -134,6 +134,23 @@ int spk_residual(spk_handle* h, const double* b, const double* x, int64_t nrhs, 
                  int where, double* relres);
 
 /*
+ * Allocation-free residual (no counterpart in the reference).  Same result
+ * as spk_residual with device-resident b and x (n x nrhs, leading dimension
+ * ld), for callers that cannot allocate device memory at call time: code
+ * running inside a stream capture, under an external memory pool or budget,
+ * or from a host callback.  It calls no cudaMalloc/cudaFree: its only work
+ * space (two doubles per right-hand side) is a file-scope device array of
+ * the library, held by every device that loads it until the process exits.
+ * At most SPK_NOALLOC_MAX_RHS right-hand sides per call (SPK_EARG beyond).
+ * The first call on a device looks up that array's device address, so make
+ * it before any stream capture.  All calls share the array (it is cleared
+ * at the start of each call): calls that overlap on the GPU, from any
+ * handle on the same device, race.
+ */
+#define SPK_NOALLOC_MAX_RHS 64
+int spk_residual_noalloc(spk_handle* h, const double* b, const double* x, int64_t nrhs, int64_t ld, double* relres);
+
+/*
  * Copy the factor of the given precision back in the reference's layout:
  * lnz[xlnz[n+1]-1], unz[xunz[n+1]-1] and ipiv[n] (1-based, local to each
  * supernode's diagonal block), exactly as _SparseBase holds them after

@@ -13,6 +13,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <type_traits>
 #include <string>
@@ -1187,6 +1188,60 @@ int spk_residual(spk_handle* h, const double* b, const double* x, int64_t nrhs, 
         ldb = ldx = n;
     }
     return residual_device(h, db, ldb, dx, ldx, nrhs, relres);
+}
+
+}  // extern "C"
+
+// Work space of spk_residual_noalloc: the two sums of squares of each
+// right-hand side.  A file-scope device array, so the entry point allocates
+// nothing; every device that loads this library holds it until exit.  Host
+// code only sees a stand-in for it: its device address is fetched once per
+// device with cudaGetSymbolAddress (with that device current) and cached.
+static __device__ __align__(256) double g_noalloc_sums[2 * SPK_NOALLOC_MAX_RHS];
+static std::mutex g_noalloc_mutex;
+static double* g_noalloc_ptr[64];
+
+static int noalloc_scratch(spk_handle* h, double** out) {
+    if (h->device < 0 || h->device >= 64) return set_err(h, SPK_EARG, "spk_residual_noalloc: device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[h->device]) {
+        double* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress((void**)&p, g_noalloc_sums);
+        if (e != cudaSuccess)
+            return set_err(h, SPK_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_noalloc_ptr[h->device] = p;
+    }
+    *out = g_noalloc_ptr[h->device];
+    return SPK_OK;
+}
+
+extern "C" {
+
+int spk_residual_noalloc(spk_handle* h, const double* b, const double* x, int64_t nrhs, int64_t ld, double* relres) {
+    int rc = check_h(h);
+    if (rc) return rc;
+    if (!relres || !b || !x || nrhs <= 0 || ld < h->n) return set_err(h, SPK_EARG, "spk_residual_noalloc: bad arguments");
+    if (nrhs > SPK_NOALLOC_MAX_RHS)
+        return set_err(h, SPK_EARG, "spk_residual_noalloc: at most SPK_NOALLOC_MAX_RHS (64) right-hand sides per call");
+    if (!h->have_values) return set_err(h, SPK_ESEQ, "Sequence error. Matrix input not done yet.");
+    double* sums = nullptr;
+    if ((rc = noalloc_scratch(h, &sums))) return rc;
+    const int n = (int)h->n;
+    CU(h, cudaMemsetAsync(sums, 0, sizeof(double) * 2 * (size_t)nrhs, h->stream));
+    dim3 grid((n + 255) / 256, (unsigned)nrhs);
+    spk::k_residual_norms<<<grid, 256, 0, h->stream>>>(h->d_aval, h->d_rowptr, h->d_col, h->d_src, x, ld, b, ld, n, sums);
+    CU(h, cudaGetLastError());
+    double host[2 * SPK_NOALLOC_MAX_RHS];
+    CU(h, cudaMemcpyAsync(host, sums, sizeof(double) * 2 * (size_t)nrhs, cudaMemcpyDeviceToHost, h->stream));
+    CU(h, cudaStreamSynchronize(h->stream));
+    double worst = 0.0;
+    for (i64 j = 0; j < nrhs; ++j) {
+        double nb = std::sqrt(host[2 * j + 1]), nr = std::sqrt(host[2 * j]);
+        double rel = nb > 0.0 ? nr / nb : nr;
+        if (!(rel <= worst)) worst = rel;
+    }
+    *relres = worst;
+    return SPK_OK;
 }
 
 int spk_refine(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where, int precision,

@@ -1227,4 +1227,32 @@ __global__ void k_residual(const double* __restrict__ aval, const int* __restric
     }
 }
 
+// Norms only: sums[2r] += ||b_r - A x_r||^2 and sums[2r+1] += ||b_r||^2, with
+// no residual vector written (used where no work space may be allocated).
+__global__ void k_residual_norms(const double* __restrict__ aval, const int* __restrict__ rowptr,
+                                 const int* __restrict__ col, const ll* __restrict__ src, const double* __restrict__ x,
+                                 ll ldx, const double* __restrict__ b, ll ldb, int n, double* __restrict__ sums) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int rhs = blockIdx.y;
+    double rr = 0.0, bb = 0.0;
+    if (i < n) {
+        double s = 0.0;
+        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) s += aval[src[k]] * x[(ll)rhs * ldx + col[k]];
+        double bi = b[(ll)rhs * ldb + i];
+        double ri = bi - s;
+        rr = ri * ri;
+        bb = bi * bi;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        rr += __shfl_down_sync(0xffffffffu, rr, off);
+        bb += __shfl_down_sync(0xffffffffu, bb, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&sums[2 * rhs], rr);
+        atomicAdd(&sums[2 * rhs + 1], bb);
+    }
+}
+
 }  // namespace spk
+

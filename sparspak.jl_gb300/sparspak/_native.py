@@ -41,6 +41,7 @@ GPU_SYMBOLS = {
     "spk_refine": (ctypes.c_int, [VP, VP, VP, i64, i64, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                   ctypes.c_int, ctypes.POINTER(ctypes.c_int), PD]),
     "spk_residual": (ctypes.c_int, [VP, VP, VP, i64, i64, ctypes.c_int, PD]),
+    "spk_residual_noalloc": (ctypes.c_int, [VP, VP, VP, i64, i64, PD]),
     "spk_get_factors": (ctypes.c_int, [VP, ctypes.c_int, PD, PD, P64]),
     "spk_stats": (ctypes.c_int, [VP, P64, P64, P64, PD]),
     "spk_profile": (ctypes.c_int, [VP, ctypes.c_uint]),

@@ -1,0 +1,47 @@
+"""The allocation-free residual entry point (spk_residual_noalloc).
+
+It exists for callers that cannot allocate device memory when they call
+the library (inside a CUDA stream capture, under a fixed memory budget, or
+from a host callback): its work space is a file-scope device array instead
+of a cudaMalloc.  Checked through the C ABI against spk_residual, on two
+calls in a row (the shared array keeps the previous call's contents, so the
+second call also checks that it is cleared).  This file is collected last.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import sparspak as S
+from sparspak import _native as N
+
+pytestmark = pytest.mark.gpu
+
+
+def test_residual_noalloc_matches_spk_residual():
+    torch = pytest.importorskip("torch")
+    A = S.gallery.laplacian((12, 12, 12), shift=1e-3)
+    n, nrhs = A.shape[0], 3
+    s = S.SparseSolver(A, precision="fp32")
+    S.findorder_(s, S.nd_grid(12, 12, 12, leaf=16))
+    S.symbolicfactor_(s)
+    S.inmatrix_(s)
+    S.factor_(s)
+    eng = s.slvr.engine
+    lib = N.gpu()
+    b = S.gallery.random_rhs(n, nrhs, seed=4)
+    b_d = torch.tensor(np.ascontiguousarray(b.T), device="cuda")   # rows are right-hand sides, ld = n
+    x_d = b_d.clone()
+    eng.solve(x_d, "fp32")                                         # FP32 solve: residual well above rounding
+    ref = eng.residual(b_d, x_d)
+    assert 1e-12 < ref < 1e-3
+    for _ in range(2):
+        rr = ctypes.c_double(-1.0)
+        rc = lib.spk_residual_noalloc(eng._h, ctypes.c_void_p(b_d.data_ptr()), ctypes.c_void_p(x_d.data_ptr()), nrhs, n,
+                                      ctypes.byref(rr))
+        assert rc == N.SPK_OK, lib.spk_last_error(eng._h).decode()
+        assert abs(rr.value - ref) <= 1e-12 * ref
+    rr = ctypes.c_double(0.0)
+    rc = lib.spk_residual_noalloc(eng._h, ctypes.c_void_p(b_d.data_ptr()), ctypes.c_void_p(x_d.data_ptr()), 65, n,
+                                  ctypes.byref(rr))
+    assert rc == N.SPK_EARG and "64" in lib.spk_last_error(eng._h).decode()
