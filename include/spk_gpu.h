@@ -175,7 +175,8 @@ int spk_stats(spk_handle* h, int64_t* nfronts, int64_t* nlevels, int64_t* factor
 #define SPK_K_BWD 6        /* backward substitution (_luusolve!)                */
 #define SPK_K_PERMUTE 7    /* right-hand side permutation                       */
 #define SPK_K_RESIDUAL 8   /* r = b - A x                                       */
-#define SPK_K_COUNT 9
+#define SPK_K_BLOCKINV 9   /* whole-block solve operators, after the factorisation */
+#define SPK_K_COUNT 10
 
 /*
  * Launch accounting (no counterpart in the reference, whose only timing is

@@ -791,7 +791,7 @@ static int factor_launches(spk_handle* h) {
         const int cnt = PL.inv_off[c + 1] - PL.inv_off[c];
         if (cnt <= 0) continue;
         const int bw = std::min(lim[c], PL.bwmax);
-        LaunchScope ls(h, SPK_K_GETRF, 0.0, 0.0);
+        LaunchScope ls(h, SPK_K_BLOCKINV, 0.0, 0.0);
         spk::k_block_inv<T><<<cnt, 256, sizeof(T) * 3 * (size_t)bw * (bw | 1), h->stream>>>(
             fac, inv, storage<T>(h).inv2, S, PL.d_blk_front, PL.d_inv_ids + PL.inv_off[c], bw);
     }

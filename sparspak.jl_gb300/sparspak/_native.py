@@ -53,7 +53,10 @@ GPU_SYMBOLS = {
 
 SPK_OK, SPK_EARG, SPK_ECUDA, SPK_ENOMEM, SPK_ESEQ, SPK_ESTRUCT, SPK_ESINGULAR, SPK_ENOCONV = 0, -1, -2, -3, -4, -5, -6, -7
 SPK_HOST, SPK_DEVICE = 0, 1
-KERNEL_CLASSES = ["assemble", "getrf", "panel", "trail", "schur", "fwd", "bwd", "permute", "residual"]
+KERNEL_CLASSES = ["assemble", "getrf", "panel", "trail", "schur", "fwd", "bwd", "permute", "residual", "blockinv"]
+KERNEL_NAMES = {"assemble": "k_scatter_values", "getrf": "k_block_lu", "panel": "k_block_panel",
+                "trail": "k_block_trail", "schur": "k_schur", "fwd": "k_fwd", "bwd": "k_bwd_u12+k_bwd",
+                "permute": "k_permute+k_unpermute", "residual": "k_residual", "blockinv": "k_block_inv"}
 SPK_FP64, SPK_FP32 = 0, 1
 
 _lock = threading.Lock()
