@@ -61,17 +61,16 @@ struct Plan {
     bool built = false;
     int bmax = 0, bwmax = 1;
     std::vector<int> blk_c0, blk_c1, blk_p0, blk_np;
-    std::vector<ll> blk_inv, blk_inv2;
+    std::vector<ll> blk_inv2;
     std::vector<int> blk_front;
-    std::vector<int> inv_ids;             // block ids grouped by width class
-    int inv_off[5] = {0, 0, 0, 0, 0};     // class c: inv_ids[inv_off[c] .. inv_off[c+1])
-    ll inv_size = 0, inv2_size = 0;
+    std::vector<int> inv_ids;             // k_block_inv entries grouped by line width (32, 64, 128)
+    int inv_off[4] = {0, 0, 0, 0};        // class c: inv_ids[inv_off[c] .. inv_off[c+1])
+    ll inv2_size = 0;
     std::vector<int> block0, nblocks;     // per front
     std::vector<LevelPlan> levels;
     std::vector<int> sched_ids, sched_prefix;
     spk::DFront* d_fronts = nullptr;
     int *d_blk_c0 = nullptr, *d_blk_c1 = nullptr, *d_blk_p0 = nullptr, *d_blk_np = nullptr;
-    ll* d_blk_inv = nullptr;
     ll* d_blk_inv2 = nullptr;
     int* d_blk_front = nullptr;
     int* d_inv_ids = nullptr;
@@ -89,7 +88,6 @@ struct HFront {
 template <typename T>
 struct Storage {
     T* d = nullptr;
-    T* inv = nullptr;       // the pieces' inverses
     T* inv2 = nullptr;      // whole-block forward / backward operators
     bool loaded = false;    // values assembled since the last factor
     bool factored = false;
@@ -504,7 +502,6 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax) {
     const int nfr = (int)h->fronts.size();
     P.block0.resize(nfr);
     P.nblocks.resize(nfr);
-    ll inv = 0;
     for (int i = 0; i < nfr; ++i) {
         const HFront& F = h->fronts[i];
         P.block0[i] = (int)P.blk_c0.size();
@@ -518,27 +515,32 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax) {
             P.blk_c1.push_back(c1);
             P.blk_p0.push_back(s);
             P.blk_np.push_back(t - s);
-            P.blk_inv.push_back(inv);
             P.blk_inv2.push_back(P.inv2_size);
             P.inv2_size += 2 * (ll)bw * bw;
             P.blk_front.push_back(i);
-            for (int q = s; q < t; ++q) inv += 2 * (ll)(h->xs[q + 1] - h->xs[q]) * (h->xs[q + 1] - h->xs[q]);
             P.bwmax = std::max(P.bwmax, bw);
             s = t;
         }
         P.nblocks[i] = (int)P.blk_c0.size() - P.block0[i];
     }
-    P.inv_size = inv;
     {
-        const int lim[4] = {16, 32, 64, 128};
-        for (int c = 0; c < 4; ++c) {
+        // k_block_inv work: blocks up to 32 wide, one entry per block; wider
+        // ones by line width 64 / 128, entries blk * 4 + kind * 2 + tile
+        const int lim[3] = {32, 64, 128};
+        for (int c = 0; c < 3; ++c) {
             P.inv_off[c] = (int)P.inv_ids.size();
             for (int b = 0; b < (int)P.blk_c0.size(); ++b) {
                 const int bw = P.blk_c1[b] - P.blk_c0[b];
-                if (bw <= lim[c] && (c == 0 || bw > lim[c - 1])) P.inv_ids.push_back(b);
+                if (!(bw <= lim[c] && (c == 0 || bw > lim[c - 1]))) continue;
+                if (c == 0) {
+                    P.inv_ids.push_back(b);
+                } else {
+                    for (int kind = 0; kind < 2; ++kind)
+                        for (int tile = 0; tile < spk::cdiv(bw, 64); ++tile) P.inv_ids.push_back(b * 4 + kind * 2 + tile);
+                }
             }
         }
-        P.inv_off[4] = (int)P.inv_ids.size();
+        P.inv_off[3] = (int)P.inv_ids.size();
     }
     const int nlev = h->nlevels;
     std::vector<std::vector<int>> at(nlev);
@@ -665,7 +667,6 @@ static int ensure_plan(spk_handle* h) {
     if ((rc = upload(h, &P.d_blk_c1, P.blk_c1))) return rc;
     if ((rc = upload(h, &P.d_blk_p0, P.blk_p0))) return rc;
     if ((rc = upload(h, &P.d_blk_np, P.blk_np))) return rc;
-    if ((rc = upload(h, &P.d_blk_inv, P.blk_inv))) return rc;
     if ((rc = upload(h, &P.d_blk_inv2, P.blk_inv2))) return rc;
     if ((rc = upload(h, &P.d_blk_front, P.blk_front))) return rc;
     if ((rc = upload(h, &P.d_inv_ids, P.inv_ids))) return rc;
@@ -684,22 +685,18 @@ static int ensure_plan(spk_handle* h) {
     S.blk_c1 = P.d_blk_c1;
     S.blk_p0 = P.d_blk_p0;
     S.blk_np = P.d_blk_np;
-    S.blk_inv = P.d_blk_inv;
     S.blk_inv2 = P.d_blk_inv2;
-    const int bw = P.bwmax;
-    CU(h, cudaFuncSetAttribute(spk::k_block_lu<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)(sizeof(T) * ((size_t)bw * (bw | 1) + 2 * (size_t)bw * spk::MAXW) +
-                                     sizeof(int) * 2 * (spk::BlockMax<T>::value + 1))));
-    CU(h, cudaFuncSetAttribute(spk::k_block_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)(sizeof(T) * 64 * (size_t)bw)));
-    CU(h, cudaFuncSetAttribute(spk::k_block_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)(sizeof(T) * 3 * (size_t)bw * (bw | 1))));
+    constexpr int BM = spk::BlockMax<T>::value;
+    CU(h, cudaFuncSetAttribute(spk::k_block_panel<T, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(sizeof(T) * BM * BM)));
+    CU(h, cudaFuncSetAttribute(spk::k_block_inv<T, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(sizeof(T) * BM * BM)));
     P.built = true;
     return SPK_OK;
 }
 
 static void free_plan(Plan& P) {
-    void* ptrs[] = {P.d_fronts, P.d_blk_c0, P.d_blk_c1, P.d_blk_p0, P.d_blk_np, P.d_blk_inv, P.d_blk_inv2,
+    void* ptrs[] = {P.d_fronts, P.d_blk_c0, P.d_blk_c1, P.d_blk_p0, P.d_blk_np, P.d_blk_inv2,
                     P.d_blk_front, P.d_inv_ids, P.d_sched_ids, P.d_sched_prefix};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -719,7 +716,6 @@ static int ensure_storage(spk_handle* h) {
     if (rc) return rc;
     Storage<T>& S = storage<T>(h);
     if (!S.d) CU(h, cudaMalloc((void**)&S.d, sizeof(T) * std::max<i64>(h->fsize, 1)));
-    if (!S.inv) CU(h, cudaMalloc((void**)&S.inv, sizeof(T) * std::max<ll>(h->plan[prec_index<T>()].inv_size, 1)));
     if (!S.inv2) CU(h, cudaMalloc((void**)&S.inv2, sizeof(T) * std::max<ll>(h->plan[prec_index<T>()].inv2_size, 1)));
     return SPK_OK;
 }
@@ -751,29 +747,34 @@ static int ensure_rhs(spk_handle* h, i64 nrhs) {
 // ---------------------------------------------------------------------------
 template <typename T>
 static int factor_launches(spk_handle* h) {
+    constexpr int BM = spk::BlockMax<T>::value;
     T* fac = storage<T>(h).d;
-    T* inv = storage<T>(h).inv;
     const Plan& PL = h->plan[prec_index<T>()];
     const spk::Sched& S = PL.sched;
     for (const LevelPlan& P : PL.levels) {
         for (size_t t = 0; t < P.blu.size(); ++t) {
             const int bw = P.blu[t].bw;
-            const size_t lu_smem = sizeof(T) * ((size_t)bw * (bw | 1) + 2 * (size_t)bw * spk::MAXW) +
-                                   sizeof(int) * 2 * (spk::BlockMax<T>::value + 1);
-            const size_t panel_smem = sizeof(T) * 64 * (size_t)bw;
             if (P.blu[t].tiles > 0) {
                 LaunchScope ls(h, SPK_K_GETRF, P.blu[t].flops, P.blu[t].words * sizeof(T));
                 if (bw <= 32)
                     spk::k_block_lu_small<T><<<(P.blu[t].count + 3) / 4, 128, 0, h->stream>>>(
-                        fac, h->d_ipiv, h->d_info, inv, S, launch_of(PL, P.blu[t]), (int)t);
+                        fac, h->d_ipiv, h->d_info, S, launch_of(PL, P.blu[t]), (int)t);
                 else
-                    spk::k_block_lu<T><<<P.blu[t].tiles, 256, lu_smem, h->stream>>>(
-                        fac, h->d_ipiv, h->d_info, inv, S, launch_of(PL, P.blu[t]), (int)t, bw);
+                    spk::k_block_lu<T><<<P.blu[t].tiles, 256, 0, h->stream>>>(
+                        fac, h->d_ipiv, h->d_info, S, launch_of(PL, P.blu[t]), (int)t);
             }
             if (P.bpanel[t].tiles > 0) {
                 LaunchScope ls(h, SPK_K_PANEL, P.bpanel[t].flops, P.bpanel[t].words * sizeof(T));
-                spk::k_block_panel<T><<<P.bpanel[t].tiles, 256, panel_smem, h->stream>>>(
-                    fac, inv, S, launch_of(PL, P.bpanel[t]), (int)t, bw);
+                const spk::Launch la = launch_of(PL, P.bpanel[t]);
+                if (bw <= 32)
+                    spk::k_block_panel<T, 32><<<P.bpanel[t].tiles, 256, sizeof(T) * 32 * 32, h->stream>>>(
+                        fac, h->d_ipiv, S, la, (int)t);
+                else if (bw <= 64)
+                    spk::k_block_panel<T, 64><<<P.bpanel[t].tiles, 256, sizeof(T) * 64 * 64, h->stream>>>(
+                        fac, h->d_ipiv, S, la, (int)t);
+                else
+                    spk::k_block_panel<T, BM><<<P.bpanel[t].tiles, 256, sizeof(T) * BM * BM, h->stream>>>(
+                        fac, h->d_ipiv, S, la, (int)t);
             }
             if (P.btrail[t].tiles > 0) {
                 LaunchScope ls(h, SPK_K_TRAIL, P.btrail[t].flops, P.btrail[t].words * sizeof(T));
@@ -786,14 +787,21 @@ static int factor_launches(spk_handle* h) {
             spk::k_schur<T><<<P.schur.tiles, 256, 0, h->stream>>>(fac, S, launch_of(PL, P.schur));
         }
     }
-    const int lim[4] = {16, 32, 64, 128};
-    for (int c = 0; c < 4; ++c) {
+    for (int c = 0; c < 3; ++c) {
         const int cnt = PL.inv_off[c + 1] - PL.inv_off[c];
         if (cnt <= 0) continue;
-        const int bw = std::min(lim[c], PL.bwmax);
         LaunchScope ls(h, SPK_K_BLOCKINV, 0.0, 0.0);
-        spk::k_block_inv<T><<<cnt, 256, sizeof(T) * 3 * (size_t)bw * (bw | 1), h->stream>>>(
-            fac, inv, storage<T>(h).inv2, S, PL.d_blk_front, PL.d_inv_ids + PL.inv_off[c], bw);
+        const int* ent = PL.d_inv_ids + PL.inv_off[c];
+        T* inv2 = storage<T>(h).inv2;
+        if (c == 0)
+            spk::k_block_inv<T, 32><<<cnt, 256, sizeof(T) * 2 * 32 * 32, h->stream>>>(fac, h->d_ipiv, inv2, S,
+                                                                                      PL.d_blk_front, ent);
+        else if (c == 1)
+            spk::k_block_inv<T, 64><<<cnt, 256, sizeof(T) * 64 * 64, h->stream>>>(fac, h->d_ipiv, inv2, S,
+                                                                                  PL.d_blk_front, ent);
+        else
+            spk::k_block_inv<T, BM><<<cnt, 256, sizeof(T) * BM * BM, h->stream>>>(fac, h->d_ipiv, inv2, S,
+                                                                                  PL.d_blk_front, ent);
     }
     CU(h, cudaGetLastError());
     return SPK_OK;
@@ -1393,7 +1401,7 @@ void spk_destroy(spk_handle* h) {
     free_plan(h->plan[0]);
     free_plan(h->plan[1]);
     void* ptrs[] = {h->d_xs, h->d_rows, h->d_runid, h->d_run_tgt, h->d_run_start, h->d_run_rel,
-                    h->d_rel, h->s64.inv, h->s32.inv, h->s64.inv2, h->s32.inv2, h->d_ipiv, h->d_info, h->d_slot, h->d_aval,
+                    h->d_rel, h->s64.inv2, h->s32.inv2, h->d_ipiv, h->d_info, h->d_slot, h->d_aval,
                     h->d_rowptr, h->d_col, h->d_src, h->d_rperm, h->d_rinvp, h->s64.d, h->s32.d, h->d_wb,
                     h->d_wy, h->d_wx, h->d_rhs, h->d_x, h->d_r, h->d_sums};
     for (void* p : ptrs)

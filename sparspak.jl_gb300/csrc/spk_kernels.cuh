@@ -66,7 +66,6 @@ struct Sched {
     const int* blk_c1;     // front-local end column of each block
     const int* blk_p0;     // first supernode (0-based) of each block
     const int* blk_np;     // supernodes in the block
-    const ll* blk_inv;     // offset in inv[] of the pieces' inverses
     const ll* blk_inv2;    // offset in inv2[] of the block's Minv (then Uinv), bw x bw each
 };
 
@@ -98,105 +97,17 @@ constexpr int MAXW = 64;
 
 // ---------------------------------------------------------------------------
 // Blocks.  The pieces of a front are processed in *blocks* of consecutive
-// pieces (at most BlockMax<T> columns).  k_block_lu factors a block in
-// shared memory piece by piece with exactly the reference's in-block
-// pivoting: ggetrf! on the piece's diagonal block (one warp), _luswap! of
-// the piece's U rows and the two _trsm! panels inside the block, and the
-// block-local trailing update.  For every piece p it also stores two w x w
-// matrices in inv[] (at 2 * sum of the earlier pieces' w^2):
-//   Ui_p = U_pp^{-1}            and   Li_p = L_pp^{-1} P_p
-// (P_p the piece's interchanges), so that the L panel below a piece is
-// X * Ui_p, the U panel to its right Li_p * Y, and the triangular-solve
-// steps of the piece Li_p * b and Ui_p * c: small dense products.
+// pieces (at most BlockMax<T> columns).  A block step is: the block LU
+// (k_block_lu / k_block_lu_small) with exactly the reference's in-piece
+// pivoting, then the block's two panels (k_block_panel), then the trailing
+// update of the front (k_block_trail).  After the factorisation
+// k_block_inv forms, per block, the two operators the triangular solves
+// apply: Minv = inv(L_B) P_B and Uinv = inv(U_B) (below).
 // ---------------------------------------------------------------------------
 template <typename T> struct BlockMax;
 template <> struct BlockMax<float> { static constexpr int value = 128; };
 template <> struct BlockMax<double> { static constexpr int value = 64; };
 
-// ggetrf! of the w x w diagonal block of a piece (w <= 64), by one warp:
-// A points at the block's first entry, column-major with leading dimension
-// lda.  piv[k] = 0-based local pivot row; returns true on a zero pivot.
-template <typename T>
-__device__ bool warp_getrf(T* A, int lda, int w, int* piv) {
-    const int lane = threadIdx.x & 31;
-    bool sing = false;
-    for (int k = 0; k < w; ++k) {
-        double key = -1.0;
-        int idx = w;
-        for (int i = k + lane; i < w; i += 32) {
-            double v = (double)tabs(A[k * lda + i]);
-            double ki = (v != v) ? ((i == k) ? __longlong_as_double(0x7ff0000000000000LL) : -1.0) : v;
-            if (ki > key || idx == w) { key = ki; idx = i; }
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            double k2 = __shfl_xor_sync(0xffffffffu, key, off);
-            int i2 = __shfl_xor_sync(0xffffffffu, idx, off);
-            if (k2 > key || (k2 == key && i2 < idx)) { key = k2; idx = i2; }
-        }
-        const int kp = idx;
-        if (lane == 0) piv[k] = kp;
-        const T pv = A[k * lda + kp];
-        __syncwarp();
-        if (pv != T(0)) {
-            if (kp != k)
-                for (int j = lane; j < w; j += 32) {
-                    T t = A[j * lda + k];
-                    A[j * lda + k] = A[j * lda + kp];
-                    A[j * lda + kp] = t;
-                }
-            __syncwarp();
-            const T inv = T(1) / A[k * lda + k];
-            for (int i = k + 1 + lane; i < w; i += 32) A[k * lda + i] *= inv;
-        } else {
-            sing = true;
-        }
-        __syncwarp();
-        for (int i = k + 1 + lane; i < w; i += 32) {
-            const T lik = A[k * lda + i];
-            for (int j = k + 1; j < w; ++j) A[j * lda + i] -= lik * A[j * lda + k];
-        }
-        __syncwarp();
-    }
-    return sing;
-}
-
-// Inverses of a factored piece: Ui = U^{-1} (upper solve on the identity,
-// as trsm 'l','u','n','n') and Li = L^{-1} P (laswp then unit-lower solve on
-// the identity, as _lulsolve!), each w x w column-major (ld w), one lane per
-// column.  Warp 0 of the caller forms Ui, warp 1 forms Li.
-template <typename T>
-__device__ void piece_inverses(const T* A, int lda, int w, const int* piv, T* Ui, T* Li) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (warp == 0) {
-        for (int j = lane; j < w; j += 32) {
-            T* u = Ui + j * w;
-            for (int i = 0; i < w; ++i) u[i] = T(i == j);
-            for (int k = j; k >= 0; --k) {
-                T uk = u[k];
-                if (uk != T(0)) {
-                    uk /= A[k * lda + k];
-                    u[k] = uk;
-                    for (int i = 0; i < k; ++i) u[i] -= uk * A[k * lda + i];
-                }
-            }
-        }
-    } else if (warp == 1) {
-        for (int j = lane; j < w; j += 32) {
-            T* v = Li + j * w;
-            for (int i = 0; i < w; ++i) v[i] = T(i == j);
-            for (int k = 0; k < w; ++k) {
-                int kp = piv[k];
-                if (kp != k) { T t = v[k]; v[k] = v[kp]; v[kp] = t; }
-            }
-            for (int k = 0; k < w; ++k) {
-                T vk = v[k];
-                if (vk != T(0))
-                    for (int i = k + 1; i < w; ++i) v[i] -= vk * A[k * lda + i];
-            }
-        }
-    }
-}
 
 // Order-preserving pivot key of |x| for a candidate row (larger key = larger
 // |x|, all candidates above non-candidates), with the ggetrf! rules: a NaN
@@ -224,14 +135,20 @@ __device__ __forceinline__ int warp_first_max(unsigned long long key) {
     return __ffs(ballot) - 1;
 }
 
-// r[k] for a runtime k without indexing a register array dynamically.
+// r[k] for a runtime k without indexing a register array dynamically: a
+// five-level tree of selects (depth 5 instead of a 31-long chain).
 template <typename T>
 __device__ __forceinline__ T pick32(const T (&r)[32], int k) {
-    T v = r[0];
+    T v16[16], v8[8], v4[4], v2[2];
 #pragma unroll
-    for (int j = 1; j < 32; ++j)
-        if (j == k) v = r[j];
-    return v;
+    for (int i = 0; i < 16; ++i) v16[i] = (k & 16) ? r[i + 16] : r[i];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v8[i] = (k & 8) ? v16[i + 8] : v16[i];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v4[i] = (k & 4) ? v8[i + 4] : v8[i];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) v2[i] = (k & 2) ? v4[i + 2] : v4[i];
+    return (k & 1) ? v2[1] : v2[0];
 }
 
 // One right-looking LU sweep over the columns [0, ncols) of a register block
@@ -289,98 +206,6 @@ __device__ bool warp_lu_sweep(T (&r)[32], int nrows, int ncols, const int* q0, i
     return sing;
 }
 
-// ggetrf! of a piece of at most 32 columns by one warp, lane i holding row
-// i in registers; A (w x w, column-major, leading dimension lda) is read and
-// written back; piv[k] receives the local pivot row.
-template <typename T>
-__device__ bool warp_getrf32(T* A, int lda, int w, int* piv) {
-    const int lane = threadIdx.x & 31;
-    T r[32];
-#pragma unroll
-    for (int j = 0; j < 32; ++j) r[j] = (lane < w && j < w) ? A[j * lda + lane] : T(0);
-    const int q0[2] = {0, w};
-    const bool sing = warp_lu_sweep(r, w, w, q0, piv);
-    if (lane < w) {
-#pragma unroll
-        for (int j = 0; j < 32; ++j)
-            if (j < w) A[j * lda + lane] = r[j];
-    }
-    return sing;
-}
-
-// Ui = U^{-1} of a factored piece (w <= 32) by one warp: trsm 'l','u','n','n'
-// on the identity, lane j forming column j.
-template <typename T>
-__device__ void warp_inv_upper32(const T* A, int lda, int w, T* Ui) {
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    T r[32];
-#pragma unroll
-    for (int j = 0; j < 32; ++j) r[j] = (lane < w && j < w) ? A[j * lda + lane] : T(0);
-    T x[32];
-#pragma unroll
-    for (int i = 0; i < 32; ++i) x[i] = T(i == lane);
-#pragma unroll 1
-    for (int k = w - 1; k >= 0; --k) {
-        const T rk = pick32(r, k);
-        T uk[32];
-#pragma unroll
-        for (int i = 0; i < 32; ++i) uk[i] = __shfl_sync(FULL, rk, i);   // column k of U
-        T xk = pick32(x, k);
-        if (xk != T(0)) {
-            xk /= pick32(uk, k);
-#pragma unroll
-            for (int i = 0; i < 32; ++i) {
-                if (i == k) x[i] = xk;
-                else if (i < k) x[i] -= xk * uk[i];
-            }
-        }
-    }
-    if (lane < w) {
-#pragma unroll
-        for (int i = 0; i < 32; ++i)
-            if (i < w) Ui[lane * w + i] = x[i];
-    }
-}
-
-// Li = L^{-1} P of a factored piece (w <= 32) by one warp: laswp then trsm
-// 'l','l','n','u' on the identity, lane j forming column j.
-template <typename T>
-__device__ void warp_inv_lower32(const T* A, int lda, int w, const int* piv, T* Li) {
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    T r[32];
-#pragma unroll
-    for (int j = 0; j < 32; ++j) r[j] = (lane < w && j < w) ? A[j * lda + lane] : T(0);
-    int pos = lane;
-    for (int k = 0; k < w; ++k) {
-        const int kp = piv[k];
-        if (pos == k) pos = kp;
-        else if (pos == kp) pos = k;
-    }
-    T x[32];
-#pragma unroll
-    for (int i = 0; i < 32; ++i) x[i] = T(i == pos);
-#pragma unroll 1
-    for (int k = 0; k < w; ++k) {
-        const T rk = pick32(r, k);
-        T lk[32];
-#pragma unroll
-        for (int i = 0; i < 32; ++i) lk[i] = __shfl_sync(FULL, rk, i);   // column k of L
-        const T xk = pick32(x, k);
-        if (xk != T(0)) {
-#pragma unroll
-            for (int i = 0; i < 32; ++i)
-                if (i > k && i < w) x[i] -= xk * lk[i];
-        }
-    }
-    if (lane < w) {
-#pragma unroll
-        for (int i = 0; i < 32; ++i)
-            if (i < w) Li[lane * w + i] = x[i];
-    }
-}
-
 // A whole block of at most 32 columns factored by one warp in registers
 // (lane i holds row i) as one right-looking sweep over its columns.  For
 // column k in piece [a, b): the pivot is the first strict maximum among rows
@@ -410,8 +235,7 @@ __device__ bool warp_block_lu32(T* A, int lda, int bw, const int* q0, int np, in
 // Blocks of at most 32 columns: one warp per block, four blocks per CTA (the
 // launch holds one block per front).  Same outputs as k_block_lu.
 template <typename T>
-__global__ void __launch_bounds__(128) k_block_lu_small(T* fac, int* ipiv, int* info, T* inv, Sched S, Launch L,
-                                                         int step) {
+__global__ void __launch_bounds__(128) k_block_lu_small(T* fac, int* ipiv, int* info, Sched S, Launch L, int step) {
     __shared__ T sA[4][32 * 33];
     __shared__ int sq[4][33];
     __shared__ int spiv[4][32];
@@ -433,14 +257,6 @@ __global__ void __launch_bounds__(128) k_block_lu_small(T* fac, int* ipiv, int* 
     for (int j = 0; j < bw; ++j)
         if (lane < bw) fac[F.loff + (ll)(c0 + j) * F.ld + c0 + lane] = A[j * lda + lane];
     if (lane < bw) ipiv[F.f + c0 + lane] = piv[lane];
-    T* out = inv + S.blk_inv[blk];
-    int woff = 0;
-    for (int pc = 0; pc < np; ++pc) {
-        const int a = q0[pc], w = q0[pc + 1] - a;
-        warp_inv_upper32(A + a * lda + a, lda, w, out + woff);
-        warp_inv_lower32(A + a * lda + a, lda, w, piv + a, out + woff + w * w);
-        woff += 2 * w * w;
-    }
     if (lane == 0 && sing) {   // sing is uniform across the warp
         for (int pc = 0; pc < np; ++pc) {
             bool z = false;
@@ -450,262 +266,416 @@ __global__ void __launch_bounds__(128) k_block_lu_small(T* fac, int* ipiv, int* 
     }
 }
 
-// One CTA (256 threads) per front: factor block `step` of the front in shared
-// memory, write it back with its pivots and the pieces' inverses.
-// Dynamic shared memory: bwmax * (bwmax | 1) + 2 * bwmax * MAXW T's, and
-// 2 * (BlockMax + 1) ints.
+// First row holding the largest key, two candidate rows per lane (`idx`
+// the row of `key`): the reference's first strict maximum.
+__device__ __forceinline__ int warp_first_max_row(unsigned long long key, int idx) {
+    const unsigned FULL = 0xffffffffu;
+    const unsigned hi = (unsigned)(key >> 32), lo = (unsigned)key;
+    const unsigned mh = __reduce_max_sync(FULL, hi);
+    const unsigned ml = __reduce_max_sync(FULL, hi == mh ? lo : 0u);
+    return (int)__reduce_min_sync(FULL, (hi == mh && lo == ml) ? (unsigned)idx : 0xffffffffu);
+}
+
+// Block LU by a whole CTA (blocks of 33..BlockMax columns; one CTA per
+// front).  The 256 threads form a 16 x 16 grid; thread (ty, tx) keeps rows
+// [ty*TR, ty*TR+TR) x columns [tx*TR, tx*TR+TR) of the block in registers
+// (TR = BlockMax / 16).  For each column k, in piece [a, b):
+//   - the owners of column k publish its rows >= k, the owners of row k
+//     publish its columns >= a (shared memory, double-buffered);
+//   - every warp finds the pivot: the first strict maximum of |A(i,k)| over
+//     the piece's rows i in [k, b) (ggetrf!; a NaN never wins except on the
+//     diagonal);
+//   - a nonzero pivot off the diagonal: the pivot row is published and rows
+//     k and kp swap over columns >= a (ggetrf! inside the piece, _luswap! of
+//     its U rows; columns left of the piece never move);
+//   - rows after k: multiplier A(i,k) / pivot (ggetrf! scaling inside the
+//     piece, the L-panel trsm 'r','u','n','n' for the block's later rows;
+//     no scaling after a zero pivot), then the rank-1 update of rows and
+//     columns after k (ggetrf!, the U-panel trsm 'r','l','t','u' and the
+//     block-local Schur update).
+// One barrier per column, two when rows swap.  ipiv receives the local
+// pivot row within the piece; a zero pivot records the piece in info.
 template <typename T>
-__global__ void __launch_bounds__(256) k_block_lu(T* fac, int* ipiv, int* info, T* inv, Sched S, Launch L, int step,
-                                                   int bwmax) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* A = reinterpret_cast<T*>(smem_raw);
-    T* W = A + bwmax * (bwmax | 1);                 // the pieces' inverses, packed as in inv[]
-    int* q0 = reinterpret_cast<int*>(W + 2 * bwmax * MAXW);
-    int* piv = q0 + BlockMax<T>::value + 1;
-    __shared__ int ssing;
-    __shared__ int src[32];
+__global__ void __launch_bounds__(256) k_block_lu(T* fac, int* ipiv, int* info, Sched S, Launch L, int step) {
+    constexpr int BM = BlockMax<T>::value, TR = BM / 16;
+    __shared__ __align__(16) T cbuf[2][BM];
+    __shared__ __align__(16) T rbuf[2][2][BM];
+    __shared__ int q0[BM + 1];
+    __shared__ int spiv[BM];
+    __shared__ int szero;
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
     const int blk = F.block0 + step;
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
-    const int lda = bw | 1;
     const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
-    const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
-    if (tid == 0) ssing = 0;
-    for (int k = tid; k <= np; k += nt) q0[k] = S.xsuper[p0 + k] - F.f - c0;
-#pragma unroll 4
-    for (int j = warp; j < bw; j += nw) {
-        const T* src = fac + F.loff + (ll)(c0 + j) * F.ld + c0;
-#pragma unroll
-        for (int q = 0; q < BlockMax<T>::value / 32; ++q) {
-            const int i = lane + 32 * q;
-            if (i < bw) A[j * lda + i] = src[i];
-        }
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15, lane = tid & 31;
+    const int r0 = ty * TR, cl0 = tx * TR;
+    for (int k = tid; k <= np; k += 256) q0[k] = S.xsuper[p0 + k] - F.f - c0;
+    for (int i = tid; i < 2 * BM; i += 256) {
+        (&cbuf[0][0])[i] = T(0);
+        (&rbuf[0][0][0])[i] = T(0);
+        (&rbuf[0][0][0])[2 * BM + i] = T(0);
     }
+    if (tid == 0) szero = INT_MAX;
+    T* blkp = fac + F.loff + (ll)c0 * F.ld + c0;   // block (i, j) at blkp[j * ld + i]
+    T a[TR][TR];
+#pragma unroll
+    for (int jj = 0; jj < TR; ++jj)
+#pragma unroll
+        for (int ii = 0; ii < TR; ++ii) {
+            const int R = r0 + ii, C = cl0 + jj;
+            a[ii][jj] = (R < bw && C < bw) ? blkp[(ll)C * F.ld + R] : T(0);
+        }
     __syncthreads();
-    int woff = 0;
-    for (int pc = 0; pc < np; ++pc) {
-        const int a = q0[pc], b = q0[pc + 1], w = b - a;
-        T* Ui = W + woff;
-        T* Li = Ui + w * w;
-        if (w <= 32) {
-            if (warp == 0 && warp_getrf32(A + a * lda + a, lda, w, piv + a)) ssing = 1;
-            __syncthreads();
-            if (tid == 0) {                          // the piece's interchanges as a gather map
-                for (int k = 0; k < w; ++k) src[k] = k;
-                for (int k = 0; k < w; ++k) {
-                    const int kp = piv[a + k];
-                    const int t0 = src[k];
-                    src[k] = src[kp];
-                    src[kp] = t0;
-                }
-            }
-            __syncthreads();
-            if (warp == 0) {
-                warp_inv_upper32(A + a * lda + a, lda, w, Ui);
-            } else if (warp == 1) {
-                warp_inv_lower32(A + a * lda + a, lda, w, piv + a, Li);
-            } else if (b < bw) {
-                // warps 2..: U panel to the right inside the block (one thread per
-                // column: _luswap! as a gather, then the unit-lower solve) and L
-                // panel below (one thread per row: X := X * inv(U_pp)), in registers
-                const int ncol = bw - b, nrow = bw - b;
-                for (int t = tid - 64; t < ncol + nrow; t += nt - 64) {
-                    if (t < ncol) {
-                        T* col = A + (b + t) * lda + a;
-                        T y[32];
-#pragma unroll
-                        for (int k = 0; k < 32; ++k) y[k] = k < w ? col[src[k]] : T(0);
+    int pc = 0;
 #pragma unroll 1
-                        for (int k = 0; k < w; ++k) {
-                            const T yk = pick32(y, k);
-                            const T* lcol = A + (a + k) * lda + a;
+    for (int kb = 0; kb * TR < bw; ++kb) {
 #pragma unroll
-                            for (int i = 0; i < 32; ++i)
-                                if (i > k && i < w) y[i] -= lcol[i] * yk;
-                        }
+        for (int kk = 0; kk < TR; ++kk) {
+            const int k = kb * TR + kk;
+            if (k >= bw) break;
+            while (q0[pc + 1] <= k) ++pc;
+            const int a0 = q0[pc], b = q0[pc + 1];
+            T* cb = cbuf[k & 1];
+            T* rk = rbuf[k & 1][0];
+            T* rp = rbuf[k & 1][1];
+            if (tx == kb) {
 #pragma unroll
-                        for (int k = 0; k < 32; ++k)
-                            if (k < w) col[k] = y[k];
-                    } else {
-                        const int i = b + (t - ncol);
-                        T x[32];
+                for (int ii = 0; ii < TR; ++ii) {
+                    const int R = r0 + ii;
+                    if (R >= k && R < bw) cb[R] = a[ii][kk];
+                }
+            }
+            if (ty == kb) {
 #pragma unroll
-                        for (int k = 0; k < 32; ++k) x[k] = k < w ? A[(a + k) * lda + i] : T(0);
-#pragma unroll 1
-                        for (int j = 0; j < w; ++j) {
-                            const T* ucol = A + (a + j) * lda + a;
-                            T acc = pick32(x, j);
-#pragma unroll
-                            for (int k = 0; k < 32; ++k)
-                                if (k < j) acc -= ucol[k] * x[k];
-                            acc *= T(1) / ucol[j];
-#pragma unroll
-                            for (int k = 0; k < 32; ++k)
-                                if (k == j) x[k] = acc;
-                        }
-#pragma unroll
-                        for (int k = 0; k < 32; ++k)
-                            if (k < w) A[(a + k) * lda + i] = x[k];
-                    }
+                for (int jj = 0; jj < TR; ++jj) {
+                    const int C = cl0 + jj;
+                    if (C >= a0 && C < bw) rk[C] = a[kk][jj];
                 }
             }
             __syncthreads();
-            if (b < bw) {
-                for (int j = b + warp; j < bw; j += nw) {   // block-local trailing update
-                    for (int i = b + lane; i < bw; i += 32) {
-                        T acc = T(0);
-                        for (int k = 0; k < w; ++k) acc += A[(a + k) * lda + i] * A[j * lda + a + k];
-                        A[j * lda + i] -= acc;
-                    }
-                }
-                __syncthreads();
+            int kp;
+            {
+                const int i1 = k + lane, i2 = k + 32 + lane;
+                const unsigned long long k1 = pivot_key(cb[min(i1, BM - 1)], i1 < b, i1 == k);
+                const unsigned long long k2 = pivot_key(cb[min(i2, BM - 1)], i2 < b, false);
+                const bool second = k2 > k1;   // ties keep the earlier row
+                kp = warp_first_max_row(second ? k2 : k1, second ? i2 : i1);
             }
-        } else {
-            if (warp == 0 && warp_getrf(A + a * lda + a, lda, w, piv + a)) ssing = 1;
-            __syncthreads();
-            piece_inverses(A + a * lda + a, lda, w, piv + a, Ui, Li);
-            __syncthreads();
-            if (b < bw) {
-                for (int j = b + warp; j < bw; j += nw) {
-                    T yv[2];
+            const T pv = cb[kp];
+            if (tid == 0) {
+                spiv[k] = kp - a0;
+                if (pv == T(0) && k < szero) szero = k;
+            }
+            const bool swap = (pv != T(0)) && kp != k;
+            if (swap) {
+                const int tp = kp / TR, ip = kp % TR;
+                if (ty == tp) {
 #pragma unroll
-                    for (int q = 0; q < 2; ++q) {
-                        const int i = lane + 32 * q;
-                        T acc = T(0);
-                        if (i < w)
-                            for (int k = 0; k < w; ++k) acc += Li[k * w + i] * A[j * lda + a + k];
-                        yv[q] = acc;
-                    }
-                    __syncwarp();
+                    for (int ii = 0; ii < TR; ++ii)
+                        if (ii == ip) {
 #pragma unroll
-                    for (int q = 0; q < 2; ++q)
-                        if (lane + 32 * q < w) A[j * lda + a + lane + 32 * q] = yv[q];
-                }
-                for (int i = b + tid; i < bw; i += nt) {
-                    for (int j = w - 1; j >= 0; --j) {
-                        T acc = T(0);
-                        for (int k = 0; k <= j; ++k) acc += A[(a + k) * lda + i] * Ui[j * w + k];
-                        A[(a + j) * lda + i] = acc;
-                    }
+                            for (int jj = 0; jj < TR; ++jj) {
+                                const int C = cl0 + jj;
+                                if (C >= a0 && C < bw) rp[C] = a[ii][jj];
+                            }
+                        }
                 }
                 __syncthreads();
-                for (int j = b + warp; j < bw; j += nw) {
-                    for (int i = b + lane; i < bw; i += 32) {
-                        T acc = T(0);
-                        for (int k = 0; k < w; ++k) acc += A[(a + k) * lda + i] * A[j * lda + a + k];
-                        A[j * lda + i] -= acc;
+                if (ty == kb) {
+#pragma unroll
+                    for (int jj = 0; jj < TR; ++jj) {
+                        const int C = cl0 + jj;
+                        if (C >= a0 && C < bw) a[kk][jj] = rp[C];
                     }
                 }
-                __syncthreads();
+                if (ty == tp) {
+#pragma unroll
+                    for (int ii = 0; ii < TR; ++ii)
+                        if (ii == ip) {
+#pragma unroll
+                            for (int jj = 0; jj < TR; ++jj) {
+                                const int C = cl0 + jj;
+                                if (C >= a0 && C < bw) a[ii][jj] = rk[C];
+                            }
+                        }
+                }
+            }
+            if (r0 + TR - 1 > k) {
+                const T* ur = swap ? rp : rk;
+                const bool scale = pv != T(0);
+                const T rinv = scale ? T(1) / pv : T(1);
+                T l[TR], u[TR];
+#pragma unroll
+                for (int ii = 0; ii < TR; ++ii) {
+                    const int R = r0 + ii;
+                    const T v = (R == kp) ? cb[k] : cb[R];
+                    l[ii] = scale ? v * rinv : v;
+                }
+#pragma unroll
+                for (int jj = 0; jj < TR; ++jj) u[jj] = ur[cl0 + jj];
+#pragma unroll
+                for (int ii = 0; ii < TR; ++ii) {
+                    if (r0 + ii > k) {
+#pragma unroll
+                        for (int jj = 0; jj < TR; ++jj)
+                            if (cl0 + jj > k) a[ii][jj] -= l[ii] * u[jj];
+                        if (tx == kb) a[ii][kk] = l[ii];
+                    }
+                }
             }
         }
-        woff += 2 * w * w;
     }
-    for (int j = warp; j < bw; j += nw)
-        for (int i = lane; i < bw; i += 32) fac[F.loff + (ll)(c0 + j) * F.ld + c0 + i] = A[j * lda + i];
-    for (int c = tid; c < bw; c += nt) ipiv[F.f + c0 + c] = piv[c];
-    T* out = inv + S.blk_inv[blk];
-    for (int e = tid; e < woff; e += nt) out[e] = W[e];
-    if (tid == 0 && ssing) {
-        for (int pc = 0; pc < np; ++pc) {   // first singular piece of the block
-            bool z = false;
-            for (int k = q0[pc]; k < q0[pc + 1]; ++k) z |= A[k * lda + k] == T(0);
-            if (z) { atomicMin(info, p0 + pc + 1); break; }
+#pragma unroll
+    for (int jj = 0; jj < TR; ++jj)
+#pragma unroll
+        for (int ii = 0; ii < TR; ++ii) {
+            const int R = r0 + ii, C = cl0 + jj;
+            if (R < bw && C < bw) blkp[(ll)C * F.ld + R] = a[ii][jj];
+        }
+    __syncthreads();
+    for (int c = tid; c < bw; c += 256) ipiv[F.f + c0 + c] = spiv[c];
+    if (tid == 0 && szero != INT_MAX) {
+        int p = 0;
+        while (q0[p + 1] <= szero) ++p;
+        atomicMin(info, p0 + p + 1);   // first singular piece of the block
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Panel sweeps on register lines.  A line (a row of X or a column of Y) of
+// a block of width bw <= W is held by 4 consecutive lanes, lane q of the
+// group owning entries [q*CQ, q*CQ + CQ), CQ = W / 4.  Column by column the
+// owner of entry k scales it (rows) and shuffles it to its group, and every
+// lane updates its entries with a row of U or a column of L read from
+// shared memory (the triangles are staged with zeros outside the strict
+// part, so the updates need no predicates).
+//   rows: X := X inv(U_B), U_B the block's upper triangle with its diagonal:
+//         sU row-major (ld W), zero on and below the diagonal, rd[k] = 1/U(k,k);
+//   cols: Y := inv(L_B) Y, L_B the block's unit lower triangle: sL
+//         column-major (ld W), zero on and above the diagonal.
+// ---------------------------------------------------------------------------
+template <typename T, int W>
+__device__ __forceinline__ void sweep_rows(T (&x)[W / 4], const T* sU, const T* rd, int bw) {
+    constexpr int CQ = W / 4;
+    const int lane = threadIdx.x & 31, q = lane & 3, base = lane & ~3;
+#pragma unroll 1
+    for (int kq = 0; kq * CQ < bw; ++kq) {
+#pragma unroll
+        for (int kk = 0; kk < CQ; ++kk) {
+            const int k = kq * CQ + kk;
+            if (k >= bw) break;
+            if (q == kq) x[kk] *= rd[k];
+            const T xk = __shfl_sync(0xffffffffu, x[kk], base | kq);
+            const T* u = sU + k * W + q * CQ;
+#pragma unroll
+            for (int jj = 0; jj < CQ; ++jj) x[jj] -= xk * u[jj];
         }
     }
 }
 
-// After the factorisation, one CTA per block (all blocks of all fronts in
-// one launch) turns the pieces' inverses into whole-block operators:
-//   Minv rows of piece q = Li_q (E_q - L_q,<q Minv_<q)     (forward, pieces in order)
-//   Uinv rows of piece p = Ui_p (E_p - U_p,>p Uinv_>p)     (backward, pieces reversed)
-// so that a triangular-solve step of the block is one product, Minv * b or
-// Uinv * c.  Both are written column-major (bw x bw) to inv2[].
-// Dynamic shared memory: 3 * bwmax * (bwmax | 1) T's.
-template <typename T>
-__global__ void __launch_bounds__(256) k_block_inv(const T* fac, const T* inv, T* inv2, Sched S, const int* blk_front,
-                                                    const int* blk_ids, int bwmax) {
+template <typename T, int W>
+__device__ __forceinline__ void sweep_cols(T (&y)[W / 4], const T* sL, int bw) {
+    constexpr int CQ = W / 4;
+    const int lane = threadIdx.x & 31, q = lane & 3, base = lane & ~3;
+#pragma unroll 1
+    for (int kq = 0; kq * CQ < bw; ++kq) {
+#pragma unroll
+        for (int kk = 0; kk < CQ; ++kk) {
+            const int k = kq * CQ + kk;
+            if (k >= bw) break;
+            const T yk = __shfl_sync(0xffffffffu, y[kk], base | kq);
+            const T* l = sL + k * W + q * CQ;
+#pragma unroll
+            for (int ii = 0; ii < CQ; ++ii) y[ii] -= l[ii] * yk;
+        }
+    }
+}
+
+// Row sources of a block's interchanges: applying, piece by piece, the
+// swaps k <-> a + ipiv[k] of the piece [a, b) to a vector v gives
+// v'[R] = v[gmap[R]]; pa[R] = first row of R's piece.  One thread per piece.
+__device__ __forceinline__ void block_gather_map(const int* ipiv_blk, const int* q0, int np, int* gmap, int* pa) {
+    for (int pc = threadIdx.x; pc < np; pc += blockDim.x) {
+        const int a = q0[pc], b = q0[pc + 1];
+        for (int i = a; i < b; ++i) {
+            gmap[i] = i;
+            pa[i] = a;
+        }
+        for (int k = a; k < b; ++k) {
+            const int kp = a + ipiv_blk[k];
+            const int t = gmap[k];
+            gmap[k] = gmap[kp];
+            gmap[kp] = t;
+        }
+    }
+}
+
+// sU and rd from the factored block (column-major at blkp, leading dimension ld).
+template <typename T, int W>
+__device__ __forceinline__ void stage_upper(T* sU, T* rd, const T* blkp, ll ld, int bw) {
+    for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
+        const int j = e % W, k = e / W;
+        sU[k * W + j] = (j > k && j < bw) ? blkp[(ll)j * ld + k] : T(0);
+    }
+    for (int k = threadIdx.x; k < W; k += blockDim.x) rd[k] = k < bw ? T(1) / blkp[(ll)k * ld + k] : T(0);
+}
+
+// sL from the factored block with the rows of each piece, in the columns
+// left of the piece, put in the piece's pivoted order: the interchanges of
+// all pieces then act once, as a gather by gmap, before the sweep (the
+// reference applies a piece's interchanges when the forward elimination
+// reaches it; moving them ahead of the earlier pieces' updates permutes
+// those updates' rows the same way).
+template <typename T, int W>
+__device__ __forceinline__ void stage_lower(T* sL, const T* blkp, ll ld, int bw, const int* gmap, const int* pa) {
+    for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
+        const int i = e % W, k = e / W;
+        T v = T(0);
+        if (i > k && i < bw) v = blkp[(ll)k * ld + (k < pa[i] ? gmap[i] : i)];
+        sL[k * W + i] = v;
+    }
+}
+
+// Panels of block `step` (block width bw <= W): 64-row tiles of the L panel
+// below the block, X := X inv(U_B) (the reference's trsm 'r','u','n','n' of
+// every piece, with the earlier pieces' updates X_p -= X_<p U_<p,p), and
+// 64-column tiles of the U panel to its right, inside the front (Lf) and in
+// U12 (Uf): Y := inv(L_B) P_B Y (_luswap! and trsm 'r','l','t','u' of every
+// piece, with Y_p -= L_p,<p Y_<p).  One line per 4 lanes.
+// Dynamic shared memory: W * W T's.
+template <typename T, int W>
+__global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, Sched S, Launch L, int step) {
+    constexpr int CQ = W / 4;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ int q0[BlockMax<T>::value + 1];
-    __shared__ int wo[BlockMax<T>::value + 1];
-    const int blk = blk_ids[blockIdx.x];
-    const DFront F = S.fronts[blk_front[blk]];
-    const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0, lda = bw | 1;
+    T* sT = reinterpret_cast<T*>(smem_raw);
+    __shared__ T rd[W];
+    __shared__ int q0[W + 1], gmap[W], pa[W];
+    int fid, tile;
+    locate(L, blockIdx.x, fid, tile);
+    const DFront F = S.fronts[fid];
+    const int blk = F.block0 + step;
+    const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
     const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
-    T* A = reinterpret_cast<T*>(smem_raw);        // block, column-major
-    T* M = A + bwmax * (bwmax | 1);               // Minv, row-major (i, j) at i * lda + j
-    T* U = M + bwmax * (bwmax | 1);               // Uinv, row-major
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nw = blockDim.x >> 5;
-    for (int k = tid; k <= np; k += blockDim.x) q0[k] = S.xsuper[p0 + k] - F.f - c0;
-    for (int j = warp; j < bw; j += nw)
-        for (int i = lane; i < bw; i += 32) A[j * lda + i] = fac[F.loff + (ll)(c0 + j) * F.ld + c0 + i];
+    const int tid = threadIdx.x, line = tid >> 2, q = tid & 3;
+    const int nL = cdiv(F.ld - c1, 64), nUa = cdiv(F.nf - c1, 64);
+    const T* blkp = fac + F.loff + (ll)c0 * F.ld + c0;
+    if (tile < nL) {
+        stage_upper<T, W>(sT, rd, blkp, F.ld, bw);
+        __syncthreads();
+        const int r = c1 + tile * 64 + line;
+        const bool ok = r < F.ld;
+        T* xp = fac + F.loff + (ll)c0 * F.ld + r;   // row r, block column j at xp[j * ld]
+        T x[CQ];
+#pragma unroll
+        for (int jj = 0; jj < CQ; ++jj) {
+            const int j = q * CQ + jj;
+            x[jj] = (ok && j < bw) ? xp[(ll)j * F.ld] : T(0);
+        }
+        sweep_rows<T, W>(x, sT, rd, bw);
+#pragma unroll
+        for (int jj = 0; jj < CQ; ++jj) {
+            const int j = q * CQ + jj;
+            if (ok && j < bw) xp[(ll)j * F.ld] = x[jj];
+        }
+    } else {
+        for (int k = tid; k <= np; k += 256) q0[k] = S.xsuper[p0 + k] - F.f - c0;
+        __syncthreads();
+        block_gather_map(ipiv + F.f + c0, q0, np, gmap, pa);
+        __syncthreads();
+        stage_lower<T, W>(sT, blkp, F.ld, bw, gmap, pa);
+        __syncthreads();
+        const bool inner = tile < nL + nUa;
+        const int col = inner ? c1 + (tile - nL) * 64 + line : (tile - nL - nUa) * 64 + line;
+        const bool ok = inner ? col < F.nf : col < F.m;
+        // block row k of this column at cp[k * stride]
+        T* cp = inner ? fac + F.loff + (ll)col * F.ld + c0 : fac + F.uoff + (ll)c0 * F.m + col;
+        const ll stride = inner ? 1 : (ll)F.m;
+        T y[CQ];
+#pragma unroll
+        for (int ii = 0; ii < CQ; ++ii) {
+            const int R = q * CQ + ii;
+            y[ii] = (ok && R < bw) ? cp[(ll)gmap[R] * stride] : T(0);
+        }
+        sweep_cols<T, W>(y, sT, bw);
+#pragma unroll
+        for (int ii = 0; ii < CQ; ++ii) {
+            const int R = q * CQ + ii;
+            if (ok && R < bw) cp[(ll)R * stride] = y[ii];
+        }
+    }
+}
+
+// After the factorisation: the whole-block solve operators of every block,
+//   Minv = inv(L_B) P_B  (the forward steps of all its pieces, in order)
+//   Uinv = inv(U_B)      (the backward steps, pieces reversed)
+// written column-major (bw x bw, Minv then Uinv) at inv2[blk_inv2[blk]], so
+// that a triangular-solve step of a block is one product.  They are the
+// panel sweeps applied to the identity: column j of Minv is the U-panel
+// sweep of e_j, row i of Uinv the L-panel sweep of e_i.  `entries` lists
+// the work: for W == 32 one CTA per block (lines 0..31 Minv columns, 32..63
+// Uinv rows); otherwise entry = blk * 4 + kind * 2 + tile (kind 0 Minv,
+// 1 Uinv; 64 lines per tile).  Dynamic shared memory: 2 * W * W T's for
+// W == 32, else W * W.
+template <typename T, int W>
+__global__ void __launch_bounds__(256) k_block_inv(const T* fac, const int* ipiv, T* inv2, Sched S,
+                                                    const int* blk_front, const int* entries) {
+    constexpr int CQ = W / 4;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ T rd[W];
+    __shared__ int q0[W + 1], gmap[W], pa[W];
+    const int e = entries[blockIdx.x];
+    const int blk = (W == 32) ? e : (e >> 2);
+    const int kind = (W == 32) ? 2 : ((e >> 1) & 1);
+    const int l0 = (W == 32) ? 0 : (e & 1) * 64;
+    const DFront F = S.fronts[blk_front[blk]];
+    const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
+    const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
+    const T* blkp = fac + F.loff + (ll)c0 * F.ld + c0;
+    T* sL = reinterpret_cast<T*>(smem_raw);
+    T* sU = (W == 32) ? sL + W * W : sL;
+    const int tid = threadIdx.x, line = tid >> 2, q = tid & 3;
+    if (kind != 1) {
+        for (int k = tid; k <= np; k += 256) q0[k] = S.xsuper[p0 + k] - F.f - c0;
+        __syncthreads();
+        block_gather_map(ipiv + F.f + c0, q0, np, gmap, pa);
+        __syncthreads();
+        stage_lower<T, W>(sL, blkp, F.ld, bw, gmap, pa);
+    }
+    if (kind != 0) stage_upper<T, W>(sU, rd, blkp, F.ld, bw);
     __syncthreads();
-    if (tid == 0) {
-        int o = 0;
-        for (int pc = 0; pc < np; ++pc) {
-            wo[pc] = o;
-            const int w = q0[pc + 1] - q0[pc];
-            o += 2 * w * w;
-        }
-    }
-    __syncthreads();
-    const T* W = inv + S.blk_inv[blk];
-    for (int pc = 0; pc < np; ++pc) {               // forward operator
-        const int a = q0[pc], b = q0[pc + 1], w = b - a;
-        const T* Li = W + wo[pc] + w * w;
-        for (int i = a + warp; i < b; i += nw)      // T = E_q - L_q,<q Minv_<q  (into M rows of q)
-            for (int j = lane; j < bw; j += 32) {
-                T acc = T(i == j);
-                for (int k = 0; k < a; ++k) acc -= A[k * lda + i] * M[k * lda + j];
-                M[i * lda + j] = acc;
-            }
-        __syncthreads();
-        for (int j = tid; j < bw; j += blockDim.x) {   // rows of q := Li_q T, one thread per column
-            T t[64];
-#pragma unroll
-            for (int k = 0; k < 64; ++k) t[k] = k < w ? M[(a + k) * lda + j] : T(0);
-            for (int i = 0; i < w; ++i) {
-                T acc = T(0);
-#pragma unroll
-                for (int k = 0; k < 64; ++k)
-                    if (k < w) acc += Li[k * w + i] * t[k];
-                M[(a + i) * lda + j] = acc;
-            }
-        }
-        __syncthreads();
-    }
-    for (int pc = np - 1; pc >= 0; --pc) {          // backward operator
-        const int a = q0[pc], b = q0[pc + 1], w = b - a;
-        const T* Ui = W + wo[pc];
-        for (int i = a + warp; i < b; i += nw)      // T = E_p - U_p,>p Uinv_>p
-            for (int j = lane; j < bw; j += 32) {
-                T acc = T(i == j);
-                for (int k = b; k < bw; ++k) acc -= A[k * lda + i] * U[k * lda + j];
-                U[i * lda + j] = acc;
-            }
-        __syncthreads();
-        for (int j = tid; j < bw; j += blockDim.x) {
-            T t[64];
-#pragma unroll
-            for (int k = 0; k < 64; ++k) t[k] = k < w ? U[(a + k) * lda + j] : T(0);
-            for (int i = 0; i < w; ++i) {
-                T acc = T(0);
-#pragma unroll
-                for (int k = 0; k < 64; ++k)
-                    if (k >= i && k < w) acc += Ui[k * w + i] * t[k];
-                U[(a + i) * lda + j] = acc;
-            }
-        }
-        __syncthreads();
-    }
+    const bool doM = (kind == 2) ? line < 32 : kind == 0;
+    const int idx = (kind == 2) ? (line & 31) : l0 + line;
+    if (__all_sync(0xffffffffu, idx >= bw)) return;   // the whole warp is past the block
+    T v[CQ];
     T* out = inv2 + S.blk_inv2[blk];
-    for (int j = warp; j < bw; j += nw)
-        for (int i = lane; i < bw; i += 32) {
-            out[(ll)j * bw + i] = M[i * lda + j];
-            out[(ll)bw * bw + (ll)j * bw + i] = U[i * lda + j];
+    if (doM) {
+#pragma unroll
+        for (int ii = 0; ii < CQ; ++ii) {
+            const int R = q * CQ + ii;
+            v[ii] = (R < bw && gmap[R] == idx) ? T(1) : T(0);
         }
+        sweep_cols<T, W>(v, sL, bw);
+        if (idx < bw) {
+#pragma unroll
+            for (int ii = 0; ii < CQ; ++ii) {
+                const int R = q * CQ + ii;
+                if (R < bw) out[(ll)idx * bw + R] = v[ii];
+            }
+        }
+    } else {
+#pragma unroll
+        for (int jj = 0; jj < CQ; ++jj) v[jj] = (q * CQ + jj == idx) ? T(1) : T(0);
+        sweep_rows<T, W>(v, sU, rd, bw);
+        if (idx < bw) {
+#pragma unroll
+            for (int jj = 0; jj < CQ; ++jj) {
+                const int j = q * CQ + jj;
+                if (j < bw) out[(ll)bw * bw + (ll)j * bw + idx] = v[jj];
+            }
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -729,124 +699,6 @@ __device__ __forceinline__ void mma_tile(const T* sA, const T* sB, int kc, T acc
         for (int i = 0; i < 4; ++i)
 #pragma unroll
             for (int j = 0; j < 4; ++j) acc[i][j] += a[i] * b[j];
-    }
-}
-
-// Panels of block `step`: 64-row tiles of the L panel below the block and
-// 64-column tiles of the U panel to its right (inside the front, stored in
-// Lf, and in U12, stored in Uf).  Piece by piece: an L row gets
-//   X_p := (X_p - X_<p U_<p,p) Ui_p,
-// a U column gets
-//   Y_p := Li_p (Y_p - L_p,<p Y_<p),
-// the reference's two _trsm! panels (after _luswap!) for every piece of the
-// block.  Block entries and inverses are read through the cache.
-// Dynamic shared memory: 64 * bwmax T's.
-template <typename T>
-__global__ void __launch_bounds__(256) k_block_panel(T* fac, const T* inv, Sched S, Launch L, int step, int bwmax) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sX = reinterpret_cast<T*>(smem_raw);   // sX[k * 64 + t], k < bw, t < 64
-    __shared__ int q0[BlockMax<T>::value + 1];
-    int fid, tile;
-    locate(L, blockIdx.x, fid, tile);
-    const DFront F = S.fronts[fid];
-    const int blk = F.block0 + step;
-    const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
-    const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
-    const int tid = threadIdx.x, t = tid & 63, g = tid >> 6;
-    const int nL = cdiv(F.ld - c1, 64), nUa = cdiv(F.nf - c1, 64);
-    const T* blockA = fac + F.loff + (ll)c0 * F.ld + c0;   // (i, j) of the block at j * ld + i
-    const T* W = inv + S.blk_inv[blk];
-    for (int k = tid; k <= np; k += 256) q0[k] = S.xsuper[p0 + k] - F.f - c0;
-    if (tile < nL) {
-        const int r0 = c1 + tile * 64, nr = min(64, F.ld - r0);
-        for (int e = tid; e < 64 * bw; e += 256) {
-            int i = e & 63, k = e >> 6;
-            sX[k * 64 + i] = i < nr ? fac[F.loff + (ll)(c0 + k) * F.ld + r0 + i] : T(0);
-        }
-        __syncthreads();
-        int woff = 0;
-        for (int pc = 0; pc < np; ++pc) {
-            const int a = q0[pc], b = q0[pc + 1], w = b - a;
-            const T* Ui = W + woff;
-            for (int j = a + g; j < b; j += 4) {       // X_p -= X_<p U_<p,p
-                T acc = T(0);
-                for (int k = 0; k < a; ++k) acc += sX[k * 64 + t] * blockA[(ll)j * F.ld + k];
-                sX[j * 64 + t] -= acc;
-            }
-            __syncthreads();
-            T out[16];                                  // X_p := X_p Ui_p, columns a+g+4q
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const int j = g + 4 * q;
-                T acc = T(0);
-                if (j < w)
-                    for (int k = 0; k <= j; ++k) acc += sX[(a + k) * 64 + t] * Ui[j * w + k];
-                out[q] = acc;
-            }
-            __syncthreads();
-#pragma unroll
-            for (int q = 0; q < 16; ++q)
-                if (g + 4 * q < w) sX[(a + g + 4 * q) * 64 + t] = out[q];
-            __syncthreads();
-            woff += 2 * w * w;
-        }
-        for (int e = tid; e < 64 * bw; e += 256) {
-            int i = e & 63, k = e >> 6;
-            if (i < nr) fac[F.loff + (ll)(c0 + k) * F.ld + r0 + i] = sX[k * 64 + i];
-        }
-    } else {
-        const bool inner = tile < nL + nUa;
-        const int col0 = inner ? c1 + (tile - nL) * 64 : (tile - nL - nUa) * 64;
-        const int nc = inner ? min(64, F.nf - col0) : min(64, F.m - col0);
-        if (inner) {
-            for (int e = tid; e < bw * 64; e += 256) {
-                int k = e % bw, c = e / bw;
-                sX[k * 64 + c] = c < nc ? fac[F.loff + (ll)(col0 + c) * F.ld + c0 + k] : T(0);
-            }
-        } else {
-            for (int e = tid; e < bw * 64; e += 256) {
-                int c = e & 63, k = e >> 6;
-                sX[k * 64 + c] = c < nc ? fac[F.uoff + (ll)(c0 + k) * F.m + col0 + c] : T(0);
-            }
-        }
-        __syncthreads();
-        int woff = 0;
-        for (int pc = 0; pc < np; ++pc) {
-            const int a = q0[pc], b = q0[pc + 1], w = b - a;
-            const T* Li = W + woff + w * w;
-            for (int i = a + g; i < b; i += 4) {       // Y_p -= L_p,<p Y_<p
-                T acc = T(0);
-                for (int k = 0; k < a; ++k) acc += blockA[(ll)k * F.ld + i] * sX[k * 64 + t];
-                sX[i * 64 + t] -= acc;
-            }
-            __syncthreads();
-            T out[16];                                  // Y_p := Li_p Y_p, rows a+g+4q
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const int i = g + 4 * q;
-                T acc = T(0);
-                if (i < w)
-                    for (int k = 0; k < w; ++k) acc += Li[k * w + i] * sX[(a + k) * 64 + t];
-                out[q] = acc;
-            }
-            __syncthreads();
-#pragma unroll
-            for (int q = 0; q < 16; ++q)
-                if (g + 4 * q < w) sX[(a + g + 4 * q) * 64 + t] = out[q];
-            __syncthreads();
-            woff += 2 * w * w;
-        }
-        if (inner) {
-            for (int e = tid; e < bw * 64; e += 256) {
-                int k = e % bw, c = e / bw;
-                if (c < nc) fac[F.loff + (ll)(col0 + c) * F.ld + c0 + k] = sX[k * 64 + c];
-            }
-        } else {
-            for (int e = tid; e < bw * 64; e += 256) {
-                int c = e & 63, k = e >> 6;
-                if (c < nc) fac[F.uoff + (ll)(c0 + k) * F.m + col0 + c] = sX[k * 64 + c];
-            }
-        }
     }
 }
 
