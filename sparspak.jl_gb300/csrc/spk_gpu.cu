@@ -633,6 +633,10 @@ static int upload_structure(spk_handle* h) {
 }
 
 // Build (once) and upload the plan of precision T.
+// Dynamic shared memory of the panel sweeps: `n` staged triangles of W lines.
+template <typename T, int W>
+static size_t sweep_smem(int n) { return sizeof(T) * (size_t)n * W * spk::SLD<T, W>::value; }
+
 template <typename T>
 static int ensure_plan(spk_handle* h) {
     Plan& P = h->plan[prec_index<T>()];
@@ -688,9 +692,9 @@ static int ensure_plan(spk_handle* h) {
     S.blk_inv2 = P.d_blk_inv2;
     constexpr int BM = spk::BlockMax<T>::value;
     CU(h, cudaFuncSetAttribute(spk::k_block_panel<T, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)(sizeof(T) * BM * BM)));
+                               (int)sweep_smem<T, BM>(1)));
     CU(h, cudaFuncSetAttribute(spk::k_block_inv<T, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)(sizeof(T) * BM * BM)));
+                               (int)sweep_smem<T, BM>(1)));
     P.built = true;
     return SPK_OK;
 }
@@ -760,20 +764,20 @@ static int factor_launches(spk_handle* h) {
                     spk::k_block_lu_small<T><<<(P.blu[t].count + 3) / 4, 128, 0, h->stream>>>(
                         fac, h->d_ipiv, h->d_info, S, launch_of(PL, P.blu[t]), (int)t);
                 else
-                    spk::k_block_lu<T><<<P.blu[t].tiles, 256, 0, h->stream>>>(
+                    spk::k_block_lu<T><<<P.blu[t].tiles, spk::LuThreads<T>::value, 0, h->stream>>>(
                         fac, h->d_ipiv, h->d_info, S, launch_of(PL, P.blu[t]), (int)t);
             }
             if (P.bpanel[t].tiles > 0) {
                 LaunchScope ls(h, SPK_K_PANEL, P.bpanel[t].flops, P.bpanel[t].words * sizeof(T));
                 const spk::Launch la = launch_of(PL, P.bpanel[t]);
                 if (bw <= 32)
-                    spk::k_block_panel<T, 32><<<P.bpanel[t].tiles, 256, sizeof(T) * 32 * 32, h->stream>>>(
+                    spk::k_block_panel<T, 32><<<P.bpanel[t].tiles, 256, sweep_smem<T, 32>(1), h->stream>>>(
                         fac, h->d_ipiv, S, la, (int)t);
                 else if (bw <= 64)
-                    spk::k_block_panel<T, 64><<<P.bpanel[t].tiles, 256, sizeof(T) * 64 * 64, h->stream>>>(
+                    spk::k_block_panel<T, 64><<<P.bpanel[t].tiles, 256, sweep_smem<T, 64>(1), h->stream>>>(
                         fac, h->d_ipiv, S, la, (int)t);
                 else
-                    spk::k_block_panel<T, BM><<<P.bpanel[t].tiles, 256, sizeof(T) * BM * BM, h->stream>>>(
+                    spk::k_block_panel<T, BM><<<P.bpanel[t].tiles, 256, sweep_smem<T, BM>(1), h->stream>>>(
                         fac, h->d_ipiv, S, la, (int)t);
             }
             if (P.btrail[t].tiles > 0) {
@@ -794,13 +798,13 @@ static int factor_launches(spk_handle* h) {
         const int* ent = PL.d_inv_ids + PL.inv_off[c];
         T* inv2 = storage<T>(h).inv2;
         if (c == 0)
-            spk::k_block_inv<T, 32><<<cnt, 256, sizeof(T) * 2 * 32 * 32, h->stream>>>(fac, h->d_ipiv, inv2, S,
+            spk::k_block_inv<T, 32><<<cnt, 256, sweep_smem<T, 32>(2), h->stream>>>(fac, h->d_ipiv, inv2, S,
                                                                                       PL.d_blk_front, ent);
         else if (c == 1)
-            spk::k_block_inv<T, 64><<<cnt, 256, sizeof(T) * 64 * 64, h->stream>>>(fac, h->d_ipiv, inv2, S,
+            spk::k_block_inv<T, 64><<<cnt, 256, sweep_smem<T, 64>(1), h->stream>>>(fac, h->d_ipiv, inv2, S,
                                                                                   PL.d_blk_front, ent);
         else
-            spk::k_block_inv<T, BM><<<cnt, 256, sizeof(T) * BM * BM, h->stream>>>(fac, h->d_ipiv, inv2, S,
+            spk::k_block_inv<T, BM><<<cnt, 256, sweep_smem<T, BM>(1), h->stream>>>(fac, h->d_ipiv, inv2, S,
                                                                                   PL.d_blk_front, ent);
     }
     CU(h, cudaGetLastError());

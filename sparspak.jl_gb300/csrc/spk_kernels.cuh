@@ -266,8 +266,8 @@ __global__ void __launch_bounds__(128) k_block_lu_small(T* fac, int* ipiv, int* 
     }
 }
 
-// First row holding the largest key, two candidate rows per lane (`idx`
-// the row of `key`): the reference's first strict maximum.
+// First row holding the largest key (`idx` the row of this lane's key):
+// the reference's first strict maximum.
 __device__ __forceinline__ int warp_first_max_row(unsigned long long key, int idx) {
     const unsigned FULL = 0xffffffffu;
     const unsigned hi = (unsigned)(key >> 32), lo = (unsigned)key;
@@ -275,11 +275,41 @@ __device__ __forceinline__ int warp_first_max_row(unsigned long long key, int id
     const unsigned ml = __reduce_max_sync(FULL, hi == mh ? lo : 0u);
     return (int)__reduce_min_sync(FULL, (hi == mh && lo == ml) ? (unsigned)idx : 0xffffffffu);
 }
+__device__ __forceinline__ int warp_first_max_row(unsigned key, int idx) {
+    const unsigned FULL = 0xffffffffu;
+    const unsigned m = __reduce_max_sync(FULL, key);
+    return (int)__reduce_min_sync(FULL, key == m ? (unsigned)idx : 0xffffffffu);
+}
+// 32-bit pivot key of a float (same order as pivot_key).
+__device__ __forceinline__ unsigned pivot_key32(float x, bool cand, bool diag) {
+    if (!cand) return 0u;
+    const unsigned b = __float_as_uint(x) & 0x7fffffffu;
+    if (b > 0x7f800000u) return diag ? 0xffffffffu : 1u;
+    return b + 2u;
+}
+template <typename T> struct PivotKey;
+template <> struct PivotKey<float> {
+    using type = unsigned;
+    __device__ static type of(float x, bool cand, bool diag) { return pivot_key32(x, cand, diag); }
+};
+template <> struct PivotKey<double> {
+    using type = unsigned long long;
+    __device__ static type of(double x, bool cand, bool diag) { return pivot_key(x, cand, diag); }
+};
+
+// r[k] for a runtime k < N, by selects (no dynamic register indexing).
+template <typename T, int N>
+__device__ __forceinline__ T pick_n(const T (&r)[N], int k) {
+    T v = r[0];
+#pragma unroll
+    for (int i = 1; i < N; ++i) v = (k == i) ? r[i] : v;
+    return v;
+}
 
 // Block LU by a whole CTA (blocks of 33..BlockMax columns; one CTA per
-// front).  The 256 threads form a 16 x 16 grid; thread (ty, tx) keeps rows
-// [ty*TR, ty*TR+TR) x columns [tx*TR, tx*TR+TR) of the block in registers
-// (TR = BlockMax / 16).  For each column k, in piece [a, b):
+// front).  The LU_THREADS threads form a G x G grid (G = BlockMax / 4);
+// thread (ty, tx) keeps rows [4ty, 4ty+4) x columns [4tx, 4tx+4) of the
+// block in registers, and a warp holds whole row groups.  For each column k, in piece [a, b):
 //   - the owners of column k publish its rows >= k, the owners of row k
 //     publish its columns >= a (shared memory, double-buffered);
 //   - every warp finds the pivot: the first strict maximum of |A(i,k)| over
@@ -293,11 +323,16 @@ __device__ __forceinline__ int warp_first_max_row(unsigned long long key, int id
 //     no scaling after a zero pivot), then the rank-1 update of rows and
 //     columns after k (ggetrf!, the U-panel trsm 'r','l','t','u' and the
 //     block-local Schur update).
-// One barrier per column, two when rows swap.  ipiv receives the local
+// One barrier per column, two when rows swap.  The column loop is unrolled
+// by the tile width, so that column / row k of a tile are fixed registers;
+// the small tile keeps the unrolled body small.  ipiv receives the local
 // pivot row within the piece; a zero pivot records the piece in info.
+template <typename T> struct LuThreads { static constexpr int value = (BlockMax<T>::value / 4) * (BlockMax<T>::value / 4); };
 template <typename T>
-__global__ void __launch_bounds__(256) k_block_lu(T* fac, int* ipiv, int* info, Sched S, Launch L, int step) {
-    constexpr int BM = BlockMax<T>::value, TR = BM / 16;
+__global__ void __launch_bounds__(LuThreads<T>::value) k_block_lu(T* fac, int* ipiv, int* info, Sched S, Launch L,
+                                                                   int step) {
+    constexpr int BM = BlockMax<T>::value, TR = 4, G = BM / TR, NT = G * G;
+    using Key = typename PivotKey<T>::type;
     __shared__ __align__(16) T cbuf[2][BM];
     __shared__ __align__(16) T rbuf[2][2][BM];
     __shared__ int q0[BM + 1];
@@ -309,10 +344,10 @@ __global__ void __launch_bounds__(256) k_block_lu(T* fac, int* ipiv, int* info, 
     const int blk = F.block0 + step;
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
     const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
-    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15, lane = tid & 31;
+    const int tid = threadIdx.x, ty = tid / G, tx = tid % G, lane = tid & 31;
     const int r0 = ty * TR, cl0 = tx * TR;
-    for (int k = tid; k <= np; k += 256) q0[k] = S.xsuper[p0 + k] - F.f - c0;
-    for (int i = tid; i < 2 * BM; i += 256) {
+    for (int k = tid; k <= np; k += NT) q0[k] = S.xsuper[p0 + k] - F.f - c0;
+    for (int i = tid; i < 2 * BM; i += NT) {
         (&cbuf[0][0])[i] = T(0);
         (&rbuf[0][0][0])[i] = T(0);
         (&rbuf[0][0][0])[2 * BM + i] = T(0);
@@ -358,8 +393,8 @@ __global__ void __launch_bounds__(256) k_block_lu(T* fac, int* ipiv, int* info, 
             int kp;
             {
                 const int i1 = k + lane, i2 = k + 32 + lane;
-                const unsigned long long k1 = pivot_key(cb[min(i1, BM - 1)], i1 < b, i1 == k);
-                const unsigned long long k2 = pivot_key(cb[min(i2, BM - 1)], i2 < b, false);
+                const Key k1 = PivotKey<T>::of(cb[min(i1, BM - 1)], i1 < b, i1 == k);
+                const Key k2 = PivotKey<T>::of(cb[min(i2, BM - 1)], i2 < b, false);
                 const bool second = k2 > k1;   // ties keep the earlier row
                 kp = warp_first_max_row(second ? k2 : k1, second ? i2 : i1);
             }
@@ -435,7 +470,7 @@ __global__ void __launch_bounds__(256) k_block_lu(T* fac, int* ipiv, int* info, 
             if (R < bw && C < bw) blkp[(ll)C * F.ld + R] = a[ii][jj];
         }
     __syncthreads();
-    for (int c = tid; c < bw; c += 256) ipiv[F.f + c0 + c] = spiv[c];
+    for (int c = tid; c < bw; c += NT) ipiv[F.f + c0 + c] = spiv[c];
     if (tid == 0 && szero != INT_MAX) {
         int p = 0;
         while (q0[p + 1] <= szero) ++p;
@@ -452,10 +487,21 @@ __global__ void __launch_bounds__(256) k_block_lu(T* fac, int* ipiv, int* info, 
 // shared memory (the triangles are staged with zeros outside the strict
 // part, so the updates need no predicates).
 //   rows: X := X inv(U_B), U_B the block's upper triangle with its diagonal:
-//         sU row-major (ld W), zero on and below the diagonal, rd[k] = 1/U(k,k);
-//   cols: Y := inv(L_B) Y, L_B the block's unit lower triangle: sL
-//         column-major (ld W), zero on and above the diagonal.
+//         sU by rows, zero on and below the diagonal, rd[k] = 1/U(k,k);
+//   cols: Y := inv(L_B) Y, L_B the block's unit lower triangle: sL by
+//         columns, zero on and above the diagonal.
+// A staged row (column) is SLD(W) entries: the four lanes' chunks of CQ
+// entries each start 16 bytes apart in the bank cycle (chunk q at
+// q * (CQ + SK)), so their 16-byte loads do not collide.
 // ---------------------------------------------------------------------------
+template <typename T> struct Skew { static constexpr int value = 16 / sizeof(T); };
+template <typename T, int W> struct SLD { static constexpr int value = W + 4 * Skew<T>::value; };
+template <typename T, int W>
+__device__ __forceinline__ int sidx(int k, int j) {   // entry j of staged row / column k
+    constexpr int CQ = W / 4, SK = Skew<T>::value;
+    return k * SLD<T, W>::value + (j / CQ) * (CQ + SK) + (j % CQ);
+}
+
 template <typename T, int W>
 __device__ __forceinline__ void sweep_rows(T (&x)[W / 4], const T* sU, const T* rd, int bw) {
     constexpr int CQ = W / 4;
@@ -468,7 +514,7 @@ __device__ __forceinline__ void sweep_rows(T (&x)[W / 4], const T* sU, const T* 
             if (k >= bw) break;
             if (q == kq) x[kk] *= rd[k];
             const T xk = __shfl_sync(0xffffffffu, x[kk], base | kq);
-            const T* u = sU + k * W + q * CQ;
+            const T* u = sU + k * SLD<T, W>::value + q * (CQ + Skew<T>::value);
 #pragma unroll
             for (int jj = 0; jj < CQ; ++jj) x[jj] -= xk * u[jj];
         }
@@ -486,7 +532,7 @@ __device__ __forceinline__ void sweep_cols(T (&y)[W / 4], const T* sL, int bw) {
             const int k = kq * CQ + kk;
             if (k >= bw) break;
             const T yk = __shfl_sync(0xffffffffu, y[kk], base | kq);
-            const T* l = sL + k * W + q * CQ;
+            const T* l = sL + k * SLD<T, W>::value + q * (CQ + Skew<T>::value);
 #pragma unroll
             for (int ii = 0; ii < CQ; ++ii) y[ii] -= l[ii] * yk;
         }
@@ -517,7 +563,7 @@ template <typename T, int W>
 __device__ __forceinline__ void stage_upper(T* sU, T* rd, const T* blkp, ll ld, int bw) {
     for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
         const int j = e % W, k = e / W;
-        sU[k * W + j] = (j > k && j < bw) ? blkp[(ll)j * ld + k] : T(0);
+        sU[sidx<T, W>(k, j)] = (j > k && j < bw) ? blkp[(ll)j * ld + k] : T(0);
     }
     for (int k = threadIdx.x; k < W; k += blockDim.x) rd[k] = k < bw ? T(1) / blkp[(ll)k * ld + k] : T(0);
 }
@@ -534,7 +580,7 @@ __device__ __forceinline__ void stage_lower(T* sL, const T* blkp, ll ld, int bw,
         const int i = e % W, k = e / W;
         T v = T(0);
         if (i > k && i < bw) v = blkp[(ll)k * ld + (k < pa[i] ? gmap[i] : i)];
-        sL[k * W + i] = v;
+        sL[sidx<T, W>(k, i)] = v;
     }
 }
 
@@ -544,7 +590,7 @@ __device__ __forceinline__ void stage_lower(T* sL, const T* blkp, ll ld, int bw,
 // 64-column tiles of the U panel to its right, inside the front (Lf) and in
 // U12 (Uf): Y := inv(L_B) P_B Y (_luswap! and trsm 'r','l','t','u' of every
 // piece, with Y_p -= L_p,<p Y_<p).  One line per 4 lanes.
-// Dynamic shared memory: W * W T's.
+// Dynamic shared memory: W * SLD(W) T's.
 template <typename T, int W>
 __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, Sched S, Launch L, int step) {
     constexpr int CQ = W / 4;
@@ -616,8 +662,8 @@ __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, Sc
 // sweep of e_j, row i of Uinv the L-panel sweep of e_i.  `entries` lists
 // the work: for W == 32 one CTA per block (lines 0..31 Minv columns, 32..63
 // Uinv rows); otherwise entry = blk * 4 + kind * 2 + tile (kind 0 Minv,
-// 1 Uinv; 64 lines per tile).  Dynamic shared memory: 2 * W * W T's for
-// W == 32, else W * W.
+// 1 Uinv; 64 lines per tile).  Dynamic shared memory: 2 * W * SLD(W) T's
+// for W == 32, else W * SLD(W).
 template <typename T, int W>
 __global__ void __launch_bounds__(256) k_block_inv(const T* fac, const int* ipiv, T* inv2, Sched S,
                                                     const int* blk_front, const int* entries) {
@@ -634,7 +680,7 @@ __global__ void __launch_bounds__(256) k_block_inv(const T* fac, const int* ipiv
     const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
     const T* blkp = fac + F.loff + (ll)c0 * F.ld + c0;
     T* sL = reinterpret_cast<T*>(smem_raw);
-    T* sU = (W == 32) ? sL + W * W : sL;
+    T* sU = (W == 32) ? sL + W * SLD<T, W>::value : sL;
     const int tid = threadIdx.x, line = tid >> 2, q = tid & 3;
     if (kind != 1) {
         for (int k = tid; k <= np; k += 256) q0[k] = S.xsuper[p0 + k] - F.f - c0;
