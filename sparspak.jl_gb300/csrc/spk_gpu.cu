@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 #include <new>
 #include <type_traits>
 #include <string>
@@ -52,9 +53,14 @@ struct Timed {
 // panel and trailing kernels; then the Schur complements; for the solves
 // the forward block steps, and backward the U12 product and block steps.
 struct LevelPlan {
-    LaunchRec schur, bwdu;
-    std::vector<LaunchRec> blu, bpanel, btrail, fwd, bwd;
+    LaunchRec schur, schur_tc, bwdu;
+    std::vector<LaunchRec> blu, bpanel, btrail, btrail_tc, fwd, bwd;
 };
+
+// FP32 fronts whose rank updates go to the tensor cores (128 x 128 tiles):
+// Schur complements with at least TC_SCHUR_M rows, trailing updates with at
+// least TC_TRAIL_ROWS rows below the block and a block of TC_TRAIL_BW columns.
+constexpr int TC_SCHUR_M = 96, TC_TRAIL_ROWS = 128, TC_TRAIL_BW = 32;
 
 // Block partition and schedule for one precision (block width BlockMax<T>).
 struct Plan {
@@ -495,7 +501,7 @@ static void add_launch(Plan* h, LaunchRec& rec, const std::vector<int>& ids, con
 
 // Group each front's pieces into blocks of at most `bmax` columns and lay
 // out the launches of every level.
-static void build_plan(const spk_handle* h, Plan& P, int bmax) {
+static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
     using spk::cdiv;
     P = Plan();
     P.bmax = bmax;
@@ -555,15 +561,16 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax) {
         L.blu.resize(maxb);
         L.bpanel.resize(maxb);
         L.btrail.resize(maxb);
+        L.btrail_tc.resize(maxb);
         L.fwd.resize(maxb);
         L.bwd.resize(maxb);
         for (int t = 0; t < maxb; ++t) {
-            std::vector<int> tl(nid), tp(nid), tt(nid), tf(nid), tb(nid);
+            std::vector<int> tl(nid), tp(nid), tt(nid), ttc(nid), tf(nid), tb(nid);
             std::vector<double> fl(nid), wl(nid), fp(nid), wp(nid), ft(nid), wt(nid), ff(nid), wf(nid), fb(nid), wb(nid);
             for (size_t k = 0; k < nid; ++k) {
                 const HFront& F = h->fronts[ids[k]];
                 const int nb = P.nblocks[ids[k]];
-                if (t >= nb) { tl[k] = tp[k] = tt[k] = tf[k] = tb[k] = 0; continue; }
+                if (t >= nb) { tl[k] = tp[k] = tt[k] = ttc[k] = tf[k] = tb[k] = 0; continue; }
                 const int blk = P.block0[ids[k]] + t;
                 const int c0 = P.blk_c0[blk], c1 = P.blk_c1[blk];
                 const double bw = c1 - c0;
@@ -576,6 +583,12 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax) {
                 fp[k] = bw * bw * rowsL + 2.0 * bw * bw * colsU;
                 wp[k] = 2.0 * bw * (rowsL + colsU) + 2.0 * bw * bw;
                 tt[k] = cdiv(ld - c1, spk::TT) * cdiv(F.nf - c1, spk::TT) + cdiv(F.nf - c1, spk::TT) * cdiv(F.m, spk::TT);
+                ttc[k] = 0;
+                if (tc && ld - c1 >= TC_TRAIL_ROWS && c1 - c0 >= TC_TRAIL_BW) {
+                    const int T2 = spk::umma::TM;
+                    ttc[k] = cdiv(ld - c1, T2) * cdiv(F.nf - c1, T2) + cdiv(F.nf - c1, T2) * cdiv(F.m, T2);
+                    tt[k] = 0;
+                }
                 const double area = (double)(ld - c1) * (F.nf - c1) + (double)(F.nf - c1) * F.m;
                 ft[k] = 2.0 * bw * area;
                 wt[k] = 2.0 * area + bw * (rowsL + colsU);
@@ -599,14 +612,20 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax) {
                 }
             L.blu[t].bw = L.bpanel[t].bw = bwl;
             add_launch(&P, L.btrail[t], ids, tt, ft, wt);
+            add_launch(&P, L.btrail_tc[t], ids, ttc, ft, wt);
             add_launch(&P, L.fwd[t], ids, tf, ff, wf);
             add_launch(&P, L.bwd[t], ids, tb, fb, wb);
         }
-        std::vector<int> tsch(nid), tbu(nid);
+        std::vector<int> tsch(nid), tsch_tc(nid), tbu(nid);
         std::vector<double> fs(nid), ws(nid), fu(nid), wu(nid);
         for (size_t k = 0; k < nid; ++k) {
             const HFront& F = h->fronts[ids[k]];
             tsch[k] = F.m > 0 ? cdiv(F.m, spk::TT) * cdiv(F.m, spk::TT) : 0;
+            tsch_tc[k] = 0;
+            if (tc && F.m >= TC_SCHUR_M) {
+                tsch_tc[k] = cdiv(F.m, spk::umma::TM) * cdiv(F.m, spk::umma::TN);
+                tsch[k] = 0;
+            }
             tbu[k] = F.m > 0 ? cdiv(F.nf, spk::TS / 32) : 0;
             fs[k] = 2.0 * (double)F.m * F.m * F.nf;
             ws[k] = 2.0 * (double)F.m * F.nf + 2.0 * (double)F.m * F.m;
@@ -614,6 +633,7 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax) {
             wu[k] = (double)F.m * F.nf;
         }
         add_launch(&P, L.schur, ids, tsch, fs, ws);
+        add_launch(&P, L.schur_tc, ids, tsch_tc, fs, ws);
         add_launch(&P, L.bwdu, ids, tbu, fu, wu);
     }
 }
@@ -628,7 +648,7 @@ static int upload_structure(spk_handle* h) {
     if ((rc = upload(h, &h->d_run_rel, h->run_rel))) return rc;
     if ((rc = upload(h, &h->d_rel, h->rel))) return rc;
     CU(h, cudaMalloc((void**)&h->d_ipiv, sizeof(int) * std::max<i64>(h->n, 1)));
-    CU(h, cudaMalloc((void**)&h->d_info, sizeof(int)));
+    CU(h, cudaMalloc((void**)&h->d_info, 2 * sizeof(int)));   // first singular piece, tensor-core timeout
     return SPK_OK;
 }
 
@@ -642,7 +662,7 @@ static int ensure_plan(spk_handle* h) {
     Plan& P = h->plan[prec_index<T>()];
     if (P.built) return SPK_OK;
     try {
-        build_plan(h, P, spk::BlockMax<T>::value);
+        build_plan(h, P, spk::BlockMax<T>::value, std::is_same<T, float>::value);
     } catch (const std::bad_alloc&) {
         return set_err(h, SPK_ENOMEM, "host allocation failed while planning");
     }
@@ -695,6 +715,11 @@ static int ensure_plan(spk_handle* h) {
                                (int)sweep_smem<T, BM>(1)));
     CU(h, cudaFuncSetAttribute(spk::k_block_inv<T, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)sweep_smem<T, BM>(1)));
+    if (std::is_same<T, float>::value) {
+        CU(h, cudaFuncSetAttribute(spk::k_schur_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, spk::umma::SMEM));
+        CU(h, cudaFuncSetAttribute(spk::k_block_trail_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   spk::umma::SMEM));
+    }
     P.built = true;
     return SPK_OK;
 }
@@ -785,10 +810,24 @@ static int factor_launches(spk_handle* h) {
                 spk::k_block_trail<T><<<P.btrail[t].tiles, 256, 0, h->stream>>>(fac, S, launch_of(PL, P.btrail[t]),
                                                                                  (int)t);
             }
+            if constexpr (std::is_same<T, float>::value) {
+                if (P.btrail_tc[t].tiles > 0) {
+                    LaunchScope ls(h, SPK_K_TRAIL, P.btrail_tc[t].flops, P.btrail_tc[t].words * sizeof(T));
+                    spk::k_block_trail_tc<<<P.btrail_tc[t].tiles, 256, spk::umma::SMEM, h->stream>>>(
+                        fac, S, launch_of(PL, P.btrail_tc[t]), (int)t, h->d_info + 1);
+                }
+            }
         }
         if (P.schur.tiles > 0) {
             LaunchScope ls(h, SPK_K_SCHUR, P.schur.flops, P.schur.words * sizeof(T));
             spk::k_schur<T><<<P.schur.tiles, 256, 0, h->stream>>>(fac, S, launch_of(PL, P.schur));
+        }
+        if constexpr (std::is_same<T, float>::value) {
+            if (P.schur_tc.tiles > 0) {
+                LaunchScope ls(h, SPK_K_SCHUR, P.schur_tc.flops, P.schur_tc.words * sizeof(T));
+                spk::k_schur_tc<<<P.schur_tc.tiles, 256, spk::umma::SMEM, h->stream>>>(fac, S, launch_of(PL, P.schur_tc),
+                                                                                      h->d_info + 1);
+            }
         }
     }
     for (int c = 0; c < 3; ++c) {
@@ -813,8 +852,8 @@ static int factor_launches(spk_handle* h) {
 
 template <typename T>
 static int run_factor(spk_handle* h) {
-    const int big = INT_MAX;
-    CU(h, cudaMemcpyAsync(h->d_info, &big, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    static const int init[2] = {INT_MAX, 0};
+    CU(h, cudaMemcpyAsync(h->d_info, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
     return via_graph(h, h->g_factor[prec_index<T>()], [&] { return factor_launches<T>(h); });
 }
 
@@ -1134,9 +1173,11 @@ int spk_factor(spk_handle* h, int precision, int64_t* first_singular) {
         if (!h->s32.loaded && (rc = load_into<float>(h))) return rc;
         if ((rc = run_factor<float>(h))) return rc;
     }
-    int info = INT_MAX;
-    CU(h, cudaMemcpyAsync(&info, h->d_info, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    int info2[2] = {INT_MAX, 0};
+    CU(h, cudaMemcpyAsync(info2, h->d_info, sizeof(info2), cudaMemcpyDeviceToHost, h->stream));
     CU(h, cudaStreamSynchronize(h->stream));
+    const int info = info2[0];
+    if (info2[1]) return set_err(h, SPK_ECUDA, "spk_factor: a tensor-core wait timed out");
     if (precision == SPK_FP64) { h->s64.loaded = false; h->s64.factored = true; }
     else { h->s32.loaded = false; h->s32.factored = true; }
     if (info != INT_MAX) {

@@ -29,6 +29,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "spk_umma.cuh"
+
 namespace spk {
 
 typedef long long ll;
@@ -830,6 +832,76 @@ __global__ void __launch_bounds__(256) k_block_trail(T* fac, Sched S, Launch L, 
     }
 }
 
+// Trailing update after block `step` on the tensor cores (FP32 storage,
+// 3xTF32 products), 128 x 128 tiles: the same regions as k_block_trail.
+__global__ void __launch_bounds__(256, 2) k_block_trail_tc(float* fac, Sched S, Launch L, int step, int* err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const umma::Ctx cx = umma::ctx_of(smem_raw);
+    const uint32_t tmem = umma::begin(cx);
+    unsigned uses = 0;
+    int fid, tile;
+    locate(L, blockIdx.x, fid, tile);
+    const DFront F = S.fronts[fid];
+    const int blk = F.block0 + step;
+    const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk];
+    const int nrL = cdiv(F.ld - c1, umma::TM), ncL = cdiv(F.nf - c1, umma::TN);
+    const bool isL = tile < nrL * ncL;
+    int r0, col0, nr, nc;
+    if (isL) {
+        r0 = c1 + (tile % nrL) * umma::TM;
+        col0 = c1 + (tile / nrL) * umma::TN;
+        nr = min(umma::TM, F.ld - r0);
+        nc = min(umma::TN, F.nf - col0);
+    } else {
+        const int t2 = tile - nrL * ncL, nrU = cdiv(F.nf - c1, umma::TM);
+        r0 = c1 + (t2 % nrU) * umma::TM;
+        col0 = (t2 / nrU) * umma::TN;   // U12 column index
+        nr = min(umma::TM, F.nf - r0);
+        nc = min(umma::TN, F.m - col0);
+    }
+    const umma::Operand A{fac + F.loff + (ll)c0 * F.ld + r0, F.ld, nr, false};
+    const umma::Operand B = isL ? umma::Operand{fac + F.loff + (ll)col0 * F.ld + c0, F.ld, nc, true}
+                                : umma::Operand{fac + F.uoff + (ll)c0 * F.m + col0, F.m, nc, false};
+    umma::tile_product(cx, tmem, A, B, c1 - c0, uses, err);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = 32 * (warp & 3) + lane;
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+        const int col = (warp >> 2) * 64 + h * 32;
+        float v[32];
+        umma::tmem_ld32(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + col, v);
+        if (r < nr) {
+            if (isL) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    if (col + j < nc) fac[F.loff + (ll)(col0 + col + j) * F.ld + r0 + r] -= v[j];
+            } else {
+                float* dst = fac + F.uoff + (ll)(r0 + r) * F.m + col0 + col;
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    if (col + j < nc) dst[j] -= v[j];
+            }
+        }
+    }
+    umma::end(cx, tmem);
+}
+
+// Subtract C(r, c) of a front's Schur complement from its ancestor: the
+// entry belongs to the front of R_F[min(r, c)], whose run gives the positions.
+template <typename T>
+__device__ __forceinline__ void schur_scatter(T* fac, const Sched& S, const int* runid, int r, int c, T v) {
+    const int x = min(r, c);
+    const int g = runid[x];
+    const DFront G = S.fronts[S.run_tgt[g]];
+    const ll base = S.run_rel[g] - S.run_start[g];
+    const int pr = S.rel[base + r], pc = S.rel[base + c];
+    if (pr < 0 || pc < 0) return;     // exact zero: (r, c) is padding of F only
+    ll addr;
+    if (r >= c || pc < G.nf) addr = G.loff + (ll)pc * G.ld + pr;
+    else addr = G.uoff + (ll)pr * G.m + (pc - G.nf);
+    atomicAdd(&fac[addr], -v);
+}
+
 // Schur complement of every front in the launch: C = L21 * U12 (m x m,
 // inner dimension nf), scatter-subtracted into the ancestors.  An entry
 // (r, c) of C belongs to the front of column R_F[c] when r >= c (an L
@@ -871,19 +943,84 @@ __global__ void __launch_bounds__(256) k_schur(T* fac, Sched S, Launch L) {
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
             const int r = r0 + tx + 16 * a;
-            if (r - r0 >= nr) continue;
-            const int x = min(r, c);
-            const int g = runid[x];
-            const DFront G = S.fronts[S.run_tgt[g]];
-            const ll base = S.run_rel[g] - S.run_start[g];
-            const int pr = S.rel[base + r], pc = S.rel[base + c];
-            if (pr < 0 || pc < 0) continue;     // exact zero: (r, c) is padding of F only
-            ll addr;
-            if (r >= c || pc < G.nf) addr = G.loff + (ll)pc * G.ld + pr;
-            else addr = G.uoff + (ll)pr * G.m + (pc - G.nf);
-            atomicAdd(&fac[addr], -acc[a][b]);
+            if (r - r0 < nr) schur_scatter(fac, S, runid, r, c, acc[a][b]);
         }
     }
+}
+
+// Schur complement on the tensor cores (FP32 storage, 3xTF32 products):
+// 128 x 128 tiles of C = L21 * U12 per CTA, scattered like k_schur.  The
+// scatter uses per-tile tables: for each tile column c the target front of
+// R_F[c] and c's position there (entries r >= c), for each tile row r the
+// same for R_F[r] (entries r < c); an entry then needs one rel[] load.
+struct ScatterRow {
+    ll rel0;     // offset in rel[] of R_F[0] for the run of this row / column
+    ll loff, uoff;
+    int ld, nf, m, pos;
+};
+
+__global__ void __launch_bounds__(256, 2) k_schur_tc(float* fac, Sched S, Launch L, int* err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ ScatterRow tab[2][umma::TM];   // [0] tile columns, [1] tile rows
+    const umma::Ctx cx = umma::ctx_of(smem_raw);
+    const uint32_t tmem = umma::begin(cx);
+    unsigned uses = 0;
+    int fid, tile;
+    locate(L, blockIdx.x, fid, tile);
+    const DFront F = S.fronts[fid];
+    const int nt = cdiv(F.m, umma::TM);
+    const int r0 = (tile % nt) * umma::TM, c0 = (tile / nt) * umma::TN;
+    const int* runid = S.runid + F.runid_off;
+    {
+        const int side = threadIdx.x >> 7, t = threadIdx.x & 127;
+        const int x = (side == 0 ? c0 : r0) + t;
+        ScatterRow e{};
+        e.pos = -1;
+        if (x < F.m) {
+            const int g = runid[x];
+            const DFront G = S.fronts[S.run_tgt[g]];
+            e.rel0 = S.run_rel[g] - S.run_start[g];
+            e.loff = G.loff;
+            e.uoff = G.uoff;
+            e.ld = G.ld;
+            e.nf = G.nf;
+            e.m = G.m;
+            e.pos = S.rel[e.rel0 + x];
+        }
+        tab[side][t] = e;
+    }
+    __syncthreads();
+    const umma::Operand A{fac + F.loff + F.nf + r0, F.ld, min(umma::TM, F.m - r0), false};
+    const umma::Operand B{fac + F.uoff + c0, F.m, min(umma::TN, F.m - c0), false};
+    umma::tile_product(cx, tmem, A, B, F.nf, uses, err);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ir = 32 * (warp & 3) + lane, r = r0 + ir;
+    const ScatterRow& R = tab[1][ir];
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+        const int col = (warp >> 2) * 64 + h * 32;
+        float v[32];
+        umma::tmem_ld32(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + col, v);
+        if (r < F.m) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const int c = c0 + col + j;
+                if (c >= F.m) continue;
+                if (r >= c) {   // L entry of the front of R_F[c]
+                    const ScatterRow& Cc = tab[0][col + j];
+                    const int pr = S.rel[Cc.rel0 + r];
+                    if (pr >= 0 && Cc.pos >= 0) atomicAdd(&fac[Cc.loff + (ll)Cc.pos * Cc.ld + pr], -v[j]);
+                } else {        // entry of the front of R_F[r]
+                    const int pc = S.rel[R.rel0 + c];
+                    if (pc >= 0 && R.pos >= 0) {
+                        const ll addr = pc < R.nf ? R.loff + (ll)pc * R.ld + R.pos : R.uoff + (ll)R.pos * R.m + (pc - R.nf);
+                        atomicAdd(&fac[addr], -v[j]);
+                    }
+                }
+            }
+        }
+    }
+    umma::end(cx, tmem);
 }
 
 // ---------------------------------------------------------------------------

@@ -219,3 +219,30 @@ def test_device_resident_arrays():
     x = bt.cpu().numpy().T
     r = b - A @ x
     assert np.max(np.linalg.norm(r, axis=0) / np.linalg.norm(b, axis=0)) < 1e-12
+
+
+@pytest.mark.parametrize("kind", ["laplace", "convdiff"])
+def test_fp32_tensor_core_updates(kind):
+    # 24^3 / 20^3 grids: fronts with m >= 96 (Schur complement on the tensor
+    # cores) and multi-block fronts with >= 128 rows below a block (trailing
+    # update on the tensor cores), 3xTF32 products into FP32 storage
+    if kind == "laplace":
+        A, g = S.gallery.laplacian((24, 24, 24), shift=1e-3), (24, 24, 24)
+    else:
+        A, g = S.gallery.convection_diffusion(k=20), (20, 20, 20)
+    s = S.SparseSolver(A, precision="fp32")
+    S.findorder_(s, S.nd_grid(*g))
+    S.symbolicfactor_(s)
+    o = oracle.OracleLU(s.slvr)
+    o.inmatrix_csc(*S.sparse_solver._matrix_arrays(A))
+    o.factor()
+    S.inmatrix_(s)
+    S.factor_(s)
+    assert np.array_equal(s.slvr.ipiv, o.ipiv)
+    assert rel(s.slvr.lnz, o.lnz) < 1e-4
+    assert rel(s.slvr.unz, o.unz[: s.slvr.unz.size]) < 1e-4
+    b = S.gallery.random_rhs(A.shape[0], 2, seed=4)
+    x, it, rr = S.refine_(s, b, precision="fp32", tol=1e-12)
+    assert rr <= 1e-12 and it <= 6
+    r = b - A @ x
+    assert np.max(np.linalg.norm(r, axis=0) / np.linalg.norm(b, axis=0)) <= 1e-12
