@@ -57,10 +57,11 @@ struct LevelPlan {
     std::vector<LaunchRec> blu, bpanel, btrail, btrail_tc, fwd, bwd;
 };
 
-// FP32 fronts whose rank updates go to the tensor cores (128 x 128 tiles):
-// Schur complements with at least TC_SCHUR_M rows, trailing updates with at
-// least TC_TRAIL_ROWS rows below the block and a block of TC_TRAIL_BW columns.
-constexpr int TC_SCHUR_M = 96, TC_TRAIL_ROWS = 128, TC_TRAIL_BW = 32;
+// FP32 fronts whose rank updates go to the tensor cores (k_tc_update,
+// 128 x 128 tiles from packed panels): a Schur complement of at least
+// TC_SCHUR_M rows, or more than one block with at least TC_TRAIL_ROWS rows
+// below the first.
+constexpr int TC_SCHUR_M = 96, TC_TRAIL_ROWS = 128;
 
 // Block partition and schedule for one precision (block width BlockMax<T>).
 struct Plan {
@@ -68,6 +69,8 @@ struct Plan {
     int bmax = 0, bwmax = 1;
     std::vector<int> blk_c0, blk_c1, blk_p0, blk_np;
     std::vector<ll> blk_inv2;
+    std::vector<ll> blk_lpack, blk_upack;  // byte offsets of the packed panels (-1: front not packed)
+    ll pack_size = 0;
     std::vector<int> blk_front;
     std::vector<int> inv_ids;             // k_block_inv entries grouped by line width (32, 64, 128)
     int inv_off[4] = {0, 0, 0, 0};        // class c: inv_ids[inv_off[c] .. inv_off[c+1])
@@ -78,6 +81,7 @@ struct Plan {
     spk::DFront* d_fronts = nullptr;
     int *d_blk_c0 = nullptr, *d_blk_c1 = nullptr, *d_blk_p0 = nullptr, *d_blk_np = nullptr;
     ll* d_blk_inv2 = nullptr;
+    ll *d_blk_lpack = nullptr, *d_blk_upack = nullptr;
     int* d_blk_front = nullptr;
     int* d_inv_ids = nullptr;
     int *d_sched_ids = nullptr, *d_sched_prefix = nullptr;
@@ -95,6 +99,7 @@ template <typename T>
 struct Storage {
     T* d = nullptr;
     T* inv2 = nullptr;      // whole-block forward / backward operators
+    unsigned char* pack = nullptr;   // packed panels of the tensor-core fronts (FP32)
     bool loaded = false;    // values assembled since the last factor
     bool factored = false;
 };
@@ -149,6 +154,7 @@ struct spk_handle {
 
     cudaStream_t own = nullptr, stream = nullptr;
     int device = -1;
+    int nsm = 1;                 // SMs of the device (grid of the persistent kernels)
     std::string err;
 
     // launch accounting and optional per-class event timing
@@ -529,6 +535,25 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
         }
         P.nblocks[i] = (int)P.blk_c0.size() - P.block0[i];
     }
+    P.blk_lpack.assign(P.blk_c0.size(), -1);
+    P.blk_upack.assign(P.blk_c0.size(), -1);
+    if (tc) {
+        const ll chunk = spk::umma::PCHUNK;
+        for (int i = 0; i < nfr; ++i) {
+            const HFront& F = h->fronts[i];
+            const int b0 = P.block0[i], nb = P.nblocks[i];
+            const bool packed = F.m >= TC_SCHUR_M || (nb > 1 && F.nf + F.m - P.blk_c1[b0] >= TC_TRAIL_ROWS);
+            if (!packed) continue;
+            const int n2 = cdiv(F.m, spk::umma::TM);
+            for (int b = b0; b < b0 + nb; ++b) {
+                const int n1 = cdiv(F.nf - P.blk_c1[b], spk::umma::TM);
+                const ll bytes = (ll)(n1 + n2) * cdiv(P.blk_c1[b] - P.blk_c0[b], spk::umma::KCH) * chunk;
+                P.blk_lpack[b] = P.pack_size;
+                P.blk_upack[b] = P.pack_size + bytes;
+                P.pack_size += 2 * bytes;
+            }
+        }
+    }
     {
         // k_block_inv work: blocks up to 32 wide, one entry per block; wider
         // ones by line width 64 / 128, entries blk * 4 + kind * 2 + tile
@@ -584,9 +609,9 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
                 wp[k] = 2.0 * bw * (rowsL + colsU) + 2.0 * bw * bw;
                 tt[k] = cdiv(ld - c1, spk::TT) * cdiv(F.nf - c1, spk::TT) + cdiv(F.nf - c1, spk::TT) * cdiv(F.m, spk::TT);
                 ttc[k] = 0;
-                if (tc && ld - c1 >= TC_TRAIL_ROWS && c1 - c0 >= TC_TRAIL_BW) {
-                    const int T2 = spk::umma::TM;
-                    ttc[k] = cdiv(ld - c1, T2) * cdiv(F.nf - c1, T2) + cdiv(F.nf - c1, T2) * cdiv(F.m, T2);
+                if (P.blk_lpack[blk] >= 0) {   // packed front: 128-tiles, row / column regions split at nf
+                    const int n1 = cdiv(F.nf - c1, spk::umma::TM), n2 = cdiv(F.m, spk::umma::TM);
+                    ttc[k] = (n1 + n2) * n1 + n1 * n2;
                     tt[k] = 0;
                 }
                 const double area = (double)(ld - c1) * (F.nf - c1) + (double)(F.nf - c1) * F.m;
@@ -622,7 +647,7 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
             const HFront& F = h->fronts[ids[k]];
             tsch[k] = F.m > 0 ? cdiv(F.m, spk::TT) * cdiv(F.m, spk::TT) : 0;
             tsch_tc[k] = 0;
-            if (tc && F.m >= TC_SCHUR_M) {
+            if (F.m > 0 && P.blk_lpack[P.block0[ids[k]]] >= 0) {
                 tsch_tc[k] = cdiv(F.m, spk::umma::TM) * cdiv(F.m, spk::umma::TN);
                 tsch[k] = 0;
             }
@@ -692,6 +717,8 @@ static int ensure_plan(spk_handle* h) {
     if ((rc = upload(h, &P.d_blk_p0, P.blk_p0))) return rc;
     if ((rc = upload(h, &P.d_blk_np, P.blk_np))) return rc;
     if ((rc = upload(h, &P.d_blk_inv2, P.blk_inv2))) return rc;
+    if ((rc = upload(h, &P.d_blk_lpack, P.blk_lpack))) return rc;
+    if ((rc = upload(h, &P.d_blk_upack, P.blk_upack))) return rc;
     if ((rc = upload(h, &P.d_blk_front, P.blk_front))) return rc;
     if ((rc = upload(h, &P.d_inv_ids, P.inv_ids))) return rc;
     if ((rc = upload(h, &P.d_sched_ids, P.sched_ids))) return rc;
@@ -710,22 +737,25 @@ static int ensure_plan(spk_handle* h) {
     S.blk_p0 = P.d_blk_p0;
     S.blk_np = P.d_blk_np;
     S.blk_inv2 = P.d_blk_inv2;
+    S.blk_lpack = P.d_blk_lpack;
+    S.blk_upack = P.d_blk_upack;
     constexpr int BM = spk::BlockMax<T>::value;
     CU(h, cudaFuncSetAttribute(spk::k_block_panel<T, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)sweep_smem<T, BM>(1)));
     CU(h, cudaFuncSetAttribute(spk::k_block_inv<T, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)sweep_smem<T, BM>(1)));
     if (std::is_same<T, float>::value) {
-        CU(h, cudaFuncSetAttribute(spk::k_schur_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, spk::umma::SMEM));
-        CU(h, cudaFuncSetAttribute(spk::k_block_trail_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   spk::umma::SMEM));
+        CU(h, cudaFuncSetAttribute(spk::k_tc_update<spk::TC_TRAIL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   spk::umma::PSMEM));
+        CU(h, cudaFuncSetAttribute(spk::k_tc_update<spk::TC_SCHUR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   spk::umma::PSMEM));
     }
     P.built = true;
     return SPK_OK;
 }
 
 static void free_plan(Plan& P) {
-    void* ptrs[] = {P.d_fronts, P.d_blk_c0, P.d_blk_c1, P.d_blk_p0, P.d_blk_np, P.d_blk_inv2,
+    void* ptrs[] = {P.d_fronts, P.d_blk_c0, P.d_blk_c1, P.d_blk_p0, P.d_blk_np, P.d_blk_inv2, P.d_blk_lpack, P.d_blk_upack,
                     P.d_blk_front, P.d_inv_ids, P.d_sched_ids, P.d_sched_prefix};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -746,6 +776,8 @@ static int ensure_storage(spk_handle* h) {
     Storage<T>& S = storage<T>(h);
     if (!S.d) CU(h, cudaMalloc((void**)&S.d, sizeof(T) * std::max<i64>(h->fsize, 1)));
     if (!S.inv2) CU(h, cudaMalloc((void**)&S.inv2, sizeof(T) * std::max<ll>(h->plan[prec_index<T>()].inv2_size, 1)));
+    if (!S.pack && h->plan[prec_index<T>()].pack_size > 0)
+        CU(h, cudaMalloc((void**)&S.pack, (size_t)h->plan[prec_index<T>()].pack_size));
     return SPK_OK;
 }
 
@@ -797,13 +829,13 @@ static int factor_launches(spk_handle* h) {
                 const spk::Launch la = launch_of(PL, P.bpanel[t]);
                 if (bw <= 32)
                     spk::k_block_panel<T, 32><<<P.bpanel[t].tiles, 256, sweep_smem<T, 32>(1), h->stream>>>(
-                        fac, h->d_ipiv, S, la, (int)t);
+                        fac, h->d_ipiv, S, la, (int)t, storage<T>(h).pack);
                 else if (bw <= 64)
                     spk::k_block_panel<T, 64><<<P.bpanel[t].tiles, 256, sweep_smem<T, 64>(1), h->stream>>>(
-                        fac, h->d_ipiv, S, la, (int)t);
+                        fac, h->d_ipiv, S, la, (int)t, storage<T>(h).pack);
                 else
                     spk::k_block_panel<T, BM><<<P.bpanel[t].tiles, 256, sweep_smem<T, BM>(1), h->stream>>>(
-                        fac, h->d_ipiv, S, la, (int)t);
+                        fac, h->d_ipiv, S, la, (int)t, storage<T>(h).pack);
             }
             if (P.btrail[t].tiles > 0) {
                 LaunchScope ls(h, SPK_K_TRAIL, P.btrail[t].flops, P.btrail[t].words * sizeof(T));
@@ -813,8 +845,9 @@ static int factor_launches(spk_handle* h) {
             if constexpr (std::is_same<T, float>::value) {
                 if (P.btrail_tc[t].tiles > 0) {
                     LaunchScope ls(h, SPK_K_TRAIL, P.btrail_tc[t].flops, P.btrail_tc[t].words * sizeof(T));
-                    spk::k_block_trail_tc<<<P.btrail_tc[t].tiles, 256, spk::umma::SMEM, h->stream>>>(
-                        fac, S, launch_of(PL, P.btrail_tc[t]), (int)t, h->d_info + 1);
+                    const int nt = P.btrail_tc[t].tiles;
+                    spk::k_tc_update<spk::TC_TRAIL><<<std::min(nt, h->nsm), spk::TC_THREADS, spk::umma::PSMEM, h->stream>>>(
+                        fac, storage<T>(h).pack, S, launch_of(PL, P.btrail_tc[t]), (int)t, nt, h->d_info + 1);
                 }
             }
         }
@@ -825,8 +858,9 @@ static int factor_launches(spk_handle* h) {
         if constexpr (std::is_same<T, float>::value) {
             if (P.schur_tc.tiles > 0) {
                 LaunchScope ls(h, SPK_K_SCHUR, P.schur_tc.flops, P.schur_tc.words * sizeof(T));
-                spk::k_schur_tc<<<P.schur_tc.tiles, 256, spk::umma::SMEM, h->stream>>>(fac, S, launch_of(PL, P.schur_tc),
-                                                                                      h->d_info + 1);
+                const int nt = P.schur_tc.tiles;
+                spk::k_tc_update<spk::TC_SCHUR><<<std::min(nt, h->nsm), spk::TC_THREADS, spk::umma::PSMEM, h->stream>>>(
+                    fac, storage<T>(h).pack, S, launch_of(PL, P.schur_tc), 0, nt, h->d_info + 1);
             }
         }
     }
@@ -1032,6 +1066,8 @@ int spk_create(int64_t n, int64_t nsuper, const int64_t* xsuper, const int64_t* 
         if (e != cudaSuccess) rc = set_err(h, SPK_ECUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
         else {
             h->device = dev;
+            if (cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || h->nsm < 1)
+                h->nsm = 1;
             e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking);
             if (e != cudaSuccess) rc = set_err(h, SPK_ECUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
             h->stream = h->own;
@@ -1446,7 +1482,7 @@ void spk_destroy(spk_handle* h) {
     free_plan(h->plan[0]);
     free_plan(h->plan[1]);
     void* ptrs[] = {h->d_xs, h->d_rows, h->d_runid, h->d_run_tgt, h->d_run_start, h->d_run_rel,
-                    h->d_rel, h->s64.inv2, h->s32.inv2, h->d_ipiv, h->d_info, h->d_slot, h->d_aval,
+                    h->d_rel, h->s64.inv2, h->s32.inv2, h->s64.pack, h->s32.pack, h->d_ipiv, h->d_info, h->d_slot, h->d_aval,
                     h->d_rowptr, h->d_col, h->d_src, h->d_rperm, h->d_rinvp, h->s64.d, h->s32.d, h->d_wb,
                     h->d_wy, h->d_wx, h->d_rhs, h->d_x, h->d_r, h->d_sums};
     for (void* p : ptrs)

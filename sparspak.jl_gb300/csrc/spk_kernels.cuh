@@ -29,6 +29,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "spk_umma.cuh"
 
 namespace spk {
@@ -69,6 +71,8 @@ struct Sched {
     const int* blk_p0;     // first supernode (0-based) of each block
     const int* blk_np;     // supernodes in the block
     const ll* blk_inv2;    // offset in inv2[] of the block's Minv (then Uinv), bw x bw each
+    const ll* blk_lpack;   // byte offset of the block's packed L panel (FP32 tensor-core fronts), -1 if none
+    const ll* blk_upack;   // byte offset of the block's packed U panel, -1 if none
 };
 
 // One launch = a list of fronts and the prefix sum of their tile counts.
@@ -586,15 +590,42 @@ __device__ __forceinline__ void stage_lower(T* sL, const T* blkp, ll ld, int bw,
     }
 }
 
+// Packed copy of one panel line for the tensor-core updates (FP32 fronts
+// with a pack): the line's entries k < nch * KCH, held CQ per lane from
+// q * CQ, split into TF32 hi / lo at tile `t`, line `i` of the block's pack.
+template <int CQ>
+__device__ __forceinline__ void pack_line(unsigned char* base, int t, int i, int q, int nch, const float (&v)[CQ]) {
+#pragma unroll
+    for (int g = 0; g < CQ / 4; ++g) {
+        const int k = q * CQ + 4 * g;
+        if (k < nch * umma::KCH) {
+            unsigned char* dst = base + ((ll)t * nch + k / umma::KCH) * umma::PCHUNK + umma::packed_offset(i, k % umma::KCH);
+            uint32_t h[4], l[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                h[e] = umma::tf32_rna(v[4 * g + e]);
+                l[e] = umma::tf32_rna(v[4 * g + e] - __uint_as_float(h[e]));
+            }
+            *reinterpret_cast<uint4*>(dst) = make_uint4(h[0], h[1], h[2], h[3]);
+            *reinterpret_cast<uint4*>(dst + umma::OPB) = make_uint4(l[0], l[1], l[2], l[3]);
+        }
+    }
+}
+
 // Panels of block `step` (block width bw <= W): 64-row tiles of the L panel
 // below the block, X := X inv(U_B) (the reference's trsm 'r','u','n','n' of
 // every piece, with the earlier pieces' updates X_p -= X_<p U_<p,p), and
 // 64-column tiles of the U panel to its right, inside the front (Lf) and in
 // U12 (Uf): Y := inv(L_B) P_B Y (_luswap! and trsm 'r','l','t','u' of every
-// piece, with Y_p -= L_p,<p Y_<p).  One line per 4 lanes.
+// piece, with Y_p -= L_p,<p Y_<p).  One line per 4 lanes.  For FP32 fronts
+// with a pack (blk_lpack >= 0) the lines are also written, split into TF32
+// hi / lo, to the packed tiles that the tensor-core updates read: rows of the
+// L panel tiled from c1 ([c1, nf)) and from nf ([nf, ld)), columns of the U
+// panel from c1 ([c1, nf)) and from 0 (U12).
 // Dynamic shared memory: W * SLD(W) T's.
 template <typename T, int W>
-__global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, Sched S, Launch L, int step) {
+__global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, Sched S, Launch L, int step,
+                                                      unsigned char* pack) {
     constexpr int CQ = W / 4;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sT = reinterpret_cast<T*>(smem_raw);
@@ -627,6 +658,15 @@ __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, Sc
             const int j = q * CQ + jj;
             if (ok && j < bw) xp[(ll)j * F.ld] = x[jj];
         }
+        if constexpr (std::is_same<T, float>::value) {
+            const ll off = S.blk_lpack[blk];
+            if (off >= 0 && ok) {
+                const int n1 = cdiv(F.nf - c1, umma::TM);
+                const int t = r < F.nf ? (r - c1) / umma::TM : n1 + (r - F.nf) / umma::TM;
+                const int i = r < F.nf ? (r - c1) % umma::TM : (r - F.nf) % umma::TM;
+                pack_line<CQ>(pack + off, t, i, q, cdiv(bw, umma::KCH), x);
+            }
+        }
     } else {
         for (int k = tid; k <= np; k += 256) q0[k] = S.xsuper[p0 + k] - F.f - c0;
         __syncthreads();
@@ -651,6 +691,15 @@ __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, Sc
         for (int ii = 0; ii < CQ; ++ii) {
             const int R = q * CQ + ii;
             if (ok && R < bw) cp[(ll)R * stride] = y[ii];
+        }
+        if constexpr (std::is_same<T, float>::value) {
+            const ll off = S.blk_upack[blk];
+            if (off >= 0 && ok) {
+                const int n1 = cdiv(F.nf - c1, umma::TM);
+                const int t = inner ? (col - c1) / umma::TM : n1 + col / umma::TM;
+                const int i = inner ? (col - c1) % umma::TM : col % umma::TM;
+                pack_line<CQ>(pack + off, t, i, q, cdiv(bw, umma::KCH), y);
+            }
         }
     }
 }
@@ -832,60 +881,6 @@ __global__ void __launch_bounds__(256) k_block_trail(T* fac, Sched S, Launch L, 
     }
 }
 
-// Trailing update after block `step` on the tensor cores (FP32 storage,
-// 3xTF32 products), 128 x 128 tiles: the same regions as k_block_trail.
-__global__ void __launch_bounds__(256, 2) k_block_trail_tc(float* fac, Sched S, Launch L, int step, int* err) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const umma::Ctx cx = umma::ctx_of(smem_raw);
-    const uint32_t tmem = umma::begin(cx);
-    unsigned uses = 0;
-    int fid, tile;
-    locate(L, blockIdx.x, fid, tile);
-    const DFront F = S.fronts[fid];
-    const int blk = F.block0 + step;
-    const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk];
-    const int nrL = cdiv(F.ld - c1, umma::TM), ncL = cdiv(F.nf - c1, umma::TN);
-    const bool isL = tile < nrL * ncL;
-    int r0, col0, nr, nc;
-    if (isL) {
-        r0 = c1 + (tile % nrL) * umma::TM;
-        col0 = c1 + (tile / nrL) * umma::TN;
-        nr = min(umma::TM, F.ld - r0);
-        nc = min(umma::TN, F.nf - col0);
-    } else {
-        const int t2 = tile - nrL * ncL, nrU = cdiv(F.nf - c1, umma::TM);
-        r0 = c1 + (t2 % nrU) * umma::TM;
-        col0 = (t2 / nrU) * umma::TN;   // U12 column index
-        nr = min(umma::TM, F.nf - r0);
-        nc = min(umma::TN, F.m - col0);
-    }
-    const umma::Operand A{fac + F.loff + (ll)c0 * F.ld + r0, F.ld, nr, false};
-    const umma::Operand B = isL ? umma::Operand{fac + F.loff + (ll)col0 * F.ld + c0, F.ld, nc, true}
-                                : umma::Operand{fac + F.uoff + (ll)c0 * F.m + col0, F.m, nc, false};
-    umma::tile_product(cx, tmem, A, B, c1 - c0, uses, err);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int r = 32 * (warp & 3) + lane;
-#pragma unroll 1
-    for (int h = 0; h < 2; ++h) {
-        const int col = (warp >> 2) * 64 + h * 32;
-        float v[32];
-        umma::tmem_ld32(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + col, v);
-        if (r < nr) {
-            if (isL) {
-#pragma unroll
-                for (int j = 0; j < 32; ++j)
-                    if (col + j < nc) fac[F.loff + (ll)(col0 + col + j) * F.ld + r0 + r] -= v[j];
-            } else {
-                float* dst = fac + F.uoff + (ll)(r0 + r) * F.m + col0 + col;
-#pragma unroll
-                for (int j = 0; j < 32; ++j)
-                    if (col + j < nc) dst[j] -= v[j];
-            }
-        }
-    }
-    umma::end(cx, tmem);
-}
-
 // Subtract C(r, c) of a front's Schur complement from its ancestor: the
 // entry belongs to the front of R_F[min(r, c)], whose run gives the positions.
 template <typename T>
@@ -948,79 +943,262 @@ __global__ void __launch_bounds__(256) k_schur(T* fac, Sched S, Launch L) {
     }
 }
 
-// Schur complement on the tensor cores (FP32 storage, 3xTF32 products):
-// 128 x 128 tiles of C = L21 * U12 per CTA, scattered like k_schur.  The
-// scatter uses per-tile tables: for each tile column c the target front of
-// R_F[c] and c's position there (entries r >= c), for each tile row r the
-// same for R_F[r] (entries r < c); an entry then needs one rel[] load.
+// ---------------------------------------------------------------------------
+// Rank updates of the FP32 fronts on the tensor cores (3xTF32), from the
+// panels packed by k_block_panel.  Tiles are 128 x 128; the rows of a
+// front are tiled in two regions, [c1, nf) from c1 (n1 tiles) and [nf, ld)
+// from nf (n2 tiles), the columns likewise ([c1, nf) of the front, then the
+// U12 columns), so that the packed tiles of every block line up with the
+// Schur complement's.
+//   TRAIL (block `step`): A = L panel row tile rt, B = U panel column tile
+//     ct, K = the block's columns; tiles (rt < n1 + n2, ct < n1) update Lf,
+//     tiles (rt < n1, n1 <= ct) update U12 in Uf.
+//   SCHUR: A = L21 row tile, B = U12 column tile, K = all blocks' columns;
+//     the product is scattered into the ancestors like k_schur.
+// Persistent: CTA b takes tiles b, b + gridDim.x, ...  Warp 0 lane 0 issues
+// the bulk copies, warp 1 lane 0 the MMAs, and the TC_EPI epilogue warps
+// (from warp 4; warp w reads TMEM lanes 32 (w % 4).. and the 32 accumulator
+// columns 32 ((w - 4) / 4)..) drain the accumulator.
+// ---------------------------------------------------------------------------
 struct ScatterRow {
     ll rel0;     // offset in rel[] of R_F[0] for the run of this row / column
     ll loff, uoff;
     int ld, nf, m, pos;
 };
 
-__global__ void __launch_bounds__(256, 2) k_schur_tc(float* fac, Sched S, Launch L, int* err) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ ScatterRow tab[2][umma::TM];   // [0] tile columns, [1] tile rows
-    const umma::Ctx cx = umma::ctx_of(smem_raw);
-    const uint32_t tmem = umma::begin(cx);
-    unsigned uses = 0;
-    int fid, tile;
-    locate(L, blockIdx.x, fid, tile);
-    const DFront F = S.fronts[fid];
-    const int nt = cdiv(F.m, umma::TM);
-    const int r0 = (tile % nt) * umma::TM, c0 = (tile / nt) * umma::TN;
-    const int* runid = S.runid + F.runid_off;
-    {
-        const int side = threadIdx.x >> 7, t = threadIdx.x & 127;
-        const int x = (side == 0 ? c0 : r0) + t;
-        ScatterRow e{};
-        e.pos = -1;
-        if (x < F.m) {
-            const int g = runid[x];
-            const DFront G = S.fronts[S.run_tgt[g]];
-            e.rel0 = S.run_rel[g] - S.run_start[g];
-            e.loff = G.loff;
-            e.uoff = G.uoff;
-            e.ld = G.ld;
-            e.nf = G.nf;
-            e.m = G.m;
-            e.pos = S.rel[e.rel0 + x];
+constexpr int TC_TRAIL = 0, TC_SCHUR = 1;
+constexpr int TC_EPI = 16, TC_THREADS = 32 * (4 + TC_EPI);
+
+struct TcTile {
+    DFront F;
+    int rt, ct, n1, n2, nchunks;
+};
+
+template <int MODE>
+__device__ __forceinline__ TcTile tc_decode(const Sched& S, const Launch& L, int step, int tile) {
+    TcTile T;
+    int fid, t;
+    locate(L, tile, fid, t);
+    T.F = S.fronts[fid];
+    const int n2 = cdiv(T.F.m, umma::TM);
+    T.n2 = n2;
+    if (MODE == TC_TRAIL) {
+        const int blk = T.F.block0 + step;
+        const int c1 = S.blk_c1[blk], bw = c1 - S.blk_c0[blk];
+        const int n1 = cdiv(T.F.nf - c1, umma::TM);
+        T.n1 = n1;
+        if (t < (n1 + n2) * n1) {
+            T.rt = t % (n1 + n2);
+            T.ct = t / (n1 + n2);
+        } else {
+            const int t2 = t - (n1 + n2) * n1;
+            T.rt = t2 % n1;
+            T.ct = n1 + t2 / n1;
         }
-        tab[side][t] = e;
+        T.nchunks = cdiv(bw, umma::KCH);
+    } else {
+        T.n1 = 0;
+        T.rt = t % n2;
+        T.ct = t / n2;
+        int nc = 0;
+        for (int b = 0; b < T.F.nblocks; ++b) {
+            const int blk = T.F.block0 + b;
+            nc += cdiv(S.blk_c1[blk] - S.blk_c0[blk], umma::KCH);
+        }
+        T.nchunks = nc;
     }
-    __syncthreads();
-    const umma::Operand A{fac + F.loff + F.nf + r0, F.ld, min(umma::TM, F.m - r0), false};
-    const umma::Operand B{fac + F.uoff + c0, F.m, min(umma::TN, F.m - c0), false};
-    umma::tile_product(cx, tmem, A, B, F.nf, uses, err);
+    return T;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const unsigned char* pack, Sched S, Launch L,
+                                                              int step, int ntiles, int* err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ ScatterRow tab[2][umma::TM];   // SCHUR: [0] tile columns, [1] tile rows
+    __shared__ int dead;
+    const umma::PCtx cx = umma::pctx_of(smem_raw);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ir = 32 * (warp & 3) + lane, r = r0 + ir;
-    const ScatterRow& R = tab[1][ir];
-#pragma unroll 1
-    for (int h = 0; h < 2; ++h) {
-        const int col = (warp >> 2) * 64 + h * 32;
-        float v[32];
-        umma::tmem_ld32(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + col, v);
-        if (r < F.m) {
-#pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                const int c = c0 + col + j;
-                if (c >= F.m) continue;
-                if (r >= c) {   // L entry of the front of R_F[c]
-                    const ScatterRow& Cc = tab[0][col + j];
-                    const int pr = S.rel[Cc.rel0 + r];
-                    if (pr >= 0 && Cc.pos >= 0) atomicAdd(&fac[Cc.loff + (ll)Cc.pos * Cc.ld + pr], -v[j]);
-                } else {        // entry of the front of R_F[r]
-                    const int pc = S.rel[R.rel0 + c];
-                    if (pc >= 0 && R.pos >= 0) {
-                        const ll addr = pc < R.nf ? R.loff + (ll)pc * R.ld + R.pos : R.uoff + (ll)R.pos * R.m + (pc - R.nf);
-                        atomicAdd(&fac[addr], -v[j]);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < umma::PST; ++s) {
+            umma::mbar_init(&cx.full[s], 1);
+            umma::mbar_init(&cx.empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            umma::mbar_init(&cx.tfull[b], 1);
+            umma::mbar_init(&cx.tempty[b], 32 * TC_EPI);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        dead = 0;
+    }
+    if (warp == 1) umma::tmem_alloc(cx.tmem_slot, 2 * umma::TN);
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    const uint32_t tmem = *cx.tmem_slot;
+    volatile int* vdead = &dead;
+
+    if (warp == 0) {
+        if (lane == 0) {   // bulk copies
+            int s = 0;
+            uint32_t ph = 0;
+            for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+                const TcTile T = tc_decode<MODE>(S, L, step, tile);
+                int b = MODE == TC_TRAIL ? T.F.block0 + step : T.F.block0;
+                int c = 0, nb = MODE == TC_TRAIL ? 0 : cdiv(S.blk_c1[b] - S.blk_c0[b], umma::KCH);
+                int n1b = MODE == TC_TRAIL ? T.n1 : cdiv(T.F.nf - S.blk_c1[b], umma::TM);
+                for (int q = 0; q < T.nchunks; ++q) {
+                    if (MODE == TC_SCHUR) {
+                        while (c == nb) {   // next block of the front
+                            ++b;
+                            c = 0;
+                            nb = cdiv(S.blk_c1[b] - S.blk_c0[b], umma::KCH);
+                            n1b = cdiv(T.F.nf - S.blk_c1[b], umma::TM);
+                        }
                     }
+                    const int nch = MODE == TC_TRAIL ? T.nchunks : nb;
+                    const int ra = MODE == TC_TRAIL ? T.rt : n1b + T.rt;
+                    const int rb = MODE == TC_TRAIL ? T.ct : n1b + T.ct;
+                    const unsigned char* pa = pack + S.blk_lpack[b] + ((ll)ra * nch + c) * umma::PCHUNK;
+                    const unsigned char* pb = pack + S.blk_upack[b] + ((ll)rb * nch + c) * umma::PCHUNK;
+                    umma::wait_bounded(&cx.empty[s], ph ^ 1, vdead, err);
+                    umma::arrive_expect_tx(&cx.full[s], 2 * umma::PCHUNK);
+                    const uint32_t dst = umma::saddr(cx.stage + s * umma::STAGE);
+                    umma::bulk_g2s(dst, pa, umma::PCHUNK, &cx.full[s]);
+                    umma::bulk_g2s(dst + umma::PCHUNK, pb, umma::PCHUNK, &cx.full[s]);
+                    ++c;
+                    if (++s == umma::PST) { s = 0; ph ^= 1; }
                 }
             }
         }
+    } else if (warp == 1) {
+        if (lane == 0) {   // MMAs
+            constexpr uint32_t IDESC = umma::idesc_tf32(umma::TM, umma::TN);
+            int s = 0;
+            uint32_t ph = 0;
+            int acc = 0;
+            uint32_t aph = 0;
+            for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+                const TcTile T = tc_decode<MODE>(S, L, step, tile);
+                umma::wait_bounded(&cx.tempty[acc], aph ^ 1, vdead, err);
+                umma::fence_after();
+                const uint32_t d = tmem + acc * umma::TN;
+                for (int q = 0; q < T.nchunks; ++q) {
+                    umma::wait_bounded(&cx.full[s], ph, vdead, err);
+                    umma::fence_after();
+                    const uint32_t a_hi = umma::saddr(cx.stage + s * umma::STAGE), a_lo = a_hi + umma::OPB;
+                    const uint32_t b_hi = a_hi + 2 * umma::OPB, b_lo = a_hi + 3 * umma::OPB;
+#pragma unroll
+                    for (int kk = 0; kk < umma::KCH / 8; ++kk) {
+                        const uint32_t o = kk * 256;
+                        const uint64_t dah = umma::desc_kmajor(a_hi + o, 128, umma::SBO);
+                        const uint64_t dal = umma::desc_kmajor(a_lo + o, 128, umma::SBO);
+                        const uint64_t dbh = umma::desc_kmajor(b_hi + o, 128, umma::SBO);
+                        const uint64_t dbl = umma::desc_kmajor(b_lo + o, 128, umma::SBO);
+                        umma::mma_tf32(d, dah, dbh, IDESC, (q > 0 || kk > 0) ? 1u : 0u);
+                        umma::mma_tf32(d, dah, dbl, IDESC, 1u);
+                        umma::mma_tf32(d, dal, dbh, IDESC, 1u);
+                    }
+                    umma::commit(&cx.empty[s]);
+                    if (++s == umma::PST) { s = 0; ph ^= 1; }
+                }
+                umma::commit(&cx.tfull[acc]);
+                if (++acc == 2) { acc = 0; aph ^= 1; }
+            }
+        }
+    } else if (warp >= 4) {   // epilogue: thread = one TMEM lane (tile row), 32 columns
+        const int q4 = warp & 3, i = 32 * q4 + lane, cg = (warp - 4) >> 2, et = threadIdx.x - 128;
+        int acc = 0;
+        uint32_t aph = 0;
+        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+            const TcTile T = tc_decode<MODE>(S, L, step, tile);
+            const DFront& F = T.F;
+            if (MODE == TC_SCHUR) {
+                asm volatile("bar.sync 1, %0;" ::"n"(32 * TC_EPI) : "memory");   // previous tile's scatter done
+                const int* runid = S.runid + F.runid_off;
+                if (et < 2 * umma::TM) {
+                    const int side = et / umma::TM, x = (side == 0 ? T.ct : T.rt) * umma::TM + (et % umma::TM);
+                    ScatterRow e{};
+                    e.pos = -1;
+                    if (x < F.m) {
+                        const int g = runid[x];
+                        const DFront G = S.fronts[S.run_tgt[g]];
+                        e.rel0 = S.run_rel[g] - S.run_start[g];
+                        e.loff = G.loff;
+                        e.uoff = G.uoff;
+                        e.ld = G.ld;
+                        e.nf = G.nf;
+                        e.m = G.m;
+                        e.pos = S.rel[e.rel0 + x];
+                    }
+                    tab[side][et % umma::TM] = e;
+                }
+                asm volatile("bar.sync 1, %0;" ::"n"(32 * TC_EPI) : "memory");
+            }
+            umma::wait_bounded(&cx.tfull[acc], aph, vdead, err);
+            umma::fence_after();
+            const uint32_t taddr = tmem + acc * umma::TN + ((uint32_t)(32 * q4) << 16);
+            if (MODE == TC_TRAIL) {
+                const int c1 = S.blk_c1[F.block0 + step];
+                const bool rL = T.rt < T.n1;   // row region [c1, nf) else [nf, ld)
+                const int row = rL ? c1 + T.rt * umma::TM + i : F.nf + (T.rt - T.n1) * umma::TM + i;
+                const bool rok = rL ? row < F.nf : row < F.ld;
+                const bool cL = T.ct < T.n1;   // column region: front columns [c1, nf) else U12
+                const int col0 = cL ? c1 + T.ct * umma::TN : (T.ct - T.n1) * umma::TN;
+                const int ncol = cL ? F.nf - col0 : F.m - col0;
+                {
+                    const int h = cg;
+                    float v[32];
+                    umma::tmem_ld32(taddr + h * 32, v);
+                    if (rok) {
+                        if (cL) {
+#pragma unroll
+                            for (int j = 0; j < 32; ++j)
+                                if (h * 32 + j < ncol) fac[F.loff + (ll)(col0 + h * 32 + j) * F.ld + row] -= v[j];
+                        } else {
+                            float* dst = fac + F.uoff + (ll)row * F.m + col0 + h * 32;
+#pragma unroll
+                            for (int j = 0; j < 32; ++j)
+                                if (h * 32 + j < ncol) dst[j] -= v[j];
+                        }
+                    }
+                }
+            } else {
+                const int r = T.rt * umma::TM + i, c0 = T.ct * umma::TN;
+                const ScatterRow& R = tab[1][i];
+                {
+                    const int h = cg;
+                    float v[32];
+                    umma::tmem_ld32(taddr + h * 32, v);
+                    if (r < F.m) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            const int c = c0 + h * 32 + j;
+                            if (c >= F.m) continue;
+                            if (r >= c) {   // L entry of the front of R_F[c]
+                                const ScatterRow& Cc = tab[0][h * 32 + j];
+                                const int pr = S.rel[Cc.rel0 + r];
+                                if (pr >= 0 && Cc.pos >= 0) atomicAdd(&fac[Cc.loff + (ll)Cc.pos * Cc.ld + pr], -v[j]);
+                            } else {        // entry of the front of R_F[r]
+                                const int pc = S.rel[R.rel0 + c];
+                                if (pc >= 0 && R.pos >= 0) {
+                                    const ll addr = pc < R.nf ? R.loff + (ll)pc * R.ld + R.pos
+                                                              : R.uoff + (ll)R.pos * R.m + (pc - R.nf);
+                                    atomicAdd(&fac[addr], -v[j]);
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+            umma::fence_before();
+            umma::arrive(&cx.tempty[acc]);
+            if (++acc == 2) { acc = 0; aph ^= 1; }
+        }
     }
-    umma::end(cx, tmem);
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    if (warp == 1) umma::tmem_dealloc(tmem, 2 * umma::TN);
 }
 
 // ---------------------------------------------------------------------------

@@ -256,5 +256,67 @@ __device__ __forceinline__ bool tile_product(const Ctx& c, uint32_t tmem, const 
     return ok;
 }
 
+// ---------------------------------------------------------------------------
+// Packed operands.  The panel kernel writes the L and U panels of a block a
+// second time as TF32 hi / lo parts already in the canonical layout: for a
+// 128-line tile and a chunk of KCH block columns, 16 KB = [hi 8 KB][lo 8 KB]
+// (byte offset of element (line i, column kk) in a part: packed_offset).  A
+// tile product then streams whole chunks with bulk asynchronous copies
+// (cp.async.bulk, completion counted in bytes on an mbarrier) through a ring
+// of PST stages; one thread issues the copies, one thread the MMAs, and four
+// warps drain a double-buffered accumulator (2 x 128 TMEM columns), so the
+// epilogue of a tile overlaps the MMAs of the next.
+// ---------------------------------------------------------------------------
+constexpr int PCHUNK = 2 * OPB;                       // one packed operand chunk (hi + lo), 16 KB
+constexpr int PST = 5;                                // stages of the packed pipeline
+constexpr int PSMEM = PST * STAGE + 2048;             // + alignment slack, barriers, TMEM address
+
+__host__ __device__ constexpr uint32_t packed_offset(int i, int kk) {
+    return (uint32_t)((i >> 3) * SBO + (kk >> 2) * 128 + (i & 7) * 16 + (kk & 3) * 4);
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(saddr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(bar)) : "memory");
+}
+
+// Wait with a poll budget that collapses after the first timeout in the CTA
+// (*dead set), so that a broken pipeline still ends quickly; false on timeout.
+__device__ __forceinline__ bool wait_bounded(uint64_t* bar, uint32_t parity, volatile int* dead, int* err) {
+    const unsigned limit = *dead ? 1u : WAIT_LIMIT;
+    for (unsigned it = 0; it < limit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    *dead = 1;
+    if (err) atomicExch(err, 1);
+    return false;
+}
+
+// Barriers and TMEM of a packed-pipeline CTA (carved from dynamic shared memory).
+struct PCtx {
+    unsigned char* stage;   // PST * STAGE bytes, 1024-aligned
+    uint64_t *full, *empty, *tfull, *tempty;
+    uint32_t* tmem_slot;
+};
+
+__device__ __forceinline__ PCtx pctx_of(unsigned char* smem_raw) {
+    unsigned char* base =
+        reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    PCtx c;
+    c.stage = base;
+    c.full = reinterpret_cast<uint64_t*>(base + PST * STAGE);
+    c.empty = c.full + PST;
+    c.tfull = c.empty + PST;
+    c.tempty = c.tfull + 2;
+    c.tmem_slot = reinterpret_cast<uint32_t*>(c.tempty + 2);
+    return c;
+}
+
 }  // namespace umma
 }  // namespace spk
