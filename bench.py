@@ -330,19 +330,46 @@ def run_ours(args):
 
     pk, pk_kind = peaks()
 
+    def traffic_of(cls):
+        """DRAM bytes per launch of the class's FP32 kernels from the committed ncu summary (40^3 capture)."""
+        names = {"getrf": ("k_block_lu<float>", "k_block_lu_small<float>"), "panel": ("k_block_panel<float",),
+                 "trail": ("k_tc_update<0>", "k_block_trail<float>"), "schur": ("k_tc_update<1>", "k_schur<float>"),
+                 "fwd": ("k_fwd<float>",), "bwd": ("k_bwd<float>", "k_bwd_u12<float>")}.get(cls, ())
+        path = os.path.join(ROOT, "profiles", "dram_traffic_laplace3d40_mixed_step.md")
+        if not names or not os.path.exists(path):
+            return None, None
+        launches = nbytes = 0.0
+        for line in open(path):
+            cells = [c.strip() for c in line.strip().strip("|").split("|")]
+            if len(cells) == 7 and cells[0].startswith(names):
+                try:
+                    launches += float(cells[1])
+                    nbytes += (float(cells[4]) + float(cells[5])) * 1e6
+                except ValueError:
+                    pass
+        if launches == 0:
+            return None, None
+        return nbytes / launches, ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, mean over one "
+                                   "mixed step of the 40^3 case (profiles/dram_traffic_laplace3d40_mixed_step.md); "
+                                   "not captured at 64^3")
+
     def roofline_of(cls):
         d = live[cls]
         if cls in ("schur", "trail", "panel", "getrf"):
             achieved = d["flops"] / (d["ms"] * 1e-3) / 1e12
             roof = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops_sustained"], "unit": "TFLOP/s",
-                    "peak_kind": f"{pk_kind} bf16 dense sustained (kernel timed inside a long step); the kernel "
-                                 f"runs FP32 FMA on CUDA cores"}
+                    "peak_kind": f"{pk_kind} bf16 dense sustained (kernel timed inside a long step); achieved counts "
+                                 f"the algorithmic FP32 flops (a 3xTF32 product issues three TF32 MMAs per term, and "
+                                 f"the TF32 dense rate is half the bf16 one)",
+                    "compute": S._native.KERNEL_UNITS.get(cls, "")}
         else:
             achieved = d["bytes"] / (d["ms"] * 1e-3) / 1e9
             roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                     "peak_kind": f"{pk_kind} HBM copy bandwidth"}
-        roof.update({"frac": roof["achieved"] / roof["peak"], "traffic": None,
-                     "kernel": S._native.KERNEL_NAMES[cls] + "<float>", "launches": d["launches"],
+        traffic, tnote = traffic_of(cls)
+        roof.update({"frac": roof["achieved"] / roof["peak"], "traffic": traffic, "traffic_unit": "bytes/launch",
+                     "traffic_note": tnote,
+                     "kernel": S._native.KERNEL_NAMES[cls] + " (float)", "launches": d["launches"],
                      "ms_per_launch": d["ms"] / max(d["launches"], 1),
                      "algorithmic_per_launch": (d["flops"] if roof["bound"] == "tensor" else d["bytes"])
                      / max(d["launches"], 1)})
