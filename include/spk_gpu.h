@@ -114,6 +114,15 @@ int spk_factor(spk_handle* h, int precision, int64_t* first_singular);
 int spk_solve(spk_handle* h, double* b, int64_t nrhs, int64_t ldb, int where, int precision);
 
 /*
+ * Solve A^T X = B with the same factors, arguments as spk_solve.  Replaces
+ * the reference's transposed solve, which exists only as a commented-out
+ * `transposetriangularsolve` (src/SparseSpdMethod/SpkSparseSpdSolver.jl:384):
+ * U^T is applied in the forward order of the fronts and blocks, then L^T
+ * (with the in-block interchanges transposed) in the backward order.
+ */
+int spk_solve_transpose(spk_handle* h, double* b, int64_t nrhs, int64_t ldb, int where, int precision);
+
+/*
  * Iterative refinement: x := solve(b) with the factor of `precision`, then
  * repeat r = b - A x (FP64), x += solve(r) until max_j ||r_j||_2/||b_j||_2
  * <= tol or max_iter corrections were applied.  b and x are n x nrhs,
@@ -124,6 +133,23 @@ int spk_solve(spk_handle* h, double* b, int64_t nrhs, int64_t ldb, int where, in
  */
 int spk_refine(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where,
                int precision, double tol, int max_iter, int* iters, double* relres);
+
+/* Iterative refinement of A^T x = b (spk_solve_transpose and the FP64
+ * residual b - A^T x), arguments and results as spk_refine. */
+int spk_refine_transpose(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where,
+                         int precision, double tol, int max_iter, int* iters, double* relres);
+
+/*
+ * Gradient with respect to A's stored entries: dA[k] = -sum_r lambda_r[i_k]
+ * x_r[j_k] for the entries (i_k, j_k) of the pattern given to
+ * spk_set_pattern, in its CSC order.  For a loss of x = A^{-1} b, lambda is
+ * the adjoint A^{-T} dloss/dx (spk_solve_transpose / spk_refine_transpose).
+ * lambda and x are n x nrhs, column-major, leading dimension ld, original
+ * order.  The reference's only derivative path is forward-mode Dual numbers
+ * through its generic Julia code (test/test_generic.jl:58-98).
+ */
+int spk_grad_pattern(spk_handle* h, const double* lambda, const double* x, int64_t nrhs, int64_t ld, int where,
+                     double* dA);
 
 /*
  * Relative residual max_j ||b_j - A x_j||_2 / ||b_j||_2 in FP64 for the

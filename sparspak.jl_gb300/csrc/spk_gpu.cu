@@ -141,6 +141,7 @@ struct spk_handle {
     double* d_aval = nullptr;
     int *d_rowptr = nullptr, *d_col = nullptr;
     ll* d_src = nullptr;
+    int *d_ccolptr = nullptr, *d_crow = nullptr, *d_ccol = nullptr;   // A's pattern in CSC order (0-based)
     int *d_rperm = nullptr, *d_rinvp = nullptr;
 
     Storage<double> s64;
@@ -170,6 +171,7 @@ struct spk_handle {
     bool use_graphs = true;
     GraphRec g_factor[2];
     GraphRec g_solve[2][spk::MAXRHS + 1];
+    GraphRec g_tsolve[2][spk::MAXRHS + 1];   // transposed solves
 };
 
 // ---------------------------------------------------------------------------
@@ -265,7 +267,10 @@ static void drop_graph(GraphRec& g) {
 
 static void drop_solve_graphs(spk_handle* h) {
     for (int p = 0; p < 2; ++p)
-        for (int r = 0; r <= spk::MAXRHS; ++r) drop_graph(h->g_solve[p][r]);
+        for (int r = 0; r <= spk::MAXRHS; ++r) {
+            drop_graph(h->g_solve[p][r]);
+            drop_graph(h->g_tsolve[p][r]);
+        }
 }
 
 // Run `body` (which issues launches on h->stream) through a CUDA graph: the
@@ -893,7 +898,7 @@ static int run_factor(spk_handle* h) {
 
 // Solve in place on the permuted work vectors: wb (rhs, consumed) -> wx.
 template <typename T>
-static int run_solve_permuted(spk_handle* h, int nrhs) {
+static int run_solve_permuted(spk_handle* h, int nrhs, bool transpose) {
     const T* fac = storage<T>(h).d;
     const T* inv = storage<T>(h).inv2;
     const Plan& PL = h->plan[prec_index<T>()];
@@ -902,6 +907,30 @@ static int run_solve_permuted(spk_handle* h, int nrhs) {
     T* y = (T*)h->d_wy;
     T* x = (T*)h->d_wx;
     const int n = (int)h->n;
+    if (transpose) {   // A^T: U^T pass in block order, then L^T pass top-down with blocks reversed
+        for (const LevelPlan& P : PL.levels)
+            for (size_t t = 0; t < P.fwd.size(); ++t)
+                if (P.fwd[t].tiles > 0) {
+                    LaunchScope ls(h, SPK_K_FWD, P.fwd[t].flops * nrhs, P.fwd[t].words * sizeof(T));
+                    spk::k_tfwd<T><<<P.fwd[t].tiles, spk::TS, 0, h->stream>>>(fac, inv, b, y, n, nrhs, S,
+                                                                               launch_of(PL, P.fwd[t]), (int)t);
+                }
+        for (size_t l = PL.levels.size(); l-- > 0;) {
+            const LevelPlan& P = PL.levels[l];
+            if (P.bwdu.tiles > 0) {
+                LaunchScope ls(h, SPK_K_BWD, P.bwdu.flops * nrhs, P.bwdu.words * sizeof(T));
+                spk::k_tbwd_l21<T><<<P.bwdu.tiles, spk::TS, 0, h->stream>>>(fac, y, x, n, nrhs, S, launch_of(PL, P.bwdu));
+            }
+            for (size_t t = 0; t < P.bwd.size(); ++t)
+                if (P.bwd[t].tiles > 0) {
+                    LaunchScope ls(h, SPK_K_BWD, P.bwd[t].flops * nrhs, P.bwd[t].words * sizeof(T));
+                    spk::k_tbwd<T><<<P.bwd[t].tiles, spk::TS, 0, h->stream>>>(fac, inv, y, x, n, nrhs, S,
+                                                                               launch_of(PL, P.bwd[t]), (int)t);
+                }
+        }
+        CU(h, cudaGetLastError());
+        return SPK_OK;
+    }
     for (const LevelPlan& P : PL.levels)
         for (size_t t = 0; t < P.fwd.size(); ++t)
             if (P.fwd[t].tiles > 0) {
@@ -926,9 +955,11 @@ static int run_solve_permuted(spk_handle* h, int nrhs) {
     return SPK_OK;
 }
 
-// x(:, 0:nrhs) (=|+=) A^{-1} rhs(:, 0:nrhs), both device FP64, original order.
+// x(:, 0:nrhs) (=|+=) A^{-1} rhs(:, 0:nrhs) (A^{-T} with `transpose`), both
+// device FP64, original order.
 template <typename T>
-static int solve_device(spk_handle* h, const double* rhs, i64 ldr, double* x, i64 ldx, i64 nrhs, int accumulate) {
+static int solve_device(spk_handle* h, const double* rhs, i64 ldr, double* x, i64 ldx, i64 nrhs, int accumulate,
+                        bool transpose = false) {
     const int n = (int)h->n;
     for (i64 c0 = 0; c0 < nrhs; c0 += spk::MAXRHS) {
         int nc = (int)std::min<i64>(spk::MAXRHS, nrhs - c0);
@@ -939,8 +970,8 @@ static int solve_device(spk_handle* h, const double* rhs, i64 ldr, double* x, i6
             spk::k_permute<double, T><<<blocks, 256, 0, h->stream>>>(rhs + c0 * ldr, ldr, (T*)h->d_wb, n, h->d_rperm,
                                                                      n, nc);
         }
-        int rc = via_graph(h, h->g_solve[prec_index<T>()][nc],
-                           [&] { return run_solve_permuted<T>(h, nc); });
+        GraphRec& g = transpose ? h->g_tsolve[prec_index<T>()][nc] : h->g_solve[prec_index<T>()][nc];
+        int rc = via_graph(h, g, [&] { return run_solve_permuted<T>(h, nc, transpose); });
         if (rc) return rc;
         {
             LaunchScope ls(h, SPK_K_PERMUTE, 0.0, (double)tot * (8 * (accumulate ? 2 : 1) + 4 + sizeof(T)));
@@ -953,15 +984,19 @@ static int solve_device(spk_handle* h, const double* rhs, i64 ldr, double* x, i6
 }
 
 static int residual_device(spk_handle* h, const double* b, i64 ldb, const double* x, i64 ldx, i64 nrhs,
-                           double* relres) {
+                           double* relres, bool transpose = false) {
     const int n = (int)h->n;
     CU(h, cudaMemsetAsync(h->d_sums, 0, sizeof(double) * 2 * (size_t)nrhs, h->stream));
     dim3 grid((n + 255) / 256, (unsigned)nrhs);
     {
         LaunchScope ls(h, SPK_K_RESIDUAL, 2.0 * h->nnz * nrhs, (double)h->nnz * (8 + 4 + 8) + 8.0 * h->nnz * nrhs +
                                                                   24.0 * n * nrhs);
-        spk::k_residual<<<grid, 256, 0, h->stream>>>(h->d_aval, h->d_rowptr, h->d_col, h->d_src, x, ldx, b, ldb, h->d_r,
-                                                     n, (int)nrhs, h->d_sums);
+        if (transpose)   // rows of A^T = A's CSC columns, values in order
+            spk::k_residual<<<grid, 256, 0, h->stream>>>(h->d_aval, h->d_ccolptr, h->d_crow, nullptr, x, ldx, b, ldb,
+                                                         h->d_r, n, (int)nrhs, h->d_sums);
+        else
+            spk::k_residual<<<grid, 256, 0, h->stream>>>(h->d_aval, h->d_rowptr, h->d_col, h->d_src, x, ldx, b, ldb,
+                                                         h->d_r, n, (int)nrhs, h->d_sums);
     }
     CU(h, cudaGetLastError());
     std::vector<double> sums(2 * nrhs);
@@ -1157,6 +1192,18 @@ int spk_set_pattern(spk_handle* h, int64_t ncols, const int64_t* colptr, const i
                 src[at] = k - (colptr[0] - b);
             }
     }
+    std::vector<int> ccolptr(n + 1), crow(nnz), ccol(nnz);
+    for (i64 j = 0; j <= n; ++j) ccolptr[j] = (int)(colptr[j] - colptr[0]);
+    for (i64 j = 0; j < n; ++j)
+        for (i64 k = colptr[j] - b; k < colptr[j + 1] - b; ++k) {
+            crow[k - (colptr[0] - b)] = (int)(rowval[k] - b);
+            ccol[k - (colptr[0] - b)] = (int)j;
+        }
+    cudaFree(h->d_ccolptr); cudaFree(h->d_crow); cudaFree(h->d_ccol);
+    h->d_ccolptr = h->d_crow = h->d_ccol = nullptr;
+    if ((rc = upload(h, &h->d_ccolptr, ccolptr))) return rc;
+    if ((rc = upload(h, &h->d_crow, crow))) return rc;
+    if ((rc = upload(h, &h->d_ccol, ccol))) return rc;
     cudaFree(h->d_slot); cudaFree(h->d_aval); cudaFree(h->d_rowptr); cudaFree(h->d_col); cudaFree(h->d_src);
     cudaFree(h->d_rperm); cudaFree(h->d_rinvp);
     h->d_slot = nullptr; h->d_aval = nullptr; h->d_rowptr = h->d_col = nullptr; h->d_src = nullptr;
@@ -1226,7 +1273,7 @@ int spk_factor(spk_handle* h, int precision, int64_t* first_singular) {
 }
 
 
-int spk_solve(spk_handle* h, double* b, int64_t nrhs, int64_t ldb, int where, int precision) {
+static int solve_impl(spk_handle* h, double* b, int64_t nrhs, int64_t ldb, int where, int precision, bool transpose) {
     int rc = check_h(h);
     if (rc) return rc;
     if (!valid_precision(precision) || nrhs < 0 || (nrhs > 0 && (!b || ldb < h->n)) ||
@@ -1247,13 +1294,21 @@ int spk_solve(spk_handle* h, double* b, int64_t nrhs, int64_t ldb, int where, in
         src = b;
         ld = ldb;
     }
-    rc = precision == SPK_FP64 ? solve_device<double>(h, src, ld, h->d_x, n, nrhs, 0)
-                               : solve_device<float>(h, src, ld, h->d_x, n, nrhs, 0);
+    rc = precision == SPK_FP64 ? solve_device<double>(h, src, ld, h->d_x, n, nrhs, 0, transpose)
+                               : solve_device<float>(h, src, ld, h->d_x, n, nrhs, 0, transpose);
     if (rc) return rc;
     CU(h, cudaMemcpy2DAsync(b, sizeof(double) * ldb, h->d_x, sizeof(double) * n, sizeof(double) * n, nrhs,
                             where == SPK_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, h->stream));
     CU(h, cudaStreamSynchronize(h->stream));
     return SPK_OK;
+}
+
+int spk_solve(spk_handle* h, double* b, int64_t nrhs, int64_t ldb, int where, int precision) {
+    return solve_impl(h, b, nrhs, ldb, where, precision, false);
+}
+
+int spk_solve_transpose(spk_handle* h, double* b, int64_t nrhs, int64_t ldb, int where, int precision) {
+    return solve_impl(h, b, nrhs, ldb, where, precision, true);
 }
 
 int spk_residual(spk_handle* h, const double* b, const double* x, int64_t nrhs, int64_t ld, int where,
@@ -1333,8 +1388,8 @@ int spk_residual_noalloc(spk_handle* h, const double* b, const double* x, int64_
     return SPK_OK;
 }
 
-int spk_refine(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where, int precision,
-               double tol, int max_iter, int* iters, double* relres) {
+static int refine_impl(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where, int precision,
+                       double tol, int max_iter, int* iters, double* relres, bool transpose) {
     int rc = check_h(h);
     if (rc) return rc;
     if (iters) *iters = 0;
@@ -1359,14 +1414,14 @@ int spk_refine(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t 
         ldb = ldx = ld;
     }
     auto solve_into = [&](const double* rhs, i64 ldr, int acc) {
-        return precision == SPK_FP64 ? solve_device<double>(h, rhs, ldr, dx, ldx, nrhs, acc)
-                                     : solve_device<float>(h, rhs, ldr, dx, ldx, nrhs, acc);
+        return precision == SPK_FP64 ? solve_device<double>(h, rhs, ldr, dx, ldx, nrhs, acc, transpose)
+                                     : solve_device<float>(h, rhs, ldr, dx, ldx, nrhs, acc, transpose);
     };
     if ((rc = solve_into(db, ldb, 0))) return rc;
     double rel = 0.0;
     int it = 0;
     for (;;) {
-        if ((rc = residual_device(h, db, ldb, dx, ldx, nrhs, &rel))) return rc;
+        if ((rc = residual_device(h, db, ldb, dx, ldx, nrhs, &rel, transpose))) return rc;
         if (rel <= tol || it >= max_iter || rel != rel) break;
         if ((rc = solve_into(h->d_r, n, 1))) return rc;
         ++it;
@@ -1385,6 +1440,52 @@ int spk_refine(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t 
     return SPK_OK;
 }
 
+
+int spk_refine(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where, int precision,
+               double tol, int max_iter, int* iters, double* relres) {
+    return refine_impl(h, b, x, nrhs, ld, where, precision, tol, max_iter, iters, relres, false);
+}
+
+int spk_refine_transpose(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where, int precision,
+                         double tol, int max_iter, int* iters, double* relres) {
+    return refine_impl(h, b, x, nrhs, ld, where, precision, tol, max_iter, iters, relres, true);
+}
+
+int spk_grad_pattern(spk_handle* h, const double* lambda, const double* x, int64_t nrhs, int64_t ld, int where,
+                     double* dA) {
+    int rc = check_h(h);
+    if (rc) return rc;
+    if (!h->have_pattern) return set_err(h, SPK_ESEQ, "Sequence error. Pattern not set yet.");
+    if (nrhs <= 0 || ld < h->n || !lambda || !x || (!dA && h->nnz > 0) || (where != SPK_HOST && where != SPK_DEVICE))
+        return set_err(h, SPK_EARG, "spk_grad_pattern: bad arguments");
+    if (h->nnz == 0) return SPK_OK;
+    const i64 n = h->n;
+    const double *dl = lambda, *dxp = x;
+    double* dg = dA;
+    double* tmp = nullptr;
+    i64 ldd = ld;
+    if (where == SPK_HOST) {   // staged through the handle's work vectors
+        if ((rc = ensure_rhs(h, nrhs))) return rc;
+        CU(h, cudaMemcpy2DAsync(h->d_rhs, sizeof(double) * n, lambda, sizeof(double) * ld, sizeof(double) * n, nrhs,
+                                cudaMemcpyHostToDevice, h->stream));
+        CU(h, cudaMemcpy2DAsync(h->d_x, sizeof(double) * n, x, sizeof(double) * ld, sizeof(double) * n, nrhs,
+                                cudaMemcpyHostToDevice, h->stream));
+        CU(h, cudaMallocAsync((void**)&tmp, sizeof(double) * (size_t)h->nnz, h->stream));
+        dl = h->d_rhs;
+        dxp = h->d_x;
+        dg = tmp;
+        ldd = n;
+    }
+    const int blocks = (int)std::min<i64>((h->nnz + 255) / 256, 152 * 16);
+    spk::k_grad_pattern<<<blocks, 256, 0, h->stream>>>(h->d_crow, h->d_ccol, dl, dxp, ldd, (int)nrhs, dg, h->nnz);
+    CU(h, cudaGetLastError());
+    if (where == SPK_HOST) {
+        CU(h, cudaMemcpyAsync(dA, tmp, sizeof(double) * (size_t)h->nnz, cudaMemcpyDeviceToHost, h->stream));
+        CU(h, cudaFreeAsync(tmp, h->stream));
+    }
+    CU(h, cudaStreamSynchronize(h->stream));
+    return SPK_OK;
+}
 
 int spk_get_factors(spk_handle* h, int precision, double* lnz, double* unz, int64_t* ipiv) {
     int rc = check_h(h);
@@ -1483,7 +1584,7 @@ void spk_destroy(spk_handle* h) {
     free_plan(h->plan[1]);
     void* ptrs[] = {h->d_xs, h->d_rows, h->d_runid, h->d_run_tgt, h->d_run_start, h->d_run_rel,
                     h->d_rel, h->s64.inv2, h->s32.inv2, h->s64.pack, h->s32.pack, h->d_ipiv, h->d_info, h->d_slot, h->d_aval,
-                    h->d_rowptr, h->d_col, h->d_src, h->d_rperm, h->d_rinvp, h->s64.d, h->s32.d, h->d_wb,
+                    h->d_rowptr, h->d_col, h->d_src, h->d_ccolptr, h->d_crow, h->d_ccol, h->d_rperm, h->d_rinvp, h->s64.d, h->s32.d, h->d_wb,
                     h->d_wy, h->d_wx, h->d_rhs, h->d_x, h->d_r, h->d_sums};
     for (void* p : ptrs)
         if (p) cudaFree(p);

@@ -1380,6 +1380,218 @@ __global__ void __launch_bounds__(TS) k_bwd(const T* fac, const T* inv2, T* y, T
 }
 
 // ---------------------------------------------------------------------------
+// Transposed solves, A^T x = b with the same factors (no reference kernel:
+// the reference's `transposetriangularsolve` is commented out,
+// SpkSparseSpdSolver.jl:384).  With A~ = L U factored block by block, the
+// forward operator is E_N ... E_1 (E_B: y_B = Minv_B b_B, b_below -=
+// L_below,B y_B) and the backward one G_1 ... G_N (G_B: x_B = Uinv_B (y_B -
+// U_B,right x_right)); A~^T = (G-chain)^T (E-chain)^T reversed:
+//   pass 1, blocks in order (children first): z_B = Uinv_B^T c_B, then the
+//     columns right of the block (front columns and U12, through R_F) get
+//     U_B,right^T z_B subtracted;
+//   pass 2, fronts top-down: the front's columns get L21^T x[R_F]
+//     subtracted, then blocks in reverse: x_B = Minv_B^T z_B, and the
+//     front's earlier columns get L_B,earlier^T x_B subtracted.
+// The tiles and launch lists are those of k_fwd / k_bwd_u12 / k_bwd.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(TS) k_tfwd(const T* fac, const T* inv2, T* b, T* z, int n, int nrhs, Sched S,
+                                             Launch L, int step) {
+    constexpr int BM = BlockMax<T>::value;
+    __shared__ T sb[BM * MAXRHS];
+    __shared__ T sp[4 * SC * MAXRHS];
+    __shared__ T sz[SC * MAXRHS];
+    int fid, tile;
+    locate(L, blockIdx.x, fid, tile);
+    const DFront F = S.fronts[fid];
+    const int blk = F.block0 + step;
+    const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
+    const int ncc = cdiv(bw, SC), cc = tile % ncc, rt = tile / ncc;
+    const int j0 = cc * SC, nj = min(SC, bw - j0);
+    const T* Ui = inv2 + S.blk_inv2[blk] + (ll)bw * bw;   // Uinv(k, j) at Ui[j * bw + k], zero for k > j
+    const int tid = threadIdx.x;
+    for (int e = tid; e < bw * nrhs; e += TS) {
+        int k = e % bw, r = e / bw;
+        sb[r * BM + k] = b[(ll)r * n + F.f + c0 + k];
+    }
+    __syncthreads();
+    {   // z_chunk = (Uinv^T)[j0:j0+nj, :] c_B : 32 columns x 4 partial sums over k <= j
+        const int j = tid & 31, kq = tid >> 5;
+        T acc[MAXRHS];
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r) acc[r] = T(0);
+        if (j < nj) {
+            const T* ucol = Ui + (ll)(j0 + j) * bw;
+#pragma unroll 8
+            for (int k = kq; k <= j0 + j; k += 4) {
+                const T uk = ucol[k];
+#pragma unroll
+                for (int r = 0; r < MAXRHS; ++r)
+                    if (r < nrhs) acc[r] += uk * sb[r * BM + k];
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r)
+            if (r < nrhs) sp[(kq * MAXRHS + r) * SC + j] = acc[r];
+    }
+    __syncthreads();
+    for (int e = tid; e < SC * nrhs; e += TS) {
+        int j = e % SC, r = e / SC;
+        sz[r * SC + j] = sp[(0 * MAXRHS + r) * SC + j] + sp[(1 * MAXRHS + r) * SC + j] +
+                         sp[(2 * MAXRHS + r) * SC + j] + sp[(3 * MAXRHS + r) * SC + j];
+    }
+    __syncthreads();
+    if (rt == 0)
+        for (int e = tid; e < nj * nrhs; e += TS) {
+            int j = e % nj, r = e / nj;
+            z[(ll)r * n + F.f + c0 + j0 + j] = sz[r * SC + j];
+        }
+    const int col = c1 + rt * TS + tid;   // a column right of the block: front column (< nf) or U12 column
+    if (col < F.ld) {
+        T uv[SC];
+        int gcol;
+        if (col < F.nf) {
+            gcol = F.f + col;
+            const T* u = fac + F.loff + (ll)col * F.ld + c0 + j0;      // U(c0 + j0 + jj, col), contiguous
+#pragma unroll
+            for (int jj = 0; jj < SC; ++jj) uv[jj] = jj < nj ? u[jj] : T(0);
+        } else {
+            const int uc = col - F.nf;
+            gcol = S.rows[F.rows_off + uc];
+            const T* u = fac + F.uoff + (ll)(c0 + j0) * F.m + uc;       // U12(c0 + j0 + jj, uc)
+#pragma unroll
+            for (int jj = 0; jj < SC; ++jj) uv[jj] = jj < nj ? u[(ll)jj * F.m] : T(0);
+        }
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r) {
+            if (r >= nrhs) break;
+            T acc = T(0);
+#pragma unroll
+            for (int jj = 0; jj < SC; ++jj) acc += uv[jj] * sz[r * SC + jj];
+            atomicAdd(&b[(ll)r * n + gcol], -acc);
+        }
+    }
+}
+
+// Pass 2, per front: z[F's columns] -= L21^T x[R_F], one warp per column
+// (L21 column k contiguous in Lf).
+template <typename T>
+__global__ void __launch_bounds__(TS) k_tbwd_l21(const T* fac, T* z, const T* x, int n, int nrhs, Sched S, Launch L) {
+    int fid, tile;
+    locate(L, blockIdx.x, fid, tile);
+    const DFront F = S.fronts[fid];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int k = tile * (TS / 32) + wid;
+    if (k >= F.nf) return;
+    const T* l = fac + F.loff + (ll)k * F.ld + F.nf;
+    const int* rows = S.rows + F.rows_off;
+    T acc[MAXRHS];
+#pragma unroll
+    for (int r = 0; r < MAXRHS; ++r) acc[r] = T(0);
+#pragma unroll 4
+    for (int i = lane; i < F.m; i += 32) {
+        const T lv = l[i];
+        const int g = rows[i];
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r)
+            if (r < nrhs) acc[r] += lv * x[(ll)r * n + g];
+    }
+#pragma unroll
+    for (int r = 0; r < MAXRHS; ++r) {
+        if (r >= nrhs) break;
+        T v = acc[r];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) z[(ll)r * n + F.f + k] -= v;
+    }
+}
+
+// Pass 2, block `step`-th from the last: x_chunk = (Minv^T)[chunk, :] z_B,
+// stored by the first tile, then the front's columns before the block get
+// L[block rows, column]^T x_chunk subtracted (atomics across chunks).
+template <typename T>
+__global__ void __launch_bounds__(TS) k_tbwd(const T* fac, const T* inv2, T* z, T* x, int n, int nrhs, Sched S,
+                                             Launch L, int step) {
+    constexpr int BM = BlockMax<T>::value;
+    __shared__ T sc[BM * MAXRHS];
+    __shared__ T sp[4 * SC * MAXRHS];
+    __shared__ T sx[SC * MAXRHS];
+    int fid, tile;
+    locate(L, blockIdx.x, fid, tile);
+    const DFront F = S.fronts[fid];
+    const int blk = F.block0 + F.nblocks - 1 - step;
+    const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
+    const int ncc = cdiv(bw, SC), cc = tile % ncc, rt = tile / ncc;
+    const int j0 = cc * SC, nj = min(SC, bw - j0);
+    const T* Mi = inv2 + S.blk_inv2[blk];   // Minv(k, j) at Mi[j * bw + k]
+    const int tid = threadIdx.x;
+    for (int e = tid; e < bw * nrhs; e += TS) {
+        int k = e % bw, r = e / bw;
+        sc[r * BM + k] = z[(ll)r * n + F.f + c0 + k];
+    }
+    __syncthreads();
+    {
+        const int j = tid & 31, kq = tid >> 5;
+        T acc[MAXRHS];
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r) acc[r] = T(0);
+        if (j < nj) {
+            const T* mcol = Mi + (ll)(j0 + j) * bw;
+#pragma unroll 8
+            for (int k = kq; k < bw; k += 4) {
+                const T mk = mcol[k];
+#pragma unroll
+                for (int r = 0; r < MAXRHS; ++r)
+                    if (r < nrhs) acc[r] += mk * sc[r * BM + k];
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r)
+            if (r < nrhs) sp[(kq * MAXRHS + r) * SC + j] = acc[r];
+    }
+    __syncthreads();
+    for (int e = tid; e < SC * nrhs; e += TS) {
+        int j = e % SC, r = e / SC;
+        sx[r * SC + j] = sp[(0 * MAXRHS + r) * SC + j] + sp[(1 * MAXRHS + r) * SC + j] +
+                         sp[(2 * MAXRHS + r) * SC + j] + sp[(3 * MAXRHS + r) * SC + j];
+    }
+    __syncthreads();
+    if (rt == 0)
+        for (int e = tid; e < nj * nrhs; e += TS) {
+            int j = e % nj, r = e / nj;
+            x[(ll)r * n + F.f + c0 + j0 + j] = sx[r * SC + j];
+        }
+    const int col = rt * TS + tid;   // a front column before the block
+    if (col < c0) {
+        T lv[SC];
+        const T* l = fac + F.loff + (ll)col * F.ld + c0 + j0;   // L(c0 + j0 + jj, col), contiguous
+#pragma unroll
+        for (int jj = 0; jj < SC; ++jj) lv[jj] = jj < nj ? l[jj] : T(0);
+#pragma unroll
+        for (int r = 0; r < MAXRHS; ++r) {
+            if (r >= nrhs) break;
+            T acc = T(0);
+#pragma unroll
+            for (int jj = 0; jj < SC; ++jj) acc += lv[jj] * sx[r * SC + jj];
+            atomicAdd(&z[(ll)r * n + F.f + col], -acc);
+        }
+    }
+}
+
+// dA (on A's pattern, CSC order) = -sum_r lambda_r x_r^T: the gradient of a
+// loss of x = A^{-1} b with respect to A's stored entries, given the adjoint
+// lambda = A^{-T} dloss/dx.
+__global__ void k_grad_pattern(const int* __restrict__ row, const int* __restrict__ colof, const double* __restrict__ lam,
+                               const double* __restrict__ x, ll ld, int nrhs, double* __restrict__ dA, ll nnz) {
+    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (ll)gridDim.x * blockDim.x) {
+        const int i = row[k], j = colof[k];
+        double s = 0.0;
+        for (int r = 0; r < nrhs; ++r) s += lam[(ll)r * ld + i] * x[(ll)r * ld + j];
+        dA[k] = -s;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Assembly, permutation, residual.
 // ---------------------------------------------------------------------------
 
@@ -1412,8 +1624,9 @@ __global__ void k_unpermute(const Tin* __restrict__ xp, ll ldp, double* __restri
     if (accumulate) x[(ll)r * ldx + j] += v; else x[(ll)r * ldx + j] = v;
 }
 
-// r = b - A x in FP64 with A in row order (values gathered from CSC order);
-// the squares of r and b are accumulated per right-hand side.
+// r = b - A x in FP64 with A in row order (values gathered from CSC order
+// through src), or r = b - A^T x with A^T's rows = A's CSC columns (src
+// null); the squares of r and b are accumulated per right-hand side.
 __global__ void k_residual(const double* __restrict__ aval, const int* __restrict__ rowptr, const int* __restrict__ col,
                            const ll* __restrict__ src, const double* __restrict__ x, ll ldx, const double* __restrict__ b,
                            ll ldb, double* __restrict__ r, int n, int nrhs, double* __restrict__ sums) {
@@ -1422,7 +1635,7 @@ __global__ void k_residual(const double* __restrict__ aval, const int* __restric
     double rr = 0.0, bb = 0.0;
     if (i < n) {
         double s = 0.0;
-        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) s += aval[src[k]] * x[(ll)rhs * ldx + col[k]];
+        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) s += aval[src ? src[k] : k] * x[(ll)rhs * ldx + col[k]];
         double bi = b[(ll)rhs * ldb + i];
         double ri = bi - s;
         r[(ll)rhs * n + i] = ri;
@@ -1450,7 +1663,7 @@ __global__ void k_residual_norms(const double* __restrict__ aval, const int* __r
     double rr = 0.0, bb = 0.0;
     if (i < n) {
         double s = 0.0;
-        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) s += aval[src[k]] * x[(ll)rhs * ldx + col[k]];
+        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) s += aval[src ? src[k] : k] * x[(ll)rhs * ldx + col[k]];
         double bi = b[(ll)rhs * ldb + i];
         double ri = bi - s;
         rr = ri * ri;

@@ -15,8 +15,8 @@ from .device import ErrorException, NumericEngine, SingularException
 from .graph import ETree, Graph, Ordering, isstructuresymmetric, makestructuresymmetric, mmd_, nd_grid
 from .problem import (Grid, Problem, computeresidual, inaij_, inbi_, infullrhs_, insparse_, makegridproblem,
                       makerhs_, outsparse, zerorhs_)
-from .sparse_solver import (SparseSolver, factor_, findorder_, findorderperm_, inmatrix_, refine_, solve_,
-                            symbolicfactor_, triangularsolve_)
+from .sparse_solver import (SparseSolver, factor_, findorder_, findorderperm_, gradient_, inmatrix_, refine_, solve_,
+                            symbolicfactor_, transposetriangularsolve_, triangularsolve_)
 
 __all__ = [
     "build", "gallery", "graph", "problem", "sparse_solver",
@@ -25,6 +25,6 @@ __all__ = [
     "ETree", "Graph", "Ordering", "isstructuresymmetric", "makestructuresymmetric", "mmd_", "nd_grid",
     "Grid", "Problem", "computeresidual", "inaij_", "inbi_", "infullrhs_", "insparse_", "makegridproblem",
     "makerhs_", "outsparse", "zerorhs_",
-    "SparseSolver", "factor_", "findorder_", "findorderperm_", "inmatrix_", "refine_", "solve_",
-    "symbolicfactor_", "triangularsolve_",
+    "SparseSolver", "factor_", "findorder_", "findorderperm_", "gradient_", "inmatrix_", "refine_", "solve_",
+    "symbolicfactor_", "transposetriangularsolve_", "triangularsolve_",
 ]

@@ -38,6 +38,10 @@ GPU_SYMBOLS = {
     "spk_load_values": (ctypes.c_int, [VP, VP, ctypes.c_int, ctypes.c_int]),
     "spk_factor": (ctypes.c_int, [VP, ctypes.c_int, P64]),
     "spk_solve": (ctypes.c_int, [VP, VP, i64, i64, ctypes.c_int, ctypes.c_int]),
+    "spk_solve_transpose": (ctypes.c_int, [VP, VP, i64, i64, ctypes.c_int, ctypes.c_int]),
+    "spk_refine_transpose": (ctypes.c_int, [VP, VP, VP, i64, i64, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                            ctypes.c_int, ctypes.POINTER(ctypes.c_int), PD]),
+    "spk_grad_pattern": (ctypes.c_int, [VP, VP, VP, i64, i64, ctypes.c_int, VP]),
     "spk_refine": (ctypes.c_int, [VP, VP, VP, i64, i64, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                   ctypes.c_int, ctypes.POINTER(ctypes.c_int), PD]),
     "spk_residual": (ctypes.c_int, [VP, VP, VP, i64, i64, ctypes.c_int, PD]),

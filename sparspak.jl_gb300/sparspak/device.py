@@ -132,14 +132,16 @@ class NumericEngine:
             raise SingularException(self._lib.spk_last_error(self._h).decode(), int(first.value))
         self._check(rc, "spk_factor")
 
-    def solve(self, b, precision="fp64"):
-        """Solve in place; b is a vector or n x nrhs column-major (numpy) / (nrhs, n) (torch)."""
+    def solve(self, b, precision="fp64", transpose=False):
+        """Solve A x = b (A^T x = b with transpose) in place; b is a vector or
+        n x nrhs column-major (numpy) / (nrhs, n) (torch)."""
         n, nrhs, ld = _shape(b)
         p, where = _ptr(b)
-        self._check(self._lib.spk_solve(self._h, p, nrhs, ld, where, _prec(precision)), "spk_solve")
+        fn = self._lib.spk_solve_transpose if transpose else self._lib.spk_solve
+        self._check(fn(self._h, p, nrhs, ld, where, _prec(precision)), "spk_solve")
         return b
 
-    def refine(self, b, x, precision="fp32", tol=1e-12, max_iter=20, raise_on_fail=True):
+    def refine(self, b, x, precision="fp32", tol=1e-12, max_iter=20, raise_on_fail=True, transpose=False):
         n, nrhs, ld = _shape(b)
         pb, wb = _ptr(b)
         px, wx = _ptr(x)
@@ -147,12 +149,31 @@ class NumericEngine:
             raise ValueError("b and x must both live on the host or both on the device")
         it = ctypes.c_int(0)
         rr = ctypes.c_double(0.0)
-        rc = self._lib.spk_refine(self._h, pb, px, nrhs, ld, wb, _prec(precision), float(tol), int(max_iter),
-                                  ctypes.byref(it), ctypes.byref(rr))
+        fn = self._lib.spk_refine_transpose if transpose else self._lib.spk_refine
+        rc = fn(self._h, pb, px, nrhs, ld, wb, _prec(precision), float(tol), int(max_iter), ctypes.byref(it),
+                ctypes.byref(rr))
         if rc == N.SPK_ENOCONV and not raise_on_fail:
             return it.value, rr.value
         self._check(rc, "spk_refine")
         return it.value, rr.value
+
+    def grad_pattern(self, lam, x):
+        """dA on A's pattern (CSC order) = -sum_r lam_r x_r^T: numpy in, numpy out (or torch CUDA in and out)."""
+        n, nrhs, ld = _shape(lam)
+        pl, wl = _ptr(lam)
+        px, wx = _ptr(x)
+        if wl != wx:
+            raise ValueError("lam and x must both live on the host or both on the device")
+        if wl == N.SPK_DEVICE:
+            import torch
+
+            out = torch.empty(self.nnz, dtype=torch.float64, device=lam.device)
+            po = ctypes.c_void_p(out.data_ptr())
+        else:
+            out = np.empty(self.nnz, np.float64)
+            po = ctypes.c_void_p(out.ctypes.data)
+        self._check(self._lib.spk_grad_pattern(self._h, pl, px, nrhs, ld, wl, po), "spk_grad_pattern")
+        return out
 
     def residual(self, b, x):
         n, nrhs, ld = _shape(b)

@@ -267,6 +267,17 @@ def triangularsolve_(s: SparseSolver, rhs=None) -> bool:
     return True
 
 
+def transposetriangularsolve_(s: SparseSolver, rhs) -> bool:
+    """Solve A^T x = rhs in place with the factors of A (the reference's
+    `transposetriangularsolve` is commented out, SpkSparseSpdSolver.jl:384)."""
+    if not s._factordone:
+        raise ErrorException("Sequence error. Factorization not done yet.")
+    if s.slvr.n == 0:
+        raise ErrorException("An empty problem. No solution.")
+    s.slvr.engine.solve(rhs, s.slvr.precision, transpose=True)
+    return True
+
+
 def solve_(s: SparseSolver, rhs=None) -> bool:
     """All phases (SpkSparseSolver.jl:80-87; with rhs, SparseCSCInterface.jl:194-201)."""
     findorder_(s) or _fail("Finding Order.")
@@ -278,7 +289,7 @@ def solve_(s: SparseSolver, rhs=None) -> bool:
 
 
 def refine_(s: SparseSolver, b: np.ndarray, x: np.ndarray | None = None, precision: str = "fp32", tol: float = 1e-12,
-            max_iter: int = 20):
+            max_iter: int = 20, transpose: bool = False):
     """Mixed-precision solve: factor in `precision` (if not yet), then FP64 iterative refinement.
 
     Returns (x, corrections, relative residual).  New in this engine; the
@@ -294,8 +305,18 @@ def refine_(s: SparseSolver, b: np.ndarray, x: np.ndarray | None = None, precisi
         factor_(s)
     b = np.asfortranarray(b, dtype=np.float64)
     x = np.zeros_like(b) if x is None else x
-    it, rr = s.slvr.engine.refine(b, x, precision, tol, max_iter)
+    it, rr = s.slvr.engine.refine(b, x, precision, tol, max_iter, transpose=transpose)
     return x, it, rr
+
+
+def gradient_(s: SparseSolver, lam: np.ndarray, x: np.ndarray) -> np.ndarray:
+    """dloss/dA on A's pattern (CSC order of the matrix given to the solver),
+    -sum_r lam_r x_r^T, for lam = A^{-T} dloss/dx (adjoint of x = A^{-1} b)."""
+    if not s._inmatrixdone:
+        raise ErrorException("Sequence error. Matrix input not done yet.")
+    lam = np.asfortranarray(lam, dtype=np.float64)
+    x = np.asfortranarray(x, dtype=np.float64)
+    return s.slvr.engine.grad_pattern(lam, x)
 
 
 def _fail(msg):
