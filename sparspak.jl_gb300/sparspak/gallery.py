@@ -101,6 +101,28 @@ def diffusion_2d(s, theta_h, theta_v, theta_d1=None, theta_d2=None):
     return _assemble(n, np.concatenate(rows), np.concatenate(cols), np.concatenate(vals))
 
 
+def batched_diffusion(nsys=512, smin=20, smax=120, seed=0):
+    """Block-diagonal union of `nsys` independent SPD systems: system k is the
+    9-point (8-neighbour) weighted graph Laplacian of an s_k x s_k grid,
+    s_k ~ U{smin..smax}, edge conductivities ~ lognormal(0, 1), Dirichlet
+    boundary terms (out-of-grid neighbours add their conductivity to the
+    diagonal).  Returns (A, sizes) with A scipy CSC and the systems in order.
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sizes = rng.integers(smin, smax + 1, size=nsys)
+    blocks = []
+    for s in sizes:
+        s = int(s)
+        th = rng.lognormal(0.0, 1.0, size=(s, s + 1))
+        tv = rng.lognormal(0.0, 1.0, size=(s + 1, s))
+        t1 = rng.lognormal(0.0, 1.0, size=(s + 1, s + 1))
+        t2 = rng.lognormal(0.0, 1.0, size=(s + 1, s + 1))
+        blocks.append(diffusion_2d(s, th, tv, t1, t2))
+    A = sp.block_diag(blocks, format="csc")
+    A.sort_indices()
+    return A, [int(s) for s in sizes]
+
+
 def random_rhs(n, nrhs=1, seed=0):
     """Entries i.i.d. uniform[-1, 1] from numpy PCG64(seed); column-major n x nrhs."""
     rng = np.random.Generator(np.random.PCG64(seed))

@@ -138,3 +138,42 @@ def nd_grid(nx: int, ny: int, nz: int = 1, leaf: int = 64):
         order.cperm, order.cinvp = perm.copy(), invp.copy()
 
     return orderfunction
+
+
+def nd_grid_batched(sizes, leaf: int = 64):
+    """Order function for the block-diagonal union of square grids (system k:
+    sizes[k] x sizes[k] vertices, consecutive): nested dissection of every
+    grid on its own, the systems kept in order.  The union's elimination
+    forest then has one tree per system, which the numeric phase factors
+    together level by level."""
+    sizes = [int(s) for s in sizes]
+
+    def orderfunction(g: Graph, order: Ordering) -> None:
+        total = sum(s * s for s in sizes)
+        if g.nv != total:
+            raise ValueError(f"graph has {g.nv} vertices, the systems {total}")
+        perm = np.zeros(g.nv, dtype=np.int64)
+        invp = np.zeros(g.nv, dtype=np.int64)
+        off = 0
+        for s in sizes:
+            nv = s * s
+            lo, hi = g.xadj[off] - 1, g.xadj[off + nv] - 1        # adjacency of the system (1-based)
+            xadj = g.xadj[off: off + nv + 1] - lo
+            adj = g.adj[lo:hi] - off
+            if adj.size and (adj.min() < 1 or adj.max() > nv):
+                raise ValueError("the systems are not independent blocks")
+            xadj = np.ascontiguousarray(xadj, dtype=np.int64)
+            adj = np.ascontiguousarray(adj if adj.size else np.zeros(1, np.int64), dtype=np.int64)
+            p = np.zeros(nv, dtype=np.int64)
+            q = np.zeros(nv, dtype=np.int64)
+            rc = N.host().spk_order_nd_grid(s, s, 1, leaf, N.p64(xadj), N.p64(adj), N.p64(p), N.p64(q))
+            if rc < 0:
+                raise ValueError(N.host_error())
+            perm[off: off + nv] = p + off
+            invp[off: off + nv] = q + off
+            off += nv
+        order.rperm, order.rinvp = perm, invp
+        order.cperm, order.cinvp = perm.copy(), invp.copy()
+
+    return orderfunction
+
