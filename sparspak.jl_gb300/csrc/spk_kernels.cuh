@@ -312,35 +312,183 @@ __device__ __forceinline__ T pick_n(const T (&r)[N], int k) {
     return v;
 }
 
+// Correctly rounded reciprocal (the value of T(1) / x).
+__device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
+
 // Block LU by a whole CTA (blocks of 33..BlockMax columns; one CTA per
-// front).  The LU_THREADS threads form a G x G grid (G = BlockMax / 4);
-// thread (ty, tx) keeps rows [4ty, 4ty+4) x columns [4tx, 4tx+4) of the
-// block in registers, and a warp holds whole row groups.  For each column k, in piece [a, b):
-//   - the owners of column k publish its rows >= k, the owners of row k
-//     publish its columns >= a (shared memory, double-buffered);
-//   - every warp finds the pivot: the first strict maximum of |A(i,k)| over
-//     the piece's rows i in [k, b) (ggetrf!; a NaN never wins except on the
-//     diagonal);
-//   - a nonzero pivot off the diagonal: the pivot row is published and rows
-//     k and kp swap over columns >= a (ggetrf! inside the piece, _luswap! of
-//     its U rows; columns left of the piece never move);
-//   - rows after k: multiplier A(i,k) / pivot (ggetrf! scaling inside the
-//     piece, the L-panel trsm 'r','u','n','n' for the block's later rows;
-//     no scaling after a zero pivot), then the rank-1 update of rows and
-//     columns after k (ggetrf!, the U-panel trsm 'r','l','t','u' and the
-//     block-local Schur update).
-// One barrier per column, two when rows swap.  The column loop is unrolled
-// by the tile width, so that column / row k of a tile are fixed registers;
-// the small tile keeps the unrolled body small.  ipiv receives the local
-// pivot row within the piece; a zero pivot records the piece in info.
-template <typename T> struct LuThreads { static constexpr int value = (BlockMax<T>::value / 4) * (BlockMax<T>::value / 4); };
-template <typename T>
-__global__ void __launch_bounds__(LuThreads<T>::value) k_block_lu(T* fac, int* ipiv, int* info, Sched S, Launch L,
-                                                                   int step) {
-    constexpr int BM = BlockMax<T>::value, TR = 4, G = BM / TR, NT = G * G;
+// front).  Warp w holds the column group [4w, 4w+4) of the block, lane l the
+// rows [RPT l, RPT l + RPT) (RPT = BlockMax / 32), in registers.  The block
+// is factored one column group at a time:
+//   A. the group's owner warp factors its four columns in order, on its own
+//      (shuffles only): for column k in piece [a, b), the pivot is the first
+//      strict maximum of |A(i,k)| over the piece's rows i in [k, b)
+//      (ggetrf!; a NaN never wins except on the diagonal); a nonzero pivot
+//      off the diagonal swaps rows k and kp over the group's columns >= a
+//      (ggetrf! inside the piece; columns left of the piece never move); the
+//      rows after k are scaled by 1 / pivot (ggetrf! scaling, the L-panel
+//      trsm 'r','u','n','n' for the block's later rows; no scaling after a
+//      zero pivot) and the group's later columns get the rank-1 update.  The
+//      multipliers and pivots go to shared memory;
+//   B. every later warp applies, column by column in the same order, the
+//      swap (_luswap! of the U rows) and the rank-1 update (the U-panel trsm
+//      'r','l','t','u' and the block-local Schur update) to its columns, with
+//      row k taken from the owning lane by shuffles: the same operations in
+//      the same order as a column-by-column elimination; earlier warps apply
+//      the swaps to their columns of the same piece.
+// The owner of the next group does its part B first and then its part A, so
+// the next panel overlaps the other warps' updates; one barrier per group.
+// ipiv receives the local pivot row within the piece; a zero pivot records
+// the piece in info.
+template <typename T> struct LuThreads { static constexpr int value = (BlockMax<T>::value / 4) * 32; };
+
+template <typename T, int RPT>
+__device__ __forceinline__ T lu_pick(const T (&a)[RPT][4], int ii, int jj) {
+    T v = a[0][jj];
+#pragma unroll
+    for (int q = 1; q < RPT; ++q) v = (ii == q) ? a[q][jj] : v;
+    return v;
+}
+
+// Part A for the group of warp `g` (called by that warp only).
+template <typename T, int RPT>
+__device__ __forceinline__ void lu_group_factor(T (&a)[RPT][4], int g, int bw, const int* q0, int& pn, T* lb, int* skp,
+                                                T* spv, int* sa0, int* spiv, int* szero) {
     using Key = typename PivotKey<T>::type;
-    __shared__ __align__(16) T cbuf[2][BM];
-    __shared__ __align__(16) T rbuf[2][2][BM];
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, r0 = RPT * lane;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int k = 4 * g + j;
+        if (k >= bw) break;
+        while (q0[pn + 1] <= k) ++pn;
+        const int a0 = q0[pn], b = q0[pn + 1];
+        Key best = 0;
+        int brow = 0;
+#pragma unroll
+        for (int ii = 0; ii < RPT; ++ii) {   // rows in ascending order: ties keep the earlier row
+            const int R = r0 + ii;
+            const Key kv = PivotKey<T>::of(a[ii][j], R >= k && R < b, R == k);
+            if (ii == 0 || kv > best) { best = kv; brow = R; }
+        }
+        const int kp = warp_first_max_row(best, brow);
+        const int lk = k / RPT, ik = k % RPT, lp = kp / RPT, ip = kp % RPT;
+        const T pv = __shfl_sync(FULL, lu_pick(a, ip, j), lp);
+        const bool scale = pv != T(0);
+        if (scale && kp != k) {   // swap rows k and kp over the group's columns >= a0
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) {
+                const T vk = __shfl_sync(FULL, lu_pick(a, ik, jj), lk);
+                const T vp = __shfl_sync(FULL, lu_pick(a, ip, jj), lp);
+                if (4 * g + jj >= a0) {
+#pragma unroll
+                    for (int ii = 0; ii < RPT; ++ii) {
+                        if (lane == lk && ii == ik) a[ii][jj] = vp;
+                        if (lane == lp && ii == ip) a[ii][jj] = vk;
+                    }
+                }
+            }
+        }
+        const T rinv = scale ? rcp_rn(pv) : T(1);
+#pragma unroll
+        for (int ii = 0; ii < RPT; ++ii) {
+            const int R = r0 + ii;
+            if (R > k) {
+                if (scale) a[ii][j] *= rinv;
+                lb[j * (32 * RPT) + R] = a[ii][j];
+            }
+        }
+#pragma unroll
+        for (int jj = j + 1; jj < 4; ++jj) {   // rank-1 update of the group's later columns
+            const T u = __shfl_sync(FULL, lu_pick(a, ik, jj), lk);
+#pragma unroll
+            for (int ii = 0; ii < RPT; ++ii)
+                if (r0 + ii > k) a[ii][jj] -= a[ii][j] * u;
+        }
+        if (lane == 0) {
+            skp[j] = kp;
+            spv[j] = pv;
+            sa0[j] = a0;
+            spiv[k] = kp - a0;
+            if (!scale && k < *szero) *szero = k;
+        }
+    }
+}
+
+// Part B of group `g` for a later warp.
+template <typename T, int RPT>
+__device__ __forceinline__ void lu_group_update(T (&a)[RPT][4], int g, int bw, const T* lb, const int* skp, const T* spv) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, r0 = RPT * lane;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int k = 4 * g + j;
+        if (k >= bw) break;
+        const int kp = skp[j];
+        const T pv = spv[j];
+        const int lk = k / RPT, ik = k % RPT;
+        if (pv != T(0) && kp != k) {   // all columns here are after k, hence >= a0
+            const int lp = kp / RPT, ip = kp % RPT;
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) {
+                const T vk = __shfl_sync(FULL, lu_pick(a, ik, jj), lk);
+                const T vp = __shfl_sync(FULL, lu_pick(a, ip, jj), lp);
+#pragma unroll
+                for (int ii = 0; ii < RPT; ++ii) {
+                    if (lane == lk && ii == ik) a[ii][jj] = vp;
+                    if (lane == lp && ii == ip) a[ii][jj] = vk;
+                }
+            }
+        }
+        T l[RPT];
+#pragma unroll
+        for (int ii = 0; ii < RPT; ++ii) l[ii] = lb[j * (32 * RPT) + r0 + ii];
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+            const T u = __shfl_sync(FULL, lu_pick(a, ik, jj), lk);
+#pragma unroll
+            for (int ii = 0; ii < RPT; ++ii)
+                if (r0 + ii > k) a[ii][jj] -= l[ii] * u;
+        }
+    }
+}
+
+// The swaps of group `g` for an earlier warp: its columns of the same piece
+// (>= the piece's first column) hold L entries that move with the rows.
+template <typename T, int RPT>
+__device__ __forceinline__ void lu_group_swap_left(T (&a)[RPT][4], int g, int bw, const int* skp, const T* spv,
+                                                   const int* sa0) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int k = 4 * g + j;
+        if (k >= bw) break;
+        const int kp = skp[j], a0 = sa0[j];
+        if (spv[j] == T(0) || kp == k || 4 * w + 3 < a0) continue;   // uniform in the warp
+        const int lk = k / RPT, ik = k % RPT, lp = kp / RPT, ip = kp % RPT;
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+            const T vk = __shfl_sync(FULL, lu_pick(a, ik, jj), lk);
+            const T vp = __shfl_sync(FULL, lu_pick(a, ip, jj), lp);
+            if (4 * w + jj >= a0) {
+#pragma unroll
+                for (int ii = 0; ii < RPT; ++ii) {
+                    if (lane == lk && ii == ik) a[ii][jj] = vp;
+                    if (lane == lp && ii == ip) a[ii][jj] = vk;
+                }
+            }
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(LuThreads<T>::value, 1) k_block_lu(T* fac, int* ipiv, int* info, Sched S, Launch L,
+                                                                      int step) {
+    constexpr int BM = BlockMax<T>::value, RPT = BM / 32;
+    __shared__ __align__(16) T lbuf[2][4 * BM];   // the group's multipliers by column and row (by group parity)
+    __shared__ T s_pv[2][4];
+    __shared__ int s_kp[2][4], s_a0[2][4];
     __shared__ int q0[BM + 1];
     __shared__ int spiv[BM];
     __shared__ int szero;
@@ -350,133 +498,44 @@ __global__ void __launch_bounds__(LuThreads<T>::value) k_block_lu(T* fac, int* i
     const int blk = F.block0 + step;
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
     const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
-    const int tid = threadIdx.x, ty = tid / G, tx = tid % G, lane = tid & 31;
-    const int r0 = ty * TR, cl0 = tx * TR;
-    for (int k = tid; k <= np; k += NT) q0[k] = S.xsuper[p0 + k] - F.f - c0;
-    for (int i = tid; i < 2 * BM; i += NT) {
-        (&cbuf[0][0])[i] = T(0);
-        (&rbuf[0][0][0])[i] = T(0);
-        (&rbuf[0][0][0])[2 * BM + i] = T(0);
-    }
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const int r0 = RPT * lane, cl0 = 4 * w;
+    for (int k = tid; k <= np; k += blockDim.x) q0[k] = S.xsuper[p0 + k] - F.f - c0;
     if (tid == 0) szero = INT_MAX;
     T* blkp = fac + F.loff + (ll)c0 * F.ld + c0;   // block (i, j) at blkp[j * ld + i]
-    T a[TR][TR];
+    T a[RPT][4];
 #pragma unroll
-    for (int jj = 0; jj < TR; ++jj)
+    for (int jj = 0; jj < 4; ++jj)
 #pragma unroll
-        for (int ii = 0; ii < TR; ++ii) {
+        for (int ii = 0; ii < RPT; ++ii) {
             const int R = r0 + ii, C = cl0 + jj;
             a[ii][jj] = (R < bw && C < bw) ? blkp[(ll)C * F.ld + R] : T(0);
         }
     __syncthreads();
-    int pc = 0;
+    const int ng = cdiv(bw, 4);
+    int pn = 0;
+    if (w == 0) lu_group_factor<T, RPT>(a, 0, bw, q0, pn, lbuf[0], s_kp[0], s_pv[0], s_a0[0], spiv, &szero);
+    __syncthreads();
 #pragma unroll 1
-    for (int kb = 0; kb * TR < bw; ++kb) {
-#pragma unroll
-        for (int kk = 0; kk < TR; ++kk) {
-            const int k = kb * TR + kk;
-            if (k >= bw) break;
-            while (q0[pc + 1] <= k) ++pc;
-            const int a0 = q0[pc], b = q0[pc + 1];
-            T* cb = cbuf[k & 1];
-            T* rk = rbuf[k & 1][0];
-            T* rp = rbuf[k & 1][1];
-            if (tx == kb) {
-#pragma unroll
-                for (int ii = 0; ii < TR; ++ii) {
-                    const int R = r0 + ii;
-                    if (R >= k && R < bw) cb[R] = a[ii][kk];
-                }
-            }
-            if (ty == kb) {
-#pragma unroll
-                for (int jj = 0; jj < TR; ++jj) {
-                    const int C = cl0 + jj;
-                    if (C >= a0 && C < bw) rk[C] = a[kk][jj];
-                }
-            }
-            __syncthreads();
-            int kp;
-            {
-                const int i1 = k + lane, i2 = k + 32 + lane;
-                const Key k1 = PivotKey<T>::of(cb[min(i1, BM - 1)], i1 < b, i1 == k);
-                const Key k2 = PivotKey<T>::of(cb[min(i2, BM - 1)], i2 < b, false);
-                const bool second = k2 > k1;   // ties keep the earlier row
-                kp = warp_first_max_row(second ? k2 : k1, second ? i2 : i1);
-            }
-            const T pv = cb[kp];
-            if (tid == 0) {
-                spiv[k] = kp - a0;
-                if (pv == T(0) && k < szero) szero = k;
-            }
-            const bool swap = (pv != T(0)) && kp != k;
-            if (swap) {
-                const int tp = kp / TR, ip = kp % TR;
-                if (ty == tp) {
-#pragma unroll
-                    for (int ii = 0; ii < TR; ++ii)
-                        if (ii == ip) {
-#pragma unroll
-                            for (int jj = 0; jj < TR; ++jj) {
-                                const int C = cl0 + jj;
-                                if (C >= a0 && C < bw) rp[C] = a[ii][jj];
-                            }
-                        }
-                }
-                __syncthreads();
-                if (ty == kb) {
-#pragma unroll
-                    for (int jj = 0; jj < TR; ++jj) {
-                        const int C = cl0 + jj;
-                        if (C >= a0 && C < bw) a[kk][jj] = rp[C];
-                    }
-                }
-                if (ty == tp) {
-#pragma unroll
-                    for (int ii = 0; ii < TR; ++ii)
-                        if (ii == ip) {
-#pragma unroll
-                            for (int jj = 0; jj < TR; ++jj) {
-                                const int C = cl0 + jj;
-                                if (C >= a0 && C < bw) a[ii][jj] = rk[C];
-                            }
-                        }
-                }
-            }
-            if (r0 + TR - 1 > k) {
-                const T* ur = swap ? rp : rk;
-                const bool scale = pv != T(0);
-                const T rinv = scale ? T(1) / pv : T(1);
-                T l[TR], u[TR];
-#pragma unroll
-                for (int ii = 0; ii < TR; ++ii) {
-                    const int R = r0 + ii;
-                    const T v = (R == kp) ? cb[k] : cb[R];
-                    l[ii] = scale ? v * rinv : v;
-                }
-#pragma unroll
-                for (int jj = 0; jj < TR; ++jj) u[jj] = ur[cl0 + jj];
-#pragma unroll
-                for (int ii = 0; ii < TR; ++ii) {
-                    if (r0 + ii > k) {
-#pragma unroll
-                        for (int jj = 0; jj < TR; ++jj)
-                            if (cl0 + jj > k) a[ii][jj] -= l[ii] * u[jj];
-                        if (tx == kb) a[ii][kk] = l[ii];
-                    }
-                }
-            }
+    for (int g = 0; g < ng; ++g) {
+        const int par = g & 1;
+        if (w < g) lu_group_swap_left<T, RPT>(a, g, bw, s_kp[par], s_pv[par], s_a0[par]);
+        if (w > g && w < ng) {
+            lu_group_update<T, RPT>(a, g, bw, lbuf[par], s_kp[par], s_pv[par]);
+            if (w == g + 1)   // the next panel while the other warps update
+                lu_group_factor<T, RPT>(a, g + 1, bw, q0, pn, lbuf[par ^ 1], s_kp[par ^ 1], s_pv[par ^ 1],
+                                        s_a0[par ^ 1], spiv, &szero);
         }
+        __syncthreads();
     }
 #pragma unroll
-    for (int jj = 0; jj < TR; ++jj)
+    for (int jj = 0; jj < 4; ++jj)
 #pragma unroll
-        for (int ii = 0; ii < TR; ++ii) {
+        for (int ii = 0; ii < RPT; ++ii) {
             const int R = r0 + ii, C = cl0 + jj;
             if (R < bw && C < bw) blkp[(ll)C * F.ld + R] = a[ii][jj];
         }
-    __syncthreads();
-    for (int c = tid; c < bw; c += NT) ipiv[F.f + c0 + c] = spiv[c];
+    for (int c = tid; c < bw; c += blockDim.x) ipiv[F.f + c0 + c] = spiv[c];
     if (tid == 0 && szero != INT_MAX) {
         int p = 0;
         while (q0[p + 1] <= szero) ++p;
