@@ -623,14 +623,30 @@ __device__ __forceinline__ void block_gather_map(const int* ipiv_blk, const int*
     }
 }
 
-// sU and rd from the factored block (column-major at blkp, leading dimension ld).
+// Asynchronous element copy global -> shared (cp.async, 4 or 8 bytes); a
+// copy with valid = false writes zero and reads nothing.
+template <typename T>
+__device__ __forceinline__ void cp_elem(T* dst, const T* src, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if constexpr (sizeof(T) == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(valid ? 4 : 0) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(src), "r"(valid ? 8 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// sU and rd from the factored block (column-major at blkp, leading dimension
+// ld); the triangle is copied asynchronously (the caller waits with
+// cp_wait_all and a barrier before using it).
 template <typename T, int W>
 __device__ __forceinline__ void stage_upper(T* sU, T* rd, const T* blkp, ll ld, int bw) {
-    for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
-        const int j = e % W, k = e / W;
-        sU[sidx<T, W>(k, j)] = (j > k && j < bw) ? blkp[(ll)j * ld + k] : T(0);
+    for (int e = threadIdx.x; e < W * W; e += blockDim.x) {   // consecutive threads read down a column
+        const int k = e % W, j = e / W;
+        const bool v = j > k && j < bw;
+        cp_elem(&sU[sidx<T, W>(k, j)], v ? blkp + (ll)j * ld + k : blkp, v);
     }
     for (int k = threadIdx.x; k < W; k += blockDim.x) rd[k] = k < bw ? T(1) / blkp[(ll)k * ld + k] : T(0);
+    cp_wait_all();
 }
 
 // sL from the factored block with the rows of each piece, in the columns
@@ -643,10 +659,10 @@ template <typename T, int W>
 __device__ __forceinline__ void stage_lower(T* sL, const T* blkp, ll ld, int bw, const int* gmap, const int* pa) {
     for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
         const int i = e % W, k = e / W;
-        T v = T(0);
-        if (i > k && i < bw) v = blkp[(ll)k * ld + (k < pa[i] ? gmap[i] : i)];
-        sL[sidx<T, W>(k, i)] = v;
+        const bool v = i > k && i < bw;
+        cp_elem(&sL[sidx<T, W>(k, i)], v ? blkp + (ll)k * ld + (k < pa[i] ? gmap[i] : i) : blkp, v);
     }
+    cp_wait_all();
 }
 
 // Packed copy of one panel line for the tensor-core updates (FP32 fronts
@@ -700,17 +716,17 @@ __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, Sc
     const int nL = cdiv(F.ld - c1, 64), nUa = cdiv(F.nf - c1, 64);
     const T* blkp = fac + F.loff + (ll)c0 * F.ld + c0;
     if (tile < nL) {
-        stage_upper<T, W>(sT, rd, blkp, F.ld, bw);
-        __syncthreads();
         const int r = c1 + tile * 64 + line;
         const bool ok = r < F.ld;
         T* xp = fac + F.loff + (ll)c0 * F.ld + r;   // row r, block column j at xp[j * ld]
         T x[CQ];
 #pragma unroll
-        for (int jj = 0; jj < CQ; ++jj) {
+        for (int jj = 0; jj < CQ; ++jj) {   // in flight while the triangle is staged
             const int j = q * CQ + jj;
             x[jj] = (ok && j < bw) ? xp[(ll)j * F.ld] : T(0);
         }
+        stage_upper<T, W>(sT, rd, blkp, F.ld, bw);
+        __syncthreads();
         sweep_rows<T, W>(x, sT, rd, bw);
 #pragma unroll
         for (int jj = 0; jj < CQ; ++jj) {
@@ -731,8 +747,6 @@ __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, Sc
         __syncthreads();
         block_gather_map(ipiv + F.f + c0, q0, np, gmap, pa);
         __syncthreads();
-        stage_lower<T, W>(sT, blkp, F.ld, bw, gmap, pa);
-        __syncthreads();
         const bool inner = tile < nL + nUa;
         const int col = inner ? c1 + (tile - nL) * 64 + line : (tile - nL - nUa) * 64 + line;
         const bool ok = inner ? col < F.nf : col < F.m;
@@ -741,10 +755,12 @@ __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, Sc
         const ll stride = inner ? 1 : (ll)F.m;
         T y[CQ];
 #pragma unroll
-        for (int ii = 0; ii < CQ; ++ii) {
+        for (int ii = 0; ii < CQ; ++ii) {   // in flight while the triangle is staged
             const int R = q * CQ + ii;
             y[ii] = (ok && R < bw) ? cp[(ll)gmap[R] * stride] : T(0);
         }
+        stage_lower<T, W>(sT, blkp, F.ld, bw, gmap, pa);
+        __syncthreads();
         sweep_cols<T, W>(y, sT, bw);
 #pragma unroll
         for (int ii = 0; ii < CQ; ++ii) {
