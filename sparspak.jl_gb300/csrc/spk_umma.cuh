@@ -1,20 +1,14 @@
 // Fifth-generation tensor cores (tcgen05) for the FP32 rank updates of the
-// factorisation: one CTA forms a 128 x 128 FP32 tile C = A * B in tensor
-// memory with three TF32 products per K step,
+// factorisation: a 128 x 128 FP32 tile C = A * B in tensor memory with three
+// TF32 products per K step,
 //     A * B ~= Ahi * Bhi + Ahi * Blo + Alo * Bhi,
 // Ahi = tf32(A) (round to nearest), Alo = tf32(A - Ahi), which carries the
 // product to about FP32 accuracy (the dropped Alo * Blo term is ~2^-22
-// relative).
-//
-// Operands are staged by the CTA's threads (global -> registers -> split ->
-// shared memory) in the canonical K-major layout without swizzle: 8-row x
-// 16-byte core matrices, K-adjacent core matrices 128 bytes apart and
-// 8-row groups SBO = KCH * 32 bytes apart, KCH K values per stage.  Two
-// stages (64 KB), so that two or three CTAs share an SM and one CTA's loads
-// and epilogue overlap another's tensor-core work; the
-// next chunk's global loads are in flight while the tensor core works on the
-// current one.  One thread issues the MMAs and commits them to the stage's
-// mbarrier; every wait is bounded and reports a timeout through `err`.
+// relative).  Operands arrive pre-split in the canonical K-major layout
+// without swizzle (8-row x 16-byte core matrices, K-adjacent core matrices
+// 128 bytes apart, 8-row groups SBO = KCH * 32 bytes apart), written by the
+// panel kernel; this header holds the descriptors, the MMA, TMEM and mbarrier
+// primitives, and the shared-memory plan of the packed pipeline.
 #pragma once
 #include <cstdint>
 
@@ -24,10 +18,7 @@ namespace umma {
 constexpr int TM = 128, TN = 128, KCH = 16;           // tile rows, tile columns, K per stage
 constexpr int OPB = TM * KCH * 4;                     // bytes of one operand part (8 KB)
 constexpr int SBO = KCH * 32;                         // bytes between 8-row groups
-constexpr int NG = TM * (KCH / 4) / 256;              // groups of 4 K values per thread and operand
 constexpr int STAGE = 4 * OPB;                        // Ahi, Alo, Bhi, Blo
-constexpr int NSTAGE = 2;
-constexpr int SMEM = NSTAGE * STAGE + 2048;           // + alignment slack, barriers, TMEM address
 constexpr unsigned WAIT_LIMIT = 1u << 20;             // polls of an mbarrier before giving up
 
 __device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -77,13 +68,6 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait for the completion of phase `parity` of `bar`; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (unsigned it = 0; it < WAIT_LIMIT; ++it)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
@@ -112,148 +96,6 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-// One operand of a 128 x KCH chunk: element (i, k), i < 128 (tile row or
-// column), k < KCH.  Memory: at p[k * ld + i] (i contiguous) or, with
-// kcontig, at p[i * ld + k]; rows i >= n and k >= kc read as zero.  Each
-// thread carries NG groups of 4 consecutive k.
-struct Operand {
-    const float* p;
-    long long ld;
-    int n;
-    bool kcontig;
-};
-
-struct Prefetch {
-    float v[NG][4];
-};
-
-__device__ __forceinline__ void load_chunk(const Operand& op, int k0, int kc, Prefetch& f) {
-#pragma unroll
-    for (int t = 0; t < NG; ++t) {
-        const int g = threadIdx.x + 256 * t, i = g & 127, kq = g >> 7;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int k = kq * 4 + q;
-            float x = 0.0f;
-            if (i < op.n && k < kc) x = op.kcontig ? op.p[(long long)i * op.ld + k0 + k] : op.p[(long long)(k0 + k) * op.ld + i];
-            f.v[t][q] = x;
-        }
-    }
-}
-
-// Split into TF32 hi / lo and store in the canonical layout:
-// byte offset (i / 8) * SBO + (k / 4) * 128 + (i % 8) * 16 + (k % 4) * 4.
-__device__ __forceinline__ void store_chunk(const Prefetch& f, unsigned char* hi, unsigned char* lo) {
-#pragma unroll
-    for (int t = 0; t < NG; ++t) {
-        const int g = threadIdx.x + 256 * t, i = g & 127, kq = g >> 7;
-        const uint32_t off = (uint32_t)((i >> 3) * SBO + kq * 128 + (i & 7) * 16);
-        uint32_t h[4], l[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            h[q] = tf32_rna(f.v[t][q]);
-            l[q] = tf32_rna(f.v[t][q] - __uint_as_float(h[q]));
-        }
-        *reinterpret_cast<uint4*>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
-        *reinterpret_cast<uint4*>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
-    }
-}
-
-// Shared state of a CTA using the tile product (256 threads).
-struct Ctx {
-    unsigned char* stage;   // NSTAGE * STAGE bytes, 1024-aligned
-    uint64_t* bar;          // NSTAGE mbarriers
-    uint32_t* tmem_slot;    // TMEM base address written by tcgen05.alloc
-};
-
-__device__ __forceinline__ Ctx ctx_of(unsigned char* smem_raw) {
-    unsigned char* base =
-        reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-    Ctx c;
-    c.stage = base;
-    c.bar = reinterpret_cast<uint64_t*>(base + NSTAGE * STAGE);
-    c.tmem_slot = reinterpret_cast<uint32_t*>(base + NSTAGE * STAGE + 64);
-    return c;
-}
-
-// Start of a CTA: barriers and 128 TMEM columns (warp 0).  Returns the TMEM base.
-__device__ __forceinline__ uint32_t begin(const Ctx& c) {
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < NSTAGE; ++s) mbar_init(&c.bar[s], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    if (threadIdx.x < 32) tmem_alloc(c.tmem_slot, TN);
-    fence_before();
-    __syncthreads();
-    fence_after();
-    return *c.tmem_slot;
-}
-
-// End of a CTA: all TMEM reads done, warp 0 frees the columns.
-__device__ __forceinline__ void end(const Ctx& c, uint32_t tmem) {
-    fence_before();
-    __syncthreads();
-    fence_after();
-    if (threadIdx.x < 32) tmem_dealloc(tmem, TN);
-}
-
-// C (128 x 128, FP32, in TMEM at `tmem`) = sum over k < K of A(i, k) B(k, j).
-// Called by all 256 threads; `uses` counts the tiles this CTA computed
-// before (mbarrier phases continue across tiles).  Returns false when a wait
-// timed out (the tile is then incomplete; *err is set).
-__device__ __forceinline__ bool tile_product(const Ctx& c, uint32_t tmem, const Operand& A, const Operand& B, int K,
-                                             unsigned& uses, int* err) {
-    constexpr uint32_t IDESC = idesc_tf32(TM, TN);
-    const int nch = (K + KCH - 1) / KCH;
-    bool ok = true;
-    Prefetch fa, fb;
-    if (nch > 0) {
-        load_chunk(A, 0, min(KCH, K), fa);
-        load_chunk(B, 0, min(KCH, K), fb);
-    }
-    for (int ch = 0; ch < nch; ++ch) {
-        const unsigned u = uses + ch;          // running use count over both stages
-        const int s = u & 1;
-        unsigned char* st = c.stage + s * STAGE;
-        if (u >= 2 && !mbar_wait(&c.bar[s], ((u - 2) >> 1) & 1)) ok = false;   // stage free
-        store_chunk(fa, st, st + OPB);
-        store_chunk(fb, st + 2 * OPB, st + 3 * OPB);
-        fence_proxy_async();
-        fence_before();
-        __syncthreads();
-        if (ch + 1 < nch) {
-            const int k0 = (ch + 1) * KCH, kc = min(KCH, K - k0);
-            load_chunk(A, k0, kc, fa);
-            load_chunk(B, k0, kc, fb);
-        }
-        if (threadIdx.x == 0) {
-            fence_after();
-            const uint32_t a_hi = saddr(st), a_lo = a_hi + OPB, b_hi = a_hi + 2 * OPB, b_lo = a_hi + 3 * OPB;
-            const int ksteps = min(KCH, K - ch * KCH);
-#pragma unroll
-            for (int kk = 0; kk < KCH / 8; ++kk) {
-                if (kk * 8 >= ksteps) break;
-                const uint32_t o = kk * 256;   // two K-adjacent core matrices per step
-                const uint64_t dah = desc_kmajor(a_hi + o, 128, SBO), dal = desc_kmajor(a_lo + o, 128, SBO);
-                const uint64_t dbh = desc_kmajor(b_hi + o, 128, SBO), dbl = desc_kmajor(b_lo + o, 128, SBO);
-                mma_tf32(tmem, dah, dbh, IDESC, (ch > 0 || kk > 0) ? 1u : 0u);
-                mma_tf32(tmem, dah, dbl, IDESC, 1u);
-                mma_tf32(tmem, dal, dbh, IDESC, 1u);
-            }
-            commit(&c.bar[s]);
-        }
-    }
-    if (nch > 0) {
-        const unsigned u = uses + nch - 1;
-        if (!mbar_wait(&c.bar[u & 1], (u >> 1) & 1)) ok = false;
-        // the other stage's last use also completed (tensor-core work completes in order)
-    }
-    uses += nch;
-    fence_after();
-    if (!ok && err) atomicExch(err, 1);
-    return ok;
 }
 
 // ---------------------------------------------------------------------------
