@@ -931,29 +931,24 @@ __global__ void __launch_bounds__(256) k_block_trail(T* fac, Sched S, Launch L, 
         __syncthreads();
     }
     const int tx = tid & 15, ty = tid >> 4;
-    if (isL) {
+    // the 16 entries are loaded before any is stored (distinct addresses the
+    // compiler cannot prove distinct)
+    T old[4][4];
+    ll addr[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
-            int c = ty + 16 * b;
-            if (c >= nc) continue;
-#pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                int r = tx + 16 * a;
-                if (r < nr) fac[F.loff + (ll)(col0 + c) * F.ld + r0 + r] -= acc[a][b];
-            }
+            const int r = isL ? tx + 16 * a : ty + 16 * a, c = isL ? ty + 16 * b : tx + 16 * b;
+            const bool in = r < nr && c < nc;
+            addr[a][b] = !in ? -1 : isL ? F.loff + (ll)(col0 + c) * F.ld + r0 + r : F.uoff + (ll)(r0 + r) * F.m + col0 + c;
+            old[a][b] = in ? fac[addr[a][b]] : T(0);
         }
-    } else {
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            int r = ty + 16 * a;
-            if (r >= nr) continue;
+    for (int a = 0; a < 4; ++a)
 #pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                int c = tx + 16 * b;
-                if (c < nc) fac[F.uoff + (ll)(r0 + r) * F.m + col0 + c] -= acc[a][b];
-            }
-        }
-    }
+        for (int b = 0; b < 4; ++b)
+            if (addr[a][b] >= 0) fac[addr[a][b]] = old[a][b] - acc[a][b];
 }
 
 // Subtract C(r, c) of a front's Schur complement from its ancestor: the
@@ -1225,15 +1220,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
                     float v[32];
                     umma::tmem_ld32(taddr + h * 32, v);
                     if (rok) {
-                        if (cL) {
+                        // all 32 loads before any store: the compiler cannot tell that the
+                        // entries are distinct, and would otherwise serialise the round trips
+                        float* dst = cL ? fac + F.loff + (ll)(col0 + h * 32) * F.ld + row
+                                        : fac + F.uoff + (ll)row * F.m + col0 + h * 32;
+                        const ll step_j = cL ? (ll)F.ld : 1;
 #pragma unroll
-                            for (int j = 0; j < 32; ++j)
-                                if (h * 32 + j < ncol) fac[F.loff + (ll)(col0 + h * 32 + j) * F.ld + row] -= v[j];
-                        } else {
-                            float* dst = fac + F.uoff + (ll)row * F.m + col0 + h * 32;
+                        for (int half = 0; half < 2; ++half) {   // 16 loads in flight, no spills
+                            float old[16];
 #pragma unroll
-                            for (int j = 0; j < 32; ++j)
-                                if (h * 32 + j < ncol) dst[j] -= v[j];
+                            for (int j = 0; j < 16; ++j) {
+                                const int jj = 16 * half + j;
+                                old[j] = (h * 32 + jj < ncol) ? dst[(ll)jj * step_j] : 0.0f;
+                            }
+#pragma unroll
+                            for (int j = 0; j < 16; ++j) {
+                                const int jj = 16 * half + j;
+                                if (h * 32 + jj < ncol) dst[(ll)jj * step_j] = old[j] - v[jj];
+                            }
                         }
                     }
                 }
@@ -1245,20 +1249,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
                     float v[32];
                     umma::tmem_ld32(taddr + h * 32, v);
                     if (r < F.m) {
+                        // positions of 16 entries first (their rel[] loads in flight
+                        // together), then the 16 scatter-adds
 #pragma unroll
-                        for (int j = 0; j < 32; ++j) {
-                            const int c = c0 + h * 32 + j;
-                            if (c >= F.m) continue;
-                            if (r >= c) {   // L entry of the front of R_F[c]
-                                const ScatterRow& Cc = tab[0][h * 32 + j];
-                                const int pr = S.rel[Cc.rel0 + r];
-                                if (pr >= 0 && Cc.pos >= 0) atomicAdd(&fac[Cc.loff + (ll)Cc.pos * Cc.ld + pr], -v[j]);
-                            } else {        // entry of the front of R_F[r]
-                                const int pc = S.rel[R.rel0 + c];
-                                if (pc >= 0 && R.pos >= 0) {
+                        for (int half = 0; half < 2; ++half) {
+                            int pos[16];
+#pragma unroll
+                            for (int j = 0; j < 16; ++j) {
+                                const int jj = 16 * half + j, c = c0 + h * 32 + jj;
+                                pos[j] = -1;
+                                if (c < F.m) pos[j] = r >= c ? S.rel[tab[0][h * 32 + jj].rel0 + r] : S.rel[R.rel0 + c];
+                            }
+#pragma unroll
+                            for (int j = 0; j < 16; ++j) {
+                                const int jj = 16 * half + j, c = c0 + h * 32 + jj;
+                                if (c >= F.m || pos[j] < 0) continue;
+                                if (r >= c) {   // L entry of the front of R_F[c]
+                                    const ScatterRow& Cc = tab[0][h * 32 + jj];
+                                    if (Cc.pos >= 0) atomicAdd(&fac[Cc.loff + (ll)Cc.pos * Cc.ld + pos[j]], -v[jj]);
+                                } else if (R.pos >= 0) {   // entry of the front of R_F[r]
+                                    const int pc = pos[j];
                                     const ll addr = pc < R.nf ? R.loff + (ll)pc * R.ld + R.pos
                                                               : R.uoff + (ll)R.pos * R.m + (pc - R.nf);
-                                    atomicAdd(&fac[addr], -v[j]);
+                                    atomicAdd(&fac[addr], -v[jj]);
                                 }
                             }
                         }
