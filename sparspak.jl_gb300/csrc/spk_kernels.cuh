@@ -951,20 +951,30 @@ __global__ void __launch_bounds__(256) k_block_trail(T* fac, Sched S, Launch L, 
             if (addr[a][b] >= 0) fac[addr[a][b]] = old[a][b] - acc[a][b];
 }
 
-// Subtract C(r, c) of a front's Schur complement from its ancestor: the
-// entry belongs to the front of R_F[min(r, c)], whose run gives the positions.
+// Scatter target of one row or column x of a Schur complement tile: the
+// front G of R_F[x] (its run), and x's position in G.
+struct ScatterRow {
+    ll rel0;     // offset in rel[] of R_F[0] for the run of this row / column
+    ll loff, uoff;
+    int ld, nf, m, pos;
+};
+
 template <typename T>
-__device__ __forceinline__ void schur_scatter(T* fac, const Sched& S, const int* runid, int r, int c, T v) {
-    const int x = min(r, c);
-    const int g = runid[x];
-    const DFront G = S.fronts[S.run_tgt[g]];
-    const ll base = S.run_rel[g] - S.run_start[g];
-    const int pr = S.rel[base + r], pc = S.rel[base + c];
-    if (pr < 0 || pc < 0) return;     // exact zero: (r, c) is padding of F only
-    ll addr;
-    if (r >= c || pc < G.nf) addr = G.loff + (ll)pc * G.ld + pr;
-    else addr = G.uoff + (ll)pr * G.m + (pc - G.nf);
-    atomicAdd(&fac[addr], -v);
+__device__ __forceinline__ ScatterRow scatter_row(const Sched& S, const DFront& F, int x) {
+    ScatterRow e{};
+    e.pos = -1;
+    if (x < F.m) {
+        const int g = S.runid[F.runid_off + x];
+        const DFront G = S.fronts[S.run_tgt[g]];
+        e.rel0 = S.run_rel[g] - S.run_start[g];
+        e.loff = G.loff;
+        e.uoff = G.uoff;
+        e.ld = G.ld;
+        e.nf = G.nf;
+        e.m = G.m;
+        e.pos = S.rel[e.rel0 + x];
+    }
+    return e;
 }
 
 // Schur complement of every front in the launch: C = L21 * U12 (m x m,
@@ -976,6 +986,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_schur(T* fac, Sched S, Launch L) {
     __shared__ T sA[KC * TT];
     __shared__ T sB[KC * TT];
+    __shared__ ScatterRow tab[2][TT];   // [0] tile columns, [1] tile rows
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
@@ -983,6 +994,7 @@ __global__ void __launch_bounds__(256) k_schur(T* fac, Sched S, Launch L) {
     const int nt = cdiv(F.m, TT);
     const int r0 = (tile % nt) * TT, c0 = (tile / nt) * TT;
     const int nr = min(TT, F.m - r0), nc = min(TT, F.m - c0);
+    if (tid < 2 * TT) tab[tid / TT][tid % TT] = scatter_row<T>(S, F, (tid < TT ? c0 : r0) + tid % TT);   // published by the first barrier below
     T acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -999,18 +1011,36 @@ __global__ void __launch_bounds__(256) k_schur(T* fac, Sched S, Launch L) {
         mma_tile<T, true>(sA, sB, kc, acc);
         __syncthreads();
     }
+    // scatter through the tile's target tables: one rel[] load per entry,
+    // the 16 loads of a thread in flight together, then its 16 scatter-adds
     const int tx = tid & 15, ty = tid >> 4;
-    const int* runid = S.runid + F.runid_off;
+    int pos[4][4];
 #pragma unroll
-    for (int b = 0; b < 4; ++b) {
-        const int c = c0 + ty + 16 * b;
-        if (c - c0 >= nc) continue;
+    for (int b = 0; b < 4; ++b)
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
-            const int r = r0 + tx + 16 * a;
-            if (r - r0 < nr) schur_scatter(fac, S, runid, r, c, acc[a][b]);
+            const int ic = ty + 16 * b, ir = tx + 16 * a, c = c0 + ic, r = r0 + ir;
+            pos[a][b] = -1;
+            if (ic < nc && ir < nr) pos[a][b] = r >= c ? S.rel[tab[0][ic].rel0 + r] : S.rel[tab[1][ir].rel0 + c];
         }
-    }
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int ic = ty + 16 * b, ir = tx + 16 * a, c = c0 + ic, r = r0 + ir;
+            const int p = pos[a][b];
+            if (p < 0) continue;
+            if (r >= c) {   // L entry of the front of R_F[c]
+                const ScatterRow& Cc = tab[0][ic];
+                if (Cc.pos >= 0) atomicAdd(&fac[Cc.loff + (ll)Cc.pos * Cc.ld + p], -acc[a][b]);
+            } else {        // entry of the front of R_F[r]
+                const ScatterRow& R = tab[1][ir];
+                if (R.pos >= 0) {
+                    const ll addr = p < R.nf ? R.loff + (ll)p * R.ld + R.pos : R.uoff + (ll)R.pos * R.m + (p - R.nf);
+                    atomicAdd(&fac[addr], -acc[a][b]);
+                }
+            }
+        }
 }
 
 // ---------------------------------------------------------------------------
@@ -1030,11 +1060,6 @@ __global__ void __launch_bounds__(256) k_schur(T* fac, Sched S, Launch L) {
 // (from warp 4; warp w reads TMEM lanes 32 (w % 4).. and the 32 accumulator
 // columns 32 ((w - 4) / 4)..) drain the accumulator.
 // ---------------------------------------------------------------------------
-struct ScatterRow {
-    ll rel0;     // offset in rel[] of R_F[0] for the run of this row / column
-    ll loff, uoff;
-    int ld, nf, m, pos;
-};
 
 constexpr int TC_TRAIL = 0, TC_SCHUR = 1;
 constexpr int TC_EPI = 16, TC_THREADS = 32 * (4 + TC_EPI);
@@ -1184,23 +1209,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
             const DFront& F = T.F;
             if (MODE == TC_SCHUR) {
                 asm volatile("bar.sync 1, %0;" ::"n"(32 * TC_EPI) : "memory");   // previous tile's scatter done
-                const int* runid = S.runid + F.runid_off;
                 if (et < 2 * umma::TM) {
                     const int side = et / umma::TM, x = (side == 0 ? T.ct : T.rt) * umma::TM + (et % umma::TM);
-                    ScatterRow e{};
-                    e.pos = -1;
-                    if (x < F.m) {
-                        const int g = runid[x];
-                        const DFront G = S.fronts[S.run_tgt[g]];
-                        e.rel0 = S.run_rel[g] - S.run_start[g];
-                        e.loff = G.loff;
-                        e.uoff = G.uoff;
-                        e.ld = G.ld;
-                        e.nf = G.nf;
-                        e.m = G.m;
-                        e.pos = S.rel[e.rel0 + x];
-                    }
-                    tab[side][et % umma::TM] = e;
+                    tab[side][et % umma::TM] = scatter_row<float>(S, F, x);
                 }
                 asm volatile("bar.sync 1, %0;" ::"n"(32 * TC_EPI) : "memory");
             }
