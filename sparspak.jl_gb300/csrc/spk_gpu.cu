@@ -656,7 +656,7 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
                 tsch_tc[k] = cdiv(F.m, spk::umma::TM) * cdiv(F.m, spk::umma::TN);
                 tsch[k] = 0;
             }
-            tbu[k] = F.m > 0 ? cdiv(F.nf, spk::TS / 32) : 0;
+            tbu[k] = F.m > 0 ? cdiv(F.nf, spk::U12_ROWS) * cdiv(F.m, spk::U12_COLS) : 0;
             fs[k] = 2.0 * (double)F.m * F.m * F.nf;
             ws[k] = 2.0 * (double)F.m * F.nf + 2.0 * (double)F.m * F.m;
             fu[k] = 2.0 * (double)F.m * F.nf;
@@ -811,6 +811,27 @@ static int ensure_rhs(spk_handle* h, i64 nrhs) {
 // ---------------------------------------------------------------------------
 // numeric phases
 // ---------------------------------------------------------------------------
+// Launch a solve kernel with programmatic stream serialisation: it may start
+// while its predecessor drains and waits for it with griddepcontrol.wait
+// after prefetching the factor data it needs.  The first chained kernel of a solve follows the
+// plain launch of k_permute, which starts only after the factorisation has
+// completed, so the factor data read before the wait is final.
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_chained(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t st,
+                                  Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, ((KArgs)args)...);
+}
+
 template <typename T>
 static int factor_launches(spk_handle* h) {
     constexpr int BM = spk::BlockMax<T>::value;
@@ -889,6 +910,7 @@ static int factor_launches(spk_handle* h) {
     return SPK_OK;
 }
 
+
 template <typename T>
 static int run_factor(spk_handle* h) {
     static const int init[2] = {INT_MAX, 0};
@@ -912,20 +934,21 @@ static int run_solve_permuted(spk_handle* h, int nrhs, bool transpose) {
             for (size_t t = 0; t < P.fwd.size(); ++t)
                 if (P.fwd[t].tiles > 0) {
                     LaunchScope ls(h, SPK_K_FWD, P.fwd[t].flops * nrhs, P.fwd[t].words * sizeof(T));
-                    spk::k_tfwd<T><<<P.fwd[t].tiles, spk::TS, 0, h->stream>>>(fac, inv, b, y, n, nrhs, S,
-                                                                               launch_of(PL, P.fwd[t]), (int)t);
+                    CU(h, launch_chained(spk::k_tfwd<T>, P.fwd[t].tiles, spk::TS, 0, h->stream, fac, inv, b, y, n, nrhs, S,
+                                         launch_of(PL, P.fwd[t]), (int)t));
                 }
         for (size_t l = PL.levels.size(); l-- > 0;) {
             const LevelPlan& P = PL.levels[l];
             if (P.bwdu.tiles > 0) {
                 LaunchScope ls(h, SPK_K_BWD, P.bwdu.flops * nrhs, P.bwdu.words * sizeof(T));
-                spk::k_tbwd_l21<T><<<P.bwdu.tiles, spk::TS, 0, h->stream>>>(fac, y, x, n, nrhs, S, launch_of(PL, P.bwdu));
+                CU(h, launch_chained(spk::k_tbwd_l21<T>, P.bwdu.tiles, 256, 0, h->stream, fac, y, x, n, nrhs, S,
+                                     launch_of(PL, P.bwdu)));
             }
             for (size_t t = 0; t < P.bwd.size(); ++t)
                 if (P.bwd[t].tiles > 0) {
                     LaunchScope ls(h, SPK_K_BWD, P.bwd[t].flops * nrhs, P.bwd[t].words * sizeof(T));
-                    spk::k_tbwd<T><<<P.bwd[t].tiles, spk::TS, 0, h->stream>>>(fac, inv, y, x, n, nrhs, S,
-                                                                               launch_of(PL, P.bwd[t]), (int)t);
+                    CU(h, launch_chained(spk::k_tbwd<T>, P.bwd[t].tiles, spk::TS, 0, h->stream, fac, inv, y, x, n, nrhs, S,
+                                         launch_of(PL, P.bwd[t]), (int)t));
                 }
         }
         CU(h, cudaGetLastError());
@@ -935,20 +958,21 @@ static int run_solve_permuted(spk_handle* h, int nrhs, bool transpose) {
         for (size_t t = 0; t < P.fwd.size(); ++t)
             if (P.fwd[t].tiles > 0) {
                 LaunchScope ls(h, SPK_K_FWD, P.fwd[t].flops * nrhs, P.fwd[t].words * sizeof(T));
-                spk::k_fwd<T><<<P.fwd[t].tiles, spk::TS, 0, h->stream>>>(fac, inv, b, y, n, nrhs, S,
-                                                                          launch_of(PL, P.fwd[t]), (int)t);
+                CU(h, launch_chained(spk::k_fwd<T>, P.fwd[t].tiles, spk::TS, 0, h->stream, fac, inv, b, y, n, nrhs, S,
+                                     launch_of(PL, P.fwd[t]), (int)t));
             }
     for (size_t l = PL.levels.size(); l-- > 0;) {
         const LevelPlan& P = PL.levels[l];
         if (P.bwdu.tiles > 0) {
             LaunchScope ls(h, SPK_K_BWD, P.bwdu.flops * nrhs, P.bwdu.words * sizeof(T));
-            spk::k_bwd_u12<T><<<P.bwdu.tiles, spk::TS, 0, h->stream>>>(fac, y, x, n, nrhs, S, launch_of(PL, P.bwdu));
+            CU(h, launch_chained(spk::k_bwd_u12<T>, P.bwdu.tiles, 256, 0, h->stream, fac, y, x, n, nrhs, S,
+                                 launch_of(PL, P.bwdu)));
         }
         for (size_t t = 0; t < P.bwd.size(); ++t)
             if (P.bwd[t].tiles > 0) {
                 LaunchScope ls(h, SPK_K_BWD, P.bwd[t].flops * nrhs, P.bwd[t].words * sizeof(T));
-                spk::k_bwd<T><<<P.bwd[t].tiles, spk::TS, 0, h->stream>>>(fac, inv, y, x, n, nrhs, S,
-                                                                          launch_of(PL, P.bwd[t]), (int)t);
+                CU(h, launch_chained(spk::k_bwd<T>, P.bwd[t].tiles, spk::TS, 0, h->stream, fac, inv, y, x, n, nrhs, S,
+                                     launch_of(PL, P.bwd[t]), (int)t));
             }
     }
     CU(h, cudaGetLastError());

@@ -94,6 +94,15 @@ __device__ __forceinline__ void locate(const Launch& L, int bid, int& fid, int& 
 
 __host__ __device__ __forceinline__ int cdiv(int a, int b) { return (a + b - 1) / b; }
 
+// Programmatic dependent launch, for kernels that form a dependent chain:
+// griddep_launch lets the next kernel of the stream launch once every CTA of
+// this one has started; griddep_wait blocks until the previous kernel has
+// completed and its writes are visible (immediately when there is no such
+// dependency).  A kernel issues the loads that do not depend on its
+// predecessor before waiting.
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 template <typename T> __device__ __forceinline__ T tabs(T x) { return x < T(0) ? -x : x; }
 
 // Widest supernode handled.  The reference's splitting rule
@@ -1319,9 +1328,11 @@ template <typename T>
 __global__ void __launch_bounds__(TS) k_fwd(const T* fac, const T* inv2, T* b, T* y, int n, int nrhs, Sched S,
                                             Launch L, int step) {
     constexpr int BM = BlockMax<T>::value;
+    __shared__ T sm[BM * SC];   // Minv[:, chunk], sm[k * SC + j]
     __shared__ T sb[BM * MAXRHS];
     __shared__ T sp[4 * SC * MAXRHS];
     __shared__ T sy[SC * MAXRHS];
+    griddep_launch();
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
@@ -1331,24 +1342,40 @@ __global__ void __launch_bounds__(TS) k_fwd(const T* fac, const T* inv2, T* b, T
     const int j0 = cc * SC, nj = min(SC, bw - j0);
     const T* Mi = inv2 + S.blk_inv2[blk];
     const int tid = threadIdx.x;
+    // Factor data (complete before the solve) first: the chunk of Minv into
+    // shared memory, this thread's row of L[:, chunk] into registers.
+    for (int e = tid; e < bw * SC; e += TS) {
+        const int k = e / SC, j = e % SC;
+        cp_elem(&sm[e], Mi + (ll)k * bw + j0 + min(j, nj - 1), j < nj);
+    }
+    const int row = c1 + rt * TS + tid;
+    const bool has_row = row < F.ld;
+    T lv[SC];
+    int grow = 0;
+    {
+        const T* lcol = fac + F.loff + (ll)(c0 + j0) * F.ld + (has_row ? row : c1);
+#pragma unroll
+        for (int j = 0; j < SC; ++j) lv[j] = (has_row && j < nj) ? lcol[(ll)j * F.ld] : T(0);
+        if (has_row) grow = row < F.nf ? F.f + row : S.rows[F.rows_off + row - F.nf];
+    }
+    griddep_wait();
     for (int e = tid; e < bw * nrhs; e += TS) {
         int k = e % bw, r = e / bw;
         sb[r * BM + k] = b[(ll)r * n + F.f + c0 + k];
     }
+    cp_wait_all();
     __syncthreads();
     {   // y_chunk = Minv[j0:j0+nj, :] b_B : 32 columns x 4 partial sums over k
         const int j = tid & 31, kq = tid >> 5;
         T acc[MAXRHS];
 #pragma unroll
         for (int r = 0; r < MAXRHS; ++r) acc[r] = T(0);
-        if (j < nj) {
 #pragma unroll 8
-            for (int k = kq; k < bw; k += 4) {
-                const T mk = Mi[(ll)k * bw + j0 + j];
+        for (int k = kq; k < bw; k += 4) {
+            const T mk = sm[k * SC + j];
 #pragma unroll
-                for (int r = 0; r < MAXRHS; ++r)
-                    if (r < nrhs) acc[r] += mk * sb[r * BM + k];
-            }
+            for (int r = 0; r < MAXRHS; ++r)
+                if (r < nrhs) acc[r] += mk * sb[r * BM + k];
         }
 #pragma unroll
         for (int r = 0; r < MAXRHS; ++r)
@@ -1366,13 +1393,7 @@ __global__ void __launch_bounds__(TS) k_fwd(const T* fac, const T* inv2, T* b, T
             int j = e % nj, r = e / nj;
             y[(ll)r * n + F.f + c0 + j0 + j] = sy[r * SC + j];
         }
-    const int row = c1 + rt * TS + tid;
-    if (row < F.ld) {
-        const int grow = row < F.nf ? F.f + row : S.rows[F.rows_off + row - F.nf];
-        T lv[SC];
-        const T* lcol = fac + F.loff + (ll)(c0 + j0) * F.ld + row;
-#pragma unroll
-        for (int j = 0; j < SC; ++j) lv[j] = j < nj ? lcol[(ll)j * F.ld] : T(0);
+    if (has_row) {
 #pragma unroll
         for (int r = 0; r < MAXRHS; ++r) {
             if (r >= nrhs) break;
@@ -1384,24 +1405,81 @@ __global__ void __launch_bounds__(TS) k_fwd(const T* fac, const T* inv2, T* b, T
     }
 }
 
-// Backward, part 1: y[F's columns] -= U12 * x[R_F] (one warp per row).
+// Products y[F.f + k] -= dot(line k, x[R_F]) over the lines of a front's
+// off-diagonal part (U12 rows for the backward solve, L21 columns for the
+// transposed one; line k at base + k * stride, F.m values, contiguous).  A
+// CTA (256 threads) takes a tile of U12_ROWS lines x U12_COLS positions of
+// R_F: it gathers x at those positions into shared memory (four right-hand
+// sides at a time), then each warp streams four lines against it, the four
+// lines' loads interleaved so that 16 are in flight per lane; partial sums go
+// to y with atomics.  The tile count of a front is
+// cdiv(F.nf, U12_ROWS) * cdiv(F.m, U12_COLS), enough CTAs to keep HBM busy
+// on the wide fronts near the root.
+constexpr int U12_ROWS = 32, U12_COLS = 512, U12_RG = 4;
 template <typename T>
-__global__ void __launch_bounds__(TS) k_bwd_u12(const T* fac, T* y, const T* x, int n, int nrhs, Sched S, Launch L) {
+__device__ __forceinline__ void front_line_dots(const T* base, ll stride, T* y, const T* x, int n, int nrhs,
+                                                const DFront& F, const int* rows, int tile) {
+    __shared__ T sx[U12_COLS * U12_RG];   // sx[c * U12_RG + r]
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int ncc = cdiv(F.m, U12_COLS);
+    const int i0 = (tile / ncc) * U12_ROWS + wid, c0 = (tile % ncc) * U12_COLS;
+    const int nc = min(U12_COLS, F.m - c0);
+    for (int r0 = 0; r0 < nrhs; r0 += U12_RG) {
+        const int nr = min(U12_RG, nrhs - r0);
+        if (r0 > 0) __syncthreads();
+        for (int c = threadIdx.x; c < nc; c += 256) {
+            const int g = rows[c0 + c];
+#pragma unroll
+            for (int r = 0; r < U12_RG; ++r) sx[c * U12_RG + r] = r < nr ? x[(ll)(r0 + r) * n + g] : T(0);
+        }
+        __syncthreads();
+        T acc[4][U12_RG];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int r = 0; r < U12_RG; ++r) acc[a][r] = T(0);
+        const T* u[4];
+        bool live[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            live[a] = i0 + 8 * a < F.nf;
+            u[a] = base + (ll)(live[a] ? i0 + 8 * a : 0) * stride + c0;
+        }
+#pragma unroll 4
+        for (int c = lane; c < nc; c += 32) {
+            T uv[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) uv[a] = live[a] ? u[a][c] : T(0);
+            T xv[U12_RG];
+#pragma unroll
+            for (int r = 0; r < U12_RG; ++r) xv[r] = sx[c * U12_RG + r];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int r = 0; r < U12_RG; ++r) acc[a][r] += uv[a] * xv[r];
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+#pragma unroll
+            for (int r = 0; r < U12_RG; ++r) {
+                T v = acc[a][r];
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+                if (lane == 0 && live[a] && r < nr) atomicAdd(&y[(ll)(r0 + r) * n + F.f + i0 + 8 * a], -v);
+            }
+        }
+    }
+}
+
+// Backward, part 1: y[F's columns] -= U12 * x[R_F] (U12 row i contiguous in Uf).
+template <typename T>
+__global__ void __launch_bounds__(256) k_bwd_u12(const T* fac, T* y, const T* x, int n, int nrhs, Sched S, Launch L) {
+    griddep_launch();
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int i = tile * (TS / 32) + wid;
-    if (i >= F.nf) return;
-    for (int r = 0; r < nrhs; ++r) {
-        T acc = T(0);
-#pragma unroll 8
-        for (int c = lane; c < F.m; c += 32)
-            acc += fac[F.uoff + (ll)i * F.m + c] * x[(ll)r * n + S.rows[F.rows_off + c]];
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-        if (lane == 0) y[(ll)r * n + F.f + i] -= acc;
-    }
+    griddep_wait();
+    front_line_dots<T>(fac + F.uoff, F.m, y, x, n, nrhs, F, S.rows + F.rows_off, tile);
 }
 
 // Backward, part 2, for the block `step`-th from the last, tiled as (128
@@ -1413,9 +1491,11 @@ template <typename T>
 __global__ void __launch_bounds__(TS) k_bwd(const T* fac, const T* inv2, T* y, T* x, int n, int nrhs, Sched S,
                                             Launch L, int step) {
     constexpr int BM = BlockMax<T>::value;
+    __shared__ T sm[BM * SC];   // Uinv[:, chunk], sm[k * SC + j] (rows k >= j0)
     __shared__ T sc[BM * MAXRHS];
     __shared__ T sp[4 * SC * MAXRHS];
     __shared__ T sx[SC * MAXRHS];
+    griddep_launch();
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
@@ -1425,10 +1505,25 @@ __global__ void __launch_bounds__(TS) k_bwd(const T* fac, const T* inv2, T* y, T
     const int j0 = cc * SC, nj = min(SC, bw - j0);
     const T* Ui = inv2 + S.blk_inv2[blk] + (ll)bw * bw;
     const int tid = threadIdx.x;
+    // Factor data first: the chunk of Uinv, this thread's row of U[:, chunk].
+    for (int e = j0 * SC + tid; e < bw * SC; e += TS) {
+        const int k = e / SC, j = e % SC;
+        cp_elem(&sm[e], Ui + (ll)k * bw + j0 + min(j, nj - 1), j < nj);
+    }
+    const int row = rt * TS + tid;
+    const bool has_row = row < c0;
+    T uv[SC];
+    {
+        const T* ucol = fac + F.loff + (ll)(c0 + j0) * F.ld + (has_row ? row : 0);
+#pragma unroll
+        for (int j = 0; j < SC; ++j) uv[j] = (has_row && j < nj) ? ucol[(ll)j * F.ld] : T(0);
+    }
+    griddep_wait();
     for (int e = tid; e < bw * nrhs; e += TS) {
         int k = e % bw, r = e / bw;
         sc[r * BM + k] = y[(ll)r * n + F.f + c0 + k];
     }
+    cp_wait_all();
     __syncthreads();
     {   // x_chunk = Uinv[j0:j0+nj, :] c_B (upper: k >= j)
         const int j = tid & 31, kq = tid >> 5;
@@ -1439,7 +1534,7 @@ __global__ void __launch_bounds__(TS) k_bwd(const T* fac, const T* inv2, T* y, T
             const int kstart = j0 + j;
 #pragma unroll 8
             for (int k = kstart + kq; k < bw; k += 4) {
-                const T uk = Ui[(ll)k * bw + j0 + j];
+                const T uk = sm[k * SC + j];
 #pragma unroll
                 for (int r = 0; r < MAXRHS; ++r)
                     if (r < nrhs) acc[r] += uk * sc[r * BM + k];
@@ -1461,12 +1556,7 @@ __global__ void __launch_bounds__(TS) k_bwd(const T* fac, const T* inv2, T* y, T
             int j = e % nj, r = e / nj;
             x[(ll)r * n + F.f + c0 + j0 + j] = sx[r * SC + j];
         }
-    const int row = rt * TS + tid;
-    if (row < c0) {
-        T uv[SC];
-        const T* ucol = fac + F.loff + (ll)(c0 + j0) * F.ld + row;
-#pragma unroll
-        for (int j = 0; j < SC; ++j) uv[j] = j < nj ? ucol[(ll)j * F.ld] : T(0);
+    if (has_row) {
 #pragma unroll
         for (int r = 0; r < MAXRHS; ++r) {
             if (r >= nrhs) break;
@@ -1500,6 +1590,7 @@ __global__ void __launch_bounds__(TS) k_tfwd(const T* fac, const T* inv2, T* b, 
     __shared__ T sb[BM * MAXRHS];
     __shared__ T sp[4 * SC * MAXRHS];
     __shared__ T sz[SC * MAXRHS];
+    griddep_launch();
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
@@ -1508,6 +1599,7 @@ __global__ void __launch_bounds__(TS) k_tfwd(const T* fac, const T* inv2, T* b, 
     const int ncc = cdiv(bw, SC), cc = tile % ncc, rt = tile / ncc;
     const int j0 = cc * SC, nj = min(SC, bw - j0);
     const T* Ui = inv2 + S.blk_inv2[blk] + (ll)bw * bw;   // Uinv(k, j) at Ui[j * bw + k], zero for k > j
+    griddep_wait();
     const int tid = threadIdx.x;
     for (int e = tid; e < bw * nrhs; e += TS) {
         int k = e % bw, r = e / bw;
@@ -1572,37 +1664,15 @@ __global__ void __launch_bounds__(TS) k_tfwd(const T* fac, const T* inv2, T* b, 
     }
 }
 
-// Pass 2, per front: z[F's columns] -= L21^T x[R_F], one warp per column
-// (L21 column k contiguous in Lf).
+// Pass 2, per front: z[F's columns] -= L21^T x[R_F] (L21 column k contiguous in Lf).
 template <typename T>
-__global__ void __launch_bounds__(TS) k_tbwd_l21(const T* fac, T* z, const T* x, int n, int nrhs, Sched S, Launch L) {
+__global__ void __launch_bounds__(256) k_tbwd_l21(const T* fac, T* z, const T* x, int n, int nrhs, Sched S, Launch L) {
+    griddep_launch();
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int k = tile * (TS / 32) + wid;
-    if (k >= F.nf) return;
-    const T* l = fac + F.loff + (ll)k * F.ld + F.nf;
-    const int* rows = S.rows + F.rows_off;
-    T acc[MAXRHS];
-#pragma unroll
-    for (int r = 0; r < MAXRHS; ++r) acc[r] = T(0);
-#pragma unroll 4
-    for (int i = lane; i < F.m; i += 32) {
-        const T lv = l[i];
-        const int g = rows[i];
-#pragma unroll
-        for (int r = 0; r < MAXRHS; ++r)
-            if (r < nrhs) acc[r] += lv * x[(ll)r * n + g];
-    }
-#pragma unroll
-    for (int r = 0; r < MAXRHS; ++r) {
-        if (r >= nrhs) break;
-        T v = acc[r];
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-        if (lane == 0) z[(ll)r * n + F.f + k] -= v;
-    }
+    griddep_wait();
+    front_line_dots<T>(fac + F.loff + F.nf, F.ld, z, x, n, nrhs, F, S.rows + F.rows_off, tile);
 }
 
 // Pass 2, block `step`-th from the last: x_chunk = (Minv^T)[chunk, :] z_B,
@@ -1615,6 +1685,7 @@ __global__ void __launch_bounds__(TS) k_tbwd(const T* fac, const T* inv2, T* z, 
     __shared__ T sc[BM * MAXRHS];
     __shared__ T sp[4 * SC * MAXRHS];
     __shared__ T sx[SC * MAXRHS];
+    griddep_launch();
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
@@ -1623,6 +1694,7 @@ __global__ void __launch_bounds__(TS) k_tbwd(const T* fac, const T* inv2, T* z, 
     const int ncc = cdiv(bw, SC), cc = tile % ncc, rt = tile / ncc;
     const int j0 = cc * SC, nj = min(SC, bw - j0);
     const T* Mi = inv2 + S.blk_inv2[blk];   // Minv(k, j) at Mi[j * bw + k]
+    griddep_wait();
     const int tid = threadIdx.x;
     for (int e = tid; e < bw * nrhs; e += TS) {
         int k = e % bw, r = e / bw;
