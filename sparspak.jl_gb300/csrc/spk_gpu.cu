@@ -131,6 +131,7 @@ struct spk_handle {
         *d_rel = nullptr;
     ll* d_run_rel = nullptr;
     int* d_ipiv = nullptr;
+    int* d_bmap = nullptr;     // row sources of each block's interchanges (k_block_lu -> panels)
     int* d_info = nullptr;
 
     // pattern and values
@@ -678,6 +679,7 @@ static int upload_structure(spk_handle* h) {
     if ((rc = upload(h, &h->d_run_rel, h->run_rel))) return rc;
     if ((rc = upload(h, &h->d_rel, h->rel))) return rc;
     CU(h, cudaMalloc((void**)&h->d_ipiv, sizeof(int) * std::max<i64>(h->n, 1)));
+    CU(h, cudaMalloc((void**)&h->d_bmap, sizeof(int) * std::max<i64>(h->n, 1)));
     CU(h, cudaMalloc((void**)&h->d_info, 2 * sizeof(int)));   // first singular piece, tensor-core timeout
     return SPK_OK;
 }
@@ -848,20 +850,20 @@ static int factor_launches(spk_handle* h) {
                         fac, h->d_ipiv, h->d_info, S, launch_of(PL, P.blu[t]), (int)t);
                 else
                     spk::k_block_lu<T><<<P.blu[t].tiles, spk::LuThreads<T>::value, 0, h->stream>>>(
-                        fac, h->d_ipiv, h->d_info, S, launch_of(PL, P.blu[t]), (int)t);
+                        fac, h->d_ipiv, h->d_info, h->d_bmap, S, launch_of(PL, P.blu[t]), (int)t);
             }
             if (P.bpanel[t].tiles > 0) {
                 LaunchScope ls(h, SPK_K_PANEL, P.bpanel[t].flops, P.bpanel[t].words * sizeof(T));
                 const spk::Launch la = launch_of(PL, P.bpanel[t]);
                 if (bw <= 32)
                     spk::k_block_panel<T, 32><<<P.bpanel[t].tiles, 256, sweep_smem<T, 32>(1), h->stream>>>(
-                        fac, h->d_ipiv, S, la, (int)t, storage<T>(h).pack);
+                        fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack);
                 else if (bw <= 64)
                     spk::k_block_panel<T, 64><<<P.bpanel[t].tiles, 256, sweep_smem<T, 64>(1), h->stream>>>(
-                        fac, h->d_ipiv, S, la, (int)t, storage<T>(h).pack);
+                        fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack);
                 else
                     spk::k_block_panel<T, BM><<<P.bpanel[t].tiles, 256, sweep_smem<T, BM>(1), h->stream>>>(
-                        fac, h->d_ipiv, S, la, (int)t, storage<T>(h).pack);
+                        fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack);
             }
             if (P.btrail[t].tiles > 0) {
                 LaunchScope ls(h, SPK_K_TRAIL, P.btrail[t].flops, P.btrail[t].words * sizeof(T));
@@ -1607,7 +1609,7 @@ void spk_destroy(spk_handle* h) {
     free_plan(h->plan[0]);
     free_plan(h->plan[1]);
     void* ptrs[] = {h->d_xs, h->d_rows, h->d_runid, h->d_run_tgt, h->d_run_start, h->d_run_rel,
-                    h->d_rel, h->s64.inv2, h->s32.inv2, h->s64.pack, h->s32.pack, h->d_ipiv, h->d_info, h->d_slot, h->d_aval,
+                    h->d_rel, h->s64.inv2, h->s32.inv2, h->s64.pack, h->s32.pack, h->d_ipiv, h->d_bmap, h->d_info, h->d_slot, h->d_aval,
                     h->d_rowptr, h->d_col, h->d_src, h->d_ccolptr, h->d_crow, h->d_ccol, h->d_rperm, h->d_rinvp, h->s64.d, h->s32.d, h->d_wb,
                     h->d_wy, h->d_wx, h->d_rhs, h->d_x, h->d_r, h->d_sums};
     for (void* p : ptrs)

@@ -321,6 +321,25 @@ __device__ __forceinline__ T pick_n(const T (&r)[N], int k) {
     return v;
 }
 
+// Row sources of a block's interchanges: applying, piece by piece, the
+// swaps k <-> a + ipiv[k] of the piece [a, b) to a vector v gives
+// v'[R] = v[gmap[R]]; pa[R] = first row of R's piece.  One thread per piece.
+__device__ __forceinline__ void block_gather_map(const int* ipiv_blk, const int* q0, int np, int* gmap, int* pa) {
+    for (int pc = threadIdx.x; pc < np; pc += blockDim.x) {
+        const int a = q0[pc], b = q0[pc + 1];
+        for (int i = a; i < b; ++i) {
+            gmap[i] = i;
+            pa[i] = a;
+        }
+        for (int k = a; k < b; ++k) {
+            const int kp = a + ipiv_blk[k];
+            const int t = gmap[k];
+            gmap[k] = gmap[kp];
+            gmap[kp] = t;
+        }
+    }
+}
+
 // Correctly rounded reciprocal (the value of T(1) / x).
 __device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
@@ -492,14 +511,14 @@ __device__ __forceinline__ void lu_group_swap_left(T (&a)[RPT][4], int g, int bw
 }
 
 template <typename T>
-__global__ void __launch_bounds__(LuThreads<T>::value, 1) k_block_lu(T* fac, int* ipiv, int* info, Sched S, Launch L,
-                                                                      int step) {
+__global__ void __launch_bounds__(LuThreads<T>::value, 1) k_block_lu(T* fac, int* ipiv, int* info, int* bmap, Sched S,
+                                                                      Launch L, int step) {
     constexpr int BM = BlockMax<T>::value, RPT = BM / 32;
     __shared__ __align__(16) T lbuf[2][4 * BM];   // the group's multipliers by column and row (by group parity)
     __shared__ T s_pv[2][4];
     __shared__ int s_kp[2][4], s_a0[2][4];
     __shared__ int q0[BM + 1];
-    __shared__ int spiv[BM];
+    __shared__ int spiv[BM], sgmap[BM], spa[BM];
     __shared__ int szero;
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
@@ -545,6 +564,9 @@ __global__ void __launch_bounds__(LuThreads<T>::value, 1) k_block_lu(T* fac, int
             if (R < bw && C < bw) blkp[(ll)C * F.ld + R] = a[ii][jj];
         }
     for (int c = tid; c < bw; c += blockDim.x) ipiv[F.f + c0 + c] = spiv[c];
+    block_gather_map(spiv, q0, np, sgmap, spa);   // spiv and q0 published by the last barrier of the loop
+    __syncthreads();
+    for (int c = tid; c < bw; c += blockDim.x) bmap[F.f + c0 + c] = sgmap[c] | (spa[c] << 8);
     if (tid == 0 && szero != INT_MAX) {
         int p = 0;
         while (q0[p + 1] <= szero) ++p;
@@ -566,10 +588,12 @@ __global__ void __launch_bounds__(LuThreads<T>::value, 1) k_block_lu(T* fac, int
 //         columns, zero on and above the diagonal.
 // A staged row (column) is SLD(W) entries: the four lanes' chunks of CQ
 // entries each start 16 bytes apart in the bank cycle (chunk q at
-// q * (CQ + SK)), so their 16-byte loads do not collide.
+// q * (CQ + SK)), so their 16-byte loads do not collide; one more 16-byte
+// unit per row puts consecutive rows 20 words apart in the 32-bank cycle, so
+// that the staging copies of 8 rows x 4 entries per warp hit 32 banks.
 // ---------------------------------------------------------------------------
 template <typename T> struct Skew { static constexpr int value = 16 / sizeof(T); };
-template <typename T, int W> struct SLD { static constexpr int value = W + 4 * Skew<T>::value; };
+template <typename T, int W> struct SLD { static constexpr int value = W + 5 * Skew<T>::value; };
 template <typename T, int W>
 __device__ __forceinline__ int sidx(int k, int j) {   // entry j of staged row / column k
     constexpr int CQ = W / 4, SK = Skew<T>::value;
@@ -613,21 +637,58 @@ __device__ __forceinline__ void sweep_cols(T (&y)[W / 4], const T* sL, int bw) {
     }
 }
 
-// Row sources of a block's interchanges: applying, piece by piece, the
-// swaps k <-> a + ipiv[k] of the piece [a, b) to a vector v gives
-// v'[R] = v[gmap[R]]; pa[R] = first row of R's piece.  One thread per piece.
-__device__ __forceinline__ void block_gather_map(const int* ipiv_blk, const int* q0, int np, int* gmap, int* pa) {
-    for (int pc = threadIdx.x; pc < np; pc += blockDim.x) {
-        const int a = q0[pc], b = q0[pc + 1];
-        for (int i = a; i < b; ++i) {
-            gmap[i] = i;
-            pa[i] = a;
+// The same sweeps for W = 128 with four lines per lane: the 16 lanes of a
+// half-warp share four lines, lane c holding entries [8c, 8c + 8) of each,
+// so that a staged row (column) read from shared memory serves four lines
+// (two 16-byte loads per lane and step instead of eight; the staged layout
+// sidx<float, 128> puts the eight chunks of a quarter-warp in distinct bank
+// quads).  The owner of entry k shuffles its four values to the half-warp.
+__device__ __forceinline__ void sweep_rows4(float (&x)[4][8], const float* sU, const float* rd, int bw) {
+    const int lane = threadIdx.x & 31, c = lane & 15, base = lane & 16;
+#pragma unroll 1
+    for (int kc = 0; kc * 8 < bw; ++kc) {
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk) {
+            const int k = kc * 8 + kk;
+            if (k >= bw) break;
+            const float r = rd[k];
+            float xk[4];
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                if (c == kc) x[l][kk] *= r;
+                xk[l] = __shfl_sync(0xffffffffu, x[l][kk], base | kc);
+            }
+            const float* u = sU + sidx<float, 128>(k, 8 * c);
+            const float4 u0 = *reinterpret_cast<const float4*>(u);
+            const float4 u1 = *reinterpret_cast<const float4*>(u + 4);
+            const float uv[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+#pragma unroll
+            for (int l = 0; l < 4; ++l)
+#pragma unroll
+                for (int jj = 0; jj < 8; ++jj) x[l][jj] -= xk[l] * uv[jj];
         }
-        for (int k = a; k < b; ++k) {
-            const int kp = a + ipiv_blk[k];
-            const int t = gmap[k];
-            gmap[k] = gmap[kp];
-            gmap[kp] = t;
+    }
+}
+
+__device__ __forceinline__ void sweep_cols4(float (&y)[4][8], const float* sL, int bw) {
+    const int lane = threadIdx.x & 31, c = lane & 15, base = lane & 16;
+#pragma unroll 1
+    for (int kc = 0; kc * 8 < bw; ++kc) {
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk) {
+            const int k = kc * 8 + kk;
+            if (k >= bw) break;
+            float yk[4];
+#pragma unroll
+            for (int l = 0; l < 4; ++l) yk[l] = __shfl_sync(0xffffffffu, y[l][kk], base | kc);
+            const float* lp = sL + sidx<float, 128>(k, 8 * c);
+            const float4 l0 = *reinterpret_cast<const float4*>(lp);
+            const float4 l1 = *reinterpret_cast<const float4*>(lp + 4);
+            const float lv[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
+#pragma unroll
+            for (int l = 0; l < 4; ++l)
+#pragma unroll
+                for (int ii = 0; ii < 8; ++ii) y[l][ii] -= lv[ii] * yk[l];
         }
     }
 }
@@ -647,10 +708,20 @@ __device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;
 // sU and rd from the factored block (column-major at blkp, leading dimension
 // ld); the triangle is copied asynchronously (the caller waits with
 // cp_wait_all and a barrier before using it).
+// Staging order: a warp copies 8 consecutive rows k x 4 consecutive entries
+// j (global: 4 columns, 32 contiguous bytes each; shared: 32 distinct banks).
+template <int W>
+__device__ __forceinline__ void stage_coords(int e, int& k, int& j) {
+    const int sub = e & 31, b = e >> 5;
+    k = (b % (W / 8)) * 8 + (sub & 7);
+    j = (b / (W / 8)) * 4 + (sub >> 3);
+}
+
 template <typename T, int W>
 __device__ __forceinline__ void stage_upper(T* sU, T* rd, const T* blkp, ll ld, int bw) {
-    for (int e = threadIdx.x; e < W * W; e += blockDim.x) {   // consecutive threads read down a column
-        const int k = e % W, j = e / W;
+    for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
+        int k, j;
+        stage_coords<W>(e, k, j);
         const bool v = j > k && j < bw;
         cp_elem(&sU[sidx<T, W>(k, j)], v ? blkp + (ll)j * ld + k : blkp, v);
     }
@@ -667,7 +738,8 @@ __device__ __forceinline__ void stage_upper(T* sU, T* rd, const T* blkp, ll ld, 
 template <typename T, int W>
 __device__ __forceinline__ void stage_lower(T* sL, const T* blkp, ll ld, int bw, const int* gmap, const int* pa) {
     for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
-        const int i = e % W, k = e / W;
+        int k, i;
+        stage_coords<W>(e, k, i);
         const bool v = i > k && i < bw;
         cp_elem(&sL[sidx<T, W>(k, i)], v ? blkp + (ll)k * ld + (k < pa[i] ? gmap[i] : i) : blkp, v);
     }
@@ -696,6 +768,121 @@ __device__ __forceinline__ void pack_line(unsigned char* base, int t, int i, int
     }
 }
 
+// Packed copy of a segment of a panel line: entries [k0, k0 + N) (N a
+// multiple of 4, k0 a multiple of 4) of line `i` at tile `t`.
+template <int N>
+__device__ __forceinline__ void pack_seg(unsigned char* base, int t, int i, int k0, int nch, const float (&v)[N]) {
+#pragma unroll
+    for (int g = 0; g < N / 4; ++g) {
+        const int k = k0 + 4 * g;
+        if (k < nch * umma::KCH) {
+            unsigned char* dst = base + ((ll)t * nch + k / umma::KCH) * umma::PCHUNK + umma::packed_offset(i, k % umma::KCH);
+            uint32_t h[4], l[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                h[e] = umma::tf32_rna(v[4 * g + e]);
+                l[e] = umma::tf32_rna(v[4 * g + e] - __uint_as_float(h[e]));
+            }
+            *reinterpret_cast<uint4*>(dst) = make_uint4(h[0], h[1], h[2], h[3]);
+            *reinterpret_cast<uint4*>(dst + umma::OPB) = make_uint4(l[0], l[1], l[2], l[3]);
+        }
+    }
+}
+
+// The panels of a block of more than 64 columns in FP32 (W = 128), four
+// lines per lane (sweep_rows4 / sweep_cols4): lane c of half-warp h holds
+// entries [8c, 8c + 8) of the tile's lines 4h .. 4h + 3.  Same tiles,
+// operations and outputs as the generic form in k_block_panel; the row
+// sources of the block's interchanges (gmap | pa << 8 per block column) come
+// from k_block_lu through bmap.
+__device__ __forceinline__ void block_panel128(float* fac, const int* bmap, const Sched& S, const DFront& F, int blk,
+                                               int tile, unsigned char* pack, float* sT, float* rd, int* gmap, int* pa) {
+    const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
+    const int tid = threadIdx.x, c = tid & 15, line0 = (tid >> 4) * 4;
+    const int nL = cdiv(F.ld - c1, 64), nUa = cdiv(F.nf - c1, 64);
+    const float* blkp = fac + F.loff + (ll)c0 * F.ld + c0;
+    const int nch = cdiv(bw, umma::KCH);
+    if (tile < nL) {
+        const int rb = c1 + tile * 64 + line0;
+        float x[4][8];
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            const bool ok = rb + l < F.ld;
+            const float* xp = fac + F.loff + (ll)c0 * F.ld + (ok ? rb + l : c1);
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) {
+                const int j = 8 * c + jj;
+                x[l][jj] = (ok && j < bw) ? xp[(ll)j * F.ld] : 0.f;
+            }
+        }
+        stage_upper<float, 128>(sT, rd, blkp, F.ld, bw);
+        __syncthreads();
+        sweep_rows4(x, sT, rd, bw);
+        const ll off = S.blk_lpack[blk];
+        const int n1 = cdiv(F.nf - c1, umma::TM);
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            const int r = rb + l;
+            if (r >= F.ld) break;
+            float* xp = fac + F.loff + (ll)c0 * F.ld + r;
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) {
+                const int j = 8 * c + jj;
+                if (j < bw) xp[(ll)j * F.ld] = x[l][jj];
+            }
+            if (off >= 0) {
+                const int t = r < F.nf ? (r - c1) / umma::TM : n1 + (r - F.nf) / umma::TM;
+                const int i = r < F.nf ? (r - c1) % umma::TM : (r - F.nf) % umma::TM;
+                pack_seg<8>(pack + off, t, i, 8 * c, nch, x[l]);
+            }
+        }
+    } else {
+        if (tid < bw) {   // the block's row sources, from k_block_lu
+            const int v = bmap[F.f + c0 + tid];
+            gmap[tid] = v & 255;
+            pa[tid] = v >> 8;
+        }
+        __syncthreads();
+        const bool inner = tile < nL + nUa;
+        const int cb = inner ? c1 + (tile - nL) * 64 + line0 : (tile - nL - nUa) * 64 + line0;
+        const int lim = inner ? F.nf : F.m;
+        const ll stride = inner ? 1 : (ll)F.m;
+        float y[4][8];
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            const bool ok = cb + l < lim;
+            const int col = ok ? cb + l : (inner ? c1 : 0);
+            const float* cp = inner ? fac + F.loff + (ll)col * F.ld + c0 : fac + F.uoff + (ll)c0 * F.m + col;
+#pragma unroll
+            for (int ii = 0; ii < 8; ++ii) {
+                const int R = 8 * c + ii;
+                y[l][ii] = (ok && R < bw) ? cp[(ll)gmap[R] * stride] : 0.f;
+            }
+        }
+        stage_lower<float, 128>(sT, blkp, F.ld, bw, gmap, pa);
+        __syncthreads();
+        sweep_cols4(y, sT, bw);
+        const ll off = S.blk_upack[blk];
+        const int n1 = cdiv(F.nf - c1, umma::TM);
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            const int col = cb + l;
+            if (col >= lim) break;
+            float* cp = inner ? fac + F.loff + (ll)col * F.ld + c0 : fac + F.uoff + (ll)c0 * F.m + col;
+#pragma unroll
+            for (int ii = 0; ii < 8; ++ii) {
+                const int R = 8 * c + ii;
+                if (R < bw) cp[(ll)R * stride] = y[l][ii];
+            }
+            if (off >= 0) {
+                const int t = inner ? (col - c1) / umma::TM : n1 + col / umma::TM;
+                const int i = inner ? (col - c1) % umma::TM : col % umma::TM;
+                pack_seg<8>(pack + off, t, i, 8 * c, nch, y[l]);
+            }
+        }
+    }
+}
+
 // Panels of block `step` (block width bw <= W): 64-row tiles of the L panel
 // below the block, X := X inv(U_B) (the reference's trsm 'r','u','n','n' of
 // every piece, with the earlier pieces' updates X_p -= X_<p U_<p,p), and
@@ -708,8 +895,8 @@ __device__ __forceinline__ void pack_line(unsigned char* base, int t, int i, int
 // panel from c1 ([c1, nf)) and from 0 (U12).
 // Dynamic shared memory: W * SLD(W) T's.
 template <typename T, int W>
-__global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, Sched S, Launch L, int step,
-                                                      unsigned char* pack) {
+__global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, const int* bmap, Sched S, Launch L,
+                                                      int step, unsigned char* pack) {
     constexpr int CQ = W / 4;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sT = reinterpret_cast<T*>(smem_raw);
@@ -719,6 +906,10 @@ __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, Sc
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
     const int blk = F.block0 + step;
+    if constexpr (std::is_same<T, float>::value && W == 128) {
+        block_panel128(fac, bmap, S, F, blk, tile, pack, sT, rd, gmap, pa);
+        return;
+    }
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
     const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
     const int tid = threadIdx.x, line = tid >> 2, q = tid & 3;
