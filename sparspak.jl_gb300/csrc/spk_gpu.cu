@@ -688,6 +688,12 @@ static int upload_structure(spk_handle* h) {
 // Dynamic shared memory of the panel sweeps: `n` staged triangles of W lines.
 template <typename T, int W>
 static size_t sweep_smem(int n) { return sizeof(T) * (size_t)n * W * spk::SLD<T, W>::value; }
+// Dynamic shared memory of k_block_panel<T, W>: the staged triangle, plus the
+// line tile of the 128-wide FP32 form.
+template <typename T, int W>
+static size_t panel_smem() {
+    return sweep_smem<T, W>(1) + ((std::is_same<T, float>::value && W == 128) ? (size_t)spk::PT_SMEM : 0);
+}
 
 template <typename T>
 static int ensure_plan(spk_handle* h) {
@@ -748,7 +754,7 @@ static int ensure_plan(spk_handle* h) {
     S.blk_upack = P.d_blk_upack;
     constexpr int BM = spk::BlockMax<T>::value;
     CU(h, cudaFuncSetAttribute(spk::k_block_panel<T, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)sweep_smem<T, BM>(1)));
+                               (int)panel_smem<T, BM>()));
     CU(h, cudaFuncSetAttribute(spk::k_block_inv<T, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)sweep_smem<T, BM>(1)));
     if (std::is_same<T, float>::value) {
@@ -862,7 +868,7 @@ static int factor_launches(spk_handle* h) {
                     spk::k_block_panel<T, 64><<<P.bpanel[t].tiles, 256, sweep_smem<T, 64>(1), h->stream>>>(
                         fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack);
                 else
-                    spk::k_block_panel<T, BM><<<P.bpanel[t].tiles, 256, sweep_smem<T, BM>(1), h->stream>>>(
+                    spk::k_block_panel<T, BM><<<P.bpanel[t].tiles, 256, panel_smem<T, BM>(), h->stream>>>(
                         fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack);
             }
             if (P.btrail[t].tiles > 0) {

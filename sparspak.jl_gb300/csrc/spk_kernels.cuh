@@ -518,7 +518,7 @@ __global__ void __launch_bounds__(LuThreads<T>::value, 1) k_block_lu(T* fac, int
     __shared__ T s_pv[2][4];
     __shared__ int s_kp[2][4], s_a0[2][4];
     __shared__ int q0[BM + 1];
-    __shared__ int spiv[BM], sgmap[BM], spa[BM];
+    __shared__ int spiv[BM], sgmap[BM];
     __shared__ int szero;
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
@@ -564,9 +564,30 @@ __global__ void __launch_bounds__(LuThreads<T>::value, 1) k_block_lu(T* fac, int
             if (R < bw && C < bw) blkp[(ll)C * F.ld + R] = a[ii][jj];
         }
     for (int c = tid; c < bw; c += blockDim.x) ipiv[F.f + c0 + c] = spiv[c];
-    block_gather_map(spiv, q0, np, sgmap, spa);   // spiv and q0 published by the last barrier of the loop
-    __syncthreads();
-    for (int c = tid; c < bw; c += blockDim.x) bmap[F.f + c0 + c] = sgmap[c] | (spa[c] << 8);
+    // Row sources of the block's interchanges (block_gather_map), a warp per
+    // piece of at most 32 columns: lane i tracks gmap[a + i] through the
+    // piece's swaps.  spiv and q0 were published by the loop's last barrier.
+    for (int pc = w; pc < np; pc += blockDim.x / 32) {
+        const int a = q0[pc], b = q0[pc + 1];
+        if (b - a <= 32) {
+            int g = a + lane;
+            for (int k = a; k < b; ++k) {
+                const int kp = a + spiv[k];
+                const int vk = __shfl_sync(0xffffffffu, g, k - a), vp = __shfl_sync(0xffffffffu, g, kp - a);
+                g = lane == k - a ? vp : (lane == kp - a ? vk : g);
+            }
+            if (lane < b - a) bmap[F.f + c0 + a + lane] = g | (a << 8);
+        } else if (lane == 0) {
+            for (int i = a; i < b; ++i) sgmap[i] = i;
+            for (int k = a; k < b; ++k) {
+                const int kp = a + spiv[k];
+                const int t = sgmap[k];
+                sgmap[k] = sgmap[kp];
+                sgmap[kp] = t;
+            }
+            for (int i = a; i < b; ++i) bmap[F.f + c0 + i] = sgmap[i] | (a << 8);
+        }
+    }
     if (tid == 0 && szero != INT_MAX) {
         int p = 0;
         while (q0[p + 1] <= szero) ++p;
@@ -794,48 +815,102 @@ __device__ __forceinline__ void pack_seg(unsigned char* base, int t, int i, int 
 // entries [8c, 8c + 8) of the tile's lines 4h .. 4h + 3.  Same tiles,
 // operations and outputs as the generic form in k_block_panel; the row
 // sources of the block's interchanges (gmap | pa << 8 per block column) come
-// from k_block_lu through bmap.
+// from k_block_lu through bmap.  The 64 lines of the tile pass through a
+// shared-memory copy sX (line li, entry j at li * PT_LD + j) so that the
+// global loads, stores and packed writes are coalesced: a warp moves 8 rows
+// x 4 columns of a column-major array (32-byte runs), and the packed writes
+// of 8 lines x 4 entries form 512 contiguous bytes.
+constexpr int PT_LD = 132;   // 16-byte rows, 4 words apart in the bank cycle
+constexpr int PT_SMEM = 64 * PT_LD * 4;
+
+// Element of a 64-line x 128-entry tile copied by lane `sub` of warp-step
+// b: 8 consecutive entries x 4 lines when `entries_fast`, else 8 lines x 4
+// entries.
+__device__ __forceinline__ void tile_coords(int e, bool entries_fast, int& li, int& j) {
+    const int sub = e & 31, b = e >> 5;
+    if (entries_fast) {
+        j = (b % 16) * 8 + (sub & 7);
+        li = (b / 16) * 4 + (sub >> 3);
+    } else {
+        li = (b % 8) * 8 + (sub & 7);
+        j = (b / 8) * 4 + (sub >> 3);
+    }
+}
+
+// Packed copy of the tile's lines [0, nl) from sX; line li goes to pack tile
+// t(li), line i(li) (computed by `where`).
+template <typename Where>
+__device__ __forceinline__ void pack_tile(unsigned char* base, const float* sX, int nl, int nch, Where where) {
+    const int lo = threadIdx.x & 7, g = threadIdx.x >> 3;   // 8 lines x 32 groups of 4 entries
+    if (4 * g >= nch * umma::KCH) return;
+#pragma unroll 2
+    for (int it = 0; it < 8; ++it) {
+        const int li = it * 8 + lo;
+        if (li >= nl) break;
+        int t, i;
+        where(li, t, i);
+        const int k = 4 * g;
+        const float4 v = *reinterpret_cast<const float4*>(sX + li * PT_LD + k);
+        const float vv[4] = {v.x, v.y, v.z, v.w};
+        uint32_t hh[4], ll_[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            hh[e] = umma::tf32_rna(vv[e]);
+            ll_[e] = umma::tf32_rna(vv[e] - __uint_as_float(hh[e]));
+        }
+        unsigned char* dst = base + ((ll)t * nch + k / umma::KCH) * umma::PCHUNK + umma::packed_offset(i, k % umma::KCH);
+        *reinterpret_cast<uint4*>(dst) = make_uint4(hh[0], hh[1], hh[2], hh[3]);
+        *reinterpret_cast<uint4*>(dst + umma::OPB) = make_uint4(ll_[0], ll_[1], ll_[2], ll_[3]);
+    }
+}
+
 __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, const Sched& S, const DFront& F, int blk,
-                                               int tile, unsigned char* pack, float* sT, float* rd, int* gmap, int* pa) {
+                                               int tile, unsigned char* pack, float* sT, float* sX, float* rd,
+                                               int* gmap, int* pa) {
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
     const int tid = threadIdx.x, c = tid & 15, line0 = (tid >> 4) * 4;
     const int nL = cdiv(F.ld - c1, 64), nUa = cdiv(F.nf - c1, 64);
     const float* blkp = fac + F.loff + (ll)c0 * F.ld + c0;
     const int nch = cdiv(bw, umma::KCH);
+    const int n1 = cdiv(F.nf - c1, umma::TM);
     if (tile < nL) {
-        const int rb = c1 + tile * 64 + line0;
+        const int rb0 = c1 + tile * 64, nl = min(64, F.ld - rb0);
+        float* xb = fac + F.loff + (ll)c0 * F.ld + rb0;   // line li, entry j at xb[j * ld + li]
+        for (int e = tid; e < 64 * 128; e += 256) {
+            int li, j;
+            tile_coords(e, false, li, j);
+            const bool v = li < nl && j < bw;
+            cp_elem(&sX[li * PT_LD + j], v ? xb + (ll)j * F.ld + li : xb, v);
+        }
+        stage_upper<float, 128>(sT, rd, blkp, F.ld, bw);   // waits for all copies
+        __syncthreads();
         float x[4][8];
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
-            const bool ok = rb + l < F.ld;
-            const float* xp = fac + F.loff + (ll)c0 * F.ld + (ok ? rb + l : c1);
-#pragma unroll
-            for (int jj = 0; jj < 8; ++jj) {
-                const int j = 8 * c + jj;
-                x[l][jj] = (ok && j < bw) ? xp[(ll)j * F.ld] : 0.f;
-            }
+            const float4 a0 = *reinterpret_cast<const float4*>(sX + (line0 + l) * PT_LD + 8 * c);
+            const float4 a1 = *reinterpret_cast<const float4*>(sX + (line0 + l) * PT_LD + 8 * c + 4);
+            x[l][0] = a0.x; x[l][1] = a0.y; x[l][2] = a0.z; x[l][3] = a0.w;
+            x[l][4] = a1.x; x[l][5] = a1.y; x[l][6] = a1.z; x[l][7] = a1.w;
         }
-        stage_upper<float, 128>(sT, rd, blkp, F.ld, bw);
-        __syncthreads();
         sweep_rows4(x, sT, rd, bw);
-        const ll off = S.blk_lpack[blk];
-        const int n1 = cdiv(F.nf - c1, umma::TM);
 #pragma unroll
-        for (int l = 0; l < 4; ++l) {
-            const int r = rb + l;
-            if (r >= F.ld) break;
-            float* xp = fac + F.loff + (ll)c0 * F.ld + r;
-#pragma unroll
-            for (int jj = 0; jj < 8; ++jj) {
-                const int j = 8 * c + jj;
-                if (j < bw) xp[(ll)j * F.ld] = x[l][jj];
-            }
-            if (off >= 0) {
-                const int t = r < F.nf ? (r - c1) / umma::TM : n1 + (r - F.nf) / umma::TM;
-                const int i = r < F.nf ? (r - c1) % umma::TM : (r - F.nf) % umma::TM;
-                pack_seg<8>(pack + off, t, i, 8 * c, nch, x[l]);
-            }
+        for (int l = 0; l < 4; ++l) {   // each lane rewrites only what it read
+            *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 8 * c) = make_float4(x[l][0], x[l][1], x[l][2], x[l][3]);
+            *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 8 * c + 4) = make_float4(x[l][4], x[l][5], x[l][6], x[l][7]);
         }
+        __syncthreads();
+        for (int e = tid; e < 64 * 128; e += 256) {
+            int li, j;
+            tile_coords(e, false, li, j);
+            if (li < nl && j < bw) xb[(ll)j * F.ld + li] = sX[li * PT_LD + j];
+        }
+        const ll off = S.blk_lpack[blk];
+        if (off >= 0)
+            pack_tile(pack + off, sX, nl, nch, [&](int li, int& t, int& i) {
+                const int r = rb0 + li;
+                t = r < F.nf ? (r - c1) / umma::TM : n1 + (r - F.nf) / umma::TM;
+                i = r < F.nf ? (r - c1) % umma::TM : (r - F.nf) % umma::TM;
+            });
     } else {
         if (tid < bw) {   // the block's row sources, from k_block_lu
             const int v = bmap[F.f + c0 + tid];
@@ -844,42 +919,46 @@ __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, cons
         }
         __syncthreads();
         const bool inner = tile < nL + nUa;
-        const int cb = inner ? c1 + (tile - nL) * 64 + line0 : (tile - nL - nUa) * 64 + line0;
-        const int lim = inner ? F.nf : F.m;
-        const ll stride = inner ? 1 : (ll)F.m;
+        const int cb0 = inner ? c1 + (tile - nL) * 64 : (tile - nL - nUa) * 64;
+        const int nl = min(64, (inner ? F.nf : F.m) - cb0);
+        // line li, block row R at yb[li * ls + R * rs]
+        float* yb = inner ? fac + F.loff + (ll)cb0 * F.ld + c0 : fac + F.uoff + (ll)c0 * F.m + cb0;
+        const ll ls = inner ? (ll)F.ld : 1, rs = inner ? 1 : (ll)F.m;
+        for (int e = tid; e < 64 * 128; e += 256) {
+            int li, R;
+            tile_coords(e, inner, li, R);
+            const bool v = li < nl && R < bw;
+            cp_elem(&sX[li * PT_LD + R], v ? yb + li * ls + (ll)gmap[R] * rs : yb, v);
+        }
+        stage_lower<float, 128>(sT, blkp, F.ld, bw, gmap, pa);   // waits for all copies
+        __syncthreads();
         float y[4][8];
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
-            const bool ok = cb + l < lim;
-            const int col = ok ? cb + l : (inner ? c1 : 0);
-            const float* cp = inner ? fac + F.loff + (ll)col * F.ld + c0 : fac + F.uoff + (ll)c0 * F.m + col;
-#pragma unroll
-            for (int ii = 0; ii < 8; ++ii) {
-                const int R = 8 * c + ii;
-                y[l][ii] = (ok && R < bw) ? cp[(ll)gmap[R] * stride] : 0.f;
-            }
+            const float4 a0 = *reinterpret_cast<const float4*>(sX + (line0 + l) * PT_LD + 8 * c);
+            const float4 a1 = *reinterpret_cast<const float4*>(sX + (line0 + l) * PT_LD + 8 * c + 4);
+            y[l][0] = a0.x; y[l][1] = a0.y; y[l][2] = a0.z; y[l][3] = a0.w;
+            y[l][4] = a1.x; y[l][5] = a1.y; y[l][6] = a1.z; y[l][7] = a1.w;
         }
-        stage_lower<float, 128>(sT, blkp, F.ld, bw, gmap, pa);
-        __syncthreads();
         sweep_cols4(y, sT, bw);
-        const ll off = S.blk_upack[blk];
-        const int n1 = cdiv(F.nf - c1, umma::TM);
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
-            const int col = cb + l;
-            if (col >= lim) break;
-            float* cp = inner ? fac + F.loff + (ll)col * F.ld + c0 : fac + F.uoff + (ll)c0 * F.m + col;
-#pragma unroll
-            for (int ii = 0; ii < 8; ++ii) {
-                const int R = 8 * c + ii;
-                if (R < bw) cp[(ll)R * stride] = y[l][ii];
-            }
-            if (off >= 0) {
-                const int t = inner ? (col - c1) / umma::TM : n1 + col / umma::TM;
-                const int i = inner ? (col - c1) % umma::TM : col % umma::TM;
-                pack_seg<8>(pack + off, t, i, 8 * c, nch, y[l]);
-            }
+            *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 8 * c) = make_float4(y[l][0], y[l][1], y[l][2], y[l][3]);
+            *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 8 * c + 4) = make_float4(y[l][4], y[l][5], y[l][6], y[l][7]);
         }
+        __syncthreads();
+        for (int e = tid; e < 64 * 128; e += 256) {
+            int li, R;
+            tile_coords(e, inner, li, R);
+            if (li < nl && R < bw) yb[li * ls + (ll)R * rs] = sX[li * PT_LD + R];
+        }
+        const ll off = S.blk_upack[blk];
+        if (off >= 0)
+            pack_tile(pack + off, sX, nl, nch, [&](int li, int& t, int& i) {
+                const int col = cb0 + li;
+                t = inner ? (col - c1) / umma::TM : n1 + col / umma::TM;
+                i = inner ? (col - c1) % umma::TM : col % umma::TM;
+            });
     }
 }
 
@@ -907,7 +986,7 @@ __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, co
     const DFront F = S.fronts[fid];
     const int blk = F.block0 + step;
     if constexpr (std::is_same<T, float>::value && W == 128) {
-        block_panel128(fac, bmap, S, F, blk, tile, pack, sT, rd, gmap, pa);
+        block_panel128(fac, bmap, S, F, blk, tile, pack, sT, sT + 128 * SLD<float, 128>::value, rd, gmap, pa);
         return;
     }
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
