@@ -54,7 +54,9 @@ struct Timed {
 // the forward block steps, and backward the U12 product and block steps.
 struct LevelPlan {
     LaunchRec schur, schur_tc, bwdu;
-    std::vector<LaunchRec> blu, bpanel, btrail, btrail_tc, fwd, bwd;
+    // btrail_tc0: tile 0 of each packed front's trailing update (it holds the
+    // next block's diagonal block); btrail_tc: its tiles 1..
+    std::vector<LaunchRec> blu, bpanel, btrail, btrail_tc0, btrail_tc, fwd, bwd;
 };
 
 // FP32 fronts whose rank updates go to the tensor cores (k_tc_update,
@@ -155,6 +157,11 @@ struct spk_handle {
     i64 rhs_cap = 0;
 
     cudaStream_t own = nullptr, stream = nullptr;
+    // Look-ahead of the factorisation: the bulk of a block step's tensor-core
+    // trailing update runs on `side` while the next block LU runs on the
+    // launch stream (evP: panels done; evB: trailing update done).
+    cudaStream_t side = nullptr;
+    cudaEvent_t evP = nullptr, evB = nullptr;
     int device = -1;
     int nsm = 1;                 // SMs of the device (grid of the persistent kernels)
     std::string err;
@@ -592,16 +599,17 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
         L.blu.resize(maxb);
         L.bpanel.resize(maxb);
         L.btrail.resize(maxb);
+        L.btrail_tc0.resize(maxb);
         L.btrail_tc.resize(maxb);
         L.fwd.resize(maxb);
         L.bwd.resize(maxb);
         for (int t = 0; t < maxb; ++t) {
-            std::vector<int> tl(nid), tp(nid), tt(nid), ttc(nid), tf(nid), tb(nid);
+            std::vector<int> tl(nid), tp(nid), tt(nid), ttc(nid), ttc0(nid), tf(nid), tb(nid);
             std::vector<double> fl(nid), wl(nid), fp(nid), wp(nid), ft(nid), wt(nid), ff(nid), wf(nid), fb(nid), wb(nid);
             for (size_t k = 0; k < nid; ++k) {
                 const HFront& F = h->fronts[ids[k]];
                 const int nb = P.nblocks[ids[k]];
-                if (t >= nb) { tl[k] = tp[k] = tt[k] = ttc[k] = tf[k] = tb[k] = 0; continue; }
+                if (t >= nb) { tl[k] = tp[k] = tt[k] = ttc[k] = ttc0[k] = tf[k] = tb[k] = 0; continue; }
                 const int blk = P.block0[ids[k]] + t;
                 const int c0 = P.blk_c0[blk], c1 = P.blk_c1[blk];
                 const double bw = c1 - c0;
@@ -614,10 +622,12 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
                 fp[k] = bw * bw * rowsL + 2.0 * bw * bw * colsU;
                 wp[k] = 2.0 * bw * (rowsL + colsU) + 2.0 * bw * bw;
                 tt[k] = cdiv(ld - c1, spk::TT) * cdiv(F.nf - c1, spk::TT) + cdiv(F.nf - c1, spk::TT) * cdiv(F.m, spk::TT);
-                ttc[k] = 0;
+                ttc[k] = ttc0[k] = 0;
                 if (P.blk_lpack[blk] >= 0) {   // packed front: 128-tiles, row / column regions split at nf
                     const int n1 = cdiv(F.nf - c1, spk::umma::TM), n2 = cdiv(F.m, spk::umma::TM);
-                    ttc[k] = (n1 + n2) * n1 + n1 * n2;
+                    const int all = (n1 + n2) * n1 + n1 * n2;
+                    ttc0[k] = all > 0 ? 1 : 0;
+                    ttc[k] = all - ttc0[k];
                     tt[k] = 0;
                 }
                 const double area = (double)(ld - c1) * (F.nf - c1) + (double)(F.nf - c1) * F.m;
@@ -643,7 +653,18 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
                 }
             L.blu[t].bw = L.bpanel[t].bw = bwl;
             add_launch(&P, L.btrail[t], ids, tt, ft, wt);
-            add_launch(&P, L.btrail_tc[t], ids, ttc, ft, wt);
+            {   // flops and words of the tensor-core update split by tiles
+                std::vector<double> f0(nid), w0(nid), f1(nid), w1(nid);
+                for (size_t k = 0; k < nid; ++k) {
+                    const double all = ttc0[k] + ttc[k], a = all > 0 ? ttc0[k] / all : 0.0;
+                    f0[k] = ft[k] * a;
+                    w0[k] = wt[k] * a;
+                    f1[k] = ft[k] - f0[k];
+                    w1[k] = wt[k] - w0[k];
+                }
+                add_launch(&P, L.btrail_tc0[t], ids, ttc0, f0, w0);
+                add_launch(&P, L.btrail_tc[t], ids, ttc, f1, w1);
+            }
             add_launch(&P, L.fwd[t], ids, tf, ff, wf);
             add_launch(&P, L.bwd[t], ids, tb, fb, wb);
         }
@@ -846,6 +867,9 @@ static int factor_launches(spk_handle* h) {
     T* fac = storage<T>(h).d;
     const Plan& PL = h->plan[prec_index<T>()];
     const spk::Sched& S = PL.sched;
+    // Look ahead (not while timing kernels one by one): see spk_handle::side.
+    const bool ahead = h->prof_mask == 0;
+    bool pending = false;
     for (const LevelPlan& P : PL.levels) {
         for (size_t t = 0; t < P.blu.size(); ++t) {
             const int bw = P.blu[t].bw;
@@ -857,6 +881,10 @@ static int factor_launches(spk_handle* h) {
                 else
                     spk::k_block_lu<T><<<P.blu[t].tiles, spk::LuThreads<T>::value, 0, h->stream>>>(
                         fac, h->d_ipiv, h->d_info, h->d_bmap, S, launch_of(PL, P.blu[t]), (int)t);
+            }
+            if (pending) {   // the panels read what the previous step's trailing update wrote
+                CU(h, cudaStreamWaitEvent(h->stream, h->evB, 0));
+                pending = false;
             }
             if (P.bpanel[t].tiles > 0) {
                 LaunchScope ls(h, SPK_K_PANEL, P.bpanel[t].flops, P.bpanel[t].words * sizeof(T));
@@ -877,13 +905,41 @@ static int factor_launches(spk_handle* h) {
                                                                                  (int)t);
             }
             if constexpr (std::is_same<T, float>::value) {
+                // Tiles 1.. of the tensor-core trailing update: on the side
+                // stream when looking ahead, on as many SMs as the next
+                // block LU and tile 0 leave free; the next panels wait for it.
                 if (P.btrail_tc[t].tiles > 0) {
-                    LaunchScope ls(h, SPK_K_TRAIL, P.btrail_tc[t].flops, P.btrail_tc[t].words * sizeof(T));
                     const int nt = P.btrail_tc[t].tiles;
+                    int grid = std::min(nt, h->nsm);
+                    cudaStream_t st = h->stream;
+                    if (ahead) {
+                        const int reserve = std::max(P.btrail_tc0[t].tiles,
+                                                     t + 1 < P.blu.size() ? P.blu[t + 1].tiles : 0);
+                        grid = std::max(std::min(nt, h->nsm - reserve), std::min(nt, h->nsm / 2));
+                        CU(h, cudaEventRecord(h->evP, h->stream));
+                        CU(h, cudaStreamWaitEvent(h->side, h->evP, 0));
+                        st = h->side;
+                    }
+                    LaunchScope ls(h, SPK_K_TRAIL, P.btrail_tc[t].flops, P.btrail_tc[t].words * sizeof(T));
+                    spk::k_tc_update<spk::TC_TRAIL><<<grid, spk::TC_THREADS, spk::umma::PSMEM, st>>>(
+                        fac, storage<T>(h).pack, S, launch_of(PL, P.btrail_tc[t]), (int)t, nt, 1, h->d_info + 1);
+                    if (ahead) {
+                        CU(h, cudaEventRecord(h->evB, h->side));
+                        pending = true;
+                    }
+                }
+                // Tile 0 (the next block's diagonal block) on the launch stream.
+                if (P.btrail_tc0[t].tiles > 0) {
+                    LaunchScope ls(h, SPK_K_TRAIL, P.btrail_tc0[t].flops, P.btrail_tc0[t].words * sizeof(T));
+                    const int nt = P.btrail_tc0[t].tiles;
                     spk::k_tc_update<spk::TC_TRAIL><<<std::min(nt, h->nsm), spk::TC_THREADS, spk::umma::PSMEM, h->stream>>>(
-                        fac, storage<T>(h).pack, S, launch_of(PL, P.btrail_tc[t]), (int)t, nt, h->d_info + 1);
+                        fac, storage<T>(h).pack, S, launch_of(PL, P.btrail_tc0[t]), (int)t, nt, 0, h->d_info + 1);
                 }
             }
+        }
+        if (pending) {   // the level's Schur complement needs every trailing update
+            CU(h, cudaStreamWaitEvent(h->stream, h->evB, 0));
+            pending = false;
         }
         if (P.schur.tiles > 0) {
             LaunchScope ls(h, SPK_K_SCHUR, P.schur.flops, P.schur.words * sizeof(T));
@@ -894,7 +950,7 @@ static int factor_launches(spk_handle* h) {
                 LaunchScope ls(h, SPK_K_SCHUR, P.schur_tc.flops, P.schur_tc.words * sizeof(T));
                 const int nt = P.schur_tc.tiles;
                 spk::k_tc_update<spk::TC_SCHUR><<<std::min(nt, h->nsm), spk::TC_THREADS, spk::umma::PSMEM, h->stream>>>(
-                    fac, storage<T>(h).pack, S, launch_of(PL, P.schur_tc), 0, nt, h->d_info + 1);
+                    fac, storage<T>(h).pack, S, launch_of(PL, P.schur_tc), 0, nt, 0, h->d_info + 1);
             }
         }
     }
@@ -1136,6 +1192,9 @@ int spk_create(int64_t n, int64_t nsuper, const int64_t* xsuper, const int64_t* 
             if (cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || h->nsm < 1)
                 h->nsm = 1;
             e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->evP, cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->evB, cudaEventDisableTiming);
             if (e != cudaSuccess) rc = set_err(h, SPK_ECUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
             h->stream = h->own;
         }
@@ -1625,6 +1684,10 @@ void spk_destroy(spk_handle* h) {
     drop_graph(h->g_factor[0]);
     drop_graph(h->g_factor[1]);
     drop_solve_graphs(h);
+    if (h->side) cudaStreamSynchronize(h->side);
+    if (h->evP) cudaEventDestroy(h->evP);
+    if (h->evB) cudaEventDestroy(h->evB);
+    if (h->side) cudaStreamDestroy(h->side);
     if (h->own) cudaStreamDestroy(h->own);
     delete h;
 }

@@ -1334,6 +1334,10 @@ __global__ void __launch_bounds__(256) k_schur(T* fac, Sched S, Launch L) {
 //     tiles (rt < n1, n1 <= ct) update U12 in Uf.
 //   SCHUR: A = L21 row tile, B = U12 column tile, K = all blocks' columns;
 //     the product is scattered into the ancestors like k_schur.
+// A launch covers local tiles tile_base.. of each front in its list (the
+// trailing update is launched as tile 0, which holds the next block's
+// diagonal block, and tiles 1.., so that the next block LU can start before
+// the rest of the update is done).
 // Persistent: CTA b takes tiles b, b + gridDim.x, ...  Warp 0 lane 0 issues
 // the bulk copies, warp 1 lane 0 the MMAs, and the TC_EPI epilogue warps
 // (from warp 4; warp w reads TMEM lanes 32 (w % 4).. and the 32 accumulator
@@ -1349,10 +1353,11 @@ struct TcTile {
 };
 
 template <int MODE>
-__device__ __forceinline__ TcTile tc_decode(const Sched& S, const Launch& L, int step, int tile) {
+__device__ __forceinline__ TcTile tc_decode(const Sched& S, const Launch& L, int step, int tile, int tile_base) {
     TcTile T;
     int fid, t;
     locate(L, tile, fid, t);
+    t += tile_base;
     T.F = S.fronts[fid];
     const int n2 = cdiv(T.F.m, umma::TM);
     T.n2 = n2;
@@ -1386,7 +1391,7 @@ __device__ __forceinline__ TcTile tc_decode(const Sched& S, const Launch& L, int
 
 template <int MODE>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const unsigned char* pack, Sched S, Launch L,
-                                                              int step, int ntiles, int* err) {
+                                                              int step, int ntiles, int tile_base, int* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ ScatterRow tab[2][umma::TM];   // SCHUR: [0] tile columns, [1] tile rows
     __shared__ int dead;
@@ -1416,7 +1421,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
             int s = 0;
             uint32_t ph = 0;
             for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-                const TcTile T = tc_decode<MODE>(S, L, step, tile);
+                const TcTile T = tc_decode<MODE>(S, L, step, tile, tile_base);
                 int b = MODE == TC_TRAIL ? T.F.block0 + step : T.F.block0;
                 int c = 0, nb = MODE == TC_TRAIL ? 0 : cdiv(S.blk_c1[b] - S.blk_c0[b], umma::KCH);
                 int n1b = MODE == TC_TRAIL ? T.n1 : cdiv(T.F.nf - S.blk_c1[b], umma::TM);
@@ -1452,7 +1457,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
             int acc = 0;
             uint32_t aph = 0;
             for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-                const TcTile T = tc_decode<MODE>(S, L, step, tile);
+                const TcTile T = tc_decode<MODE>(S, L, step, tile, tile_base);
                 umma::wait_bounded(&cx.tempty[acc], aph ^ 1, vdead, err);
                 umma::fence_after();
                 const uint32_t d = tmem + acc * umma::TN;
@@ -1484,7 +1489,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
         int acc = 0;
         uint32_t aph = 0;
         for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-            const TcTile T = tc_decode<MODE>(S, L, step, tile);
+            const TcTile T = tc_decode<MODE>(S, L, step, tile, tile_base);
             const DFront& F = T.F;
             if (MODE == TC_SCHUR) {
                 asm volatile("bar.sync 1, %0;" ::"n"(32 * TC_EPI) : "memory");   // previous tile's scatter done
