@@ -518,6 +518,10 @@ static void add_launch(Plan* h, LaunchRec& rec, const std::vector<int>& ids, con
     rec.tiles = acc;
 }
 
+// Lines per panel tile: the 128-wide FP32 form (a launch with a block wider
+// than 64 columns) takes spk::PT_LINES, the others 64.
+static int panel_lines(bool fp32, bool wide) { return fp32 && wide ? spk::PT_LINES : 64; }
+
 // Group each front's pieces into blocks of at most `bmax` columns and lay
 // out the launches of every level.
 static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
@@ -603,6 +607,10 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
         L.btrail_tc.resize(maxb);
         L.fwd.resize(maxb);
         L.bwd.resize(maxb);
+        std::vector<char> wide(maxb, 0);   // a block of the step is wider than 64 columns
+        for (int id : ids)
+            for (int t = 0; t < P.nblocks[id]; ++t)
+                if (P.blk_c1[P.block0[id] + t] - P.blk_c0[P.block0[id] + t] > 64) wide[t] = 1;
         for (int t = 0; t < maxb; ++t) {
             std::vector<int> tl(nid), tp(nid), tt(nid), ttc(nid), ttc0(nid), tf(nid), tb(nid);
             std::vector<double> fl(nid), wl(nid), fp(nid), wp(nid), ft(nid), wt(nid), ff(nid), wf(nid), fb(nid), wb(nid);
@@ -617,7 +625,8 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
                 tl[k] = 1;
                 fl[k] = 2.0 * bw * bw * bw;
                 wl[k] = 4.0 * bw * bw;
-                tp[k] = cdiv(ld - c1, 64) + cdiv(F.nf - c1, 64) + cdiv(F.m, 64);
+                const int lpt = panel_lines(tc, wide[t]);
+                tp[k] = cdiv(ld - c1, lpt) + cdiv(F.nf - c1, lpt) + cdiv(F.m, lpt);
                 const double rowsL = ld - c1, colsU = (double)(F.nf - c1) + F.m;
                 fp[k] = bw * bw * rowsL + 2.0 * bw * bw * colsU;
                 wp[k] = 2.0 * bw * (rowsL + colsU) + 2.0 * bw * bw;
@@ -711,6 +720,10 @@ template <typename T, int W>
 static size_t sweep_smem(int n) { return sizeof(T) * (size_t)n * W * spk::SLD<T, W>::value; }
 // Dynamic shared memory of k_block_panel<T, W>: the staged triangle, plus the
 // line tile of the 128-wide FP32 form.
+template <typename T, int W>
+static int panel_threads() {
+    return (std::is_same<T, float>::value && W == 128) ? 4 * spk::PT_LINES : 256;
+}
 template <typename T, int W>
 static size_t panel_smem() {
     return sweep_smem<T, W>(1) + ((std::is_same<T, float>::value && W == 128) ? (size_t)spk::PT_SMEM : 0);
@@ -896,7 +909,7 @@ static int factor_launches(spk_handle* h) {
                     spk::k_block_panel<T, 64><<<P.bpanel[t].tiles, 256, sweep_smem<T, 64>(1), h->stream>>>(
                         fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack);
                 else
-                    spk::k_block_panel<T, BM><<<P.bpanel[t].tiles, 256, panel_smem<T, BM>(), h->stream>>>(
+                    spk::k_block_panel<T, BM><<<P.bpanel[t].tiles, panel_threads<T, BM>(), panel_smem<T, BM>(), h->stream>>>(
                         fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack);
             }
             if (P.btrail[t].tiles > 0) {

@@ -665,51 +665,71 @@ __device__ __forceinline__ void sweep_cols(T (&y)[W / 4], const T* sL, int bw) {
 // sidx<float, 128> puts the eight chunks of a quarter-warp in distinct bank
 // quads).  The owner of entry k shuffles its four values to the half-warp.
 __device__ __forceinline__ void sweep_rows4(float (&x)[4][8], const float* sU, const float* rd, int bw) {
+    // Steps past bw are no-ops (zero staged rows, rd = 0, zero entries), so
+    // whole chunks of 8 run unguarded; the next step's row and rd are loaded
+    // one step ahead, and the update of the next step's pivot entry comes
+    // first.
     const int lane = threadIdx.x & 31, c = lane & 15, base = lane & 16;
+    const int nk = cdiv(bw, 8);
+    float4 n0 = *reinterpret_cast<const float4*>(sU + sidx<float, 128>(0, 8 * c));
+    float4 n1 = *reinterpret_cast<const float4*>(sU + sidx<float, 128>(0, 8 * c) + 4);
+    float nr = rd[0];
 #pragma unroll 1
-    for (int kc = 0; kc * 8 < bw; ++kc) {
+    for (int kc = 0; kc < nk; ++kc) {
 #pragma unroll
         for (int kk = 0; kk < 8; ++kk) {
             const int k = kc * 8 + kk;
-            if (k >= bw) break;
-            const float r = rd[k];
+            const float4 u0 = n0, u1 = n1;
+            const float r = nr;
+            const int kn = k + 1 < 128 ? k + 1 : k;
+            n0 = *reinterpret_cast<const float4*>(sU + sidx<float, 128>(kn, 8 * c));
+            n1 = *reinterpret_cast<const float4*>(sU + sidx<float, 128>(kn, 8 * c) + 4);
+            nr = rd[kn];
             float xk[4];
 #pragma unroll
             for (int l = 0; l < 4; ++l) {
                 if (c == kc) x[l][kk] *= r;
                 xk[l] = __shfl_sync(0xffffffffu, x[l][kk], base | kc);
             }
-            const float* u = sU + sidx<float, 128>(k, 8 * c);
-            const float4 u0 = *reinterpret_cast<const float4*>(u);
-            const float4 u1 = *reinterpret_cast<const float4*>(u + 4);
             const float uv[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+            const int jn = (kk + 1) & 7;
+#pragma unroll
+            for (int l = 0; l < 4; ++l) x[l][jn] -= xk[l] * uv[jn];
 #pragma unroll
             for (int l = 0; l < 4; ++l)
 #pragma unroll
-                for (int jj = 0; jj < 8; ++jj) x[l][jj] -= xk[l] * uv[jj];
+                for (int jj = 0; jj < 8; ++jj)
+                    if (jj != jn) x[l][jj] -= xk[l] * uv[jj];
         }
     }
 }
 
 __device__ __forceinline__ void sweep_cols4(float (&y)[4][8], const float* sL, int bw) {
     const int lane = threadIdx.x & 31, c = lane & 15, base = lane & 16;
+    const int nk = cdiv(bw, 8);
+    float4 n0 = *reinterpret_cast<const float4*>(sL + sidx<float, 128>(0, 8 * c));
+    float4 n1 = *reinterpret_cast<const float4*>(sL + sidx<float, 128>(0, 8 * c) + 4);
 #pragma unroll 1
-    for (int kc = 0; kc * 8 < bw; ++kc) {
+    for (int kc = 0; kc < nk; ++kc) {
 #pragma unroll
         for (int kk = 0; kk < 8; ++kk) {
             const int k = kc * 8 + kk;
-            if (k >= bw) break;
+            const float4 l0 = n0, l1 = n1;
+            const int kn = k + 1 < 128 ? k + 1 : k;
+            n0 = *reinterpret_cast<const float4*>(sL + sidx<float, 128>(kn, 8 * c));
+            n1 = *reinterpret_cast<const float4*>(sL + sidx<float, 128>(kn, 8 * c) + 4);
             float yk[4];
 #pragma unroll
             for (int l = 0; l < 4; ++l) yk[l] = __shfl_sync(0xffffffffu, y[l][kk], base | kc);
-            const float* lp = sL + sidx<float, 128>(k, 8 * c);
-            const float4 l0 = *reinterpret_cast<const float4*>(lp);
-            const float4 l1 = *reinterpret_cast<const float4*>(lp + 4);
             const float lv[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
+            const int jn = (kk + 1) & 7;
+#pragma unroll
+            for (int l = 0; l < 4; ++l) y[l][jn] -= lv[jn] * yk[l];
 #pragma unroll
             for (int l = 0; l < 4; ++l)
 #pragma unroll
-                for (int ii = 0; ii < 8; ++ii) y[l][ii] -= lv[ii] * yk[l];
+                for (int ii = 0; ii < 8; ++ii)
+                    if (ii != jn) y[l][ii] -= lv[ii] * yk[l];
         }
     }
 }
@@ -821,10 +841,11 @@ __device__ __forceinline__ void pack_seg(unsigned char* base, int t, int i, int 
 // x 4 columns of a column-major array (32-byte runs), and the packed writes
 // of 8 lines x 4 entries form 512 contiguous bytes.
 constexpr int PT_LD = 132;   // 16-byte rows, 4 words apart in the bank cycle
-constexpr int PT_SMEM = 64 * PT_LD * 4;
+constexpr int PT_LINES = 64;  // lines per CTA (4 * PT_LINES threads)
+constexpr int PT_SMEM = PT_LINES * PT_LD * 4;
 
-// Element of a 64-line x 128-entry tile copied by lane `sub` of warp-step
-// b: 8 consecutive entries x 4 lines when `entries_fast`, else 8 lines x 4
+// Element e of a PT_LINES-line x 128-entry tile: a warp copies 8
+// consecutive entries x 4 lines when `entries_fast`, else 8 lines x 4
 // entries.
 __device__ __forceinline__ void tile_coords(int e, bool entries_fast, int& li, int& j) {
     const int sub = e & 31, b = e >> 5;
@@ -832,8 +853,8 @@ __device__ __forceinline__ void tile_coords(int e, bool entries_fast, int& li, i
         j = (b % 16) * 8 + (sub & 7);
         li = (b / 16) * 4 + (sub >> 3);
     } else {
-        li = (b % 8) * 8 + (sub & 7);
-        j = (b / 8) * 4 + (sub >> 3);
+        li = (b % (PT_LINES / 8)) * 8 + (sub & 7);
+        j = (b / (PT_LINES / 8)) * 4 + (sub >> 3);
     }
 }
 
@@ -841,12 +862,9 @@ __device__ __forceinline__ void tile_coords(int e, bool entries_fast, int& li, i
 // t(li), line i(li) (computed by `where`).
 template <typename Where>
 __device__ __forceinline__ void pack_tile(unsigned char* base, const float* sX, int nl, int nch, Where where) {
-    const int lo = threadIdx.x & 7, g = threadIdx.x >> 3;   // 8 lines x 32 groups of 4 entries
-    if (4 * g >= nch * umma::KCH) return;
-#pragma unroll 2
-    for (int it = 0; it < 8; ++it) {
-        const int li = it * 8 + lo;
-        if (li >= nl) break;
+    for (int item = threadIdx.x; item < PT_LINES * 32; item += blockDim.x) {   // 8 lines x 32 groups of 4 entries
+        const int g = (item >> 3) & 31, li = (item >> 8) * 8 + (item & 7);
+        if (li >= nl || 4 * g >= nch * umma::KCH) continue;
         int t, i;
         where(li, t, i);
         const int k = 4 * g;
@@ -869,14 +887,14 @@ __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, cons
                                                int* gmap, int* pa) {
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
     const int tid = threadIdx.x, c = tid & 15, line0 = (tid >> 4) * 4;
-    const int nL = cdiv(F.ld - c1, 64), nUa = cdiv(F.nf - c1, 64);
+    const int nL = cdiv(F.ld - c1, PT_LINES), nUa = cdiv(F.nf - c1, PT_LINES);
     const float* blkp = fac + F.loff + (ll)c0 * F.ld + c0;
     const int nch = cdiv(bw, umma::KCH);
     const int n1 = cdiv(F.nf - c1, umma::TM);
     if (tile < nL) {
-        const int rb0 = c1 + tile * 64, nl = min(64, F.ld - rb0);
+        const int rb0 = c1 + tile * PT_LINES, nl = min(PT_LINES, F.ld - rb0);
         float* xb = fac + F.loff + (ll)c0 * F.ld + rb0;   // line li, entry j at xb[j * ld + li]
-        for (int e = tid; e < 64 * 128; e += 256) {
+        for (int e = tid; e < PT_LINES * 128; e += PT_LINES * 4) {
             int li, j;
             tile_coords(e, false, li, j);
             const bool v = li < nl && j < bw;
@@ -899,7 +917,7 @@ __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, cons
             *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 8 * c + 4) = make_float4(x[l][4], x[l][5], x[l][6], x[l][7]);
         }
         __syncthreads();
-        for (int e = tid; e < 64 * 128; e += 256) {
+        for (int e = tid; e < PT_LINES * 128; e += PT_LINES * 4) {
             int li, j;
             tile_coords(e, false, li, j);
             if (li < nl && j < bw) xb[(ll)j * F.ld + li] = sX[li * PT_LD + j];
@@ -919,12 +937,12 @@ __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, cons
         }
         __syncthreads();
         const bool inner = tile < nL + nUa;
-        const int cb0 = inner ? c1 + (tile - nL) * 64 : (tile - nL - nUa) * 64;
-        const int nl = min(64, (inner ? F.nf : F.m) - cb0);
+        const int cb0 = inner ? c1 + (tile - nL) * PT_LINES : (tile - nL - nUa) * PT_LINES;
+        const int nl = min(PT_LINES, (inner ? F.nf : F.m) - cb0);
         // line li, block row R at yb[li * ls + R * rs]
         float* yb = inner ? fac + F.loff + (ll)cb0 * F.ld + c0 : fac + F.uoff + (ll)c0 * F.m + cb0;
         const ll ls = inner ? (ll)F.ld : 1, rs = inner ? 1 : (ll)F.m;
-        for (int e = tid; e < 64 * 128; e += 256) {
+        for (int e = tid; e < PT_LINES * 128; e += PT_LINES * 4) {
             int li, R;
             tile_coords(e, inner, li, R);
             const bool v = li < nl && R < bw;
@@ -947,7 +965,7 @@ __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, cons
             *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 8 * c + 4) = make_float4(y[l][4], y[l][5], y[l][6], y[l][7]);
         }
         __syncthreads();
-        for (int e = tid; e < 64 * 128; e += 256) {
+        for (int e = tid; e < PT_LINES * 128; e += PT_LINES * 4) {
             int li, R;
             tile_coords(e, inner, li, R);
             if (li < nl && R < bw) yb[li * ls + (ll)R * rs] = sX[li * PT_LD + R];
