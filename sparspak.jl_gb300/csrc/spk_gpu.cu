@@ -57,6 +57,14 @@ struct LevelPlan {
     // btrail_tc0: tile 0 of each packed front's trailing update (it holds the
     // next block's diagonal block); btrail_tc: its tiles 1..
     std::vector<LaunchRec> blu, bpanel, btrail, btrail_tc0, btrail_tc, fwd, bwd;
+    // Solves: fronts with many blocks by one cluster launch each direction
+    // (front_big, one tile per front), the others by block steps
+    // (fwd_small / bwd_small); the transposed solves use fwd / bwd.
+    LaunchRec front_big, front_l21;   // front_l21: tiles of k_fwd_l21 for the front_big fronts
+    // Small fronts (one block of at most 32 columns, m <= spk::LEAF_M) by
+    // k_solve_leaf, a warp per front; bwdu_small: U12 products of the others.
+    LaunchRec front_leaf, bwdu_small;
+    std::vector<LaunchRec> fwd_small, bwd_small;
 };
 
 // FP32 fronts whose rank updates go to the tensor cores (k_tc_update,
@@ -607,6 +615,42 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
         L.btrail_tc.resize(maxb);
         L.fwd.resize(maxb);
         L.bwd.resize(maxb);
+        L.fwd_small.resize(maxb);
+        L.bwd_small.resize(maxb);
+        std::vector<char> big(nid, 0), leaf(nid, 0);
+        {
+            std::vector<int> tl1(nid);
+            std::vector<double> fl1(nid), wl1(nid);
+            for (size_t k = 0; k < nid; ++k) {
+                const HFront& F = h->fronts[ids[k]];
+                leaf[k] = P.nblocks[ids[k]] == 1 && F.nf <= 32 && F.m <= spk::LEAF_M;
+                tl1[k] = leaf[k] ? 1 : 0;
+                fl1[k] = 2.0 * F.nf * (double)F.nf + 2.0 * F.nf * (double)F.m;   // per right-hand side and direction
+                wl1[k] = F.nf * (double)F.nf + F.nf * (double)F.m;
+            }
+            add_launch(&P, L.front_leaf, ids, tl1, fl1, wl1);
+        }
+        {
+            std::vector<int> tbig(nid);
+            std::vector<double> fbig(nid), wbig(nid);
+            for (size_t k = 0; k < nid; ++k) {
+                const HFront& F = h->fronts[ids[k]];
+                const int nb = P.nblocks[ids[k]];
+                big[k] = nb >= spk::FC_MINB && nb <= spk::FC * spk::FC_OWN;
+                tbig[k] = big[k] ? 1 : 0;
+                const double nf = F.nf;
+                fbig[k] = 2.0 * nf * nf;   // per right-hand side, both directions alike
+                wbig[k] = nf * nf;
+            }
+            add_launch(&P, L.front_big, ids, tbig, fbig, wbig);
+            for (size_t k = 0; k < nid; ++k) {
+                const HFront& F = h->fronts[ids[k]];
+                tbig[k] = big[k] && F.m > 0 ? cdiv(F.m, spk::L21_ROWS) * cdiv(F.nf, spk::L21_COLS) : 0;
+                fbig[k] = 2.0 * F.nf * (double)F.m;
+                wbig[k] = F.nf * (double)F.m;
+            }
+            add_launch(&P, L.front_l21, ids, tbig, fbig, wbig);
+        }
         std::vector<char> wide(maxb, 0);   // a block of the step is wider than 64 columns
         for (int id : ids)
             for (int t = 0; t < P.nblocks[id]; ++t)
@@ -676,6 +720,10 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
             }
             add_launch(&P, L.fwd[t], ids, tf, ff, wf);
             add_launch(&P, L.bwd[t], ids, tb, fb, wb);
+            for (size_t k = 0; k < nid; ++k)
+                if (big[k] || leaf[k]) tf[k] = tb[k] = 0;
+            add_launch(&P, L.fwd_small[t], ids, tf, ff, wf);
+            add_launch(&P, L.bwd_small[t], ids, tb, fb, wb);
         }
         std::vector<int> tsch(nid), tsch_tc(nid), tbu(nid);
         std::vector<double> fs(nid), ws(nid), fu(nid), wu(nid);
@@ -696,6 +744,9 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
         add_launch(&P, L.schur, ids, tsch, fs, ws);
         add_launch(&P, L.schur_tc, ids, tsch_tc, fs, ws);
         add_launch(&P, L.bwdu, ids, tbu, fu, wu);
+        for (size_t k = 0; k < nid; ++k)
+            if (leaf[k]) tbu[k] = 0;
+        add_launch(&P, L.bwdu_small, ids, tbu, fu, wu);
     }
 }
 
@@ -791,6 +842,10 @@ static int ensure_plan(spk_handle* h) {
                                (int)panel_smem<T, BM>()));
     CU(h, cudaFuncSetAttribute(spk::k_block_inv<T, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)sweep_smem<T, BM>(1)));
+    CU(h, cudaFuncSetAttribute(spk::k_front_solve<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)spk::FcSmem<T>::bytes));
+    CU(h, cudaFuncSetAttribute(spk::k_front_solve<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)spk::FcSmem<T>::bytes));
     if (std::is_same<T, float>::value) {
         CU(h, cudaFuncSetAttribute(spk::k_tc_update<spk::TC_TRAIL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    spk::umma::PSMEM));
@@ -1031,25 +1086,52 @@ static int run_solve_permuted(spk_handle* h, int nrhs, bool transpose) {
         CU(h, cudaGetLastError());
         return SPK_OK;
     }
-    for (const LevelPlan& P : PL.levels)
-        for (size_t t = 0; t < P.fwd.size(); ++t)
-            if (P.fwd[t].tiles > 0) {
-                LaunchScope ls(h, SPK_K_FWD, P.fwd[t].flops * nrhs, P.fwd[t].words * sizeof(T));
-                CU(h, launch_chained(spk::k_fwd<T>, P.fwd[t].tiles, spk::TS, 0, h->stream, fac, inv, b, y, n, nrhs, S,
-                                     launch_of(PL, P.fwd[t]), (int)t));
+    constexpr size_t fc_smem = spk::FcSmem<T>::bytes;
+    for (const LevelPlan& P : PL.levels) {
+        if (P.front_leaf.tiles > 0) {
+            LaunchScope ls(h, SPK_K_FWD, P.front_leaf.flops * nrhs, P.front_leaf.words * sizeof(T));
+            CU(h, launch_chained(spk::k_solve_leaf<T, true>, (P.front_leaf.count + 7) / 8, 256, 0, h->stream, fac, inv,
+                                 b, y, (const T*)nullptr, n, nrhs, S, launch_of(PL, P.front_leaf)));
+        }
+        if (P.front_big.tiles > 0) {
+            LaunchScope ls(h, SPK_K_FWD, P.front_big.flops * nrhs, P.front_big.words * sizeof(T));
+            spk::k_front_solve<T, true><<<spk::FC * P.front_big.tiles, spk::FC_THREADS, fc_smem, h->stream>>>(
+                fac, inv, b, y, n, nrhs, S, launch_of(PL, P.front_big));
+        }
+        if (P.front_l21.tiles > 0) {
+            LaunchScope ls(h, SPK_K_FWD, P.front_l21.flops * nrhs, P.front_l21.words * sizeof(T));
+            CU(h, launch_chained(spk::k_fwd_l21<T>, P.front_l21.tiles, 256, 0, h->stream, fac, b, (const T*)y, n, nrhs,
+                                 S, launch_of(PL, P.front_l21)));
+        }
+        for (size_t t = 0; t < P.fwd_small.size(); ++t)
+            if (P.fwd_small[t].tiles > 0) {
+                LaunchScope ls(h, SPK_K_FWD, P.fwd_small[t].flops * nrhs, P.fwd_small[t].words * sizeof(T));
+                CU(h, launch_chained(spk::k_fwd<T>, P.fwd_small[t].tiles, spk::TS, 0, h->stream, fac, inv, b, y, n,
+                                     nrhs, S, launch_of(PL, P.fwd_small[t]), (int)t));
             }
+    }
     for (size_t l = PL.levels.size(); l-- > 0;) {
         const LevelPlan& P = PL.levels[l];
-        if (P.bwdu.tiles > 0) {
-            LaunchScope ls(h, SPK_K_BWD, P.bwdu.flops * nrhs, P.bwdu.words * sizeof(T));
-            CU(h, launch_chained(spk::k_bwd_u12<T>, P.bwdu.tiles, 256, 0, h->stream, fac, y, x, n, nrhs, S,
-                                 launch_of(PL, P.bwdu)));
+        if (P.front_leaf.tiles > 0) {
+            LaunchScope ls(h, SPK_K_BWD, P.front_leaf.flops * nrhs, P.front_leaf.words * sizeof(T));
+            CU(h, launch_chained(spk::k_solve_leaf<T, false>, (P.front_leaf.count + 7) / 8, 256, 0, h->stream, fac, inv,
+                                 y, x, (const T*)x, n, nrhs, S, launch_of(PL, P.front_leaf)));
         }
-        for (size_t t = 0; t < P.bwd.size(); ++t)
-            if (P.bwd[t].tiles > 0) {
-                LaunchScope ls(h, SPK_K_BWD, P.bwd[t].flops * nrhs, P.bwd[t].words * sizeof(T));
-                CU(h, launch_chained(spk::k_bwd<T>, P.bwd[t].tiles, spk::TS, 0, h->stream, fac, inv, y, x, n, nrhs, S,
-                                     launch_of(PL, P.bwd[t]), (int)t));
+        if (P.bwdu_small.tiles > 0) {
+            LaunchScope ls(h, SPK_K_BWD, P.bwdu_small.flops * nrhs, P.bwdu_small.words * sizeof(T));
+            CU(h, launch_chained(spk::k_bwd_u12<T>, P.bwdu_small.tiles, 256, 0, h->stream, fac, y, x, n, nrhs, S,
+                                 launch_of(PL, P.bwdu_small)));
+        }
+        if (P.front_big.tiles > 0) {
+            LaunchScope ls(h, SPK_K_BWD, P.front_big.flops * nrhs, P.front_big.words * sizeof(T));
+            spk::k_front_solve<T, false><<<spk::FC * P.front_big.tiles, spk::FC_THREADS, fc_smem, h->stream>>>(
+                fac, inv, y, x, n, nrhs, S, launch_of(PL, P.front_big));
+        }
+        for (size_t t = 0; t < P.bwd_small.size(); ++t)
+            if (P.bwd_small[t].tiles > 0) {
+                LaunchScope ls(h, SPK_K_BWD, P.bwd_small[t].flops * nrhs, P.bwd_small[t].words * sizeof(T));
+                CU(h, launch_chained(spk::k_bwd<T>, P.bwd_small[t].tiles, spk::TS, 0, h->stream, fac, inv, y, x, n,
+                                     nrhs, S, launch_of(PL, P.bwd_small[t]), (int)t));
             }
     }
     CU(h, cudaGetLastError());

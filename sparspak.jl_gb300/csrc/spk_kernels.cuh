@@ -26,6 +26,7 @@
 // fronts.  Kernel boundaries are the only synchronisation.
 #pragma once
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -1857,6 +1858,313 @@ __global__ void __launch_bounds__(TS) k_bwd(const T* fac, const T* inv2, T* y, T
 #pragma unroll
             for (int j = 0; j < SC; ++j) acc += uv[j] * sx[r * SC + j];
             atomicAdd(&y[(ll)r * n + F.f + row], -acc);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Solves of a front with many blocks by a cluster of FC CTAs, all its block
+// steps in one launch.  Step t handles block t (forward) or block nb-1-t
+// (backward); CTA rank (t mod FC) owns step t: it holds that block's
+// right-hand side in shared memory, receives the updates of the earlier
+// steps there, and computes the step's solution (Minv b_B forward, Uinv c_B
+// backward).  The solution is published in the owner's shared memory; every
+// CTA reads it through distributed shared memory and subtracts its product
+// with the block's column of the factor (L below the block forward, U above
+// it backward) from the blocks it owns.  The operator of an owned step and
+// the block linking it to the previous step are prefetched into shared
+// memory while the earlier steps run.  One cluster barrier phase per step,
+// split: a CTA arrives as soon as it has read the step's solution (the
+// owner of the next step after publishing it), so that only the next
+// owner's work is on the chain.  Same operations as k_fwd / k_bwd per step
+// inside the front; forward, the R_F rows get L21 y_F afterwards from
+// k_fwd_l21 (all the GPU's SMs).  Right-hand sides FC_RG at a time.  Fronts
+// with at least FC_MINB and at most FC * FC_OWN blocks take this path (the
+// plan decides).
+// ---------------------------------------------------------------------------
+constexpr int FC = 8, FC_MINB = 4, FC_OWN = 16, FC_RG = 4, FC_THREADS = 1024;
+
+// Vectors of a block for FC_RG right-hand sides: entry (k, r) at k * FC_RG + r.
+template <typename T> struct RgVec;
+template <> struct RgVec<float> {
+    using type = float4;
+    __device__ static void get(const float* p, float (&v)[FC_RG]) {
+        const float4 q = *reinterpret_cast<const float4*>(p);
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    }
+};
+template <> struct RgVec<double> {
+    __device__ static void get(const double* p, double (&v)[FC_RG]) {
+        const double2 q0 = *reinterpret_cast<const double2*>(p), q1 = *reinterpret_cast<const double2*>(p + 2);
+        v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
+    }
+};
+
+template <typename T>
+struct FcSmem {
+    static constexpr int BM = BlockMax<T>::value, CS = FC_THREADS / BM;
+    static constexpr size_t ypub = 0, ycur = ypub + BM * FC_RG, own = ycur + BM * FC_RG,
+                            part = own + (size_t)FC_OWN * BM * FC_RG, preA = part + (size_t)CS * BM * FC_RG,
+                            preM = preA + (size_t)BM * BM, total = preM + (size_t)BM * BM;   // in T's
+    static constexpr size_t bytes = total * sizeof(T);
+};
+
+// v[i * FC_RG + r] -= sum_j A(i, j) w[j * FC_RG + r], i < nrow, j < ncol,
+// with A(i, j) = a[j * lda + i] (a block of the factor in global memory, or
+// its prefetched copy in shared memory).  Thread (i, cs) takes columns
+// cs, cs + CS, ...; all its loads are issued before the first use.
+template <typename T>
+__device__ __forceinline__ void fc_tile_update(const T* a, ll lda, int nrow, int ncol, T* v, const T* w, T* part) {
+    constexpr int BM = BlockMax<T>::value, CS = FC_THREADS / BM, NJ = BM / CS;
+    const int i = threadIdx.x % BM, cs = threadIdx.x / BM;
+    T av[NJ];
+#pragma unroll
+    for (int q = 0; q < NJ; ++q) {
+        const int j = cs + q * CS;
+        av[q] = (i < nrow && j < ncol) ? a[(ll)j * lda + i] : T(0);
+    }
+    T acc[FC_RG];
+#pragma unroll
+    for (int r = 0; r < FC_RG; ++r) acc[r] = T(0);
+#pragma unroll
+    for (int q = 0; q < NJ; ++q) {
+        T wv[FC_RG];
+        RgVec<T>::get(w + (cs + q * CS) * FC_RG, wv);
+#pragma unroll
+        for (int r = 0; r < FC_RG; ++r) acc[r] += av[q] * wv[r];
+    }
+#pragma unroll
+    for (int r = 0; r < FC_RG; ++r) part[(cs * BM + i) * FC_RG + r] = acc[r];
+    __syncthreads();
+    for (int e = threadIdx.x; e < nrow * FC_RG; e += FC_THREADS) {
+        T sum = T(0);
+#pragma unroll
+        for (int c = 0; c < CS; ++c) sum += part[c * BM * FC_RG + e];
+        v[e] -= sum;
+    }
+    __syncthreads();
+}
+
+// out[j * FC_RG + r] = sum_k op(j, k) v[k * FC_RG + r] for the block's solve
+// operator (forward Minv, backward Uinv; op(j, k) at m[k * BM + j]).
+template <typename T, bool FWD>
+__device__ __forceinline__ void fc_block_solve(const T* m, int bw, const T* v, T* out, T* part, int nr) {
+    constexpr int BM = BlockMax<T>::value, CS = FC_THREADS / BM;
+    const int j = threadIdx.x % BM, cs = threadIdx.x / BM;
+    T acc[FC_RG];
+#pragma unroll
+    for (int r = 0; r < FC_RG; ++r) acc[r] = T(0);
+    if (j < bw) {
+#pragma unroll 4
+        for (int k = (FWD ? 0 : j) + cs; k < bw; k += CS) {
+            const T mv = m[k * BM + j];
+            T vv[FC_RG];
+            RgVec<T>::get(v + k * FC_RG, vv);
+#pragma unroll
+            for (int r = 0; r < FC_RG; ++r) acc[r] += mv * vv[r];
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < FC_RG; ++r) part[(cs * BM + j) * FC_RG + r] = acc[r];
+    __syncthreads();
+    for (int e = threadIdx.x; e < BM * FC_RG; e += FC_THREADS) {
+        const int jj = e / FC_RG, r = e % FC_RG;
+        T sum = T(0);
+        if (jj < bw && r < nr)
+#pragma unroll
+            for (int c = 0; c < CS; ++c) sum += part[c * BM * FC_RG + e];
+        out[e] = sum;
+    }
+    __syncthreads();
+}
+
+template <typename T, bool FWD>
+__global__ void __cluster_dims__(FC, 1, 1) __launch_bounds__(FC_THREADS, 1)
+    k_front_solve(const T* fac, const T* inv2, T* in, T* out, int n, int nrhs, Sched S, Launch L) {
+    namespace cg = cooperative_groups;
+    constexpr int BM = BlockMax<T>::value;
+    using SM = FcSmem<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sm = reinterpret_cast<T*>(smem_raw);
+    T* ypub = sm + SM::ypub;
+    T* ycur = sm + SM::ycur;
+    T* own = sm + SM::own;
+    T* part = sm + SM::part;
+    T* preA = sm + SM::preA;   // A(block of step st, block of step st - 1), [j * BM + i]
+    T* preM = sm + SM::preM;   // solve operator of step st, [k * BM + j]
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const DFront F = S.fronts[L.front_ids[blockIdx.x / FC]];
+    const int nb = F.nblocks, tid = threadIdx.x;
+    auto blk_of = [&](int step) { return F.block0 + (FWD ? step : nb - 1 - step); };
+    auto a_of = [&](int bs, int bt) { return fac + F.loff + (ll)S.blk_c0[bt] * F.ld + S.blk_c0[bs]; };
+    // The factor data of owned step st (its operator, and the block linking
+    // it to step st - 1) is copied asynchronously while other steps run.
+    auto prefetch = [&](int st) {
+        if (st >= nb) return;
+        const int bs = blk_of(st), bw = S.blk_c1[bs] - S.blk_c0[bs];
+        const T* Mi = inv2 + S.blk_inv2[bs] + (FWD ? 0 : (ll)bw * bw);
+        for (int e = tid; e < BM * BM; e += FC_THREADS) {
+            const int j = e % BM, k = e / BM;
+            const bool v = j < bw && k < bw;
+            cp_elem(&preM[e], v ? Mi + (ll)k * bw + j : Mi, v);
+        }
+        if (st > 0) {
+            const int bt = blk_of(st - 1), ncol = S.blk_c1[bt] - S.blk_c0[bt];
+            const T* a = a_of(bs, bt);
+            for (int e = tid; e < BM * BM; e += FC_THREADS) {
+                const int i = e % BM, j = e / BM;
+                const bool v = i < bw && j < ncol;
+                cp_elem(&preA[e], v ? a + (ll)j * F.ld + i : a, v);
+            }
+        }
+    };
+    for (int r0 = 0; r0 < nrhs; r0 += FC_RG) {
+        const int nr = min(FC_RG, nrhs - r0);
+        prefetch(rank);
+        for (int st = rank, o = 0; st < nb; st += FC, ++o) {   // the owned blocks' right-hand sides
+            const int blk = blk_of(st), c0 = S.blk_c0[blk], bw = S.blk_c1[blk] - c0;
+            T* v = own + (size_t)o * BM * FC_RG;
+            for (int e = tid; e < BM * FC_RG; e += FC_THREADS) {
+                const int k = e / FC_RG, r = e % FC_RG;
+                v[e] = (k < bw && r < nr) ? in[(ll)(r0 + r) * n + F.f + c0 + k] : T(0);
+            }
+        }
+        __syncthreads();
+        auto solve_step = [&](int st) {   // owner: publish the solution of step st
+            const int blk = blk_of(st), c0 = S.blk_c0[blk], bw = S.blk_c1[blk] - c0;
+            fc_block_solve<T, FWD>(preM, bw, own + (size_t)(st / FC) * BM * FC_RG, ypub, part, nr);
+            for (int e = tid; e < bw * nr; e += FC_THREADS) {
+                const int j = e % bw, r = e / bw;
+                out[(ll)(r0 + r) * n + F.f + c0 + j] = ypub[j * FC_RG + r];
+            }
+            prefetch(st + FC);   // preM / preA are free again
+        };
+        if (rank == 0) {
+            cp_wait_all();
+            __syncthreads();
+            solve_step(0);
+        }
+        cl.barrier_arrive();
+        for (int t = 0; t < nb; ++t) {
+            cl.barrier_wait();
+            const T* src = cl.map_shared_rank(ypub, t % FC);
+            for (int e = tid; e < BM * FC_RG; e += FC_THREADS) ycur[e] = src[e];
+            __syncthreads();
+            const int bt = blk_of(t), ncol = S.blk_c1[bt] - S.blk_c0[bt];
+            const bool next = t + 1 < nb && (t + 1) % FC == rank;
+            if (next) {   // the next step's block first, from its prefetched copy: it is on the chain
+                cp_wait_all();
+                __syncthreads();
+                const int bs = blk_of(t + 1);
+                fc_tile_update<T>(preA, BM, S.blk_c1[bs] - S.blk_c0[bs], ncol,
+                                  own + (size_t)((t + 1) / FC) * BM * FC_RG, ycur, part);
+                solve_step(t + 1);
+            }
+            cl.barrier_arrive();
+            for (int st = rank, o = 0; st < nb; st += FC, ++o)
+                if (st > t && !(next && st == t + 1)) {
+                    const int bs = blk_of(st);
+                    fc_tile_update<T>(a_of(bs, bt), F.ld, S.blk_c1[bs] - S.blk_c0[bs], ncol,
+                                      own + (size_t)o * BM * FC_RG, ycur, part);
+                }
+            __syncthreads();
+        }
+        cl.barrier_wait();   // every CTA has read every published solution
+        cp_wait_all();   // no copy outlives the group
+        __syncthreads();
+    }
+}
+
+// Solves of small fronts (one block of at most 32 columns, m <= LEAF_M), one
+// warp per front, eight fronts per CTA: the whole front in one pass.
+//   forward:  y_F = Minv b_F; b[R_F] -= L21 y_F (atomics, the rows are
+//             shared with sibling fronts);
+//   backward: c_F = y_F - U12 x[R_F]; x_F = Uinv c_F.
+// Lane j holds column j of the front; the front's right-hand side values are
+// exchanged by shuffles.  Same operations as k_fwd / k_bwd_u12 / k_bwd.
+constexpr int LEAF_M = 128;
+template <typename T, bool FWD>
+__global__ void __launch_bounds__(256) k_solve_leaf(const T* fac, const T* inv2, T* in, T* out, const T* xs, int n,
+                                                     int nrhs, Sched S, Launch L) {
+    griddep_launch();
+    const int lane = threadIdx.x & 31, idx = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (idx >= L.count) return;   // whole warp
+    const DFront F = S.fronts[L.front_ids[idx]];
+    const int blk = F.block0, bw = F.nf;
+    const T* Mi = inv2 + S.blk_inv2[blk] + (FWD ? 0 : (ll)bw * bw);
+    const int* rows = S.rows + F.rows_off;
+    griddep_wait();
+    for (int r = 0; r < nrhs; ++r) {
+        T v = lane < bw ? in[(ll)r * n + F.f + lane] : T(0);
+        if constexpr (!FWD) {   // c_F = y_F - U12 x[R_F] (U12 row j contiguous in Uf)
+            if (lane < bw) {
+                const T* u = fac + F.uoff + (ll)lane * F.m;
+                T acc = T(0);
+#pragma unroll 4
+                for (int i = 0; i < F.m; ++i) acc += u[i] * xs[(ll)r * n + rows[i]];
+                v -= acc;
+            }
+        }
+        T y = T(0);   // lane j: sum_k op(j, k) v_k, op(j, k) at Mi[k * bw + j]
+        for (int k = (FWD ? 0 : 0); k < bw; ++k) {
+            const T vk = __shfl_sync(0xffffffffu, v, k);
+            if (lane < bw && (FWD || k >= lane)) y += Mi[(ll)k * bw + lane] * vk;
+        }
+        if (lane < bw) out[(ll)r * n + F.f + lane] = y;
+        if constexpr (FWD) {   // b[R_F] -= L21 y_F (L21 column k contiguous in Lf)
+            for (int i0 = 0; i0 < F.m; i0 += 32) {
+                const int i = i0 + lane;
+                T acc = T(0);
+                for (int k = 0; k < bw; ++k) {
+                    const T yk = __shfl_sync(0xffffffffu, y, k);
+                    if (i < F.m) acc += fac[F.loff + (ll)k * F.ld + F.nf + i] * yk;
+                }
+                if (i < F.m) atomicAdd(&in[(ll)r * n + rows[i]], -acc);
+            }
+        }
+    }
+}
+
+// Forward, after k_front_solve: b[R_F] -= L21 y_F for the fronts it solved.
+// Tiles of 256 R_F rows x 128 front columns; a thread takes one row
+// (L21 column k contiguous in Lf), y_F of the tile's columns in shared
+// memory, partial sums added to b with atomics.
+constexpr int L21_ROWS = 256, L21_COLS = 128;
+template <typename T>
+__global__ void __launch_bounds__(256) k_fwd_l21(const T* fac, T* b, const T* y, int n, int nrhs, Sched S, Launch L) {
+    __shared__ T sy[L21_COLS * FC_RG];
+    griddep_launch();
+    int fid, tile;
+    locate(L, blockIdx.x, fid, tile);
+    const DFront F = S.fronts[fid];
+    const int nrt = cdiv(F.m, L21_ROWS), i0 = (tile % nrt) * L21_ROWS, k0 = (tile / nrt) * L21_COLS;
+    const int nk = min(L21_COLS, F.nf - k0), i = i0 + threadIdx.x;
+    const bool ok = i < F.m;
+    const int grow = ok ? S.rows[F.rows_off + i] : 0;
+    const T* a = fac + F.loff + (ll)k0 * F.ld + F.nf + (ok ? i : 0);
+    griddep_wait();
+    for (int r0 = 0; r0 < nrhs; r0 += FC_RG) {
+        const int nr = min(FC_RG, nrhs - r0);
+        if (r0 > 0) __syncthreads();
+        for (int e = threadIdx.x; e < L21_COLS * FC_RG; e += blockDim.x) {
+            const int k = e % L21_COLS, r = e / L21_COLS;
+            sy[e] = (k < nk && r < nr) ? y[(ll)(r0 + r) * n + F.f + k0 + k] : T(0);
+        }
+        __syncthreads();
+        T acc[FC_RG];
+#pragma unroll
+        for (int r = 0; r < FC_RG; ++r) acc[r] = T(0);
+        if (ok) {
+#pragma unroll 16
+            for (int k = 0; k < nk; ++k) {
+                const T av = a[(ll)k * F.ld];
+#pragma unroll
+                for (int r = 0; r < FC_RG; ++r) acc[r] += av * sy[r * L21_COLS + k];
+            }
+#pragma unroll
+            for (int r = 0; r < FC_RG; ++r)
+                if (r < nr) atomicAdd(&b[(ll)(r0 + r) * n + grow], -acc[r]);
         }
     }
 }
