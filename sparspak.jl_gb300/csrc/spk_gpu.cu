@@ -169,6 +169,7 @@ struct spk_handle {
     // trailing update runs on `side` while the next block LU runs on the
     // launch stream (evP: panels done; evB: trailing update done).
     cudaStream_t side = nullptr;
+    bool fc16 = false;   // front solves by clusters of 16 CTAs
     cudaEvent_t evP = nullptr, evB = nullptr;
     int device = -1;
     int nsm = 1;                 // SMs of the device (grid of the persistent kernels)
@@ -842,10 +843,37 @@ static int ensure_plan(spk_handle* h) {
                                (int)panel_smem<T, BM>()));
     CU(h, cudaFuncSetAttribute(spk::k_block_inv<T, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)sweep_smem<T, BM>(1)));
-    CU(h, cudaFuncSetAttribute(spk::k_front_solve<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    CU(h, cudaFuncSetAttribute(spk::k_front_solve<T, true, spk::FC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)spk::FcSmem<T>::bytes));
-    CU(h, cudaFuncSetAttribute(spk::k_front_solve<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    CU(h, cudaFuncSetAttribute(spk::k_front_solve<T, false, spk::FC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)spk::FcSmem<T>::bytes));
+    {   // clusters of 16 (a non-portable size) where the GPU can hold one
+        h->fc16 = false;
+        auto k16f = spk::k_front_solve<T, true, 16>;
+        auto k16b = spk::k_front_solve<T, false, 16>;
+        if (cudaFuncSetAttribute(k16f, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+            cudaFuncSetAttribute(k16b, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+            cudaFuncSetAttribute(k16f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spk::FcSmem<T>::bytes) ==
+                cudaSuccess &&
+            cudaFuncSetAttribute(k16b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spk::FcSmem<T>::bytes) ==
+                cudaSuccess) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(16);
+            cfg.blockDim = dim3(spk::FC_THREADS);
+            cfg.dynamicSmemBytes = spk::FcSmem<T>::bytes;
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = 16;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            int nclusters = 0;
+            if (cudaOccupancyMaxActiveClusters(&nclusters, (void*)k16f, &cfg) == cudaSuccess && nclusters >= 1)
+                h->fc16 = true;
+        }
+        cudaGetLastError();   // a refused query leaves clusters of 8
+    }
     if (std::is_same<T, float>::value) {
         CU(h, cudaFuncSetAttribute(spk::k_tc_update<spk::TC_TRAIL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    spk::umma::PSMEM));
@@ -1095,8 +1123,12 @@ static int run_solve_permuted(spk_handle* h, int nrhs, bool transpose) {
         }
         if (P.front_big.tiles > 0) {
             LaunchScope ls(h, SPK_K_FWD, P.front_big.flops * nrhs, P.front_big.words * sizeof(T));
-            spk::k_front_solve<T, true><<<spk::FC * P.front_big.tiles, spk::FC_THREADS, fc_smem, h->stream>>>(
-                fac, inv, b, y, n, nrhs, S, launch_of(PL, P.front_big));
+            if (h->fc16)
+                spk::k_front_solve<T, true, 16><<<16 * P.front_big.tiles, spk::FC_THREADS, fc_smem, h->stream>>>(
+                    fac, inv, b, y, n, nrhs, S, launch_of(PL, P.front_big));
+            else
+                spk::k_front_solve<T, true, spk::FC><<<spk::FC * P.front_big.tiles, spk::FC_THREADS, fc_smem,
+                                                       h->stream>>>(fac, inv, b, y, n, nrhs, S, launch_of(PL, P.front_big));
         }
         if (P.front_l21.tiles > 0) {
             LaunchScope ls(h, SPK_K_FWD, P.front_l21.flops * nrhs, P.front_l21.words * sizeof(T));
@@ -1124,8 +1156,12 @@ static int run_solve_permuted(spk_handle* h, int nrhs, bool transpose) {
         }
         if (P.front_big.tiles > 0) {
             LaunchScope ls(h, SPK_K_BWD, P.front_big.flops * nrhs, P.front_big.words * sizeof(T));
-            spk::k_front_solve<T, false><<<spk::FC * P.front_big.tiles, spk::FC_THREADS, fc_smem, h->stream>>>(
-                fac, inv, y, x, n, nrhs, S, launch_of(PL, P.front_big));
+            if (h->fc16)
+                spk::k_front_solve<T, false, 16><<<16 * P.front_big.tiles, spk::FC_THREADS, fc_smem, h->stream>>>(
+                    fac, inv, y, x, n, nrhs, S, launch_of(PL, P.front_big));
+            else
+                spk::k_front_solve<T, false, spk::FC><<<spk::FC * P.front_big.tiles, spk::FC_THREADS, fc_smem,
+                                                        h->stream>>>(fac, inv, y, x, n, nrhs, S, launch_of(PL, P.front_big));
         }
         for (size_t t = 0; t < P.bwd_small.size(); ++t)
             if (P.bwd_small[t].tiles > 0) {

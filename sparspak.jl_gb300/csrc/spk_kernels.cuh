@@ -1863,8 +1863,9 @@ __global__ void __launch_bounds__(TS) k_bwd(const T* fac, const T* inv2, T* y, T
 }
 
 // ---------------------------------------------------------------------------
-// Solves of a front with many blocks by a cluster of FC CTAs, all its block
-// steps in one launch.  Step t handles block t (forward) or block nb-1-t
+// Solves of a front with many blocks by a cluster of NC CTAs (16 where the
+// GPU can hold such clusters, else FC = 8), all its block steps in one
+// launch.  Step t handles block t (forward) or block nb-1-t
 // (backward); CTA rank (t mod FC) owns step t: it holds that block's
 // right-hand side in shared memory, receives the updates of the earlier
 // steps there, and computes the step's solution (Minv b_B forward, Uinv c_B
@@ -1978,9 +1979,10 @@ __device__ __forceinline__ void fc_block_solve(const T* m, int bw, const T* v, T
     __syncthreads();
 }
 
-template <typename T, bool FWD>
-__global__ void __cluster_dims__(FC, 1, 1) __launch_bounds__(FC_THREADS, 1)
+template <typename T, bool FWD, int NC>
+__global__ void __cluster_dims__(NC, 1, 1) __launch_bounds__(FC_THREADS, 1)
     k_front_solve(const T* fac, const T* inv2, T* in, T* out, int n, int nrhs, Sched S, Launch L) {
+    constexpr int FC = NC;   // CTAs of the cluster
     namespace cg = cooperative_groups;
     constexpr int BM = BlockMax<T>::value;
     using SM = FcSmem<T>;

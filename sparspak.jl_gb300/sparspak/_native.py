@@ -60,7 +60,8 @@ SPK_HOST, SPK_DEVICE = 0, 1
 KERNEL_CLASSES = ["assemble", "getrf", "panel", "trail", "schur", "fwd", "bwd", "permute", "residual", "blockinv"]
 KERNEL_NAMES = {"assemble": "k_scatter_values", "getrf": "k_block_lu+k_block_lu_small", "panel": "k_block_panel",
                 "trail": "k_tc_update<TC_TRAIL>+k_block_trail", "schur": "k_tc_update<TC_SCHUR>+k_schur",
-                "fwd": "k_fwd", "bwd": "k_bwd_u12+k_bwd", "permute": "k_permute+k_unpermute",
+                "fwd": "k_fwd+k_front_solve<fwd>+k_fwd_l21+k_solve_leaf<fwd>",
+                "bwd": "k_bwd_u12+k_bwd+k_front_solve<bwd>+k_solve_leaf<bwd>", "permute": "k_permute+k_unpermute",
                 "residual": "k_residual", "blockinv": "k_block_inv"}
 # How each class's FP32 form computes: tensor cores (tcgen05, 3xTF32) or CUDA cores.
 KERNEL_UNITS = {"trail": "tcgen05 3xTF32 (fronts with a pack) + FP32 FMA", "schur": "tcgen05 3xTF32 (fronts with a pack) + FP32 FMA",
