@@ -60,6 +60,7 @@ struct LevelPlan {
     // Solves: fronts with many blocks by one cluster launch each direction
     // (front_big, one tile per front), the others by block steps
     // (fwd_small / bwd_small); the transposed solves use fwd / bwd.
+    LaunchRec leaf_factor;            // fronts factored whole by k_leaf_factor (a warp each)
     LaunchRec front_big, front_l21;   // front_l21: tiles of k_fwd_l21 for the front_big fronts
     // Small fronts (one block of at most 32 columns, m <= spk::LEAF_M) by
     // k_solve_leaf, a warp per front; bwdu_small: U12 products of the others.
@@ -652,6 +653,20 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
             }
             add_launch(&P, L.front_l21, ids, tbig, fbig, wbig);
         }
+        std::vector<char> leafF(nid, 0);   // factored whole by k_leaf_factor
+        {
+            std::vector<int> tlf(nid);
+            std::vector<double> flf(nid), wlf(nid);
+            for (size_t k = 0; k < nid; ++k) {
+                const HFront& F = h->fronts[ids[k]];
+                leafF[k] = P.nblocks[ids[k]] == 1 && F.nf <= 32 && F.m <= spk::LF_M;
+                tlf[k] = leafF[k] ? 1 : 0;
+                const double nf = F.nf, m = F.m;
+                flf[k] = 2.0 * nf * nf * nf + 3.0 * nf * nf * m + 2.0 * m * m * nf;
+                wlf[k] = nf * nf + 2.0 * nf * m + m * m;
+            }
+            add_launch(&P, L.leaf_factor, ids, tlf, flf, wlf);
+        }
         std::vector<char> wide(maxb, 0);   // a block of the step is wider than 64 columns
         for (int id : ids)
             for (int t = 0; t < P.nblocks[id]; ++t)
@@ -667,11 +682,11 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
                 const int c0 = P.blk_c0[blk], c1 = P.blk_c1[blk];
                 const double bw = c1 - c0;
                 const int ld = F.nf + F.m;
-                tl[k] = 1;
+                tl[k] = leafF[k] ? 0 : 1;
                 fl[k] = 2.0 * bw * bw * bw;
                 wl[k] = 4.0 * bw * bw;
                 const int lpt = panel_lines(tc, wide[t]);
-                tp[k] = cdiv(ld - c1, lpt) + cdiv(F.nf - c1, lpt) + cdiv(F.m, lpt);
+                tp[k] = leafF[k] ? 0 : cdiv(ld - c1, lpt) + cdiv(F.nf - c1, lpt) + cdiv(F.m, lpt);
                 const double rowsL = ld - c1, colsU = (double)(F.nf - c1) + F.m;
                 fp[k] = bw * bw * rowsL + 2.0 * bw * bw * colsU;
                 wp[k] = 2.0 * bw * (rowsL + colsU) + 2.0 * bw * bw;
@@ -730,7 +745,7 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
         std::vector<double> fs(nid), ws(nid), fu(nid), wu(nid);
         for (size_t k = 0; k < nid; ++k) {
             const HFront& F = h->fronts[ids[k]];
-            tsch[k] = F.m > 0 ? cdiv(F.m, spk::TT) * cdiv(F.m, spk::TT) : 0;
+            tsch[k] = F.m > 0 && !leafF[k] ? cdiv(F.m, spk::TT) * cdiv(F.m, spk::TT) : 0;
             tsch_tc[k] = 0;
             if (F.m > 0 && P.blk_lpack[P.block0[ids[k]]] >= 0) {
                 tsch_tc[k] = cdiv(F.m, spk::umma::TM) * cdiv(F.m, spk::umma::TN);
@@ -843,6 +858,8 @@ static int ensure_plan(spk_handle* h) {
                                (int)panel_smem<T, BM>()));
     CU(h, cudaFuncSetAttribute(spk::k_block_inv<T, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)sweep_smem<T, BM>(1)));
+    CU(h, cudaFuncSetAttribute(spk::k_leaf_factor<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)spk::LeafSmem<T>::bytes));
     CU(h, cudaFuncSetAttribute(spk::k_front_solve<T, true, spk::FC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)spk::FcSmem<T>::bytes));
     CU(h, cudaFuncSetAttribute(spk::k_front_solve<T, false, spk::FC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -967,6 +984,12 @@ static int factor_launches(spk_handle* h) {
     const bool ahead = h->prof_mask == 0;
     bool pending = false;
     for (const LevelPlan& P : PL.levels) {
+        if (P.leaf_factor.tiles > 0) {
+            LaunchScope ls(h, SPK_K_GETRF, P.leaf_factor.flops, P.leaf_factor.words * sizeof(T));
+            spk::k_leaf_factor<T><<<(P.leaf_factor.count + spk::LF_WARPS - 1) / spk::LF_WARPS, 32 * spk::LF_WARPS,
+                                    spk::LeafSmem<T>::bytes, h->stream>>>(fac, h->d_ipiv, h->d_info, S,
+                                                                          launch_of(PL, P.leaf_factor));
+        }
         for (size_t t = 0; t < P.blu.size(); ++t) {
             const int bw = P.blu[t].bw;
             if (P.blu[t].tiles > 0) {

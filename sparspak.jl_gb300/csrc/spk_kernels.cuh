@@ -1275,6 +1275,139 @@ __device__ __forceinline__ ScatterRow scatter_row(const Sched& S, const DFront& 
     return e;
 }
 
+// Small fronts (one block of at most 32 columns, m <= LF_M) factored whole
+// by one warp each, four per CTA: the block LU of k_block_lu_small, then
+// the L21 rows (x := x U^-1, a lane per row), the U12 columns (interchanges
+// of the block, then u := L^-1 u, a lane per column), both in the entry
+// order of the panel sweeps, and the Schur complement L21 U12 (k in order)
+// scatter-subtracted into the ancestors like k_schur.  Replaces, for these
+// fronts, k_block_lu_small + k_block_panel + k_schur (three launches whose
+// CTAs would be mostly idle on fronts this small).
+constexpr int LF_M = 64, LF_WARPS = 4, LF_LD = 33;
+template <typename T> struct LeafSmem {
+    static constexpr size_t warp_bytes = (size_t)(32 + LF_M) * LF_LD * sizeof(T) + LF_M * sizeof(ScatterRow) +
+                                         32 * sizeof(T) + (33 + 3 * 32) * sizeof(int);
+    static constexpr size_t bytes = LF_WARPS * ((warp_bytes + 15) / 16 * 16);
+};
+
+template <typename T>
+__global__ void __launch_bounds__(32 * LF_WARPS) k_leaf_factor(T* fac, int* ipiv, int* info, Sched S, Launch L) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char* base = smem_raw + (size_t)warp * ((LeafSmem<T>::warp_bytes + 15) / 16 * 16);
+    ScatterRow* tab = reinterpret_cast<ScatterRow*>(base);
+    T* sD = reinterpret_cast<T*>(tab + LF_M);          // diagonal block, D(i, j) at sD[j * LF_LD + i]
+    T* sL = sD + 32 * LF_LD;                           // L21 rows, L21(r, k) at sL[r * LF_LD + k]
+    T* srv = sL + LF_M * LF_LD;                        // 1 / U(k, k)
+    int* q0 = reinterpret_cast<int*>(srv + 32);
+    int* piv = q0 + 33;
+    int* gm = piv + 32;
+    int* pam = gm + 32;
+    const int idx = blockIdx.x * LF_WARPS + warp;
+    if (idx >= L.count) return;   // whole warp; the kernel has no CTA barrier
+    const DFront F = S.fronts[L.front_ids[idx]];
+    const int blk = F.block0, bw = F.nf, m = F.m;
+    const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
+    for (int k = lane; k <= np; k += 32) q0[k] = S.xsuper[p0 + k] - F.f;
+    for (int j = 0; j < bw; ++j)
+        if (lane < bw) sD[j * LF_LD + lane] = fac[F.loff + (ll)j * F.ld + lane];
+    for (int x = lane; x < m; x += 32) tab[x] = scatter_row<T>(S, F, x);
+    __syncwarp();
+    // block LU (ggetrf! pivots inside each piece)
+    const bool sing = warp_block_lu32(sD, LF_LD, bw, q0, np, piv);
+    for (int j = 0; j < bw; ++j)
+        if (lane < bw) fac[F.loff + (ll)j * F.ld + lane] = sD[j * LF_LD + lane];
+    if (lane < bw) {
+        ipiv[F.f + lane] = piv[lane];
+        srv[lane] = rcp_rn(sD[lane * LF_LD + lane]);   // as the panel's 1 / U(k, k)
+    }
+    if (lane == 0 && sing) {
+        for (int pc = 0; pc < np; ++pc) {
+            bool z = false;
+            for (int k = q0[pc]; k < q0[pc + 1]; ++k) z |= sD[k * LF_LD + k] == T(0);
+            if (z) { atomicMin(info, p0 + pc + 1); break; }
+        }
+    }
+    for (int pc = lane; pc < np; pc += 32) {   // row sources of the interchanges (block_gather_map)
+        const int a = q0[pc], b = q0[pc + 1];
+        for (int i = a; i < b; ++i) {
+            gm[i] = i;
+            pam[i] = a;
+        }
+        for (int k = a; k < b; ++k) {
+            const int kp = a + piv[k];
+            const int t = gm[k];
+            gm[k] = gm[kp];
+            gm[kp] = t;
+        }
+    }
+    __syncwarp();
+    // L21 rows: x := x U^-1 (left-looking: entry j gets k = 0, 1, .. then its scaling)
+    for (int r = lane; r < m; r += 32) {
+        T x[32];
+#pragma unroll
+        for (int k = 0; k < 32; ++k) x[k] = k < bw ? fac[F.loff + (ll)k * F.ld + bw + r] : T(0);
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            if (j < bw) {
+#pragma unroll
+                for (int k = 0; k < j; ++k) x[j] -= x[k] * sD[j * LF_LD + k];
+                x[j] *= srv[j];
+            }
+#pragma unroll
+        for (int k = 0; k < 32; ++k)
+            if (k < bw) {
+                fac[F.loff + (ll)k * F.ld + bw + r] = x[k];
+                sL[r * LF_LD + k] = x[k];
+            }
+    }
+    // U12 columns: y := inv(L) P y; then the Schur complement, a lane per column
+    T y[2][32];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int c = lane + 32 * h;
+#pragma unroll
+        for (int k = 0; k < 32; ++k) y[h][k] = (c < m && k < bw) ? fac[F.uoff + (ll)gm[k] * m + c] : T(0);
+#pragma unroll
+        for (int i = 0; i < 32; ++i)
+            if (i < bw) {
+#pragma unroll
+                for (int k = 0; k < i; ++k) {
+                    const T l = k < pam[i] ? sD[k * LF_LD + gm[i]] : sD[k * LF_LD + i];
+                    y[h][i] -= l * y[h][k];
+                }
+            }
+        if (c < m)
+#pragma unroll
+            for (int k = 0; k < 32; ++k)
+                if (k < bw) fac[F.uoff + (ll)k * m + c] = y[h][k];
+    }
+    __syncwarp();
+    for (int r = 0; r < m; ++r) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int c = lane + 32 * h;
+            if (c >= m) continue;
+            T acc = T(0);
+#pragma unroll
+            for (int k = 0; k < 32; ++k)
+                if (k < bw) acc += sL[r * LF_LD + k] * y[h][k];
+            if (r >= c) {   // L entry of the front of R_F[c]
+                const ScatterRow& Cc = tab[c];
+                const int p = S.rel[Cc.rel0 + r];
+                if (Cc.pos >= 0 && p >= 0) atomicAdd(&fac[Cc.loff + (ll)Cc.pos * Cc.ld + p], -acc);
+            } else {        // entry of the front of R_F[r]
+                const ScatterRow& R = tab[r];
+                const int p = S.rel[R.rel0 + c];
+                if (R.pos >= 0 && p >= 0) {
+                    const ll addr = p < R.nf ? R.loff + (ll)p * R.ld + R.pos : R.uoff + (ll)R.pos * R.m + (p - R.nf);
+                    atomicAdd(&fac[addr], -acc);
+                }
+            }
+        }
+    }
+}
+
 // Schur complement of every front in the launch: C = L21 * U12 (m x m,
 // inner dimension nf), scatter-subtracted into the ancestors.  An entry
 // (r, c) of C belongs to the front of column R_F[c] when r >= c (an L
