@@ -334,7 +334,8 @@ def run_ours(args):
 
     def traffic_of(cls):
         """DRAM bytes per launch of the class's FP32 kernels from the committed ncu summary (40^3 capture)."""
-        names = {"getrf": ("k_block_lu<float>", "k_block_lu_small<float>"), "panel": ("k_block_panel<float",),
+        names = {"getrf": ("k_block_lu<float>", "k_block_lu_small<float>", "k_leaf_factor<float>"),
+                 "panel": ("k_block_panel<float",),
                  "trail": ("k_tc_update<0>", "k_block_trail<float>"), "schur": ("k_tc_update<1>", "k_schur<float>"),
                  "fwd": ("k_fwd<float>", "k_front_solve<float, 1>", "k_fwd_l21<float>", "k_solve_leaf<float, 1>"),
                  "bwd": ("k_bwd<float>", "k_bwd_u12<float>", "k_front_solve<float, 0>", "k_solve_leaf<float, 0>")}.get(cls, ())
