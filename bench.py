@@ -337,8 +337,8 @@ def run_ours(args):
         names = {"getrf": ("k_block_lu<float>", "k_block_lu_small<float>", "k_leaf_factor<float>"),
                  "panel": ("k_block_panel<float",),
                  "trail": ("k_tc_update<0>", "k_block_trail<float>"), "schur": ("k_tc_update<1>", "k_schur<float>"),
-                 "fwd": ("k_fwd<float>", "k_front_solve<float, 1>", "k_fwd_l21<float>", "k_solve_leaf<float, 1>"),
-                 "bwd": ("k_bwd<float>", "k_bwd_u12<float>", "k_front_solve<float, 0>", "k_solve_leaf<float, 0>")}.get(cls, ())
+                 "fwd": ("k_fwd<float>", "k_front_solve<float, 1,", "k_fwd_l21<float>", "k_solve_leaf<float, 1>"),
+                 "bwd": ("k_bwd<float>", "k_bwd_u12<float>", "k_front_solve<float, 0,", "k_solve_leaf<float, 0>")}.get(cls, ())
         path = os.path.join(ROOT, "profiles", "dram_traffic_laplace3d40_mixed_step.md")
         if not names or not os.path.exists(path):
             return None, None

@@ -2222,6 +2222,7 @@ constexpr int LEAF_M = 128;
 template <typename T, bool FWD>
 __global__ void __launch_bounds__(256) k_solve_leaf(const T* fac, const T* inv2, T* in, T* out, const T* xs, int n,
                                                      int nrhs, Sched S, Launch L) {
+    constexpr int RG = 4;   // right-hand sides per pass
     griddep_launch();
     const int lane = threadIdx.x & 31, idx = blockIdx.x * 8 + (threadIdx.x >> 5);
     if (idx >= L.count) return;   // whole warp
@@ -2230,32 +2231,66 @@ __global__ void __launch_bounds__(256) k_solve_leaf(const T* fac, const T* inv2,
     const T* Mi = inv2 + S.blk_inv2[blk] + (FWD ? 0 : (ll)bw * bw);
     const int* rows = S.rows + F.rows_off;
     griddep_wait();
-    for (int r = 0; r < nrhs; ++r) {
-        T v = lane < bw ? in[(ll)r * n + F.f + lane] : T(0);
+    for (int r0 = 0; r0 < nrhs; r0 += RG) {
+        const int nr = min(RG, nrhs - r0);
+        T v[RG];
+#pragma unroll
+        for (int r = 0; r < RG; ++r) v[r] = (lane < bw && r < nr) ? in[(ll)(r0 + r) * n + F.f + lane] : T(0);
         if constexpr (!FWD) {   // c_F = y_F - U12 x[R_F] (U12 row j contiguous in Uf)
             if (lane < bw) {
                 const T* u = fac + F.uoff + (ll)lane * F.m;
-                T acc = T(0);
+                T acc[RG];
+#pragma unroll
+                for (int r = 0; r < RG; ++r) acc[r] = T(0);
 #pragma unroll 4
-                for (int i = 0; i < F.m; ++i) acc += u[i] * xs[(ll)r * n + rows[i]];
-                v -= acc;
+                for (int i = 0; i < F.m; ++i) {
+                    const T uv = u[i];
+                    const int g = rows[i];
+#pragma unroll
+                    for (int r = 0; r < RG; ++r)
+                        if (r < nr) acc[r] += uv * xs[(ll)(r0 + r) * n + g];
+                }
+#pragma unroll
+                for (int r = 0; r < RG; ++r) v[r] -= acc[r];
             }
         }
-        T y = T(0);   // lane j: sum_k op(j, k) v_k, op(j, k) at Mi[k * bw + j]
-        for (int k = (FWD ? 0 : 0); k < bw; ++k) {
-            const T vk = __shfl_sync(0xffffffffu, v, k);
-            if (lane < bw && (FWD || k >= lane)) y += Mi[(ll)k * bw + lane] * vk;
+        T y[RG];   // lane j: sum_k op(j, k) v_k, op(j, k) at Mi[k * bw + j]
+#pragma unroll
+        for (int r = 0; r < RG; ++r) y[r] = T(0);
+        for (int k = 0; k < bw; ++k) {
+            T vk[RG];
+#pragma unroll
+            for (int r = 0; r < RG; ++r) vk[r] = __shfl_sync(0xffffffffu, v[r], k);
+            if (lane < bw && (FWD || k >= lane)) {
+                const T mv = Mi[(ll)k * bw + lane];
+#pragma unroll
+                for (int r = 0; r < RG; ++r) y[r] += mv * vk[r];
+            }
         }
-        if (lane < bw) out[(ll)r * n + F.f + lane] = y;
+        if (lane < bw)
+#pragma unroll
+            for (int r = 0; r < RG; ++r)
+                if (r < nr) out[(ll)(r0 + r) * n + F.f + lane] = y[r];
         if constexpr (FWD) {   // b[R_F] -= L21 y_F (L21 column k contiguous in Lf)
             for (int i0 = 0; i0 < F.m; i0 += 32) {
                 const int i = i0 + lane;
-                T acc = T(0);
+                T acc[RG];
+#pragma unroll
+                for (int r = 0; r < RG; ++r) acc[r] = T(0);
                 for (int k = 0; k < bw; ++k) {
-                    const T yk = __shfl_sync(0xffffffffu, y, k);
-                    if (i < F.m) acc += fac[F.loff + (ll)k * F.ld + F.nf + i] * yk;
+                    T yk[RG];
+#pragma unroll
+                    for (int r = 0; r < RG; ++r) yk[r] = __shfl_sync(0xffffffffu, y[r], k);
+                    if (i < F.m) {
+                        const T lv = fac[F.loff + (ll)k * F.ld + F.nf + i];
+#pragma unroll
+                        for (int r = 0; r < RG; ++r) acc[r] += lv * yk[r];
+                    }
                 }
-                if (i < F.m) atomicAdd(&in[(ll)r * n + rows[i]], -acc);
+                if (i < F.m)
+#pragma unroll
+                    for (int r = 0; r < RG; ++r)
+                        if (r < nr) atomicAdd(&in[(ll)(r0 + r) * n + rows[i]], -acc[r]);
             }
         }
     }
