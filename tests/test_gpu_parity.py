@@ -246,3 +246,27 @@ def test_fp32_tensor_core_updates(kind):
     assert rr <= 1e-12 and it <= 6
     r = b - A @ x
     assert np.max(np.linalg.norm(r, axis=0) / np.linalg.norm(b, axis=0)) <= 1e-12
+
+
+@pytest.mark.parametrize("nrhs", [5, 20])
+def test_many_rhs_front_and_leaf_solves(nrhs):
+    # 24^3: the separators near the root have 4 to 10 blocks (the cluster
+    # front solves), the leaves are single blocks of a few columns (the
+    # warp-per-front solves); 5 and 20 right-hand sides cross the solvers'
+    # groups of 4 and the 16-column batches of the C ABI.  Plain and
+    # transposed solves against the oracle and scipy, FP64.
+    import scipy.sparse.linalg as spla
+    k = 24
+    A = S.gallery.convection_diffusion(k=k)
+    b = S.gallery.random_rhs(A.shape[0], nrhs, seed=nrhs)
+    s, o = run_both(A, S.nd_grid(k, k, k))
+    x = b.copy(order="F")
+    S.triangularsolve_(s, x)
+    xo = o.solve(b)
+    assert rel(x, xo) < 1e-10
+    r = b - A @ x
+    assert np.max(np.linalg.norm(r, axis=0) / np.linalg.norm(b, axis=0)) <= 1e-12
+    xt = b.copy(order="F")
+    S.transposetriangularsolve_(s, xt)
+    xr = spla.splu(sp.csc_matrix(A.T)).solve(b)
+    assert rel(xt, xr) < 1e-9
