@@ -379,10 +379,17 @@ __device__ __forceinline__ T lu_pick(const T (&a)[RPT][4], int ii, int jj) {
     return v;
 }
 
-// Part A for the group of warp `g` (called by that warp only).
+// Scaling factor 1 / pivot of the FP32 block LU: the hardware reciprocal
+// (within 2 ulp; the FP32 factor is refined in FP64); FP64 keeps the
+// correctly rounded one.
+__device__ __forceinline__ float lu_recip(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ double lu_recip(double x) { return rcp_rn(x); }
+
+// Part A for the group of warp `g` (called by that warp only).  cpa / cpb:
+// first and end column of each column's piece.
 template <typename T, int RPT>
-__device__ __forceinline__ void lu_group_factor(T (&a)[RPT][4], int g, int bw, const int* q0, int& pn, T* lb, int* skp,
-                                                T* spv, int* sa0, int* spiv, int* szero) {
+__device__ __forceinline__ void lu_group_factor(T (&a)[RPT][4], int g, int bw, const int* cpa, const int* cpb, T* lb,
+                                                int* skp, T* spv, int* sa0, int* spiv, int* szero) {
     using Key = typename PivotKey<T>::type;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, r0 = RPT * lane;
@@ -390,8 +397,7 @@ __device__ __forceinline__ void lu_group_factor(T (&a)[RPT][4], int g, int bw, c
     for (int j = 0; j < 4; ++j) {
         const int k = 4 * g + j;
         if (k >= bw) break;
-        while (q0[pn + 1] <= k) ++pn;
-        const int a0 = q0[pn], b = q0[pn + 1];
+        const int a0 = cpa[k], b = cpb[k];
         Key best = 0;
         int brow = 0;
 #pragma unroll
@@ -418,7 +424,7 @@ __device__ __forceinline__ void lu_group_factor(T (&a)[RPT][4], int g, int bw, c
                 }
             }
         }
-        const T rinv = scale ? rcp_rn(pv) : T(1);
+        const T rinv = scale ? lu_recip(pv) : T(1);
 #pragma unroll
         for (int ii = 0; ii < RPT; ++ii) {
             const int R = r0 + ii;
@@ -519,7 +525,7 @@ __global__ void __launch_bounds__(LuThreads<T>::value, 1) k_block_lu(T* fac, int
     __shared__ T s_pv[2][4];
     __shared__ int s_kp[2][4], s_a0[2][4];
     __shared__ int q0[BM + 1];
-    __shared__ int spiv[BM], sgmap[BM];
+    __shared__ int spiv[BM], sgmap[BM], cpa[BM], cpb[BM];
     __shared__ int szero;
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
@@ -531,6 +537,12 @@ __global__ void __launch_bounds__(LuThreads<T>::value, 1) k_block_lu(T* fac, int
     const int r0 = RPT * lane, cl0 = 4 * w;
     for (int k = tid; k <= np; k += blockDim.x) q0[k] = S.xsuper[p0 + k] - F.f - c0;
     if (tid == 0) szero = INT_MAX;
+    __syncthreads();
+    for (int pc = tid; pc < np; pc += blockDim.x)
+        for (int k = q0[pc]; k < q0[pc + 1]; ++k) {
+            cpa[k] = q0[pc];
+            cpb[k] = q0[pc + 1];
+        }
     T* blkp = fac + F.loff + (ll)c0 * F.ld + c0;   // block (i, j) at blkp[j * ld + i]
     T a[RPT][4];
 #pragma unroll
@@ -542,8 +554,7 @@ __global__ void __launch_bounds__(LuThreads<T>::value, 1) k_block_lu(T* fac, int
         }
     __syncthreads();
     const int ng = cdiv(bw, 4);
-    int pn = 0;
-    if (w == 0) lu_group_factor<T, RPT>(a, 0, bw, q0, pn, lbuf[0], s_kp[0], s_pv[0], s_a0[0], spiv, &szero);
+    if (w == 0) lu_group_factor<T, RPT>(a, 0, bw, cpa, cpb, lbuf[0], s_kp[0], s_pv[0], s_a0[0], spiv, &szero);
     __syncthreads();
 #pragma unroll 1
     for (int g = 0; g < ng; ++g) {
@@ -552,7 +563,7 @@ __global__ void __launch_bounds__(LuThreads<T>::value, 1) k_block_lu(T* fac, int
         if (w > g && w < ng) {
             lu_group_update<T, RPT>(a, g, bw, lbuf[par], s_kp[par], s_pv[par]);
             if (w == g + 1)   // the next panel while the other warps update
-                lu_group_factor<T, RPT>(a, g + 1, bw, q0, pn, lbuf[par ^ 1], s_kp[par ^ 1], s_pv[par ^ 1],
+                lu_group_factor<T, RPT>(a, g + 1, bw, cpa, cpb, lbuf[par ^ 1], s_kp[par ^ 1], s_pv[par ^ 1],
                                         s_a0[par ^ 1], spiv, &szero);
         }
         __syncthreads();
