@@ -2178,8 +2178,11 @@ __global__ void __cluster_dims__(NC, 1, 1) __launch_bounds__(FC_THREADS, 1)
         }
         __syncthreads();
         auto solve_step = [&](int st) {   // owner: publish the solution of step st
-            const int blk = blk_of(st), c0 = S.blk_c0[blk], bw = S.blk_c1[blk] - c0;
+            const int blk = blk_of(st), bw = S.blk_c1[blk] - S.blk_c0[blk];
             fc_block_solve<T, FWD>(preM, bw, own + (size_t)(st / FC) * BM * FC_RG, ypub, part, nr);
+        };
+        auto finish_step = [&](int st) {   // owner, after the barrier arrival: output and next prefetch
+            const int blk = blk_of(st), c0 = S.blk_c0[blk], bw = S.blk_c1[blk] - c0;
             for (int e = tid; e < bw * nr; e += FC_THREADS) {
                 const int j = e % bw, r = e / bw;
                 out[(ll)(r0 + r) * n + F.f + c0 + j] = ypub[j * FC_RG + r];
@@ -2192,6 +2195,7 @@ __global__ void __cluster_dims__(NC, 1, 1) __launch_bounds__(FC_THREADS, 1)
             solve_step(0);
         }
         cl.barrier_arrive();
+        if (rank == 0) finish_step(0);
         for (int t = 0; t < nb; ++t) {
             cl.barrier_wait();
             const T* src = cl.map_shared_rank(ypub, t % FC);
@@ -2208,6 +2212,7 @@ __global__ void __cluster_dims__(NC, 1, 1) __launch_bounds__(FC_THREADS, 1)
                 solve_step(t + 1);
             }
             cl.barrier_arrive();
+            if (next) finish_step(t + 1);
             for (int st = rank, o = 0; st < nb; st += FC, ++o)
                 if (st > t && !(next && st == t + 1)) {
                     const int bs = blk_of(st);
