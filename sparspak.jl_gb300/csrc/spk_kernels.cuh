@@ -1294,7 +1294,7 @@ __device__ __forceinline__ ScatterRow scatter_row(const Sched& S, const DFront& 
 // scatter-subtracted into the ancestors like k_schur.  Replaces, for these
 // fronts, k_block_lu_small + k_block_panel + k_schur (three launches whose
 // CTAs would be mostly idle on fronts this small).
-constexpr int LF_M = 64, LF_WARPS = 4, LF_LD = 33;
+constexpr int LF_M = 32, LF_WARPS = 4, LF_LD = 33;
 template <typename T> struct LeafSmem {
     static constexpr size_t warp_bytes = (size_t)(32 + LF_M) * LF_LD * sizeof(T) + LF_M * sizeof(ScatterRow) +
                                          32 * sizeof(T) + (33 + 3 * 32) * sizeof(int);
