@@ -83,8 +83,9 @@ struct Plan {
     std::vector<ll> blk_lpack, blk_upack;  // byte offsets of the packed panels (-1: front not packed)
     ll pack_size = 0;
     std::vector<int> blk_front;
-    std::vector<int> inv_ids;             // k_block_inv entries grouped by line width (32, 64, 128)
-    int inv_off[4] = {0, 0, 0, 0};        // class c: inv_ids[inv_off[c] .. inv_off[c+1])
+    std::vector<int> inv_ids;             // k_block_inv entries grouped by level group, then line width (32, 64, 128)
+    int inv_off[2][4] = {};               // group g, class c: inv_ids[inv_off[g][c] .. inv_off[g][c+1])
+    int inv_split = 0;                    // group 0: blocks of fronts below this level (final before it starts)
     ll inv2_size = 0;
     std::vector<int> block0, nblocks;     // per front
     std::vector<LevelPlan> levels;
@@ -170,6 +171,11 @@ struct spk_handle {
     // trailing update runs on `side` while the next block LU runs on the
     // launch stream (evP: panels done; evB: trailing update done).
     cudaStream_t side = nullptr;
+    // The solve operators of the lower levels' blocks (k_block_inv) run on
+    // side2 while the last levels are factored (evP2: those levels done; evI:
+    // the operators done).
+    cudaStream_t side2 = nullptr;
+    cudaEvent_t evP2 = nullptr, evI = nullptr;
     bool fc16 = false;   // front solves by clusters of 16 CTAs
     cudaEvent_t evP = nullptr, evB = nullptr;
     int device = -1;
@@ -583,22 +589,29 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
     }
     {
         // k_block_inv work: blocks up to 32 wide, one entry per block; wider
-        // ones by line width 64 / 128, entries blk * 4 + kind * 2 + tile
+        // ones by line width 64 / 128, entries blk * 4 + kind * 2 + tile.
+        // Group 0 (fronts below the last two levels) can run beside the top
+        // of the factorisation, group 1 after it.
         const int lim[3] = {32, 64, 128};
-        for (int c = 0; c < 3; ++c) {
-            P.inv_off[c] = (int)P.inv_ids.size();
-            for (int b = 0; b < (int)P.blk_c0.size(); ++b) {
-                const int bw = P.blk_c1[b] - P.blk_c0[b];
-                if (!(bw <= lim[c] && (c == 0 || bw > lim[c - 1]))) continue;
-                if (c == 0) {
-                    P.inv_ids.push_back(b);
-                } else {
-                    for (int kind = 0; kind < 2; ++kind)
-                        for (int tile = 0; tile < spk::cdiv(bw, 64); ++tile) P.inv_ids.push_back(b * 4 + kind * 2 + tile);
+        P.inv_split = std::max(0, h->nlevels - 2);
+        for (int g = 0; g < 2; ++g) {
+            for (int c = 0; c < 3; ++c) {
+                P.inv_off[g][c] = (int)P.inv_ids.size();
+                for (int b = 0; b < (int)P.blk_c0.size(); ++b) {
+                    const int bw = P.blk_c1[b] - P.blk_c0[b];
+                    if (!(bw <= lim[c] && (c == 0 || bw > lim[c - 1]))) continue;
+                    if ((h->fronts[P.blk_front[b]].level < P.inv_split) != (g == 0)) continue;
+                    if (c == 0) {
+                        P.inv_ids.push_back(b);
+                    } else {
+                        for (int kind = 0; kind < 2; ++kind)
+                            for (int tile = 0; tile < spk::cdiv(bw, 64); ++tile)
+                                P.inv_ids.push_back(b * 4 + kind * 2 + tile);
+                    }
                 }
             }
+            P.inv_off[g][3] = (int)P.inv_ids.size();
         }
-        P.inv_off[3] = (int)P.inv_ids.size();
     }
     const int nlev = h->nlevels;
     std::vector<std::vector<int>> at(nlev);
@@ -982,8 +995,36 @@ static int factor_launches(spk_handle* h) {
     const spk::Sched& S = PL.sched;
     // Look ahead (not while timing kernels one by one): see spk_handle::side.
     const bool ahead = h->prof_mask == 0;
-    bool pending = false;
-    for (const LevelPlan& P : PL.levels) {
+    bool pending = false, pending_inv = false;
+    // The whole-block solve operators of level group g (k_block_inv).
+    auto launch_inv = [&](int g, cudaStream_t st) {
+        for (int c = 0; c < 3; ++c) {
+            const int cnt = PL.inv_off[g][c + 1] - PL.inv_off[g][c];
+            if (cnt <= 0) continue;
+            LaunchScope ls(h, SPK_K_BLOCKINV, 0.0, 0.0);
+            const int* ent = PL.d_inv_ids + PL.inv_off[g][c];
+            T* inv2 = storage<T>(h).inv2;
+            if (c == 0)
+                spk::k_block_inv<T, 32><<<cnt, 256, sweep_smem<T, 32>(2), st>>>(fac, h->d_ipiv, inv2, S,
+                                                                                  PL.d_blk_front, ent);
+            else if (c == 1)
+                spk::k_block_inv<T, 64><<<cnt, 256, sweep_smem<T, 64>(1), st>>>(fac, h->d_ipiv, inv2, S,
+                                                                                  PL.d_blk_front, ent);
+            else
+                spk::k_block_inv<T, BM><<<cnt, 256, sweep_smem<T, BM>(1), st>>>(fac, h->d_ipiv, inv2, S,
+                                                                                  PL.d_blk_front, ent);
+        }
+    };
+    for (size_t lvl = 0; lvl < PL.levels.size(); ++lvl) {
+        const LevelPlan& P = PL.levels[lvl];
+        if (ahead && (int)lvl == PL.inv_split && PL.inv_off[0][3] > PL.inv_off[0][0]) {
+            // group 0's blocks are final: their operators beside the last levels
+            CU(h, cudaEventRecord(h->evP2, h->stream));
+            CU(h, cudaStreamWaitEvent(h->side2, h->evP2, 0));
+            launch_inv(0, h->side2);
+            CU(h, cudaEventRecord(h->evI, h->side2));
+            pending_inv = true;
+        }
         if (P.leaf_factor.tiles > 0) {
             LaunchScope ls(h, SPK_K_GETRF, P.leaf_factor.flops, P.leaf_factor.words * sizeof(T));
             spk::k_leaf_factor<T><<<(P.leaf_factor.count + spk::LF_WARPS - 1) / spk::LF_WARPS, 32 * spk::LF_WARPS,
@@ -1073,22 +1114,9 @@ static int factor_launches(spk_handle* h) {
             }
         }
     }
-    for (int c = 0; c < 3; ++c) {
-        const int cnt = PL.inv_off[c + 1] - PL.inv_off[c];
-        if (cnt <= 0) continue;
-        LaunchScope ls(h, SPK_K_BLOCKINV, 0.0, 0.0);
-        const int* ent = PL.d_inv_ids + PL.inv_off[c];
-        T* inv2 = storage<T>(h).inv2;
-        if (c == 0)
-            spk::k_block_inv<T, 32><<<cnt, 256, sweep_smem<T, 32>(2), h->stream>>>(fac, h->d_ipiv, inv2, S,
-                                                                                      PL.d_blk_front, ent);
-        else if (c == 1)
-            spk::k_block_inv<T, 64><<<cnt, 256, sweep_smem<T, 64>(1), h->stream>>>(fac, h->d_ipiv, inv2, S,
-                                                                                  PL.d_blk_front, ent);
-        else
-            spk::k_block_inv<T, BM><<<cnt, 256, sweep_smem<T, BM>(1), h->stream>>>(fac, h->d_ipiv, inv2, S,
-                                                                                  PL.d_blk_front, ent);
-    }
+    if (pending_inv) CU(h, cudaStreamWaitEvent(h->stream, h->evI, 0));
+    else launch_inv(0, h->stream);
+    launch_inv(1, h->stream);
     CU(h, cudaGetLastError());
     return SPK_OK;
 }
@@ -1349,6 +1377,9 @@ int spk_create(int64_t n, int64_t nsuper, const int64_t* xsuper, const int64_t* 
             if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->evP, cudaEventDisableTiming);
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->evB, cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side2, cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->evP2, cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->evI, cudaEventDisableTiming);
             if (e != cudaSuccess) rc = set_err(h, SPK_ECUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
             h->stream = h->own;
         }
@@ -1839,9 +1870,13 @@ void spk_destroy(spk_handle* h) {
     drop_graph(h->g_factor[1]);
     drop_solve_graphs(h);
     if (h->side) cudaStreamSynchronize(h->side);
+    if (h->side2) cudaStreamSynchronize(h->side2);
     if (h->evP) cudaEventDestroy(h->evP);
     if (h->evB) cudaEventDestroy(h->evB);
+    if (h->evP2) cudaEventDestroy(h->evP2);
+    if (h->evI) cudaEventDestroy(h->evI);
     if (h->side) cudaStreamDestroy(h->side);
+    if (h->side2) cudaStreamDestroy(h->side2);
     if (h->own) cudaStreamDestroy(h->own);
     delete h;
 }
