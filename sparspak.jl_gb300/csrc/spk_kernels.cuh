@@ -997,12 +997,15 @@ __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, cons
 // every piece, with the earlier pieces' updates X_p -= X_<p U_<p,p), and
 // 64-column tiles of the U panel to its right, inside the front (Lf) and in
 // U12 (Uf): Y := inv(L_B) P_B Y (_luswap! and trsm 'r','l','t','u' of every
-// piece, with Y_p -= L_p,<p Y_<p).  One line per 4 lanes.  For FP32 fronts
-// with a pack (blk_lpack >= 0) the lines are also written, split into TF32
-// hi / lo, to the packed tiles that the tensor-core updates read: rows of the
-// L panel tiled from c1 ([c1, nf)) and from nf ([nf, ld)), columns of the U
-// panel from c1 ([c1, nf)) and from 0 (U12).
-// Dynamic shared memory: W * SLD(W) T's.
+// piece, with Y_p -= L_p,<p Y_<p).  One line per 4 lanes (W = 32, 64); FP32
+// blocks wider than 64 columns take block_panel128 (four lines per 16
+// lanes, PT_LINES-line tiles).  For FP32 fronts with a pack (blk_lpack >= 0)
+// the lines are also written, split into TF32 hi / lo, to the packed tiles
+// that the tensor-core updates read: rows of the L panel tiled from c1
+// ([c1, nf)) and from nf ([nf, ld)), columns of the U panel from c1
+// ([c1, nf)) and from 0 (U12).
+// Dynamic shared memory: W * SLD(W) T's (plus the line tile of
+// block_panel128).
 template <typename T, int W>
 __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, const int* bmap, Sched S, Launch L,
                                                       int step, unsigned char* pack) {
