@@ -1257,7 +1257,7 @@ static int residual_device(spk_handle* h, const double* b, i64 ldb, const double
                            double* relres, bool transpose = false) {
     const int n = (int)h->n;
     CU(h, cudaMemsetAsync(h->d_sums, 0, sizeof(double) * 2 * (size_t)nrhs, h->stream));
-    dim3 grid((n + 255) / 256, (unsigned)nrhs);
+    dim3 grid((n + 255) / 256);
     {
         LaunchScope ls(h, SPK_K_RESIDUAL, 2.0 * h->nnz * nrhs, (double)h->nnz * (8 + 4 + 8) + 8.0 * h->nnz * nrhs +
                                                                   24.0 * n * nrhs);
@@ -1648,8 +1648,9 @@ int spk_residual_noalloc(spk_handle* h, const double* b, const double* x, int64_
     if ((rc = noalloc_scratch(h, &sums))) return rc;
     const int n = (int)h->n;
     CU(h, cudaMemsetAsync(sums, 0, sizeof(double) * 2 * (size_t)nrhs, h->stream));
-    dim3 grid((n + 255) / 256, (unsigned)nrhs);
-    spk::k_residual_norms<<<grid, 256, 0, h->stream>>>(h->d_aval, h->d_rowptr, h->d_col, h->d_src, x, ld, b, ld, n, sums);
+    dim3 grid((n + 255) / 256);
+    spk::k_residual_norms<<<grid, 256, 0, h->stream>>>(h->d_aval, h->d_rowptr, h->d_col, h->d_src, x, ld, b, ld, n,
+                                                       (int)nrhs, sums);
     CU(h, cudaGetLastError());
     double host[2 * SPK_NOALLOC_MAX_RHS];
     CU(h, cudaMemcpyAsync(host, sums, sizeof(double) * 2 * (size_t)nrhs, cudaMemcpyDeviceToHost, h->stream));

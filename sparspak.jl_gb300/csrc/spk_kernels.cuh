@@ -2585,59 +2585,107 @@ __global__ void k_unpermute(const Tin* __restrict__ xp, ll ldp, double* __restri
     if (accumulate) x[(ll)r * ldx + j] += v; else x[(ll)r * ldx + j] = v;
 }
 
+// Sums of the squares of r and b for RES_RG right-hand sides over a CTA
+// (256 threads), one atomic per sum and CTA.
+constexpr int RES_RG = 4;
+__device__ __forceinline__ void residual_sums(double (&rr)[RES_RG], double (&bb)[RES_RG], int r0, int nr,
+                                              double* __restrict__ sums) {
+    __shared__ double part[8][2 * RES_RG];
+#pragma unroll
+    for (int q = 0; q < RES_RG; ++q)
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            rr[q] += __shfl_down_sync(0xffffffffu, rr[q], off);
+            bb[q] += __shfl_down_sync(0xffffffffu, bb[q], off);
+        }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+        for (int q = 0; q < RES_RG; ++q) {
+            part[w][2 * q] = rr[q];
+            part[w][2 * q + 1] = bb[q];
+        }
+    __syncthreads();
+    if (threadIdx.x < 2 * nr) {
+        double t = 0.0;
+        for (int v = 0; v < (int)(blockDim.x >> 5); ++v) t += part[v][threadIdx.x];
+        atomicAdd(&sums[2 * r0 + threadIdx.x], t);
+    }
+    __syncthreads();
+}
+
 // r = b - A x in FP64 with A in row order (values gathered from CSC order
 // through src), or r = b - A^T x with A^T's rows = A's CSC columns (src
-// null); the squares of r and b are accumulated per right-hand side.
-__global__ void k_residual(const double* __restrict__ aval, const int* __restrict__ rowptr, const int* __restrict__ col,
-                           const ll* __restrict__ src, const double* __restrict__ x, ll ldx, const double* __restrict__ b,
-                           ll ldb, double* __restrict__ r, int n, int nrhs, double* __restrict__ sums) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int rhs = blockIdx.y;
-    double rr = 0.0, bb = 0.0;
-    if (i < n) {
-        double s = 0.0;
-        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) s += aval[src ? src[k] : k] * x[(ll)rhs * ldx + col[k]];
-        double bi = b[(ll)rhs * ldb + i];
-        double ri = bi - s;
-        r[(ll)rhs * n + i] = ri;
-        rr = ri * ri;
-        bb = bi * bi;
-    }
+// null); the squares of r and b are accumulated per right-hand side.  A
+// thread takes a row for RES_RG right-hand sides at a time.
+__global__ void __launch_bounds__(256) k_residual(const double* __restrict__ aval, const int* __restrict__ rowptr,
+                                                  const int* __restrict__ col, const ll* __restrict__ src,
+                                                  const double* __restrict__ x, ll ldx, const double* __restrict__ b,
+                                                  ll ldb, double* __restrict__ r, int n, int nrhs,
+                                                  double* __restrict__ sums) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int r0 = 0; r0 < nrhs; r0 += RES_RG) {
+        const int nr = min(RES_RG, nrhs - r0);
+        double rr[RES_RG], bb[RES_RG];
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        rr += __shfl_down_sync(0xffffffffu, rr, off);
-        bb += __shfl_down_sync(0xffffffffu, bb, off);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(&sums[2 * rhs], rr);
-        atomicAdd(&sums[2 * rhs + 1], bb);
+        for (int q = 0; q < RES_RG; ++q) rr[q] = bb[q] = 0.0;
+        if (i < n) {
+            double s[RES_RG];
+#pragma unroll
+            for (int q = 0; q < RES_RG; ++q) s[q] = 0.0;
+            for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+                const double a = aval[src ? src[k] : k];
+                const int c = col[k];
+#pragma unroll
+                for (int q = 0; q < RES_RG; ++q)
+                    if (q < nr) s[q] += a * x[(ll)(r0 + q) * ldx + c];
+            }
+#pragma unroll
+            for (int q = 0; q < RES_RG; ++q)
+                if (q < nr) {
+                    const double bi = b[(ll)(r0 + q) * ldb + i], ri = bi - s[q];
+                    r[(ll)(r0 + q) * n + i] = ri;
+                    rr[q] = ri * ri;
+                    bb[q] = bi * bi;
+                }
+        }
+        residual_sums(rr, bb, r0, nr, sums);
     }
 }
 
 // Norms only: sums[2r] += ||b_r - A x_r||^2 and sums[2r+1] += ||b_r||^2, with
 // no residual vector written (used where no work space may be allocated).
-__global__ void k_residual_norms(const double* __restrict__ aval, const int* __restrict__ rowptr,
-                                 const int* __restrict__ col, const ll* __restrict__ src, const double* __restrict__ x,
-                                 ll ldx, const double* __restrict__ b, ll ldb, int n, double* __restrict__ sums) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int rhs = blockIdx.y;
-    double rr = 0.0, bb = 0.0;
-    if (i < n) {
-        double s = 0.0;
-        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) s += aval[src ? src[k] : k] * x[(ll)rhs * ldx + col[k]];
-        double bi = b[(ll)rhs * ldb + i];
-        double ri = bi - s;
-        rr = ri * ri;
-        bb = bi * bi;
-    }
+__global__ void __launch_bounds__(256) k_residual_norms(const double* __restrict__ aval, const int* __restrict__ rowptr,
+                                                        const int* __restrict__ col, const ll* __restrict__ src,
+                                                        const double* __restrict__ x, ll ldx,
+                                                        const double* __restrict__ b, ll ldb, int n, int nrhs,
+                                                        double* __restrict__ sums) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int r0 = 0; r0 < nrhs; r0 += RES_RG) {
+        const int nr = min(RES_RG, nrhs - r0);
+        double rr[RES_RG], bb[RES_RG];
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        rr += __shfl_down_sync(0xffffffffu, rr, off);
-        bb += __shfl_down_sync(0xffffffffu, bb, off);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(&sums[2 * rhs], rr);
-        atomicAdd(&sums[2 * rhs + 1], bb);
+        for (int q = 0; q < RES_RG; ++q) rr[q] = bb[q] = 0.0;
+        if (i < n) {
+            double s[RES_RG];
+#pragma unroll
+            for (int q = 0; q < RES_RG; ++q) s[q] = 0.0;
+            for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+                const double a = aval[src ? src[k] : k];
+                const int c = col[k];
+#pragma unroll
+                for (int q = 0; q < RES_RG; ++q)
+                    if (q < nr) s[q] += a * x[(ll)(r0 + q) * ldx + c];
+            }
+#pragma unroll
+            for (int q = 0; q < RES_RG; ++q)
+                if (q < nr) {
+                    const double bi = b[(ll)(r0 + q) * ldb + i], ri = bi - s[q];
+                    rr[q] = ri * ri;
+                    bb[q] = bi * bi;
+                }
+        }
+        residual_sums(rr, bb, r0, nr, sums);
     }
 }
 
