@@ -676,13 +676,13 @@ __device__ __forceinline__ void sweep_cols(T (&y)[W / 4], const T* sL, int bw) {
 // (two 16-byte loads per lane and step instead of eight; the staged layout
 // sidx<float, 128> puts the eight chunks of a quarter-warp in distinct bank
 // quads).  The owner of entry k shuffles its four values to the half-warp.
-__device__ __forceinline__ void sweep_rows4(float (&x)[4][8], const float* sU, const float* rd, int bw) {
+__device__ __forceinline__ void sweep_rows4(float (&x)[4][8], const float* sU, const float* rd, int bw, int kc_end) {
     // Steps past bw are no-ops (zero staged rows, rd = 0, zero entries), so
     // whole chunks of 8 run unguarded; the next step's row and rd are loaded
     // one step ahead, and the update of the next step's pivot entry comes
-    // first.
+    // first.  Chunks [0, kc_end) only.
     const int lane = threadIdx.x & 31, c = lane & 15, base = lane & 16;
-    const int nk = cdiv(bw, 8);
+    const int nk = min(cdiv(bw, 8), kc_end);
     float4 n0 = *reinterpret_cast<const float4*>(sU + sidx<float, 128>(0, 8 * c));
     float4 n1 = *reinterpret_cast<const float4*>(sU + sidx<float, 128>(0, 8 * c) + 4);
     float nr = rd[0];
@@ -716,9 +716,9 @@ __device__ __forceinline__ void sweep_rows4(float (&x)[4][8], const float* sU, c
     }
 }
 
-__device__ __forceinline__ void sweep_cols4(float (&y)[4][8], const float* sL, int bw) {
+__device__ __forceinline__ void sweep_cols4(float (&y)[4][8], const float* sL, int bw, int kc_end) {
     const int lane = threadIdx.x & 31, c = lane & 15, base = lane & 16;
-    const int nk = cdiv(bw, 8);
+    const int nk = min(cdiv(bw, 8), kc_end);
     float4 n0 = *reinterpret_cast<const float4*>(sL + sidx<float, 128>(0, 8 * c));
     float4 n1 = *reinterpret_cast<const float4*>(sL + sidx<float, 128>(0, 8 * c) + 4);
 #pragma unroll 1
@@ -741,6 +741,84 @@ __device__ __forceinline__ void sweep_cols4(float (&y)[4][8], const float* sL, i
             for (int l = 0; l < 4; ++l)
 #pragma unroll
                 for (int ii = 0; ii < 8; ++ii)
+                    if (ii != jn) y[l][ii] -= lv[ii] * yk[l];
+        }
+    }
+}
+
+// Second phase of the 128-wide sweeps: from step 64 on only entries 64..127
+// are still updated, so lane c of a half-warp takes entries [64 + 4c,
+// 64 + 4c + 4) of the same four lines (moved there from lane 8 + c / 2),
+// four per lane instead of eight.  Entries below 64 are final after the
+// first phase and stay with their lanes.
+__device__ __forceinline__ void sweep_to_hi(const float (&x)[4][8], float (&x2)[4][4]) {
+    const int lane = threadIdx.x & 31, c = lane & 15, src = (lane & 16) | (8 + (c >> 1));
+#pragma unroll
+    for (int l = 0; l < 4; ++l)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float v0 = __shfl_sync(0xffffffffu, x[l][q], src), v1 = __shfl_sync(0xffffffffu, x[l][4 + q], src);
+            x2[l][q] = (c & 1) ? v1 : v0;
+        }
+}
+
+__device__ __forceinline__ void sweep_rows4_hi(float (&x)[4][4], const float* sU, const float* rd, int bw) {
+    const int lane = threadIdx.x & 31, c = lane & 15, base = lane & 16;
+    const int nk = cdiv(bw - 64, 4);
+    float4 n0 = *reinterpret_cast<const float4*>(sU + sidx<float, 128>(64, 64 + 4 * c));
+    float nr = rd[64];
+#pragma unroll 1
+    for (int kc = 0; kc < nk; ++kc) {
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+            const int k = 64 + kc * 4 + kk;
+            const float4 u0 = n0;
+            const float r = nr;
+            const int kn = k + 1 < 128 ? k + 1 : k;
+            n0 = *reinterpret_cast<const float4*>(sU + sidx<float, 128>(kn, 64 + 4 * c));
+            nr = rd[kn];
+            float xk[4];
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                if (c == kc) x[l][kk] *= r;
+                xk[l] = __shfl_sync(0xffffffffu, x[l][kk], base | kc);
+            }
+            const float uv[4] = {u0.x, u0.y, u0.z, u0.w};
+            const int jn = (kk + 1) & 3;
+#pragma unroll
+            for (int l = 0; l < 4; ++l) x[l][jn] -= xk[l] * uv[jn];
+#pragma unroll
+            for (int l = 0; l < 4; ++l)
+#pragma unroll
+                for (int jj = 0; jj < 4; ++jj)
+                    if (jj != jn) x[l][jj] -= xk[l] * uv[jj];
+        }
+    }
+}
+
+__device__ __forceinline__ void sweep_cols4_hi(float (&y)[4][4], const float* sL, int bw) {
+    const int lane = threadIdx.x & 31, c = lane & 15, base = lane & 16;
+    const int nk = cdiv(bw - 64, 4);
+    float4 n0 = *reinterpret_cast<const float4*>(sL + sidx<float, 128>(64, 64 + 4 * c));
+#pragma unroll 1
+    for (int kc = 0; kc < nk; ++kc) {
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+            const int k = 64 + kc * 4 + kk;
+            const float4 l0 = n0;
+            const int kn = k + 1 < 128 ? k + 1 : k;
+            n0 = *reinterpret_cast<const float4*>(sL + sidx<float, 128>(kn, 64 + 4 * c));
+            float yk[4];
+#pragma unroll
+            for (int l = 0; l < 4; ++l) yk[l] = __shfl_sync(0xffffffffu, y[l][kk], base | kc);
+            const float lv[4] = {l0.x, l0.y, l0.z, l0.w};
+            const int jn = (kk + 1) & 3;
+#pragma unroll
+            for (int l = 0; l < 4; ++l) y[l][jn] -= lv[jn] * yk[l];
+#pragma unroll
+            for (int l = 0; l < 4; ++l)
+#pragma unroll
+                for (int ii = 0; ii < 4; ++ii)
                     if (ii != jn) y[l][ii] -= lv[ii] * yk[l];
         }
     }
@@ -922,12 +1000,20 @@ __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, cons
             x[l][0] = a0.x; x[l][1] = a0.y; x[l][2] = a0.z; x[l][3] = a0.w;
             x[l][4] = a1.x; x[l][5] = a1.y; x[l][6] = a1.z; x[l][7] = a1.w;
         }
-        sweep_rows4(x, sT, rd, bw);
+        sweep_rows4(x, sT, rd, bw, 8);   // steps 0..63
+        float x2[4][4];
+        sweep_to_hi(x, x2);
+        sweep_rows4_hi(x2, sT, rd, bw);  // steps 64..
 #pragma unroll
-        for (int l = 0; l < 4; ++l) {   // each lane rewrites only what it read
-            *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 8 * c) = make_float4(x[l][0], x[l][1], x[l][2], x[l][3]);
-            *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 8 * c + 4) = make_float4(x[l][4], x[l][5], x[l][6], x[l][7]);
+        for (int l = 0; l < 4; ++l) {   // entries 0..63 from the first phase, 64..127 from the second
+            if (c < 8) {
+                *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 8 * c) = make_float4(x[l][0], x[l][1], x[l][2], x[l][3]);
+                *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 8 * c + 4) = make_float4(x[l][4], x[l][5], x[l][6], x[l][7]);
+            }
         }
+#pragma unroll
+        for (int l = 0; l < 4; ++l)
+            *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 64 + 4 * c) = make_float4(x2[l][0], x2[l][1], x2[l][2], x2[l][3]);
         __syncthreads();
         for (int e = tid; e < PT_LINES * 128; e += PT_LINES * 4) {
             int li, j;
@@ -970,12 +1056,20 @@ __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, cons
             y[l][0] = a0.x; y[l][1] = a0.y; y[l][2] = a0.z; y[l][3] = a0.w;
             y[l][4] = a1.x; y[l][5] = a1.y; y[l][6] = a1.z; y[l][7] = a1.w;
         }
-        sweep_cols4(y, sT, bw);
+        sweep_cols4(y, sT, bw, 8);
+        float y2[4][4];
+        sweep_to_hi(y, y2);
+        sweep_cols4_hi(y2, sT, bw);
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
-            *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 8 * c) = make_float4(y[l][0], y[l][1], y[l][2], y[l][3]);
-            *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 8 * c + 4) = make_float4(y[l][4], y[l][5], y[l][6], y[l][7]);
+            if (c < 8) {
+                *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 8 * c) = make_float4(y[l][0], y[l][1], y[l][2], y[l][3]);
+                *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 8 * c + 4) = make_float4(y[l][4], y[l][5], y[l][6], y[l][7]);
+            }
         }
+#pragma unroll
+        for (int l = 0; l < 4; ++l)
+            *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 64 + 4 * c) = make_float4(y2[l][0], y2[l][1], y2[l][2], y2[l][3]);
         __syncthreads();
         for (int e = tid; e < PT_LINES * 128; e += PT_LINES * 4) {
             int li, R;
