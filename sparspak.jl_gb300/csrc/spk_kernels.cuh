@@ -764,7 +764,7 @@ __device__ __forceinline__ void sweep_to_hi(const float (&x)[4][8], float (&x2)[
 
 __device__ __forceinline__ void sweep_rows4_hi(float (&x)[4][4], const float* sU, const float* rd, int bw) {
     const int lane = threadIdx.x & 31, c = lane & 15, base = lane & 16;
-    const int nk = cdiv(bw - 64, 4);
+    const int nk = min(cdiv(bw - 64, 4), 8);   // steps 64..95
     float4 n0 = *reinterpret_cast<const float4*>(sU + sidx<float, 128>(64, 64 + 4 * c));
     float nr = rd[64];
 #pragma unroll 1
@@ -798,7 +798,7 @@ __device__ __forceinline__ void sweep_rows4_hi(float (&x)[4][4], const float* sU
 
 __device__ __forceinline__ void sweep_cols4_hi(float (&y)[4][4], const float* sL, int bw) {
     const int lane = threadIdx.x & 31, c = lane & 15, base = lane & 16;
-    const int nk = cdiv(bw - 64, 4);
+    const int nk = min(cdiv(bw - 64, 4), 8);   // steps 64..95
     float4 n0 = *reinterpret_cast<const float4*>(sL + sidx<float, 128>(64, 64 + 4 * c));
 #pragma unroll 1
     for (int kc = 0; kc < nk; ++kc) {
@@ -820,6 +820,51 @@ __device__ __forceinline__ void sweep_cols4_hi(float (&y)[4][4], const float* sL
 #pragma unroll
                 for (int ii = 0; ii < 4; ++ii)
                     if (ii != jn) y[l][ii] -= lv[ii] * yk[l];
+        }
+    }
+}
+
+// Third phase, from step 96 on: entries 96..127, lane c taking [96 + 2c,
+// 96 + 2c + 2) (moved from lane 8 + c / 2 of the second phase).
+__device__ __forceinline__ void sweep_to_top(const float (&x2)[4][4], float (&x3)[4][2]) {
+    const int lane = threadIdx.x & 31, c = lane & 15, src = (lane & 16) | (8 + (c >> 1));
+#pragma unroll
+    for (int l = 0; l < 4; ++l)
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const float v0 = __shfl_sync(0xffffffffu, x2[l][q], src), v1 = __shfl_sync(0xffffffffu, x2[l][2 + q], src);
+            x3[l][q] = (c & 1) ? v1 : v0;
+        }
+}
+
+template <bool ROWS>
+__device__ __forceinline__ void sweep_top(float (&x)[4][2], const float* sT, const float* rd, int bw) {
+    const int lane = threadIdx.x & 31, c = lane & 15, base = lane & 16;
+    const int nk = cdiv(bw - 96, 2);
+    float2 n0 = *reinterpret_cast<const float2*>(sT + sidx<float, 128>(96, 96 + 2 * c));
+    float nr = ROWS ? rd[96] : 0.f;
+#pragma unroll 1
+    for (int kc = 0; kc < nk; ++kc) {
+#pragma unroll
+        for (int kk = 0; kk < 2; ++kk) {
+            const int k = 96 + kc * 2 + kk;
+            const float2 u0 = n0;
+            const float r = nr;
+            const int kn = k + 1 < 128 ? k + 1 : k;
+            n0 = *reinterpret_cast<const float2*>(sT + sidx<float, 128>(kn, 96 + 2 * c));
+            if (ROWS) nr = rd[kn];
+            float xk[4];
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                if (ROWS && c == kc) x[l][kk] *= r;
+                xk[l] = __shfl_sync(0xffffffffu, x[l][kk], base | kc);
+            }
+            const float uv[2] = {u0.x, u0.y};
+            const int jn = (kk + 1) & 1;
+#pragma unroll
+            for (int l = 0; l < 4; ++l) x[l][jn] -= xk[l] * uv[jn];
+#pragma unroll
+            for (int l = 0; l < 4; ++l) x[l][kk] -= xk[l] * uv[kk];
         }
     }
 }
@@ -1003,17 +1048,20 @@ __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, cons
         sweep_rows4(x, sT, rd, bw, 8);   // steps 0..63
         float x2[4][4];
         sweep_to_hi(x, x2);
-        sweep_rows4_hi(x2, sT, rd, bw);  // steps 64..
+        sweep_rows4_hi(x2, sT, rd, bw);  // steps 64..95
+        float x3[4][2];
+        sweep_to_top(x2, x3);
+        sweep_top<true>(x3, sT, rd, bw);  // steps 96..
 #pragma unroll
-        for (int l = 0; l < 4; ++l) {   // entries 0..63 from the first phase, 64..127 from the second
+        for (int l = 0; l < 4; ++l) {   // entries 0..63, 64..95, 96..127 from the three phases
+            float* dst = sX + (line0 + l) * PT_LD;
             if (c < 8) {
-                *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 8 * c) = make_float4(x[l][0], x[l][1], x[l][2], x[l][3]);
-                *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 8 * c + 4) = make_float4(x[l][4], x[l][5], x[l][6], x[l][7]);
+                *reinterpret_cast<float4*>(dst + 8 * c) = make_float4(x[l][0], x[l][1], x[l][2], x[l][3]);
+                *reinterpret_cast<float4*>(dst + 8 * c + 4) = make_float4(x[l][4], x[l][5], x[l][6], x[l][7]);
+                *reinterpret_cast<float4*>(dst + 64 + 4 * c) = make_float4(x2[l][0], x2[l][1], x2[l][2], x2[l][3]);
             }
+            *reinterpret_cast<float2*>(dst + 96 + 2 * c) = make_float2(x3[l][0], x3[l][1]);
         }
-#pragma unroll
-        for (int l = 0; l < 4; ++l)
-            *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 64 + 4 * c) = make_float4(x2[l][0], x2[l][1], x2[l][2], x2[l][3]);
         __syncthreads();
         for (int e = tid; e < PT_LINES * 128; e += PT_LINES * 4) {
             int li, j;
@@ -1060,16 +1108,19 @@ __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, cons
         float y2[4][4];
         sweep_to_hi(y, y2);
         sweep_cols4_hi(y2, sT, bw);
+        float y3[4][2];
+        sweep_to_top(y2, y3);
+        sweep_top<false>(y3, sT, nullptr, bw);
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
+            float* dst = sX + (line0 + l) * PT_LD;
             if (c < 8) {
-                *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 8 * c) = make_float4(y[l][0], y[l][1], y[l][2], y[l][3]);
-                *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 8 * c + 4) = make_float4(y[l][4], y[l][5], y[l][6], y[l][7]);
+                *reinterpret_cast<float4*>(dst + 8 * c) = make_float4(y[l][0], y[l][1], y[l][2], y[l][3]);
+                *reinterpret_cast<float4*>(dst + 8 * c + 4) = make_float4(y[l][4], y[l][5], y[l][6], y[l][7]);
+                *reinterpret_cast<float4*>(dst + 64 + 4 * c) = make_float4(y2[l][0], y2[l][1], y2[l][2], y2[l][3]);
             }
+            *reinterpret_cast<float2*>(dst + 96 + 2 * c) = make_float2(y3[l][0], y3[l][1]);
         }
-#pragma unroll
-        for (int l = 0; l < 4; ++l)
-            *reinterpret_cast<float4*>(sX + (line0 + l) * PT_LD + 64 + 4 * c) = make_float4(y2[l][0], y2[l][1], y2[l][2], y2[l][3]);
         __syncthreads();
         for (int e = tid; e < PT_LINES * 128; e += PT_LINES * 4) {
             int li, R;
