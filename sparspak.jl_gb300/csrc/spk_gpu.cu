@@ -968,9 +968,10 @@ static int ensure_rhs(spk_handle* h, i64 nrhs) {
 // ---------------------------------------------------------------------------
 // Launch a solve kernel with programmatic stream serialisation: it may start
 // while its predecessor drains and waits for it with griddepcontrol.wait
-// after prefetching the factor data it needs.  The first chained kernel of a solve follows the
-// plain launch of k_permute, which starts only after the factorisation has
-// completed, so the factor data read before the wait is final.
+// after prefetching the factor data it needs.  The first chained kernel of a
+// solve follows the plain launch of k_permute, which starts only after the
+// factorisation has completed, so the factor data read before the wait is
+// final.
 template <typename... KArgs, typename... Args>
 static cudaError_t launch_chained(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t st,
                                   Args... args) {

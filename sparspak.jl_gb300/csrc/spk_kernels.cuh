@@ -313,15 +313,6 @@ template <> struct PivotKey<double> {
     __device__ static type of(double x, bool cand, bool diag) { return pivot_key(x, cand, diag); }
 };
 
-// r[k] for a runtime k < N, by selects (no dynamic register indexing).
-template <typename T, int N>
-__device__ __forceinline__ T pick_n(const T (&r)[N], int k) {
-    T v = r[0];
-#pragma unroll
-    for (int i = 1; i < N; ++i) v = (k == i) ? r[i] : v;
-    return v;
-}
-
 // Row sources of a block's interchanges: applying, piece by piece, the
 // swaps k <-> a + ipiv[k] of the piece [a, b) to a vector v gives
 // v'[R] = v[gmap[R]]; pa[R] = first row of R's piece.  One thread per piece.
@@ -930,27 +921,6 @@ __device__ __forceinline__ void pack_line(unsigned char* base, int t, int i, int
 #pragma unroll
     for (int g = 0; g < CQ / 4; ++g) {
         const int k = q * CQ + 4 * g;
-        if (k < nch * umma::KCH) {
-            unsigned char* dst = base + ((ll)t * nch + k / umma::KCH) * umma::PCHUNK + umma::packed_offset(i, k % umma::KCH);
-            uint32_t h[4], l[4];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                h[e] = umma::tf32_rna(v[4 * g + e]);
-                l[e] = umma::tf32_rna(v[4 * g + e] - __uint_as_float(h[e]));
-            }
-            *reinterpret_cast<uint4*>(dst) = make_uint4(h[0], h[1], h[2], h[3]);
-            *reinterpret_cast<uint4*>(dst + umma::OPB) = make_uint4(l[0], l[1], l[2], l[3]);
-        }
-    }
-}
-
-// Packed copy of a segment of a panel line: entries [k0, k0 + N) (N a
-// multiple of 4, k0 a multiple of 4) of line `i` at tile `t`.
-template <int N>
-__device__ __forceinline__ void pack_seg(unsigned char* base, int t, int i, int k0, int nch, const float (&v)[N]) {
-#pragma unroll
-    for (int g = 0; g < N / 4; ++g) {
-        const int k = k0 + 4 * g;
         if (k < nch * umma::KCH) {
             unsigned char* dst = base + ((ll)t * nch + k / umma::KCH) * umma::PCHUNK + umma::packed_offset(i, k % umma::KCH);
             uint32_t h[4], l[4];
