@@ -162,16 +162,22 @@ int spk_residual(spk_handle* h, const double* b, const double* x, int64_t nrhs, 
 /*
  * Allocation-free residual (no counterpart in the reference).  Same result
  * as spk_residual with device-resident b and x (n x nrhs, leading dimension
- * ld), for callers that cannot allocate device memory at call time: code
- * running inside a stream capture, under an external memory pool or budget,
- * or from a host callback.  It calls no cudaMalloc/cudaFree: its only work
- * space (two doubles per right-hand side) is a file-scope device array of
- * the library, held by every device that loads it until the process exits.
+ * ld), for callers that cannot allocate device memory when they call the
+ * library: applications that hand all device memory to their own pool or
+ * run under a fixed memory budget (a cudaMalloc there fails or evicts
+ * something else), and latency-critical loops that cannot afford the
+ * device-wide synchronisation cudaMalloc/cudaFree may cause.  It calls no
+ * cudaMalloc/cudaFree and no allocating library routine: its only work space
+ * (two doubles per right-hand side) is a file-scope device array of the
+ * library, held by every device that loads it until the process exits.
  * At most SPK_NOALLOC_MAX_RHS right-hand sides per call (SPK_EARG beyond).
- * The first call on a device looks up that array's device address, so make
- * it before any stream capture.  All calls share the array (it is cleared
- * at the start of each call): calls that overlap on the GPU, from any
- * handle on the same device, race.
+ * Like spk_residual it waits for the handle's stream before it returns.
+ * The first call on a device looks up that array's device address (with the
+ * device current) and keeps it for the life of the process, so make the
+ * first call before any stream capture, and do not use it across a
+ * cudaDeviceReset.  All calls share the array (it is cleared at the start of
+ * each call): calls that overlap on the GPU, from any handle on the same
+ * device, race.
  */
 #define SPK_NOALLOC_MAX_RHS 64
 int spk_residual_noalloc(spk_handle* h, const double* b, const double* x, int64_t nrhs, int64_t ld, double* relres);
@@ -195,14 +201,17 @@ int spk_stats(spk_handle* h, int64_t* nfronts, int64_t* nlevels, int64_t* factor
 #define SPK_K_ASSEMBLE 0   /* value scatter (_inmatrix!)                        */
 #define SPK_K_GETRF 1      /* first diagonal block of each front                */
 #define SPK_K_PANEL 2      /* panel triangular solves (_trsm!, _luswap!)         */
-#define SPK_K_TRAIL 3      /* rank-w update inside a front (+ next diagonal LU)  */
-#define SPK_K_SCHUR 4      /* front Schur complement + scatter-add (_gemm!, _assmb!) */
+#define SPK_K_TRAIL 3      /* rank-w update inside a front, CUDA cores           */
+#define SPK_K_SCHUR 4      /* front Schur complement + scatter-add (_gemm!, _assmb!),
+                              CUDA cores                                         */
 #define SPK_K_FWD 5        /* forward substitution (_lulsolve!)                 */
 #define SPK_K_BWD 6        /* backward substitution (_luusolve!)                */
 #define SPK_K_PERMUTE 7    /* right-hand side permutation                       */
 #define SPK_K_RESIDUAL 8   /* r = b - A x                                       */
 #define SPK_K_BLOCKINV 9   /* whole-block solve operators, after the factorisation */
-#define SPK_K_COUNT 10
+#define SPK_K_TC_TRAIL 10  /* rank-w update inside a front, tensor cores (tcgen05) */
+#define SPK_K_TC_SCHUR 11  /* front Schur complement + scatter-add, tensor cores  */
+#define SPK_K_COUNT 12
 
 /*
  * Launch accounting (no counterpart in the reference, whose only timing is

@@ -2,13 +2,22 @@
 
 ctypes binding of ``spk_oracle.c``, the plain-C restatement of the
 reference's numeric phase (_inmatrix!, _lufactor!, _lulsolve!, _luusolve!,
-_triangularsolve!; citations in the C file).  Only tests/, the smoke check
-of __graft_entry__ and bench.py's CPU-baseline leg use it, as the checker;
-the product never imports it.
+_triangularsolve!), and of ``spk_oracle_struct.c``, the restatement of its
+structure phase (graph symmetrisation here in numpy, multiple minimum
+degree, elimination tree, postorders, column counts, supernodes, symbolic
+factorisation) plus the grid nested-dissection ordering plug-in; citations
+in the C files.  Only tests/, the smoke check of __graft_entry__ and
+bench.py's CPU-baseline leg and reference arm use it, as the checker; the
+product never imports it, and it never loads the product's libraries.
+
+``use_blas()`` routes the dense calls through the BLAS/LAPACK that scipy
+bundles (OpenBLAS, threads = host cores), as the reference's Float64 path
+does through libblastrampoline (src/SparseSpdMethod/SpkSpdMMOps.jl:222-351).
 
 It is pinned against the reference's golden vectors in tests/golden/ (the
 post-inmatrix! and post-factor! lnz/unz of the n=11 tridiagonal problem and
-its intermediate forward-solve vector, test/test_sparse_method.jl).
+its intermediate forward-solve vector, the MMD permutation and the symbolic
+arrays, test/test_sparse_method.jl).
 """
 from __future__ import annotations
 
@@ -19,7 +28,7 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRC = os.path.join(HERE, "spk_oracle.c")
+SRCS = [os.path.join(HERE, "spk_oracle.c"), os.path.join(HERE, "spk_oracle_struct.c")]
 SO = os.path.join(HERE, "liboracle.so")
 
 _P = ctypes.POINTER(ctypes.c_int64)
@@ -29,8 +38,8 @@ _lib = None
 
 def build(force: bool = False) -> str:
     """Compile the oracle with gcc (no FMA contraction, so every host gives the same bits)."""
-    if force or not os.path.exists(SO) or os.path.getmtime(SO) < os.path.getmtime(SRC):
-        cmd = ["gcc", "-O2", "-std=c99", "-fPIC", "-shared", "-ffp-contract=off", "-o", SO, SRC, "-lm"]
+    if force or not os.path.exists(SO) or any(os.path.getmtime(SO) < os.path.getmtime(f) for f in SRCS):
+        cmd = ["gcc", "-O2", "-std=c99", "-fPIC", "-shared", "-ffp-contract=off", "-o", SO] + SRCS + ["-lm"]
         subprocess.run(cmd, check=True, capture_output=True)
     return SO
 
@@ -45,12 +54,30 @@ def lib():
         L.oracle_inmatrix_csc.argtypes = [i, i, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _D, _P, _D]
         L.oracle_lufactor.restype = i
         L.oracle_lufactor.argtypes = [i, i, _P, _P, _P, _P, _P, _D, _P, _D, _P, _P]
+        L.oracle_lu_begin.restype = ctypes.c_void_p
+        L.oracle_lu_begin.argtypes = [i, i, _P, _P, _P, _P, _P, _D, _P, _D, _P]
+        L.oracle_lu_run.restype = i
+        L.oracle_lu_run.argtypes = [ctypes.c_void_p, i]
+        L.oracle_lu_end.restype = i
+        L.oracle_lu_end.argtypes = [ctypes.c_void_p, _P]
         L.oracle_lulsolve.restype = None
         L.oracle_lulsolve.argtypes = [i, _P, _P, _P, _P, _D, _P, _D]
         L.oracle_luusolve.restype = None
         L.oracle_luusolve.argtypes = [i, i, _P, _P, _P, _P, _D, _P, _D, _D]
         L.oracle_triangularsolve.restype = None
         L.oracle_triangularsolve.argtypes = [i, i, _P, _P, _P, _P, _D, _P, _D, _P, _P, _P, _D]
+        vp = ctypes.c_void_p
+        L.oracle_set_blas.restype = None
+        L.oracle_set_blas.argtypes = [vp, vp, vp, vp, vp]
+        L.oracle_blas_mode.restype = ctypes.c_int
+        L.oracle_mmd.restype = None
+        L.oracle_mmd.argtypes = [i, _P, _P, _P, _P]
+        L.oracle_nd_grid.restype = i
+        L.oracle_nd_grid.argtypes = [i, i, i, i, _P, _P, _P, _P]
+        L.oracle_symbolic1.restype = i
+        L.oracle_symbolic1.argtypes = [i, _P, _P, _P, _P, i, _P, _P, _P, _P, _P, _P]
+        L.oracle_symbolic2.restype = i
+        L.oracle_symbolic2.argtypes = [i, _P, _P, _P, _P, _P, i, _P, _P, _P, _P]
         _lib = L
     return _lib
 
@@ -104,6 +131,23 @@ class OracleLU:
         self.first_singular = int(fs[0])
         return int(iflag)
 
+    def factor_slices(self, bounds):
+        """_lufactor! run as consecutive slices of supernodes: bounds[k] is the
+        last (1-based) supernode of slice k.  Yields after each slice (the
+        caller times them); returns iflag like factor()."""
+        L = lib()
+        ctx = L.oracle_lu_begin(self.n, self.nsuper, _p(self.xsuper), _p(self.snode), _p(self.xlindx),
+                                _p(self.lindx), _p(self.xlnz), _d(self.lnz), _p(self.xunz), _d(self.unz),
+                                _p(self.ipiv))
+        try:
+            for js_end in bounds:
+                L.oracle_lu_run(ctx, int(js_end))
+                yield int(js_end)
+        finally:
+            fs = np.zeros(1, dtype=np.int64)
+            self.iflag = int(L.oracle_lu_end(ctx, _p(fs)))
+            self.first_singular = int(fs[0])
+
     def lulsolve(self, rhs_permuted):
         r = np.ascontiguousarray(rhs_permuted, np.float64).copy()
         lib().oracle_lulsolve(self.nsuper, _p(self.xsuper), _p(self.xlindx), _p(self.lindx), _p(self.xlnz),
@@ -122,3 +166,165 @@ class OracleLU:
                                          _p(self.rperm), _p(self.rinvp), _d(v))
             out[:, j] = v
         return out.reshape(b.shape)
+
+
+# ---------------------------------------------------------------------------
+# BLAS mode
+# ---------------------------------------------------------------------------
+
+_blas_info = None
+
+
+def use_blas(on: bool = True) -> dict | None:
+    """Route the oracle's dense calls through scipy's BLAS/LAPACK (LP64
+    Fortran interface, taken from scipy.linalg.cython_blas / cython_lapack),
+    or back to the generic loops.  Returns a description of the library
+    (name, threads) or None when switched off."""
+    global _blas_info
+    L = lib()
+    if not on:
+        L.oracle_set_blas(None, None, None, None, None)
+        return None
+    import scipy.linalg.cython_blas as cb
+    import scipy.linalg.cython_lapack as cl
+
+    get = ctypes.pythonapi.PyCapsule_GetPointer
+    get.restype = ctypes.c_void_p
+    get.argtypes = [ctypes.py_object, ctypes.c_char_p]
+    getname = ctypes.pythonapi.PyCapsule_GetName
+    getname.restype = ctypes.c_char_p
+    getname.argtypes = [ctypes.py_object]
+
+    def fn(mod, name):
+        cap = mod.__pyx_capi__[name]
+        return get(cap, getname(cap))
+
+    L.oracle_set_blas(fn(cb, "dgemm"), fn(cb, "dtrsm"), fn(cl, "dgetrf"), fn(cl, "dlaswp"), fn(cb, "dgemv"))
+    if _blas_info is None:
+        _blas_info = {"library": "scipy-bundled BLAS", "threads": os.cpu_count()}
+        try:
+            import glob
+
+            import scipy
+
+            libs = glob.glob(os.path.join(os.path.dirname(scipy.__file__), os.pardir, "scipy.libs", "*openblas*"))
+            if libs:
+                ob = ctypes.CDLL(libs[0])
+                _blas_info["library"] = "OpenBLAS (" + os.path.basename(libs[0]) + ")"
+                for sym in ("scipy_openblas_get_num_threads", "openblas_get_num_threads"):
+                    if hasattr(ob, sym):
+                        f = getattr(ob, sym)
+                        f.restype = ctypes.c_int
+                        _blas_info["threads"] = int(f())
+                        break
+        except OSError:
+            pass
+    return dict(_blas_info)
+
+
+# ---------------------------------------------------------------------------
+# structure phase
+# ---------------------------------------------------------------------------
+
+
+class _Order:
+    def __init__(self, rperm, rinvp):
+        self.rperm, self.rinvp = rperm, rinvp
+
+
+class OracleStructure:
+    """What _symbolicfactor! leaves in a _SparseBase: n, nsuper, xsuper,
+    snode, xlindx, lindx, xlnz, xunz, colcnt and order.rperm/rinvp (all
+    1-based int64), computed by the oracle alone."""
+
+    def __init__(self, n, perm, invp, colcnt, nsuper, xsuper, snode, xlindx, lindx, xlnz, xunz):
+        self.n, self.nsuper = int(n), int(nsuper)
+        self.order = _Order(perm, invp)
+        self.colcnt, self.xsuper, self.snode = colcnt, xsuper, snode
+        self.xlindx, self.lindx, self.xlnz, self.xunz = xlindx, lindx, xlnz, xunz
+
+
+def graph_of(colptr, rowval, n):
+    """Graph(m::SparseMatrixCSC) followed by makestructuresymmetric
+    (src/SparseCSCInterface/SparseCSCInterface.jl:12-56,
+    src/Graph/SpkGraph.jl:94-289): column lists without the diagonal; a
+    structurally symmetric pattern is kept as stored, otherwise the lists
+    become the sorted union of A's and A^T's."""
+    colptr = np.asarray(colptr, np.int64)
+    rowval = np.asarray(rowval, np.int64)
+    cols = np.repeat(np.arange(1, n + 1, dtype=np.int64), np.diff(colptr))
+    keep = rowval != cols
+    r, c = rowval[keep], cols[keep]
+    fwd = set(zip(r.tolist(), c.tolist())) if r.size < 2_000_000 else None
+    if fwd is not None:
+        sym = all((b, a) in fwd for a, b in fwd)
+    else:
+        key = np.sort(r * (n + 1) + c)
+        key_t = np.sort(c * (n + 1) + r)
+        sym = np.array_equal(key, key_t)
+    if not sym:
+        rr = np.concatenate([r, c])
+        cc = np.concatenate([c, r])
+        key = np.unique(cc * (n + 1) + rr)
+        c, r = key // (n + 1), key % (n + 1)
+    counts = np.bincount(c - 1, minlength=n)
+    xadj = np.concatenate([[1], 1 + np.cumsum(counts)]).astype(np.int64)
+    return xadj, np.ascontiguousarray(r, dtype=np.int64)
+
+
+def mmd(xadj, adj, n):
+    """_generalmmd: (perm, invp), 1-based."""
+    perm = np.zeros(n, np.int64)
+    invp = np.zeros(n, np.int64)
+    lib().oracle_mmd(n, _p(xadj), _p(adj), _p(perm), _p(invp))
+    return perm, invp
+
+
+def nd_grid(xadj, adj, nx, ny, nz=1, leaf=64):
+    """Grid nested dissection (the ordering plug-in), (perm, invp), 1-based."""
+    n = nx * ny * nz
+    perm = np.zeros(n, np.int64)
+    invp = np.zeros(n, np.int64)
+    got = lib().oracle_nd_grid(nx, ny, nz, leaf, _p(xadj), _p(adj), _p(perm), _p(invp))
+    if got != n:
+        raise ValueError(f"nested dissection ordered {got} of {n} vertices")
+    return perm, invp
+
+
+def symbolic(xadj, adj, perm, invp, maxblocksize=30) -> OracleStructure:
+    """_symbolicfactor! for the graph and an initial ordering."""
+    n = int(xadj.shape[0] - 1)
+    perm = np.ascontiguousarray(perm, np.int64).copy()
+    invp = np.ascontiguousarray(invp, np.int64).copy()
+    colcnt = np.zeros(n, np.int64)
+    snode = np.zeros(n, np.int64)
+    xsuper = np.zeros(n + 1, np.int64)
+    xlnz = np.zeros(n + 1, np.int64)
+    xunz = np.zeros(n + 1, np.int64)
+    nsub = np.zeros(1, np.int64)
+    L = lib()
+    nsuper = int(L.oracle_symbolic1(n, _p(xadj), _p(adj), _p(perm), _p(invp), maxblocksize, _p(colcnt), _p(snode),
+                                    _p(xsuper), _p(xlnz), _p(xunz), _p(nsub)))
+    xsuper = xsuper[: nsuper + 1].copy()
+    xlindx = np.zeros(nsuper + 1, np.int64)
+    lindx = np.zeros(max(int(nsub[0]), 1), np.int64)
+    rc = L.oracle_symbolic2(n, _p(xadj), _p(adj), _p(perm), _p(invp), _p(colcnt), nsuper, _p(xsuper), _p(snode),
+                            _p(xlindx), _p(lindx))
+    if rc != 0:
+        raise ValueError("Inconsistency in data structure.")
+    return OracleStructure(n, perm, invp, colcnt, nsuper, xsuper, snode, xlindx, lindx[: int(nsub[0])], xlnz, xunz)
+
+
+def structure_csc(colptr, rowval, n, ordering="mmd", grid=None, leaf=64, maxblocksize=30) -> OracleStructure:
+    """Ordering + symbolic factorisation of a CSC pattern (1-based colptr /
+    rowval): ordering "mmd" (the reference default) or "nd" with
+    grid = (nx, ny, nz)."""
+    xadj, adj = graph_of(colptr, rowval, n)
+    if ordering == "mmd":
+        perm, invp = mmd(xadj, adj, n)
+    elif ordering == "nd":
+        nx, ny, nz = grid
+        perm, invp = nd_grid(xadj, adj, nx, ny, nz, leaf)
+    else:
+        raise ValueError(ordering)
+    return symbolic(xadj, adj, perm, invp, maxblocksize)

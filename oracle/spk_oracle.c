@@ -113,6 +113,64 @@ static void o_trsv_lunn(i64 m, const double* a, i64 lda, double* b) {
         }
 }
 
+
+/* ---- optional BLAS/LAPACK mode ------------------------------------------- */
+
+/* The reference calls BLAS/LAPACK for Float64 (dgemm_, dgetrf_, dtrsm_,
+ * dlaswp_, dgemv_: src/SparseSpdMethod/SpkSpdMMOps.jl:222-351).  With
+ * oracle_set_blas the same calls go to the given routines (LP64 Fortran
+ * interface, e.g. the OpenBLAS bundled with scipy); without it the generic
+ * loops above are used (the reference's path for other element types). */
+typedef void (*dgemm_f)(char*, char*, int*, int*, int*, double*, double*, int*, double*, int*, double*, double*, int*);
+typedef void (*dtrsm_f)(char*, char*, char*, char*, int*, int*, double*, double*, int*, double*, int*);
+typedef void (*dgetrf_f)(int*, int*, double*, int*, int*, int*);
+typedef void (*dlaswp_f)(int*, double*, int*, int*, int*, int*, int*);
+typedef void (*dgemv_f)(char*, int*, int*, double*, double*, int*, double*, int*, double*, double*, int*);
+static struct {
+    dgemm_f gemm;
+    dtrsm_f trsm;
+    dgetrf_f getrf;
+    dlaswp_f laswp;
+    dgemv_f gemv;
+} g_blas;
+
+/* All five pointers, or all NULL to return to the generic loops. */
+void oracle_set_blas(void* gemm, void* trsm, void* getrf, void* laswp, void* gemv) {
+    g_blas.gemm = (dgemm_f)gemm;
+    g_blas.trsm = (dtrsm_f)trsm;
+    g_blas.getrf = (dgetrf_f)getrf;
+    g_blas.laswp = (dlaswp_f)laswp;
+    g_blas.gemv = (dgemv_f)gemv;
+}
+
+int oracle_blas_mode(void) { return g_blas.gemm != NULL; }
+
+/* _gemm!('n','t') */
+static void x_gemm_nt(i64 m, i64 n, i64 k, double alpha, double* a, i64 lda, double* b, i64 ldb, double beta, double* c,
+                      i64 ldc) {
+    if (!g_blas.gemm) { o_gemm_nt(m, n, k, alpha, a, lda, b, ldb, beta, c, ldc); return; }
+    char tn = 'N', tt = 'T';
+    int im = (int)m, in = (int)n, ik = (int)k, ia = (int)lda, ib = (int)ldb, ic = (int)ldc;
+    g_blas.gemm(&tn, &tt, &im, &in, &ik, &alpha, a, &ia, b, &ib, &beta, c, &ic);
+}
+
+/* _getrf! on an n x n block; ipiv local 1..n */
+static void x_getrf(i64 n, double* a, i64 lda, i64* ipiv) {
+    if (!g_blas.getrf) { o_getrf(n, n, a, lda, ipiv); return; }
+    int in = (int)n, ia = (int)lda, info = 0;
+    int* p = (int*)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    g_blas.getrf(&in, &in, a, &ia, p, &info);
+    for (i64 k = 0; k < n; ++k) ipiv[k] = p[k];
+    free(p);
+}
+
+/* _trsm!(side, uplo, transa, diag) with alpha = 1 */
+static void x_trsm(char side, char uplo, char ta, char diag, i64 m, i64 n, double* a, i64 lda, double* b, i64 ldb) {
+    int im = (int)m, in = (int)n, ia = (int)lda, ib = (int)ldb;
+    double one = 1.0;
+    g_blas.trsm(&side, &uplo, &ta, &diag, &im, &in, &one, a, &ia, b, &ib);
+}
+
 /* ---- _inmatrix! (CSC) ---------------------------------------------------- */
 
 /* Returns 0, or -(1 + position) of the first entry with no slot. */
@@ -155,27 +213,55 @@ i64 oracle_inmatrix_csc(i64 n, i64 ncols, const i64* colptr, const i64* rowval, 
 
 /* ---- _lufactor! ---------------------------------------------------------- */
 
-/* Returns iflag as the reference computes it (last diagonal block wins),
- * and in *first_singular the first supernode whose block had a zero pivot. */
-i64 oracle_lufactor(i64 n, i64 nsuper, const i64* xsuper, const i64* snode, const i64* xlindx, const i64* lindx,
-                    const i64* xlnz, double* lnz, const i64* xunz, double* unz, i64* ipvt, i64* first_singular) {
-    i64* link = (i64*)calloc((size_t)nsuper + 1, sizeof(i64));
-    i64* lngth = (i64*)calloc((size_t)nsuper + 1, sizeof(i64));
-    i64* map = (i64*)calloc((size_t)n + 1, sizeof(i64));
-    i64* relind = (i64*)calloc((size_t)n + 1, sizeof(i64));
-    i64 tmpsiz = 0, iflag = 0;
-    *first_singular = 0;
+/* State of one left-looking factorisation, so that it can run in slices of
+ * consecutive supernodes (bench.py's reference arm times the slices of one
+ * complete factorisation as its steps). */
+typedef struct {
+    i64 n, nsuper;
+    const i64 *xsuper, *snode, *xlindx, *lindx, *xlnz, *xunz;
+    double *lnz, *unz;
+    i64* ipvt;
+    i64 *link, *lngth, *map, *relind;
+    double* temp;
+    i64 tmpsiz, iflag, first_singular, next;
+} LuCtx;
+
+void* oracle_lu_begin(i64 n, i64 nsuper, const i64* xsuper, const i64* snode, const i64* xlindx, const i64* lindx,
+                      const i64* xlnz, double* lnz, const i64* xunz, double* unz, i64* ipvt) {
+    LuCtx* c = (LuCtx*)calloc(1, sizeof(LuCtx));
+    c->n = n; c->nsuper = nsuper;
+    c->xsuper = xsuper; c->snode = snode; c->xlindx = xlindx; c->lindx = lindx; c->xlnz = xlnz; c->xunz = xunz;
+    c->lnz = lnz; c->unz = unz; c->ipvt = ipvt;
+    c->link = (i64*)calloc((size_t)nsuper + 1, sizeof(i64));
+    c->lngth = (i64*)calloc((size_t)nsuper + 1, sizeof(i64));
+    c->map = (i64*)calloc((size_t)n + 1, sizeof(i64));
+    c->relind = (i64*)calloc((size_t)n + 1, sizeof(i64));
     for (i64 i = 1; i <= nsuper; ++i) {
-        lngth[i] = A1(xlindx, i + 1) - A1(xlindx, i);
+        c->lngth[i] = A1(xlindx, i + 1) - A1(xlindx, i);
         i64 w = A1(xsuper, i + 1) - A1(xsuper, i);
         i64 need = w * (A1(xlnz, A1(xsuper, i) + 1) - A1(xlnz, A1(xsuper, i)));
-        if (need > tmpsiz) tmpsiz = need;
+        if (need > c->tmpsiz) c->tmpsiz = need;
     }
-    double* temp = (double*)calloc((size_t)tmpsiz + 1, sizeof(double));
-    double* L = lnz - 1; /* L[p] == reference lnz[p] */
-    double* U = unz - 1;
+    c->temp = (double*)calloc((size_t)c->tmpsiz + 1, sizeof(double));
+    c->next = 1;
+    return c;
+}
 
-    for (i64 js = 1; js <= nsuper; ++js) {
+/* Factor supernodes c->next .. js_end (the body of _lufactor!'s jsup loop,
+ * SpkLUFactor.jl:89-252); returns the next supernode to factor. */
+i64 oracle_lu_run(void* ctx, i64 js_end) {
+    LuCtx* c = (LuCtx*)ctx;
+    const i64 *xsuper = c->xsuper, *snode = c->snode, *xlindx = c->xlindx, *lindx = c->lindx, *xlnz = c->xlnz,
+              *xunz = c->xunz;
+    i64* ipvt = c->ipvt;
+    i64 *link = c->link, *lngth = c->lngth, *map = c->map, *relind = c->relind;
+    double* temp = c->temp;
+    const i64 tmpsiz = c->tmpsiz;
+    i64 iflag = c->iflag;
+    double* L = c->lnz - 1; /* L[p] == reference lnz[p] */
+    double* U = c->unz - 1;
+    if (js_end > c->nsuper) js_end = c->nsuper;
+    for (i64 js = c->next; js <= js_end; ++js) {
         i64 fj = A1(xsuper, js), lj = A1(xsuper, js + 1) - 1, nj = lj - fj + 1;
         i64 jlen = A1(xlnz, fj + 1) - A1(xlnz, fj);
         i64 jx = A1(xlindx, js), jl = A1(xlnz, fj), ju = A1(xunz, fj);
@@ -195,9 +281,9 @@ i64 oracle_lufactor(i64 n, i64 nsuper, const i64* xsuper, const i64* snode, cons
             i64 ku = A1(xunz, fk + 1) - klen;
             i64 nups;
             if (klen == jlen) {
-                o_gemm_nt(jlen, nj, nk, -1.0, &L[kl], kslen, &U[ku], kslen - nk, 1.0, &L[jl], jlen);
+                x_gemm_nt(jlen, nj, nk, -1.0, &L[kl], kslen, &U[ku], kslen - nk, 1.0, &L[jl], jlen);
                 if (jlen > nj)
-                    o_gemm_nt(jlen - nj, nj, nk, -1.0, &U[ku + nj], kslen - nk, &L[kl], kslen, 1.0, &U[ju],
+                    x_gemm_nt(jlen - nj, nj, nk, -1.0, &U[ku + nj], kslen - nk, &L[kl], kslen, 1.0, &U[ju],
                               jlen - nj);
                 nups = nj;
                 if (klen > nj) nxt = A1(lindx, jx + nj);
@@ -225,22 +311,22 @@ i64 oracle_lufactor(i64 n, i64 nsuper, const i64* xsuper, const i64* snode, cons
                     i64 inddif = map[kfirst] - map[klast];
                     if (inddif < klen) {
                         i64 il = A1(xlnz, kfirst) + (kfirst - fj);
-                        o_gemm_nt(klen, nups, nk, -1.0, &L[kl], kslen, &U[ku], kslen - nk, 1.0, &L[il], jlen);
+                        x_gemm_nt(klen, nups, nk, -1.0, &L[kl], kslen, &U[ku], kslen - nk, 1.0, &L[il], jlen);
                         i64 iu = A1(xunz, kfirst);
                         if (klen > nups)
-                            o_gemm_nt(klen - nups, nups, nk, -1.0, &U[ku + nups], kslen - nk, &L[kl], kslen, 1.0,
+                            x_gemm_nt(klen - nups, nups, nk, -1.0, &U[ku + nups], kslen - nk, &L[kl], kslen, 1.0,
                                       &U[iu], jlen - nj);
                     } else {
                         if (klen * nups > tmpsiz) iflag = -2;
                         for (i64 j = 1; j <= klen; ++j) relind[j] = map[A1(lindx, kx + j - 1)];
-                        o_gemm_nt(klen, nups, nk, -1.0, &L[kl], kslen, &U[ku], kslen - nk, 0.0, temp, klen);
+                        x_gemm_nt(klen, nups, nk, -1.0, &L[kl], kslen, &U[ku], kslen - nk, 0.0, temp, klen);
                         /* _assmb! into the columns of L */
                         for (i64 j = 1; j <= nups; ++j) {
                             i64 lbot = A1(xlnz, fj + jlen - relind[j]) - 1;
                             for (i64 k = 1; k <= klen; ++k) L[lbot - relind[k]] += temp[(j - 1) * klen + k - 1];
                         }
                         if (klen > nups) {
-                            o_gemm_nt(klen - nups, nups, nk, -1.0, &U[ku + nups], kslen - nk, &L[kl], kslen, 0.0,
+                            x_gemm_nt(klen - nups, nups, nk, -1.0, &U[ku + nups], kslen - nk, &L[kl], kslen, 0.0,
                                       temp, klen - nups);
                             for (i64 j = 1; j <= nups; ++j) {
                                 i64 lbot = A1(xunz, fj + jlen - relind[j]) - 1;
@@ -261,15 +347,16 @@ i64 oracle_lufactor(i64 n, i64 nsuper, const i64* xsuper, const i64* snode, cons
             }
         }
         /* diagonal block, then the two panels */
-        o_getrf(nj, nj, &L[jl], jlen, &A1(ipvt, fj));
+        x_getrf(nj, &L[jl], jlen, &A1(ipvt, fj));
         {
             int sing = 0;
             for (i64 k = 0; k < nj; ++k)
                 if (L[jl + k * jlen + k] == 0.0) sing = 1;
             iflag = sing ? -1 : 0;
-            if (sing && *first_singular == 0) *first_singular = js;
+            if (sing && c->first_singular == 0) c->first_singular = js;
         }
-        o_trsm_runn(jlen - nj, nj, &L[jl], jlen, &L[jl + nj], jlen);
+        if (g_blas.trsm) x_trsm('R', 'U', 'N', 'N', jlen - nj, nj, &L[jl], jlen, &L[jl + nj], jlen);
+        else o_trsm_runn(jlen - nj, nj, &L[jl], jlen, &L[jl + nj], jlen);
         if (jlen > nj) {
             /* _luswap!: swap U-panel rows k <-> ipvt[k], in order */
             i64 ld = jlen - nj;
@@ -279,7 +366,8 @@ i64 oracle_lufactor(i64 n, i64 nsuper, const i64* xsuper, const i64* snode, cons
                 double* cb = &U[ju + (ip - 1) * ld];
                 for (i64 t = 0; t < ld; ++t) { double x = cb[t]; cb[t] = ca[t]; ca[t] = x; }
             }
-            o_trsm_rltu(jlen - nj, nj, &L[jl], jlen, &U[ju], jlen - nj);
+            if (g_blas.trsm) x_trsm('R', 'L', 'T', 'U', jlen - nj, nj, &L[jl], jlen, &U[ju], jlen - nj);
+            else o_trsm_rltu(jlen - nj, nj, &L[jl], jlen, &U[ju], jlen - nj);
         }
         if (jlen > nj) {
             nxt = A1(lindx, jx + nj);
@@ -291,12 +379,29 @@ i64 oracle_lufactor(i64 n, i64 nsuper, const i64* xsuper, const i64* snode, cons
             lngth[js] = 0;
         }
     }
-    free(link);
-    free(lngth);
-    free(map);
-    free(relind);
-    free(temp);
+    c->iflag = iflag;
+    c->next = js_end + 1;
+    return c->next;
+}
+
+/* Returns iflag as the reference computes it (last diagonal block wins),
+ * and in *first_singular the first supernode whose block had a zero pivot;
+ * releases the state. */
+i64 oracle_lu_end(void* ctx, i64* first_singular) {
+    LuCtx* c = (LuCtx*)ctx;
+    i64 iflag = c->iflag;
+    *first_singular = c->first_singular;
+    free(c->link); free(c->lngth); free(c->map); free(c->relind); free(c->temp);
+    free(c);
     return iflag;
+}
+
+/* _lufactor! in one call. */
+i64 oracle_lufactor(i64 n, i64 nsuper, const i64* xsuper, const i64* snode, const i64* xlindx, const i64* lindx,
+                    const i64* xlnz, double* lnz, const i64* xunz, double* unz, i64* ipvt, i64* first_singular) {
+    void* c = oracle_lu_begin(n, nsuper, xsuper, snode, xlindx, lindx, xlnz, lnz, xunz, unz, ipvt);
+    oracle_lu_run(c, nsuper);
+    return oracle_lu_end(c, first_singular);
 }
 
 /* ---- _lulsolve! / _luusolve! ---------------------------------------------- */
@@ -305,10 +410,27 @@ void oracle_lulsolve(i64 nsuper, const i64* xsuper, const i64* xlindx, const i64
                      const double* lnz, const i64* ipiv, double* rhs) {
     const double* L = lnz - 1;
     double* R = rhs - 1;
+    i64 maxlen = 1;
+    for (i64 js = 1; js <= nsuper; ++js)
+        if (A1(xlindx, js + 1) - A1(xlindx, js) > maxlen) maxlen = A1(xlindx, js + 1) - A1(xlindx, js);
+    double* temp = g_blas.gemv ? (double*)calloc((size_t)maxlen, sizeof(double)) : NULL;
+    int* ip32 = g_blas.laswp ? (int*)calloc((size_t)maxlen, sizeof(int)) : NULL;
     for (i64 js = 1; js <= nsuper; ++js) {
         i64 fj = A1(xsuper, js), nj = A1(xsuper, js + 1) - fj;
         i64 jlen = A1(xlnz, fj + 1) - A1(xlnz, fj);
         i64 jx = A1(xlindx, js), jl = A1(xlnz, fj);
+        if (g_blas.gemv) {   /* _laswp!, _trsm!('l','l','n','u'), _gemv!('n'), scatter-add */
+            int one = 1, inj = (int)nj, im = (int)(jlen - nj), ild = (int)jlen, inc = 1;
+            double mone = -1.0, zero = 0.0;
+            for (i64 i = 0; i < nj; ++i) ip32[i] = (int)A1(ipiv, fj + i);
+            g_blas.laswp(&one, &R[fj], &inj, &one, &inj, ip32, &inc);
+            x_trsm('L', 'L', 'N', 'U', nj, 1, (double*)&L[jl], jlen, &R[fj], nj);
+            if (im > 0) {
+                g_blas.gemv("N", &im, &inj, &mone, (double*)&L[jl + nj], &ild, &R[fj], &inc, &zero, temp, &inc);
+                for (i64 j = 1; j <= jlen - nj; ++j) R[A1(lindx, jx + nj + j - 1)] += temp[j - 1];
+            }
+            continue;
+        }
         for (i64 i = 1; i <= nj; ++i) { /* glaswp! */
             i64 ip = A1(ipiv, fj + i - 1);
             if (ip != i) { double t = R[fj + i - 1]; R[fj + i - 1] = R[fj + ip - 1]; R[fj + ip - 1] = t; }
@@ -320,6 +442,8 @@ void oracle_lulsolve(i64 nsuper, const i64* xsuper, const i64* xlindx, const i64
             R[A1(lindx, jx + nj + j - 1)] += t;
         }
     }
+    free(temp);
+    free(ip32);
 }
 
 void oracle_luusolve(i64 n, i64 nsuper, const i64* xsuper, const i64* xlindx, const i64* lindx, const i64* xlnz,
@@ -328,10 +452,24 @@ void oracle_luusolve(i64 n, i64 nsuper, const i64* xsuper, const i64* xlindx, co
     const double* L = lnz - 1;
     const double* U = unz - 1;
     double* R = rhs - 1;
+    i64 maxlen = 1;
+    for (i64 js = 1; js <= nsuper; ++js)
+        if (A1(xlindx, js + 1) - A1(xlindx, js) > maxlen) maxlen = A1(xlindx, js + 1) - A1(xlindx, js);
+    double* temp = g_blas.gemv ? (double*)calloc((size_t)maxlen, sizeof(double)) : NULL;
     for (i64 js = nsuper; js >= 1; --js) {
         i64 fj = A1(xsuper, js), nj = A1(xsuper, js + 1) - fj;
         i64 jlen = A1(xlnz, fj + 1) - A1(xlnz, fj);
         i64 jx = A1(xlindx, js), jl = A1(xlnz, fj), ju = A1(xunz, fj);
+        if (g_blas.gemv) {   /* gather, _gemv!('t'), _trsm!('l','u','n','n') */
+            if (jlen > nj) {
+                int im = (int)(jlen - nj), inj = (int)nj, inc = 1;
+                double mone = -1.0, one = 1.0;
+                for (i64 j = 1; j <= jlen - nj; ++j) temp[j - 1] = R[A1(lindx, jx + nj + j - 1)];
+                g_blas.gemv("T", &im, &inj, &mone, (double*)&U[ju], &im, temp, &inc, &one, &R[fj], &inc);
+            }
+            x_trsm('L', 'U', 'N', 'N', nj, 1, (double*)&L[jl], jlen, &R[fj], nj);
+            continue;
+        }
         if (jlen > nj) { /* gather, then ggemv!('t') */
             for (i64 k = 0; k < nj; ++k) {
                 double t = 0.0;
@@ -341,6 +479,7 @@ void oracle_luusolve(i64 n, i64 nsuper, const i64* xsuper, const i64* xlindx, co
         }
         o_trsv_lunn(nj, &L[jl], jlen, &R[fj]);
     }
+    free(temp);
 }
 
 /* _triangularsolve!: permute, forward, backward, unpermute (in place). */

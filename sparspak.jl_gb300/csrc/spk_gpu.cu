@@ -1081,7 +1081,7 @@ static int factor_launches(spk_handle* h) {
                         CU(h, cudaStreamWaitEvent(h->side, h->evP, 0));
                         st = h->side;
                     }
-                    LaunchScope ls(h, SPK_K_TRAIL, P.btrail_tc[t].flops, P.btrail_tc[t].words * sizeof(T));
+                    LaunchScope ls(h, SPK_K_TC_TRAIL, P.btrail_tc[t].flops, P.btrail_tc[t].words * sizeof(T));
                     spk::k_tc_update<spk::TC_TRAIL><<<grid, spk::TC_THREADS, spk::umma::PSMEM, st>>>(
                         fac, storage<T>(h).pack, S, launch_of(PL, P.btrail_tc[t]), (int)t, nt, 1, h->d_info + 1);
                     if (ahead) {
@@ -1091,7 +1091,7 @@ static int factor_launches(spk_handle* h) {
                 }
                 // Tile 0 (the next block's diagonal block) on the launch stream.
                 if (P.btrail_tc0[t].tiles > 0) {
-                    LaunchScope ls(h, SPK_K_TRAIL, P.btrail_tc0[t].flops, P.btrail_tc0[t].words * sizeof(T));
+                    LaunchScope ls(h, SPK_K_TC_TRAIL, P.btrail_tc0[t].flops, P.btrail_tc0[t].words * sizeof(T));
                     const int nt = P.btrail_tc0[t].tiles;
                     spk::k_tc_update<spk::TC_TRAIL><<<std::min(nt, h->nsm), spk::TC_THREADS, spk::umma::PSMEM, h->stream>>>(
                         fac, storage<T>(h).pack, S, launch_of(PL, P.btrail_tc0[t]), (int)t, nt, 0, h->d_info + 1);
@@ -1108,7 +1108,7 @@ static int factor_launches(spk_handle* h) {
         }
         if constexpr (std::is_same<T, float>::value) {
             if (P.schur_tc.tiles > 0) {
-                LaunchScope ls(h, SPK_K_SCHUR, P.schur_tc.flops, P.schur_tc.words * sizeof(T));
+                LaunchScope ls(h, SPK_K_TC_SCHUR, P.schur_tc.flops, P.schur_tc.words * sizeof(T));
                 const int nt = P.schur_tc.tiles;
                 spk::k_tc_update<spk::TC_SCHUR><<<std::min(nt, h->nsm), spk::TC_THREADS, spk::umma::PSMEM, h->stream>>>(
                     fac, storage<T>(h).pack, S, launch_of(PL, P.schur_tc), 0, nt, 0, h->d_info + 1);

@@ -23,7 +23,8 @@ GPU_SO = os.path.join(LIBDIR, "libspk_gpu.so")
 
 HOST_SRC = [os.path.join(CSRC, "spk_symbolic.cpp")]
 GPU_SRC = [os.path.join(CSRC, "spk_gpu.cu")]
-GPU_DEPS = GPU_SRC + [os.path.join(CSRC, "spk_kernels.cuh"), os.path.join(INCLUDE, "spk_gpu.h")]
+GPU_DEPS = GPU_SRC + [os.path.join(CSRC, "spk_kernels.cuh"), os.path.join(CSRC, "spk_umma.cuh"),
+                      os.path.join(INCLUDE, "spk_gpu.h")]
 HOST_DEPS = HOST_SRC + [os.path.join(INCLUDE, "spk_host.h")]
 
 NVCC = os.environ.get("SPK_NVCC", "nvcc")

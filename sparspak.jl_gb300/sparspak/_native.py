@@ -57,15 +57,18 @@ GPU_SYMBOLS = {
 
 SPK_OK, SPK_EARG, SPK_ECUDA, SPK_ENOMEM, SPK_ESEQ, SPK_ESTRUCT, SPK_ESINGULAR, SPK_ENOCONV = 0, -1, -2, -3, -4, -5, -6, -7
 SPK_HOST, SPK_DEVICE = 0, 1
-KERNEL_CLASSES = ["assemble", "getrf", "panel", "trail", "schur", "fwd", "bwd", "permute", "residual", "blockinv"]
+KERNEL_CLASSES = ["assemble", "getrf", "panel", "trail", "schur", "fwd", "bwd", "permute", "residual", "blockinv",
+                  "tc_trail", "tc_schur"]
 KERNEL_NAMES = {"assemble": "k_scatter_values", "getrf": "k_block_lu+k_block_lu_small+k_leaf_factor",
                 "panel": "k_block_panel",
-                "trail": "k_tc_update<TC_TRAIL>+k_block_trail", "schur": "k_tc_update<TC_SCHUR>+k_schur",
+                "trail": "k_block_trail", "schur": "k_schur",
                 "fwd": "k_fwd+k_front_solve<fwd>+k_fwd_l21+k_solve_leaf<fwd>",
                 "bwd": "k_bwd_u12+k_bwd+k_front_solve<bwd>+k_solve_leaf<bwd>", "permute": "k_permute+k_unpermute",
-                "residual": "k_residual", "blockinv": "k_block_inv"}
+                "residual": "k_residual", "blockinv": "k_block_inv",
+                "tc_trail": "k_tc_update<TC_TRAIL>", "tc_schur": "k_tc_update<TC_SCHUR>"}
 # How each class's FP32 form computes: tensor cores (tcgen05, 3xTF32) or CUDA cores.
-KERNEL_UNITS = {"trail": "tcgen05 3xTF32 (fronts with a pack) + FP32 FMA", "schur": "tcgen05 3xTF32 (fronts with a pack) + FP32 FMA",
+KERNEL_UNITS = {"tc_trail": "tcgen05 kind::tf32, 3xTF32 per term", "tc_schur": "tcgen05 kind::tf32, 3xTF32 per term",
+                "trail": "FP32/FP64 FMA (fronts without a pack)", "schur": "FP32/FP64 FMA (fronts without a pack)",
                 "getrf": "FP32 FMA, latency-bound (one CTA per front, sequential pivot columns; small fronts a warp each)",
                 "panel": "FP32 FMA (register-line triangular sweeps)"}
 SPK_FP64, SPK_FP32 = 0, 1

@@ -2,8 +2,9 @@
 
 Reads the reference package's test files *as text* (Julia cannot run here)
 and pulls out the literal arrays the tests assert against.  Run from the
-repository root with the reference checked out at REFERENCE (default
-/root/reference):  python tests/golden/extract_golden.py
+repository root with the path of a checkout of the reference as the
+argument (or in the REFERENCE environment variable):
+    python tests/golden/extract_golden.py <path-to-Sparspak.jl>
 The JSON it writes is committed; the tests never read the reference.
 """
 import json
@@ -11,7 +12,9 @@ import os
 import re
 import sys
 
-REF = os.environ.get("REFERENCE", "/root/reference")
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REFERENCE")
+if not REF:
+    sys.exit("usage: extract_golden.py <path-to-Sparspak.jl>  (or set REFERENCE)")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_vectors.json")
 
 

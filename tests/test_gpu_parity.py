@@ -237,7 +237,13 @@ def test_fp32_tensor_core_updates(kind):
     o.inmatrix_csc(*S.sparse_solver._matrix_arrays(A))
     o.factor()
     S.inmatrix_(s)
+    eng = s.slvr.engine
+    eng.profile_reset()
     S.factor_(s)
+    prof = eng.profile_read()
+    assert prof["tc_schur"]["launches"] > 0, "the tensor-core Schur kernel did not run"
+    if kind == "laplace":
+        assert prof["tc_trail"]["launches"] > 0, "the tensor-core trailing kernel did not run"
     assert np.array_equal(s.slvr.ipiv, o.ipiv)
     assert rel(s.slvr.lnz, o.lnz) < 1e-4
     assert rel(s.slvr.unz, o.unz[: s.slvr.unz.size]) < 1e-4

@@ -140,3 +140,108 @@ def test_singular_block_reported():
     o = oracle.OracleLU(s.slvr)
     o.inmatrix_csc(*csc_arrays(p))
     assert o.factor() == -1 and o.first_singular == 1
+
+
+# ---------------------------------------------------------------------------
+# The oracle's own structure phase (spk_oracle_struct.c), independent of the
+# product's host library: pinned by the reference's golden vectors, then
+# compared with the product's permutation, supernodes and subscripts.
+# ---------------------------------------------------------------------------
+
+def _tridiag_csc(n):
+    m = sp.diags([-np.ones(n - 1), 4 * np.ones(n), -np.ones(n - 1)], [-1, 0, 1], format="csc")
+    return m.indptr.astype(np.int64) + 1, m.indices.astype(np.int64) + 1
+
+
+def test_oracle_structure_golden_tridiag11(golden):
+    # msprs003 (MMD perm, test/test_sparse_method.jl:87-90) and msprs004
+    # (symbolic arrays, :127-131)
+    cp, rv = _tridiag_csc(11)
+    xadj, adj = oracle.graph_of(cp, rv, 11)
+    perm, invp = oracle.mmd(xadj, adj, 11)
+    assert perm.tolist() == golden["tridiag11_rperm"]
+    assert invp.tolist() == golden["tridiag11_rinvp"]
+    o = oracle.symbolic(xadj, adj, perm, invp)
+    assert o.xlnz.tolist() == golden["tridiag11_xlnz"]
+    assert o.xunz.tolist() == golden["tridiag11_xunz"]
+    assert o.xlindx.tolist() == golden["tridiag11_xlindx"]
+    assert o.lindx.tolist() == golden["tridiag11_lindx"]
+
+
+def test_oracle_graph_fig313(golden):
+    # test/test_graph.jl:10-23 (symmetric) and :84-99 (symmetrised)
+    for key in ("fig313", "fig313_unsym"):
+        I, J = np.array(golden[key + "_I"]), np.array(golden[key + "_J"])
+        m = sp.csc_matrix((np.ones(I.size), (I - 1, J - 1)), shape=(6, 6))
+        xadj, adj = oracle.graph_of(m.indptr.astype(np.int64) + 1, m.indices.astype(np.int64) + 1, 6)
+        assert xadj.tolist() == golden["fig313_xadj"]
+        assert adj.tolist() == golden["fig313_adj"]
+
+
+def _structure_cases():
+    rng_cases = [("sprand_spd", 301), ("sprand_spd", 1357), ("sprand_unsym", 400)]
+    grid_cases = [((20, 20, 1), "mmd"), ((100, 100, 1), "mmd"), ((100, 100, 1), "nd"), ((9, 10, 11), "mmd"),
+                  ((24, 24, 24), "nd"), ((17, 13, 9), "nd")]
+    return rng_cases + grid_cases
+
+
+@pytest.mark.parametrize("case", _structure_cases(), ids=lambda c: str(c))
+def test_oracle_structure_equals_product(case):
+    if case[0] == "sprand_spd":
+        A = sprand_spd_like(case[1], case[1])
+        ordering, grid, orderfunction = "mmd", None, None
+    elif case[0] == "sprand_unsym":
+        A = sprand_unsym(case[1], 0.01, 7)
+        ordering, grid, orderfunction = "mmd", None, None
+    else:
+        grid, ordering = case
+        A = S.gallery.laplacian(grid if grid[2] > 1 else grid[:2])
+        orderfunction = S.nd_grid(*grid) if ordering == "nd" else None
+    A = sp.csc_matrix(A)
+    n = A.shape[0]
+    cp, rv = A.indptr.astype(np.int64) + 1, A.indices.astype(np.int64) + 1
+    o = oracle.structure_csc(cp, rv, n, ordering, grid)
+    s = S.SparseSolver(A)
+    S.findorder_(s, orderfunction)
+    S.symbolicfactor_(s)
+    b = s.slvr
+    assert o.order.rperm.tolist() == b.order.rperm.tolist()
+    assert o.order.rinvp.tolist() == b.order.rinvp.tolist()
+    assert o.nsuper == b.nsuper
+    for k in ("xsuper", "snode", "xlindx", "lindx", "xlnz", "xunz"):
+        assert np.array_equal(getattr(o, k), np.asarray(getattr(b, k))), k
+
+
+def test_oracle_blas_mode_matches_generic():
+    # the BLAS/LAPACK path (the reference's Float64 dispatch) against the
+    # generic loops on a 3-D grid with 30-column pieces: same pivots, factors
+    # to rounding, and the sliced factorisation equals the one-call form
+    A = S.gallery.laplacian((14, 14, 14), shift=1e-3)
+    n = A.shape[0]
+    cp, rv, nz = A.indptr.astype(np.int64) + 1, A.indices.astype(np.int64) + 1, A.data
+    st = oracle.structure_csc(cp, rv, n, "nd", (14, 14, 14))
+    oracle.use_blas(False)
+    g = oracle.OracleLU(st)
+    g.inmatrix_csc(cp, rv, nz)
+    assert g.factor() == 0
+    try:
+        info = oracle.use_blas(True)
+        assert info["threads"] >= 1
+        bl = oracle.OracleLU(st)
+        bl.inmatrix_csc(cp, rv, nz)
+        assert bl.factor() == 0
+        sl = oracle.OracleLU(st)
+        sl.inmatrix_csc(cp, rv, nz)
+        bounds = np.linspace(0, st.nsuper, 6).astype(int)[1:]
+        assert list(sl.factor_slices(bounds)) == bounds.tolist()
+        assert sl.iflag == 0
+        assert np.array_equal(sl.lnz, bl.lnz) and np.array_equal(sl.ipiv, bl.ipiv)
+        b = np.random.default_rng(0).uniform(-1, 1, n)
+        xb = bl.solve(b)
+    finally:
+        oracle.use_blas(False)
+    assert np.array_equal(g.ipiv, bl.ipiv)
+    scale = np.max(np.abs(g.lnz))
+    assert np.max(np.abs(g.lnz - bl.lnz)) / scale < 1e-13
+    xg = g.solve(b)
+    assert np.max(np.abs(xg - xb)) / np.max(np.abs(xg)) < 1e-12

@@ -1,8 +1,9 @@
 """The allocation-free residual entry point (spk_residual_noalloc).
 
 It exists for callers that cannot allocate device memory when they call
-the library (inside a CUDA stream capture, under a fixed memory budget, or
-from a host callback): its work space is a file-scope device array instead
+the library (an application that gives all device memory to its own pool,
+a fixed memory budget, a loop that cannot afford the device synchronisation
+of cudaMalloc/cudaFree): its work space is a file-scope device array instead
 of a cudaMalloc.  Checked through the C ABI against spk_residual, on two
 calls in a row (the shared array keeps the previous call's contents, so the
 second call also checks that it is cleared).  This file is collected last.
