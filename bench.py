@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--sample-grid", type=int, default=48, help="grid of the CPU baseline's bounded sample")
     ap.add_argument("--one-step", action="store_true",
                     help="profiling aid: one warm-up step, then exactly one mixed step, no other work")
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"], help="precision of --one-step")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "bf16s"], help="precision of --one-step")
     ap.add_argument("--config", default="laplace3d", choices=["laplace3d", "batched"],
                     help="laplace3d: the headline 64^3 workload; batched: 512 independent SPD systems (solves/s)")
     return ap.parse_args()
@@ -209,13 +209,16 @@ def cpu_baseline(args, F_full):
 
 
 def cpu_model():
+    parts = {"0xd4f": "Arm Neoverse-V2", "0xd40": "Arm Neoverse-V1", "0xd0c": "Arm Neoverse-N1",
+             "0xd8e": "Arm Neoverse-N3", "0xd84": "Arm Neoverse-V3"}
     try:
         with open("/proc/cpuinfo") as f:
             txt = f.read()
         for key in ("model name", "CPU part"):
             for line in txt.splitlines():
                 if line.lower().startswith(key.lower()):
-                    return line.split(":", 1)[1].strip() + f" x{os.cpu_count()}"
+                    v = line.split(":", 1)[1].strip()
+                    return f"{parts.get(v, v)} x{os.cpu_count()}"
     except OSError:
         pass
     import platform
@@ -309,6 +312,9 @@ def run_ours(args):
     def step(prec):
         eng.load_values(nz_d, prec)
         eng.factor(prec)
+        if prec == "bf16s":   # plain refinement, then GMRES-IR once it stagnates
+            it, rr, used = eng.refine(b_d, x_d, prec, TOL, 200, solver="auto")
+            return it, rr, used
         return eng.refine(b_d, x_d, prec, TOL, 30)
 
     def barrier():
@@ -331,7 +337,7 @@ def run_ours(args):
         step(args.precision)
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        it, rr = step(args.precision)
+        it, rr = step(args.precision)[:2]
         torch.cuda.synchronize(dev)
         print(json.dumps({"one_step_ms": (time.perf_counter() - t0) * 1e3, "precision": args.precision,
                           "corrections": it, "relres": rr, "grid": k}))
@@ -353,6 +359,7 @@ def run_ours(args):
         ms_mixed, (it_mixed, rr_mixed) = timed(lambda: step("fp32"), args.steps)
     clocks = clk.summary()
     launches = sum(v["launches"] for v in eng.profile_read().values())
+    x_mixed = x_d.cpu().numpy().T.copy()
     # live roofline: the same steps with CUDA events around every launch of the dominant class
     # (and of the Schur-complement kernel, the factor's main product)
     eng.profile(sorted({dom, "tc_schur"}))
@@ -364,9 +371,21 @@ def run_ours(args):
     # factor-only timings for GFLOP/s
     eng.load_values(nz_d, "fp32")
     ms_f32, _ = timed(lambda: (eng.load_values(nz_d, "fp32"), eng.factor("fp32")), args.steps)
+    # the BF16 form: BF16 tensor-core rank updates, FP64 refinement / GMRES-IR
+    for _ in range(args.warmup):
+        step("bf16s")
+    ms_bf16, (it_bf16, rr_bf16, used_bf16) = timed(lambda: step("bf16s"), args.steps)
+    x_bf16 = x_d.cpu().numpy().T.copy()
+    ms_fb16, _ = timed(lambda: (eng.load_values(nz_d, "bf16s"), eng.factor("bf16s")), args.steps)
+    eng.profile(["tc_schur", "tc_trail"])
+    eng.profile_reset()
+    timed(lambda: (eng.load_values(nz_d, "bf16s"), eng.factor("bf16s")), 1)
+    live_bf16 = eng.profile_read()
+    eng.profile([])
     for _ in range(args.warmup):
         step("fp64")
     ms_fp64, (it_fp64, rr_fp64) = timed(lambda: step("fp64"), args.steps)
+    x_fp64 = x_d.cpu().numpy().T.copy()
     ms_f64, _ = timed(lambda: (eng.load_values(nz_d, "fp64"), eng.factor("fp64")), max(1, args.steps // 2))
     ms_asm32, _ = timed(lambda: eng.load_values(nz_d, "fp32"), args.steps)
     ms_asm64, _ = timed(lambda: eng.load_values(nz_d, "fp64"), args.steps)
@@ -396,6 +415,15 @@ def run_ours(args):
         return
 
     pk, pk_kind = peaks()
+    import ctypes
+
+    p32, p64, pdm = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    S._native.gpu().spk_measure_peaks(ctypes.byref(p32), ctypes.byref(p64), ctypes.byref(pdm))
+    simt = {"fp32_fma_tflops": p32.value, "fp64_fma_tflops": p64.value, "fp64_dmma_tflops": pdm.value,
+            "how": "spk_measure_peaks: one timed launch of 8 CTAs per SM x 256 threads, 8 independent chains each"}
+
+    def fwd_err(x):
+        return float(np.max(np.abs(x - x_fp64)) / np.max(np.abs(x_fp64)))
 
     def traffic_of(cls):
         """DRAM bytes per launch of the class's FP32 kernels from the committed ncu summary (40^3 capture)."""
@@ -423,14 +451,20 @@ def run_ours(args):
                                    "mixed step of the 40^3 case (profiles/dram_traffic_laplace3d40_mixed_step.md); "
                                    "not captured at 64^3")
 
-    def roofline_of(cls):
-        d = live[cls]
-        if cls in ("schur", "trail", "tc_schur", "tc_trail", "panel", "getrf"):
+    def roofline_of(cls, prof_live, kind="float"):
+        d = prof_live[cls]
+        if cls in ("tc_schur", "tc_trail"):
             achieved = d["flops"] / (d["ms"] * 1e-3) / 1e12
             roof = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops_sustained"], "unit": "TFLOP/s",
                     "peak_kind": f"{pk_kind} bf16 dense sustained (kernel timed inside a long step); achieved counts "
-                                 f"the algorithmic FP32 flops (a 3xTF32 product issues three TF32 MMAs per term, and "
-                                 f"the TF32 dense rate is half the bf16 one)",
+                                 f"the algorithmic flops of the rank updates (the FP32 form issues three TF32 MMAs "
+                                 f"per term, at half the bf16 rate; the BF16 form one bf16 MMA)",
+                    "compute": S._native.KERNEL_UNITS.get(cls, "")}
+        elif cls in ("schur", "trail", "panel", "getrf"):
+            achieved = d["flops"] / (d["ms"] * 1e-3) / 1e12
+            roof = {"bound": "fp32_simt", "achieved": achieved, "peak": simt["fp32_fma_tflops"], "unit": "TFLOP/s",
+                    "peak_kind": "FP32 FMA rate of the CUDA cores, measured live (spk_measure_peaks); the kernel "
+                                 "computes on CUDA cores, not the tensor pipe",
                     "compute": S._native.KERNEL_UNITS.get(cls, "")}
         else:
             achieved = d["bytes"] / (d["ms"] * 1e-3) / 1e9
@@ -439,14 +473,15 @@ def run_ours(args):
         traffic, tnote = traffic_of(cls)
         roof.update({"frac": roof["achieved"] / roof["peak"], "traffic": traffic, "traffic_unit": "bytes/launch",
                      "traffic_note": tnote,
-                     "kernel": S._native.KERNEL_NAMES[cls] + " (float)", "launches": d["launches"],
+                     "kernel": S._native.KERNEL_NAMES[cls] + f" ({kind})", "launches": d["launches"],
                      "ms_per_launch": d["ms"] / max(d["launches"], 1),
                      "algorithmic_per_launch": (d["flops"] if roof["bound"] == "tensor" else d["bytes"])
                      / max(d["launches"], 1)})
         return roof
 
-    roof = roofline_of(dom)
-    roof_schur = roofline_of("tc_schur")
+    roof = roofline_of(dom, live)
+    roof_schur = roofline_of("tc_schur", live)
+    roof_schur_bf16 = roofline_of("tc_schur", live_bf16, "bf16 operands")
     nnz_full = float(s.slvr.xlnz[-1] - 1 + s.slvr.xunz[-1] - 1)
     cpu = cpu_baseline(args, F) if ws == 1 else None
     h2d = nzval.nbytes + b.nbytes
@@ -463,14 +498,24 @@ def run_ours(args):
                   "relres_host_check": rr_check,
                   "factor_ms": ms_f32, "factor_gflops": F / (ms_f32 * 1e-3) / 1e9, "assembly_ms": ms_asm32},
         "fp64": {"ms": ms_fp64, "corrections": it_fp64, "relres": rr_fp64, "factor_ms": ms_f64,
-                 "factor_gflops": F / (ms_f64 * 1e-3) / 1e9, "assembly_ms": ms_asm64},
+                 "factor_gflops": F / (ms_f64 * 1e-3) / 1e9, "assembly_ms": ms_asm64,
+                 "factor_frac_of_fp64_fma": F / (ms_f64 * 1e-3) / 1e12 / simt["fp64_fma_tflops"],
+                 "factor_frac_of_fp64_dmma": F / (ms_f64 * 1e-3) / 1e12 / simt["fp64_dmma_tflops"]},
+        "bf16s": {"ms": ms_bf16, "preconditioned_solves": it_bf16, "solver": used_bf16, "relres": rr_bf16,
+                  "factor_ms": ms_fb16, "factor_gflops": F / (ms_fb16 * 1e-3) / 1e9},
+        "forward_error_vs_fp64": {"mixed": fwd_err(x_mixed), "bf16s": fwd_err(x_bf16),
+                                  "note": "max-norm, against the FP64 GPU solution of the same step (which the "
+                                          "parity tests hold within 1e-10 of the oracle's)"},
         "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
+        "speedup_bf16s_vs_fp64": ms_fp64 / ms_bf16,
+        "measured_peaks": simt,
         "host_once_per_pattern": host_t,
         "profile_mixed_step": {c: {"ms": round(v["ms"], 4), "launches": v["launches"],
                                    "gflops": round(v["flops"] / max(v["ms"], 1e-9) / 1e6, 1),
                                    "gbs": round(v["bytes"] / max(v["ms"], 1e-9) / 1e6, 1)} for c, v in prof.items()},
         "roofline": roof,
         "roofline_schur": roof_schur,
+        "roofline_schur_bf16": roof_schur_bf16,
         "cpu_baseline": cpu,
         "e2e": {"value": ms_e2e, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "corrections": it_e2e, "relres": rr_e2e},

@@ -44,7 +44,14 @@ extern "C" {
 
 #define SPK_FP64 0         /* factor, solve and residual in double                */
 #define SPK_FP32 1         /* factor and solve in float; residual and correction
-                              in double (mixed form for spk_refine)               */
+                              in double (mixed form for spk_refine); the large
+                              rank updates as 3xTF32 tensor-core products        */
+#define SPK_BF16S 2        /* as SPK_FP32, but the large rank updates (Schur
+                              complements and trailing updates) take BF16
+                              operands with a power-of-two scale per block panel
+                              and FP32 accumulation on the tensor cores; for
+                              spk_refine, GMRES-IR when plain refinement
+                              stagnates                                          */
 
 typedef struct spk_handle spk_handle;
 
@@ -129,10 +136,34 @@ int spk_solve_transpose(spk_handle* h, double* b, int64_t nrhs, int64_t ldb, int
  * column-major, leading dimension ld, original order.  Reports the number
  * of corrections and the final relative residual.  Returns SPK_ENOCONV if
  * tol was not reached.  Modelled on the reference's commented-out
- * refinement (src/SparseSpdMethod/SpkSparseSpdSolver.jl:267-343).
+ * refinement (src/SparseSpdMethod/SpkSparseSpdSolver.jl:267-343).  When a
+ * correction fails to halve the residual (as with SPK_BF16S factors of
+ * ill-conditioned systems) it continues with GMRES-IR (spk_refine_ex,
+ * SPK_SOLVER_AUTO).
  */
 int spk_refine(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where,
                int precision, double tol, int max_iter, int* iters, double* relres);
+
+/*
+ * Iterative refinement with a choice of solver for the correction equation
+ * A d = r (no counterpart in the reference):
+ *   SPK_SOLVER_IR     plain refinement, d = solve(r), as spk_refine;
+ *   SPK_SOLVER_GMRES  GMRES-IR: restarted GMRES in FP64 on A d = r,
+ *                     preconditioned on the right by the factor of
+ *                     `precision` (one triangular solve per iteration);
+ *   SPK_SOLVER_AUTO   plain refinement while each correction at least halves
+ *                     the residual, then (a correction that made it worse is
+ *                     taken back) GMRES-IR; spk_refine behaves like this.
+ * max_iter bounds the preconditioned solves after the first (corrections
+ * plus GMRES iterations), reported in *iters; *solver_used (may be NULL)
+ * receives SPK_SOLVER_IR or SPK_SOLVER_GMRES.  Other arguments and results
+ * as spk_refine.
+ */
+#define SPK_SOLVER_AUTO 0
+#define SPK_SOLVER_IR 1
+#define SPK_SOLVER_GMRES 2
+int spk_refine_ex(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where, int precision,
+                  double tol, int max_iter, int solver, int* iters, double* relres, int* solver_used);
 
 /* Iterative refinement of A^T x = b (spk_solve_transpose and the FP64
  * residual b - A^T x), arguments and results as spk_refine. */
@@ -225,6 +256,15 @@ int spk_stats(spk_handle* h, int64_t* nfronts, int64_t* nlevels, int64_t* factor
 int spk_profile(spk_handle* h, unsigned mask);
 int spk_profile_reset(spk_handle* h);
 int spk_profile_read(spk_handle* h, int kind, double* ms, int64_t* launches, double* flops, double* bytes);
+
+/*
+ * Measured throughput of the current device (no counterpart in the
+ * reference; the denominators of the CUDA-core kernels' roofline figures):
+ * FP32 FMA, FP64 FMA and FP64 tensor-core (mma.sync m8n8k4 f64) rates in
+ * TFLOP/s, each from one timed launch of several CTAs per SM running
+ * independent chains.  Any pointer may be NULL.
+ */
+int spk_measure_peaks(double* fp32_tflops, double* fp64_tflops, double* dmma_tflops);
 
 /* Text of the last error on this handle (never NULL); with h == NULL, the
  * reason the last spk_create on this thread failed. */

@@ -159,12 +159,17 @@ struct spk_handle {
 
     Storage<double> s64;
     Storage<float> s32;
+    Storage<float> s16;   // SPK_BF16S: float factor, BF16 packed panels
+    int fmode = 0;        // which float form the float paths use: 0 SPK_FP32, 1 SPK_BF16S
 
     // solve work space (sized for MAXRHS right-hand sides)
     void *d_wb = nullptr, *d_wy = nullptr, *d_wx = nullptr;   // factor precision
     double *d_rhs = nullptr, *d_x = nullptr, *d_r = nullptr;  // FP64, n*cap
     double* d_sums = nullptr;
     i64 rhs_cap = 0;
+    // GMRES-IR work space (spk_refine_ex): bases V (GM_M + 1 blocks) and
+    // Z = M^-1 V (GM_M blocks) of n x GM_MAXRHS, w, and the small coefficients
+    double *gm_V = nullptr, *gm_Z = nullptr, *gm_w = nullptr, *gm_c = nullptr;
 
     cudaStream_t own = nullptr, stream = nullptr;
     // Look-ahead of the factorisation: the bulk of a block step's tensor-core
@@ -193,9 +198,10 @@ struct spk_handle {
 
     // captured sequences: factor per precision, solve per precision x right-hand sides
     bool use_graphs = true;
-    GraphRec g_factor[2];
-    GraphRec g_solve[2][spk::MAXRHS + 1];
-    GraphRec g_tsolve[2][spk::MAXRHS + 1];   // transposed solves
+    // [0] FP64, [1] FP32, [2] BF16S
+    GraphRec g_factor[3];
+    GraphRec g_solve[3][spk::MAXRHS + 1];
+    GraphRec g_tsolve[3][spk::MAXRHS + 1];   // transposed solves
 };
 
 // ---------------------------------------------------------------------------
@@ -234,6 +240,10 @@ static spk::Launch launch_of(const Plan& P, const LaunchRec& r) {
 
 template <typename T>
 static constexpr int prec_index() { return std::is_same<T, float>::value ? 1 : 0; }
+
+// Slot of the captured graphs: FP64, FP32 or BF16S (the float form selected).
+template <typename T>
+static int graph_index(const spk_handle* h) { return std::is_same<T, float>::value ? 1 + h->fmode : 0; }
 
 static cudaEvent_t take_event(spk_handle* h) {
     if (!h->event_pool.empty()) {
@@ -290,7 +300,7 @@ static void drop_graph(GraphRec& g) {
 }
 
 static void drop_solve_graphs(spk_handle* h) {
-    for (int p = 0; p < 2; ++p)
+    for (int p = 0; p < 3; ++p)
         for (int r = 0; r <= spk::MAXRHS; ++r) {
             drop_graph(h->g_solve[p][r]);
             drop_graph(h->g_tsolve[p][r]);
@@ -905,9 +915,13 @@ static int ensure_plan(spk_handle* h) {
         cudaGetLastError();   // a refused query leaves clusters of 8
     }
     if (std::is_same<T, float>::value) {
-        CU(h, cudaFuncSetAttribute(spk::k_tc_update<spk::TC_TRAIL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        CU(h, cudaFuncSetAttribute(spk::k_tc_update<spk::TC_TRAIL, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    spk::umma::PSMEM));
-        CU(h, cudaFuncSetAttribute(spk::k_tc_update<spk::TC_SCHUR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        CU(h, cudaFuncSetAttribute(spk::k_tc_update<spk::TC_SCHUR, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   spk::umma::PSMEM));
+        CU(h, cudaFuncSetAttribute(spk::k_tc_update<spk::TC_TRAIL, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   spk::umma::PSMEM));
+        CU(h, cudaFuncSetAttribute(spk::k_tc_update<spk::TC_SCHUR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    spk::umma::PSMEM));
     }
     P.built = true;
@@ -927,7 +941,7 @@ static Storage<T>& storage(spk_handle* h);
 template <>
 Storage<double>& storage<double>(spk_handle* h) { return h->s64; }
 template <>
-Storage<float>& storage<float>(spk_handle* h) { return h->s32; }
+Storage<float>& storage<float>(spk_handle* h) { return h->fmode ? h->s16 : h->s32; }
 
 template <typename T>
 static int ensure_storage(spk_handle* h) {
@@ -936,8 +950,9 @@ static int ensure_storage(spk_handle* h) {
     Storage<T>& S = storage<T>(h);
     if (!S.d) CU(h, cudaMalloc((void**)&S.d, sizeof(T) * std::max<i64>(h->fsize, 1)));
     if (!S.inv2) CU(h, cudaMalloc((void**)&S.inv2, sizeof(T) * std::max<ll>(h->plan[prec_index<T>()].inv2_size, 1)));
-    if (!S.pack && h->plan[prec_index<T>()].pack_size > 0)
-        CU(h, cudaMalloc((void**)&S.pack, (size_t)h->plan[prec_index<T>()].pack_size));
+    // BF16 packs take a quarter of the TF32 hi + lo bytes (same tiles and chunks)
+    const ll pack_bytes = h->plan[prec_index<T>()].pack_size / (std::is_same<T, float>::value && h->fmode ? 4 : 1);
+    if (!S.pack && pack_bytes > 0) CU(h, cudaMalloc((void**)&S.pack, (size_t)pack_bytes));
     return SPK_OK;
 }
 
@@ -996,6 +1011,7 @@ static int factor_launches(spk_handle* h) {
     const spk::Sched& S = PL.sched;
     // Look ahead (not while timing kernels one by one): see spk_handle::side.
     const bool ahead = h->prof_mask == 0;
+    const int bf16 = std::is_same<T, float>::value ? h->fmode : 0;
     bool pending = false, pending_inv = false;
     // The whole-block solve operators of level group g (k_block_inv).
     auto launch_inv = [&](int g, cudaStream_t st) {
@@ -1052,13 +1068,13 @@ static int factor_launches(spk_handle* h) {
                 const spk::Launch la = launch_of(PL, P.bpanel[t]);
                 if (bw <= 32)
                     spk::k_block_panel<T, 32><<<P.bpanel[t].tiles, 256, sweep_smem<T, 32>(1), h->stream>>>(
-                        fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack);
+                        fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack, bf16);
                 else if (bw <= 64)
                     spk::k_block_panel<T, 64><<<P.bpanel[t].tiles, 256, sweep_smem<T, 64>(1), h->stream>>>(
-                        fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack);
+                        fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack, bf16);
                 else
                     spk::k_block_panel<T, BM><<<P.bpanel[t].tiles, panel_threads<T, BM>(), panel_smem<T, BM>(), h->stream>>>(
-                        fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack);
+                        fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack, bf16);
             }
             if (P.btrail[t].tiles > 0) {
                 LaunchScope ls(h, SPK_K_TRAIL, P.btrail[t].flops, P.btrail[t].words * sizeof(T));
@@ -1082,7 +1098,8 @@ static int factor_launches(spk_handle* h) {
                         st = h->side;
                     }
                     LaunchScope ls(h, SPK_K_TC_TRAIL, P.btrail_tc[t].flops, P.btrail_tc[t].words * sizeof(T));
-                    spk::k_tc_update<spk::TC_TRAIL><<<grid, spk::TC_THREADS, spk::umma::PSMEM, st>>>(
+                    auto kern = bf16 ? spk::k_tc_update<spk::TC_TRAIL, true> : spk::k_tc_update<spk::TC_TRAIL, false>;
+                    kern<<<grid, spk::TC_THREADS, spk::umma::PSMEM, st>>>(
                         fac, storage<T>(h).pack, S, launch_of(PL, P.btrail_tc[t]), (int)t, nt, 1, h->d_info + 1);
                     if (ahead) {
                         CU(h, cudaEventRecord(h->evB, h->side));
@@ -1093,7 +1110,8 @@ static int factor_launches(spk_handle* h) {
                 if (P.btrail_tc0[t].tiles > 0) {
                     LaunchScope ls(h, SPK_K_TC_TRAIL, P.btrail_tc0[t].flops, P.btrail_tc0[t].words * sizeof(T));
                     const int nt = P.btrail_tc0[t].tiles;
-                    spk::k_tc_update<spk::TC_TRAIL><<<std::min(nt, h->nsm), spk::TC_THREADS, spk::umma::PSMEM, h->stream>>>(
+                    auto kern = bf16 ? spk::k_tc_update<spk::TC_TRAIL, true> : spk::k_tc_update<spk::TC_TRAIL, false>;
+                    kern<<<std::min(nt, h->nsm), spk::TC_THREADS, spk::umma::PSMEM, h->stream>>>(
                         fac, storage<T>(h).pack, S, launch_of(PL, P.btrail_tc0[t]), (int)t, nt, 0, h->d_info + 1);
                 }
             }
@@ -1110,7 +1128,8 @@ static int factor_launches(spk_handle* h) {
             if (P.schur_tc.tiles > 0) {
                 LaunchScope ls(h, SPK_K_TC_SCHUR, P.schur_tc.flops, P.schur_tc.words * sizeof(T));
                 const int nt = P.schur_tc.tiles;
-                spk::k_tc_update<spk::TC_SCHUR><<<std::min(nt, h->nsm), spk::TC_THREADS, spk::umma::PSMEM, h->stream>>>(
+                auto kern = bf16 ? spk::k_tc_update<spk::TC_SCHUR, true> : spk::k_tc_update<spk::TC_SCHUR, false>;
+                kern<<<std::min(nt, h->nsm), spk::TC_THREADS, spk::umma::PSMEM, h->stream>>>(
                     fac, storage<T>(h).pack, S, launch_of(PL, P.schur_tc), 0, nt, 0, h->d_info + 1);
             }
         }
@@ -1127,7 +1146,7 @@ template <typename T>
 static int run_factor(spk_handle* h) {
     static const int init[2] = {INT_MAX, 0};
     CU(h, cudaMemcpyAsync(h->d_info, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
-    return via_graph(h, h->g_factor[prec_index<T>()], [&] { return factor_launches<T>(h); });
+    return via_graph(h, h->g_factor[graph_index<T>(h)], [&] { return factor_launches<T>(h); });
 }
 
 // Solve in place on the permuted work vectors: wb (rhs, consumed) -> wx.
@@ -1241,7 +1260,7 @@ static int solve_device(spk_handle* h, const double* rhs, i64 ldr, double* x, i6
             spk::k_permute<double, T><<<blocks, 256, 0, h->stream>>>(rhs + c0 * ldr, ldr, (T*)h->d_wb, n, h->d_rperm,
                                                                      n, nc);
         }
-        GraphRec& g = transpose ? h->g_tsolve[prec_index<T>()][nc] : h->g_solve[prec_index<T>()][nc];
+        GraphRec& g = transpose ? h->g_tsolve[graph_index<T>(h)][nc] : h->g_solve[graph_index<T>(h)][nc];
         int rc = via_graph(h, g, [&] { return run_solve_permuted<T>(h, nc, transpose); });
         if (rc) return rc;
         {
@@ -1255,7 +1274,7 @@ static int solve_device(spk_handle* h, const double* rhs, i64 ldr, double* x, i6
 }
 
 static int residual_device(spk_handle* h, const double* b, i64 ldb, const double* x, i64 ldx, i64 nrhs,
-                           double* relres, bool transpose = false) {
+                           double* relres, bool transpose = false, std::vector<double>* sq = nullptr) {
     const int n = (int)h->n;
     CU(h, cudaMemsetAsync(h->d_sums, 0, sizeof(double) * 2 * (size_t)nrhs, h->stream));
     dim3 grid((n + 255) / 256);
@@ -1280,6 +1299,137 @@ static int residual_device(spk_handle* h, const double* b, i64 ldb, const double
         if (!(rel <= worst)) worst = rel;   // NaN propagates
     }
     *relres = worst;
+    if (sq) *sq = sums;   // ||r_j||^2, ||b_j||^2 interleaved
+    return SPK_OK;
+}
+
+// ---------------------------------------------------------------------------
+// GMRES-IR: restarted GMRES (cycles of at most GM_M iterations) on A d = r
+// in FP64, preconditioned on the right by the factor of the selected float
+// form (z = M^-1 v is one triangular solve), classical Gram-Schmidt with
+// reorthogonalisation, Givens rotations on the host.  Every cycle starts
+// from the true FP64 residual of x and ends with x += Z y.  Right-hand sides
+// in groups of spk::GM_MAXRHS, each with its own Krylov space.
+// ---------------------------------------------------------------------------
+constexpr int GM_M = 30;
+
+static int ensure_gmres(spk_handle* h) {
+    if (h->gm_V) return SPK_OK;
+    const size_t blk = sizeof(double) * (size_t)h->n * spk::GM_MAXRHS;
+    CU(h, cudaMalloc((void**)&h->gm_V, blk * (GM_M + 1)));
+    CU(h, cudaMalloc((void**)&h->gm_Z, blk * GM_M));
+    CU(h, cudaMalloc((void**)&h->gm_w, blk));
+    CU(h, cudaMalloc((void**)&h->gm_c, sizeof(double) * (2 * (GM_M + 1) + 1) * spk::GM_MAXRHS));
+    return SPK_OK;
+}
+
+// Columns [0, nrhs) of b / x (nrhs <= GM_MAXRHS).  `budget` preconditioned
+// solves at most; *used receives the number made, *cycles the restarts.
+template <typename T>
+static int gmres_ir(spk_handle* h, const double* b, i64 ldb, double* x, i64 ldx, int nrhs, double tol, int budget,
+                    double* relres, int* used, int* cycles) {
+    int rc = ensure_gmres(h);
+    if (rc) return rc;
+    const int n = (int)h->n;
+    const ll tot = (ll)n * nrhs;
+    const int vgrid = (int)std::min<ll>((tot + 255) / 256, 8LL * h->nsm);
+    const int dgrid = std::max(1, std::min((n + 255) / 256, 2 * h->nsm));
+    double* c = h->gm_c;                       // [h1 (GM_M+1) x nrhs | h2 (GM_M+1) x nrhs | norm^2 nrhs]
+    double* h1 = c;
+    double* h2 = c + (GM_M + 1) * nrhs;
+    double* nrm = c + 2 * (GM_M + 1) * nrhs;
+    std::vector<double> H((size_t)nrhs * (GM_M + 1) * GM_M), cs((size_t)nrhs * GM_M), sn((size_t)nrhs * GM_M),
+        g((size_t)nrhs * (GM_M + 1)), hc(2 * (GM_M + 1) * nrhs + nrhs), y((size_t)GM_M * nrhs);
+    std::vector<int> k(nrhs);
+    std::vector<double> sq;
+    *used = 0;
+    *cycles = 0;
+    double rel = 0.0;
+    for (;;) {
+        if ((rc = residual_device(h, b, ldb, x, ldx, nrhs, &rel, false, &sq))) return rc;
+        if (rel <= tol || *used >= budget || rel != rel) break;
+        ++*cycles;
+        std::vector<double> beta2(nrhs), target(nrhs);
+        std::vector<char> active(nrhs);
+        for (int r = 0; r < nrhs; ++r) {
+            beta2[r] = sq[2 * r];
+            const double nb = std::sqrt(sq[2 * r + 1]);
+            target[r] = 0.5 * tol * (nb > 0.0 ? nb : 1.0);
+            active[r] = std::sqrt(beta2[r]) > target[r];
+            g[(size_t)r * (GM_M + 1)] = std::sqrt(beta2[r]);
+            k[r] = 0;
+        }
+        // V_0 = r / ||r|| (the residual kernel left r in d_r, leading dimension n)
+        CU(h, cudaMemcpyAsync(nrm, beta2.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, h->stream));
+        spk::k_gm_scale<<<vgrid, 256, 0, h->stream>>>(h->d_r, nrm, h->gm_V, n, nrhs);
+        for (int j = 0; j < GM_M && *used < budget; ++j) {
+            double* Vj = h->gm_V + (ll)j * tot;
+            double* Zj = h->gm_Z + (ll)j * tot;
+            if ((rc = solve_device<T>(h, Vj, n, Zj, n, nrhs, 0, false))) return rc;
+            ++*used;
+            {
+                LaunchScope ls(h, SPK_K_RESIDUAL, 2.0 * h->nnz * nrhs, (double)h->nnz * (8 + 4 + 8) + 8.0 * h->nnz * nrhs);
+                spk::k_gm_spmv<<<(n + 255) / 256, 256, 0, h->stream>>>(h->d_aval, h->d_rowptr, h->d_col, h->d_src, Zj,
+                                                                       h->gm_w, n, nrhs);
+            }
+            CU(h, cudaMemsetAsync(c, 0, sizeof(double) * (2 * (GM_M + 1) + 1) * nrhs, h->stream));
+            spk::k_gm_dots<<<dim3(dgrid, j + 1), 256, 0, h->stream>>>(h->gm_V, h->gm_w, n, nrhs, h1);
+            spk::k_gm_axpy<<<vgrid, 256, 0, h->stream>>>(h->gm_V, h1, h->gm_w, n, n, nrhs, j + 1, -1.0);
+            spk::k_gm_dots<<<dim3(dgrid, j + 1), 256, 0, h->stream>>>(h->gm_V, h->gm_w, n, nrhs, h2);
+            spk::k_gm_axpy<<<vgrid, 256, 0, h->stream>>>(h->gm_V, h2, h->gm_w, n, n, nrhs, j + 1, -1.0);
+            spk::k_gm_dots<<<dim3(dgrid, 1), 256, 0, h->stream>>>(h->gm_w, h->gm_w, n, nrhs, nrm);
+            spk::k_gm_scale<<<vgrid, 256, 0, h->stream>>>(h->gm_w, nrm, h->gm_V + (ll)(j + 1) * tot, n, nrhs);
+            CU(h, cudaGetLastError());
+            CU(h, cudaMemcpyAsync(hc.data(), c, sizeof(double) * hc.size(), cudaMemcpyDeviceToHost, h->stream));
+            CU(h, cudaStreamSynchronize(h->stream));
+            bool any = false;
+            for (int r = 0; r < nrhs; ++r) {
+                if (!active[r]) continue;
+                double* col = H.data() + ((size_t)r * GM_M + j) * (GM_M + 1);
+                for (int i = 0; i <= j; ++i) col[i] = hc[(size_t)i * nrhs + r] + hc[(size_t)(GM_M + 1 + i) * nrhs + r];
+                col[j + 1] = std::sqrt(std::max(hc[(size_t)2 * (GM_M + 1) * nrhs + r], 0.0));
+                double* csr = cs.data() + (size_t)r * GM_M;
+                double* snr = sn.data() + (size_t)r * GM_M;
+                for (int i = 0; i < j; ++i) {   // earlier rotations
+                    const double a = col[i], bb = col[i + 1];
+                    col[i] = csr[i] * a + snr[i] * bb;
+                    col[i + 1] = -snr[i] * a + csr[i] * bb;
+                }
+                const double a = col[j], bb = col[j + 1], rr = std::hypot(a, bb);
+                csr[j] = rr > 0.0 ? a / rr : 1.0;
+                snr[j] = rr > 0.0 ? bb / rr : 0.0;
+                col[j] = rr;
+                col[j + 1] = 0.0;
+                double* gr = g.data() + (size_t)r * (GM_M + 1);
+                gr[j + 1] = -snr[j] * gr[j];
+                gr[j] = csr[j] * gr[j];
+                k[r] = j + 1;
+                const double hn = std::sqrt(std::max(hc[(size_t)2 * (GM_M + 1) * nrhs + r], 0.0));
+                if (std::fabs(gr[j + 1]) <= target[r] || hn == 0.0) active[r] = 0;
+                else any = true;
+            }
+            if (!any) break;
+        }
+        // x += Z y, y from the rotated Hessenberg systems
+        int kmax = 0;
+        std::fill(y.begin(), y.end(), 0.0);
+        for (int r = 0; r < nrhs; ++r) {
+            const int kr = k[r];
+            kmax = std::max(kmax, kr);
+            const double* gr = g.data() + (size_t)r * (GM_M + 1);
+            for (int i = kr - 1; i >= 0; --i) {
+                double t = gr[i];
+                for (int l = i + 1; l < kr; ++l) t -= H[((size_t)r * GM_M + l) * (GM_M + 1) + i] * y[(size_t)l * nrhs + r];
+                const double d = H[((size_t)r * GM_M + i) * (GM_M + 1) + i];
+                y[(size_t)i * nrhs + r] = d != 0.0 ? t / d : 0.0;
+            }
+        }
+        if (kmax == 0) break;
+        CU(h, cudaMemcpyAsync(c, y.data(), sizeof(double) * (size_t)kmax * nrhs, cudaMemcpyHostToDevice, h->stream));
+        spk::k_gm_axpy<<<vgrid, 256, 0, h->stream>>>(h->gm_Z, c, x, ldx, n, nrhs, kmax, 1.0);
+        CU(h, cudaGetLastError());
+    }
+    *relres = rel;
     return SPK_OK;
 }
 
@@ -1292,7 +1442,14 @@ static int check_h(spk_handle* h) {
     return SPK_OK;
 }
 
-static bool valid_precision(int p) { return p == SPK_FP64 || p == SPK_FP32; }
+static bool valid_precision(int p) { return p == SPK_FP64 || p == SPK_FP32 || p == SPK_BF16S; }
+
+// Point the float paths at the storage of the given float form.
+static void select_form(spk_handle* h, int precision) { h->fmode = precision == SPK_BF16S ? 1 : 0; }
+
+static Storage<float>& float_storage(spk_handle* h, int precision) {
+    return precision == SPK_BF16S ? h->s16 : h->s32;
+}
 
 template <typename T>
 static int load_into(spk_handle* h) {
@@ -1321,7 +1478,7 @@ static int fetch_factor(spk_handle* h, std::vector<double>& out) {
 }
 
 static bool factored(spk_handle* h, int precision) {
-    return precision == SPK_FP64 ? h->s64.factored : h->s32.factored;
+    return precision == SPK_FP64 ? h->s64.factored : float_storage(h, precision).factored;
 }
 
 // Does (i, j) (permuted, 0-based) belong to the reference's structure?  L
@@ -1497,6 +1654,7 @@ int spk_set_pattern(spk_handle* h, int64_t ncols, const int64_t* colptr, const i
     h->have_values = false;
     h->s64.loaded = h->s64.factored = false;
     h->s32.loaded = h->s32.factored = false;
+    h->s16.loaded = h->s16.factored = false;
     return SPK_OK;
 }
 
@@ -1511,9 +1669,11 @@ int spk_load_values(spk_handle* h, const double* nzval, int where, int precision
         CU(h, cudaMemcpyAsync(h->d_aval, nzval, sizeof(double) * (size_t)h->nnz,
                               where == SPK_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, h->stream));
     h->have_values = true;
-    // a new A invalidates both factors
+    // a new A invalidates every factor
     h->s64.loaded = h->s64.factored = false;
     h->s32.loaded = h->s32.factored = false;
+    h->s16.loaded = h->s16.factored = false;
+    select_form(h, precision);
     rc = precision == SPK_FP64 ? load_into<double>(h) : load_into<float>(h);
     if (rc) return rc;
     if (where == SPK_HOST) CU(h, cudaStreamSynchronize(h->stream));
@@ -1526,11 +1686,12 @@ int spk_factor(spk_handle* h, int precision, int64_t* first_singular) {
     if (first_singular) *first_singular = 0;
     if (!valid_precision(precision)) return set_err(h, SPK_EARG, "spk_factor: bad precision");
     if (!h->have_values) return set_err(h, SPK_ESEQ, "Sequence error. Matrix input not done yet.");
+    select_form(h, precision);
     if (precision == SPK_FP64) {
         if (!h->s64.loaded && (rc = load_into<double>(h))) return rc;
         if ((rc = run_factor<double>(h))) return rc;
     } else {
-        if (!h->s32.loaded && (rc = load_into<float>(h))) return rc;
+        if (!float_storage(h, precision).loaded && (rc = load_into<float>(h))) return rc;
         if ((rc = run_factor<float>(h))) return rc;
     }
     int info2[2] = {INT_MAX, 0};
@@ -1539,7 +1700,7 @@ int spk_factor(spk_handle* h, int precision, int64_t* first_singular) {
     const int info = info2[0];
     if (info2[1]) return set_err(h, SPK_ECUDA, "spk_factor: a tensor-core wait timed out");
     if (precision == SPK_FP64) { h->s64.loaded = false; h->s64.factored = true; }
-    else { h->s32.loaded = false; h->s32.factored = true; }
+    else { float_storage(h, precision).loaded = false; float_storage(h, precision).factored = true; }
     if (info != INT_MAX) {
         if (first_singular) *first_singular = info;
         char buf[128];
@@ -1559,6 +1720,7 @@ static int solve_impl(spk_handle* h, double* b, int64_t nrhs, int64_t ldb, int w
     if (!factored(h, precision)) return set_err(h, SPK_ESEQ, "Sequence error. Factorization not done yet.");
     if (nrhs == 0) return SPK_OK;
     if ((rc = ensure_rhs(h, nrhs))) return rc;
+    select_form(h, precision);
     const i64 n = h->n;
     double* src;
     i64 ld;
@@ -1667,15 +1829,19 @@ int spk_residual_noalloc(spk_handle* h, const double* b, const double* x, int64_
 }
 
 static int refine_impl(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where, int precision,
-                       double tol, int max_iter, int* iters, double* relres, bool transpose) {
+                       double tol, int max_iter, int solver, int* iters, double* relres, int* solver_used,
+                       bool transpose) {
     int rc = check_h(h);
     if (rc) return rc;
     if (iters) *iters = 0;
+    if (solver_used) *solver_used = SPK_SOLVER_IR;
     if (!valid_precision(precision) || nrhs <= 0 || !b || !x || ld < h->n || max_iter < 0 ||
-        (where != SPK_HOST && where != SPK_DEVICE))
+        (where != SPK_HOST && where != SPK_DEVICE) || solver < SPK_SOLVER_AUTO || solver > SPK_SOLVER_GMRES ||
+        (transpose && solver == SPK_SOLVER_GMRES))
         return set_err(h, SPK_EARG, "spk_refine: bad arguments");
     if (!factored(h, precision)) return set_err(h, SPK_ESEQ, "Sequence error. Factorization not done yet.");
     if ((rc = ensure_rhs(h, nrhs))) return rc;
+    select_form(h, precision);
     const i64 n = h->n;
     const double* db;
     double* dx;
@@ -1696,13 +1862,50 @@ static int refine_impl(spk_handle* h, const double* b, double* x, int64_t nrhs, 
                                      : solve_device<float>(h, rhs, ldr, dx, ldx, nrhs, acc, transpose);
     };
     if ((rc = solve_into(db, ldb, 0))) return rc;
-    double rel = 0.0;
+    double rel = 0.0, prev = 0.0;
     int it = 0;
+    bool gmres = solver == SPK_SOLVER_GMRES;
+    // AUTO: plain refinement while every correction at least halves the
+    // residual; on the first that does not, take back a correction that made
+    // it worse and continue with GMRES-IR from there (not for A^T).
+    const bool can_switch = solver == SPK_SOLVER_AUTO && !transpose;
+    const bool backup = can_switch && nrhs <= spk::GM_MAXRHS;   // x before each correction, in gm_w
     for (;;) {
         if ((rc = residual_device(h, db, ldb, dx, ldx, nrhs, &rel, transpose))) return rc;
         if (rel <= tol || it >= max_iter || rel != rel) break;
+        if (it > 0 && can_switch && !(rel <= 0.5 * prev)) {
+            if (backup && !(rel <= prev)) {   // take the last correction back
+                CU(h, cudaMemcpy2DAsync(dx, sizeof(double) * ldx, h->gm_w, sizeof(double) * n, sizeof(double) * n,
+                                        nrhs, cudaMemcpyDeviceToDevice, h->stream));
+                rel = prev;
+            }
+            gmres = true;
+        }
+        if (gmres) break;
+        if (backup) {
+            if ((rc = ensure_gmres(h))) return rc;
+            CU(h, cudaMemcpy2DAsync(h->gm_w, sizeof(double) * n, dx, sizeof(double) * ldx, sizeof(double) * n, nrhs,
+                                    cudaMemcpyDeviceToDevice, h->stream));
+        }
+        prev = rel;
         if ((rc = solve_into(h->d_r, n, 1))) return rc;
         ++it;
+    }
+    if (gmres && !(rel <= tol) && rel == rel) {
+        if (solver_used) *solver_used = SPK_SOLVER_GMRES;
+        double worst = 0.0;
+        for (i64 c0 = 0; c0 < nrhs; c0 += spk::GM_MAXRHS) {
+            const int nc = (int)std::min<i64>(spk::GM_MAXRHS, nrhs - c0);
+            double r = 0.0;
+            int used = 0, cycles = 0;
+            rc = precision == SPK_FP64
+                     ? gmres_ir<double>(h, db + c0 * ldb, ldb, dx + c0 * ldx, ldx, nc, tol, max_iter - it, &r, &used, &cycles)
+                     : gmres_ir<float>(h, db + c0 * ldb, ldb, dx + c0 * ldx, ldx, nc, tol, max_iter - it, &r, &used, &cycles);
+            if (rc) return rc;
+            it += used;
+            if (!(r <= worst)) worst = r;
+        }
+        rel = worst;
     }
     if (where == SPK_HOST)
         CU(h, cudaMemcpy2DAsync(x, sizeof(double) * ld, dx, sizeof(double) * n, sizeof(double) * n, nrhs,
@@ -1711,22 +1914,29 @@ static int refine_impl(spk_handle* h, const double* b, double* x, int64_t nrhs, 
     if (iters) *iters = it;
     if (relres) *relres = rel;
     if (!(rel <= tol)) {
-        char buf[128];
-        std::snprintf(buf, sizeof buf, "refinement stopped at relative residual %.3e after %d corrections", rel, it);
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "refinement stopped at relative residual %.3e after %d preconditioned solves",
+                      rel, it);
         return set_err(h, SPK_ENOCONV, buf);
     }
     return SPK_OK;
 }
 
-
 int spk_refine(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where, int precision,
                double tol, int max_iter, int* iters, double* relres) {
-    return refine_impl(h, b, x, nrhs, ld, where, precision, tol, max_iter, iters, relres, false);
+    return refine_impl(h, b, x, nrhs, ld, where, precision, tol, max_iter, SPK_SOLVER_AUTO, iters, relres, nullptr,
+                       false);
+}
+
+int spk_refine_ex(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where, int precision,
+                  double tol, int max_iter, int solver, int* iters, double* relres, int* solver_used) {
+    return refine_impl(h, b, x, nrhs, ld, where, precision, tol, max_iter, solver, iters, relres, solver_used, false);
 }
 
 int spk_refine_transpose(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where, int precision,
                          double tol, int max_iter, int* iters, double* relres) {
-    return refine_impl(h, b, x, nrhs, ld, where, precision, tol, max_iter, iters, relres, true);
+    return refine_impl(h, b, x, nrhs, ld, where, precision, tol, max_iter, SPK_SOLVER_IR, iters, relres, nullptr,
+                       true);
 }
 
 int spk_grad_pattern(spk_handle* h, const double* lambda, const double* x, int64_t nrhs, int64_t ld, int where,
@@ -1770,7 +1980,8 @@ int spk_get_factors(spk_handle* h, int precision, double* lnz, double* unz, int6
     if (rc) return rc;
     if (!valid_precision(precision)) return set_err(h, SPK_EARG, "spk_get_factors: bad precision");
     const bool done = factored(h, precision);
-    const bool loaded = precision == SPK_FP64 ? h->s64.loaded : h->s32.loaded;
+    const bool loaded = precision == SPK_FP64 ? h->s64.loaded : float_storage(h, precision).loaded;
+    select_form(h, precision);
     if (!done && !loaded) return set_err(h, SPK_ESEQ, "Sequence error. Matrix input not done yet.");
     std::vector<double> fac;
     rc = precision == SPK_FP64 ? fetch_factor<double>(h, fac) : fetch_factor<float>(h, fac);
@@ -1861,15 +2072,16 @@ void spk_destroy(spk_handle* h) {
     free_plan(h->plan[0]);
     free_plan(h->plan[1]);
     void* ptrs[] = {h->d_xs, h->d_rows, h->d_runid, h->d_run_tgt, h->d_run_start, h->d_run_rel,
-                    h->d_rel, h->s64.inv2, h->s32.inv2, h->s64.pack, h->s32.pack, h->d_ipiv, h->d_bmap, h->d_info, h->d_slot, h->d_aval,
-                    h->d_rowptr, h->d_col, h->d_src, h->d_ccolptr, h->d_crow, h->d_ccol, h->d_rperm, h->d_rinvp, h->s64.d, h->s32.d, h->d_wb,
-                    h->d_wy, h->d_wx, h->d_rhs, h->d_x, h->d_r, h->d_sums};
+                    h->d_rel, h->s64.inv2, h->s32.inv2, h->s16.inv2, h->s64.pack, h->s32.pack, h->s16.pack, h->d_ipiv, h->d_bmap, h->d_info, h->d_slot, h->d_aval,
+                    h->d_rowptr, h->d_col, h->d_src, h->d_ccolptr, h->d_crow, h->d_ccol, h->d_rperm, h->d_rinvp, h->s64.d, h->s32.d, h->s16.d, h->d_wb,
+                    h->d_wy, h->d_wx, h->d_rhs, h->d_x, h->d_r, h->d_sums, h->gm_V, h->gm_Z, h->gm_w, h->gm_c};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     collect_events(h);
     for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
     drop_graph(h->g_factor[0]);
     drop_graph(h->g_factor[1]);
+    drop_graph(h->g_factor[2]);
     drop_solve_graphs(h);
     if (h->side) cudaStreamSynchronize(h->side);
     if (h->side2) cudaStreamSynchronize(h->side2);

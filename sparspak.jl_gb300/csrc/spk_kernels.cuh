@@ -935,6 +935,38 @@ __device__ __forceinline__ void pack_line(unsigned char* base, int t, int i, int
     }
 }
 
+// BF16 form of pack_line: the line's entries times `scale` (a power of two)
+// as BF16 at tile `t`, line `i` of the block's BF16 pack.
+template <int CQ>
+__device__ __forceinline__ void pack_line16(unsigned char* base, int t, int i, int q, int nch, const float (&v)[CQ],
+                                            float scale) {
+#pragma unroll
+    for (int g = 0; g < CQ / 4; ++g) {
+        const int k = q * CQ + 4 * g;
+        if (k < nch * umma::KCH) {
+            unsigned char* dst =
+                base + ((ll)t * nch + k / umma::KCH) * umma::PCHUNK16 + umma::packed_offset16(i, k % umma::KCH);
+            *reinterpret_cast<uint2*>(dst) = make_uint2(umma::pack_bf16x2(v[4 * g] * scale, v[4 * g + 1] * scale),
+                                                        umma::pack_bf16x2(v[4 * g + 2] * scale, v[4 * g + 3] * scale));
+        }
+    }
+}
+
+// Per-block exponent of the BF16 panel scaling: e = floor(E / 2), E the
+// binary exponent of the largest |diagonal entry of U_B|; the L panel is
+// packed times 2^e and the U panel times 2^-e, so L U^T is unchanged and both
+// scaled panels are about 2^(E/2) in size.  Every CTA of the block's panel
+// launch computes the same e from the final diagonal block (all threads
+// call; contains a barrier).
+__device__ __forceinline__ int block_scale_exp(const float* blkp, int ld, int bw, int* smax) {
+    if (threadIdx.x == 0) *smax = 0;
+    __syncthreads();
+    if ((int)threadIdx.x < bw) atomicMax(smax, __float_as_int(fabsf(blkp[(ll)threadIdx.x * ld + threadIdx.x])));
+    __syncthreads();
+    const int E = ((*smax >> 23) & 255) - 127;
+    return E >> 1;
+}
+
 // The panels of a block of more than 64 columns in FP32 (W = 128), four
 // lines per lane (sweep_rows4 / sweep_cols4): lane c of half-warp h holds
 // entries [8c, 8c + 8) of the tile's lines 4h .. 4h + 3.  Same tiles,
@@ -987,9 +1019,27 @@ __device__ __forceinline__ void pack_tile(unsigned char* base, const float* sX, 
     }
 }
 
+// BF16 form of pack_tile: entries times `scale`, one BF16 part per chunk.
+template <typename Where>
+__device__ __forceinline__ void pack_tile16(unsigned char* base, const float* sX, int nl, int nch, float scale,
+                                            Where where) {
+    for (int item = threadIdx.x; item < PT_LINES * 32; item += blockDim.x) {
+        const int g = (item >> 3) & 31, li = (item >> 8) * 8 + (item & 7);
+        if (li >= nl || 4 * g >= nch * umma::KCH) continue;
+        int t, i;
+        where(li, t, i);
+        const int k = 4 * g;
+        const float4 v = *reinterpret_cast<const float4*>(sX + li * PT_LD + k);
+        unsigned char* dst =
+            base + ((ll)t * nch + k / umma::KCH) * umma::PCHUNK16 + umma::packed_offset16(i, k % umma::KCH);
+        *reinterpret_cast<uint2*>(dst) =
+            make_uint2(umma::pack_bf16x2(v.x * scale, v.y * scale), umma::pack_bf16x2(v.z * scale, v.w * scale));
+    }
+}
+
 __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, const Sched& S, const DFront& F, int blk,
                                                int tile, unsigned char* pack, float* sT, float* sX, float* rd,
-                                               int* gmap, int* pa) {
+                                               int* gmap, int* pa, int bf16, int* smax) {
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
     const int tid = threadIdx.x, c = tid & 15, line0 = (tid >> 4) * 4;
     const int nL = cdiv(F.ld - c1, PT_LINES), nUa = cdiv(F.nf - c1, PT_LINES);
@@ -1039,12 +1089,17 @@ __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, cons
             if (li < nl && j < bw) xb[(ll)j * F.ld + li] = sX[li * PT_LD + j];
         }
         const ll off = S.blk_lpack[blk];
-        if (off >= 0)
-            pack_tile(pack + off, sX, nl, nch, [&](int li, int& t, int& i) {
-                const int r = rb0 + li;
-                t = r < F.nf ? (r - c1) / umma::TM : n1 + (r - F.nf) / umma::TM;
-                i = r < F.nf ? (r - c1) % umma::TM : (r - F.nf) % umma::TM;
-            });
+        auto whereL = [&](int li, int& t, int& i) {
+            const int r = rb0 + li;
+            t = r < F.nf ? (r - c1) / umma::TM : n1 + (r - F.nf) / umma::TM;
+            i = r < F.nf ? (r - c1) % umma::TM : (r - F.nf) % umma::TM;
+        };
+        if (off >= 0 && bf16) {
+            const float scale = umma::exp2i(block_scale_exp(blkp, F.ld, bw, smax));
+            pack_tile16(pack + (off >> 2), sX, nl, nch, scale, whereL);
+        } else if (off >= 0) {
+            pack_tile(pack + off, sX, nl, nch, whereL);
+        }
     } else {
         if (tid < bw) {   // the block's row sources, from k_block_lu
             const int v = bmap[F.f + c0 + tid];
@@ -1098,12 +1153,17 @@ __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, cons
             if (li < nl && R < bw) yb[li * ls + (ll)R * rs] = sX[li * PT_LD + R];
         }
         const ll off = S.blk_upack[blk];
-        if (off >= 0)
-            pack_tile(pack + off, sX, nl, nch, [&](int li, int& t, int& i) {
-                const int col = cb0 + li;
-                t = inner ? (col - c1) / umma::TM : n1 + col / umma::TM;
-                i = inner ? (col - c1) % umma::TM : col % umma::TM;
-            });
+        auto whereU = [&](int li, int& t, int& i) {
+            const int col = cb0 + li;
+            t = inner ? (col - c1) / umma::TM : n1 + col / umma::TM;
+            i = inner ? (col - c1) % umma::TM : col % umma::TM;
+        };
+        if (off >= 0 && bf16) {
+            const float scale = umma::exp2i(-block_scale_exp(blkp, F.ld, bw, smax));
+            pack_tile16(pack + (off >> 2), sX, nl, nch, scale, whereU);
+        } else if (off >= 0) {
+            pack_tile(pack + off, sX, nl, nch, whereU);
+        }
     }
 }
 
@@ -1123,18 +1183,20 @@ __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, cons
 // block_panel128).
 template <typename T, int W>
 __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, const int* bmap, Sched S, Launch L,
-                                                      int step, unsigned char* pack) {
+                                                      int step, unsigned char* pack, int bf16) {
     constexpr int CQ = W / 4;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sT = reinterpret_cast<T*>(smem_raw);
     __shared__ T rd[W];
     __shared__ int q0[W + 1], gmap[W], pa[W];
+    __shared__ int smax;
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
     const int blk = F.block0 + step;
     if constexpr (std::is_same<T, float>::value && W == 128) {
-        block_panel128(fac, bmap, S, F, blk, tile, pack, sT, sT + 128 * SLD<float, 128>::value, rd, gmap, pa);
+        block_panel128(fac, bmap, S, F, blk, tile, pack, sT, sT + 128 * SLD<float, 128>::value, rd, gmap, pa, bf16,
+                       &smax);
         return;
     }
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
@@ -1162,11 +1224,13 @@ __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, co
         }
         if constexpr (std::is_same<T, float>::value) {
             const ll off = S.blk_lpack[blk];
+            const float scale = (off >= 0 && bf16) ? umma::exp2i(block_scale_exp(blkp, F.ld, bw, &smax)) : 1.0f;
             if (off >= 0 && ok) {
                 const int n1 = cdiv(F.nf - c1, umma::TM);
                 const int t = r < F.nf ? (r - c1) / umma::TM : n1 + (r - F.nf) / umma::TM;
                 const int i = r < F.nf ? (r - c1) % umma::TM : (r - F.nf) % umma::TM;
-                pack_line<CQ>(pack + off, t, i, q, cdiv(bw, umma::KCH), x);
+                if (bf16) pack_line16<CQ>(pack + (off >> 2), t, i, q, cdiv(bw, umma::KCH), x, scale);
+                else pack_line<CQ>(pack + off, t, i, q, cdiv(bw, umma::KCH), x);
             }
         }
     } else {
@@ -1196,11 +1260,13 @@ __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, co
         }
         if constexpr (std::is_same<T, float>::value) {
             const ll off = S.blk_upack[blk];
+            const float scale = (off >= 0 && bf16) ? umma::exp2i(-block_scale_exp(blkp, F.ld, bw, &smax)) : 1.0f;
             if (off >= 0 && ok) {
                 const int n1 = cdiv(F.nf - c1, umma::TM);
                 const int t = inner ? (col - c1) / umma::TM : n1 + col / umma::TM;
                 const int i = inner ? (col - c1) % umma::TM : col % umma::TM;
-                pack_line<CQ>(pack + off, t, i, q, cdiv(bw, umma::KCH), y);
+                if (bf16) pack_line16<CQ>(pack + (off >> 2), t, i, q, cdiv(bw, umma::KCH), y, scale);
+                else pack_line<CQ>(pack + off, t, i, q, cdiv(bw, umma::KCH), y);
             }
         }
     }
@@ -1670,7 +1736,39 @@ __device__ __forceinline__ TcTile tc_decode(const Sched& S, const Launch& L, int
     return T;
 }
 
-template <int MODE>
+// The K loop of one tile as a sequence of pipeline stages: (block, first
+// chunk, chunks).  TRAIL: the chunks of block `step`; SCHUR: those of every
+// block of the front in turn.  A stage holds one chunk (TF32: hi + lo of A
+// and of B) or, in the BF16 form, up to umma::BF_GROUP consecutive chunks of
+// one block.  The copy and the MMA threads walk the same sequence.
+template <int MODE, bool BF>
+struct ChunkWalk {
+    static constexpr int G = BF ? umma::BF_GROUP : 1;
+    int b, c, nb, left;   // current block, its next chunk, its chunks; chunks of the tile left
+    __device__ __forceinline__ ChunkWalk(const Sched& S, const TcTile& T, int step) {
+        b = MODE == TC_TRAIL ? T.F.block0 + step : T.F.block0;
+        c = 0;
+        nb = cdiv(S.blk_c1[b] - S.blk_c0[b], umma::KCH);
+        left = T.nchunks;
+    }
+    // Next stage: block, first chunk, number of chunks; false when done.
+    __device__ __forceinline__ bool next(const Sched& S, int& blk, int& c0, int& kc) {
+        if (left <= 0) return false;
+        while (c == nb) {   // SCHUR: the next block of the front
+            ++b;
+            c = 0;
+            nb = cdiv(S.blk_c1[b] - S.blk_c0[b], umma::KCH);
+        }
+        blk = b;
+        c0 = c;
+        kc = min(G, nb - c);
+        c += kc;
+        left -= kc;
+        return true;
+    }
+};
+
+template <int MODE, bool BF>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const unsigned char* pack, Sched S, Launch L,
                                                               int step, int ntiles, int tile_base, int* err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1696,6 +1794,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
     umma::fence_after();
     const uint32_t tmem = *cx.tmem_slot;
     volatile int* vdead = &dead;
+    // bytes of one chunk of one operand, and where operand B starts in a stage
+    constexpr uint32_t CB = BF ? umma::PCHUNK16 : umma::PCHUNK;
+    constexpr uint32_t BOFF = 2 * umma::OPB;
 
     if (warp == 0) {
         if (lane == 0) {   // bulk copies
@@ -1703,36 +1804,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
             uint32_t ph = 0;
             for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
                 const TcTile T = tc_decode<MODE>(S, L, step, tile, tile_base);
-                int b = MODE == TC_TRAIL ? T.F.block0 + step : T.F.block0;
-                int c = 0, nb = MODE == TC_TRAIL ? 0 : cdiv(S.blk_c1[b] - S.blk_c0[b], umma::KCH);
-                int n1b = MODE == TC_TRAIL ? T.n1 : cdiv(T.F.nf - S.blk_c1[b], umma::TM);
-                for (int q = 0; q < T.nchunks; ++q) {
-                    if (MODE == TC_SCHUR) {
-                        while (c == nb) {   // next block of the front
-                            ++b;
-                            c = 0;
-                            nb = cdiv(S.blk_c1[b] - S.blk_c0[b], umma::KCH);
-                            n1b = cdiv(T.F.nf - S.blk_c1[b], umma::TM);
-                        }
-                    }
-                    const int nch = MODE == TC_TRAIL ? T.nchunks : nb;
+                ChunkWalk<MODE, BF> w(S, T, step);
+                int b, c, kc;
+                while (w.next(S, b, c, kc)) {
+                    const int nch = w.nb;
+                    const int n1b = MODE == TC_TRAIL ? T.n1 : cdiv(T.F.nf - S.blk_c1[b], umma::TM);
                     const int ra = MODE == TC_TRAIL ? T.rt : n1b + T.rt;
                     const int rb = MODE == TC_TRAIL ? T.ct : n1b + T.ct;
-                    const unsigned char* pa = pack + S.blk_lpack[b] + ((ll)ra * nch + c) * umma::PCHUNK;
-                    const unsigned char* pb = pack + S.blk_upack[b] + ((ll)rb * nch + c) * umma::PCHUNK;
+                    const ll lp = BF ? (S.blk_lpack[b] >> 2) : S.blk_lpack[b];
+                    const ll up = BF ? (S.blk_upack[b] >> 2) : S.blk_upack[b];
+                    const unsigned char* pa = pack + lp + ((ll)ra * nch + c) * CB;
+                    const unsigned char* pb = pack + up + ((ll)rb * nch + c) * CB;
                     umma::wait_bounded(&cx.empty[s], ph ^ 1, vdead, err);
-                    umma::arrive_expect_tx(&cx.full[s], 2 * umma::PCHUNK);
+                    umma::arrive_expect_tx(&cx.full[s], 2 * kc * CB);
                     const uint32_t dst = umma::saddr(cx.stage + s * umma::STAGE);
-                    umma::bulk_g2s(dst, pa, umma::PCHUNK, &cx.full[s]);
-                    umma::bulk_g2s(dst + umma::PCHUNK, pb, umma::PCHUNK, &cx.full[s]);
-                    ++c;
+                    umma::bulk_g2s(dst, pa, kc * CB, &cx.full[s]);
+                    umma::bulk_g2s(dst + BOFF, pb, kc * CB, &cx.full[s]);
                     if (++s == umma::PST) { s = 0; ph ^= 1; }
                 }
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {   // MMAs
-            constexpr uint32_t IDESC = umma::idesc_tf32(umma::TM, umma::TN);
+            constexpr uint32_t IDESC = BF ? umma::idesc_bf16(umma::TM, umma::TN) : umma::idesc_tf32(umma::TM, umma::TN);
             int s = 0;
             uint32_t ph = 0;
             int acc = 0;
@@ -1742,22 +1836,35 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
                 umma::wait_bounded(&cx.tempty[acc], aph ^ 1, vdead, err);
                 umma::fence_after();
                 const uint32_t d = tmem + acc * umma::TN;
-                for (int q = 0; q < T.nchunks; ++q) {
+                ChunkWalk<MODE, BF> w(S, T, step);
+                int b, c, kc;
+                bool first = true;
+                while (w.next(S, b, c, kc)) {
                     umma::wait_bounded(&cx.full[s], ph, vdead, err);
                     umma::fence_after();
-                    const uint32_t a_hi = umma::saddr(cx.stage + s * umma::STAGE), a_lo = a_hi + umma::OPB;
-                    const uint32_t b_hi = a_hi + 2 * umma::OPB, b_lo = a_hi + 3 * umma::OPB;
+                    const uint32_t a0 = umma::saddr(cx.stage + s * umma::STAGE), b0 = a0 + BOFF;
+                    if constexpr (BF) {
+                        for (int j = 0; j < kc; ++j) {   // one K = 16 product per chunk
+                            const uint64_t da = umma::desc_kmajor(a0 + j * CB, 128, umma::SBO16);
+                            const uint64_t db = umma::desc_kmajor(b0 + j * CB, 128, umma::SBO16);
+                            umma::mma_bf16(d, da, db, IDESC, (first && j == 0) ? 0u : 1u);
+                        }
+                    } else {
+                        const uint32_t a_hi = a0, a_lo = a0 + umma::OPB;
+                        const uint32_t b_hi = b0, b_lo = b0 + umma::OPB;
 #pragma unroll
-                    for (int kk = 0; kk < umma::KCH / 8; ++kk) {
-                        const uint32_t o = kk * 256;
-                        const uint64_t dah = umma::desc_kmajor(a_hi + o, 128, umma::SBO);
-                        const uint64_t dal = umma::desc_kmajor(a_lo + o, 128, umma::SBO);
-                        const uint64_t dbh = umma::desc_kmajor(b_hi + o, 128, umma::SBO);
-                        const uint64_t dbl = umma::desc_kmajor(b_lo + o, 128, umma::SBO);
-                        umma::mma_tf32(d, dah, dbh, IDESC, (q > 0 || kk > 0) ? 1u : 0u);
-                        umma::mma_tf32(d, dah, dbl, IDESC, 1u);
-                        umma::mma_tf32(d, dal, dbh, IDESC, 1u);
+                        for (int kk = 0; kk < umma::KCH / 8; ++kk) {
+                            const uint32_t o = kk * 256;
+                            const uint64_t dah = umma::desc_kmajor(a_hi + o, 128, umma::SBO);
+                            const uint64_t dal = umma::desc_kmajor(a_lo + o, 128, umma::SBO);
+                            const uint64_t dbh = umma::desc_kmajor(b_hi + o, 128, umma::SBO);
+                            const uint64_t dbl = umma::desc_kmajor(b_lo + o, 128, umma::SBO);
+                            umma::mma_tf32(d, dah, dbh, IDESC, (first && kk == 0) ? 0u : 1u);
+                            umma::mma_tf32(d, dah, dbl, IDESC, 1u);
+                            umma::mma_tf32(d, dal, dbh, IDESC, 1u);
+                        }
                     }
+                    first = false;
                     umma::commit(&cx.empty[s]);
                     if (++s == umma::PST) { s = 0; ph ^= 1; }
                 }
@@ -2765,6 +2872,88 @@ __global__ void __launch_bounds__(256) k_residual(const double* __restrict__ ava
                 }
         }
         residual_sums(rr, bb, r0, nr, sums);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// GMRES-IR (refinement whose correction equation A d = r is solved by GMRES
+// in FP64, preconditioned on the right by the low-precision LU).  Vectors are
+// n x nrhs column-major (ld n); a basis is an array of such blocks, vector j
+// at V + j * n * nrhs.  Every right-hand side has its own Krylov space.
+// ---------------------------------------------------------------------------
+
+// w = A z (FP64, rows of A gathered from CSC order through src).
+__global__ void __launch_bounds__(256) k_gm_spmv(const double* __restrict__ aval, const int* __restrict__ rowptr,
+                                                 const int* __restrict__ col, const ll* __restrict__ src,
+                                                 const double* __restrict__ z, double* __restrict__ w, int n, int nrhs) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        for (int r0 = 0; r0 < nrhs; r0 += RES_RG) {
+            double acc[RES_RG] = {0.0, 0.0, 0.0, 0.0};
+            for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+                const double a = aval[src[k]];
+                const int c = col[k];
+#pragma unroll
+                for (int q = 0; q < RES_RG; ++q)
+                    if (r0 + q < nrhs) acc[q] += a * z[(ll)(r0 + q) * n + c];
+            }
+#pragma unroll
+            for (int q = 0; q < RES_RG; ++q)
+                if (r0 + q < nrhs) w[(ll)(r0 + q) * n + i] = acc[q];
+        }
+    }
+}
+
+constexpr int GM_MAXRHS = 16;
+
+// out[j * nrhs + r] += <V_j[:, r], w[:, r]> for the basis vectors j = blockIdx.y
+// (w may be V itself with nv = 1: squared norms).
+__global__ void __launch_bounds__(256) k_gm_dots(const double* __restrict__ V, const double* __restrict__ w, int n,
+                                                 int nrhs, double* __restrict__ out) {
+    __shared__ double part[8][GM_MAXRHS];
+    const int j = blockIdx.y;
+    const double* v = V + (ll)j * n * nrhs;
+    double acc[GM_MAXRHS];
+#pragma unroll
+    for (int r = 0; r < GM_MAXRHS; ++r) acc[r] = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+#pragma unroll
+        for (int r = 0; r < GM_MAXRHS; ++r)
+            if (r < nrhs) acc[r] += v[(ll)r * n + i] * w[(ll)r * n + i];
+    const int wp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int r = 0; r < GM_MAXRHS; ++r) {
+        double t = acc[r];
+        for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
+        if (lane == 0) part[wp][r] = t;
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < nrhs) {
+        double t = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += part[q][threadIdx.x];
+        atomicAdd(&out[(ll)j * nrhs + threadIdx.x], t);
+    }
+}
+
+// w[:, r] += sign * sum_{j < nv} c[j * nrhs + r] V_j[:, r]  (w has leading dimension ldw).
+__global__ void __launch_bounds__(256) k_gm_axpy(const double* __restrict__ V, const double* __restrict__ c,
+                                                 double* __restrict__ w, ll ldw, int n, int nrhs, int nv, double sign) {
+    const ll tot = (ll)n * nrhs;
+    for (ll e = (ll)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (ll)gridDim.x * blockDim.x) {
+        const int r = (int)(e / n);
+        const int i = (int)(e - (ll)r * n);
+        double t = 0.0;
+        for (int j = 0; j < nv; ++j) t += c[(ll)j * nrhs + r] * V[(ll)j * tot + e];
+        w[(ll)r * ldw + i] += sign * t;
+    }
+}
+
+// v[:, r] = w[:, r] / sqrt(nrm2[r]) (zero where the norm is zero).
+__global__ void __launch_bounds__(256) k_gm_scale(const double* __restrict__ w, const double* __restrict__ nrm2,
+                                                  double* __restrict__ v, int n, int nrhs) {
+    const ll tot = (ll)n * nrhs;
+    for (ll e = (ll)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (ll)gridDim.x * blockDim.x) {
+        const double s = nrm2[e / n];
+        v[e] = s > 0.0 ? w[e] / sqrt(s) : 0.0;
     }
 }
 

@@ -1,6 +1,6 @@
 // Fifth-generation tensor cores (tcgen05) for the FP32 rank updates of the
-// factorisation: a 128 x 128 FP32 tile C = A * B in tensor memory with three
-// TF32 products per K step,
+// factorisation: a 128 x 128 FP32 tile C = A * B in tensor memory.  The
+// FP32 form takes three TF32 products per K step,
 //     A * B ~= Ahi * Bhi + Ahi * Blo + Alo * Bhi,
 // Ahi = tf32(A) (round to nearest), Alo = tf32(A - Ahi), which carries the
 // product to about FP32 accuracy (the dropped Alo * Blo term is ~2^-22
@@ -9,6 +9,11 @@
 // 128 bytes apart, 8-row groups SBO = KCH * 32 bytes apart), written by the
 // panel kernel; this header holds the descriptors, the MMA, TMEM and mbarrier
 // primitives, and the shared-memory plan of the packed pipeline.
+// The BF16 form (SPK_BF16S) takes one kind::f16 product with BF16 A and B
+// and FP32 accumulation per K step; its operands are single BF16 copies of
+// the panels (a quarter of the TF32 hi + lo bytes), each block's L panel
+// scaled by 2^e and its U panel by 2^-e (e from the block's diagonal), so
+// that every product L U^T is unchanged and the scaled panels stay near 1.
 #pragma once
 #include <cstdint>
 
@@ -35,6 +40,11 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int m, int n) {
     return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
+// Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
 __device__ __forceinline__ uint32_t tf32_rna(float x) {
     uint32_t r;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
@@ -45,6 +55,13 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b
     asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
         "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
 }
 
@@ -116,6 +133,30 @@ constexpr int PSMEM = PST * STAGE + 2048;             // + alignment slack, barr
 __host__ __device__ constexpr uint32_t packed_offset(int i, int kk) {
     return (uint32_t)((i >> 3) * SBO + (kk >> 2) * 128 + (i & 7) * 16 + (kk & 3) * 4);
 }
+
+// BF16 packed operands: the same tiles and 16-column chunks, one BF16 part
+// per chunk (4 KB: 8-row x 16-byte core matrices, the two K-adjacent ones
+// 128 bytes apart, 8-row groups SBO16 apart).  The byte offset of a block's
+// BF16 pack is a quarter of its TF32 pack offset.  A pipeline stage carries
+// up to BF_GROUP consecutive chunks of one tile and block (one bulk copy per
+// operand), i.e. BF_GROUP MMAs of K = 16.
+constexpr int PCHUNK16 = TM * KCH * 2;                // 4 KB
+constexpr int SBO16 = KCH * 16;                       // 256 bytes between 8-row groups
+constexpr int BF_GROUP = 4;                           // chunks per stage: 16 KB per operand
+
+__host__ __device__ constexpr uint32_t packed_offset16(int i, int kk) {
+    return (uint32_t)((i >> 3) * SBO16 + (kk >> 3) * 128 + (i & 7) * 16 + (kk & 7) * 2);
+}
+
+// Two floats as round-to-nearest BF16, low half first.
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    uint32_t r;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
+
+// 2^e as a float (e in the normal range).
+__device__ __forceinline__ float exp2i(int e) { return __int_as_float((127 + e) << 23); }
 
 __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint64_t* bar) {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),

@@ -22,7 +22,7 @@ HOST_SO = os.path.join(LIBDIR, "libspk_host.so")
 GPU_SO = os.path.join(LIBDIR, "libspk_gpu.so")
 
 HOST_SRC = [os.path.join(CSRC, "spk_symbolic.cpp")]
-GPU_SRC = [os.path.join(CSRC, "spk_gpu.cu")]
+GPU_SRC = [os.path.join(CSRC, "spk_gpu.cu"), os.path.join(CSRC, "spk_probe.cu")]
 GPU_DEPS = GPU_SRC + [os.path.join(CSRC, "spk_kernels.cuh"), os.path.join(CSRC, "spk_umma.cuh"),
                       os.path.join(INCLUDE, "spk_gpu.h")]
 HOST_DEPS = HOST_SRC + [os.path.join(INCLUDE, "spk_host.h")]

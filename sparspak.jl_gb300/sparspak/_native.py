@@ -44,6 +44,10 @@ GPU_SYMBOLS = {
     "spk_grad_pattern": (ctypes.c_int, [VP, VP, VP, i64, i64, ctypes.c_int, VP]),
     "spk_refine": (ctypes.c_int, [VP, VP, VP, i64, i64, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                   ctypes.c_int, ctypes.POINTER(ctypes.c_int), PD]),
+    "spk_measure_peaks": (ctypes.c_int, [PD, PD, PD]),
+    "spk_refine_ex": (ctypes.c_int, [VP, VP, VP, i64, i64, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                     ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), PD,
+                                     ctypes.POINTER(ctypes.c_int)]),
     "spk_residual": (ctypes.c_int, [VP, VP, VP, i64, i64, ctypes.c_int, PD]),
     "spk_residual_noalloc": (ctypes.c_int, [VP, VP, VP, i64, i64, PD]),
     "spk_get_factors": (ctypes.c_int, [VP, ctypes.c_int, PD, PD, P64]),
@@ -71,7 +75,9 @@ KERNEL_UNITS = {"tc_trail": "tcgen05 kind::tf32, 3xTF32 per term", "tc_schur": "
                 "trail": "FP32/FP64 FMA (fronts without a pack)", "schur": "FP32/FP64 FMA (fronts without a pack)",
                 "getrf": "FP32 FMA, latency-bound (one CTA per front, sequential pivot columns; small fronts a warp each)",
                 "panel": "FP32 FMA (register-line triangular sweeps)"}
-SPK_FP64, SPK_FP32 = 0, 1
+SPK_FP64, SPK_FP32, SPK_BF16S = 0, 1, 2
+SPK_SOLVER_AUTO, SPK_SOLVER_IR, SPK_SOLVER_GMRES = 0, 1, 2
+SOLVERS = {"auto": SPK_SOLVER_AUTO, "ir": SPK_SOLVER_IR, "gmres": SPK_SOLVER_GMRES}
 
 _lock = threading.Lock()
 _host = None

@@ -13,7 +13,7 @@ import numpy as np
 
 from . import _native as N
 
-PRECISIONS = {"fp64": N.SPK_FP64, "fp32": N.SPK_FP32}
+PRECISIONS = {"fp64": N.SPK_FP64, "fp32": N.SPK_FP32, "bf16s": N.SPK_BF16S}
 
 
 class ErrorException(Exception):
@@ -33,7 +33,7 @@ def _prec(p) -> int:
         try:
             return PRECISIONS[p.lower()]
         except KeyError:
-            raise ValueError(f"unknown precision {p!r}; use 'fp64' or 'fp32'") from None
+            raise ValueError(f"unknown precision {p!r}; use 'fp64', 'fp32' or 'bf16s'") from None
     return int(p)
 
 
@@ -141,7 +141,11 @@ class NumericEngine:
         self._check(fn(self._h, p, nrhs, ld, where, _prec(precision)), "spk_solve")
         return b
 
-    def refine(self, b, x, precision="fp32", tol=1e-12, max_iter=20, raise_on_fail=True, transpose=False):
+    def refine(self, b, x, precision="fp32", tol=1e-12, max_iter=20, raise_on_fail=True, transpose=False,
+               solver=None):
+        """FP64 refinement of x for A x = b (A^T x = b with `transpose`).  Returns
+        (preconditioned solves after the first, relative residual); with
+        `solver` ('auto', 'ir', 'gmres') the solver actually used is appended."""
         n, nrhs, ld = _shape(b)
         pb, wb = _ptr(b)
         px, wx = _ptr(x)
@@ -149,13 +153,19 @@ class NumericEngine:
             raise ValueError("b and x must both live on the host or both on the device")
         it = ctypes.c_int(0)
         rr = ctypes.c_double(0.0)
-        fn = self._lib.spk_refine_transpose if transpose else self._lib.spk_refine
-        rc = fn(self._h, pb, px, nrhs, ld, wb, _prec(precision), float(tol), int(max_iter), ctypes.byref(it),
-                ctypes.byref(rr))
-        if rc == N.SPK_ENOCONV and not raise_on_fail:
+        used = ctypes.c_int(0)
+        if transpose:
+            rc = self._lib.spk_refine_transpose(self._h, pb, px, nrhs, ld, wb, _prec(precision), float(tol),
+                                                int(max_iter), ctypes.byref(it), ctypes.byref(rr))
+        else:
+            rc = self._lib.spk_refine_ex(self._h, pb, px, nrhs, ld, wb, _prec(precision), float(tol), int(max_iter),
+                                         N.SOLVERS[solver or "auto"], ctypes.byref(it), ctypes.byref(rr),
+                                         ctypes.byref(used))
+        if not (rc == N.SPK_ENOCONV and not raise_on_fail):
+            self._check(rc, "spk_refine")
+        if solver is None:
             return it.value, rr.value
-        self._check(rc, "spk_refine")
-        return it.value, rr.value
+        return it.value, rr.value, {N.SPK_SOLVER_IR: "ir", N.SPK_SOLVER_GMRES: "gmres"}.get(used.value, "ir")
 
     def grad_pattern(self, lam, x):
         """dA on A's pattern (CSC order) = -sum_r lam_r x_r^T: numpy in, numpy out (or torch CUDA in and out)."""

@@ -165,7 +165,7 @@ def _triangularsolve_(s: _SparseBase, solution: np.ndarray) -> bool:
 class SparseSolver:
     """SparseSolver(p::Problem) or SparseSolver(m::SparseMatrixCSC) - SpkSparseSolver.jl:17-73.
 
-    ``precision`` ('fp64' or 'fp32') selects the factor the numeric phases use.
+    ``precision`` ('fp64', 'fp32' or 'bf16s') selects the factor the numeric phases use.
     """
 
     def __init__(self, p, precision: str = "fp64", maxblocksize: int = 30):
@@ -289,10 +289,14 @@ def solve_(s: SparseSolver, rhs=None) -> bool:
 
 
 def refine_(s: SparseSolver, b: np.ndarray, x: np.ndarray | None = None, precision: str = "fp32", tol: float = 1e-12,
-            max_iter: int = 20, transpose: bool = False):
-    """Mixed-precision solve: factor in `precision` (if not yet), then FP64 iterative refinement.
+            max_iter: int = 20, transpose: bool = False, solver: str | None = None):
+    """Mixed-precision solve: factor in `precision` ('fp32', 'bf16s' or
+    'fp64'; if not yet), then FP64 iterative refinement - plain, or GMRES-IR
+    once plain refinement stagnates (solver 'auto'), or as chosen ('ir',
+    'gmres').
 
-    Returns (x, corrections, relative residual).  New in this engine; the
+    Returns (x, preconditioned solves after the first, relative residual),
+    plus the solver used when `solver` is given.  New in this engine; the
     reference's refinement exists only as a commented-out Fortran
     translation (SpkSparseSpdSolver.jl:267-343).
     """
@@ -305,8 +309,8 @@ def refine_(s: SparseSolver, b: np.ndarray, x: np.ndarray | None = None, precisi
         factor_(s)
     b = np.asfortranarray(b, dtype=np.float64)
     x = np.zeros_like(b) if x is None else x
-    it, rr = s.slvr.engine.refine(b, x, precision, tol, max_iter, transpose=transpose)
-    return x, it, rr
+    out = s.slvr.engine.refine(b, x, precision, tol, max_iter, transpose=transpose, solver=solver)
+    return (x,) + tuple(out)
 
 
 def gradient_(s: SparseSolver, lam: np.ndarray, x: np.ndarray) -> np.ndarray:
