@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--grid", type=int, default=64)
     ap.add_argument("--nrhs", type=int, default=4)
     ap.add_argument("--sample-grid", type=int, default=48, help="grid of the CPU baseline's bounded sample")
+    ap.add_argument("--ordering", default="nd_grid", choices=["nd_grid", "nd_graph"],
+                    help="nested dissection: geometric (box grid) or level-structure (general graph)")
     ap.add_argument("--one-step", action="store_true",
                     help="profiling aid: one warm-up step, then exactly one mixed step, no other work")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "bf16s"], help="precision of --one-step")
@@ -117,12 +119,18 @@ def workload(k, nrhs):
     return A, np.asfortranarray(b.reshape(A.shape[0], nrhs))
 
 
-def symbolic(A, k):
+def orderfunction(ordering, k):
+    import sparspak as S
+
+    return S.nd_grid(k, k, k) if ordering == "nd_grid" else S.nd_graph()
+
+
+def symbolic(A, k, ordering="nd_grid"):
     import sparspak as S
 
     s = S.SparseSolver(A)
     t0 = time.perf_counter()
-    S.findorder_(s, S.nd_grid(k, k, k))
+    S.findorder_(s, orderfunction(ordering, k))
     t1 = time.perf_counter()
     S.symbolicfactor_(s)
     t2 = time.perf_counter()
@@ -153,7 +161,7 @@ def csc1(A):
     return A.indptr.astype(np.int64) + 1, A.indices.astype(np.int64) + 1, np.ascontiguousarray(A.data)
 
 
-def oracle_run(k, nrhs, slices=1):
+def oracle_run(k, nrhs, slices=1, ordering="nd_grid"):
     """The reference's numeric phase on the host cores, by the oracle alone
     (its own ordering plug-in and structure phase, dense calls through the
     scipy-bundled BLAS/LAPACK): _inmatrix!, _lufactor!, one _triangularsolve!
@@ -167,7 +175,7 @@ def oracle_run(k, nrhs, slices=1):
     n = A.shape[0]
     cp, rv, nz = csc1(A)
     t0 = time.perf_counter()
-    st = oracle.structure_csc(cp, rv, n, "nd", (k, k, k))
+    st = oracle.structure_csc(cp, rv, n, "nd" if ordering == "nd_grid" else "nd_graph", (k, k, k))
     t_struct = time.perf_counter() - t0
     blas = oracle.use_blas(True)
     nslices = max(int(slices), 1)
@@ -195,7 +203,7 @@ def oracle_run(k, nrhs, slices=1):
 def cpu_baseline(args, F_full):
     """The oracle (BLAS mode) on the complete numeric phase of the --sample-grid^3
     instance of the same workload, scaled to the full grid by the LU flop ratio."""
-    r = oracle_run(args.sample_grid, args.nrhs)
+    r = oracle_run(args.sample_grid, args.nrhs, ordering=args.ordering)
     rate = r["flops"] / r["factor_s"]
     est_ms = r["total_s"] * F_full / r["flops"] * 1e3
     return {"value": est_ms, "unit": "ms", "cores": int(r["blas"]["threads"]), "kind": "port",
@@ -241,9 +249,15 @@ def dist_setup(args):
     return ws, rank, local
 
 
-def config_of(k, nrhs, n, nnz_a):
+ORDERING_NAMES = {"nd_grid": "nested dissection (geometric, box grid)",
+                  "nd_graph": "nested dissection (level-structure separators, general graph)"}
+
+
+def config_of(k, nrhs, n, nnz_a, ordering="nd_grid"):
+    """The workload, identical in both arms' lines."""
     return {"workload": f"laplace3d_{k}^3_shift1e-3_nd_{nrhs}rhs", "n": n, "nnz_A": nnz_a, "nrhs": nrhs,
-            "ordering": "nested dissection (grid)", "maxblocksize": 30}
+            "ordering": ORDERING_NAMES[ordering], "maxblocksize": 30,
+            "l2": "inputs larger than L2 (the 64^3 FP32 factor is 1.2 GB)", "parallelism": "replicas"}
 
 
 def run_reference(args):
@@ -259,13 +273,13 @@ def run_reference(args):
     if rank != 0:
         return
     for _ in range(args.warmup):
-        oracle_run(16, args.nrhs)
-    r = oracle_run(args.grid, args.nrhs, slices=args.steps)
+        oracle_run(16, args.nrhs, ordering=args.ordering)
+    r = oracle_run(args.grid, args.nrhs, slices=args.steps, ordering=args.ordering)
     v = r["total_s"] * 1e3
     line = {"metric": METRIC, "value": v, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": v / args.steps, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": config_of(args.grid, args.nrhs, r["n"], r["nnz_A"]),
+            "config": config_of(args.grid, args.nrhs, r["n"], r["nnz_A"], args.ordering),
             "step": (f"step = one of {args.steps} consecutive slices of a single complete {args.grid}^3 numeric "
                      f"phase (slice 0 with _inmatrix!, the last with the {args.nrhs} solves); value = their sum; "
                      f"warm-up steps: the complete 16^3 instance"),
@@ -293,7 +307,7 @@ def run_ours(args):
     k, nrhs = args.grid, args.nrhs
     A, b = workload(k, nrhs)
     n = A.shape[0]
-    s, host_t = symbolic(A, k)
+    s, host_t = symbolic(A, k, args.ordering)
     F = lu_flops(s.slvr)
     eng = _ensure_engine(s.slvr)
     colptr, rowval, nzval = _matrix_arrays(A)
@@ -490,10 +504,9 @@ def run_ours(args):
         "metric": METRIC, "value": ms_mixed, "unit": "ms", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_mixed, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 factor/solve + f64 residual/correction", "data": "synthetic",
-        "config": {"workload": f"laplace3d_{k}^3_shift1e-3_nd_{nrhs}rhs", "n": n, "nnz_A": int(A.nnz),
-                   "nrhs": nrhs, "ordering": "nested dissection (grid)", "maxblocksize": 30,
-                   "nnz_LU": int(nnz_full), "lu_flops": F, "fronts": stats["fronts"], "levels": stats["levels"],
-                   "l2": "inputs larger than L2 (factor %.2f GB)" % (nnz_full * 4 / 1e9), "parallelism": "replicas"},
+        "config": config_of(k, nrhs, n, int(A.nnz), args.ordering),
+        "structure": {"nnz_LU": int(nnz_full), "lu_flops": F, "fronts": stats["fronts"], "levels": stats["levels"],
+                      "factor_gb_fp32": nnz_full * 4 / 1e9},
         "mixed": {"ms": ms_mixed, "ms_eager_profiled": ms_mixed_eager, "corrections": it_mixed, "relres": rr_mixed,
                   "relres_host_check": rr_check,
                   "factor_ms": ms_f32, "factor_gflops": F / (ms_f32 * 1e-3) / 1e9, "assembly_ms": ms_asm32},

@@ -46,6 +46,15 @@ extern "C" {
 #define SPK_FP32 1         /* factor and solve in float; residual and correction
                               in double (mixed form for spk_refine); the large
                               rank updates as 3xTF32 tensor-core products        */
+#define SPK_SPD 16         /* flag, or-ed with a precision: the symmetric form for
+                              symmetric positive definite A (the SPD solver's
+                              Cholesky, src/SparseSpdMethod/SpkLDLtFactor.jl,
+                              on the LU supernode partition): no interchanges
+                              (POTRF-like diagonal blocks), only the lower part
+                              of every rank update is formed (SYRK-like, half
+                              the update flops) and the U side, U = D L^T, is
+                              written from the L panels; solves as for LU.
+                              Its own factor storage, beside the LU one.     */
 #define SPK_BF16S 2        /* as SPK_FP32, but the large rank updates (Schur
                               complements and trailing updates) take BF16
                               operands with a power-of-two scale per block panel
@@ -219,7 +228,12 @@ int spk_residual_noalloc(spk_handle* h, const double* b, const double* x, int64_
  * supernode's diagonal block), exactly as _SparseBase holds them after
  * factor! (src/SparseMethod/SpkSparseBase.jl:99-125).  Before spk_factor
  * (after spk_load_values) it returns the assembled A, with ipiv all zero, as
- * after inmatrix!.  Any pointer may be NULL.
+ * after inmatrix!.  Any pointer may be NULL.  With SPK_SPD: the Cholesky
+ * factor C (A = C C^T) in lnz's lower part (each supernode's diagonal block
+ * and the rows below it, the layout of the SPD solver's lnz,
+ * src/SparseSpdMethod/SpkSparseSpdBase.jl:210-227), C^T in the upper part
+ * of the diagonal blocks and in unz, ipiv the identity; SPK_ESINGULAR if a
+ * pivot is not positive.
  */
 int spk_get_factors(spk_handle* h, int precision, double* lnz, double* unz, int64_t* ipiv);
 

@@ -70,6 +70,17 @@ int spk_order_nd_grid(int64_t nx, int64_t ny, int64_t nz, int64_t leaf,
                       const int64_t* xadj, const int64_t* adj,
                       int64_t* perm, int64_t* invp);
 
+/*
+ * Nested dissection of a general symmetric graph (1-based xadj/adj without
+ * self loops): level-structure separators from pseudo-peripheral vertices,
+ * recursively, separators last; sets of at most `leaf` vertices ordered by
+ * minimum degree.  Like spk_order_nd_grid, a project ordering for findorder!'s
+ * orderfunction slot (src/SparseMethod/SpkSparseBase.jl:173-181); the
+ * reference has no nested dissection.  perm[new] = old, invp[old] = new.
+ */
+int spk_order_nd_graph(int64_t nv, const int64_t* xadj, const int64_t* adj, int64_t leaf,
+                       int64_t* perm, int64_t* invp);
+
 /* Opaque result of the symbolic phase. */
 typedef struct spk_symbolic spk_symbolic;
 

@@ -30,6 +30,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRCS = [os.path.join(HERE, "spk_oracle.c"), os.path.join(HERE, "spk_oracle_struct.c")]
 SO = os.path.join(HERE, "liboracle.so")
+DUAL_SRC = os.path.join(HERE, "spk_oracle_dual.cpp")
+DUAL_SO = os.path.join(HERE, "liboracle_dual.so")
 
 _P = ctypes.POINTER(ctypes.c_int64)
 _D = ctypes.POINTER(ctypes.c_double)
@@ -40,6 +42,9 @@ def build(force: bool = False) -> str:
     """Compile the oracle with gcc (no FMA contraction, so every host gives the same bits)."""
     if force or not os.path.exists(SO) or any(os.path.getmtime(SO) < os.path.getmtime(f) for f in SRCS):
         cmd = ["gcc", "-O2", "-std=c99", "-fPIC", "-shared", "-ffp-contract=off", "-o", SO] + SRCS + ["-lm"]
+        subprocess.run(cmd, check=True, capture_output=True)
+    if force or not os.path.exists(DUAL_SO) or os.path.getmtime(DUAL_SO) < os.path.getmtime(DUAL_SRC):
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-o", DUAL_SO, DUAL_SRC]
         subprocess.run(cmd, check=True, capture_output=True)
     return SO
 
@@ -54,6 +59,8 @@ def lib():
         L.oracle_inmatrix_csc.argtypes = [i, i, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _D, _P, _D]
         L.oracle_lufactor.restype = i
         L.oracle_lufactor.argtypes = [i, i, _P, _P, _P, _P, _P, _D, _P, _D, _P, _P]
+        L.oracle_cholfactor.restype = i
+        L.oracle_cholfactor.argtypes = [i, i, _P, _P, _P, _P, _P, _D]
         L.oracle_lu_begin.restype = ctypes.c_void_p
         L.oracle_lu_begin.argtypes = [i, i, _P, _P, _P, _P, _P, _D, _P, _D, _P]
         L.oracle_lu_run.restype = i
@@ -72,6 +79,8 @@ def lib():
         L.oracle_blas_mode.restype = ctypes.c_int
         L.oracle_mmd.restype = None
         L.oracle_mmd.argtypes = [i, _P, _P, _P, _P]
+        L.oracle_nd_graph.restype = i
+        L.oracle_nd_graph.argtypes = [i, _P, _P, i, _P, _P]
         L.oracle_nd_grid.restype = i
         L.oracle_nd_grid.argtypes = [i, i, i, i, _P, _P, _P, _P]
         L.oracle_symbolic1.restype = i
@@ -130,6 +139,25 @@ class OracleLU:
                                       _p(self.ipiv), _p(fs))
         self.first_singular = int(fs[0])
         return int(iflag)
+
+    def cholfactor(self) -> int:
+        """Supernodal Cholesky of an SPD matrix on the same partition (after
+        inmatrix_csc): lnz's lower parts receive C, A = C C^T.  Returns 0 or
+        the 1-based column of the first non-positive pivot."""
+        return int(lib().oracle_cholfactor(self.n, self.nsuper, _p(self.xsuper), _p(self.snode), _p(self.xlindx),
+                                           _p(self.lindx), _p(self.xlnz), _d(self.lnz)))
+
+    def lower_mask(self):
+        """Boolean mask of the lnz entries on or below the diagonal (row t of
+        supernode column k is on or below it when t >= k)."""
+        m = np.zeros(self.lnz.shape[0], dtype=bool)
+        for js in range(self.nsuper):
+            f, l = int(self.xsuper[js]), int(self.xsuper[js + 1])
+            jlen = int(self.xlindx[js + 1] - self.xlindx[js])
+            for k in range(l - f):
+                base = int(self.xlnz[f - 1 + k]) - 1
+                m[base + k: base + jlen] = True
+        return m
 
     def factor_slices(self, bounds):
         """_lufactor! run as consecutive slices of supernodes: bounds[k] is the
@@ -291,6 +319,16 @@ def nd_grid(xadj, adj, nx, ny, nz=1, leaf=64):
     return perm, invp
 
 
+def nd_graph(xadj, adj, n, leaf=64):
+    """General-graph nested dissection (the ordering plug-in), (perm, invp), 1-based."""
+    perm = np.zeros(n, np.int64)
+    invp = np.zeros(n, np.int64)
+    got = lib().oracle_nd_graph(n, _p(xadj), _p(adj), leaf, _p(perm), _p(invp))
+    if got != n:
+        raise ValueError(f"nested dissection ordered {got} of {n} vertices")
+    return perm, invp
+
+
 def symbolic(xadj, adj, perm, invp, maxblocksize=30) -> OracleStructure:
     """_symbolicfactor! for the graph and an initial ordering."""
     n = int(xadj.shape[0] - 1)
@@ -317,14 +355,58 @@ def symbolic(xadj, adj, perm, invp, maxblocksize=30) -> OracleStructure:
 
 def structure_csc(colptr, rowval, n, ordering="mmd", grid=None, leaf=64, maxblocksize=30) -> OracleStructure:
     """Ordering + symbolic factorisation of a CSC pattern (1-based colptr /
-    rowval): ordering "mmd" (the reference default) or "nd" with
-    grid = (nx, ny, nz)."""
+    rowval): ordering "mmd" (the reference default), "nd" (geometric, with
+    grid = (nx, ny, nz)) or "nd_graph" (level-structure nested dissection)."""
     xadj, adj = graph_of(colptr, rowval, n)
     if ordering == "mmd":
         perm, invp = mmd(xadj, adj, n)
     elif ordering == "nd":
         nx, ny, nz = grid
         perm, invp = nd_grid(xadj, adj, nx, ny, nz, leaf)
+    elif ordering == "nd_graph":
+        perm, invp = nd_graph(xadj, adj, n, leaf)
     else:
         raise ValueError(ordering)
     return symbolic(xadj, adj, perm, invp, maxblocksize)
+
+
+# ---------------------------------------------------------------------------
+# forward-mode (Dual number) derivatives through the LU path
+# ---------------------------------------------------------------------------
+
+_dual = None
+
+
+def dual_solve(sym, colptr, rowval, nzval, dnz, b):
+    """x = A^{-1} b and dx/dp for A's values with partials dnz (nnz x k,
+    k <= 16 directions), by the reference's LU path on Dual numbers
+    (spk_oracle_dual.cpp).  sym: a structure (OracleStructure or the
+    package's _SparseBase).  Returns (x, dx) with dx of shape n x k."""
+    global _dual
+    if _dual is None:
+        build()
+        L = ctypes.CDLL(DUAL_SO)
+        i = ctypes.c_int64
+        L.oracle_dual_solve.restype = i
+        L.oracle_dual_solve.argtypes = [i, i, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _D, _D, _D, _D, _D]
+        L.oracle_dual_partials.restype = ctypes.c_int
+        _dual = L
+    g = lambda a: np.ascontiguousarray(a, dtype=np.int64)
+    n = int(sym.n)
+    npart = _dual.oracle_dual_partials()
+    dnz = np.asarray(dnz, np.float64)
+    k = dnz.shape[1]
+    if k > npart:
+        raise ValueError(f"at most {npart} directions per call")
+    dpad = np.zeros((dnz.shape[0], npart))
+    dpad[:, :k] = dnz
+    x = np.zeros(n)
+    dx = np.zeros((n, npart))
+    rc = _dual.oracle_dual_solve(n, int(sym.nsuper), _p(g(sym.xsuper)), _p(g(sym.snode)), _p(g(sym.xlindx)),
+                                 _p(g(sym.lindx)), _p(g(sym.xlnz)), _p(g(sym.xunz)), _p(g(sym.order.rperm)),
+                                 _p(g(sym.order.rinvp)), _p(g(colptr)), _p(g(rowval)),
+                                 _d(np.ascontiguousarray(nzval, np.float64)), _d(dpad),
+                                 _d(np.ascontiguousarray(b, np.float64)), _d(x), _d(dx))
+    if rc != 0:
+        raise ValueError(f"No space for matrix element at CSC position {-rc}")
+    return x, dx[:, :k]

@@ -404,6 +404,112 @@ i64 oracle_lufactor(i64 n, i64 nsuper, const i64* xsuper, const i64* snode, cons
     return oracle_lu_end(c, first_singular);
 }
 
+/* ---- supernodal Cholesky on the LU partition ------------------------------ */
+
+/* The symmetric form of _lufactor! for symmetric positive definite A: the
+ * same left-looking loop over supernodes and the same link lists
+ * (SpkLUFactor.jl:89-252), with L alone: the update of jsup by ksup is
+ * L_j -= L_k L_k(jsup rows)^T (the _gemm!('n','t') of the L part with the
+ * U-panel operand replaced by L's own rows), the diagonal block is factored
+ * by a POTRF (lower, no interchanges: the correct form of the SPD solver's
+ * _pchole!, SpkLDLtFactor.jl:347-378, whose scaling is misplaced) and the
+ * rows below by _trsm!('r','l','t','n').  On return lnz holds the Cholesky
+ * factor C (A = C C^T) in the lower part of every supernode block; the
+ * upper part of the diagonal blocks is not meaningful.  Returns 0, or the
+ * 1-based column of the first non-positive pivot. */
+i64 oracle_cholfactor(i64 n, i64 nsuper, const i64* xsuper, const i64* snode, const i64* xlindx, const i64* lindx,
+                      const i64* xlnz, double* lnz) {
+    i64* link = (i64*)calloc((size_t)nsuper + 1, sizeof(i64));
+    i64* lngth = (i64*)calloc((size_t)nsuper + 1, sizeof(i64));
+    i64* map = (i64*)calloc((size_t)n + 1, sizeof(i64));
+    i64* relind = (i64*)calloc((size_t)n + 1, sizeof(i64));
+    i64 tmpsiz = 0, bad = 0;
+    for (i64 i = 1; i <= nsuper; ++i) {
+        lngth[i] = A1(xlindx, i + 1) - A1(xlindx, i);
+        i64 w = A1(xsuper, i + 1) - A1(xsuper, i);
+        i64 need = w * (A1(xlnz, A1(xsuper, i) + 1) - A1(xlnz, A1(xsuper, i)));
+        if (need > tmpsiz) tmpsiz = need;
+    }
+    double* temp = (double*)calloc((size_t)tmpsiz + 1, sizeof(double));
+    double* L = lnz - 1;
+    for (i64 js = 1; js <= nsuper; ++js) {
+        i64 fj = A1(xsuper, js), lj = A1(xsuper, js + 1) - 1, nj = lj - fj + 1;
+        i64 jlen = A1(xlnz, fj + 1) - A1(xlnz, fj);
+        i64 jx = A1(xlindx, js), jl = A1(xlnz, fj);
+        for (i64 j = 1, kk = jlen - 1; j <= jlen; ++j, --kk) map[A1(lindx, jx + j - 1)] = kk;
+        i64 nxt = 0;
+        for (;;) {
+            i64 ks = link[js];
+            if (ks == 0) break;
+            link[js] = link[ks];
+            link[ks] = 0;
+            i64 fk = A1(xsuper, ks);
+            i64 kslen = A1(xlnz, fk + 1) - A1(xlnz, fk);
+            i64 nk = A1(xsuper, ks + 1) - fk;
+            i64 klen = lngth[ks];
+            i64 kx = A1(xlindx, ks + 1) - klen;
+            i64 kl = A1(xlnz, fk + 1) - klen;
+            i64 nups;
+            if (klen == jlen) {
+                x_gemm_nt(jlen, nj, nk, -1.0, &L[kl], kslen, &L[kl], kslen, 1.0, &L[jl], jlen);
+                nups = nj;
+                if (klen > nj) nxt = A1(lindx, jx + nj);
+            } else {
+                nups = klen;
+                for (i64 i = 0; i <= klen - 1; ++i) {
+                    nxt = A1(lindx, kx + i);
+                    if (nxt > lj) { nups = i; break; }
+                }
+                for (i64 j = 1; j <= klen; ++j) relind[j] = map[A1(lindx, kx + j - 1)];
+                x_gemm_nt(klen, nups, nk, -1.0, &L[kl], kslen, &L[kl], kslen, 0.0, temp, klen);
+                for (i64 j = 1; j <= nups; ++j) {   /* _assmb! into the columns of L */
+                    i64 lbot = A1(xlnz, fj + jlen - relind[j]) - 1;
+                    for (i64 k = j; k <= klen; ++k) L[lbot - relind[k]] += temp[(j - 1) * klen + k - 1];
+                }
+            }
+            (void)nk;
+            if (klen > nups) {
+                i64 ns = A1(snode, nxt);
+                link[ks] = link[ns];
+                link[ns] = ks;
+                lngth[ks] = klen - nups;
+            } else {
+                lngth[ks] = 0;
+            }
+        }
+        /* POTRF of the diagonal block (lower), then L21 := A21 L11^-T */
+        for (i64 k = 0; k < nj; ++k) {
+            double* ck = &L[jl + k * jlen];
+            for (i64 p = 0; p < k; ++p) {
+                const double* cp = &L[jl + p * jlen];
+                for (i64 i = k; i < jlen; ++i) ck[i] -= cp[i] * cp[k];
+            }
+            if (!(ck[k] > 0.0)) {
+                if (bad == 0) bad = fj + k;
+                ck[k] = 1.0;
+            }
+            double d = sqrt(ck[k]);
+            ck[k] = d;
+            for (i64 i = k + 1; i < jlen; ++i) ck[i] /= d;
+        }
+        if (jlen > nj) {
+            nxt = A1(lindx, jx + nj);
+            i64 ns = A1(snode, nxt);
+            link[js] = link[ns];
+            link[ns] = js;
+            lngth[js] = jlen - nj;
+        } else {
+            lngth[js] = 0;
+        }
+    }
+    free(link);
+    free(lngth);
+    free(map);
+    free(relind);
+    free(temp);
+    return bad;
+}
+
 /* ---- _lulsolve! / _luusolve! ---------------------------------------------- */
 
 void oracle_lulsolve(i64 nsuper, const i64* xsuper, const i64* xlindx, const i64* lindx, const i64* xlnz,

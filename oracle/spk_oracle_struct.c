@@ -19,12 +19,13 @@
  *   _symbolicfact!       src/SparseSpdMethod/SpkSymFct.jl:105-246
  * in the order _symbolicfactor! calls them (SpkSparseBase.jl:193-251).
  *
- * The geometric nested dissection of a box grid is not reference code: it is
- * the ordering plug-in the package passes through findorder!'s
- * orderfunction slot (SpkSparseBase.jl:173-181), restated here (boxes split
- * through the middle of the longest side, halves first, separator plane
- * last, leaf boxes ordered by this file's minimum degree) so that the oracle
- * reproduces the ordering without the product library.
+ * The two nested-dissection orderings are not reference code: they are the
+ * ordering plug-ins the package passes through findorder!'s orderfunction
+ * slot (SpkSparseBase.jl:173-181), restated here (the geometric one of a box
+ * grid: boxes split through the middle of the longest side, halves first,
+ * separator plane last; the general one: level-structure separators), with
+ * leaf sets ordered by this file's minimum degree, so that the oracle
+ * reproduces the orderings without the product library.
  *
  * All index arrays are int64 and 1-based (the reference's convention); a
  * pointer argument addresses element 1.
@@ -433,6 +434,200 @@ i64 oracle_nd_grid(i64 nx, i64 ny, i64 nz, i64 leaf, const i64* xadj, const i64*
     d.local = (i64*)calloc((size_t)n + 2, sizeof(i64));
     nd_dissect(&d, 0, nx, 0, ny, 0, nz);
     free(d.local);
+    if (d.count != n) return d.count;
+    for (i64 t = 0; t < n; ++t) invp[perm[t] - 1] = t + 1;
+    return n;
+}
+
+/* ---- nested dissection of a general graph (ordering plug-in) -------------- */
+
+/* The package's level-structure nested dissection restated: a connected set
+ * larger than `leaf` is split at the middle level of a breadth-first level
+ * structure from a pseudo-peripheral vertex (restart from a least-degree
+ * vertex of the last level while the eccentricity grows, at most 8 times),
+ * the middle level trimmed of vertices without a neighbour in the next level
+ * (they join the first part); parts first, recursively, separator last;
+ * small or shallow sets by minimum degree; disconnected sets component by
+ * component. */
+typedef struct {
+    i64 n, leaf;
+    const i64 *xadj, *adj;   /* 1-based arrays, pointers address element 1 */
+    i64 *order, count;
+    i64 *stamp_of, *level, *local;
+    i64 stamp;
+} Gnd;
+
+typedef struct {
+    i64* v;
+    i64 n, cap;
+} Vec;
+
+static void vpush(Vec* a, i64 x) {
+    if (a->n == a->cap) {
+        a->cap = a->cap ? 2 * a->cap : 16;
+        a->v = (i64*)realloc(a->v, sizeof(i64) * (size_t)a->cap);
+    }
+    a->v[a->n++] = x;
+}
+
+static void gnd_bfs(Gnd* d, i64 root, i64 st, Vec* seen) {
+    seen->n = 0;
+    vpush(seen, root);
+    d->level[root] = 0;
+    d->stamp_of[root] = st + 1;
+    for (i64 h = 0; h < seen->n; ++h) {
+        i64 v = seen->v[h];
+        for (i64 e = d->xadj[v - 1]; e < d->xadj[v]; ++e) {
+            i64 w = d->adj[e - 1];
+            if (d->stamp_of[w] == st) {
+                d->stamp_of[w] = st + 1;
+                d->level[w] = d->level[v] + 1;
+                vpush(seen, w);
+            }
+        }
+    }
+    for (i64 h = 0; h < seen->n; ++h) d->stamp_of[seen->v[h]] = st;
+}
+
+static i64 gnd_deg(const Gnd* d, i64 v, i64 st) {
+    i64 k = 0;
+    for (i64 e = d->xadj[v - 1]; e < d->xadj[v]; ++e) k += d->stamp_of[d->adj[e - 1]] == st;
+    return k;
+}
+
+static void gnd_leaf(Gnd* d, const i64* verts, i64 m) {
+    if (m == 0) return;
+    for (i64 t = 0; t < m; ++t) d->local[verts[t]] = t + 1;
+    i64 cap = 0;
+    for (i64 t = 0; t < m; ++t) cap += d->xadj[verts[t]] - d->xadj[verts[t] - 1];
+    i64* sx = (i64*)malloc(sizeof(i64) * (size_t)(m + 1));
+    i64* sa = (i64*)malloc(sizeof(i64) * (size_t)(cap > 0 ? cap : 1));
+    i64 ne = 0;
+    sx[0] = 1;
+    for (i64 t = 0; t < m; ++t) {
+        i64 v = verts[t];
+        for (i64 e = d->xadj[v - 1]; e < d->xadj[v]; ++e) {
+            i64 w = d->adj[e - 1];
+            if (d->local[w] > 0) sa[ne++] = d->local[w];
+        }
+        sx[t + 1] = ne + 1;
+    }
+    i64* p = (i64*)malloc(sizeof(i64) * (size_t)m);
+    i64* q = (i64*)malloc(sizeof(i64) * (size_t)m);
+    oracle_mmd(m, sx, sa, p, q);
+    for (i64 t = 0; t < m; ++t) d->order[d->count++] = verts[p[t] - 1];
+    for (i64 t = 0; t < m; ++t) d->local[verts[t]] = 0;
+    free(sx); free(sa); free(p); free(q);
+}
+
+static void gnd_dissect(Gnd* d, const i64* verts, i64 nv) {
+    if (nv <= d->leaf) {
+        gnd_leaf(d, verts, nv);
+        return;
+    }
+    d->stamp += 2;
+    const i64 st = d->stamp;
+    for (i64 t = 0; t < nv; ++t) d->stamp_of[verts[t]] = st;
+    Vec seen = {0, 0, 0};
+    gnd_bfs(d, verts[0], st, &seen);
+    if (seen.n < nv) {   /* components, each on its own */
+        Vec all = {0, 0, 0}, starts = {0, 0, 0};
+        Vec c = {0, 0, 0};
+        for (i64 t = 0; t < nv; ++t) {
+            i64 v = verts[t];
+            if (d->stamp_of[v] != st) continue;
+            gnd_bfs(d, v, st, &c);
+            vpush(&starts, all.n);
+            for (i64 h = 0; h < c.n; ++h) {
+                d->stamp_of[c.v[h]] = st - 1;
+                vpush(&all, c.v[h]);
+            }
+        }
+        vpush(&starts, all.n);
+        for (i64 k = 0; k + 1 < starts.n; ++k) gnd_dissect(d, all.v + starts.v[k], starts.v[k + 1] - starts.v[k]);
+        free(all.v); free(starts.v); free(c.v); free(seen.v);
+        return;
+    }
+    i64 root = verts[0], best = -1;
+    for (i64 t = 0; t < nv; ++t) {
+        i64 dg = gnd_deg(d, verts[t], st);
+        if (best < 0 || dg < best) { best = dg; root = verts[t]; }
+    }
+    gnd_bfs(d, root, st, &seen);
+    i64 ecc = d->level[seen.v[seen.n - 1]];
+    Vec s2 = {0, 0, 0};
+    for (int it = 0; it < 8; ++it) {
+        i64 cand = seen.v[seen.n - 1], cd = -1;
+        for (i64 t = seen.n; t-- > 0 && d->level[seen.v[t]] == ecc;) {
+            i64 dg = gnd_deg(d, seen.v[t], st);
+            if (cd < 0 || dg < cd) { cd = dg; cand = seen.v[t]; }
+        }
+        gnd_bfs(d, cand, st, &s2);
+        if (d->level[s2.v[s2.n - 1]] <= ecc) {
+            gnd_bfs(d, root, st, &seen);
+            break;
+        }
+        root = cand;
+        Vec tmp = seen; seen = s2; s2 = tmp;
+        ecc = d->level[seen.v[seen.n - 1]];
+    }
+    free(s2.v);
+    if (ecc < 2) {
+        gnd_leaf(d, verts, nv);
+        free(seen.v);
+        return;
+    }
+    i64* count = (i64*)calloc((size_t)ecc + 1, sizeof(i64));
+    for (i64 h = 0; h < seen.n; ++h) ++count[d->level[seen.v[h]]];
+    i64 mid = 1, acc = 0;
+    for (i64 l = 0; l <= ecc; ++l) {
+        acc += count[l];
+        if (2 * acc >= nv) {
+            mid = l < 1 ? 1 : l;
+            if (mid > ecc - 1) mid = ecc - 1;
+            break;
+        }
+    }
+    free(count);
+    Vec A = {0, 0, 0}, B = {0, 0, 0}, S = {0, 0, 0};
+    for (i64 h = 0; h < seen.n; ++h) {
+        i64 v = seen.v[h], l = d->level[v];
+        if (l < mid) vpush(&A, v);
+        else if (l > mid) vpush(&B, v);
+        else {
+            int next = 0;
+            for (i64 e = d->xadj[v - 1]; e < d->xadj[v] && !next; ++e) {
+                i64 w = d->adj[e - 1];
+                next = d->stamp_of[w] == st && d->level[w] == mid + 1;
+            }
+            vpush(next ? &S : &A, v);
+        }
+    }
+    free(seen.v);
+    gnd_dissect(d, A.v, A.n);
+    gnd_dissect(d, B.v, B.n);
+    for (i64 h = 0; h < S.n; ++h) d->order[d->count++] = S.v[h];
+    free(A.v); free(B.v); free(S.v);
+}
+
+/* Returns the number of vertices ordered (n on success). */
+i64 oracle_nd_graph(i64 n, const i64* xadj, const i64* adj, i64 leaf, i64* perm, i64* invp) {
+    Gnd d;
+    d.n = n;
+    d.leaf = leaf > 1 ? leaf : 1;
+    d.xadj = xadj;
+    d.adj = adj;
+    d.order = perm;
+    d.count = 0;
+    d.stamp = 0;
+    d.stamp_of = (i64*)calloc((size_t)n + 2, sizeof(i64));
+    d.level = (i64*)calloc((size_t)n + 2, sizeof(i64));
+    d.local = (i64*)calloc((size_t)n + 2, sizeof(i64));
+    i64* all = (i64*)malloc(sizeof(i64) * (size_t)(n > 0 ? n : 1));
+    for (i64 v = 0; v < n; ++v) all[v] = v + 1;
+    if (n > 0) gnd_dissect(&d, all, n);
+    free(all);
+    free(d.stamp_of); free(d.level); free(d.local);
     if (d.count != n) return d.count;
     for (i64 t = 0; t < n; ++t) invp[perm[t] - 1] = t + 1;
     return n;

@@ -77,6 +77,7 @@ constexpr int TC_SCHUR_M = 96, TC_TRAIL_ROWS = 128;
 // Block partition and schedule for one precision (block width BlockMax<T>).
 struct Plan {
     bool built = false;
+    bool sym = false;                     // the symmetric (SPD) form's tiles
     int bmax = 0, bwmax = 1;
     std::vector<int> blk_c0, blk_c1, blk_p0, blk_np;
     std::vector<ll> blk_inv2;
@@ -131,7 +132,7 @@ struct spk_handle {
     std::vector<int> runid, run_tgt, run_start;
     std::vector<ll> run_rel;
     std::vector<int> rel;
-    Plan plan[2];                   // [0] FP64, [1] FP32
+    Plan plan[4];                   // [0] FP64, [1] FP32, [2] FP64 SPD form, [3] FP32 SPD form
     int nlevels = 0;
     i64 fsize = 0;
     int wmax = 1;             // widest supernode
@@ -157,10 +158,12 @@ struct spk_handle {
     int *d_ccolptr = nullptr, *d_crow = nullptr, *d_ccol = nullptr;   // A's pattern in CSC order (0-based)
     int *d_rperm = nullptr, *d_rinvp = nullptr;
 
-    Storage<double> s64;
-    Storage<float> s32;
-    Storage<float> s16;   // SPK_BF16S: float factor, BF16 packed panels
+    // factor storage per precision, [0] LU form, [1] SPD (symmetric) form
+    Storage<double> s64[2];
+    Storage<float> s32[2];
+    Storage<float> s16[2];   // SPK_BF16S: float factor, BF16 packed panels
     int fmode = 0;        // which float form the float paths use: 0 SPK_FP32, 1 SPK_BF16S
+    int sym = 0;          // which factorisation the paths use: 0 LU, 1 SPD form (SPK_SPD)
 
     // solve work space (sized for MAXRHS right-hand sides)
     void *d_wb = nullptr, *d_wy = nullptr, *d_wx = nullptr;   // factor precision
@@ -198,10 +201,10 @@ struct spk_handle {
 
     // captured sequences: factor per precision, solve per precision x right-hand sides
     bool use_graphs = true;
-    // [0] FP64, [1] FP32, [2] BF16S
-    GraphRec g_factor[3];
-    GraphRec g_solve[3][spk::MAXRHS + 1];
-    GraphRec g_tsolve[3][spk::MAXRHS + 1];   // transposed solves
+    // [0] FP64, [1] FP32, [2] BF16S; + 3 for the SPD form
+    GraphRec g_factor[6];
+    GraphRec g_solve[6][spk::MAXRHS + 1];
+    GraphRec g_tsolve[6][spk::MAXRHS + 1];   // transposed solves
 };
 
 // ---------------------------------------------------------------------------
@@ -241,9 +244,14 @@ static spk::Launch launch_of(const Plan& P, const LaunchRec& r) {
 template <typename T>
 static constexpr int prec_index() { return std::is_same<T, float>::value ? 1 : 0; }
 
-// Slot of the captured graphs: FP64, FP32 or BF16S (the float form selected).
+// Slot of the captured graphs: FP64, FP32 or BF16S (the float form
+// selected), LU or SPD form.
 template <typename T>
-static int graph_index(const spk_handle* h) { return std::is_same<T, float>::value ? 1 + h->fmode : 0; }
+static int graph_index(const spk_handle* h) { return (std::is_same<T, float>::value ? 1 + h->fmode : 0) + 3 * h->sym; }
+
+// Plan of the selected form: block partition of precision T, LU or SPD tiles.
+template <typename T>
+static int plan_index(const spk_handle* h) { return prec_index<T>() + 2 * h->sym; }
 
 static cudaEvent_t take_event(spk_handle* h) {
     if (!h->event_pool.empty()) {
@@ -300,7 +308,7 @@ static void drop_graph(GraphRec& g) {
 }
 
 static void drop_solve_graphs(spk_handle* h) {
-    for (int p = 0; p < 3; ++p)
+    for (int p = 0; p < 6; ++p)
         for (int r = 0; r <= spk::MAXRHS; ++r) {
             drop_graph(h->g_solve[p][r]);
             drop_graph(h->g_tsolve[p][r]);
@@ -550,10 +558,11 @@ static int panel_lines(bool fp32, bool wide) { return fp32 && wide ? spk::PT_LIN
 
 // Group each front's pieces into blocks of at most `bmax` columns and lay
 // out the launches of every level.
-static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
+static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc, bool sym) {
     using spk::cdiv;
     P = Plan();
     P.bmax = bmax;
+    P.sym = sym;
     const int nfr = (int)h->fronts.size();
     P.block0.resize(nfr);
     P.nblocks.resize(nfr);
@@ -685,7 +694,8 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
                 leafF[k] = P.nblocks[ids[k]] == 1 && F.nf <= 32 && F.m <= spk::LF_M;
                 tlf[k] = leafF[k] ? 1 : 0;
                 const double nf = F.nf, m = F.m;
-                flf[k] = 2.0 * nf * nf * nf + 3.0 * nf * nf * m + 2.0 * m * m * nf;
+                flf[k] = sym ? 2.0 * nf * nf * nf + nf * nf * m + m * (m + 1.0) * nf
+                             : 2.0 * nf * nf * nf + 3.0 * nf * nf * m + 2.0 * m * m * nf;
                 wlf[k] = nf * nf + 2.0 * nf * m + m * m;
             }
             add_launch(&P, L.leaf_factor, ids, tlf, flf, wlf);
@@ -709,20 +719,25 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
                 fl[k] = 2.0 * bw * bw * bw;
                 wl[k] = 4.0 * bw * bw;
                 const int lpt = panel_lines(tc, wide[t]);
-                tp[k] = leafF[k] ? 0 : cdiv(ld - c1, lpt) + cdiv(F.nf - c1, lpt) + cdiv(F.m, lpt);
+                // the SPD form launches the L-panel tiles only (they also write the U side)
+                tp[k] = leafF[k] ? 0 : cdiv(ld - c1, lpt) + (sym ? 0 : cdiv(F.nf - c1, lpt) + cdiv(F.m, lpt));
                 const double rowsL = ld - c1, colsU = (double)(F.nf - c1) + F.m;
-                fp[k] = bw * bw * rowsL + 2.0 * bw * bw * colsU;
+                fp[k] = bw * bw * rowsL + (sym ? 0.0 : 2.0 * bw * bw * colsU);
                 wp[k] = 2.0 * bw * (rowsL + colsU) + 2.0 * bw * bw;
-                tt[k] = cdiv(ld - c1, spk::TT) * cdiv(F.nf - c1, spk::TT) + cdiv(F.nf - c1, spk::TT) * cdiv(F.m, spk::TT);
+                tt[k] = sym ? spk::lower_tiles(cdiv(ld - c1, spk::TT), cdiv(F.nf - c1, spk::TT))
+                            : cdiv(ld - c1, spk::TT) * cdiv(F.nf - c1, spk::TT) + cdiv(F.nf - c1, spk::TT) * cdiv(F.m, spk::TT);
                 ttc[k] = ttc0[k] = 0;
                 if (P.blk_lpack[blk] >= 0) {   // packed front: 128-tiles, row / column regions split at nf
                     const int n1 = cdiv(F.nf - c1, spk::umma::TM), n2 = cdiv(F.m, spk::umma::TM);
-                    const int all = (n1 + n2) * n1 + n1 * n2;
+                    const int all = sym ? spk::lower_tiles(n1 + n2, n1) : (n1 + n2) * n1 + n1 * n2;
                     ttc0[k] = all > 0 ? 1 : 0;
                     ttc[k] = all - ttc0[k];
                     tt[k] = 0;
                 }
-                const double area = (double)(ld - c1) * (F.nf - c1) + (double)(F.nf - c1) * F.m;
+                // SPD form: only the lower part of the front columns (and none of U12)
+                const double nfc = F.nf - c1;
+                const double area = sym ? nfc * (ld - c1) - 0.5 * nfc * (nfc - 1.0)
+                                        : (double)(ld - c1) * (F.nf - c1) + (double)(F.nf - c1) * F.m;
                 ft[k] = 2.0 * bw * area;
                 wt[k] = 2.0 * area + bw * (rowsL + colsU);
                 tf[k] = std::max(1, cdiv(ld - c1, spk::TS)) * cdiv(c1 - c0, spk::SC);
@@ -768,14 +783,16 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc) {
         std::vector<double> fs(nid), ws(nid), fu(nid), wu(nid);
         for (size_t k = 0; k < nid; ++k) {
             const HFront& F = h->fronts[ids[k]];
-            tsch[k] = F.m > 0 && !leafF[k] ? cdiv(F.m, spk::TT) * cdiv(F.m, spk::TT) : 0;
+            const int nts = cdiv(F.m, spk::TT), ntc = cdiv(F.m, spk::umma::TM);
+            tsch[k] = F.m > 0 && !leafF[k] ? (sym ? spk::lower_tiles(nts, nts) : nts * nts) : 0;
             tsch_tc[k] = 0;
             if (F.m > 0 && P.blk_lpack[P.block0[ids[k]]] >= 0) {
-                tsch_tc[k] = cdiv(F.m, spk::umma::TM) * cdiv(F.m, spk::umma::TN);
+                tsch_tc[k] = sym ? spk::lower_tiles(ntc, ntc) : ntc * ntc;
                 tsch[k] = 0;
             }
             tbu[k] = F.m > 0 ? cdiv(F.nf, spk::U12_ROWS) * cdiv(F.m, spk::U12_COLS) : 0;
-            fs[k] = 2.0 * (double)F.m * F.m * F.nf;
+            // SPD form: the lower part with the diagonal, m (m + 1) / 2 entries
+            fs[k] = (sym ? (double)F.m * (F.m + 1.0) : 2.0 * (double)F.m * F.m) * F.nf;
             ws[k] = 2.0 * (double)F.m * F.nf + 2.0 * (double)F.m * F.m;
             fu[k] = 2.0 * (double)F.m * F.nf;
             wu[k] = (double)F.m * F.nf;
@@ -821,10 +838,10 @@ static size_t panel_smem() {
 
 template <typename T>
 static int ensure_plan(spk_handle* h) {
-    Plan& P = h->plan[prec_index<T>()];
+    Plan& P = h->plan[plan_index<T>(h)];
     if (P.built) return SPK_OK;
     try {
-        build_plan(h, P, spk::BlockMax<T>::value, std::is_same<T, float>::value);
+        build_plan(h, P, spk::BlockMax<T>::value, std::is_same<T, float>::value, h->sym != 0);
     } catch (const std::bad_alloc&) {
         return set_err(h, SPK_ENOMEM, "host allocation failed while planning");
     }
@@ -876,6 +893,7 @@ static int ensure_plan(spk_handle* h) {
     S.blk_inv2 = P.d_blk_inv2;
     S.blk_lpack = P.d_blk_lpack;
     S.blk_upack = P.d_blk_upack;
+    S.sym = P.sym ? 1 : 0;
     constexpr int BM = spk::BlockMax<T>::value;
     CU(h, cudaFuncSetAttribute(spk::k_block_panel<T, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)panel_smem<T, BM>()));
@@ -939,9 +957,9 @@ static void free_plan(Plan& P) {
 template <typename T>
 static Storage<T>& storage(spk_handle* h);
 template <>
-Storage<double>& storage<double>(spk_handle* h) { return h->s64; }
+Storage<double>& storage<double>(spk_handle* h) { return h->s64[h->sym]; }
 template <>
-Storage<float>& storage<float>(spk_handle* h) { return h->fmode ? h->s16 : h->s32; }
+Storage<float>& storage<float>(spk_handle* h) { return h->fmode ? h->s16[h->sym] : h->s32[h->sym]; }
 
 template <typename T>
 static int ensure_storage(spk_handle* h) {
@@ -949,9 +967,9 @@ static int ensure_storage(spk_handle* h) {
     if (rc) return rc;
     Storage<T>& S = storage<T>(h);
     if (!S.d) CU(h, cudaMalloc((void**)&S.d, sizeof(T) * std::max<i64>(h->fsize, 1)));
-    if (!S.inv2) CU(h, cudaMalloc((void**)&S.inv2, sizeof(T) * std::max<ll>(h->plan[prec_index<T>()].inv2_size, 1)));
+    if (!S.inv2) CU(h, cudaMalloc((void**)&S.inv2, sizeof(T) * std::max<ll>(h->plan[plan_index<T>(h)].inv2_size, 1)));
     // BF16 packs take a quarter of the TF32 hi + lo bytes (same tiles and chunks)
-    const ll pack_bytes = h->plan[prec_index<T>()].pack_size / (std::is_same<T, float>::value && h->fmode ? 4 : 1);
+    const ll pack_bytes = h->plan[plan_index<T>(h)].pack_size / (std::is_same<T, float>::value && h->fmode ? 4 : 1);
     if (!S.pack && pack_bytes > 0) CU(h, cudaMalloc((void**)&S.pack, (size_t)pack_bytes));
     return SPK_OK;
 }
@@ -1007,7 +1025,7 @@ template <typename T>
 static int factor_launches(spk_handle* h) {
     constexpr int BM = spk::BlockMax<T>::value;
     T* fac = storage<T>(h).d;
-    const Plan& PL = h->plan[prec_index<T>()];
+    const Plan& PL = h->plan[plan_index<T>(h)];
     const spk::Sched& S = PL.sched;
     // Look ahead (not while timing kernels one by one): see spk_handle::side.
     const bool ahead = h->prof_mask == 0;
@@ -1154,7 +1172,7 @@ template <typename T>
 static int run_solve_permuted(spk_handle* h, int nrhs, bool transpose) {
     const T* fac = storage<T>(h).d;
     const T* inv = storage<T>(h).inv2;
-    const Plan& PL = h->plan[prec_index<T>()];
+    const Plan& PL = h->plan[plan_index<T>(h)];
     const spk::Sched& S = PL.sched;
     T* b = (T*)h->d_wb;
     T* y = (T*)h->d_wy;
@@ -1442,13 +1460,23 @@ static int check_h(spk_handle* h) {
     return SPK_OK;
 }
 
-static bool valid_precision(int p) { return p == SPK_FP64 || p == SPK_FP32 || p == SPK_BF16S; }
+// A precision code: SPK_FP64, SPK_FP32 or SPK_BF16S, optionally | SPK_SPD.
+static int base_precision(int p) { return p & ~SPK_SPD; }
+static bool valid_precision(int p) {
+    const int b = base_precision(p);
+    return b == SPK_FP64 || b == SPK_FP32 || b == SPK_BF16S;
+}
+static bool is_fp64(int p) { return base_precision(p) == SPK_FP64; }
 
 // Point the float paths at the storage of the given float form.
-static void select_form(spk_handle* h, int precision) { h->fmode = precision == SPK_BF16S ? 1 : 0; }
+static void select_form(spk_handle* h, int precision) {
+    h->fmode = base_precision(precision) == SPK_BF16S ? 1 : 0;
+    h->sym = (precision & SPK_SPD) ? 1 : 0;
+}
 
 static Storage<float>& float_storage(spk_handle* h, int precision) {
-    return precision == SPK_BF16S ? h->s16 : h->s32;
+    const int y = (precision & SPK_SPD) ? 1 : 0;
+    return base_precision(precision) == SPK_BF16S ? h->s16[y] : h->s32[y];
 }
 
 template <typename T>
@@ -1478,7 +1506,7 @@ static int fetch_factor(spk_handle* h, std::vector<double>& out) {
 }
 
 static bool factored(spk_handle* h, int precision) {
-    return precision == SPK_FP64 ? h->s64.factored : float_storage(h, precision).factored;
+    return is_fp64(precision) ? h->s64[(precision & SPK_SPD) ? 1 : 0].factored : float_storage(h, precision).factored;
 }
 
 // Does (i, j) (permuted, 0-based) belong to the reference's structure?  L
@@ -1652,9 +1680,11 @@ int spk_set_pattern(spk_handle* h, int64_t ncols, const int64_t* colptr, const i
     h->nnz = nnz;
     h->have_pattern = true;
     h->have_values = false;
-    h->s64.loaded = h->s64.factored = false;
-    h->s32.loaded = h->s32.factored = false;
-    h->s16.loaded = h->s16.factored = false;
+    for (int y = 0; y < 2; ++y) {
+        h->s64[y].loaded = h->s64[y].factored = false;
+        h->s32[y].loaded = h->s32[y].factored = false;
+        h->s16[y].loaded = h->s16[y].factored = false;
+    }
     return SPK_OK;
 }
 
@@ -1670,11 +1700,13 @@ int spk_load_values(spk_handle* h, const double* nzval, int where, int precision
                               where == SPK_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, h->stream));
     h->have_values = true;
     // a new A invalidates every factor
-    h->s64.loaded = h->s64.factored = false;
-    h->s32.loaded = h->s32.factored = false;
-    h->s16.loaded = h->s16.factored = false;
+    for (int y = 0; y < 2; ++y) {
+        h->s64[y].loaded = h->s64[y].factored = false;
+        h->s32[y].loaded = h->s32[y].factored = false;
+        h->s16[y].loaded = h->s16[y].factored = false;
+    }
     select_form(h, precision);
-    rc = precision == SPK_FP64 ? load_into<double>(h) : load_into<float>(h);
+    rc = is_fp64(precision) ? load_into<double>(h) : load_into<float>(h);
     if (rc) return rc;
     if (where == SPK_HOST) CU(h, cudaStreamSynchronize(h->stream));
     return SPK_OK;
@@ -1687,8 +1719,8 @@ int spk_factor(spk_handle* h, int precision, int64_t* first_singular) {
     if (!valid_precision(precision)) return set_err(h, SPK_EARG, "spk_factor: bad precision");
     if (!h->have_values) return set_err(h, SPK_ESEQ, "Sequence error. Matrix input not done yet.");
     select_form(h, precision);
-    if (precision == SPK_FP64) {
-        if (!h->s64.loaded && (rc = load_into<double>(h))) return rc;
+    if (is_fp64(precision)) {
+        if (!storage<double>(h).loaded && (rc = load_into<double>(h))) return rc;
         if ((rc = run_factor<double>(h))) return rc;
     } else {
         if (!float_storage(h, precision).loaded && (rc = load_into<float>(h))) return rc;
@@ -1699,7 +1731,7 @@ int spk_factor(spk_handle* h, int precision, int64_t* first_singular) {
     CU(h, cudaStreamSynchronize(h->stream));
     const int info = info2[0];
     if (info2[1]) return set_err(h, SPK_ECUDA, "spk_factor: a tensor-core wait timed out");
-    if (precision == SPK_FP64) { h->s64.loaded = false; h->s64.factored = true; }
+    if (is_fp64(precision)) { storage<double>(h).loaded = false; storage<double>(h).factored = true; }
     else { float_storage(h, precision).loaded = false; float_storage(h, precision).factored = true; }
     if (info != INT_MAX) {
         if (first_singular) *first_singular = info;
@@ -1733,7 +1765,7 @@ static int solve_impl(spk_handle* h, double* b, int64_t nrhs, int64_t ldb, int w
         src = b;
         ld = ldb;
     }
-    rc = precision == SPK_FP64 ? solve_device<double>(h, src, ld, h->d_x, n, nrhs, 0, transpose)
+    rc = is_fp64(precision) ? solve_device<double>(h, src, ld, h->d_x, n, nrhs, 0, transpose)
                                : solve_device<float>(h, src, ld, h->d_x, n, nrhs, 0, transpose);
     if (rc) return rc;
     CU(h, cudaMemcpy2DAsync(b, sizeof(double) * ldb, h->d_x, sizeof(double) * n, sizeof(double) * n, nrhs,
@@ -1858,7 +1890,7 @@ static int refine_impl(spk_handle* h, const double* b, double* x, int64_t nrhs, 
         ldb = ldx = ld;
     }
     auto solve_into = [&](const double* rhs, i64 ldr, int acc) {
-        return precision == SPK_FP64 ? solve_device<double>(h, rhs, ldr, dx, ldx, nrhs, acc, transpose)
+        return is_fp64(precision) ? solve_device<double>(h, rhs, ldr, dx, ldx, nrhs, acc, transpose)
                                      : solve_device<float>(h, rhs, ldr, dx, ldx, nrhs, acc, transpose);
     };
     if ((rc = solve_into(db, ldb, 0))) return rc;
@@ -1898,7 +1930,7 @@ static int refine_impl(spk_handle* h, const double* b, double* x, int64_t nrhs, 
             const int nc = (int)std::min<i64>(spk::GM_MAXRHS, nrhs - c0);
             double r = 0.0;
             int used = 0, cycles = 0;
-            rc = precision == SPK_FP64
+            rc = is_fp64(precision)
                      ? gmres_ir<double>(h, db + c0 * ldb, ldb, dx + c0 * ldx, ldx, nc, tol, max_iter - it, &r, &used, &cycles)
                      : gmres_ir<float>(h, db + c0 * ldb, ldb, dx + c0 * ldx, ldx, nc, tol, max_iter - it, &r, &used, &cycles);
             if (rc) return rc;
@@ -1980,16 +2012,35 @@ int spk_get_factors(spk_handle* h, int precision, double* lnz, double* unz, int6
     if (rc) return rc;
     if (!valid_precision(precision)) return set_err(h, SPK_EARG, "spk_get_factors: bad precision");
     const bool done = factored(h, precision);
-    const bool loaded = precision == SPK_FP64 ? h->s64.loaded : float_storage(h, precision).loaded;
+    const bool loaded = is_fp64(precision) ? h->s64[(precision & SPK_SPD) ? 1 : 0].loaded : float_storage(h, precision).loaded;
     select_form(h, precision);
     if (!done && !loaded) return set_err(h, SPK_ESEQ, "Sequence error. Matrix input not done yet.");
     std::vector<double> fac;
-    rc = precision == SPK_FP64 ? fetch_factor<double>(h, fac) : fetch_factor<float>(h, fac);
+    rc = is_fp64(precision) ? fetch_factor<double>(h, fac) : fetch_factor<float>(h, fac);
     if (rc) return rc;
+    // SPD form: the stored factor is the unit lower L and U = D L^T; the
+    // Cholesky factor is C = L D^1/2 (A = C C^T), returned in both layouts
+    // (lnz: C in the lower part of each supernode, C^T above the diagonal;
+    // unz: the rows of C^T right of the diagonal block)
+    const bool chol = (precision & SPK_SPD) && done;
+    std::vector<double> sq;
     for (const HFront& F : h->fronts) {
         const int ld = F.nf + F.m;
         const int* R = h->rows.data() + F.rows_off;
         std::vector<int> pos;
+        if (chol) {
+            sq.resize(F.nf);
+            for (int x = 0; x < F.nf; ++x) {
+                const double d = fac[F.loff + (i64)x * ld + x];
+                if (!(d > 0.0)) {
+                    char buf[160];
+                    std::snprintf(buf, sizeof buf, "not positive definite: pivot %.3e at column %lld", d,
+                                  (long long)(F.f + x + 1));
+                    return set_err(h, SPK_ESINGULAR, buf);
+                }
+                sq[x] = std::sqrt(d);
+            }
+        }
         for (int s = F.piece0; s < F.piece0 + F.npieces; ++s) {
             const int p0 = h->xs[s] - (int)F.f, w = h->xs[s + 1] - h->xs[s];
             const i64 a = h->xlindx0[s], jlen = h->xlindx0[s + 1] - a;
@@ -2002,13 +2053,19 @@ int spk_get_factors(spk_handle* h, int precision, double* lnz, double* unz, int6
             }
             const i64 lbase = h->xlnz0[h->xs[s]], ubase = h->xunz0[h->xs[s]];
             for (int k = 0; k < w; ++k) {
+                const int col = p0 + k;
                 if (lnz)
-                    for (i64 t = 0; t < jlen; ++t) lnz[lbase + k * jlen + t] = fac[F.loff + (i64)(p0 + k) * ld + pos[t]];
+                    for (i64 t = 0; t < jlen; ++t) {
+                        double v = fac[F.loff + (i64)col * ld + pos[t]];
+                        if (chol) v = pos[t] > col ? v * sq[col] : pos[t] == col ? sq[col] : v / sq[pos[t]];
+                        lnz[lbase + k * jlen + t] = v;
+                    }
                 if (unz)
                     for (i64 i = 0; i < jlen - w; ++i) {
                         const int c = pos[w + i];
-                        unz[ubase + k * (jlen - w) + i] = c < F.nf ? fac[F.loff + (i64)c * ld + p0 + k]
-                                                                   : fac[F.uoff + (i64)(p0 + k) * F.m + (c - F.nf)];
+                        double v = c < F.nf ? fac[F.loff + (i64)c * ld + col] : fac[F.uoff + (i64)col * F.m + (c - F.nf)];
+                        if (chol) v /= sq[col];
+                        unz[ubase + k * (jlen - w) + i] = v;
                     }
             }
         }
@@ -2069,19 +2126,22 @@ void spk_destroy(spk_handle* h) {
     if (!h) return;
     if (h->device >= 0) cudaSetDevice(h->device);
     if (h->own) cudaStreamSynchronize(h->own);
-    free_plan(h->plan[0]);
-    free_plan(h->plan[1]);
+    for (Plan& P : h->plan) free_plan(P);
     void* ptrs[] = {h->d_xs, h->d_rows, h->d_runid, h->d_run_tgt, h->d_run_start, h->d_run_rel,
-                    h->d_rel, h->s64.inv2, h->s32.inv2, h->s16.inv2, h->s64.pack, h->s32.pack, h->s16.pack, h->d_ipiv, h->d_bmap, h->d_info, h->d_slot, h->d_aval,
-                    h->d_rowptr, h->d_col, h->d_src, h->d_ccolptr, h->d_crow, h->d_ccol, h->d_rperm, h->d_rinvp, h->s64.d, h->s32.d, h->s16.d, h->d_wb,
+                    h->d_rel, h->d_ipiv, h->d_bmap, h->d_info, h->d_slot, h->d_aval,
+                    h->d_rowptr, h->d_col, h->d_src, h->d_ccolptr, h->d_crow, h->d_ccol, h->d_rperm, h->d_rinvp, h->d_wb,
                     h->d_wy, h->d_wx, h->d_rhs, h->d_x, h->d_r, h->d_sums, h->gm_V, h->gm_Z, h->gm_w, h->gm_c};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    for (int y = 0; y < 2; ++y) {
+        void* st[] = {h->s64[y].d, h->s64[y].inv2, h->s64[y].pack, h->s32[y].d, h->s32[y].inv2, h->s32[y].pack,
+                      h->s16[y].d, h->s16[y].inv2, h->s16[y].pack};
+        for (void* p : st)
+            if (p) cudaFree(p);
+    }
     collect_events(h);
     for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
-    drop_graph(h->g_factor[0]);
-    drop_graph(h->g_factor[1]);
-    drop_graph(h->g_factor[2]);
+    for (GraphRec& g : h->g_factor) drop_graph(g);
     drop_solve_graphs(h);
     if (h->side) cudaStreamSynchronize(h->side);
     if (h->side2) cudaStreamSynchronize(h->side2);

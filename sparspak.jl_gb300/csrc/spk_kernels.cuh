@@ -74,6 +74,10 @@ struct Sched {
     const ll* blk_inv2;    // offset in inv2[] of the block's Minv (then Uinv), bw x bw each
     const ll* blk_lpack;   // byte offset of the block's packed L panel (FP32 tensor-core fronts), -1 if none
     const ll* blk_upack;   // byte offset of the block's packed U panel, -1 if none
+    // 1: the symmetric form for SPD matrices (POTRF-like: no interchanges;
+    // only the lower part of every update is formed, SYRK-like; the U side,
+    // U = D L^T, is written from the L panel; LU storage otherwise)
+    int sym;
 };
 
 // One launch = a list of fronts and the prefix sum of their tile counts.
@@ -176,7 +180,7 @@ __device__ __forceinline__ T pick32(const T (&r)[32], int k) {
 // rank-1 update of rows and columns after k (ggetrf!, the U-panel trsm
 // 'r','l','t','u' and the block-local update).  `nrows` rows take part.
 template <typename T>
-__device__ bool warp_lu_sweep(T (&r)[32], int nrows, int ncols, const int* q0, int* piv) {
+__device__ bool warp_lu_sweep(T (&r)[32], int nrows, int ncols, const int* q0, int* piv, bool sym) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     bool sing = false;
@@ -186,7 +190,7 @@ __device__ bool warp_lu_sweep(T (&r)[32], int nrows, int ncols, const int* q0, i
         while (q0[pc + 1] <= k) ++pc;
         const int a = q0[pc], b = q0[pc + 1];
         const T rk0 = pick32(r, k);
-        const int kp = warp_first_max(pivot_key(rk0, lane >= k && lane < b, lane == k));
+        const int kp = warp_first_max(pivot_key(rk0, sym ? lane == k : (lane >= k && lane < b), lane == k));
         if (lane == 0) piv[k] = kp - a;
         const T pv = __shfl_sync(FULL, rk0, kp);
         if (pv != T(0)) {
@@ -232,13 +236,13 @@ __device__ bool warp_lu_sweep(T (&r)[32], int nrows, int ncols, const int* q0, i
 // and columns after k (ggetrf!, the U-panel trsm 'r','l','t','u' and the
 // block-local update).  Columns left of the piece are never interchanged.
 template <typename T>
-__device__ bool warp_block_lu32(T* A, int lda, int bw, const int* q0, int np, int* piv) {
+__device__ bool warp_block_lu32(T* A, int lda, int bw, const int* q0, int np, int* piv, bool sym) {
     const int lane = threadIdx.x & 31;
     (void)np;
     T r[32];
 #pragma unroll
     for (int j = 0; j < 32; ++j) r[j] = (lane < bw && j < bw) ? A[j * lda + lane] : T(0);
-    const bool sing = warp_lu_sweep(r, bw, bw, q0, piv);
+    const bool sing = warp_lu_sweep(r, bw, bw, q0, piv, sym);
     if (lane < bw) {
 #pragma unroll
         for (int j = 0; j < 32; ++j)
@@ -266,10 +270,12 @@ __global__ void __launch_bounds__(128) k_block_lu_small(T* fac, int* ipiv, int* 
     int* q0 = sq[warp];
     int* piv = spiv[warp];
     for (int k = lane; k <= np; k += 32) q0[k] = S.xsuper[p0 + k] - F.f - c0;
-    for (int j = 0; j < bw; ++j)
-        if (lane < bw) A[j * lda + lane] = fac[F.loff + (ll)(c0 + j) * F.ld + c0 + lane];
+    for (int j = 0; j < bw; ++j)   // symmetric form: the upper triangle mirrors the lower one
+        if (lane < bw)
+            A[j * lda + lane] = (S.sym && lane < j) ? fac[F.loff + (ll)(c0 + lane) * F.ld + c0 + j]
+                                                    : fac[F.loff + (ll)(c0 + j) * F.ld + c0 + lane];
     __syncwarp();
-    const bool sing = warp_block_lu32(A, lda, bw, q0, np, piv);
+    const bool sing = warp_block_lu32(A, lda, bw, q0, np, piv, S.sym != 0);
     for (int j = 0; j < bw; ++j)
         if (lane < bw) fac[F.loff + (ll)(c0 + j) * F.ld + c0 + lane] = A[j * lda + lane];
     if (lane < bw) ipiv[F.f + c0 + lane] = piv[lane];
@@ -380,7 +386,7 @@ __device__ __forceinline__ double lu_recip(double x) { return rcp_rn(x); }
 // first and end column of each column's piece.
 template <typename T, int RPT>
 __device__ __forceinline__ void lu_group_factor(T (&a)[RPT][4], int g, int bw, const int* cpa, const int* cpb, T* lb,
-                                                int* skp, T* spv, int* sa0, int* spiv, int* szero) {
+                                                int* skp, T* spv, int* sa0, int* spiv, int* szero, bool sym) {
     using Key = typename PivotKey<T>::type;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, r0 = RPT * lane;
@@ -394,7 +400,7 @@ __device__ __forceinline__ void lu_group_factor(T (&a)[RPT][4], int g, int bw, c
 #pragma unroll
         for (int ii = 0; ii < RPT; ++ii) {   // rows in ascending order: ties keep the earlier row
             const int R = r0 + ii;
-            const Key kv = PivotKey<T>::of(a[ii][j], R >= k && R < b, R == k);
+            const Key kv = PivotKey<T>::of(a[ii][j], sym ? R == k : (R >= k && R < b), R == k);
             if (ii == 0 || kv > best) { best = kv; brow = R; }
         }
         const int kp = warp_first_max_row(best, brow);
@@ -541,11 +547,13 @@ __global__ void __launch_bounds__(LuThreads<T>::value, 1) k_block_lu(T* fac, int
 #pragma unroll
         for (int ii = 0; ii < RPT; ++ii) {
             const int R = r0 + ii, C = cl0 + jj;
-            a[ii][jj] = (R < bw && C < bw) ? blkp[(ll)C * F.ld + R] : T(0);
+            // symmetric form: the upper triangle mirrors the lower one
+            a[ii][jj] = (R < bw && C < bw) ? ((S.sym && R < C) ? blkp[(ll)R * F.ld + C] : blkp[(ll)C * F.ld + R]) : T(0);
         }
     __syncthreads();
     const int ng = cdiv(bw, 4);
-    if (w == 0) lu_group_factor<T, RPT>(a, 0, bw, cpa, cpb, lbuf[0], s_kp[0], s_pv[0], s_a0[0], spiv, &szero);
+    const bool sym = S.sym != 0;
+    if (w == 0) lu_group_factor<T, RPT>(a, 0, bw, cpa, cpb, lbuf[0], s_kp[0], s_pv[0], s_a0[0], spiv, &szero, sym);
     __syncthreads();
 #pragma unroll 1
     for (int g = 0; g < ng; ++g) {
@@ -555,7 +563,7 @@ __global__ void __launch_bounds__(LuThreads<T>::value, 1) k_block_lu(T* fac, int
             lu_group_update<T, RPT>(a, g, bw, lbuf[par], s_kp[par], s_pv[par]);
             if (w == g + 1)   // the next panel while the other warps update
                 lu_group_factor<T, RPT>(a, g + 1, bw, cpa, cpb, lbuf[par ^ 1], s_kp[par ^ 1], s_pv[par ^ 1],
-                                        s_a0[par ^ 1], spiv, &szero);
+                                        s_a0[par ^ 1], spiv, &szero, sym);
         }
         __syncthreads();
     }
@@ -1039,7 +1047,7 @@ __device__ __forceinline__ void pack_tile16(unsigned char* base, const float* sX
 
 __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, const Sched& S, const DFront& F, int blk,
                                                int tile, unsigned char* pack, float* sT, float* sX, float* rd,
-                                               int* gmap, int* pa, int bf16, int* smax) {
+                                               int* gmap, int* pa, int bf16, int* smax, float* sd) {
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
     const int tid = threadIdx.x, c = tid & 15, line0 = (tid >> 4) * 4;
     const int nL = cdiv(F.ld - c1, PT_LINES), nUa = cdiv(F.nf - c1, PT_LINES);
@@ -1055,6 +1063,7 @@ __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, cons
             const bool v = li < nl && j < bw;
             cp_elem(&sX[li * PT_LD + j], v ? xb + (ll)j * F.ld + li : xb, v);
         }
+        if (S.sym && tid < bw) sd[tid] = blkp[(ll)tid * F.ld + tid];   // U(j, j) for the U side
         stage_upper<float, 128>(sT, rd, blkp, F.ld, bw);   // waits for all copies
         __syncthreads();
         float x[4][8];
@@ -1094,11 +1103,32 @@ __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, cons
             t = r < F.nf ? (r - c1) / umma::TM : n1 + (r - F.nf) / umma::TM;
             i = r < F.nf ? (r - c1) % umma::TM : (r - F.nf) % umma::TM;
         };
-        if (off >= 0 && bf16) {
-            const float scale = umma::exp2i(block_scale_exp(blkp, F.ld, bw, smax));
-            pack_tile16(pack + (off >> 2), sX, nl, nch, scale, whereL);
-        } else if (off >= 0) {
-            pack_tile(pack + off, sX, nl, nch, whereL);
+        const int e = (off >= 0 && bf16) ? block_scale_exp(blkp, F.ld, bw, smax) : 0;
+        if (off >= 0 && bf16) pack_tile16(pack + (off >> 2), sX, nl, nch, umma::exp2i(e), whereL);
+        else if (off >= 0) pack_tile(pack + off, sX, nl, nch, whereL);
+        if (S.sym) {   // the U side: U(c0 + j, r) = U(j, j) L(r, c0 + j), stored and packed
+            __syncthreads();   // the L pack has read the tile
+            for (int q = tid; q < PT_LINES * 128; q += PT_LINES * 4) {
+                int li, j;
+                tile_coords(q, true, li, j);
+                if (li < nl && j < bw) sX[li * PT_LD + j] *= sd[j];
+            }
+            __syncthreads();
+            for (int q = tid; q < PT_LINES * 128; q += PT_LINES * 4) {   // rows r < nf: column r of Lf
+                int li, j;
+                tile_coords(q, true, li, j);
+                const int r = rb0 + li;
+                if (li < nl && j < bw && r < F.nf) fac[F.loff + (ll)r * F.ld + c0 + j] = sX[li * PT_LD + j];
+            }
+            for (int q = tid; q < PT_LINES * 128; q += PT_LINES * 4) {   // rows r >= nf: U12 in Uf
+                int li, j;
+                tile_coords(q, false, li, j);
+                const int r = rb0 + li;
+                if (li < nl && j < bw && r >= F.nf) fac[F.uoff + (ll)(c0 + j) * F.m + (r - F.nf)] = sX[li * PT_LD + j];
+            }
+            const ll offu = S.blk_upack[blk];
+            if (offu >= 0 && bf16) pack_tile16(pack + (offu >> 2), sX, nl, nch, umma::exp2i(-e), whereL);
+            else if (offu >= 0) pack_tile(pack + offu, sX, nl, nch, whereL);
         }
     } else {
         if (tid < bw) {   // the block's row sources, from k_block_lu
@@ -1190,13 +1220,14 @@ __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, co
     __shared__ T rd[W];
     __shared__ int q0[W + 1], gmap[W], pa[W];
     __shared__ int smax;
+    __shared__ T sdg[W];   // symmetric form: U(j, j) of the block
     int fid, tile;
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
     const int blk = F.block0 + step;
     if constexpr (std::is_same<T, float>::value && W == 128) {
         block_panel128(fac, bmap, S, F, blk, tile, pack, sT, sT + 128 * SLD<float, 128>::value, rd, gmap, pa, bf16,
-                       &smax);
+                       &smax, sdg);
         return;
     }
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
@@ -1214,6 +1245,7 @@ __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, co
             const int j = q * CQ + jj;
             x[jj] = (ok && j < bw) ? xp[(ll)j * F.ld] : T(0);
         }
+        if (S.sym && tid < bw) sdg[tid] = blkp[(ll)tid * F.ld + tid];   // U(j, j) for the U side
         stage_upper<T, W>(sT, rd, blkp, F.ld, bw);
         __syncthreads();
         sweep_rows<T, W>(x, sT, rd, bw);
@@ -1222,15 +1254,30 @@ __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, co
             const int j = q * CQ + jj;
             if (ok && j < bw) xp[(ll)j * F.ld] = x[jj];
         }
+        T u[CQ];   // symmetric form: the U side, U(c0 + j, r) = U(j, j) L(r, c0 + j)
+#pragma unroll
+        for (int jj = 0; jj < CQ; ++jj) {
+            const int j = q * CQ + jj;
+            u[jj] = (S.sym && j < bw) ? x[jj] * sdg[j] : T(0);
+            if (S.sym && ok && j < bw) {
+                if (r < F.nf) fac[F.loff + (ll)r * F.ld + c0 + j] = u[jj];
+                else fac[F.uoff + (ll)(c0 + j) * F.m + (r - F.nf)] = u[jj];
+            }
+        }
         if constexpr (std::is_same<T, float>::value) {
             const ll off = S.blk_lpack[blk];
-            const float scale = (off >= 0 && bf16) ? umma::exp2i(block_scale_exp(blkp, F.ld, bw, &smax)) : 1.0f;
+            const int e = (off >= 0 && bf16) ? block_scale_exp(blkp, F.ld, bw, &smax) : 0;
             if (off >= 0 && ok) {
                 const int n1 = cdiv(F.nf - c1, umma::TM);
                 const int t = r < F.nf ? (r - c1) / umma::TM : n1 + (r - F.nf) / umma::TM;
                 const int i = r < F.nf ? (r - c1) % umma::TM : (r - F.nf) % umma::TM;
-                if (bf16) pack_line16<CQ>(pack + (off >> 2), t, i, q, cdiv(bw, umma::KCH), x, scale);
+                if (bf16) pack_line16<CQ>(pack + (off >> 2), t, i, q, cdiv(bw, umma::KCH), x, umma::exp2i(e));
                 else pack_line<CQ>(pack + off, t, i, q, cdiv(bw, umma::KCH), x);
+                const ll offu = S.blk_upack[blk];   // symmetric form: the U side's pack, same tiles
+                if (S.sym && offu >= 0) {
+                    if (bf16) pack_line16<CQ>(pack + (offu >> 2), t, i, q, cdiv(bw, umma::KCH), u, umma::exp2i(-e));
+                    else pack_line<CQ>(pack + offu, t, i, q, cdiv(bw, umma::KCH), u);
+                }
             }
         }
     } else {
@@ -1351,6 +1398,23 @@ __global__ void __launch_bounds__(256) k_block_inv(const T* fac, const int* ipiv
 constexpr int TT = 64;
 constexpr int KC = 32;
 
+// Symmetric form: the tiles (i, j) of an nr x nc tile grid with i >= j
+// (the lower part and the diagonal tiles), column by column: column j holds
+// nr - j tiles.  Tile number t -> (i, j).
+__host__ __device__ __forceinline__ void lower_tile(int t, int nr, int& i, int& j) {
+    j = 0;
+    while (t >= nr - j) {
+        t -= nr - j;
+        ++j;
+    }
+    i = j + t;
+}
+__host__ __device__ __forceinline__ int lower_tiles(int nr, int nc) {
+    int n = 0;
+    for (int j = 0; j < nc && j < nr; ++j) n += nr - j;
+    return n;
+}
+
 template <typename T, bool rows_fast>
 __device__ __forceinline__ void mma_tile(const T* sA, const T* sB, int kc, T acc[4][4]) {
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -1382,11 +1446,13 @@ __global__ void __launch_bounds__(256) k_block_trail(T* fac, Sched S, Launch L, 
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk];
     const int tid = threadIdx.x;
     const int nrL = cdiv(F.ld - c1, TT), ncL = cdiv(F.nf - c1, TT);
-    const bool isL = tile < nrL * ncL;
+    const bool isL = S.sym || tile < nrL * ncL;   // the symmetric form: lower L tiles only
     int r0, col0, nr, nc;
     if (isL) {
-        r0 = c1 + (tile % nrL) * TT;
-        col0 = c1 + (tile / nrL) * TT;
+        int ti = tile % nrL, tj = tile / nrL;
+        if (S.sym) lower_tile(tile, nrL, ti, tj);
+        r0 = c1 + ti * TT;
+        col0 = c1 + tj * TT;
         nr = min(TT, F.ld - r0);
         nc = min(TT, F.nf - col0);
     } else {
@@ -1503,13 +1569,15 @@ __global__ void __launch_bounds__(32 * LF_WARPS) k_leaf_factor(T* fac, int* ipiv
     const DFront F = S.fronts[L.front_ids[idx]];
     const int blk = F.block0, bw = F.nf, m = F.m;
     const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
+    const bool sym = S.sym != 0;
     for (int k = lane; k <= np; k += 32) q0[k] = S.xsuper[p0 + k] - F.f;
-    for (int j = 0; j < bw; ++j)
-        if (lane < bw) sD[j * LF_LD + lane] = fac[F.loff + (ll)j * F.ld + lane];
+    for (int j = 0; j < bw; ++j)   // symmetric form: the upper triangle mirrors the lower one
+        if (lane < bw)
+            sD[j * LF_LD + lane] = (sym && lane < j) ? fac[F.loff + (ll)lane * F.ld + j] : fac[F.loff + (ll)j * F.ld + lane];
     for (int x = lane; x < m; x += 32) tab[x] = scatter_row<T>(S, F, x);
     __syncwarp();
-    // block LU (ggetrf! pivots inside each piece)
-    const bool sing = warp_block_lu32(sD, LF_LD, bw, q0, np, piv);
+    // block LU (ggetrf! pivots inside each piece; none in the symmetric form)
+    const bool sing = warp_block_lu32(sD, LF_LD, bw, q0, np, piv, sym);
     for (int j = 0; j < bw; ++j)
         if (lane < bw) fac[F.loff + (ll)j * F.ld + lane] = sD[j * LF_LD + lane];
     if (lane < bw) {
@@ -1556,22 +1624,28 @@ __global__ void __launch_bounds__(32 * LF_WARPS) k_leaf_factor(T* fac, int* ipiv
                 sL[r * LF_LD + k] = x[k];
             }
     }
-    // U12 columns: y := inv(L) P y; then the Schur complement, a lane per column
+    // U12 columns: y := inv(L) P y (symmetric form: y_k = U(k, k) L21(c, k),
+    // from this lane's own L21 row); then the Schur complement, a lane per column
     T y[2][32];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const int c = lane + 32 * h;
+        if (sym) {
 #pragma unroll
-        for (int k = 0; k < 32; ++k) y[h][k] = (c < m && k < bw) ? fac[F.uoff + (ll)gm[k] * m + c] : T(0);
+            for (int k = 0; k < 32; ++k) y[h][k] = (c < m && k < bw) ? sD[k * LF_LD + k] * sL[c * LF_LD + k] : T(0);
+        } else {
 #pragma unroll
-        for (int i = 0; i < 32; ++i)
-            if (i < bw) {
+            for (int k = 0; k < 32; ++k) y[h][k] = (c < m && k < bw) ? fac[F.uoff + (ll)gm[k] * m + c] : T(0);
 #pragma unroll
-                for (int k = 0; k < i; ++k) {
-                    const T l = k < pam[i] ? sD[k * LF_LD + gm[i]] : sD[k * LF_LD + i];
-                    y[h][i] -= l * y[h][k];
+            for (int i = 0; i < 32; ++i)
+                if (i < bw) {
+#pragma unroll
+                    for (int k = 0; k < i; ++k) {
+                        const T l = k < pam[i] ? sD[k * LF_LD + gm[i]] : sD[k * LF_LD + i];
+                        y[h][i] -= l * y[h][k];
+                    }
                 }
-            }
+        }
         if (c < m)
 #pragma unroll
             for (int k = 0; k < 32; ++k)
@@ -1582,7 +1656,7 @@ __global__ void __launch_bounds__(32 * LF_WARPS) k_leaf_factor(T* fac, int* ipiv
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int c = lane + 32 * h;
-            if (c >= m) continue;
+            if (c >= m || (sym && r < c)) continue;   // the symmetric form forms the lower part only
             T acc = T(0);
 #pragma unroll
             for (int k = 0; k < 32; ++k)
@@ -1591,7 +1665,7 @@ __global__ void __launch_bounds__(32 * LF_WARPS) k_leaf_factor(T* fac, int* ipiv
                 const ScatterRow& Cc = tab[c];
                 const int p = S.rel[Cc.rel0 + r];
                 if (Cc.pos >= 0 && p >= 0) atomicAdd(&fac[Cc.loff + (ll)Cc.pos * Cc.ld + p], -acc);
-            } else {        // entry of the front of R_F[r]
+            } else if (!sym) {   // entry of the front of R_F[r] (the symmetric form keeps no U updates)
                 const ScatterRow& R = tab[r];
                 const int p = S.rel[R.rel0 + c];
                 if (R.pos >= 0 && p >= 0) {
@@ -1618,7 +1692,9 @@ __global__ void __launch_bounds__(256) k_schur(T* fac, Sched S, Launch L) {
     const DFront F = S.fronts[fid];
     const int tid = threadIdx.x;
     const int nt = cdiv(F.m, TT);
-    const int r0 = (tile % nt) * TT, c0 = (tile / nt) * TT;
+    int ti = tile % nt, tj = tile / nt;
+    if (S.sym) lower_tile(tile, nt, ti, tj);   // the symmetric form: lower tiles only
+    const int r0 = ti * TT, c0 = tj * TT;
     const int nr = min(TT, F.m - r0), nc = min(TT, F.m - c0);
     if (tid < 2 * TT) tab[tid / TT][tid % TT] = scatter_row<T>(S, F, (tid < TT ? c0 : r0) + tid % TT);   // published by the first barrier below
     T acc[4][4];
@@ -1647,7 +1723,8 @@ __global__ void __launch_bounds__(256) k_schur(T* fac, Sched S, Launch L) {
         for (int a = 0; a < 4; ++a) {
             const int ic = ty + 16 * b, ir = tx + 16 * a, c = c0 + ic, r = r0 + ir;
             pos[a][b] = -1;
-            if (ic < nc && ir < nr) pos[a][b] = r >= c ? S.rel[tab[0][ic].rel0 + r] : S.rel[tab[1][ir].rel0 + c];
+            if (ic < nc && ir < nr && (r >= c || !S.sym))
+                pos[a][b] = r >= c ? S.rel[tab[0][ic].rel0 + r] : S.rel[tab[1][ir].rel0 + c];
         }
 #pragma unroll
     for (int b = 0; b < 4; ++b)
@@ -1713,7 +1790,9 @@ __device__ __forceinline__ TcTile tc_decode(const Sched& S, const Launch& L, int
         const int c1 = S.blk_c1[blk], bw = c1 - S.blk_c0[blk];
         const int n1 = cdiv(T.F.nf - c1, umma::TM);
         T.n1 = n1;
-        if (t < (n1 + n2) * n1) {
+        if (S.sym) {   // lower tiles of the front columns only
+            lower_tile(t, n1 + n2, T.rt, T.ct);
+        } else if (t < (n1 + n2) * n1) {
             T.rt = t % (n1 + n2);
             T.ct = t / (n1 + n2);
         } else {
@@ -1726,6 +1805,7 @@ __device__ __forceinline__ TcTile tc_decode(const Sched& S, const Launch& L, int
         T.n1 = 0;
         T.rt = t % n2;
         T.ct = t / n2;
+        if (S.sym) lower_tile(t, n2, T.rt, T.ct);
         int nc = 0;
         for (int b = 0; b < T.F.nblocks; ++b) {
             const int blk = T.F.block0 + b;
@@ -1941,7 +2021,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
                             for (int j = 0; j < 16; ++j) {
                                 const int jj = 16 * half + j, c = c0 + h * 32 + jj;
                                 pos[j] = -1;
-                                if (c < F.m) pos[j] = r >= c ? S.rel[tab[0][h * 32 + jj].rel0 + r] : S.rel[R.rel0 + c];
+                                if (c < F.m && (r >= c || !S.sym))
+                                    pos[j] = r >= c ? S.rel[tab[0][h * 32 + jj].rel0 + r] : S.rel[R.rel0 + c];
                             }
 #pragma unroll
                             for (int j = 0; j < 16; ++j) {

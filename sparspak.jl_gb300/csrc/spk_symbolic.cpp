@@ -548,6 +548,174 @@ extern "C" int spk_order_nd_grid(int64_t nx, int64_t ny, int64_t nz, int64_t lea
 }
 
 // ---------------------------------------------------------------------------
+// Nested dissection of a general graph (project ordering plug-in; the
+// reference has none).  A connected vertex set larger than `leaf` is split by
+// a level-structure separator: breadth-first levels from a pseudo-peripheral
+// vertex (George and Liu's search: restart from a vertex of least degree in
+// the last level while the eccentricity grows), the middle level as
+// separator, trimmed of the vertices that have no neighbour in the next
+// level (they join the first part).  The parts are numbered first, each
+// recursively, the separator last.  Sets of at most `leaf` vertices, and
+// sets whose level structure is too shallow to split, are ordered by
+// minimum degree on their induced subgraph; disconnected sets component by
+// component.
+// ---------------------------------------------------------------------------
+namespace {
+struct GraphND {
+    i64 n, leaf;
+    const i64* xadj;   // xadj[v - 1] .. xadj[v] - 1: 1-based positions in adj
+    const i64* adj;
+    ivec& order;
+    ivec stamp_of, level, local;
+    i64 stamp = 0;
+
+    // Breadth-first levels of the set stamped `st` from `root`; returns the
+    // visit order, level[] holds each vertex's level.
+    void bfs(i64 root, i64 st, ivec& seen) {
+        seen.clear();
+        seen.push_back(root);
+        level[root] = 0;
+        stamp_of[root] = st + 1;   // visited marker for this search
+        for (size_t h = 0; h < seen.size(); ++h) {
+            const i64 v = seen[h];
+            for (i64 e = xadj[v - 1]; e < xadj[v]; ++e) {
+                const i64 w = adj[e - 1];
+                if (stamp_of[w] == st) {
+                    stamp_of[w] = st + 1;
+                    level[w] = level[v] + 1;
+                    seen.push_back(w);
+                }
+            }
+        }
+        for (i64 v : seen) stamp_of[v] = st;   // back to "in the set"
+    }
+
+    i64 degree_in(i64 v, i64 st) const {
+        i64 d = 0;
+        for (i64 e = xadj[v - 1]; e < xadj[v]; ++e) d += stamp_of[adj[e - 1]] == st;
+        return d;
+    }
+
+    void leaf_order(const ivec& verts) {
+        const i64 m = (i64)verts.size();
+        if (m == 0) return;
+        for (i64 t = 0; t < m; ++t) local[verts[t]] = t + 1;
+        ivec sx(m + 1), sa;
+        sx[0] = 1;
+        for (i64 t = 0; t < m; ++t) {
+            const i64 v = verts[t];
+            for (i64 e = xadj[v - 1]; e < xadj[v]; ++e) {
+                const i64 w = adj[e - 1];
+                if (local[w] > 0) sa.push_back(local[w]);
+            }
+            sx[t + 1] = (i64)sa.size() + 1;
+        }
+        ivec p, q;
+        mmd_order(m, sx.data(), sa.data(), p, q);
+        for (i64 t = 1; t <= m; ++t) order.push_back(verts[p[t] - 1]);
+        for (i64 t = 0; t < m; ++t) local[verts[t]] = 0;
+    }
+
+    void dissect(const ivec& verts) {
+        if ((i64)verts.size() <= leaf) {
+            leaf_order(verts);
+            return;
+        }
+        stamp += 2;
+        const i64 st = stamp;
+        for (i64 v : verts) stamp_of[v] = st;
+        // connected components of the set
+        ivec seen;
+        bfs(verts[0], st, seen);
+        if (seen.size() < verts.size()) {
+            std::vector<ivec> comps;
+            for (i64 v : verts) {
+                if (stamp_of[v] != st) continue;
+                ivec c;
+                bfs(v, st, c);
+                for (i64 w : c) stamp_of[w] = st - 1;   // assigned
+                comps.push_back(std::move(c));
+            }
+            for (const ivec& c : comps) dissect(c);
+            return;
+        }
+        // pseudo-peripheral root
+        i64 root = verts[0], best = -1;
+        for (i64 v : verts)
+            if (best < 0 || degree_in(v, st) < best) { best = degree_in(v, st); root = v; }
+        bfs(root, st, seen);
+        i64 ecc = level[seen.back()];
+        for (int it = 0; it < 8; ++it) {
+            i64 cand = seen.back(), cd = -1;
+            for (size_t t = seen.size(); t-- > 0 && level[seen[t]] == ecc;)
+                if (cd < 0 || degree_in(seen[t], st) < cd) { cd = degree_in(seen[t], st); cand = seen[t]; }
+            ivec s2;
+            bfs(cand, st, s2);
+            if (level[s2.back()] <= ecc) {
+                bfs(root, st, seen);   // restore the levels of the best root
+                break;
+            }
+            root = cand;
+            seen.swap(s2);
+            ecc = level[seen.back()];
+        }
+        if (ecc < 2) {
+            leaf_order(verts);
+            return;
+        }
+        // middle level: first level whose cumulative count reaches half
+        ivec count(ecc + 1, 0);
+        for (i64 v : seen) ++count[level[v]];
+        i64 mid = 1, acc = 0;
+        for (i64 l = 0; l <= ecc; ++l) {
+            acc += count[l];
+            if (2 * acc >= (i64)verts.size()) { mid = std::min(std::max<i64>(l, 1), ecc - 1); break; }
+        }
+        ivec A, B, Sep;
+        for (i64 v : seen) {
+            const i64 l = level[v];
+            if (l < mid) A.push_back(v);
+            else if (l > mid) B.push_back(v);
+            else {
+                bool next = false;
+                for (i64 e = xadj[v - 1]; e < xadj[v] && !next; ++e) {
+                    const i64 w = adj[e - 1];
+                    next = stamp_of[w] == st && level[w] == mid + 1;
+                }
+                (next ? Sep : A).push_back(v);
+            }
+        }
+        dissect(A);
+        dissect(B);
+        for (i64 v : Sep) order.push_back(v);
+    }
+};
+}  // namespace
+
+extern "C" int spk_order_nd_graph(int64_t nv, const int64_t* xadj, const int64_t* adj, int64_t leaf, int64_t* perm,
+                                  int64_t* invp) {
+    if (nv < 0 || (nv > 0 && (!perm || !invp))) return fail(SPK_HOST_EARG, "spk_order_nd_graph: bad arguments");
+    int rc = check_graph(nv, xadj, adj, "spk_order_nd_graph");
+    if (rc) return rc;
+    try {
+        ivec order;
+        order.reserve(nv);
+        GraphND nd{nv, std::max<i64>(leaf, 1), xadj, adj, order, ivec(nv + 2, 0), ivec(nv + 2, 0), ivec(nv + 2, 0)};
+        ivec all(nv);
+        for (i64 v = 0; v < nv; ++v) all[v] = v + 1;
+        if (nv > 0) nd.dissect(all);
+        if ((i64)order.size() != nv) return fail(SPK_HOST_ESTRUCT, "spk_order_nd_graph: ordering incomplete");
+        for (i64 t = 0; t < nv; ++t) {
+            perm[t] = order[t];
+            invp[order[t] - 1] = t + 1;
+        }
+    } catch (const std::bad_alloc&) {
+        return fail(SPK_HOST_ENOMEM, "spk_order_nd_graph: out of memory");
+    }
+    return SPK_HOST_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Elimination tree, postorders, column counts (src/ETree/SpkETree.jl,
 // src/SparseSpdMethod/SpkSymFct.jl:37-59)
 // ---------------------------------------------------------------------------

@@ -12,7 +12,8 @@ from . import gallery, graph, problem, sparse_solver
 from ._build import build
 from .csc import ldiv, ldiv_, sparspaklu, sparspaklu_
 from .device import ErrorException, NumericEngine, SingularException
-from .graph import ETree, Graph, Ordering, isstructuresymmetric, makestructuresymmetric, mmd_, nd_grid, nd_grid_batched
+from .graph import (ETree, Graph, Ordering, isstructuresymmetric, makestructuresymmetric, mmd_, nd_graph, nd_grid,
+                    nd_grid_batched)
 from .problem import (Grid, Problem, computeresidual, inaij_, inbi_, infullrhs_, insparse_, makegridproblem,
                       makerhs_, outsparse, zerorhs_)
 from .sparse_solver import (SparseSolver, factor_, findorder_, findorderperm_, gradient_, inmatrix_, refine_, solve_,
@@ -22,7 +23,7 @@ __all__ = [
     "build", "gallery", "graph", "problem", "sparse_solver",
     "ldiv", "ldiv_", "sparspaklu", "sparspaklu_",
     "ErrorException", "NumericEngine", "SingularException",
-    "ETree", "Graph", "Ordering", "isstructuresymmetric", "makestructuresymmetric", "mmd_", "nd_grid",
+    "ETree", "Graph", "Ordering", "isstructuresymmetric", "makestructuresymmetric", "mmd_", "nd_graph", "nd_grid",
     "nd_grid_batched",
     "Grid", "Problem", "computeresidual", "inaij_", "inbi_", "infullrhs_", "insparse_", "makegridproblem",
     "makerhs_", "outsparse", "zerorhs_",

@@ -25,6 +25,7 @@ HOST_SYMBOLS = {
     "spk_graph_symmetrize": (ctypes.c_int, [i64, P64, P64, P64, P64, P64]),
     "spk_order_mmd": (ctypes.c_int, [i64, P64, P64, P64, P64]),
     "spk_order_nd_grid": (ctypes.c_int, [i64, i64, i64, i64, P64, P64, P64, P64]),
+    "spk_order_nd_graph": (ctypes.c_int, [i64, P64, P64, i64, P64, P64]),
     "spk_symbolic_create": (ctypes.c_int, [i64, P64, P64, P64, P64, i64, ctypes.POINTER(VP)]),
     "spk_symbolic_sizes": (ctypes.c_int, [VP, P64, P64, P64, P64]),
     "spk_symbolic_get": (ctypes.c_int, [VP, P64, P64, P64, P64, P64, P64, P64, P64, P64, P64]),
@@ -76,6 +77,7 @@ KERNEL_UNITS = {"tc_trail": "tcgen05 kind::tf32, 3xTF32 per term", "tc_schur": "
                 "getrf": "FP32 FMA, latency-bound (one CTA per front, sequential pivot columns; small fronts a warp each)",
                 "panel": "FP32 FMA (register-line triangular sweeps)"}
 SPK_FP64, SPK_FP32, SPK_BF16S = 0, 1, 2
+SPK_SPD = 16   # or-ed with a precision: the symmetric (SPD, Cholesky) form
 SPK_SOLVER_AUTO, SPK_SOLVER_IR, SPK_SOLVER_GMRES = 0, 1, 2
 SOLVERS = {"auto": SPK_SOLVER_AUTO, "ir": SPK_SOLVER_IR, "gmres": SPK_SOLVER_GMRES}
 

@@ -29,11 +29,13 @@ class SingularException(ErrorException):
 
 
 def _prec(p) -> int:
+    """Precision code of 'fp64' / 'fp32' / 'bf16s', with '+spd' for the
+    symmetric (Cholesky) form of SPD matrices, or an int code."""
     if isinstance(p, str):
-        try:
-            return PRECISIONS[p.lower()]
-        except KeyError:
-            raise ValueError(f"unknown precision {p!r}; use 'fp64', 'fp32' or 'bf16s'") from None
+        base, _, form = p.lower().partition("+")
+        if base not in PRECISIONS or form not in ("", "spd"):
+            raise ValueError(f"unknown precision {p!r}; use 'fp64', 'fp32' or 'bf16s', optionally with '+spd'")
+        return PRECISIONS[base] | (N.SPK_SPD if form == "spd" else 0)
     return int(p)
 
 

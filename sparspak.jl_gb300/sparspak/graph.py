@@ -140,6 +140,23 @@ def nd_grid(nx: int, ny: int, nz: int = 1, leaf: int = 64):
     return orderfunction
 
 
+def nd_graph(leaf: int = 64):
+    """Order function for any symmetric graph: nested dissection by
+    level-structure separators (pseudo-peripheral roots, middle level,
+    separators last), minimum degree inside sets of <= leaf vertices."""
+
+    def orderfunction(g: Graph, order: Ordering) -> None:
+        perm = np.zeros(g.nv, dtype=np.int64)
+        invp = np.zeros(g.nv, dtype=np.int64)
+        rc = N.host().spk_order_nd_graph(g.nv, N.p64(g.xadj), N.p64(g.adj), leaf, N.p64(perm), N.p64(invp))
+        if rc < 0:
+            raise ValueError(N.host_error())
+        order.rperm, order.rinvp = perm, invp
+        order.cperm, order.cinvp = perm.copy(), invp.copy()
+
+    return orderfunction
+
+
 def nd_grid_batched(sizes, leaf: int = 64):
     """Order function for the block-diagonal union of square grids (system k:
     sizes[k] x sizes[k] vertices, consecutive): nested dissection of every

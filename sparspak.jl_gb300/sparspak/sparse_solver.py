@@ -165,10 +165,14 @@ def _triangularsolve_(s: _SparseBase, solution: np.ndarray) -> bool:
 class SparseSolver:
     """SparseSolver(p::Problem) or SparseSolver(m::SparseMatrixCSC) - SpkSparseSolver.jl:17-73.
 
-    ``precision`` ('fp64', 'fp32' or 'bf16s') selects the factor the numeric phases use.
+    ``precision`` ('fp64', 'fp32' or 'bf16s') selects the factor the numeric
+    phases use; ``spd=True`` selects the symmetric form for symmetric positive
+    definite matrices (Cholesky: no interchanges, half the update work; the
+    role of the reference's SparseSpdSolver, src/SparseSpdMethod), whose
+    factor reads back as the Cholesky factor C, A = C C^T.
     """
 
-    def __init__(self, p, precision: str = "fp64", maxblocksize: int = 30):
+    def __init__(self, p, precision: str = "fp64", maxblocksize: int = 30, spd: bool = False):
         if isinstance(p, Problem):
             self.ma, self.na = p.nrows, p.ncols
         else:
@@ -178,7 +182,8 @@ class SparseSolver:
         self.n = self.ma
         self.mc = self.nc = 0
         self.slvr = _SparseBase(p, maxblocksize)
-        self.slvr.precision = precision
+        self.spd = bool(spd)
+        self.slvr.precision = _form(precision, self.spd)
         self._orderdone = self._symbolicdone = self._inmatrixdone = False
         self._factordone = self._trisolvedone = self._refinedone = self._condestdone = False
 
@@ -288,6 +293,11 @@ def solve_(s: SparseSolver, rhs=None) -> bool:
     return True
 
 
+def _form(precision: str, spd: bool) -> str:
+    precision = precision.lower()
+    return precision + "+spd" if spd and "+spd" not in precision else precision
+
+
 def refine_(s: SparseSolver, b: np.ndarray, x: np.ndarray | None = None, precision: str = "fp32", tol: float = 1e-12,
             max_iter: int = 20, transpose: bool = False, solver: str | None = None):
     """Mixed-precision solve: factor in `precision` ('fp32', 'bf16s' or
@@ -302,6 +312,7 @@ def refine_(s: SparseSolver, b: np.ndarray, x: np.ndarray | None = None, precisi
     """
     findorder_(s)
     symbolicfactor_(s)
+    precision = _form(precision, getattr(s, "spd", False))
     if s.slvr.precision != precision or not s._factordone:
         s.slvr.precision = precision
         s._inmatrixdone = False

@@ -164,3 +164,59 @@ def test_adjoint_gradient_anisotropic_diffusion_256():
             losses.append(0.5 * np.sum((xp - xt) ** 2))
         fd = (losses[0] - losses[1]) / (2 * h)
         assert abs(fd - analytic) <= 1e-4 * max(abs(analytic), 1e-8 * np.sum((x - xt) ** 2)), (e, fd, analytic)
+
+
+def test_adjoint_gradient_vs_dual_oracle():
+    # Config 5 on a reduced grid (48 x 48 anisotropic diffusion, theta_e =
+    # exp(g), g ~ N(0, 0.5)): dloss/dtheta for loss = 1/2 ||x - x_t||^2 on 32
+    # random interior edges from the GPU adjoint (transposed solve reusing the
+    # factors + the pattern-restricted gradient kernel) against forward-mode
+    # derivatives through the reference's LU path on Dual numbers (the
+    # reference's derivative check, test/test_generic.jl:58-98), 16 edges per
+    # Dual pass.
+    import oracle
+    from sparspak.sparse_solver import _matrix_arrays
+
+    n1 = 48
+    th, tv = diffusion_problem(n1, 2)
+    A = sp.csc_matrix(S.gallery.diffusion_2d(n1, th, tv))
+    n = A.shape[0]
+    rng = np.random.Generator(np.random.PCG64(5))
+    xt = rng.uniform(-1.0, 1.0, n)
+    b = rng.uniform(-1.0, 1.0, n)
+    lu = S.sparspaklu(A, orderfunction=S.nd_grid(n1, n1, 1))
+    x = np.array(b)
+    S.ldiv_(lu, x)
+    lam = np.asfortranarray(x - xt)
+    S.transposetriangularsolve_(lu, lam)
+    G = S.gradient_(lu, lam, x)
+
+    def entry(i, j):
+        lo, hi = A.indptr[j], A.indptr[j + 1]
+        return lo + int(np.searchsorted(A.indices[lo:hi], i))
+
+    ids = np.arange(n).reshape(n1, n1)
+    picks = rng.choice(2 * n1 * (n1 - 1), size=32, replace=False)
+    edges = []
+    for e in picks:
+        if e < n1 * (n1 - 1):
+            i, j = divmod(int(e), n1 - 1)
+            edges.append((ids[i, j], ids[i, j + 1]))
+        else:
+            i, j = divmod(int(e) - n1 * (n1 - 1), n1)
+            edges.append((ids[i, j], ids[i + 1, j]))
+    cp, rv, nz = _matrix_arrays(A)
+    for g0 in range(0, len(edges), 16):
+        group = edges[g0: g0 + 16]
+        dnz = np.zeros((A.nnz, len(group)))
+        for k, (a, c) in enumerate(group):   # dA/dtheta_e = (e_a - e_c)(e_a - e_c)^T
+            dnz[entry(a, a), k] += 1.0
+            dnz[entry(c, c), k] += 1.0
+            dnz[entry(a, c), k] -= 1.0
+            dnz[entry(c, a), k] -= 1.0
+        xd, dx = oracle.dual_solve(lu.slvr, cp, rv, nz, dnz, b)
+        assert np.max(np.abs(xd - x)) / np.max(np.abs(x)) < 1e-10
+        dual = (xd - xt) @ dx
+        for k, (a, c) in enumerate(group):
+            adj = G[entry(a, a)] + G[entry(c, c)] - G[entry(a, c)] - G[entry(c, a)]
+            assert abs(adj - dual[k]) <= 1e-9 * max(abs(dual[k]), 1e-12 * np.sum((x - xt) ** 2)), (a, c, adj, dual[k])

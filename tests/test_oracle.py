@@ -181,7 +181,8 @@ def test_oracle_graph_fig313(golden):
 def _structure_cases():
     rng_cases = [("sprand_spd", 301), ("sprand_spd", 1357), ("sprand_unsym", 400)]
     grid_cases = [((20, 20, 1), "mmd"), ((100, 100, 1), "mmd"), ((100, 100, 1), "nd"), ((9, 10, 11), "mmd"),
-                  ((24, 24, 24), "nd"), ((17, 13, 9), "nd")]
+                  ((24, 24, 24), "nd"), ((17, 13, 9), "nd"), ((100, 100, 1), "nd_graph"), ((24, 24, 24), "nd_graph"),
+                  ((17, 13, 9), "nd_graph")]
     return rng_cases + grid_cases
 
 
@@ -196,7 +197,7 @@ def test_oracle_structure_equals_product(case):
     else:
         grid, ordering = case
         A = S.gallery.laplacian(grid if grid[2] > 1 else grid[:2])
-        orderfunction = S.nd_grid(*grid) if ordering == "nd" else None
+        orderfunction = {"nd": S.nd_grid(*grid), "nd_graph": S.nd_graph(), "mmd": None}[ordering]
     A = sp.csc_matrix(A)
     n = A.shape[0]
     cp, rv = A.indptr.astype(np.int64) + 1, A.indices.astype(np.int64) + 1
@@ -245,3 +246,77 @@ def test_oracle_blas_mode_matches_generic():
     assert np.max(np.abs(g.lnz - bl.lnz)) / scale < 1e-13
     xg = g.solve(b)
     assert np.max(np.abs(xg - xb)) / np.max(np.abs(xg)) < 1e-12
+
+
+def test_oracle_cholesky_reconstructs_a():
+    # the oracle's supernodal Cholesky: C C^T = P A P^T on 2-D and 3-D grids
+    # with MMD and nested dissection (pieces of up to 46 columns)
+    for shape, ordering in [((10, 10), "mmd"), ((7, 8, 9), "mmd"), ((12, 12, 12), "nd")]:
+        A = S.gallery.laplacian(shape, shift=1e-3)
+        n = A.shape[0]
+        cp, rv, nz = A.indptr.astype(np.int64) + 1, A.indices.astype(np.int64) + 1, A.data
+        grid = shape + (1,) * (3 - len(shape))
+        st = oracle.structure_csc(cp, rv, n, ordering, grid)
+        o = oracle.OracleLU(st)
+        o.inmatrix_csc(cp, rv, nz)
+        assert o.cholfactor() == 0
+        C = np.zeros((n, n))
+        for js in range(st.nsuper):
+            f, l = int(st.xsuper[js]), int(st.xsuper[js + 1])
+            rows = st.lindx[st.xlindx[js] - 1: st.xlindx[js + 1] - 1] - 1
+            for k in range(l - f):
+                base = int(st.xlnz[f - 1 + k]) - 1
+                sel = rows >= f - 1 + k
+                C[rows[sel], f - 1 + k] = o.lnz[base: base + rows.size][sel]
+        P = st.order.rperm - 1
+        assert np.max(np.abs(C @ C.T - A.toarray()[np.ix_(P, P)])) < 1e-12
+
+
+def test_oracle_cholesky_rejects_indefinite():
+    A = sp.csc_matrix(S.gallery.laplacian((5, 5)) - 5.0 * sp.identity(25))
+    cp, rv, nz = A.indptr.astype(np.int64) + 1, A.indices.astype(np.int64) + 1, A.data
+    st = oracle.structure_csc(cp, rv, 25, "mmd")
+    o = oracle.OracleLU(st)
+    o.inmatrix_csc(cp, rv, nz)
+    assert o.cholfactor() > 0
+
+
+def test_dual_oracle_gradient_through_sparse_solve():
+    # test/test_generic.jl:58-98 (generic002): d/dp sum(A(p) \\ ones) for the
+    # 20 x 20 tridiagonal A(p) = Tridiagonal(-0.1, p^i, -0.1), p in 1:0.1:10,
+    # through the LU path on Dual numbers, against the dense derivative
+    # -1' A^-1 (dA/dp) A^-1 1 (the reference compares with ForwardDiff on the
+    # dense solve, to rtol sqrt(eps))
+    n = 20
+    for p in np.arange(1.0, 10.0 + 1e-9, 0.1):
+        i = np.arange(1, n + 1, dtype=np.float64)
+        A = sp.diags([-0.1 * np.ones(n - 1), p ** i, -0.1 * np.ones(n - 1)], [-1, 0, 1], format="csc")
+        dA = sp.diags([np.zeros(n - 1), i * p ** (i - 1), np.zeros(n - 1)], [-1, 0, 1], format="csc")
+        cp, rv = A.indptr.astype(np.int64) + 1, A.indices.astype(np.int64) + 1
+        st = oracle.structure_csc(cp, rv, n, "mmd")
+        cols = np.repeat(np.arange(n), np.diff(A.indptr))
+        dnz = np.asarray(dA.toarray()[A.indices, cols]).reshape(-1, 1)   # dA/dp on A's pattern, CSC order
+        x, dx = oracle.dual_solve(st, cp, rv, A.data, dnz, np.ones(n))
+        Ad = A.toarray()
+        y = np.linalg.solve(Ad, np.ones(n))
+        dense = -np.ones(n) @ np.linalg.solve(Ad, dA.toarray() @ y)
+        assert np.isclose(np.sum(dx[:, 0]), dense, rtol=1e-10, atol=0.0), (p, np.sum(dx[:, 0]), dense)
+        assert np.allclose(x, y, rtol=1e-12, atol=0.0)
+
+
+def test_dual_oracle_matches_finite_differences():
+    A = sp.csc_matrix(S.gallery.convection_diffusion(k=6))
+    n = A.shape[0]
+    cp, rv = A.indptr.astype(np.int64) + 1, A.indices.astype(np.int64) + 1
+    st = oracle.structure_csc(cp, rv, n, "mmd")
+    rng = np.random.default_rng(3)
+    dnz = rng.standard_normal((A.nnz, 5))
+    b = rng.uniform(-1, 1, n)
+    x, dx = oracle.dual_solve(st, cp, rv, A.data, dnz, b)
+    for k in range(5):
+        h = 1e-6
+        Ap, Am = A.copy(), A.copy()
+        Ap.data = A.data + h * dnz[:, k]
+        Am.data = A.data - h * dnz[:, k]
+        fd = (np.linalg.solve(Ap.toarray(), b) - np.linalg.solve(Am.toarray(), b)) / (2 * h)
+        assert np.max(np.abs(fd - dx[:, k])) / np.max(np.abs(fd)) < 1e-7
