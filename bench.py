@@ -144,6 +144,14 @@ def lu_flops(b):
     return float(np.sum((c - 1) + 2.0 * (c - 1) ** 2))
 
 
+def chol_flops(b):
+    """Cholesky flops sum_j 1 + (c_j - 1) + (c_j - 1) c_j over the column counts."""
+    w = np.diff(b.xsuper)
+    ln = np.diff(b.xlindx)
+    c = np.concatenate([ln[i] - np.arange(w[i]) for i in range(b.nsuper)]).astype(np.float64)
+    return float(np.sum(1.0 + (c - 1) + (c - 1) * c))
+
+
 def supernode_flops(b):
     """Per supernode, the LU flop count of its columns: a proxy of the work
     between two supernodes of _lufactor!'s outer loop, used to cut the
@@ -295,6 +303,50 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def config1(args, dev, stream, timed):
+    """Config 1: the 2-D 5-point Laplacian on a 100 x 100 grid (n = 10,000),
+    one right-hand side U[-1,1] (seed 0), minimum-degree ordering (the
+    reference's default): LU and Cholesky (SPD form) factorisations in FP64
+    and the time to a solution, on the device."""
+    import torch
+
+    import sparspak as S
+    from sparspak.sparse_solver import _ensure_engine, _matrix_arrays
+
+    A = S.gallery.laplacian((100, 100))
+    n = A.shape[0]
+    b = S.gallery.random_rhs(n, 1, seed=0)
+    s = S.SparseSolver(A)
+    S.findorder_(s)
+    S.symbolicfactor_(s)
+    eng = _ensure_engine(s.slvr)
+    colptr, rowval, nzval = _matrix_arrays(A)
+    eng.set_pattern(colptr, rowval, s.slvr.order.rperm, s.slvr.order.rinvp, index_base=1)
+    eng.set_stream(stream.cuda_stream)
+    nz_d = torch.tensor(nzval, device=dev)
+    b_d = torch.tensor(b.reshape(1, n), device=dev)
+    x_d = torch.zeros_like(b_d)
+    out = {"workload": "laplace2d_100x100_mmd_1rhs", "n": n, "lu_flops": lu_flops(s.slvr),
+           "cholesky_flops": chol_flops(s.slvr)}
+    for form, flops in (("fp64", out["lu_flops"]), ("fp64+spd", out["cholesky_flops"])):
+        def fac():
+            eng.load_values(nz_d, form)
+            eng.factor(form)
+
+        def sol():
+            fac()
+            return eng.refine(b_d, x_d, form, TOL, 5)
+
+        for _ in range(args.warmup):
+            sol()
+        ms_f, _ = timed(fac, args.steps)
+        ms_s, (it, rr) = timed(sol, args.steps)
+        out["lu" if form == "fp64" else "cholesky"] = {"factor_ms": ms_f, "factor_gflops": flops / (ms_f * 1e-3) / 1e9,
+                                                       "time_to_1e-12_ms": ms_s, "relres": rr, "corrections": it}
+    eng.close()
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -309,6 +361,7 @@ def run_ours(args):
     n = A.shape[0]
     s, host_t = symbolic(A, k, args.ordering)
     F = lu_flops(s.slvr)
+    FC = chol_flops(s.slvr)
     eng = _ensure_engine(s.slvr)
     colptr, rowval, nzval = _matrix_arrays(A)
     t0 = time.perf_counter()
@@ -326,7 +379,7 @@ def run_ours(args):
     def step(prec):
         eng.load_values(nz_d, prec)
         eng.factor(prec)
-        if prec == "bf16s":   # plain refinement, then GMRES-IR once it stagnates
+        if prec.startswith("bf16s"):   # plain refinement, then GMRES-IR once it stagnates
             it, rr, used = eng.refine(b_d, x_d, prec, TOL, 200, solver="auto")
             return it, rr, used
         return eng.refine(b_d, x_d, prec, TOL, 30)
@@ -396,6 +449,15 @@ def run_ours(args):
     timed(lambda: (eng.load_values(nz_d, "bf16s"), eng.factor("bf16s")), 1)
     live_bf16 = eng.profile_read()
     eng.profile([])
+    # the SPD (Cholesky) form of the same matrix: FP32 factor + FP64 refinement, and FP64
+    for _ in range(args.warmup):
+        step("fp32+spd")
+    ms_spd, (it_spd, rr_spd) = timed(lambda: step("fp32+spd"), args.steps)
+    x_spd = x_d.cpu().numpy().T.copy()
+    ms_fspd, _ = timed(lambda: (eng.load_values(nz_d, "fp32+spd"), eng.factor("fp32+spd")), args.steps)
+    step("fp64+spd")
+    ms_spd64, (it_spd64, rr_spd64) = timed(lambda: step("fp64+spd"), max(1, args.steps // 2))
+    ms_fspd64, _ = timed(lambda: (eng.load_values(nz_d, "fp64+spd"), eng.factor("fp64+spd")), max(1, args.steps // 2))
     for _ in range(args.warmup):
         step("fp64")
     ms_fp64, (it_fp64, rr_fp64) = timed(lambda: step("fp64"), args.steps)
@@ -403,6 +465,8 @@ def run_ours(args):
     ms_f64, _ = timed(lambda: (eng.load_values(nz_d, "fp64"), eng.factor("fp64")), max(1, args.steps // 2))
     ms_asm32, _ = timed(lambda: eng.load_values(nz_d, "fp32"), args.steps)
     ms_asm64, _ = timed(lambda: eng.load_values(nz_d, "fp64"), args.steps)
+
+    cfg1 = config1(args, dev, stream, timed)
 
     # e2e through the public API with pinned host buffers
     nz_h = torch.tensor(nzval).pin_memory().numpy()
@@ -516,9 +580,15 @@ def run_ours(args):
                  "factor_frac_of_fp64_dmma": F / (ms_f64 * 1e-3) / 1e12 / simt["fp64_dmma_tflops"]},
         "bf16s": {"ms": ms_bf16, "preconditioned_solves": it_bf16, "solver": used_bf16, "relres": rr_bf16,
                   "factor_ms": ms_fb16, "factor_gflops": F / (ms_fb16 * 1e-3) / 1e9},
-        "forward_error_vs_fp64": {"mixed": fwd_err(x_mixed), "bf16s": fwd_err(x_bf16),
+        "spd": {"ms": ms_spd, "corrections": it_spd, "relres": rr_spd, "factor_ms": ms_fspd,
+                "factor_gflops": FC / (ms_fspd * 1e-3) / 1e9, "fp64_ms": ms_spd64, "fp64_factor_ms": ms_fspd64,
+                "fp64_factor_gflops": FC / (ms_fspd64 * 1e-3) / 1e9, "cholesky_flops": FC,
+                "form": "SPK_SPD: no interchanges, lower-only (SYRK-like) rank updates, FP32 factor + FP64 "
+                        "refinement; GFLOP/s count the Cholesky flops"},
+        "forward_error_vs_fp64": {"mixed": fwd_err(x_mixed), "bf16s": fwd_err(x_bf16), "spd": fwd_err(x_spd),
                                   "note": "max-norm, against the FP64 GPU solution of the same step (which the "
                                           "parity tests hold within 1e-10 of the oracle's)"},
+        "config1_grid2d_100": cfg1,
         "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
         "speedup_bf16s_vs_fp64": ms_fp64 / ms_bf16,
         "measured_peaks": simt,
