@@ -276,3 +276,31 @@ def test_many_rhs_front_and_leaf_solves(nrhs):
     S.transposetriangularsolve_(s, xt)
     xr = spla.splu(sp.csc_matrix(A.T)).solve(b)
     assert rel(xt, xr) < 1e-9
+
+
+@pytest.mark.parametrize("kind", ["dense300", "unsym_pivoting"])
+def test_fp32_block_lu_with_pivoting(kind):
+    # FP32 blocks of up to 128 columns with real in-piece interchanges: a
+    # dense 300 x 300 block (one front, 27-28-column pieces, 128-column
+    # blocks) and a sparse unsymmetric matrix with a small diagonal.  Same
+    # pivots as the FP64 oracle, factors to FP32 accuracy (pivoting only
+    # inside pieces allows growth), refinement to 1e-12.
+    rng = np.random.default_rng(21)
+    if kind == "dense300":
+        n = 300
+        A = sp.csc_matrix(rng.standard_normal((n, n)) + 0.5 * np.sqrt(n) * np.eye(n))
+    else:
+        n = 600
+        a = sp.random(n, n, density=8.0 / n, random_state=rng, format="csc")
+        A = sp.csc_matrix(a + a.T.multiply(rng.uniform(0.5, 1.5)) + 0.05 * sp.identity(n))
+    s, o = run_both(A, None, precision="fp32")
+    b_ = s.slvr
+    ident = np.concatenate([np.arange(1, b_.xsuper[k + 1] - b_.xsuper[k] + 1) for k in range(b_.nsuper)])
+    assert not np.array_equal(o.ipiv, ident), "the case should exercise in-block interchanges"
+    assert np.array_equal(b_.ipiv, o.ipiv)
+    assert rel(b_.lnz, o.lnz) < 5e-3
+    b = S.gallery.random_rhs(n, 2, seed=8)
+    x, it, rr = S.refine_(s, b, precision="fp32", tol=1e-12)
+    assert rr <= 1e-12
+    r = b - A @ x
+    assert np.max(np.linalg.norm(r, axis=0) / np.linalg.norm(b, axis=0)) <= 1e-12
