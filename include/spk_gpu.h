@@ -38,6 +38,9 @@ extern "C" {
                               slot in the factor ("No space for matrix element")   */
 #define SPK_ESINGULAR (-6) /* a diagonal block had an exactly zero pivot           */
 #define SPK_ENOCONV (-7)   /* refinement did not reach the requested tolerance     */
+#define SPK_ETIMEOUT (-8)  /* a bounded device wait ran out (no progress within its
+                              budget): the factors are invalid, the context stays
+                              usable and the next spk_factor reassembles A       */
 
 #define SPK_HOST 0
 #define SPK_DEVICE 1
@@ -279,6 +282,48 @@ int spk_profile_read(spk_handle* h, int kind, double* ms, int64_t* launches, dou
  * independent chains.  Any pointer may be NULL.
  */
 int spk_measure_peaks(double* fp32_tflops, double* fp64_tflops, double* dmma_tflops);
+
+/*
+ * Options of the factorisation (no counterpart in the reference).  Changing
+ * one takes effect at the next spk_factor; the tensor-core thresholds also
+ * discard the FP32 / BF16S factors (factor again after spk_load_values).
+ *  SPK_OPT_LEAF_QUEUE    1: the bottom subtrees of small fronts (one block
+ *                        of at most 32 columns, at most 32 rows below it,
+ *                        every descendant alike) are factored by one
+ *                        persistent launch: a work queue in level order with
+ *                        a dependency counter per front and bounded waits;
+ *                        0 (default): one launch per level and width class.
+ *                        The reference's own work list is the `link` list of
+ *                        _lufactor! (src/SparseMethod/SpkLUFactor.jl:89-228).
+ *  SPK_OPT_WAIT_BUDGET   polls of a queue wait before it gives up and the
+ *                        factorisation returns SPK_ETIMEOUT (default 2^20,
+ *                        about a second at the longest).
+ *  SPK_OPT_STALL_TEST    test hook: the queue position whose wait nothing
+ *                        ends (-1, the default: none); with a small budget it
+ *                        shows the timeout path without a GPU fault.
+ *  SPK_OPT_TC_SCHUR_M    FP32 / BF16S: a front with at least this many rows
+ *                        below its pivot columns takes the tensor-core rank
+ *                        updates (default 96);
+ *  SPK_OPT_TC_TRAIL_ROWS or one of several blocks with at least this many
+ *                        rows below its first block (default 128).
+ */
+#define SPK_OPT_LEAF_QUEUE 0
+#define SPK_OPT_WAIT_BUDGET 1
+#define SPK_OPT_STALL_TEST 2
+#define SPK_OPT_TC_SCHUR_M 3
+#define SPK_OPT_TC_TRAIL_ROWS 4
+int spk_set_option(spk_handle* h, int option, int64_t value);
+int spk_get_option(spk_handle* h, int option, int64_t* value);
+
+/*
+ * Tune the options above for the loaded A in the given precision (no
+ * counterpart in the reference): times `reps` factorisations (median, CUDA
+ * events, after one untimed) with the leaf queue off and on, then, for the
+ * float forms, a set of tensor-core thresholds; keeps the fastest, leaves A
+ * assembled for spk_factor and returns the best factor time in *best_ms (may
+ * be NULL).  Needs spk_load_values first.
+ */
+int spk_autotune(spk_handle* h, int precision, int reps, double* best_ms);
 
 /* Text of the last error on this handle (never NULL); with h == NULL, the
  * reason the last spk_create on this thread failed. */

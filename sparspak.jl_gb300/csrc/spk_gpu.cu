@@ -60,7 +60,9 @@ struct LevelPlan {
     // Solves: fronts with many blocks by one cluster launch each direction
     // (front_big, one tile per front), the others by block steps
     // (fwd_small / bwd_small); the transposed solves use fwd / bwd.
-    LaunchRec leaf_factor;            // fronts factored whole by k_leaf_factor (a warp each)
+    // fronts factored whole by k_leaf_factor (a warp each), by width class;
+    // leaf_q: the leaf queue's fronts of this level, for when the queue is off
+    LaunchRec leaf_factor[spk::LF_CLASSES], leaf_q[spk::LF_CLASSES];
     LaunchRec front_big, front_l21;   // front_l21: tiles of k_fwd_l21 for the front_big fronts
     // Small fronts (one block of at most 32 columns, m <= spk::LEAF_M) by
     // k_solve_leaf, a warp per front; bwdu_small: U12 products of the others.
@@ -70,9 +72,12 @@ struct LevelPlan {
 
 // FP32 fronts whose rank updates go to the tensor cores (k_tc_update,
 // 128 x 128 tiles from packed panels): a Schur complement of at least
-// TC_SCHUR_M rows, or more than one block with at least TC_TRAIL_ROWS rows
-// below the first.
+// tc_schur_m rows, or more than one block with at least tc_trail_rows rows
+// below the first (spk_handle; defaults below, SPK_OPT_TC_* to change).
 constexpr int TC_SCHUR_M = 96, TC_TRAIL_ROWS = 128;
+// Polls of a bounded device wait (the leaf queue's dependency waits) before
+// it gives up and records a timeout.
+constexpr long long WAIT_BUDGET = 1 << 20;
 
 // Block partition and schedule for one precision (block width BlockMax<T>).
 struct Plan {
@@ -91,6 +96,14 @@ struct Plan {
     std::vector<int> block0, nblocks;     // per front
     std::vector<LevelPlan> levels;
     std::vector<int> sched_ids, sched_prefix;
+    // The leaf queue (k_leaf_queue): the fronts factored whole (by a warp)
+    // whose descendants all are, in level order.  Per queue position: the
+    // front, and its parent when that is in the queue (else -1); per front:
+    // the number of its children in the queue.
+    std::vector<int> q_order, q_parent, q_deps;
+    int nq = 0, q_grid = 1;
+    double q_flops = 0.0, q_words = 0.0;
+    int *d_q_order = nullptr, *d_q_parent = nullptr, *d_q_deps0 = nullptr, *d_q_deps = nullptr, *d_q_next = nullptr;
     spk::DFront* d_fronts = nullptr;
     int *d_blk_c0 = nullptr, *d_blk_c1 = nullptr, *d_blk_p0 = nullptr, *d_blk_np = nullptr;
     ll* d_blk_inv2 = nullptr;
@@ -188,6 +201,11 @@ struct spk_handle {
     cudaEvent_t evP = nullptr, evB = nullptr;
     int device = -1;
     int nsm = 1;                 // SMs of the device (grid of the persistent kernels)
+    // options (spk_set_option)
+    int leaf_queue = 0;                    // SPK_OPT_LEAF_QUEUE (off: slower on the measured workloads)
+    long long wait_budget = WAIT_BUDGET;   // SPK_OPT_WAIT_BUDGET
+    int stall_test = -1;                   // SPK_OPT_STALL_TEST
+    int tc_schur_m = TC_SCHUR_M, tc_trail_rows = TC_TRAIL_ROWS;
     std::string err;
 
     // launch accounting and optional per-class event timing
@@ -594,7 +612,7 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc, bool sym
         for (int i = 0; i < nfr; ++i) {
             const HFront& F = h->fronts[i];
             const int b0 = P.block0[i], nb = P.nblocks[i];
-            const bool packed = F.m >= TC_SCHUR_M || (nb > 1 && F.nf + F.m - P.blk_c1[b0] >= TC_TRAIL_ROWS);
+            const bool packed = F.m >= h->tc_schur_m || (nb > 1 && F.nf + F.m - P.blk_c1[b0] >= h->tc_trail_rows);
             if (!packed) continue;
             const int n2 = cdiv(F.m, spk::umma::TM);
             for (int b = b0; b < b0 + nb; ++b) {
@@ -635,6 +653,26 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc, bool sym
     const int nlev = h->nlevels;
     std::vector<std::vector<int>> at(nlev);
     for (int i = 0; i < nfr; ++i) at[h->fronts[i].level].push_back(i);
+    // the leaf queue: a front factored whole (one block of at most 32
+    // columns, m <= LF_M) whose children all are in the queue
+    std::vector<char> inq(nfr, 0);
+    for (int i = 0; i < nfr; ++i) {
+        const HFront& F = h->fronts[i];
+        inq[i] = P.nblocks[i] == 1 && F.nf <= 32 && F.m <= spk::LF_M;
+    }
+    for (int l = 0; l < nlev; ++l)   // children before parents
+        for (int i : at[l])
+            if (!inq[i] && h->fronts[i].parent >= 0) inq[h->fronts[i].parent] = 0;
+    P.q_deps.assign(nfr, 0);
+    for (int l = 0; l < nlev; ++l)
+        for (int i : at[l])
+            if (inq[i]) {
+                const int par = h->fronts[i].parent;
+                P.q_order.push_back(i);
+                P.q_parent.push_back(par >= 0 && inq[par] ? par : -1);
+                if (par >= 0 && inq[par]) ++P.q_deps[par];
+            }
+    P.nq = (int)P.q_order.size();
     P.levels.assign(nlev, LevelPlan());
     for (int l = 0; l < nlev; ++l) {
         LevelPlan& L = P.levels[l];
@@ -685,20 +723,29 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc, bool sym
             }
             add_launch(&P, L.front_l21, ids, tbig, fbig, wbig);
         }
-        std::vector<char> leafF(nid, 0);   // factored whole by k_leaf_factor
+        std::vector<char> leafF(nid, 0);   // factored whole by k_leaf_factor or k_leaf_queue
         {
-            std::vector<int> tlf(nid);
+            std::vector<int> tlf(nid), tlq(nid);
             std::vector<double> flf(nid), wlf(nid);
             for (size_t k = 0; k < nid; ++k) {
                 const HFront& F = h->fronts[ids[k]];
                 leafF[k] = P.nblocks[ids[k]] == 1 && F.nf <= 32 && F.m <= spk::LF_M;
-                tlf[k] = leafF[k] ? 1 : 0;
                 const double nf = F.nf, m = F.m;
                 flf[k] = sym ? 2.0 * nf * nf * nf + nf * nf * m + m * (m + 1.0) * nf
                              : 2.0 * nf * nf * nf + 3.0 * nf * nf * m + 2.0 * m * m * nf;
                 wlf[k] = nf * nf + 2.0 * nf * m + m * m;
             }
-            add_launch(&P, L.leaf_factor, ids, tlf, flf, wlf);
+            for (int c = 0; c < spk::LF_CLASSES; ++c) {
+                for (size_t k = 0; k < nid; ++k) {
+                    const bool in_class = leafF[k] && spk::leaf_class(h->fronts[ids[k]].nf) == c;
+                    tlf[k] = in_class && !inq[ids[k]] ? 1 : 0;
+                    tlq[k] = in_class && inq[ids[k]] ? 1 : 0;
+                }
+                add_launch(&P, L.leaf_factor[c], ids, tlf, flf, wlf);
+                add_launch(&P, L.leaf_q[c], ids, tlq, flf, wlf);
+                P.q_flops += L.leaf_q[c].flops;
+                P.q_words += L.leaf_q[c].words;
+            }
         }
         std::vector<char> wide(maxb, 0);   // a block of the step is wider than 64 columns
         for (int id : ids)
@@ -817,7 +864,8 @@ static int upload_structure(spk_handle* h) {
     if ((rc = upload(h, &h->d_rel, h->rel))) return rc;
     CU(h, cudaMalloc((void**)&h->d_ipiv, sizeof(int) * std::max<i64>(h->n, 1)));
     CU(h, cudaMalloc((void**)&h->d_bmap, sizeof(int) * std::max<i64>(h->n, 1)));
-    CU(h, cudaMalloc((void**)&h->d_info, 2 * sizeof(int)));   // first singular piece, tensor-core timeout
+    // first singular piece, tensor-core wait timeout, leaf-queue wait timeout
+    CU(h, cudaMalloc((void**)&h->d_info, 3 * sizeof(int)));
     return SPK_OK;
 }
 
@@ -877,6 +925,11 @@ static int ensure_plan(spk_handle* h) {
     if ((rc = upload(h, &P.d_inv_ids, P.inv_ids))) return rc;
     if ((rc = upload(h, &P.d_sched_ids, P.sched_ids))) return rc;
     if ((rc = upload(h, &P.d_sched_prefix, P.sched_prefix))) return rc;
+    if ((rc = upload(h, &P.d_q_order, P.q_order))) return rc;
+    if ((rc = upload(h, &P.d_q_parent, P.q_parent))) return rc;
+    if ((rc = upload(h, &P.d_q_deps0, P.q_deps))) return rc;
+    if ((rc = upload(h, &P.d_q_deps, P.q_deps))) return rc;
+    CU(h, cudaMalloc((void**)&P.d_q_next, sizeof(int)));
     spk::Sched& S = P.sched;
     S.fronts = P.d_fronts;
     S.xsuper = h->d_xs;
@@ -899,8 +952,22 @@ static int ensure_plan(spk_handle* h) {
                                (int)panel_smem<T, BM>()));
     CU(h, cudaFuncSetAttribute(spk::k_block_inv<T, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)sweep_smem<T, BM>(1)));
-    CU(h, cudaFuncSetAttribute(spk::k_leaf_factor<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)spk::LeafSmem<T>::bytes));
+    CU(h, cudaFuncSetAttribute(spk::k_leaf_factor<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)spk::LeafSmem<T, 4>::bytes));
+    CU(h, cudaFuncSetAttribute(spk::k_leaf_factor<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)spk::LeafSmem<T, 8>::bytes));
+    CU(h, cudaFuncSetAttribute(spk::k_leaf_factor<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)spk::LeafSmem<T, 16>::bytes));
+    CU(h, cudaFuncSetAttribute(spk::k_leaf_factor<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)spk::LeafSmem<T, 32>::bytes));
+    CU(h, cudaFuncSetAttribute(spk::k_leaf_queue<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)spk::LeafSmem<T, 32>::bytes));
+    {   // the queue's persistent grid: every CTA the SMs hold at once
+        int per_sm = 0;
+        CU(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, spk::k_leaf_queue<T>, 32 * spk::LF_WARPS,
+                                                            spk::LeafSmem<T, 32>::bytes));
+        P.q_grid = std::max(1, std::min(h->nsm * std::max(per_sm, 1), spk::cdiv(std::max(P.nq, 1), spk::LF_WARPS)));
+    }
     CU(h, cudaFuncSetAttribute(spk::k_front_solve<T, true, spk::FC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)spk::FcSmem<T>::bytes));
     CU(h, cudaFuncSetAttribute(spk::k_front_solve<T, false, spk::FC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -947,8 +1014,9 @@ static int ensure_plan(spk_handle* h) {
 }
 
 static void free_plan(Plan& P) {
-    void* ptrs[] = {P.d_fronts, P.d_blk_c0, P.d_blk_c1, P.d_blk_p0, P.d_blk_np, P.d_blk_inv2, P.d_blk_lpack, P.d_blk_upack,
-                    P.d_blk_front, P.d_inv_ids, P.d_sched_ids, P.d_sched_prefix};
+    void* ptrs[] = {P.d_fronts,     P.d_blk_c0,      P.d_blk_c1,   P.d_blk_p0,     P.d_blk_np,    P.d_blk_inv2,
+                    P.d_blk_lpack,  P.d_blk_upack,   P.d_blk_front, P.d_inv_ids,   P.d_sched_ids, P.d_sched_prefix,
+                    P.d_q_order,    P.d_q_parent,    P.d_q_deps0,  P.d_q_deps,     P.d_q_next};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     P = Plan();
@@ -1021,6 +1089,20 @@ static cudaError_t launch_chained(void (*kern)(KArgs...), int grid, int block, s
     return cudaLaunchKernelEx(&cfg, kern, ((KArgs)args)...);
 }
 
+// k_leaf_factor of width class c over the fronts of `la`.
+template <typename T>
+static cudaError_t launch_leaf(int c, const spk::Launch& la, T* fac, int* ipiv, int* info, const spk::Sched& S,
+                               cudaStream_t st) {
+    const int grid = (la.count + spk::LF_WARPS - 1) / spk::LF_WARPS, block = 32 * spk::LF_WARPS;
+    switch (c) {
+    case 0: spk::k_leaf_factor<T, 4><<<grid, block, spk::LeafSmem<T, 4>::bytes, st>>>(fac, ipiv, info, S, la); break;
+    case 1: spk::k_leaf_factor<T, 8><<<grid, block, spk::LeafSmem<T, 8>::bytes, st>>>(fac, ipiv, info, S, la); break;
+    case 2: spk::k_leaf_factor<T, 16><<<grid, block, spk::LeafSmem<T, 16>::bytes, st>>>(fac, ipiv, info, S, la); break;
+    default: spk::k_leaf_factor<T, 32><<<grid, block, spk::LeafSmem<T, 32>::bytes, st>>>(fac, ipiv, info, S, la); break;
+    }
+    return cudaGetLastError();
+}
+
 template <typename T>
 static int factor_launches(spk_handle* h) {
     constexpr int BM = spk::BlockMax<T>::value;
@@ -1050,6 +1132,17 @@ static int factor_launches(spk_handle* h) {
                                                                                   PL.d_blk_front, ent);
         }
     };
+    const bool queue = h->leaf_queue != 0 && PL.nq > 0;
+    if (queue) {   // the bottom subtrees first, in one persistent launch
+        CU(h, cudaMemcpyAsync(PL.d_q_deps, PL.d_q_deps0, sizeof(int) * h->fronts.size(), cudaMemcpyDeviceToDevice,
+                              h->stream));
+        CU(h, cudaMemsetAsync(PL.d_q_next, 0, sizeof(int), h->stream));
+        LaunchScope ls(h, SPK_K_GETRF, PL.q_flops, PL.q_words * sizeof(T));
+        const unsigned budget = (unsigned)std::min<long long>(h->wait_budget, 0xffffffffLL);
+        spk::k_leaf_queue<T><<<PL.q_grid, 32 * spk::LF_WARPS, spk::LeafSmem<T, 32>::bytes, h->stream>>>(
+            fac, h->d_ipiv, h->d_info, S, PL.d_q_order, PL.d_q_parent, PL.nq, PL.d_q_next, PL.d_q_deps, budget,
+            h->stall_test, h->d_info + 2);
+    }
     for (size_t lvl = 0; lvl < PL.levels.size(); ++lvl) {
         const LevelPlan& P = PL.levels[lvl];
         if (ahead && (int)lvl == PL.inv_split && PL.inv_off[0][3] > PL.inv_off[0][0]) {
@@ -1060,11 +1153,15 @@ static int factor_launches(spk_handle* h) {
             CU(h, cudaEventRecord(h->evI, h->side2));
             pending_inv = true;
         }
-        if (P.leaf_factor.tiles > 0) {
-            LaunchScope ls(h, SPK_K_GETRF, P.leaf_factor.flops, P.leaf_factor.words * sizeof(T));
-            spk::k_leaf_factor<T><<<(P.leaf_factor.count + spk::LF_WARPS - 1) / spk::LF_WARPS, 32 * spk::LF_WARPS,
-                                    spk::LeafSmem<T>::bytes, h->stream>>>(fac, h->d_ipiv, h->d_info, S,
-                                                                          launch_of(PL, P.leaf_factor));
+        for (int c = 0; c < spk::LF_CLASSES; ++c) {
+            if (P.leaf_factor[c].tiles > 0) {
+                LaunchScope ls(h, SPK_K_GETRF, P.leaf_factor[c].flops, P.leaf_factor[c].words * sizeof(T));
+                CU(h, launch_leaf<T>(c, launch_of(PL, P.leaf_factor[c]), fac, h->d_ipiv, h->d_info, S, h->stream));
+            }
+            if (!queue && P.leaf_q[c].tiles > 0) {
+                LaunchScope ls(h, SPK_K_GETRF, P.leaf_q[c].flops, P.leaf_q[c].words * sizeof(T));
+                CU(h, launch_leaf<T>(c, launch_of(PL, P.leaf_q[c]), fac, h->d_ipiv, h->d_info, S, h->stream));
+            }
         }
         for (size_t t = 0; t < P.blu.size(); ++t) {
             const int bw = P.blu[t].bw;
@@ -1162,7 +1259,7 @@ static int factor_launches(spk_handle* h) {
 
 template <typename T>
 static int run_factor(spk_handle* h) {
-    static const int init[2] = {INT_MAX, 0};
+    static const int init[3] = {INT_MAX, 0, 0};
     CU(h, cudaMemcpyAsync(h->d_info, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
     return via_graph(h, h->g_factor[graph_index<T>(h)], [&] { return factor_launches<T>(h); });
 }
@@ -1726,11 +1823,16 @@ int spk_factor(spk_handle* h, int precision, int64_t* first_singular) {
         if (!float_storage(h, precision).loaded && (rc = load_into<float>(h))) return rc;
         if ((rc = run_factor<float>(h))) return rc;
     }
-    int info2[2] = {INT_MAX, 0};
+    int info2[3] = {INT_MAX, 0, 0};
     CU(h, cudaMemcpyAsync(info2, h->d_info, sizeof(info2), cudaMemcpyDeviceToHost, h->stream));
     CU(h, cudaStreamSynchronize(h->stream));
     const int info = info2[0];
-    if (info2[1]) return set_err(h, SPK_ECUDA, "spk_factor: a tensor-core wait timed out");
+    if (info2[1] || info2[2]) {   // the factors are invalid; the next factor reassembles A
+        if (is_fp64(precision)) storage<double>(h).loaded = storage<double>(h).factored = false;
+        else float_storage(h, precision).loaded = float_storage(h, precision).factored = false;
+        return set_err(h, SPK_ETIMEOUT, info2[2] ? "spk_factor: a leaf-queue dependency wait timed out"
+                                                 : "spk_factor: a tensor-core wait timed out");
+    }
     if (is_fp64(precision)) { storage<double>(h).loaded = false; storage<double>(h).factored = true; }
     else { float_storage(h, precision).loaded = false; float_storage(h, precision).factored = true; }
     if (info != INT_MAX) {
@@ -1742,6 +1844,146 @@ int spk_factor(spk_handle* h, int precision, int64_t* first_singular) {
     return SPK_OK;
 }
 
+
+// Drop what depends on the float plans' tensor-core partition: the plans,
+// their packs, graphs and factors (the next factor reassembles A).
+static void reset_float_plans(spk_handle* h) {
+    for (int y = 0; y < 2; ++y) {
+        free_plan(h->plan[1 + 2 * y]);
+        for (Storage<float>* S : {&h->s32[y], &h->s16[y]}) {
+            if (S->pack) cudaFree(S->pack);
+            S->pack = nullptr;
+            S->loaded = S->factored = false;
+        }
+    }
+    for (GraphRec& g : h->g_factor) drop_graph(g);
+    drop_solve_graphs(h);
+}
+
+int spk_set_option(spk_handle* h, int option, int64_t value) {
+    int rc = check_h(h);
+    if (rc) return rc;
+    switch (option) {
+    case SPK_OPT_LEAF_QUEUE:
+        if (value != 0 && value != 1) break;
+        h->leaf_queue = (int)value;
+        for (GraphRec& g : h->g_factor) drop_graph(g);
+        return SPK_OK;
+    case SPK_OPT_WAIT_BUDGET:
+        if (value < 1 || value > 0xffffffffLL) break;
+        h->wait_budget = value;
+        for (GraphRec& g : h->g_factor) drop_graph(g);
+        return SPK_OK;
+    case SPK_OPT_STALL_TEST:
+        if (value < -1 || value > INT_MAX) break;
+        h->stall_test = (int)value;
+        for (GraphRec& g : h->g_factor) drop_graph(g);
+        return SPK_OK;
+    case SPK_OPT_TC_SCHUR_M:
+    case SPK_OPT_TC_TRAIL_ROWS: {
+        if (value < 1 || value > INT_MAX) break;
+        int& field = option == SPK_OPT_TC_SCHUR_M ? h->tc_schur_m : h->tc_trail_rows;
+        if (field != (int)value) {
+            field = (int)value;
+            reset_float_plans(h);
+        }
+        return SPK_OK;
+    }
+    default:
+        break;
+    }
+    return set_err(h, SPK_EARG, "spk_set_option: unknown option or value out of range");
+}
+
+int spk_get_option(spk_handle* h, int option, int64_t* value) {
+    int rc = check_h(h);
+    if (rc) return rc;
+    if (!value) return set_err(h, SPK_EARG, "spk_get_option: value is NULL");
+    switch (option) {
+    case SPK_OPT_LEAF_QUEUE: *value = h->leaf_queue; return SPK_OK;
+    case SPK_OPT_WAIT_BUDGET: *value = h->wait_budget; return SPK_OK;
+    case SPK_OPT_STALL_TEST: *value = h->stall_test; return SPK_OK;
+    case SPK_OPT_TC_SCHUR_M: *value = h->tc_schur_m; return SPK_OK;
+    case SPK_OPT_TC_TRAIL_ROWS: *value = h->tc_trail_rows; return SPK_OK;
+    default: return set_err(h, SPK_EARG, "spk_get_option: unknown option");
+    }
+}
+
+}  // extern "C"
+
+// Factor time of the current options: `reps` timed factorisations (CUDA
+// events on the handle's stream) after one untimed, each of freshly
+// assembled values; the median.
+template <typename T>
+static int time_factor(spk_handle* h, int reps, double* ms) {
+    cudaEvent_t e0, e1;
+    CU(h, cudaEventCreate(&e0));
+    CU(h, cudaEventCreate(&e1));
+    std::vector<double> t;
+    int rc = SPK_OK;
+    for (int r = 0; r <= reps && rc == SPK_OK; ++r) {
+        if ((rc = load_into<T>(h))) break;
+        if (cudaEventRecord(e0, h->stream) != cudaSuccess) { rc = set_err(h, SPK_ECUDA, "cudaEventRecord"); break; }
+        if ((rc = run_factor<T>(h))) break;
+        if (cudaEventRecord(e1, h->stream) != cudaSuccess) { rc = set_err(h, SPK_ECUDA, "cudaEventRecord"); break; }
+        int info[3] = {INT_MAX, 0, 0};
+        float f = 0.f;
+        if (cudaMemcpyAsync(info, h->d_info, sizeof(info), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+            cudaStreamSynchronize(h->stream) != cudaSuccess || cudaEventElapsedTime(&f, e0, e1) != cudaSuccess) {
+            rc = set_err(h, SPK_ECUDA, "spk_autotune: timing failed");
+            break;
+        }
+        if (info[1] || info[2]) rc = set_err(h, SPK_ETIMEOUT, "spk_autotune: a device wait timed out");
+        if (r > 0) t.push_back(f);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    std::sort(t.begin(), t.end());
+    *ms = t[t.size() / 2];
+    return SPK_OK;
+}
+
+extern "C" {
+
+int spk_autotune(spk_handle* h, int precision, int reps, double* best_ms) {
+    int rc = check_h(h);
+    if (rc) return rc;
+    if (!valid_precision(precision) || reps < 1) return set_err(h, SPK_EARG, "spk_autotune: bad arguments");
+    if (!h->have_values) return set_err(h, SPK_ESEQ, "Sequence error. Matrix input not done yet.");
+    if (h->prof_mask) return set_err(h, SPK_ESEQ, "spk_autotune: event timing (spk_profile) is on");
+    select_form(h, precision);
+    const bool f64 = is_fp64(precision);
+    auto measure = [&](double* ms) { return f64 ? time_factor<double>(h, reps, ms) : time_factor<float>(h, reps, ms); };
+    // the leaf queue on or off
+    double best = 0.0, ms = 0.0;
+    int best_q = h->leaf_queue;
+    for (int q = 0; q < 2; ++q) {
+        if ((rc = spk_set_option(h, SPK_OPT_LEAF_QUEUE, q))) return rc;
+        if ((rc = measure(&ms))) return rc;
+        if (q == 0 || ms < best) { best = ms; best_q = q; }
+    }
+    if ((rc = spk_set_option(h, SPK_OPT_LEAF_QUEUE, best_q))) return rc;
+    if (!f64) {   // the tensor-core partition of the float forms
+        static const int cand[][2] = {{96, 128}, {64, 128}, {128, 128}, {192, 128}, {96, 256}, {128, 256}, {256, 256}};
+        const int s0 = h->tc_schur_m, t0 = h->tc_trail_rows;   // `best` was measured with these
+        int bs = s0, bt = t0;
+        for (const auto& c : cand) {
+            if (c[0] == s0 && c[1] == t0) continue;
+            if ((rc = spk_set_option(h, SPK_OPT_TC_SCHUR_M, c[0]))) return rc;
+            if ((rc = spk_set_option(h, SPK_OPT_TC_TRAIL_ROWS, c[1]))) return rc;
+            if ((rc = measure(&ms))) return rc;
+            if (ms < best) { best = ms; bs = c[0]; bt = c[1]; }
+        }
+        if ((rc = spk_set_option(h, SPK_OPT_TC_SCHUR_M, bs))) return rc;
+        if ((rc = spk_set_option(h, SPK_OPT_TC_TRAIL_ROWS, bt))) return rc;
+    }
+    // leave A assembled in the chosen form, ready for spk_factor
+    if ((rc = f64 ? load_into<double>(h) : load_into<float>(h))) return rc;
+    CU(h, cudaStreamSynchronize(h->stream));
+    if (best_ms) *best_ms = best;
+    return SPK_OK;
+}
 
 static int solve_impl(spk_handle* h, double* b, int64_t nrhs, int64_t ldb, int where, int precision, bool transpose) {
     int rc = check_h(h);

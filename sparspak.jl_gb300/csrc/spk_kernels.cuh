@@ -156,20 +156,20 @@ __device__ __forceinline__ int warp_first_max(unsigned long long key) {
 }
 
 // r[k] for a runtime k without indexing a register array dynamically: a
-// five-level tree of selects (depth 5 instead of a 31-long chain).
-template <typename T>
-__device__ __forceinline__ T pick32(const T (&r)[32], int k) {
-    T v16[16], v8[8], v4[4], v2[2];
+// tree of selects (depth log2 W instead of a W-long chain); W a power of 2.
+template <int W, typename T>
+__device__ __forceinline__ T pickw(const T (&r)[W], int k) {
+    if constexpr (W == 1) {
+        return r[0];
+    } else {
+        T h[W / 2];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v16[i] = (k & 16) ? r[i + 16] : r[i];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) v8[i] = (k & 8) ? v16[i + 8] : v16[i];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) v4[i] = (k & 4) ? v8[i + 4] : v8[i];
-#pragma unroll
-    for (int i = 0; i < 2; ++i) v2[i] = (k & 2) ? v4[i + 2] : v4[i];
-    return (k & 1) ? v2[1] : v2[0];
+        for (int i = 0; i < W / 2; ++i) h[i] = (k & (W / 2)) ? r[i + W / 2] : r[i];
+        return pickw<W / 2>(h, k);
+    }
 }
+template <typename T>
+__device__ __forceinline__ T pick32(const T (&r)[32], int k) { return pickw<32>(r, k); }
 
 // One right-looking LU sweep over the columns [0, ncols) of a register block
 // held one row per lane (rows/columns below 32).  For column k in piece
@@ -178,9 +178,10 @@ __device__ __forceinline__ T pick32(const T (&r)[32], int k) {
 // _luswap! of its U rows), column k scaled below the diagonal (ggetrf!
 // scaling, and the L-panel trsm 'r','u','n','n' for rows past the piece),
 // rank-1 update of rows and columns after k (ggetrf!, the U-panel trsm
-// 'r','l','t','u' and the block-local update).  `nrows` rows take part.
-template <typename T>
-__device__ bool warp_lu_sweep(T (&r)[32], int nrows, int ncols, const int* q0, int* piv, bool sym) {
+// 'r','l','t','u' and the block-local update).  `nrows` rows take part;
+// W (a power of 2, at most 32) bounds the columns held.
+template <typename T, int W>
+__device__ bool warp_lu_sweep(T (&r)[W], int nrows, int ncols, const int* q0, int* piv, bool sym) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     bool sing = false;
@@ -189,14 +190,14 @@ __device__ bool warp_lu_sweep(T (&r)[32], int nrows, int ncols, const int* q0, i
     for (int k = 0; k < ncols; ++k) {
         while (q0[pc + 1] <= k) ++pc;
         const int a = q0[pc], b = q0[pc + 1];
-        const T rk0 = pick32(r, k);
+        const T rk0 = pickw<W>(r, k);
         const int kp = warp_first_max(pivot_key(rk0, sym ? lane == k : (lane >= k && lane < b), lane == k));
         if (lane == 0) piv[k] = kp - a;
         const T pv = __shfl_sync(FULL, rk0, kp);
         if (pv != T(0)) {
             if (kp != k) {
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
+                for (int j = 0; j < W; ++j) {
                     const T vk = __shfl_sync(FULL, r[j], k), vp = __shfl_sync(FULL, r[j], kp);
                     if (j >= a) {
                         if (lane == k) r[j] = vp;
@@ -207,19 +208,19 @@ __device__ bool warp_lu_sweep(T (&r)[32], int nrows, int ncols, const int* q0, i
             const T inv = T(1) / pv;
             if (lane > k && lane < nrows) {
 #pragma unroll
-                for (int j = 0; j < 32; ++j)
+                for (int j = 0; j < W; ++j)
                     if (j == k) r[j] *= inv;
             }
         } else {
             sing = true;
         }
-        const T lk = pick32(r, k);
-        T u[32];
+        const T lk = pickw<W>(r, k);
+        T u[W];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) u[j] = __shfl_sync(FULL, r[j], k);
+        for (int j = 0; j < W; ++j) u[j] = __shfl_sync(FULL, r[j], k);
         if (lane > k && lane < nrows) {
 #pragma unroll
-            for (int j = 0; j < 32; ++j)
+            for (int j = 0; j < W; ++j)
                 if (j > k) r[j] -= lk * u[j];
         }
     }
@@ -235,17 +236,17 @@ __device__ bool warp_lu_sweep(T (&r)[32], int nrows, int ncols, const int* q0, i
 // trsm 'r','u','n','n' for rows below it) and the rank-1 update covers rows
 // and columns after k (ggetrf!, the U-panel trsm 'r','l','t','u' and the
 // block-local update).  Columns left of the piece are never interchanged.
-template <typename T>
+template <typename T, int W = 32>
 __device__ bool warp_block_lu32(T* A, int lda, int bw, const int* q0, int np, int* piv, bool sym) {
     const int lane = threadIdx.x & 31;
     (void)np;
-    T r[32];
+    T r[W];
 #pragma unroll
-    for (int j = 0; j < 32; ++j) r[j] = (lane < bw && j < bw) ? A[j * lda + lane] : T(0);
-    const bool sing = warp_lu_sweep(r, bw, bw, q0, piv, sym);
+    for (int j = 0; j < W; ++j) r[j] = (lane < bw && j < bw) ? A[j * lda + lane] : T(0);
+    const bool sing = warp_lu_sweep<T, W>(r, bw, bw, q0, piv, sym);
     if (lane < bw) {
 #pragma unroll
-        for (int j = 0; j < 32; ++j)
+        for (int j = 0; j < W; ++j)
             if (j < bw) A[j * lda + lane] = r[j];
     }
     __syncwarp();
@@ -1543,51 +1544,64 @@ __device__ __forceinline__ ScatterRow scatter_row(const Sched& S, const DFront& 
 // order of the panel sweeps, and the Schur complement L21 U12 (k in order)
 // scatter-subtracted into the ancestors like k_schur.  Replaces, for these
 // fronts, k_block_lu_small + k_block_panel + k_schur (three launches whose
-// CTAs would be mostly idle on fronts this small).
-constexpr int LF_M = 32, LF_WARPS = 4, LF_LD = 33;
-template <typename T> struct LeafSmem {
-    static constexpr size_t warp_bytes = (size_t)(32 + LF_M) * LF_LD * sizeof(T) + LF_M * sizeof(ScatterRow) +
-                                         32 * sizeof(T) + (33 + 3 * 32) * sizeof(int);
-    static constexpr size_t bytes = LF_WARPS * ((warp_bytes + 15) / 16 * 16);
+// CTAs would be mostly idle on fronts this small).  Each launch holds fronts
+// of one width class W (block width <= W, W = 4, 8, 16 or 32), so that the
+// unrolled register loops and the shared memory are sized to the class.
+constexpr int LF_M = 32, LF_WARPS = 4;
+constexpr int LF_CLASSES = 4;   // W = 4 << class
+__host__ __device__ constexpr int leaf_class(int bw) { return bw <= 4 ? 0 : bw <= 8 ? 1 : bw <= 16 ? 2 : 3; }
+template <typename T, int W> struct LeafSmem {
+    static constexpr int LD = W + 1;
+    static constexpr size_t warp_bytes = (((size_t)(W + LF_M) * LD + W) * sizeof(T) + LF_M * sizeof(ScatterRow) +
+                                          (W + 1 + 3 * W) * sizeof(int) + 15) / 16 * 16;
+    static constexpr size_t bytes = LF_WARPS * warp_bytes;
 };
 
-template <typename T>
-__global__ void __launch_bounds__(32 * LF_WARPS) k_leaf_factor(T* fac, int* ipiv, int* info, Sched S, Launch L) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char* base = smem_raw + (size_t)warp * ((LeafSmem<T>::warp_bytes + 15) / 16 * 16);
+// A load of factor data that other CTAs of the same launch may have updated
+// (COH: at L2, bypassing the SM's L1, which is not coherent across SMs).
+template <bool COH, typename T>
+__device__ __forceinline__ T ld_fac(const T* p) {
+    if constexpr (COH) return __ldcg(p);
+    else return *p;
+}
+
+// One small front (block width <= W) factored whole by the calling warp;
+// `base` is the warp's slice of LeafSmem<T, W>.
+template <typename T, bool COH, int W>
+__device__ __forceinline__ void leaf_front(T* fac, int* ipiv, int* info, const Sched& S, const DFront& F,
+                                           unsigned char* base) {
+    constexpr int LD = LeafSmem<T, W>::LD;
+    const int lane = threadIdx.x & 31;
     ScatterRow* tab = reinterpret_cast<ScatterRow*>(base);
-    T* sD = reinterpret_cast<T*>(tab + LF_M);          // diagonal block, D(i, j) at sD[j * LF_LD + i]
-    T* sL = sD + 32 * LF_LD;                           // L21 rows, L21(r, k) at sL[r * LF_LD + k]
-    T* srv = sL + LF_M * LF_LD;                        // 1 / U(k, k)
-    int* q0 = reinterpret_cast<int*>(srv + 32);
-    int* piv = q0 + 33;
-    int* gm = piv + 32;
-    int* pam = gm + 32;
-    const int idx = blockIdx.x * LF_WARPS + warp;
-    if (idx >= L.count) return;   // whole warp; the kernel has no CTA barrier
-    const DFront F = S.fronts[L.front_ids[idx]];
+    T* sD = reinterpret_cast<T*>(tab + LF_M);          // diagonal block, D(i, j) at sD[j * LD + i]
+    T* sL = sD + W * LD;                               // L21 rows, L21(r, k) at sL[r * LD + k]
+    T* srv = sL + LF_M * LD;                           // 1 / U(k, k)
+    int* q0 = reinterpret_cast<int*>(srv + W);
+    int* piv = q0 + W + 1;
+    int* gm = piv + W;
+    int* pam = gm + W;
     const int blk = F.block0, bw = F.nf, m = F.m;
     const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
     const bool sym = S.sym != 0;
     for (int k = lane; k <= np; k += 32) q0[k] = S.xsuper[p0 + k] - F.f;
     for (int j = 0; j < bw; ++j)   // symmetric form: the upper triangle mirrors the lower one
         if (lane < bw)
-            sD[j * LF_LD + lane] = (sym && lane < j) ? fac[F.loff + (ll)lane * F.ld + j] : fac[F.loff + (ll)j * F.ld + lane];
+            sD[j * LD + lane] = (sym && lane < j) ? ld_fac<COH>(fac + F.loff + (ll)lane * F.ld + j)
+                                                  : ld_fac<COH>(fac + F.loff + (ll)j * F.ld + lane);
     for (int x = lane; x < m; x += 32) tab[x] = scatter_row<T>(S, F, x);
     __syncwarp();
     // block LU (ggetrf! pivots inside each piece; none in the symmetric form)
-    const bool sing = warp_block_lu32(sD, LF_LD, bw, q0, np, piv, sym);
+    const bool sing = warp_block_lu32<T, W>(sD, LD, bw, q0, np, piv, sym);
     for (int j = 0; j < bw; ++j)
-        if (lane < bw) fac[F.loff + (ll)j * F.ld + lane] = sD[j * LF_LD + lane];
+        if (lane < bw) fac[F.loff + (ll)j * F.ld + lane] = sD[j * LD + lane];
     if (lane < bw) {
         ipiv[F.f + lane] = piv[lane];
-        srv[lane] = rcp_rn(sD[lane * LF_LD + lane]);   // as the panel's 1 / U(k, k)
+        srv[lane] = rcp_rn(sD[lane * LD + lane]);   // as the panel's 1 / U(k, k)
     }
     if (lane == 0 && sing) {
         for (int pc = 0; pc < np; ++pc) {
             bool z = false;
-            for (int k = q0[pc]; k < q0[pc + 1]; ++k) z |= sD[k * LF_LD + k] == T(0);
+            for (int k = q0[pc]; k < q0[pc + 1]; ++k) z |= sD[k * LD + k] == T(0);
             if (z) { atomicMin(info, p0 + pc + 1); break; }
         }
     }
@@ -1605,68 +1619,65 @@ __global__ void __launch_bounds__(32 * LF_WARPS) k_leaf_factor(T* fac, int* ipiv
         }
     }
     __syncwarp();
-    // L21 rows: x := x U^-1 (left-looking: entry j gets k = 0, 1, .. then its scaling)
-    for (int r = lane; r < m; r += 32) {
-        T x[32];
+    // L21 rows (m <= 32: a lane per row): x := x U^-1 (left-looking: entry j
+    // gets k = 0, 1, .. then its scaling)
+    const int r = lane;
+    if (r < m) {
+        T x[W];
 #pragma unroll
-        for (int k = 0; k < 32; ++k) x[k] = k < bw ? fac[F.loff + (ll)k * F.ld + bw + r] : T(0);
+        for (int k = 0; k < W; ++k) x[k] = k < bw ? ld_fac<COH>(fac + F.loff + (ll)k * F.ld + bw + r) : T(0);
 #pragma unroll
-        for (int j = 0; j < 32; ++j)
+        for (int j = 0; j < W; ++j)
             if (j < bw) {
 #pragma unroll
-                for (int k = 0; k < j; ++k) x[j] -= x[k] * sD[j * LF_LD + k];
+                for (int k = 0; k < j; ++k) x[j] -= x[k] * sD[j * LD + k];
                 x[j] *= srv[j];
             }
 #pragma unroll
-        for (int k = 0; k < 32; ++k)
+        for (int k = 0; k < W; ++k)
             if (k < bw) {
                 fac[F.loff + (ll)k * F.ld + bw + r] = x[k];
-                sL[r * LF_LD + k] = x[k];
+                sL[r * LD + k] = x[k];
             }
     }
-    // U12 columns: y := inv(L) P y (symmetric form: y_k = U(k, k) L21(c, k),
-    // from this lane's own L21 row); then the Schur complement, a lane per column
-    T y[2][32];
+    // U12 columns, a lane per column c: y := inv(L) P y (symmetric form:
+    // y_k = U(k, k) L21(c, k), from this lane's own L21 row)
+    const int c = lane;
+    T y[W];
+    if (sym) {
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int c = lane + 32 * h;
-        if (sym) {
+        for (int k = 0; k < W; ++k) y[k] = (c < m && k < bw) ? sD[k * LD + k] * sL[c * LD + k] : T(0);
+    } else {
 #pragma unroll
-            for (int k = 0; k < 32; ++k) y[h][k] = (c < m && k < bw) ? sD[k * LF_LD + k] * sL[c * LF_LD + k] : T(0);
-        } else {
+        for (int k = 0; k < W; ++k) y[k] = (c < m && k < bw) ? ld_fac<COH>(fac + F.uoff + (ll)gm[k] * m + c) : T(0);
 #pragma unroll
-            for (int k = 0; k < 32; ++k) y[h][k] = (c < m && k < bw) ? fac[F.uoff + (ll)gm[k] * m + c] : T(0);
+        for (int i = 0; i < W; ++i)
+            if (i < bw) {
 #pragma unroll
-            for (int i = 0; i < 32; ++i)
-                if (i < bw) {
-#pragma unroll
-                    for (int k = 0; k < i; ++k) {
-                        const T l = k < pam[i] ? sD[k * LF_LD + gm[i]] : sD[k * LF_LD + i];
-                        y[h][i] -= l * y[h][k];
-                    }
+                for (int k = 0; k < i; ++k) {
+                    const T l = k < pam[i] ? sD[k * LD + gm[i]] : sD[k * LD + i];
+                    y[i] -= l * y[k];
                 }
-        }
-        if (c < m)
-#pragma unroll
-            for (int k = 0; k < 32; ++k)
-                if (k < bw) fac[F.uoff + (ll)k * m + c] = y[h][k];
+            }
     }
-    __syncwarp();
-    for (int r = 0; r < m; ++r) {
+    if (c < m)
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int c = lane + 32 * h;
-            if (c >= m || (sym && r < c)) continue;   // the symmetric form forms the lower part only
+        for (int k = 0; k < W; ++k)
+            if (k < bw) fac[F.uoff + (ll)k * m + c] = y[k];
+    __syncwarp();
+    // Schur complement, a lane per column c, rows in order
+    if (c < m) {
+        for (int rr = sym ? c : 0; rr < m; ++rr) {   // the symmetric form forms the lower part only
             T acc = T(0);
 #pragma unroll
-            for (int k = 0; k < 32; ++k)
-                if (k < bw) acc += sL[r * LF_LD + k] * y[h][k];
-            if (r >= c) {   // L entry of the front of R_F[c]
+            for (int k = 0; k < W; ++k)
+                if (k < bw) acc += sL[rr * LD + k] * y[k];
+            if (rr >= c) {   // L entry of the front of R_F[c]
                 const ScatterRow& Cc = tab[c];
-                const int p = S.rel[Cc.rel0 + r];
+                const int p = S.rel[Cc.rel0 + rr];
                 if (Cc.pos >= 0 && p >= 0) atomicAdd(&fac[Cc.loff + (ll)Cc.pos * Cc.ld + p], -acc);
-            } else if (!sym) {   // entry of the front of R_F[r] (the symmetric form keeps no U updates)
-                const ScatterRow& R = tab[r];
+            } else {   // entry of the front of R_F[rr] (not in the symmetric form)
+                const ScatterRow& R = tab[rr];
                 const int p = S.rel[R.rel0 + c];
                 if (R.pos >= 0 && p >= 0) {
                     const ll addr = p < R.nf ? R.loff + (ll)p * R.ld + R.pos : R.uoff + (ll)R.pos * R.m + (p - R.nf);
@@ -1674,6 +1685,67 @@ __global__ void __launch_bounds__(32 * LF_WARPS) k_leaf_factor(T* fac, int* ipiv
                 }
             }
         }
+    }
+}
+
+template <typename T, int W>
+__global__ void __launch_bounds__(32 * LF_WARPS) k_leaf_factor(T* fac, int* ipiv, int* info, Sched S, Launch L) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int warp = threadIdx.x >> 5;
+    unsigned char* base = smem_raw + (size_t)warp * LeafSmem<T, W>::warp_bytes;
+    const int idx = blockIdx.x * LF_WARPS + warp;
+    if (idx >= L.count) return;   // whole warp; the kernel has no CTA barrier
+    leaf_front<T, false, W>(fac, ipiv, info, S, S.fronts[L.front_ids[idx]], base);
+}
+
+// The bottom subtrees of small fronts (every front of the subtree factored
+// whole, as by k_leaf_factor) in one persistent launch: a merged work queue
+// in level order.  A warp takes the next front (atomic counter `next`),
+// waits until the front's children have signalled (deps[front] == 0; a
+// bounded spin of `budget` polls, after which it records a timeout in *err
+// and goes on, so that the launch always ends), factors it, makes its writes
+// visible (fence) and signals its parent (qparent[position], -1 when the
+// parent is factored by the level launches).  A front's children come
+// earlier in the queue, so every front waited on is held by a running warp.
+// `stall` (a queue position, or -1) makes that position's wait one that
+// nothing ends, so that the timeout path can be tested.  Shared memory is
+// sized for the widest class.
+template <typename T>
+__global__ void __launch_bounds__(32 * LF_WARPS) k_leaf_queue(T* fac, int* ipiv, int* info, Sched S, const int* order,
+                                                              const int* qparent, int nq, int* next, int* deps,
+                                                              unsigned budget, int stall, int* err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char* base = smem_raw + (size_t)warp * LeafSmem<T, 32>::warp_bytes;
+    for (;;) {
+        int pos = 0;
+        if (lane == 0) pos = atomicAdd(next, 1);
+        pos = __shfl_sync(0xffffffffu, pos, 0);
+        if (pos >= nq) break;
+        const int fid = order[pos];
+        if (lane == 0) {
+            const int done = pos == stall ? -1 : 0;   // deps never falls below 0
+            unsigned it = 0;
+            while (*reinterpret_cast<volatile int*>(deps + fid) > done) {
+                if (++it >= budget) {
+                    atomicExch(err, 1);
+                    break;
+                }
+                if (it > 32) __nanosleep(64);
+            }
+            __threadfence();
+        }
+        __syncwarp();
+        const DFront F = S.fronts[fid];
+        switch (leaf_class(F.nf)) {
+        case 0: leaf_front<T, true, 4>(fac, ipiv, info, S, F, base); break;
+        case 1: leaf_front<T, true, 8>(fac, ipiv, info, S, F, base); break;
+        case 2: leaf_front<T, true, 16>(fac, ipiv, info, S, F, base); break;
+        default: leaf_front<T, true, 32>(fac, ipiv, info, S, F, base); break;
+        }
+        __threadfence();
+        __syncwarp();
+        if (lane == 0 && qparent[pos] >= 0) atomicSub(deps + qparent[pos], 1);
     }
 }
 

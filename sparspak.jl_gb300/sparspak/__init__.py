@@ -11,7 +11,7 @@ libspk_gpu.so (include/spk_gpu.h); there is no CPU fallback.
 from . import gallery, graph, problem, sparse_solver
 from ._build import build
 from .csc import ldiv, ldiv_, sparspaklu, sparspaklu_
-from .device import ErrorException, NumericEngine, SingularException
+from .device import DeviceTimeoutError, ErrorException, NumericEngine, SingularException
 from .graph import (ETree, Graph, Ordering, isstructuresymmetric, makestructuresymmetric, mmd_, nd_graph, nd_grid,
                     nd_grid_batched)
 from .problem import (Grid, Problem, computeresidual, inaij_, inbi_, infullrhs_, insparse_, makegridproblem,
@@ -22,7 +22,7 @@ from .sparse_solver import (SparseSolver, factor_, findorder_, findorderperm_, g
 __all__ = [
     "build", "gallery", "graph", "problem", "sparse_solver",
     "ldiv", "ldiv_", "sparspaklu", "sparspaklu_",
-    "ErrorException", "NumericEngine", "SingularException",
+    "DeviceTimeoutError", "ErrorException", "NumericEngine", "SingularException",
     "ETree", "Graph", "Ordering", "isstructuresymmetric", "makestructuresymmetric", "mmd_", "nd_graph", "nd_grid",
     "nd_grid_batched",
     "Grid", "Problem", "computeresidual", "inaij_", "inbi_", "infullrhs_", "insparse_", "makegridproblem",

@@ -46,6 +46,9 @@ GPU_SYMBOLS = {
     "spk_refine": (ctypes.c_int, [VP, VP, VP, i64, i64, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                   ctypes.c_int, ctypes.POINTER(ctypes.c_int), PD]),
     "spk_measure_peaks": (ctypes.c_int, [PD, PD, PD]),
+    "spk_set_option": (ctypes.c_int, [VP, ctypes.c_int, i64]),
+    "spk_get_option": (ctypes.c_int, [VP, ctypes.c_int, P64]),
+    "spk_autotune": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int, PD]),
     "spk_refine_ex": (ctypes.c_int, [VP, VP, VP, i64, i64, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                      ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), PD,
                                      ctypes.POINTER(ctypes.c_int)]),
@@ -61,10 +64,13 @@ GPU_SYMBOLS = {
 }
 
 SPK_OK, SPK_EARG, SPK_ECUDA, SPK_ENOMEM, SPK_ESEQ, SPK_ESTRUCT, SPK_ESINGULAR, SPK_ENOCONV = 0, -1, -2, -3, -4, -5, -6, -7
+SPK_ETIMEOUT = -8
+# spk_set_option / spk_get_option
+OPTIONS = {"leaf_queue": 0, "wait_budget": 1, "stall_test": 2, "tc_schur_m": 3, "tc_trail_rows": 4}
 SPK_HOST, SPK_DEVICE = 0, 1
 KERNEL_CLASSES = ["assemble", "getrf", "panel", "trail", "schur", "fwd", "bwd", "permute", "residual", "blockinv",
                   "tc_trail", "tc_schur"]
-KERNEL_NAMES = {"assemble": "k_scatter_values", "getrf": "k_block_lu+k_block_lu_small+k_leaf_factor",
+KERNEL_NAMES = {"assemble": "k_scatter_values", "getrf": "k_block_lu+k_block_lu_small+k_leaf_factor+k_leaf_queue",
                 "panel": "k_block_panel",
                 "trail": "k_block_trail", "schur": "k_schur",
                 "fwd": "k_fwd+k_front_solve<fwd>+k_fwd_l21+k_solve_leaf<fwd>",

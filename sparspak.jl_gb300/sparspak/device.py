@@ -28,6 +28,11 @@ class SingularException(ErrorException):
         self.supernode = supernode
 
 
+class DeviceTimeoutError(ErrorException):
+    """A bounded device wait ran out (SPK_ETIMEOUT): the factors are invalid,
+    the CUDA context is still usable and the next factor reassembles A."""
+
+
 def _prec(p) -> int:
     """Precision code of 'fp64' / 'fp32' / 'bf16s', with '+spd' for the
     symmetric (Cholesky) form of SPD matrices, or an int code."""
@@ -94,6 +99,8 @@ class NumericEngine:
         msg = self._lib.spk_last_error(self._h).decode()
         if rc == N.SPK_ESINGULAR:
             raise SingularException(msg, None)
+        if rc == N.SPK_ETIMEOUT:
+            raise DeviceTimeoutError(f"{what}: {msg}")
         raise ErrorException(f"{what}: {msg}")
 
     def close(self):
@@ -209,6 +216,24 @@ class NumericEngine:
         self._check(self._lib.spk_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(f)),
                     "spk_stats")
         return {"fronts": a.value, "levels": b.value, "factor_entries": c.value, "lu_flops": f.value}
+
+    # -- options --------------------------------------------------------------
+    def set_option(self, name, value):
+        """Set a factorisation option (_native.OPTIONS: leaf_queue, wait_budget,
+        stall_test, tc_schur_m, tc_trail_rows); takes effect at the next factor."""
+        self._check(self._lib.spk_set_option(self._h, N.OPTIONS[name], int(value)), "spk_set_option")
+
+    def get_option(self, name):
+        v = ctypes.c_int64()
+        self._check(self._lib.spk_get_option(self._h, N.OPTIONS[name], ctypes.byref(v)), "spk_get_option")
+        return int(v.value)
+
+    def autotune(self, precision="fp32", reps=3):
+        """Time the option sets for the loaded values, keep the fastest and
+        return ({option: value}, best factor ms); A stays assembled."""
+        ms = ctypes.c_double()
+        self._check(self._lib.spk_autotune(self._h, _prec(precision), int(reps), ctypes.byref(ms)), "spk_autotune")
+        return {k: self.get_option(k) for k in ("leaf_queue", "tc_schur_m", "tc_trail_rows")}, ms.value
 
     # -- launch accounting ----------------------------------------------------
     def profile(self, classes=()):

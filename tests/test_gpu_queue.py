@@ -1,0 +1,138 @@
+"""The persistent leaf queue (k_leaf_queue), its bounded waits, and the
+option autotuner, through the C ABI.
+
+* Queue on and off (the default): the FP64 factors of grid Laplacians (MMD
+  and ND orderings, 2D and 3D), a convection-diffusion matrix, the batched
+  2D diffusion systems and the symmetric (SPD) form match the oracle's -
+  identical pivots, factors within 1e-12 - and the queue replaces launches.
+* The timeout path: a small wait budget and a stalled queue position make
+  spk_factor return SPK_ETIMEOUT (DeviceTimeoutError) without a fault; with
+  the defaults back the next factor is correct again.
+* spk_autotune chooses options from its set, leaves A assembled, and the
+  factor that follows refines to 1e-12.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import sparspak as S
+from sparspak.sparse_solver import _factor_, _inmatrix_, _matrix_arrays
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))
+
+
+def relres(A, x, b):
+    r = b - A @ x
+    return float(np.max(np.linalg.norm(r, axis=0) / np.linalg.norm(b, axis=0)))
+
+
+def _case(kind):
+    if kind == "laplace2d_mmd":
+        return S.gallery.laplacian((40, 40)), None
+    if kind == "laplace3d_nd":
+        return S.gallery.laplacian((20, 20, 20), shift=1e-3), S.nd_grid(20, 20, 20)
+    if kind == "convdiff_nd":
+        return S.gallery.convection_diffusion(k=16), S.nd_grid(16, 16, 16)
+    A, sizes = S.gallery.batched_diffusion(24, 12, 40, seed=2)
+    return A, S.nd_grid_batched(sizes)
+
+
+def _solver(A, of, **kw):
+    s = S.SparseSolver(A, **kw)
+    S.findorder_(s, of)
+    S.symbolicfactor_(s)
+    return s
+
+
+def _factor_with(s, A, **opts):
+    """Assemble A again and factor with the given options; the engine."""
+    _inmatrix_(s.slvr, A)
+    eng = s.slvr.engine
+    for k, v in opts.items():
+        eng.set_option(k, v)
+        assert eng.get_option(k) == v
+    eng.profile_reset()
+    _factor_(s.slvr)
+    return eng
+
+
+@pytest.mark.parametrize("kind", ["laplace2d_mmd", "laplace3d_nd", "convdiff_nd", "batched"])
+def test_leaf_queue_on_off_vs_oracle(kind):
+    A, of = _case(kind)
+    s = _solver(A, of)
+    o = oracle.OracleLU(s.slvr)
+    o.inmatrix_csc(*_matrix_arrays(A))
+    assert o.factor() == 0
+    b = S.gallery.random_rhs(A.shape[0], 2, seed=4)
+    xo = o.solve(b)
+    launches = {}
+    for q in (1, 0):
+        eng = _factor_with(s, A, leaf_queue=q)
+        launches[q] = eng.profile_read()["getrf"]["launches"]
+        assert np.array_equal(s.slvr.ipiv, o.ipiv), q
+        assert rel(s.slvr.lnz, o.lnz) <= 1e-12, q
+        assert rel(s.slvr.unz, o.unz[: s.slvr.unz.size]) <= 1e-12, q
+        x = eng.solve(np.array(b, order="F"))
+        assert rel(x, xo) < 1e-10
+        assert relres(A, x, b) <= 1e-12
+    print(f"{kind}: getrf-class launches with the queue {launches[1]}, without {launches[0]}")
+    assert launches[1] < launches[0], "the queue replaced no launches"
+
+
+def test_leaf_queue_spd_form_vs_oracle_cholesky():
+    A = S.gallery.laplacian((24, 24, 24), shift=1e-3)
+    s = _solver(A, S.nd_grid(24, 24, 24), spd=True)
+    o = oracle.OracleLU(s.slvr)
+    o.inmatrix_csc(*_matrix_arrays(A))
+    assert o.cholfactor() == 0
+    mask = o.lower_mask()
+    for q in (1, 0):
+        _factor_with(s, A, leaf_queue=q)
+        assert rel(s.slvr.lnz[mask], o.lnz[mask]) <= 1e-12, q
+
+
+def test_queue_wait_timeout_is_reported_and_recoverable():
+    # queue position 0 waits on a condition nothing sets; after 2000 polls it
+    # gives up, the factorisation reports the timeout and nothing faults
+    A = S.gallery.laplacian((32, 32))
+    s = _solver(A, S.nd_grid(32, 32, 1, leaf=16))
+    o = oracle.OracleLU(s.slvr)
+    o.inmatrix_csc(*_matrix_arrays(A))
+    assert o.factor() == 0
+    with pytest.raises(S.DeviceTimeoutError, match="leaf-queue"):
+        _factor_with(s, A, leaf_queue=1, wait_budget=2000, stall_test=0)
+    eng = s.slvr.engine
+    with pytest.raises(S.ErrorException, match="Factorization not done"):
+        eng.solve(np.ones(A.shape[0]))
+    eng.set_option("stall_test", -1)
+    eng.set_option("wait_budget", 1 << 20)
+    eng.factor("fp64")   # reassembles A: the timed-out factor left it invalid
+    assert np.array_equal(s.slvr.ipiv, o.ipiv)
+    assert rel(s.slvr.lnz, o.lnz) <= 1e-12
+    for bad in (("leaf_queue", 2), ("wait_budget", 0), ("stall_test", -2), ("tc_schur_m", 0)):
+        with pytest.raises(S.ErrorException):
+            eng.set_option(*bad)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_autotune_then_factor_and_refine(prec):
+    A = S.gallery.laplacian((28, 28, 28), shift=1e-3)
+    n = A.shape[0]
+    s = _solver(A, S.nd_grid(28, 28, 28), precision=prec)
+    _inmatrix_(s.slvr, A)
+    eng = s.slvr.engine
+    opts, ms = eng.autotune(prec, reps=2)
+    print(f"autotune {prec}: {opts}, best factor {ms:.3f} ms")
+    assert ms > 0 and opts["leaf_queue"] in (0, 1)
+    if prec == "fp32":
+        assert (opts["tc_schur_m"], opts["tc_trail_rows"]) in {(96, 128), (64, 128), (128, 128), (192, 128),
+                                                               (96, 256), (128, 256), (256, 256)}
+    eng.factor(prec)   # A was left assembled
+    b = S.gallery.random_rhs(n, 2, seed=8)
+    x = np.zeros_like(b, order="F")
+    it, rr = eng.refine(np.asfortranarray(b), x, prec, 1e-12, 20)
+    assert rr <= 1e-12 and relres(A, x, b) <= 1e-12
