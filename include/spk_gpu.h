@@ -306,12 +306,16 @@ int spk_measure_peaks(double* fp32_tflops, double* fp64_tflops, double* dmma_tfl
  *                        updates (default 96);
  *  SPK_OPT_TC_TRAIL_ROWS or one of several blocks with at least this many
  *                        rows below its first block (default 128).
+ *  SPK_OPT_TC_WIDE       1 (default): the tensor-core Schur complements in
+ *                        tiles of 128 x 256 (each staged L chunk serves two
+ *                        products); 0: tiles of 128 x 128.
  */
 #define SPK_OPT_LEAF_QUEUE 0
 #define SPK_OPT_WAIT_BUDGET 1
 #define SPK_OPT_STALL_TEST 2
 #define SPK_OPT_TC_SCHUR_M 3
 #define SPK_OPT_TC_TRAIL_ROWS 4
+#define SPK_OPT_TC_WIDE 5
 int spk_set_option(spk_handle* h, int option, int64_t value);
 int spk_get_option(spk_handle* h, int option, int64_t* value);
 
@@ -319,7 +323,8 @@ int spk_get_option(spk_handle* h, int option, int64_t* value);
  * Tune the options above for the loaded A in the given precision (no
  * counterpart in the reference): times `reps` factorisations (median, CUDA
  * events, after one untimed) with the leaf queue off and on, then, for the
- * float forms, a set of tensor-core thresholds; keeps the fastest, leaves A
+ * float forms, a set of tensor-core thresholds and the Schur tile width;
+ * keeps the fastest, leaves A
  * assembled for spk_factor and returns the best factor time in *best_ms (may
  * be NULL).  Needs spk_load_values first.
  */

@@ -83,6 +83,7 @@ constexpr long long WAIT_BUDGET = 1 << 20;
 struct Plan {
     bool built = false;
     bool sym = false;                     // the symmetric (SPD) form's tiles
+    int schur_nh = 1;                     // 128-column tiles per tensor-core Schur tile (wide: 2)
     int bmax = 0, bwmax = 1;
     std::vector<int> blk_c0, blk_c1, blk_p0, blk_np;
     std::vector<ll> blk_inv2;
@@ -206,6 +207,7 @@ struct spk_handle {
     long long wait_budget = WAIT_BUDGET;   // SPK_OPT_WAIT_BUDGET
     int stall_test = -1;                   // SPK_OPT_STALL_TEST
     int tc_schur_m = TC_SCHUR_M, tc_trail_rows = TC_TRAIL_ROWS;
+    int tc_wide = 1;                       // SPK_OPT_TC_WIDE: Schur tiles of 128 x 256
     std::string err;
 
     // launch accounting and optional per-class event timing
@@ -581,6 +583,7 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc, bool sym
     P = Plan();
     P.bmax = bmax;
     P.sym = sym;
+    P.schur_nh = h->tc_wide ? 2 : 1;
     const int nfr = (int)h->fronts.size();
     P.block0.resize(nfr);
     P.nblocks.resize(nfr);
@@ -834,7 +837,7 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc, bool sym
             tsch[k] = F.m > 0 && !leafF[k] ? (sym ? spk::lower_tiles(nts, nts) : nts * nts) : 0;
             tsch_tc[k] = 0;
             if (F.m > 0 && P.blk_lpack[P.block0[ids[k]]] >= 0) {
-                tsch_tc[k] = sym ? spk::lower_tiles(ntc, ntc) : ntc * ntc;
+                tsch_tc[k] = sym ? spk::lower_tiles_w(ntc, P.schur_nh) : ntc * cdiv(ntc, P.schur_nh);
                 tsch[k] = 0;
             }
             tbu[k] = F.m > 0 ? cdiv(F.nf, spk::U12_ROWS) * cdiv(F.m, spk::U12_COLS) : 0;
@@ -1008,6 +1011,10 @@ static int ensure_plan(spk_handle* h) {
                                    spk::umma::PSMEM));
         CU(h, cudaFuncSetAttribute(spk::k_tc_update<spk::TC_SCHUR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    spk::umma::PSMEM));
+        CU(h, cudaFuncSetAttribute(spk::k_tc_update<spk::TC_SCHUR, false, 2>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, spk::umma::PGeo<2>::SMEM));
+        CU(h, cudaFuncSetAttribute(spk::k_tc_update<spk::TC_SCHUR, true, 2>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, spk::umma::PGeo<2>::SMEM));
     }
     P.built = true;
     return SPK_OK;
@@ -1243,9 +1250,16 @@ static int factor_launches(spk_handle* h) {
             if (P.schur_tc.tiles > 0) {
                 LaunchScope ls(h, SPK_K_TC_SCHUR, P.schur_tc.flops, P.schur_tc.words * sizeof(T));
                 const int nt = P.schur_tc.tiles;
-                auto kern = bf16 ? spk::k_tc_update<spk::TC_SCHUR, true> : spk::k_tc_update<spk::TC_SCHUR, false>;
-                kern<<<std::min(nt, h->nsm), spk::TC_THREADS, spk::umma::PSMEM, h->stream>>>(
-                    fac, storage<T>(h).pack, S, launch_of(PL, P.schur_tc), 0, nt, 0, h->d_info + 1);
+                const spk::Launch la = launch_of(PL, P.schur_tc);
+                if (PL.schur_nh == 2) {   // 128 x 256 tiles
+                    auto kern = bf16 ? spk::k_tc_update<spk::TC_SCHUR, true, 2> : spk::k_tc_update<spk::TC_SCHUR, false, 2>;
+                    kern<<<std::min(nt, h->nsm), spk::TC_THREADS, spk::umma::PGeo<2>::SMEM, h->stream>>>(
+                        fac, storage<T>(h).pack, S, la, 0, nt, 0, h->d_info + 1);
+                } else {
+                    auto kern = bf16 ? spk::k_tc_update<spk::TC_SCHUR, true> : spk::k_tc_update<spk::TC_SCHUR, false>;
+                    kern<<<std::min(nt, h->nsm), spk::TC_THREADS, spk::umma::PSMEM, h->stream>>>(
+                        fac, storage<T>(h).pack, S, la, 0, nt, 0, h->d_info + 1);
+                }
             }
         }
     }
@@ -1880,9 +1894,11 @@ int spk_set_option(spk_handle* h, int option, int64_t value) {
         for (GraphRec& g : h->g_factor) drop_graph(g);
         return SPK_OK;
     case SPK_OPT_TC_SCHUR_M:
-    case SPK_OPT_TC_TRAIL_ROWS: {
-        if (value < 1 || value > INT_MAX) break;
-        int& field = option == SPK_OPT_TC_SCHUR_M ? h->tc_schur_m : h->tc_trail_rows;
+    case SPK_OPT_TC_TRAIL_ROWS:
+    case SPK_OPT_TC_WIDE: {
+        if (value < (option == SPK_OPT_TC_WIDE ? 0 : 1) || value > (option == SPK_OPT_TC_WIDE ? 1 : INT_MAX)) break;
+        int& field = option == SPK_OPT_TC_SCHUR_M ? h->tc_schur_m
+                     : option == SPK_OPT_TC_TRAIL_ROWS ? h->tc_trail_rows : h->tc_wide;
         if (field != (int)value) {
             field = (int)value;
             reset_float_plans(h);
@@ -1905,6 +1921,7 @@ int spk_get_option(spk_handle* h, int option, int64_t* value) {
     case SPK_OPT_STALL_TEST: *value = h->stall_test; return SPK_OK;
     case SPK_OPT_TC_SCHUR_M: *value = h->tc_schur_m; return SPK_OK;
     case SPK_OPT_TC_TRAIL_ROWS: *value = h->tc_trail_rows; return SPK_OK;
+    case SPK_OPT_TC_WIDE: *value = h->tc_wide; return SPK_OK;
     default: return set_err(h, SPK_EARG, "spk_get_option: unknown option");
     }
 }
@@ -1977,6 +1994,11 @@ int spk_autotune(spk_handle* h, int precision, int reps, double* best_ms) {
         }
         if ((rc = spk_set_option(h, SPK_OPT_TC_SCHUR_M, bs))) return rc;
         if ((rc = spk_set_option(h, SPK_OPT_TC_TRAIL_ROWS, bt))) return rc;
+        const int w0 = h->tc_wide;   // then the Schur tile width
+        if ((rc = spk_set_option(h, SPK_OPT_TC_WIDE, 1 - w0))) return rc;
+        if ((rc = measure(&ms))) return rc;
+        if (ms < best) best = ms;
+        else if ((rc = spk_set_option(h, SPK_OPT_TC_WIDE, w0))) return rc;
     }
     // leave A assembled in the chosen form, ready for spk_factor
     if ((rc = f64 ? load_into<double>(h) : load_into<float>(h))) return rc;

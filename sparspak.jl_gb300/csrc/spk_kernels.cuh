@@ -1415,6 +1415,21 @@ __host__ __device__ __forceinline__ int lower_tiles(int nr, int nc) {
     for (int j = 0; j < nc && j < nr; ++j) n += nr - j;
     return n;
 }
+// The same for groups of w adjacent tile columns (wide tiles): group j
+// covers columns w j .. w j + w - 1 and rows w j .. nr - 1.
+__host__ __device__ __forceinline__ void lower_tile_w(int t, int nr, int w, int& i, int& j) {
+    j = 0;
+    while (t >= nr - w * j) {
+        t -= nr - w * j;
+        ++j;
+    }
+    i = w * j + t;
+}
+__host__ __device__ __forceinline__ int lower_tiles_w(int nr, int w) {
+    int n = 0;
+    for (int j = 0; w * j < nr; ++j) n += nr - w * j;
+    return n;
+}
 
 template <typename T, bool rows_fast>
 __device__ __forceinline__ void mma_tile(const T* sA, const T* sB, int kc, T acc[4][4]) {
@@ -1846,9 +1861,10 @@ constexpr int TC_EPI = 16, TC_THREADS = 32 * (4 + TC_EPI);
 struct TcTile {
     DFront F;
     int rt, ct, n1, n2, nchunks;
+    int nh;   // 128-column tiles of the (wide) tile that exist: ct .. ct + nh - 1
 };
 
-template <int MODE>
+template <int MODE, int NH = 1>
 __device__ __forceinline__ TcTile tc_decode(const Sched& S, const Launch& L, int step, int tile, int tile_base) {
     TcTile T;
     int fid, t;
@@ -1873,11 +1889,19 @@ __device__ __forceinline__ TcTile tc_decode(const Sched& S, const Launch& L, int
             T.ct = n1 + t2 / n1;
         }
         T.nchunks = cdiv(bw, umma::KCH);
+        T.nh = 1;
     } else {
         T.n1 = 0;
-        T.rt = t % n2;
-        T.ct = t / n2;
-        if (S.sym) lower_tile(t, n2, T.rt, T.ct);
+        int g;
+        if (S.sym) {
+            lower_tile_w(t, n2, NH, T.rt, g);
+        } else {
+            T.rt = t % n2;
+            g = t / n2;
+        }
+        T.ct = NH * g;
+        T.nh = min(NH, n2 - T.ct);
+        if (S.sym) T.nh = min(T.nh, T.rt - T.ct + 1);   // no tile above the diagonal
         int nc = 0;
         for (int b = 0; b < T.F.nblocks; ++b) {
             const int blk = T.F.block0 + b;
@@ -1920,16 +1944,18 @@ struct ChunkWalk {
     }
 };
 
-template <int MODE, bool BF>
+template <int MODE, bool BF, int NH = 1>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const unsigned char* pack, Sched S, Launch L,
                                                               int step, int ntiles, int tile_base, int* err) {
+    static_assert(MODE == TC_SCHUR || NH == 1, "wide tiles are for the Schur complements");
+    using G = umma::PGeo<NH>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ ScatterRow tab[2][umma::TM];   // SCHUR: [0] tile columns, [1] tile rows
+    __shared__ ScatterRow tab[NH + 1][umma::TM];   // SCHUR: [h] columns of tile h, [NH] tile rows
     __shared__ int dead;
-    const umma::PCtx cx = umma::pctx_of(smem_raw);
+    const umma::PCtx cx = umma::pctx_of<NH>(smem_raw);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
-        for (int s = 0; s < umma::PST; ++s) {
+        for (int s = 0; s < G::NST; ++s) {
             umma::mbar_init(&cx.full[s], 1);
             umma::mbar_init(&cx.empty[s], 1);
         }
@@ -1940,22 +1966,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         dead = 0;
     }
-    if (warp == 1) umma::tmem_alloc(cx.tmem_slot, 2 * umma::TN);
+    if (warp == 1) umma::tmem_alloc(cx.tmem_slot, G::TMEM_COLS);
     umma::fence_before();
     __syncthreads();
     umma::fence_after();
     const uint32_t tmem = *cx.tmem_slot;
     volatile int* vdead = &dead;
-    // bytes of one chunk of one operand, and where operand B starts in a stage
+    // bytes of one chunk of one operand; B tile h of a stage at BOFF + h * BSTEP
     constexpr uint32_t CB = BF ? umma::PCHUNK16 : umma::PCHUNK;
-    constexpr uint32_t BOFF = 2 * umma::OPB;
+    constexpr uint32_t BOFF = 2 * umma::OPB, BSTEP = 2 * umma::OPB;
+    constexpr uint32_t ACC_COLS = NH * umma::TN;
 
     if (warp == 0) {
         if (lane == 0) {   // bulk copies
             int s = 0;
             uint32_t ph = 0;
             for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-                const TcTile T = tc_decode<MODE>(S, L, step, tile, tile_base);
+                const TcTile T = tc_decode<MODE, NH>(S, L, step, tile, tile_base);
                 ChunkWalk<MODE, BF> w(S, T, step);
                 int b, c, kc;
                 while (w.next(S, b, c, kc)) {
@@ -1966,13 +1993,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
                     const ll lp = BF ? (S.blk_lpack[b] >> 2) : S.blk_lpack[b];
                     const ll up = BF ? (S.blk_upack[b] >> 2) : S.blk_upack[b];
                     const unsigned char* pa = pack + lp + ((ll)ra * nch + c) * CB;
-                    const unsigned char* pb = pack + up + ((ll)rb * nch + c) * CB;
                     umma::wait_bounded(&cx.empty[s], ph ^ 1, vdead, err);
-                    umma::arrive_expect_tx(&cx.full[s], 2 * kc * CB);
-                    const uint32_t dst = umma::saddr(cx.stage + s * umma::STAGE);
+                    umma::arrive_expect_tx(&cx.full[s], (1 + T.nh) * kc * CB);
+                    const uint32_t dst = umma::saddr(cx.stage + s * G::STAGE);
                     umma::bulk_g2s(dst, pa, kc * CB, &cx.full[s]);
-                    umma::bulk_g2s(dst + BOFF, pb, kc * CB, &cx.full[s]);
-                    if (++s == umma::PST) { s = 0; ph ^= 1; }
+                    for (int h = 0; h < T.nh; ++h) {
+                        const unsigned char* pb = pack + up + ((ll)(rb + h) * nch + c) * CB;
+                        umma::bulk_g2s(dst + BOFF + h * BSTEP, pb, kc * CB, &cx.full[s]);
+                    }
+                    if (++s == G::NST) { s = 0; ph ^= 1; }
                 }
             }
         }
@@ -1984,64 +2013,68 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
             int acc = 0;
             uint32_t aph = 0;
             for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-                const TcTile T = tc_decode<MODE>(S, L, step, tile, tile_base);
+                const TcTile T = tc_decode<MODE, NH>(S, L, step, tile, tile_base);
                 umma::wait_bounded(&cx.tempty[acc], aph ^ 1, vdead, err);
                 umma::fence_after();
-                const uint32_t d = tmem + acc * umma::TN;
                 ChunkWalk<MODE, BF> w(S, T, step);
                 int b, c, kc;
                 bool first = true;
                 while (w.next(S, b, c, kc)) {
                     umma::wait_bounded(&cx.full[s], ph, vdead, err);
                     umma::fence_after();
-                    const uint32_t a0 = umma::saddr(cx.stage + s * umma::STAGE), b0 = a0 + BOFF;
-                    if constexpr (BF) {
-                        for (int j = 0; j < kc; ++j) {   // one K = 16 product per chunk
-                            const uint64_t da = umma::desc_kmajor(a0 + j * CB, 128, umma::SBO16);
-                            const uint64_t db = umma::desc_kmajor(b0 + j * CB, 128, umma::SBO16);
-                            umma::mma_bf16(d, da, db, IDESC, (first && j == 0) ? 0u : 1u);
-                        }
-                    } else {
-                        const uint32_t a_hi = a0, a_lo = a0 + umma::OPB;
-                        const uint32_t b_hi = b0, b_lo = b0 + umma::OPB;
+                    const uint32_t a0 = umma::saddr(cx.stage + s * G::STAGE);
+                    for (int h = 0; h < T.nh; ++h) {
+                        const uint32_t d = tmem + acc * ACC_COLS + h * umma::TN;
+                        const uint32_t b0 = a0 + BOFF + h * BSTEP;
+                        if constexpr (BF) {
+                            for (int j = 0; j < kc; ++j) {   // one K = 16 product per chunk
+                                const uint64_t da = umma::desc_kmajor(a0 + j * CB, 128, umma::SBO16);
+                                const uint64_t db = umma::desc_kmajor(b0 + j * CB, 128, umma::SBO16);
+                                umma::mma_bf16(d, da, db, IDESC, (first && j == 0) ? 0u : 1u);
+                            }
+                        } else {
+                            const uint32_t a_hi = a0, a_lo = a0 + umma::OPB;
+                            const uint32_t b_hi = b0, b_lo = b0 + umma::OPB;
 #pragma unroll
-                        for (int kk = 0; kk < umma::KCH / 8; ++kk) {
-                            const uint32_t o = kk * 256;
-                            const uint64_t dah = umma::desc_kmajor(a_hi + o, 128, umma::SBO);
-                            const uint64_t dal = umma::desc_kmajor(a_lo + o, 128, umma::SBO);
-                            const uint64_t dbh = umma::desc_kmajor(b_hi + o, 128, umma::SBO);
-                            const uint64_t dbl = umma::desc_kmajor(b_lo + o, 128, umma::SBO);
-                            umma::mma_tf32(d, dah, dbh, IDESC, (first && kk == 0) ? 0u : 1u);
-                            umma::mma_tf32(d, dah, dbl, IDESC, 1u);
-                            umma::mma_tf32(d, dal, dbh, IDESC, 1u);
+                            for (int kk = 0; kk < umma::KCH / 8; ++kk) {
+                                const uint32_t o = kk * 256;
+                                const uint64_t dah = umma::desc_kmajor(a_hi + o, 128, umma::SBO);
+                                const uint64_t dal = umma::desc_kmajor(a_lo + o, 128, umma::SBO);
+                                const uint64_t dbh = umma::desc_kmajor(b_hi + o, 128, umma::SBO);
+                                const uint64_t dbl = umma::desc_kmajor(b_lo + o, 128, umma::SBO);
+                                umma::mma_tf32(d, dah, dbh, IDESC, (first && kk == 0) ? 0u : 1u);
+                                umma::mma_tf32(d, dah, dbl, IDESC, 1u);
+                                umma::mma_tf32(d, dal, dbh, IDESC, 1u);
+                            }
                         }
                     }
                     first = false;
                     umma::commit(&cx.empty[s]);
-                    if (++s == umma::PST) { s = 0; ph ^= 1; }
+                    if (++s == G::NST) { s = 0; ph ^= 1; }
                 }
                 umma::commit(&cx.tfull[acc]);
                 if (++acc == 2) { acc = 0; aph ^= 1; }
             }
         }
-    } else if (warp >= 4) {   // epilogue: thread = one TMEM lane (tile row), 32 columns
+    } else if (warp >= 4) {   // epilogue: thread = one TMEM lane (tile row), 32 columns of each tile
         const int q4 = warp & 3, i = 32 * q4 + lane, cg = (warp - 4) >> 2, et = threadIdx.x - 128;
         int acc = 0;
         uint32_t aph = 0;
         for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-            const TcTile T = tc_decode<MODE>(S, L, step, tile, tile_base);
+            const TcTile T = tc_decode<MODE, NH>(S, L, step, tile, tile_base);
             const DFront& F = T.F;
             if (MODE == TC_SCHUR) {
                 asm volatile("bar.sync 1, %0;" ::"n"(32 * TC_EPI) : "memory");   // previous tile's scatter done
-                if (et < 2 * umma::TM) {
-                    const int side = et / umma::TM, x = (side == 0 ? T.ct : T.rt) * umma::TM + (et % umma::TM);
-                    tab[side][et % umma::TM] = scatter_row<float>(S, F, x);
+                for (int e = et; e < (T.nh + 1) * umma::TM; e += 32 * TC_EPI) {
+                    const int side = e / umma::TM, rows = side == T.nh;
+                    const int x = (rows ? T.rt : T.ct + side) * umma::TM + (e % umma::TM);
+                    tab[rows ? NH : side][e % umma::TM] = scatter_row<float>(S, F, x);
                 }
                 asm volatile("bar.sync 1, %0;" ::"n"(32 * TC_EPI) : "memory");
             }
             umma::wait_bounded(&cx.tfull[acc], aph, vdead, err);
             umma::fence_after();
-            const uint32_t taddr = tmem + acc * umma::TN + ((uint32_t)(32 * q4) << 16);
+            const uint32_t taddr = tmem + acc * ACC_COLS + ((uint32_t)(32 * q4) << 16);
             if (MODE == TC_TRAIL) {
                 const int c1 = S.blk_c1[F.block0 + step];
                 const bool rL = T.rt < T.n1;   // row region [c1, nf) else [nf, ld)
@@ -2077,12 +2110,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
                     }
                 }
             } else {
-                const int r = T.rt * umma::TM + i, c0 = T.ct * umma::TN;
-                const ScatterRow& R = tab[1][i];
-                {
+                const int r = T.rt * umma::TM + i;
+                const ScatterRow& R = tab[NH][i];
+                for (int th = 0; th < T.nh; ++th) {
+                    const int c0 = (T.ct + th) * umma::TN;
                     const int h = cg;
                     float v[32];
-                    umma::tmem_ld32(taddr + h * 32, v);
+                    umma::tmem_ld32(taddr + th * umma::TN + h * 32, v);
                     if (r < F.m) {
                         // positions of 16 entries first (their rel[] loads in flight
                         // together), then the 16 scatter-adds
@@ -2094,14 +2128,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
                                 const int jj = 16 * half + j, c = c0 + h * 32 + jj;
                                 pos[j] = -1;
                                 if (c < F.m && (r >= c || !S.sym))
-                                    pos[j] = r >= c ? S.rel[tab[0][h * 32 + jj].rel0 + r] : S.rel[R.rel0 + c];
+                                    pos[j] = r >= c ? S.rel[tab[th][h * 32 + jj].rel0 + r] : S.rel[R.rel0 + c];
                             }
 #pragma unroll
                             for (int j = 0; j < 16; ++j) {
                                 const int jj = 16 * half + j, c = c0 + h * 32 + jj;
                                 if (c >= F.m || pos[j] < 0) continue;
                                 if (r >= c) {   // L entry of the front of R_F[c]
-                                    const ScatterRow& Cc = tab[0][h * 32 + jj];
+                                    const ScatterRow& Cc = tab[th][h * 32 + jj];
                                     if (Cc.pos >= 0) atomicAdd(&fac[Cc.loff + (ll)Cc.pos * Cc.ld + pos[j]], -v[jj]);
                                 } else if (R.pos >= 0) {   // entry of the front of R_F[r]
                                     const int pc = pos[j];
@@ -2122,7 +2156,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
     umma::fence_before();
     __syncthreads();
     umma::fence_after();
-    if (warp == 1) umma::tmem_dealloc(tmem, 2 * umma::TN);
+    if (warp == 1) umma::tmem_dealloc(tmem, G::TMEM_COLS);
 }
 
 // ---------------------------------------------------------------------------

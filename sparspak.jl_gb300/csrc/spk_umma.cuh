@@ -181,21 +181,34 @@ __device__ __forceinline__ bool wait_bounded(uint64_t* bar, uint32_t parity, vol
     return false;
 }
 
+// Wide tiles: a CTA computes NH adjacent 128 x 128 tiles of one tile row
+// (128 x 128 NH), so that each A chunk it stages serves NH products.  A
+// stage holds A (hi, lo) and NH B chunks (hi, lo), B tile h at (2 + 2h) OPB;
+// the accumulator takes NH x 128 TMEM columns, double-buffered.
+template <int NH>
+struct PGeo {
+    static constexpr int STAGE = (2 + 2 * NH) * OPB;
+    static constexpr int NST = NH == 1 ? PST : 4;           // stages that fit beside the rest
+    static constexpr int SMEM = NST * STAGE + 2048;
+    static constexpr uint32_t TMEM_COLS = 2 * NH * TN;
+};
+
 // Barriers and TMEM of a packed-pipeline CTA (carved from dynamic shared memory).
 struct PCtx {
-    unsigned char* stage;   // PST * STAGE bytes, 1024-aligned
+    unsigned char* stage;   // NST * STAGE bytes, 1024-aligned
     uint64_t *full, *empty, *tfull, *tempty;
     uint32_t* tmem_slot;
 };
 
+template <int NH = 1>
 __device__ __forceinline__ PCtx pctx_of(unsigned char* smem_raw) {
     unsigned char* base =
         reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     PCtx c;
     c.stage = base;
-    c.full = reinterpret_cast<uint64_t*>(base + PST * STAGE);
-    c.empty = c.full + PST;
-    c.tfull = c.empty + PST;
+    c.full = reinterpret_cast<uint64_t*>(base + PGeo<NH>::NST * PGeo<NH>::STAGE);
+    c.empty = c.full + PGeo<NH>::NST;
+    c.tfull = c.empty + PGeo<NH>::NST;
     c.tempty = c.tfull + 2;
     c.tmem_slot = reinterpret_cast<uint32_t*>(c.tempty + 2);
     return c;

@@ -220,7 +220,7 @@ class NumericEngine:
     # -- options --------------------------------------------------------------
     def set_option(self, name, value):
         """Set a factorisation option (_native.OPTIONS: leaf_queue, wait_budget,
-        stall_test, tc_schur_m, tc_trail_rows); takes effect at the next factor."""
+        stall_test, tc_schur_m, tc_trail_rows, tc_wide); takes effect at the next factor."""
         self._check(self._lib.spk_set_option(self._h, N.OPTIONS[name], int(value)), "spk_set_option")
 
     def get_option(self, name):
@@ -233,7 +233,7 @@ class NumericEngine:
         return ({option: value}, best factor ms); A stays assembled."""
         ms = ctypes.c_double()
         self._check(self._lib.spk_autotune(self._h, _prec(precision), int(reps), ctypes.byref(ms)), "spk_autotune")
-        return {k: self.get_option(k) for k in ("leaf_queue", "tc_schur_m", "tc_trail_rows")}, ms.value
+        return {k: self.get_option(k) for k in ("leaf_queue", "tc_schur_m", "tc_trail_rows", "tc_wide")}, ms.value
 
     # -- launch accounting ----------------------------------------------------
     def profile(self, classes=()):

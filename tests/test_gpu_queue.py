@@ -8,6 +8,9 @@ option autotuner, through the C ABI.
 * The timeout path: a small wait budget and a stalled queue position make
   spk_factor return SPK_ETIMEOUT (DeviceTimeoutError) without a fault; with
   the defaults back the next factor is correct again.
+* Wide tensor-core Schur tiles (128 x 256, SPK_OPT_TC_WIDE) against the
+  128 x 128 ones: the same factors to FP32 rounding (the scatter-adds into
+  the parents come in another order), in the FP32, BF16 and SPD forms.
 * spk_autotune chooses options from its set, leaves A assembled, and the
   factor that follows refines to 1e-12.
 """
@@ -118,6 +121,27 @@ def test_queue_wait_timeout_is_reported_and_recoverable():
             eng.set_option(*bad)
 
 
+@pytest.mark.parametrize("prec", ["fp32", "bf16s", "fp32+spd"])
+def test_wide_schur_tiles_match_narrow(prec):
+    A = S.gallery.laplacian((30, 30, 30), shift=1e-3)
+    n = A.shape[0]
+    base, _, form = prec.partition("+")
+    s = _solver(A, S.nd_grid(30, 30, 30), precision=base, spd=form == "spd")
+    b = S.gallery.random_rhs(n, 2, seed=6)
+    lnz = {}
+    for wide in (1, 0):
+        eng = _factor_with(s, A, tc_wide=wide)
+        prof = eng.profile_read()
+        assert prof["tc_schur"]["launches"] > 0
+        lnz[wide] = s.slvr.lnz.copy()
+        x = np.zeros_like(b, order="F")
+        it, rr = eng.refine(np.asfortranarray(b), x, prec, 1e-12, 100)
+        assert rr <= 1e-12 and relres(A, x, b) <= 1e-12, (wide, rr, it)
+    d = rel(lnz[1], lnz[0])
+    print(f"{prec}: wide vs narrow Schur tiles, factors differ by {d:.1e}")
+    assert d < (5e-3 if base == "bf16s" else 1e-5)
+
+
 @pytest.mark.parametrize("prec", ["fp32", "fp64"])
 def test_autotune_then_factor_and_refine(prec):
     A = S.gallery.laplacian((28, 28, 28), shift=1e-3)
@@ -131,6 +155,7 @@ def test_autotune_then_factor_and_refine(prec):
     if prec == "fp32":
         assert (opts["tc_schur_m"], opts["tc_trail_rows"]) in {(96, 128), (64, 128), (128, 128), (192, 128),
                                                                (96, 256), (128, 256), (256, 256)}
+        assert opts["tc_wide"] in (0, 1)
     eng.factor(prec)   # A was left assembled
     b = S.gallery.random_rhs(n, 2, seed=8)
     x = np.zeros_like(b, order="F")
