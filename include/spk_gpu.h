@@ -309,6 +309,15 @@ int spk_measure_peaks(double* fp32_tflops, double* fp64_tflops, double* dmma_tfl
  *  SPK_OPT_TC_WIDE       1 (default): the tensor-core Schur complements in
  *                        tiles of 128 x 256 (each staged L chunk serves two
  *                        products); 0: tiles of 128 x 128.
+ *  SPK_OPT_LU_PIECES     1: blocks whose pieces (supernodes) are all at
+ *                        most 32 columns wide are factored piece by piece
+ *                        (a warp per piece's diagonal block, then the block's
+ *                        triangular solves and update in parallel): the
+ *                        reference's operation order (ggetrf!, trsm, gemm
+ *                        per supernode), hence FP64 factors closer to its
+ *                        rounding, but a slower chain on GB300 (the piece's
+ *                        column steps are as long as the block form's);
+ *                        0 (default): every wide block in column groups.
  */
 #define SPK_OPT_LEAF_QUEUE 0
 #define SPK_OPT_WAIT_BUDGET 1
@@ -316,6 +325,7 @@ int spk_measure_peaks(double* fp32_tflops, double* fp64_tflops, double* dmma_tfl
 #define SPK_OPT_TC_SCHUR_M 3
 #define SPK_OPT_TC_TRAIL_ROWS 4
 #define SPK_OPT_TC_WIDE 5
+#define SPK_OPT_LU_PIECES 6
 int spk_set_option(spk_handle* h, int option, int64_t value);
 int spk_get_option(spk_handle* h, int option, int64_t* value);
 

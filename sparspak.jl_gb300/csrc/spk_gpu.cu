@@ -57,6 +57,7 @@ struct LevelPlan {
     // btrail_tc0: tile 0 of each packed front's trailing update (it holds the
     // next block's diagonal block); btrail_tc: its tiles 1..
     std::vector<LaunchRec> blu, bpanel, btrail, btrail_tc0, btrail_tc, fwd, bwd;
+    std::vector<char> blu_pc;   // every piece of the step's blocks is at most 32 columns (k_block_lu_pc)
     // Solves: fronts with many blocks by one cluster launch each direction
     // (front_big, one tile per front), the others by block steps
     // (fwd_small / bwd_small); the transposed solves use fwd / bwd.
@@ -208,6 +209,7 @@ struct spk_handle {
     int stall_test = -1;                   // SPK_OPT_STALL_TEST
     int tc_schur_m = TC_SCHUR_M, tc_trail_rows = TC_TRAIL_ROWS;
     int tc_wide = 1;                       // SPK_OPT_TC_WIDE: Schur tiles of 128 x 256
+    int lu_pieces = 0;                     // SPK_OPT_LU_PIECES: block LU by pieces (slower on GB300, see header)
     std::string err;
 
     // launch accounting and optional per-class event timing
@@ -684,6 +686,7 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc, bool sym
         int maxb = 0;
         for (int id : ids) maxb = std::max(maxb, P.nblocks[id]);
         L.blu.resize(maxb);
+        L.blu_pc.assign(maxb, 1);
         L.bpanel.resize(maxb);
         L.btrail.resize(maxb);
         L.btrail_tc0.resize(maxb);
@@ -801,6 +804,12 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc, bool sym
                 wb[k] = 0.5 * rbw * rbw + rbw * r0;
             }
             add_launch(&P, L.blu[t], ids, tl, fl, wl);
+            for (size_t k = 0; k < nid; ++k)
+                if (tl[k] > 0) {
+                    const int blk = P.block0[ids[k]] + t;
+                    for (int q = P.blk_p0[blk]; q < P.blk_p0[blk] + P.blk_np[blk]; ++q)
+                        if (h->xs[q + 1] - h->xs[q] > 32) L.blu_pc[t] = 0;
+                }
             add_launch(&P, L.bpanel[t], ids, tp, fp, wp);
             int bwl = 1;
             for (size_t k = 0; k < nid; ++k)
@@ -953,6 +962,8 @@ static int ensure_plan(spk_handle* h) {
     constexpr int BM = spk::BlockMax<T>::value;
     CU(h, cudaFuncSetAttribute(spk::k_block_panel<T, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)panel_smem<T, BM>()));
+    CU(h, cudaFuncSetAttribute(spk::k_block_lu_pc<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)spk::PcLu<T>::smem));
     CU(h, cudaFuncSetAttribute(spk::k_block_inv<T, BM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)sweep_smem<T, BM>(1)));
     CU(h, cudaFuncSetAttribute(spk::k_leaf_factor<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1177,6 +1188,9 @@ static int factor_launches(spk_handle* h) {
                 if (bw <= 32)
                     spk::k_block_lu_small<T><<<(P.blu[t].count + 3) / 4, 128, 0, h->stream>>>(
                         fac, h->d_ipiv, h->d_info, S, launch_of(PL, P.blu[t]), (int)t);
+                else if (h->lu_pieces && P.blu_pc[t])
+                    spk::k_block_lu_pc<T><<<P.blu[t].tiles, spk::PC_THREADS, spk::PcLu<T>::smem, h->stream>>>(
+                        fac, h->d_ipiv, h->d_info, h->d_bmap, S, launch_of(PL, P.blu[t]), (int)t);
                 else
                     spk::k_block_lu<T><<<P.blu[t].tiles, spk::LuThreads<T>::value, 0, h->stream>>>(
                         fac, h->d_ipiv, h->d_info, h->d_bmap, S, launch_of(PL, P.blu[t]), (int)t);
@@ -1893,6 +1907,11 @@ int spk_set_option(spk_handle* h, int option, int64_t value) {
         h->stall_test = (int)value;
         for (GraphRec& g : h->g_factor) drop_graph(g);
         return SPK_OK;
+    case SPK_OPT_LU_PIECES:
+        if (value != 0 && value != 1) break;
+        h->lu_pieces = (int)value;
+        for (GraphRec& g : h->g_factor) drop_graph(g);
+        return SPK_OK;
     case SPK_OPT_TC_SCHUR_M:
     case SPK_OPT_TC_TRAIL_ROWS:
     case SPK_OPT_TC_WIDE: {
@@ -1922,6 +1941,7 @@ int spk_get_option(spk_handle* h, int option, int64_t* value) {
     case SPK_OPT_TC_SCHUR_M: *value = h->tc_schur_m; return SPK_OK;
     case SPK_OPT_TC_TRAIL_ROWS: *value = h->tc_trail_rows; return SPK_OK;
     case SPK_OPT_TC_WIDE: *value = h->tc_wide; return SPK_OK;
+    case SPK_OPT_LU_PIECES: *value = h->lu_pieces; return SPK_OK;
     default: return set_err(h, SPK_EARG, "spk_get_option: unknown option");
     }
 }

@@ -155,6 +155,31 @@ __device__ __forceinline__ int warp_first_max(unsigned long long key) {
     return __ffs(ballot) - 1;
 }
 
+// Correctly rounded reciprocal (the value of T(1) / x).
+__device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
+
+// Scaling factor 1 / pivot of the FP32 block LU: the hardware reciprocal
+// (within 2 ulp; the FP32 factor is refined in FP64); FP64 keeps the
+// correctly rounded one.
+__device__ __forceinline__ float lu_recip(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ double lu_recip(double x) { return rcp_rn(x); }
+
+// The pivot lane of a column (first strict maximum of |x| among the
+// candidates, pivot_key's rules): one 32-bit reduction for FP32, two for FP64.
+__device__ __forceinline__ int warp_pivot_lane(float x, bool cand, bool diag) {
+    unsigned key = 0u;
+    if (cand) {
+        const unsigned b = __float_as_uint(x) & 0x7fffffffu;
+        key = b > 0x7f800000u ? (diag ? 0xffffffffu : 1u) : b + 2u;
+    }
+    const unsigned m = __reduce_max_sync(0xffffffffu, key);
+    return __ffs(__ballot_sync(0xffffffffu, key == m)) - 1;
+}
+__device__ __forceinline__ int warp_pivot_lane(double x, bool cand, bool diag) {
+    return warp_first_max(pivot_key(x, cand, diag));
+}
+
 // r[k] for a runtime k without indexing a register array dynamically: a
 // tree of selects (depth log2 W instead of a W-long chain); W a power of 2.
 template <int W, typename T>
@@ -186,42 +211,80 @@ __device__ bool warp_lu_sweep(T (&r)[W], int nrows, int ncols, const int* q0, in
     const int lane = threadIdx.x & 31;
     bool sing = false;
     int pc = 0;
-#pragma unroll 1
-    for (int k = 0; k < ncols; ++k) {
-        while (q0[pc + 1] <= k) ++pc;
-        const int a = q0[pc], b = q0[pc + 1];
-        const T rk0 = pickw<W>(r, k);
-        const int kp = warp_first_max(pivot_key(rk0, sym ? lane == k : (lane >= k && lane < b), lane == k));
-        if (lane == 0) piv[k] = kp - a;
-        const T pv = __shfl_sync(FULL, rk0, kp);
-        if (pv != T(0)) {
-            if (kp != k) {
+    if constexpr (W <= 8) {
+        // Narrow blocks: unrolled over the column index, so that r[k] and the
+        // columns after k are compile-time registers.
 #pragma unroll
-                for (int j = 0; j < W; ++j) {
-                    const T vk = __shfl_sync(FULL, r[j], k), vp = __shfl_sync(FULL, r[j], kp);
-                    if (j >= a) {
-                        if (lane == k) r[j] = vp;
-                        else if (lane == kp) r[j] = vk;
+        for (int k = 0; k < W; ++k) {
+            if (k < ncols) {
+                while (q0[pc + 1] <= k) ++pc;
+                const int a = q0[pc], b = q0[pc + 1];
+                const int kp = warp_pivot_lane(r[k], sym ? lane == k : (lane >= k && lane < b), lane == k);
+                if (lane == 0) piv[k] = kp - a;
+                const T pv = __shfl_sync(FULL, r[k], kp);
+                if (pv != T(0)) {
+                    if (kp != k) {
+#pragma unroll
+                        for (int j = 0; j < W; ++j) {
+                            const T vk = __shfl_sync(FULL, r[j], k), vp = __shfl_sync(FULL, r[j], kp);
+                            if (j >= a) {
+                                if (lane == k) r[j] = vp;
+                                else if (lane == kp) r[j] = vk;
+                            }
+                        }
                     }
+                    const T inv = lu_recip(pv);
+                    if (lane > k && lane < nrows) r[k] *= inv;
+                } else {
+                    sing = true;
+                }
+                const T lk = r[k];
+                const bool upd = lane > k && lane < nrows;
+#pragma unroll
+                for (int j = k + 1; j < W; ++j) {
+                    const T u = __shfl_sync(FULL, r[j], k);
+                    if (upd) r[j] -= lk * u;
                 }
             }
-            const T inv = T(1) / pv;
-            if (lane > k && lane < nrows) {
-#pragma unroll
-                for (int j = 0; j < W; ++j)
-                    if (j == k) r[j] *= inv;
-            }
-        } else {
-            sing = true;
         }
-        const T lk = pickw<W>(r, k);
-        T u[W];
+    } else {
+        // Wider blocks: a rolled loop (the unrolled form's code outgrows the
+        // instruction cache), r[k] picked by a tree of selects.
+#pragma unroll 1
+        for (int k = 0; k < ncols; ++k) {
+            while (q0[pc + 1] <= k) ++pc;
+            const int a = q0[pc], b = q0[pc + 1];
+            const T rk0 = pickw<W>(r, k);
+            const int kp = warp_pivot_lane(rk0, sym ? lane == k : (lane >= k && lane < b), lane == k);
+            if (lane == 0) piv[k] = kp - a;
+            const T pv = __shfl_sync(FULL, rk0, kp);
+            if (pv != T(0)) {
+                if (kp != k) {
 #pragma unroll
-        for (int j = 0; j < W; ++j) u[j] = __shfl_sync(FULL, r[j], k);
-        if (lane > k && lane < nrows) {
+                    for (int j = 0; j < W; ++j) {
+                        const T vk = __shfl_sync(FULL, r[j], k), vp = __shfl_sync(FULL, r[j], kp);
+                        if (j >= a) {
+                            if (lane == k) r[j] = vp;
+                            else if (lane == kp) r[j] = vk;
+                        }
+                    }
+                }
+                const T inv = lu_recip(pv);
+                if (lane > k && lane < nrows) {
 #pragma unroll
-            for (int j = 0; j < W; ++j)
-                if (j > k) r[j] -= lk * u[j];
+                    for (int j = 0; j < W; ++j)
+                        if (j == k) r[j] *= inv;
+                }
+            } else {
+                sing = true;
+            }
+            const T lk = pickw<W>(r, k);
+            const bool upd = lane > k && lane < nrows;
+#pragma unroll
+            for (int j = 0; j < W; ++j) {
+                const T u = __shfl_sync(FULL, r[j], k);
+                if (upd && j > k) r[j] -= lk * u;
+            }
         }
     }
     return sing;
@@ -339,9 +402,6 @@ __device__ __forceinline__ void block_gather_map(const int* ipiv_blk, const int*
     }
 }
 
-// Correctly rounded reciprocal (the value of T(1) / x).
-__device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
-__device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
 
 // Block LU by a whole CTA (blocks of 33..BlockMax columns; one CTA per
 // front).  Warp w holds the column group [4w, 4w+4) of the block, lane l the
@@ -377,11 +437,6 @@ __device__ __forceinline__ T lu_pick(const T (&a)[RPT][4], int ii, int jj) {
     return v;
 }
 
-// Scaling factor 1 / pivot of the FP32 block LU: the hardware reciprocal
-// (within 2 ulp; the FP32 factor is refined in FP64); FP64 keeps the
-// correctly rounded one.
-__device__ __forceinline__ float lu_recip(float x) { return __fdividef(1.0f, x); }
-__device__ __forceinline__ double lu_recip(double x) { return rcp_rn(x); }
 
 // Part A for the group of warp `g` (called by that warp only).  cpa / cpb:
 // first and end column of each column's piece.
@@ -600,6 +655,182 @@ __global__ void __launch_bounds__(LuThreads<T>::value, 1) k_block_lu(T* fac, int
             for (int i = a; i < b; ++i) bmap[F.f + c0 + i] = sgmap[i] | (a << 8);
         }
     }
+    if (tid == 0 && szero != INT_MAX) {
+        int p = 0;
+        while (q0[p + 1] <= szero) ++p;
+        atomicMin(info, p0 + p + 1);   // first singular piece of the block
+    }
+}
+
+// Block LU by pieces, for blocks whose pieces are all at most 32 columns
+// wide (the supernode partition's maxblocksize, 30 by default).  The
+// block is staged in shared memory; for each piece [a, b) in turn:
+//   (1) one warp factors the piece's diagonal block in registers
+//       (warp_lu_sweep: ggetrf!, pivots among the piece's rows);
+//   (2) a thread per column right of the piece applies the piece's
+//       interchanges and solves U12 := inv(L11) P A12 (_luswap!, trsm
+//       'l','l','n','u'), and a thread per row below it solves
+//       L21 := A21 inv(U11) (trsm 'r','u','n','n');
+//   (3) the rest of the block takes the rank-w update A22 -= L21 U12 (gemm),
+//       a warp per four columns with its lanes on the rows.
+// Only the w rows of the piece are on the sequential path of (1); the rows
+// below are solved in parallel afterwards, which is where this form gains
+// over k_block_lu (whose owner warp sweeps all rows of the block for every
+// column).  Same outputs as k_block_lu: the factored block, ipiv, the row
+// sources of the interchanges (bmap) and the first singular piece.
+constexpr int PC_THREADS = 512;
+template <typename T> struct PcLu {
+    static constexpr int BM = BlockMax<T>::value;
+    static constexpr int LDS = BM + 1;   // column stride of the staged block (conflict-free rows and columns)
+    static constexpr size_t smem = sizeof(T) * ((size_t)BM * LDS + (size_t)32 * BM + 32);
+};
+
+template <typename T>
+__global__ void __launch_bounds__(PC_THREADS, 1) k_block_lu_pc(T* fac, int* ipiv, int* info, int* bmap, Sched S,
+                                                                Launch L, int step) {
+    constexpr int BM = BlockMax<T>::value, LDS = PcLu<T>::LDS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sA = reinterpret_cast<T*>(smem_raw);   // A(i, j) at sA[j * LDS + i]
+    T* sU = sA + BM * LDS;                    // U(a + k, b + c) of the current piece at sU[k * BM + c]
+    T* srv = sU + 32 * BM;                    // 1 / U(a + k, a + k)
+    __shared__ int q0[BM + 1], spiv[BM], sgm[32], sgmap[BM], sq[2];
+    __shared__ int szero;
+    int fid, tile;
+    locate(L, blockIdx.x, fid, tile);
+    const DFront F = S.fronts[fid];
+    const int blk = F.block0 + step;
+    const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
+    const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const bool sym = S.sym != 0;
+    for (int k = tid; k <= np; k += PC_THREADS) q0[k] = S.xsuper[p0 + k] - F.f - c0;
+    if (tid == 0) szero = INT_MAX;
+    T* blkp = fac + F.loff + (ll)c0 * F.ld + c0;   // block (i, j) at blkp[j * ld + i]
+    for (int e = tid; e < bw * bw; e += PC_THREADS) {
+        const int C = e / bw, R = e - C * bw;
+        // symmetric form: the upper triangle mirrors the lower one
+        sA[C * LDS + R] = (sym && R < C) ? blkp[(ll)R * F.ld + C] : blkp[(ll)C * F.ld + R];
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int pc = 0; pc < np; ++pc) {
+        const int a = q0[pc], b = q0[pc + 1], wd = b - a, nr = bw - b;
+        if (w == 0) {   // (1) the piece's diagonal block
+            if (lane == 0) {
+                sq[0] = 0;
+                sq[1] = wd;
+            }
+            T r[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) r[j] = (lane < wd && j < wd) ? sA[(a + j) * LDS + a + lane] : T(0);
+            __syncwarp();
+            const bool sing = warp_lu_sweep<T, 32>(r, wd, wd, sq, spiv + a, sym);
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                if (lane < wd && j < wd) sA[(a + j) * LDS + a + lane] = r[j];
+            const T d = pickw<32>(r, lane);
+            if (lane < wd) srv[lane] = d != T(0) ? T(1) / d : T(1);
+            if (sing) {   // uniform in the warp
+                const unsigned z = __ballot_sync(0xffffffffu, lane < wd && d == T(0));
+                if (lane == 0 && z) szero = min(szero, a + __ffs(z) - 1);
+            }
+            __syncwarp();
+            // the row now at position i of the piece came from row sgm[i]
+            int g = lane;
+            for (int k = 0; k < wd; ++k) {
+                const int kp = spiv[a + k];
+                const int vk = __shfl_sync(0xffffffffu, g, k), vp = __shfl_sync(0xffffffffu, g, kp);
+                g = lane == k ? vp : (lane == kp ? vk : g);
+            }
+            if (lane < wd) sgm[lane] = g;
+        }
+        __syncthreads();
+        // (2) U12 columns (threads 0..) and L21 rows (threads 256..) inside the block
+        if (tid < nr) {
+            const int j = b + tid;
+            T y[32];
+#pragma unroll
+            for (int i = 0; i < 32; ++i) y[i] = i < wd ? sA[j * LDS + a + sgm[i]] : T(0);
+#pragma unroll
+            for (int k = 0; k < 32; ++k)
+                if (k < wd) {
+#pragma unroll
+                    for (int i = k + 1; i < 32; ++i)
+                        if (i < wd) y[i] -= sA[(a + k) * LDS + a + i] * y[k];
+                }
+#pragma unroll
+            for (int i = 0; i < 32; ++i)
+                if (i < wd) {
+                    sA[j * LDS + a + i] = y[i];
+                    sU[i * BM + tid] = y[i];
+                }
+        } else if (tid >= PC_THREADS / 2 && tid - PC_THREADS / 2 < nr) {
+            const int rr = b + tid - PC_THREADS / 2;
+            T x[32];
+#pragma unroll
+            for (int k = 0; k < 32; ++k) x[k] = k < wd ? sA[(a + k) * LDS + rr] : T(0);
+#pragma unroll
+            for (int k = 0; k < 32; ++k)
+                if (k < wd) {
+                    x[k] *= srv[k];
+#pragma unroll
+                    for (int jj = k + 1; jj < 32; ++jj)
+                        if (jj < wd) x[jj] -= x[k] * sA[(a + jj) * LDS + a + k];
+                }
+#pragma unroll
+            for (int k = 0; k < 32; ++k)
+                if (k < wd) sA[(a + k) * LDS + rr] = x[k];
+        }
+        __syncthreads();
+        // (3) A22 -= L21 U12: warp per four columns, lane + 32 q on the rows
+        if (nr > 0) {
+            const int ncg = cdiv(nr, 4);
+            for (int cg = w; cg < ncg; cg += PC_THREADS / 32) {
+                const int j0 = 4 * cg;
+                T acc[4][4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) acc[q][c] = T(0);
+                for (int k = 0; k < wd; ++k) {
+                    T l[4], u[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) l[q] = lane + 32 * q < nr ? sA[(a + k) * LDS + b + lane + 32 * q] : T(0);
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) u[c] = sU[k * BM + j0 + c];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) acc[q][c] += l[q] * u[c];
+                }
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    if (j0 + c < nr)
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            if (lane + 32 * q < nr) sA[(b + j0 + c) * LDS + b + lane + 32 * q] -= acc[q][c];
+            }
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < bw * bw; e += PC_THREADS) {
+        const int C = e / bw, R = e - C * bw;
+        blkp[(ll)C * F.ld + R] = sA[C * LDS + R];
+    }
+    for (int c = tid; c < bw; c += PC_THREADS) ipiv[F.f + c0 + c] = spiv[c];
+    // Row sources of the block's interchanges (block_gather_map), a warp per
+    // piece: lane i tracks gmap[a + i] through the piece's swaps.
+    for (int pc = w; pc < np; pc += PC_THREADS / 32) {
+        const int a = q0[pc], b = q0[pc + 1];
+        int g = a + lane;
+        for (int k = a; k < b; ++k) {
+            const int kp = a + spiv[k];
+            const int vk = __shfl_sync(0xffffffffu, g, k - a), vp = __shfl_sync(0xffffffffu, g, kp - a);
+            g = lane == k - a ? vp : (lane == kp - a ? vk : g);
+        }
+        if (lane < b - a) bmap[F.f + c0 + a + lane] = g | (a << 8);
+    }
+    (void)sgmap;
     if (tid == 0 && szero != INT_MAX) {
         int p = 0;
         while (q0[p + 1] <= szero) ++p;

@@ -66,11 +66,13 @@ GPU_SYMBOLS = {
 SPK_OK, SPK_EARG, SPK_ECUDA, SPK_ENOMEM, SPK_ESEQ, SPK_ESTRUCT, SPK_ESINGULAR, SPK_ENOCONV = 0, -1, -2, -3, -4, -5, -6, -7
 SPK_ETIMEOUT = -8
 # spk_set_option / spk_get_option
-OPTIONS = {"leaf_queue": 0, "wait_budget": 1, "stall_test": 2, "tc_schur_m": 3, "tc_trail_rows": 4, "tc_wide": 5}
+OPTIONS = {"leaf_queue": 0, "wait_budget": 1, "stall_test": 2, "tc_schur_m": 3, "tc_trail_rows": 4, "tc_wide": 5,
+           "lu_pieces": 6}
 SPK_HOST, SPK_DEVICE = 0, 1
 KERNEL_CLASSES = ["assemble", "getrf", "panel", "trail", "schur", "fwd", "bwd", "permute", "residual", "blockinv",
                   "tc_trail", "tc_schur"]
-KERNEL_NAMES = {"assemble": "k_scatter_values", "getrf": "k_block_lu+k_block_lu_small+k_leaf_factor+k_leaf_queue",
+KERNEL_NAMES = {"assemble": "k_scatter_values",
+                "getrf": "k_block_lu_pc+k_block_lu+k_block_lu_small+k_leaf_factor+k_leaf_queue",
                 "panel": "k_block_panel",
                 "trail": "k_block_trail", "schur": "k_schur",
                 "fwd": "k_fwd+k_front_solve<fwd>+k_fwd_l21+k_solve_leaf<fwd>",

@@ -11,11 +11,17 @@ option autotuner, through the C ABI.
 * Wide tensor-core Schur tiles (128 x 256, SPK_OPT_TC_WIDE) against the
   128 x 128 ones: the same factors to FP32 rounding (the scatter-adds into
   the parents come in another order), in the FP32, BF16 and SPD forms.
+* The block LU by pieces (SPK_OPT_LU_PIECES, a warp per piece's diagonal
+  block, then the block's solves and update in parallel) against the
+  column-by-column form, on a dense block with real interchanges: the
+  oracle's pivots in both, FP64 factors within 1e-12.
 * spk_autotune chooses options from its set, leaves A assembled, and the
   factor that follows refines to 1e-12.
 """
 import numpy as np
 import pytest
+
+import scipy.sparse as sp
 
 import oracle
 import sparspak as S
@@ -140,6 +146,39 @@ def test_wide_schur_tiles_match_narrow(prec):
     d = rel(lnz[1], lnz[0])
     print(f"{prec}: wide vs narrow Schur tiles, factors differ by {d:.1e}")
     assert d < (5e-3 if base == "bf16s" else 1e-5)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp64+spd"])
+def test_block_lu_by_pieces_vs_columns(prec):
+    rng = np.random.default_rng(21)
+    n = 300
+    M = rng.standard_normal((n, n))
+    base, _, form = prec.partition("+")
+    if form == "spd":
+        A = sp.csc_matrix(M @ M.T / n + np.eye(n))
+    else:
+        A = sp.csc_matrix(M + 0.5 * np.sqrt(n) * np.eye(n))
+    s = _solver(A, None, precision=base, spd=form == "spd")
+    o = oracle.OracleLU(s.slvr)
+    o.inmatrix_csc(*_matrix_arrays(A))
+    assert (o.cholfactor() if form == "spd" else o.factor()) == 0
+    mask = o.lower_mask() if form == "spd" else slice(None)
+    b = S.gallery.random_rhs(n, 2, seed=3)
+    got = {}
+    for pcs in (1, 0):
+        eng = _factor_with(s, A, lu_pieces=pcs)
+        if form != "spd":
+            assert np.array_equal(s.slvr.ipiv, o.ipiv), pcs
+        got[pcs] = s.slvr.lnz.copy()
+        e = rel(got[pcs][mask], o.lnz[mask])
+        # the column form's rank-1 order differs from the reference's
+        # piece-wise trsm / gemm more than the piece form's (4.8e-12 here)
+        assert e <= ((1e-12 if pcs else 1e-11) if base == "fp64" else 5e-3), (pcs, e)
+        print(f"{prec} lu_pieces={pcs}: factors vs oracle {e:.1e}")
+        x = np.zeros_like(b, order="F")
+        it, rr = eng.refine(np.asfortranarray(b), x, prec, 1e-12, 30)
+        assert rr <= 1e-12 and relres(A, x, b) <= 1e-12
+    print(f"{prec}: by pieces vs column groups, factors differ by {rel(got[1], got[0]):.1e}")
 
 
 @pytest.mark.parametrize("prec", ["fp32", "fp64"])
