@@ -67,7 +67,7 @@ struct LevelPlan {
     LaunchRec front_big, front_l21;   // front_l21: tiles of k_fwd_l21 for the front_big fronts
     // Small fronts (one block of at most 32 columns, m <= spk::LEAF_M) by
     // k_solve_leaf, a warp per front; bwdu_small: U12 products of the others.
-    LaunchRec front_leaf, bwdu_small;
+    LaunchRec front_leaf[spk::LF_CLASSES], bwdu_small;   // front_leaf by width class (k_solve_leaf<W>)
     std::vector<LaunchRec> fwd_small, bwd_small;
 };
 
@@ -706,7 +706,11 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc, bool sym
                 fl1[k] = 2.0 * F.nf * (double)F.nf + 2.0 * F.nf * (double)F.m;   // per right-hand side and direction
                 wl1[k] = F.nf * (double)F.nf + F.nf * (double)F.m;
             }
-            add_launch(&P, L.front_leaf, ids, tl1, fl1, wl1);
+            for (int c = 0; c < spk::LF_CLASSES; ++c) {
+                std::vector<int> tc(nid);
+                for (size_t k = 0; k < nid; ++k) tc[k] = tl1[k] && spk::leaf_class(h->fronts[ids[k]].nf) == c ? 1 : 0;
+                add_launch(&P, L.front_leaf[c], ids, tc, fl1, wl1);
+            }
         }
         {
             std::vector<int> tbig(nid);
@@ -1292,6 +1296,19 @@ static int run_factor(spk_handle* h) {
     return via_graph(h, h->g_factor[graph_index<T>(h)], [&] { return factor_launches<T>(h); });
 }
 
+// k_solve_leaf of width class c over `count` fronts (chained launch).
+template <typename T, bool FWD>
+static cudaError_t launch_solve_leaf(int c, int count, cudaStream_t st, const T* fac, const T* inv, T* in, T* out,
+                                     const T* xs, int n, int nrhs, const spk::Sched& S, const spk::Launch& la) {
+    const int grid = (count + 7) / 8;
+    switch (c) {
+    case 0: return launch_chained(spk::k_solve_leaf<T, FWD, 4>, grid, 256, 0, st, fac, inv, in, out, xs, n, nrhs, S, la);
+    case 1: return launch_chained(spk::k_solve_leaf<T, FWD, 8>, grid, 256, 0, st, fac, inv, in, out, xs, n, nrhs, S, la);
+    case 2: return launch_chained(spk::k_solve_leaf<T, FWD, 16>, grid, 256, 0, st, fac, inv, in, out, xs, n, nrhs, S, la);
+    default: return launch_chained(spk::k_solve_leaf<T, FWD, 32>, grid, 256, 0, st, fac, inv, in, out, xs, n, nrhs, S, la);
+    }
+}
+
 // Solve in place on the permuted work vectors: wb (rhs, consumed) -> wx.
 template <typename T>
 static int run_solve_permuted(spk_handle* h, int nrhs, bool transpose) {
@@ -1330,10 +1347,12 @@ static int run_solve_permuted(spk_handle* h, int nrhs, bool transpose) {
     }
     constexpr size_t fc_smem = spk::FcSmem<T>::bytes;
     for (const LevelPlan& P : PL.levels) {
-        if (P.front_leaf.tiles > 0) {
-            LaunchScope ls(h, SPK_K_FWD, P.front_leaf.flops * nrhs, P.front_leaf.words * sizeof(T));
-            CU(h, launch_chained(spk::k_solve_leaf<T, true>, (P.front_leaf.count + 7) / 8, 256, 0, h->stream, fac, inv,
-                                 b, y, (const T*)nullptr, n, nrhs, S, launch_of(PL, P.front_leaf)));
+        for (int c = 0; c < spk::LF_CLASSES; ++c) {
+            const LaunchRec& R = P.front_leaf[c];
+            if (R.tiles == 0) continue;
+            LaunchScope ls(h, SPK_K_FWD, R.flops * nrhs, R.words * sizeof(T));
+            CU(h, (launch_solve_leaf<T, true>(c, R.count, h->stream, fac, inv, b, y, (const T*)nullptr, n, nrhs, S,
+                                              launch_of(PL, R))));
         }
         if (P.front_big.tiles > 0) {
             LaunchScope ls(h, SPK_K_FWD, P.front_big.flops * nrhs, P.front_big.words * sizeof(T));
@@ -1358,10 +1377,12 @@ static int run_solve_permuted(spk_handle* h, int nrhs, bool transpose) {
     }
     for (size_t l = PL.levels.size(); l-- > 0;) {
         const LevelPlan& P = PL.levels[l];
-        if (P.front_leaf.tiles > 0) {
-            LaunchScope ls(h, SPK_K_BWD, P.front_leaf.flops * nrhs, P.front_leaf.words * sizeof(T));
-            CU(h, launch_chained(spk::k_solve_leaf<T, false>, (P.front_leaf.count + 7) / 8, 256, 0, h->stream, fac, inv,
-                                 y, x, (const T*)x, n, nrhs, S, launch_of(PL, P.front_leaf)));
+        for (int c = 0; c < spk::LF_CLASSES; ++c) {
+            const LaunchRec& R = P.front_leaf[c];
+            if (R.tiles == 0) continue;
+            LaunchScope ls(h, SPK_K_BWD, R.flops * nrhs, R.words * sizeof(T));
+            CU(h, (launch_solve_leaf<T, false>(c, R.count, h->stream, fac, inv, y, x, (const T*)x, n, nrhs, S,
+                                               launch_of(PL, R))));
         }
         if (P.bwdu_small.tiles > 0) {
             LaunchScope ls(h, SPK_K_BWD, P.bwdu_small.flops * nrhs, P.bwdu_small.words * sizeof(T));

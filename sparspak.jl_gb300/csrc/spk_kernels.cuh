@@ -2875,13 +2875,21 @@ __global__ void __cluster_dims__(NC, 1, 1) __launch_bounds__(FC_THREADS, 1)
 //   forward:  y_F = Minv b_F; b[R_F] -= L21 y_F (atomics, the rows are
 //             shared with sibling fronts);
 //   backward: c_F = y_F - U12 x[R_F]; x_F = Uinv c_F.
-// Lane j holds column j of the front; the front's right-hand side values are
-// exchanged by shuffles.  Same operations as k_fwd / k_bwd_u12 / k_bwd.
+// Each launch holds fronts of one width class W (block width <= W, the
+// classes of k_leaf_factor).  Lane j holds column j of the front; the
+// front's right-hand side values are exchanged by shuffles.  Every factor
+// load of a pass (a lane's column of the operator, its row of L21, its part
+// of U12 for 32 rows) is issued before the first use, so that a pass waits
+// for one memory round trip, not one per column.  U12 x[R_F]: for W <= 8 a
+// lane per row accumulates all W columns and the warp reduces once at the
+// end; wider fronts keep a lane per column and shuffle x.  Same operations as
+// k_fwd / k_bwd_u12 / k_bwd.
 constexpr int LEAF_M = 128;
-template <typename T, bool FWD>
+template <typename T, bool FWD, int W>
 __global__ void __launch_bounds__(256) k_solve_leaf(const T* fac, const T* inv2, T* in, T* out, const T* xs, int n,
                                                      int nrhs, Sched S, Launch L) {
     constexpr int RG = 4;   // right-hand sides per pass
+    const unsigned FULL = 0xffffffffu;
     griddep_launch();
     const int lane = threadIdx.x & 31, idx = blockIdx.x * 8 + (threadIdx.x >> 5);
     if (idx >= L.count) return;   // whole warp
@@ -2896,34 +2904,73 @@ __global__ void __launch_bounds__(256) k_solve_leaf(const T* fac, const T* inv2,
 #pragma unroll
         for (int r = 0; r < RG; ++r) v[r] = (lane < bw && r < nr) ? in[(ll)(r0 + r) * n + F.f + lane] : T(0);
         if constexpr (!FWD) {   // c_F = y_F - U12 x[R_F] (U12 row j contiguous in Uf)
-            if (lane < bw) {
-                const T* u = fac + F.uoff + (ll)lane * F.m;
-                T acc[RG];
+            T acc[RG];
 #pragma unroll
-                for (int r = 0; r < RG; ++r) acc[r] = T(0);
-#pragma unroll 4
-                for (int i = 0; i < F.m; ++i) {
-                    const T uv = u[i];
-                    const int g = rows[i];
+            for (int r = 0; r < RG; ++r) acc[r] = T(0);
+            if constexpr (W <= 8) {
+                T pw[W][RG];   // lane: its rows' share of every column's sum
 #pragma unroll
-                    for (int r = 0; r < RG; ++r)
-                        if (r < nr) acc[r] += uv * xs[(ll)(r0 + r) * n + g];
+                for (int j = 0; j < W; ++j)
+#pragma unroll
+                    for (int r = 0; r < RG; ++r) pw[j][r] = T(0);
+                for (int i0 = 0; i0 < F.m; i0 += 32) {
+                    const int il = i0 + lane;
+                    const bool ok = il < F.m;
+                    const int g = ok ? rows[il] : 0;
+                    T uv[W], xv[RG];
+#pragma unroll
+                    for (int j = 0; j < W; ++j) uv[j] = (ok && j < bw) ? fac[F.uoff + (ll)j * F.m + il] : T(0);
+#pragma unroll
+                    for (int r = 0; r < RG; ++r) xv[r] = (ok && r < nr) ? xs[(ll)(r0 + r) * n + g] : T(0);
+#pragma unroll
+                    for (int j = 0; j < W; ++j)
+#pragma unroll
+                        for (int r = 0; r < RG; ++r) pw[j][r] += uv[j] * xv[r];
                 }
 #pragma unroll
-                for (int r = 0; r < RG; ++r) v[r] -= acc[r];
+                for (int j = 0; j < W; ++j)
+#pragma unroll
+                    for (int r = 0; r < RG; ++r) {
+                        T t = pw[j][r];
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(FULL, t, o);
+                        if (lane == j) acc[r] = t;
+                    }
+            } else {
+                const T* u = fac + F.uoff + (ll)lane * F.m;
+                for (int i0 = 0; i0 < F.m; i0 += 32) {
+                    // lane l: x at row R_F[i0 + l]; lane j: U12(j, i0 ..)
+                    const int il = i0 + lane;
+                    T xv[RG];
+                    const int g = il < F.m ? rows[il] : 0;
+#pragma unroll
+                    for (int r = 0; r < RG; ++r) xv[r] = (il < F.m && r < nr) ? xs[(ll)(r0 + r) * n + g] : T(0);
+                    T uv[32];
+#pragma unroll
+                    for (int q = 0; q < 32; ++q) uv[q] = (lane < bw && i0 + q < F.m) ? u[i0 + q] : T(0);
+#pragma unroll
+                    for (int q = 0; q < 32; ++q) {
+                        if (i0 + q < F.m) {   // uniform
+#pragma unroll
+                            for (int r = 0; r < RG; ++r) acc[r] += uv[q] * __shfl_sync(FULL, xv[r], q);
+                        }
+                    }
+                }
             }
+#pragma unroll
+            for (int r = 0; r < RG; ++r) v[r] -= acc[r];
         }
-        T y[RG];   // lane j: sum_k op(j, k) v_k, op(j, k) at Mi[k * bw + j]
+        T mv[W];   // op(lane, k), op(j, k) at Mi[k * bw + j]
+#pragma unroll
+        for (int k = 0; k < W; ++k) mv[k] = (k < bw && lane < bw && (FWD || k >= lane)) ? Mi[(ll)k * bw + lane] : T(0);
+        T y[RG];   // lane j: sum_k op(j, k) v_k
 #pragma unroll
         for (int r = 0; r < RG; ++r) y[r] = T(0);
-        for (int k = 0; k < bw; ++k) {
-            T vk[RG];
 #pragma unroll
-            for (int r = 0; r < RG; ++r) vk[r] = __shfl_sync(0xffffffffu, v[r], k);
-            if (lane < bw && (FWD || k >= lane)) {
-                const T mv = Mi[(ll)k * bw + lane];
+        for (int k = 0; k < W; ++k) {
+            if (k < bw) {   // uniform
 #pragma unroll
-                for (int r = 0; r < RG; ++r) y[r] += mv * vk[r];
+                for (int r = 0; r < RG; ++r) y[r] += mv[k] * __shfl_sync(FULL, v[r], k);
             }
         }
         if (lane < bw)
@@ -2933,17 +2980,17 @@ __global__ void __launch_bounds__(256) k_solve_leaf(const T* fac, const T* inv2,
         if constexpr (FWD) {   // b[R_F] -= L21 y_F (L21 column k contiguous in Lf)
             for (int i0 = 0; i0 < F.m; i0 += 32) {
                 const int i = i0 + lane;
+                T lv[W];   // this lane's row of L21
+#pragma unroll
+                for (int k = 0; k < W; ++k) lv[k] = (k < bw && i < F.m) ? fac[F.loff + (ll)k * F.ld + F.nf + i] : T(0);
                 T acc[RG];
 #pragma unroll
                 for (int r = 0; r < RG; ++r) acc[r] = T(0);
-                for (int k = 0; k < bw; ++k) {
-                    T yk[RG];
 #pragma unroll
-                    for (int r = 0; r < RG; ++r) yk[r] = __shfl_sync(0xffffffffu, y[r], k);
-                    if (i < F.m) {
-                        const T lv = fac[F.loff + (ll)k * F.ld + F.nf + i];
+                for (int k = 0; k < W; ++k) {
+                    if (k < bw) {   // uniform
 #pragma unroll
-                        for (int r = 0; r < RG; ++r) acc[r] += lv * yk[r];
+                        for (int r = 0; r < RG; ++r) acc[r] += lv[k] * __shfl_sync(FULL, y[r], k);
                     }
                 }
                 if (i < F.m)
