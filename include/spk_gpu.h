@@ -318,6 +318,10 @@ int spk_measure_peaks(double* fp32_tflops, double* fp64_tflops, double* dmma_tfl
  *                        rounding, but a slower chain on GB300 (the piece's
  *                        column steps are as long as the block form's);
  *                        0 (default): every wide block in column groups.
+ *  SPK_OPT_SOLVE_CLUSTER_MINB  fronts of at least this many blocks (2..128,
+ *                        default 4) are solved by one 16-CTA cluster each
+ *                        (all block steps in one launch); smaller ones by a
+ *                        launch per block step.  Keeps the factors.
  */
 #define SPK_OPT_LEAF_QUEUE 0
 #define SPK_OPT_WAIT_BUDGET 1
@@ -326,6 +330,7 @@ int spk_measure_peaks(double* fp32_tflops, double* fp64_tflops, double* dmma_tfl
 #define SPK_OPT_TC_TRAIL_ROWS 4
 #define SPK_OPT_TC_WIDE 5
 #define SPK_OPT_LU_PIECES 6
+#define SPK_OPT_SOLVE_CLUSTER_MINB 7
 int spk_set_option(spk_handle* h, int option, int64_t value);
 int spk_get_option(spk_handle* h, int option, int64_t* value);
 

@@ -210,6 +210,7 @@ struct spk_handle {
     int tc_schur_m = TC_SCHUR_M, tc_trail_rows = TC_TRAIL_ROWS;
     int tc_wide = 1;                       // SPK_OPT_TC_WIDE: Schur tiles of 128 x 256
     int lu_pieces = 0;                     // SPK_OPT_LU_PIECES: block LU by pieces (slower on GB300, see header)
+    int fc_minb = spk::FC_MINB;            // SPK_OPT_SOLVE_CLUSTER_MINB: blocks of a front for the cluster solve
     std::string err;
 
     // launch accounting and optional per-class event timing
@@ -718,7 +719,7 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc, bool sym
             for (size_t k = 0; k < nid; ++k) {
                 const HFront& F = h->fronts[ids[k]];
                 const int nb = P.nblocks[ids[k]];
-                big[k] = nb >= spk::FC_MINB && nb <= spk::FC * spk::FC_OWN;
+                big[k] = nb >= h->fc_minb && nb <= spk::FC * spk::FC_OWN;
                 tbig[k] = big[k] ? 1 : 0;
                 const double nf = F.nf;
                 fbig[k] = 2.0 * nf * nf;   // per right-hand side, both directions alike
@@ -1292,6 +1293,8 @@ static int factor_launches(spk_handle* h) {
 template <typename T>
 static int run_factor(spk_handle* h) {
     static const int init[3] = {INT_MAX, 0, 0};
+    int rc = ensure_plan<T>(h);   // rebuilt after an option dropped it
+    if (rc) return rc;
     CU(h, cudaMemcpyAsync(h->d_info, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
     return via_graph(h, h->g_factor[graph_index<T>(h)], [&] { return factor_launches<T>(h); });
 }
@@ -1361,7 +1364,8 @@ static int run_solve_permuted(spk_handle* h, int nrhs, bool transpose) {
                     fac, inv, b, y, n, nrhs, S, launch_of(PL, P.front_big));
             else
                 spk::k_front_solve<T, true, spk::FC><<<spk::FC * P.front_big.tiles, spk::FC_THREADS, fc_smem,
-                                                       h->stream>>>(fac, inv, b, y, n, nrhs, S, launch_of(PL, P.front_big));
+                                                       h->stream>>>(fac, inv, b, y, n, nrhs, S,
+                                                                    launch_of(PL, P.front_big));
         }
         if (P.front_l21.tiles > 0) {
             LaunchScope ls(h, SPK_K_FWD, P.front_l21.flops * nrhs, P.front_l21.words * sizeof(T));
@@ -1396,7 +1400,8 @@ static int run_solve_permuted(spk_handle* h, int nrhs, bool transpose) {
                     fac, inv, y, x, n, nrhs, S, launch_of(PL, P.front_big));
             else
                 spk::k_front_solve<T, false, spk::FC><<<spk::FC * P.front_big.tiles, spk::FC_THREADS, fc_smem,
-                                                        h->stream>>>(fac, inv, y, x, n, nrhs, S, launch_of(PL, P.front_big));
+                                                        h->stream>>>(fac, inv, y, x, n, nrhs, S,
+                                                                     launch_of(PL, P.front_big));
         }
         for (size_t t = 0; t < P.bwd_small.size(); ++t)
             if (P.bwd_small[t].tiles > 0) {
@@ -1415,6 +1420,8 @@ template <typename T>
 static int solve_device(spk_handle* h, const double* rhs, i64 ldr, double* x, i64 ldx, i64 nrhs, int accumulate,
                         bool transpose = false) {
     const int n = (int)h->n;
+    int rc0 = ensure_plan<T>(h);   // rebuilt after an option dropped it (the factors are kept)
+    if (rc0) return rc0;
     for (i64 c0 = 0; c0 < nrhs; c0 += spk::MAXRHS) {
         int nc = (int)std::min<i64>(spk::MAXRHS, nrhs - c0);
         ll tot = (ll)n * nc;
@@ -1909,6 +1916,14 @@ static void reset_float_plans(spk_handle* h) {
     drop_solve_graphs(h);
 }
 
+// Drop every plan and captured graph but keep the factors (an option that
+// changes only the solves' launch lists).
+static void reset_plans_keep_factors(spk_handle* h) {
+    for (Plan& P : h->plan) free_plan(P);
+    for (GraphRec& g : h->g_factor) drop_graph(g);
+    drop_solve_graphs(h);
+}
+
 int spk_set_option(spk_handle* h, int option, int64_t value) {
     int rc = check_h(h);
     if (rc) return rc;
@@ -1927,6 +1942,13 @@ int spk_set_option(spk_handle* h, int option, int64_t value) {
         if (value < -1 || value > INT_MAX) break;
         h->stall_test = (int)value;
         for (GraphRec& g : h->g_factor) drop_graph(g);
+        return SPK_OK;
+    case SPK_OPT_SOLVE_CLUSTER_MINB:
+        if (value < 2 || value > spk::FC * spk::FC_OWN) break;
+        if (h->fc_minb != (int)value) {
+            h->fc_minb = (int)value;
+            reset_plans_keep_factors(h);
+        }
         return SPK_OK;
     case SPK_OPT_LU_PIECES:
         if (value != 0 && value != 1) break;
@@ -1963,6 +1985,7 @@ int spk_get_option(spk_handle* h, int option, int64_t* value) {
     case SPK_OPT_TC_TRAIL_ROWS: *value = h->tc_trail_rows; return SPK_OK;
     case SPK_OPT_TC_WIDE: *value = h->tc_wide; return SPK_OK;
     case SPK_OPT_LU_PIECES: *value = h->lu_pieces; return SPK_OK;
+    case SPK_OPT_SOLVE_CLUSTER_MINB: *value = h->fc_minb; return SPK_OK;
     default: return set_err(h, SPK_EARG, "spk_get_option: unknown option");
     }
 }

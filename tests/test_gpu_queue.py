@@ -15,6 +15,8 @@ option autotuner, through the C ABI.
   block, then the block's solves and update in parallel) against the
   column-by-column form, on a dense block with real interchanges: the
   oracle's pivots in both, FP64 factors within 1e-12.
+* The cluster-solve threshold (SPK_OPT_SOLVE_CLUSTER_MINB) changes only the
+  solves' launch lists: the factors are kept, and the solutions agree.
 * spk_autotune chooses options from its set, leaves A assembled, and the
   factor that follows refines to 1e-12.
 """
@@ -179,6 +181,22 @@ def test_block_lu_by_pieces_vs_columns(prec):
         it, rr = eng.refine(np.asfortranarray(b), x, prec, 1e-12, 30)
         assert rr <= 1e-12 and relres(A, x, b) <= 1e-12
     print(f"{prec}: by pieces vs column groups, factors differ by {rel(got[1], got[0]):.1e}")
+
+
+def test_solve_cluster_threshold_keeps_factors():
+    A = S.gallery.laplacian((24, 24, 24), shift=1e-3)
+    n = A.shape[0]
+    s = _solver(A, S.nd_grid(24, 24, 24))
+    eng = _factor_with(s, A)
+    b = S.gallery.random_rhs(n, 3, seed=2)
+    xs = {}
+    for mb in (4, 2, 128):
+        eng.set_option("solve_cluster_minb", mb)   # no new factorisation
+        xs[mb] = eng.solve(np.array(b, order="F"))
+        assert relres(A, xs[mb], b) <= 1e-12, mb
+    assert rel(xs[2], xs[4]) < 1e-12 and rel(xs[128], xs[4]) < 1e-12
+    with pytest.raises(S.ErrorException):
+        eng.set_option("solve_cluster_minb", 1)
 
 
 @pytest.mark.parametrize("prec", ["fp32", "fp64"])
