@@ -177,6 +177,21 @@ int spk_refine(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t 
 int spk_refine_ex(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where, int precision,
                   double tol, int max_iter, int solver, int* iters, double* relres, int* solver_used);
 
+/*
+ * Factorisation and refined solve in one call (the role of the reference's
+ * solve!, which runs factor! and the triangular solve in turn,
+ * src/SparseMethod/SpkSparseSolver.jl:237-256): spk_factor, then
+ * spk_refine_ex, with the first solve's forward substitution of all but the
+ * last two levels of the front tree run beside the factorisation of those
+ * two levels (once its fronts are final).  Same arguments and results as
+ * spk_refine_ex, plus *first_singular (may be NULL) as spk_factor.  At most
+ * MAXRHS (16) right-hand sides take the overlapped path; more are factored
+ * and refined one after the other.
+ */
+int spk_factor_refine(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where, int precision,
+                      double tol, int max_iter, int solver, int* iters, double* relres, int* solver_used,
+                      int64_t* first_singular);
+
 /* Iterative refinement of A^T x = b (spk_solve_transpose and the FP64
  * residual b - A^T x), arguments and results as spk_refine. */
 int spk_refine_transpose(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where,

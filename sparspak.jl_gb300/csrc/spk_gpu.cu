@@ -226,6 +226,11 @@ struct spk_handle {
     bool use_graphs = true;
     // [0] FP64, [1] FP32, [2] BF16S; + 3 for the SPD form
     GraphRec g_factor[6];
+    // fused factorisation + first solve (spk_factor_refine), per right-hand
+    // sides: the factorisation with the lower levels' forward substitution,
+    // and the rest of that solve
+    GraphRec g_factor_fs[6][spk::MAXRHS + 1];
+    GraphRec g_fs_tail[6][spk::MAXRHS + 1];
     GraphRec g_solve[6][spk::MAXRHS + 1];
     GraphRec g_tsolve[6][spk::MAXRHS + 1];   // transposed solves
 };
@@ -335,6 +340,18 @@ static void drop_solve_graphs(spk_handle* h) {
         for (int r = 0; r <= spk::MAXRHS; ++r) {
             drop_graph(h->g_solve[p][r]);
             drop_graph(h->g_tsolve[p][r]);
+            drop_graph(h->g_factor_fs[p][r]);
+            drop_graph(h->g_fs_tail[p][r]);
+        }
+}
+
+// Every captured factorisation (plain and fused with a solve).
+static void drop_factor_graphs(spk_handle* h) {
+    for (GraphRec& g : h->g_factor) drop_graph(g);
+    for (int p = 0; p < 6; ++p)
+        for (int r = 0; r <= spk::MAXRHS; ++r) {
+            drop_graph(h->g_factor_fs[p][r]);
+            drop_graph(h->g_fs_tail[p][r]);
         }
 }
 
@@ -1127,7 +1144,23 @@ static cudaError_t launch_leaf(int c, const spk::Launch& la, T* fac, int* ipiv, 
 }
 
 template <typename T>
-static int factor_launches(spk_handle* h) {
+static int solve_fwd_levels(spk_handle* h, int nrhs, size_t l0, size_t l1, cudaStream_t st);
+
+// Levels whose forward substitution a fused factorisation + solve runs
+// inside the factorisation: those below inv_split, on the second stream
+// once their block operators are formed (not while timing kernels one by
+// one, when nothing runs on the side streams).
+template <typename T>
+static size_t fused_split(const spk_handle* h) {
+    const Plan& PL = h->plan[plan_index<T>(h)];
+    return h->prof_mask == 0 && PL.inv_split > 0 ? (size_t)PL.inv_split : 0;
+}
+
+// The factorisation's launches.  fs_nrhs > 0: also the forward
+// substitution of the levels below fused_split for fs_nrhs right-hand sides
+// held in d_rhs (leading dimension n), overlapped with the last levels.
+template <typename T>
+static int factor_launches(spk_handle* h, int fs_nrhs = 0) {
     constexpr int BM = spk::BlockMax<T>::value;
     T* fac = storage<T>(h).d;
     const Plan& PL = h->plan[plan_index<T>(h)];
@@ -1168,11 +1201,20 @@ static int factor_launches(spk_handle* h) {
     }
     for (size_t lvl = 0; lvl < PL.levels.size(); ++lvl) {
         const LevelPlan& P = PL.levels[lvl];
-        if (ahead && (int)lvl == PL.inv_split && PL.inv_off[0][3] > PL.inv_off[0][0]) {
+        const bool fs_here = fs_nrhs > 0 && (size_t)lvl == fused_split<T>(h) && lvl > 0;
+        if (ahead && (int)lvl == PL.inv_split && (PL.inv_off[0][3] > PL.inv_off[0][0] || fs_here)) {
             // group 0's blocks are final: their operators beside the last levels
             CU(h, cudaEventRecord(h->evP2, h->stream));
             CU(h, cudaStreamWaitEvent(h->side2, h->evP2, 0));
             launch_inv(0, h->side2);
+            if (fs_here) {   // and the forward substitution of those levels (a plain launch first)
+                const ll tot = (ll)h->n * fs_nrhs;
+                LaunchScope ls(h, SPK_K_PERMUTE, 0.0, (double)tot * (8 + 4 + sizeof(T)));
+                spk::k_permute<double, T><<<(int)((tot + 255) / 256), 256, 0, h->side2>>>(
+                    h->d_rhs, h->n, (T*)h->d_wb, (int)h->n, h->d_rperm, (int)h->n, fs_nrhs);
+                int rc = solve_fwd_levels<T>(h, fs_nrhs, 0, lvl, h->side2);
+                if (rc) return rc;
+            }
             CU(h, cudaEventRecord(h->evI, h->side2));
             pending_inv = true;
         }
@@ -1312,6 +1354,99 @@ static cudaError_t launch_solve_leaf(int c, int count, cudaStream_t st, const T*
     }
 }
 
+// The forward substitution over levels [l0, l1) on the permuted work
+// vectors (wb, consumed, -> wy), launched on `st`.
+template <typename T>
+static int solve_fwd_levels(spk_handle* h, int nrhs, size_t l0, size_t l1, cudaStream_t st) {
+    const T* fac = storage<T>(h).d;
+    const T* inv = storage<T>(h).inv2;
+    const Plan& PL = h->plan[plan_index<T>(h)];
+    const spk::Sched& S = PL.sched;
+    T* b = (T*)h->d_wb;
+    T* y = (T*)h->d_wy;
+    const int n = (int)h->n;
+    constexpr size_t fc_smem = spk::FcSmem<T>::bytes;
+    for (size_t l = l0; l < l1; ++l) {
+        const LevelPlan& P = PL.levels[l];
+        for (int c = 0; c < spk::LF_CLASSES; ++c) {
+            const LaunchRec& R = P.front_leaf[c];
+            if (R.tiles == 0) continue;
+            LaunchScope ls(h, SPK_K_FWD, R.flops * nrhs, R.words * sizeof(T));
+            CU(h, (launch_solve_leaf<T, true>(c, R.count, st, fac, inv, b, y, (const T*)nullptr, n, nrhs, S,
+                                              launch_of(PL, R))));
+        }
+        if (P.front_big.tiles > 0) {
+            LaunchScope ls(h, SPK_K_FWD, P.front_big.flops * nrhs, P.front_big.words * sizeof(T));
+            if (h->fc16)
+                spk::k_front_solve<T, true, 16><<<16 * P.front_big.tiles, spk::FC_THREADS, fc_smem, st>>>(
+                    fac, inv, b, y, n, nrhs, S, launch_of(PL, P.front_big));
+            else
+                spk::k_front_solve<T, true, spk::FC><<<spk::FC * P.front_big.tiles, spk::FC_THREADS, fc_smem,
+                                                       st>>>(fac, inv, b, y, n, nrhs, S,
+                                                                    launch_of(PL, P.front_big));
+        }
+        if (P.front_l21.tiles > 0) {
+            LaunchScope ls(h, SPK_K_FWD, P.front_l21.flops * nrhs, P.front_l21.words * sizeof(T));
+            CU(h, launch_chained(spk::k_fwd_l21<T>, P.front_l21.tiles, 256, 0, st, fac, b, (const T*)y, n, nrhs,
+                                 S, launch_of(PL, P.front_l21)));
+        }
+        for (size_t t = 0; t < P.fwd_small.size(); ++t)
+            if (P.fwd_small[t].tiles > 0) {
+                LaunchScope ls(h, SPK_K_FWD, P.fwd_small[t].flops * nrhs, P.fwd_small[t].words * sizeof(T));
+                CU(h, launch_chained(spk::k_fwd<T>, P.fwd_small[t].tiles, spk::TS, 0, st, fac, inv, b, y, n,
+                                     nrhs, S, launch_of(PL, P.fwd_small[t]), (int)t));
+            }
+    }
+    CU(h, cudaGetLastError());
+    return SPK_OK;
+}
+
+// The backward substitution over every level (wy -> wx), launched on `st`.
+template <typename T>
+static int solve_bwd_levels(spk_handle* h, int nrhs, cudaStream_t st) {
+    const T* fac = storage<T>(h).d;
+    const T* inv = storage<T>(h).inv2;
+    const Plan& PL = h->plan[plan_index<T>(h)];
+    const spk::Sched& S = PL.sched;
+    T* y = (T*)h->d_wy;
+    T* x = (T*)h->d_wx;
+    const int n = (int)h->n;
+    constexpr size_t fc_smem = spk::FcSmem<T>::bytes;
+    for (size_t l = PL.levels.size(); l-- > 0;) {
+        const LevelPlan& P = PL.levels[l];
+        for (int c = 0; c < spk::LF_CLASSES; ++c) {
+            const LaunchRec& R = P.front_leaf[c];
+            if (R.tiles == 0) continue;
+            LaunchScope ls(h, SPK_K_BWD, R.flops * nrhs, R.words * sizeof(T));
+            CU(h, (launch_solve_leaf<T, false>(c, R.count, st, fac, inv, y, x, (const T*)x, n, nrhs, S,
+                                               launch_of(PL, R))));
+        }
+        if (P.bwdu_small.tiles > 0) {
+            LaunchScope ls(h, SPK_K_BWD, P.bwdu_small.flops * nrhs, P.bwdu_small.words * sizeof(T));
+            CU(h, launch_chained(spk::k_bwd_u12<T>, P.bwdu_small.tiles, 256, 0, st, fac, y, x, n, nrhs, S,
+                                 launch_of(PL, P.bwdu_small)));
+        }
+        if (P.front_big.tiles > 0) {
+            LaunchScope ls(h, SPK_K_BWD, P.front_big.flops * nrhs, P.front_big.words * sizeof(T));
+            if (h->fc16)
+                spk::k_front_solve<T, false, 16><<<16 * P.front_big.tiles, spk::FC_THREADS, fc_smem, st>>>(
+                    fac, inv, y, x, n, nrhs, S, launch_of(PL, P.front_big));
+            else
+                spk::k_front_solve<T, false, spk::FC><<<spk::FC * P.front_big.tiles, spk::FC_THREADS, fc_smem,
+                                                        st>>>(fac, inv, y, x, n, nrhs, S,
+                                                                     launch_of(PL, P.front_big));
+        }
+        for (size_t t = 0; t < P.bwd_small.size(); ++t)
+            if (P.bwd_small[t].tiles > 0) {
+                LaunchScope ls(h, SPK_K_BWD, P.bwd_small[t].flops * nrhs, P.bwd_small[t].words * sizeof(T));
+                CU(h, launch_chained(spk::k_bwd<T>, P.bwd_small[t].tiles, spk::TS, 0, st, fac, inv, y, x, n,
+                                     nrhs, S, launch_of(PL, P.bwd_small[t]), (int)t));
+            }
+    }
+    CU(h, cudaGetLastError());
+    return SPK_OK;
+}
+
 // Solve in place on the permuted work vectors: wb (rhs, consumed) -> wx.
 template <typename T>
 static int run_solve_permuted(spk_handle* h, int nrhs, bool transpose) {
@@ -1348,70 +1483,9 @@ static int run_solve_permuted(spk_handle* h, int nrhs, bool transpose) {
         CU(h, cudaGetLastError());
         return SPK_OK;
     }
-    constexpr size_t fc_smem = spk::FcSmem<T>::bytes;
-    for (const LevelPlan& P : PL.levels) {
-        for (int c = 0; c < spk::LF_CLASSES; ++c) {
-            const LaunchRec& R = P.front_leaf[c];
-            if (R.tiles == 0) continue;
-            LaunchScope ls(h, SPK_K_FWD, R.flops * nrhs, R.words * sizeof(T));
-            CU(h, (launch_solve_leaf<T, true>(c, R.count, h->stream, fac, inv, b, y, (const T*)nullptr, n, nrhs, S,
-                                              launch_of(PL, R))));
-        }
-        if (P.front_big.tiles > 0) {
-            LaunchScope ls(h, SPK_K_FWD, P.front_big.flops * nrhs, P.front_big.words * sizeof(T));
-            if (h->fc16)
-                spk::k_front_solve<T, true, 16><<<16 * P.front_big.tiles, spk::FC_THREADS, fc_smem, h->stream>>>(
-                    fac, inv, b, y, n, nrhs, S, launch_of(PL, P.front_big));
-            else
-                spk::k_front_solve<T, true, spk::FC><<<spk::FC * P.front_big.tiles, spk::FC_THREADS, fc_smem,
-                                                       h->stream>>>(fac, inv, b, y, n, nrhs, S,
-                                                                    launch_of(PL, P.front_big));
-        }
-        if (P.front_l21.tiles > 0) {
-            LaunchScope ls(h, SPK_K_FWD, P.front_l21.flops * nrhs, P.front_l21.words * sizeof(T));
-            CU(h, launch_chained(spk::k_fwd_l21<T>, P.front_l21.tiles, 256, 0, h->stream, fac, b, (const T*)y, n, nrhs,
-                                 S, launch_of(PL, P.front_l21)));
-        }
-        for (size_t t = 0; t < P.fwd_small.size(); ++t)
-            if (P.fwd_small[t].tiles > 0) {
-                LaunchScope ls(h, SPK_K_FWD, P.fwd_small[t].flops * nrhs, P.fwd_small[t].words * sizeof(T));
-                CU(h, launch_chained(spk::k_fwd<T>, P.fwd_small[t].tiles, spk::TS, 0, h->stream, fac, inv, b, y, n,
-                                     nrhs, S, launch_of(PL, P.fwd_small[t]), (int)t));
-            }
-    }
-    for (size_t l = PL.levels.size(); l-- > 0;) {
-        const LevelPlan& P = PL.levels[l];
-        for (int c = 0; c < spk::LF_CLASSES; ++c) {
-            const LaunchRec& R = P.front_leaf[c];
-            if (R.tiles == 0) continue;
-            LaunchScope ls(h, SPK_K_BWD, R.flops * nrhs, R.words * sizeof(T));
-            CU(h, (launch_solve_leaf<T, false>(c, R.count, h->stream, fac, inv, y, x, (const T*)x, n, nrhs, S,
-                                               launch_of(PL, R))));
-        }
-        if (P.bwdu_small.tiles > 0) {
-            LaunchScope ls(h, SPK_K_BWD, P.bwdu_small.flops * nrhs, P.bwdu_small.words * sizeof(T));
-            CU(h, launch_chained(spk::k_bwd_u12<T>, P.bwdu_small.tiles, 256, 0, h->stream, fac, y, x, n, nrhs, S,
-                                 launch_of(PL, P.bwdu_small)));
-        }
-        if (P.front_big.tiles > 0) {
-            LaunchScope ls(h, SPK_K_BWD, P.front_big.flops * nrhs, P.front_big.words * sizeof(T));
-            if (h->fc16)
-                spk::k_front_solve<T, false, 16><<<16 * P.front_big.tiles, spk::FC_THREADS, fc_smem, h->stream>>>(
-                    fac, inv, y, x, n, nrhs, S, launch_of(PL, P.front_big));
-            else
-                spk::k_front_solve<T, false, spk::FC><<<spk::FC * P.front_big.tiles, spk::FC_THREADS, fc_smem,
-                                                        h->stream>>>(fac, inv, y, x, n, nrhs, S,
-                                                                     launch_of(PL, P.front_big));
-        }
-        for (size_t t = 0; t < P.bwd_small.size(); ++t)
-            if (P.bwd_small[t].tiles > 0) {
-                LaunchScope ls(h, SPK_K_BWD, P.bwd_small[t].flops * nrhs, P.bwd_small[t].words * sizeof(T));
-                CU(h, launch_chained(spk::k_bwd<T>, P.bwd_small[t].tiles, spk::TS, 0, h->stream, fac, inv, y, x, n,
-                                     nrhs, S, launch_of(PL, P.bwd_small[t]), (int)t));
-            }
-    }
-    CU(h, cudaGetLastError());
-    return SPK_OK;
+    int rc = solve_fwd_levels<T>(h, nrhs, 0, PL.levels.size(), h->stream);
+    if (rc) return rc;
+    return solve_bwd_levels<T>(h, nrhs, h->stream);
 }
 
 // x(:, 0:nrhs) (=|+=) A^{-1} rhs(:, 0:nrhs) (A^{-T} with `transpose`), both
@@ -1912,7 +1986,7 @@ static void reset_float_plans(spk_handle* h) {
             S->loaded = S->factored = false;
         }
     }
-    for (GraphRec& g : h->g_factor) drop_graph(g);
+    drop_factor_graphs(h);
     drop_solve_graphs(h);
 }
 
@@ -1920,7 +1994,7 @@ static void reset_float_plans(spk_handle* h) {
 // changes only the solves' launch lists).
 static void reset_plans_keep_factors(spk_handle* h) {
     for (Plan& P : h->plan) free_plan(P);
-    for (GraphRec& g : h->g_factor) drop_graph(g);
+    drop_factor_graphs(h);
     drop_solve_graphs(h);
 }
 
@@ -1931,17 +2005,17 @@ int spk_set_option(spk_handle* h, int option, int64_t value) {
     case SPK_OPT_LEAF_QUEUE:
         if (value != 0 && value != 1) break;
         h->leaf_queue = (int)value;
-        for (GraphRec& g : h->g_factor) drop_graph(g);
+        drop_factor_graphs(h);
         return SPK_OK;
     case SPK_OPT_WAIT_BUDGET:
         if (value < 1 || value > 0xffffffffLL) break;
         h->wait_budget = value;
-        for (GraphRec& g : h->g_factor) drop_graph(g);
+        drop_factor_graphs(h);
         return SPK_OK;
     case SPK_OPT_STALL_TEST:
         if (value < -1 || value > INT_MAX) break;
         h->stall_test = (int)value;
-        for (GraphRec& g : h->g_factor) drop_graph(g);
+        drop_factor_graphs(h);
         return SPK_OK;
     case SPK_OPT_SOLVE_CLUSTER_MINB:
         if (value < 2 || value > spk::FC * spk::FC_OWN) break;
@@ -1953,7 +2027,7 @@ int spk_set_option(spk_handle* h, int option, int64_t value) {
     case SPK_OPT_LU_PIECES:
         if (value != 0 && value != 1) break;
         h->lu_pieces = (int)value;
-        for (GraphRec& g : h->g_factor) drop_graph(g);
+        drop_factor_graphs(h);
         return SPK_OK;
     case SPK_OPT_TC_SCHUR_M:
     case SPK_OPT_TC_TRAIL_ROWS:
@@ -2188,9 +2262,11 @@ int spk_residual_noalloc(spk_handle* h, const double* b, const double* x, int64_
     return SPK_OK;
 }
 
+// first_done: the first solve has run (spk_factor_refine): its solution is
+// in x (device) or d_x (host b), and a host b is already in d_rhs.
 static int refine_impl(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where, int precision,
                        double tol, int max_iter, int solver, int* iters, double* relres, int* solver_used,
-                       bool transpose) {
+                       bool transpose, bool first_done = false) {
     int rc = check_h(h);
     if (rc) return rc;
     if (iters) *iters = 0;
@@ -2207,8 +2283,9 @@ static int refine_impl(spk_handle* h, const double* b, double* x, int64_t nrhs, 
     double* dx;
     i64 ldb, ldx;
     if (where == SPK_HOST) {
-        CU(h, cudaMemcpy2DAsync(h->d_rhs, sizeof(double) * n, b, sizeof(double) * ld, sizeof(double) * n, nrhs,
-                                cudaMemcpyHostToDevice, h->stream));
+        if (!first_done)
+            CU(h, cudaMemcpy2DAsync(h->d_rhs, sizeof(double) * n, b, sizeof(double) * ld, sizeof(double) * n, nrhs,
+                                    cudaMemcpyHostToDevice, h->stream));
         db = h->d_rhs;
         dx = h->d_x;
         ldb = ldx = n;
@@ -2221,7 +2298,7 @@ static int refine_impl(spk_handle* h, const double* b, double* x, int64_t nrhs, 
         return is_fp64(precision) ? solve_device<double>(h, rhs, ldr, dx, ldx, nrhs, acc, transpose)
                                      : solve_device<float>(h, rhs, ldr, dx, ldx, nrhs, acc, transpose);
     };
-    if ((rc = solve_into(db, ldb, 0))) return rc;
+    if (!first_done && (rc = solve_into(db, ldb, 0))) return rc;
     double rel = 0.0, prev = 0.0;
     int it = 0;
     bool gmres = solver == SPK_SOLVER_GMRES;
@@ -2291,6 +2368,91 @@ int spk_refine(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t 
 int spk_refine_ex(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where, int precision,
                   double tol, int max_iter, int solver, int* iters, double* relres, int* solver_used) {
     return refine_impl(h, b, x, nrhs, ld, where, precision, tol, max_iter, solver, iters, relres, solver_used, false);
+}
+
+}  // extern "C"
+
+// Factorisation and the first solve of the refinement, the forward
+// substitution of the lower levels overlapped with the last levels of the
+// factorisation; then refinement as spk_refine_ex.
+template <typename T>
+static int factor_refine_first(spk_handle* h, int nrhs, double* dx, i64 ldx, int64_t* first_singular) {
+    static const int init[3] = {INT_MAX, 0, 0};
+    int rc = ensure_plan<T>(h);
+    if (rc) return rc;
+    CU(h, cudaMemcpyAsync(h->d_info, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
+    const int gi = graph_index<T>(h);
+    if ((rc = via_graph(h, h->g_factor_fs[gi][nrhs], [&] { return factor_launches<T>(h, nrhs); }))) return rc;
+    int info[3] = {INT_MAX, 0, 0};
+    CU(h, cudaMemcpyAsync(info, h->d_info, sizeof(info), cudaMemcpyDeviceToHost, h->stream));
+    CU(h, cudaStreamSynchronize(h->stream));
+    Storage<T>& St = storage<T>(h);
+    St.loaded = false;
+    if (info[1] || info[2]) {
+        St.factored = false;
+        return set_err(h, SPK_ETIMEOUT, info[2] ? "spk_factor_refine: a leaf-queue dependency wait timed out"
+                                                : "spk_factor_refine: a tensor-core wait timed out");
+    }
+    St.factored = true;
+    if (info[0] != INT_MAX) {
+        if (first_singular) *first_singular = info[0];
+        char buf[128];
+        std::snprintf(buf, sizeof buf, "zero pivot in the diagonal block of supernode %d", info[0]);
+        return set_err(h, SPK_ESINGULAR, buf);
+    }
+    const size_t split = fused_split<T>(h);
+    const Plan& PL = h->plan[plan_index<T>(h)];
+    rc = via_graph(h, h->g_fs_tail[gi][nrhs], [&] {
+        if (split == 0) {   // nothing of this solve ran beside the factorisation
+            const ll tot = (ll)h->n * nrhs;
+            LaunchScope ls(h, SPK_K_PERMUTE, 0.0, (double)tot * (8 + 4 + sizeof(T)));
+            spk::k_permute<double, T><<<(int)((tot + 255) / 256), 256, 0, h->stream>>>(
+                h->d_rhs, h->n, (T*)h->d_wb, (int)h->n, h->d_rperm, (int)h->n, nrhs);
+        }
+        int r = solve_fwd_levels<T>(h, nrhs, split, PL.levels.size(), h->stream);
+        return r ? r : solve_bwd_levels<T>(h, nrhs, h->stream);
+    });
+    if (rc) return rc;
+    const ll tot = (ll)h->n * nrhs;
+    LaunchScope ls(h, SPK_K_PERMUTE, 0.0, (double)tot * (8 + 4 + sizeof(T)));
+    spk::k_unpermute<T><<<(int)((tot + 255) / 256), 256, 0, h->stream>>>((const T*)h->d_wx, (int)h->n, dx, ldx,
+                                                                        h->d_rinvp, (int)h->n, nrhs, 0);
+    CU(h, cudaGetLastError());
+    return SPK_OK;
+}
+
+extern "C" {
+
+int spk_factor_refine(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where, int precision,
+                      double tol, int max_iter, int solver, int* iters, double* relres, int* solver_used,
+                      int64_t* first_singular) {
+    int rc = check_h(h);
+    if (rc) return rc;
+    if (first_singular) *first_singular = 0;
+    if (!valid_precision(precision) || nrhs <= 0 || !b || !x || ld < h->n || max_iter < 0 ||
+        (where != SPK_HOST && where != SPK_DEVICE) || solver < SPK_SOLVER_AUTO || solver > SPK_SOLVER_GMRES)
+        return set_err(h, SPK_EARG, "spk_factor_refine: bad arguments");
+    if (!h->have_values) return set_err(h, SPK_ESEQ, "Sequence error. Matrix input not done yet.");
+    if (nrhs > spk::MAXRHS) {   // beyond one solve pass: factor, then refine
+        if ((rc = spk_factor(h, precision, first_singular))) return rc;
+        return refine_impl(h, b, x, nrhs, ld, where, precision, tol, max_iter, solver, iters, relres, solver_used,
+                           false);
+    }
+    select_form(h, precision);
+    const bool f64 = is_fp64(precision);
+    if (f64 ? !storage<double>(h).loaded : !float_storage(h, precision).loaded)
+        if ((rc = f64 ? load_into<double>(h) : load_into<float>(h))) return rc;
+    if ((rc = ensure_rhs(h, nrhs))) return rc;
+    const i64 n = h->n;
+    CU(h, cudaMemcpy2DAsync(h->d_rhs, sizeof(double) * n, b, sizeof(double) * ld, sizeof(double) * n, nrhs,
+                            where == SPK_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, h->stream));
+    double* dx = where == SPK_HOST ? h->d_x : x;
+    const i64 ldx = where == SPK_HOST ? n : ld;
+    rc = f64 ? factor_refine_first<double>(h, (int)nrhs, dx, ldx, first_singular)
+             : factor_refine_first<float>(h, (int)nrhs, dx, ldx, first_singular);
+    if (rc) return rc;
+    return refine_impl(h, b, x, nrhs, ld, where, precision, tol, max_iter, solver, iters, relres, solver_used, false,
+                       true);
 }
 
 int spk_refine_transpose(spk_handle* h, const double* b, double* x, int64_t nrhs, int64_t ld, int where, int precision,
@@ -2469,7 +2631,7 @@ void spk_destroy(spk_handle* h) {
     }
     collect_events(h);
     for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
-    for (GraphRec& g : h->g_factor) drop_graph(g);
+    drop_factor_graphs(h);
     drop_solve_graphs(h);
     if (h->side) cudaStreamSynchronize(h->side);
     if (h->side2) cudaStreamSynchronize(h->side2);

@@ -52,6 +52,9 @@ GPU_SYMBOLS = {
     "spk_refine_ex": (ctypes.c_int, [VP, VP, VP, i64, i64, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                      ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), PD,
                                      ctypes.POINTER(ctypes.c_int)]),
+    "spk_factor_refine": (ctypes.c_int, [VP, VP, VP, i64, i64, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                         ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), PD,
+                                         ctypes.POINTER(ctypes.c_int), P64]),
     "spk_residual": (ctypes.c_int, [VP, VP, VP, i64, i64, ctypes.c_int, PD]),
     "spk_residual_noalloc": (ctypes.c_int, [VP, VP, VP, i64, i64, PD]),
     "spk_get_factors": (ctypes.c_int, [VP, ctypes.c_int, PD, PD, P64]),

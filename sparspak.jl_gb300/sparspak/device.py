@@ -176,6 +176,30 @@ class NumericEngine:
             return it.value, rr.value
         return it.value, rr.value, {N.SPK_SOLVER_IR: "ir", N.SPK_SOLVER_GMRES: "gmres"}.get(used.value, "ir")
 
+    def factor_refine(self, b, x, precision="fp32", tol=1e-12, max_iter=20, raise_on_fail=True, solver=None):
+        """Factor (values as loaded) and refine x for A x = b in one call, the
+        first solve's lower levels overlapped with the factorisation.  Returns
+        as refine."""
+        n, nrhs, ld = _shape(b)
+        pb, wb = _ptr(b)
+        px, wx = _ptr(x)
+        if wb != wx:
+            raise ValueError("b and x must both live on the host or both on the device")
+        it = ctypes.c_int(0)
+        rr = ctypes.c_double(0.0)
+        used = ctypes.c_int(0)
+        first = ctypes.c_int64(0)
+        rc = self._lib.spk_factor_refine(self._h, pb, px, nrhs, ld, wb, _prec(precision), float(tol), int(max_iter),
+                                         N.SOLVERS[solver or "auto"], ctypes.byref(it), ctypes.byref(rr),
+                                         ctypes.byref(used), ctypes.byref(first))
+        if rc == N.SPK_ESINGULAR:
+            raise SingularException(self._lib.spk_last_error(self._h).decode(), int(first.value))
+        if not (rc == N.SPK_ENOCONV and not raise_on_fail):
+            self._check(rc, "spk_factor_refine")
+        if solver is None:
+            return it.value, rr.value
+        return it.value, rr.value, {N.SPK_SOLVER_IR: "ir", N.SPK_SOLVER_GMRES: "gmres"}.get(used.value, "ir")
+
     def grad_pattern(self, lam, x):
         """dA on A's pattern (CSC order) = -sum_r lam_r x_r^T: numpy in, numpy out (or torch CUDA in and out)."""
         n, nrhs, ld = _shape(lam)
