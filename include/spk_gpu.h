@@ -229,7 +229,9 @@ int spk_residual(spk_handle* h, const double* b, const double* x, int64_t nrhs, 
  * (two doubles per right-hand side) is a file-scope device array of the
  * library, held by every device that loads it until the process exits.
  * At most SPK_NOALLOC_MAX_RHS right-hand sides per call (SPK_EARG beyond).
- * Like spk_residual it waits for the handle's stream before it returns.
+ * Like spk_residual it waits for the handle's stream before it returns, so
+ * it cannot be part of a stream capture: called while the handle's stream
+ * is capturing it returns SPK_ESEQ and leaves the capture untouched.
  * The first call on a device looks up that array's device address (with the
  * device current) and keeps it for the life of the process, so make the
  * first call before any stream capture, and do not use it across a

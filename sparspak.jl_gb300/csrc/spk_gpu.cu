@@ -2241,6 +2241,13 @@ int spk_residual_noalloc(spk_handle* h, const double* b, const double* x, int64_
     if (nrhs > SPK_NOALLOC_MAX_RHS)
         return set_err(h, SPK_EARG, "spk_residual_noalloc: at most SPK_NOALLOC_MAX_RHS (64) right-hand sides per call");
     if (!h->have_values) return set_err(h, SPK_ESEQ, "Sequence error. Matrix input not done yet.");
+    {   // the call ends with a wait for the stream, which a capture does not allow: refuse before any work
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        CU(h, cudaStreamIsCapturing(h->stream, &cs));
+        if (cs != cudaStreamCaptureStatusNone)
+            return set_err(h, SPK_ESEQ, "spk_residual_noalloc: the handle's stream is being captured (the call waits "
+                                        "for the stream); call it outside the capture");
+    }
     double* sums = nullptr;
     if ((rc = noalloc_scratch(h, &sums))) return rc;
     const int n = (int)h->n;
