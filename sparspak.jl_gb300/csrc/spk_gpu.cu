@@ -93,6 +93,7 @@ struct Plan {
     std::vector<int> blk_front;
     std::vector<int> inv_ids;             // k_block_inv entries grouped by level group, then line width (32, 64, 128)
     int inv_off[2][4] = {};               // group g, class c: inv_ids[inv_off[g][c] .. inv_off[g][c+1])
+    int inv_sub[2][spk::LF_CLASSES + 1] = {};   // class 0 split by width class (k_block_inv_small<W>)
     int inv_split = 0;                    // group 0: blocks of fronts below this level (final before it starts)
     ll inv2_size = 0;
     std::vector<int> block0, nblocks;     // per front
@@ -168,6 +169,7 @@ struct spk_handle {
     std::vector<int> rperm0, rinvp0;
     ll* d_slot = nullptr;
     double* d_aval = nullptr;
+    double* d_acsr = nullptr;   // A's values in CSR order (the residuals)
     int *d_rowptr = nullptr, *d_col = nullptr;
     ll* d_src = nullptr;
     int *d_ccolptr = nullptr, *d_crow = nullptr, *d_ccol = nullptr;   // A's pattern in CSC order (0-based)
@@ -657,12 +659,23 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc, bool sym
         for (int g = 0; g < 2; ++g) {
             for (int c = 0; c < 3; ++c) {
                 P.inv_off[g][c] = (int)P.inv_ids.size();
+                if (c == 0)
+                    for (int wc = 0; wc < spk::LF_CLASSES; ++wc) {
+                        P.inv_sub[g][wc] = (int)P.inv_ids.size();
+                        for (int b = 0; b < (int)P.blk_c0.size(); ++b) {
+                            const int bw = P.blk_c1[b] - P.blk_c0[b];
+                            if (bw > 32 || spk::leaf_class(bw) != wc) continue;
+                            if ((h->fronts[P.blk_front[b]].level < P.inv_split) != (g == 0)) continue;
+                            P.inv_ids.push_back(b);
+                        }
+                    }
+                if (c == 0) P.inv_sub[g][spk::LF_CLASSES] = (int)P.inv_ids.size();
                 for (int b = 0; b < (int)P.blk_c0.size(); ++b) {
                     const int bw = P.blk_c1[b] - P.blk_c0[b];
                     if (!(bw <= lim[c] && (c == 0 || bw > lim[c - 1]))) continue;
                     if ((h->fronts[P.blk_front[b]].level < P.inv_split) != (g == 0)) continue;
                     if (c == 0) {
-                        P.inv_ids.push_back(b);
+                        continue;   // below, by width class
                     } else {
                         for (int kind = 0; kind < 2; ++kind)
                             for (int tile = 0; tile < spk::cdiv(bw, 64); ++tile)
@@ -1177,10 +1190,20 @@ static int factor_launches(spk_handle* h, int fs_nrhs = 0) {
             LaunchScope ls(h, SPK_K_BLOCKINV, 0.0, 0.0);
             const int* ent = PL.d_inv_ids + PL.inv_off[g][c];
             T* inv2 = storage<T>(h).inv2;
-            if (c == 0)
-                spk::k_block_inv<T, 32><<<cnt, 256, sweep_smem<T, 32>(2), st>>>(fac, h->d_ipiv, inv2, S,
-                                                                                  PL.d_blk_front, ent);
-            else if (c == 1)
+            if (c == 0) {   // a warp per block, by width class
+                for (int wc = 0; wc < spk::LF_CLASSES; ++wc) {
+                    const int n = PL.inv_sub[g][wc + 1] - PL.inv_sub[g][wc];
+                    if (n <= 0) continue;
+                    const int* e = PL.d_inv_ids + PL.inv_sub[g][wc];
+                    const int grid = spk::cdiv(n, spk::BI_WARPS), blk = 32 * spk::BI_WARPS;
+                    switch (wc) {
+                    case 0: spk::k_block_inv_small<T, 4><<<grid, blk, 0, st>>>(fac, h->d_ipiv, inv2, S, PL.d_blk_front, e, n); break;
+                    case 1: spk::k_block_inv_small<T, 8><<<grid, blk, 0, st>>>(fac, h->d_ipiv, inv2, S, PL.d_blk_front, e, n); break;
+                    case 2: spk::k_block_inv_small<T, 16><<<grid, blk, 0, st>>>(fac, h->d_ipiv, inv2, S, PL.d_blk_front, e, n); break;
+                    default: spk::k_block_inv_small<T, 32><<<grid, blk, 0, st>>>(fac, h->d_ipiv, inv2, S, PL.d_blk_front, e, n); break;
+                    }
+                }
+            } else if (c == 1)
                 spk::k_block_inv<T, 64><<<cnt, 256, sweep_smem<T, 64>(1), st>>>(fac, h->d_ipiv, inv2, S,
                                                                                   PL.d_blk_front, ent);
             else
@@ -1530,7 +1553,7 @@ static int residual_device(spk_handle* h, const double* b, i64 ldb, const double
             spk::k_residual<<<grid, 256, 0, h->stream>>>(h->d_aval, h->d_ccolptr, h->d_crow, nullptr, x, ldx, b, ldb,
                                                          h->d_r, n, (int)nrhs, h->d_sums);
         else
-            spk::k_residual<<<grid, 256, 0, h->stream>>>(h->d_aval, h->d_rowptr, h->d_col, h->d_src, x, ldx, b, ldb,
+            spk::k_residual<<<grid, 256, 0, h->stream>>>(h->d_acsr, h->d_rowptr, h->d_col, nullptr, x, ldx, b, ldb,
                                                          h->d_r, n, (int)nrhs, h->d_sums);
     }
     CU(h, cudaGetLastError());
@@ -1614,7 +1637,7 @@ static int gmres_ir(spk_handle* h, const double* b, i64 ldb, double* x, i64 ldx,
             ++*used;
             {
                 LaunchScope ls(h, SPK_K_RESIDUAL, 2.0 * h->nnz * nrhs, (double)h->nnz * (8 + 4 + 8) + 8.0 * h->nnz * nrhs);
-                spk::k_gm_spmv<<<(n + 255) / 256, 256, 0, h->stream>>>(h->d_aval, h->d_rowptr, h->d_col, h->d_src, Zj,
+                spk::k_gm_spmv<<<(n + 255) / 256, 256, 0, h->stream>>>(h->d_acsr, h->d_rowptr, h->d_col, nullptr, Zj,
                                                                        h->gm_w, n, nrhs);
             }
             CU(h, cudaMemsetAsync(c, 0, sizeof(double) * (2 * (GM_M + 1) + 1) * nrhs, h->stream));
@@ -1893,9 +1916,10 @@ int spk_set_pattern(spk_handle* h, int64_t ncols, const int64_t* colptr, const i
     if ((rc = upload(h, &h->d_ccolptr, ccolptr))) return rc;
     if ((rc = upload(h, &h->d_crow, crow))) return rc;
     if ((rc = upload(h, &h->d_ccol, ccol))) return rc;
-    cudaFree(h->d_slot); cudaFree(h->d_aval); cudaFree(h->d_rowptr); cudaFree(h->d_col); cudaFree(h->d_src);
+    cudaFree(h->d_slot); cudaFree(h->d_aval); cudaFree(h->d_acsr); cudaFree(h->d_rowptr); cudaFree(h->d_col);
+    cudaFree(h->d_src);
     cudaFree(h->d_rperm); cudaFree(h->d_rinvp);
-    h->d_slot = nullptr; h->d_aval = nullptr; h->d_rowptr = h->d_col = nullptr; h->d_src = nullptr;
+    h->d_slot = nullptr; h->d_aval = nullptr; h->d_acsr = nullptr; h->d_rowptr = h->d_col = nullptr; h->d_src = nullptr;
     h->d_rperm = h->d_rinvp = nullptr;
     if ((rc = upload(h, &h->d_slot, slot))) return rc;
     if ((rc = upload(h, &h->d_rowptr, rowptr))) return rc;
@@ -1904,6 +1928,7 @@ int spk_set_pattern(spk_handle* h, int64_t ncols, const int64_t* colptr, const i
     if ((rc = upload(h, &h->d_rperm, h->rperm0))) return rc;
     if ((rc = upload(h, &h->d_rinvp, h->rinvp0))) return rc;
     CU(h, cudaMalloc((void**)&h->d_aval, sizeof(double) * std::max<i64>(nnz, 1)));
+    CU(h, cudaMalloc((void**)&h->d_acsr, sizeof(double) * std::max<i64>(nnz, 1)));
     h->nnz = nnz;
     h->have_pattern = true;
     h->have_values = false;
@@ -1922,9 +1947,13 @@ int spk_load_values(spk_handle* h, const double* nzval, int where, int precision
     if (!h->have_pattern) return set_err(h, SPK_ESEQ, "Sequence error. Pattern not set yet.");
     if ((!nzval && h->nnz > 0) || (where != SPK_HOST && where != SPK_DEVICE) || !valid_precision(precision))
         return set_err(h, SPK_EARG, "spk_load_values: bad arguments");
-    if (h->nnz > 0)
+    if (h->nnz > 0) {
         CU(h, cudaMemcpyAsync(h->d_aval, nzval, sizeof(double) * (size_t)h->nnz,
                               where == SPK_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, h->stream));
+        LaunchScope ls(h, SPK_K_ASSEMBLE, 0.0, (double)h->nnz * (8 + 8 + 8));
+        spk::k_gather_csr<<<(int)std::min<i64>((h->nnz + 255) / 256, 152 * 16), 256, 0, h->stream>>>(
+            h->d_aval, h->d_src, h->d_acsr, h->nnz);
+    }
     h->have_values = true;
     // a new A invalidates every factor
     for (int y = 0; y < 2; ++y) {
@@ -2253,7 +2282,7 @@ int spk_residual_noalloc(spk_handle* h, const double* b, const double* x, int64_
     const int n = (int)h->n;
     CU(h, cudaMemsetAsync(sums, 0, sizeof(double) * 2 * (size_t)nrhs, h->stream));
     dim3 grid((n + 255) / 256);
-    spk::k_residual_norms<<<grid, 256, 0, h->stream>>>(h->d_aval, h->d_rowptr, h->d_col, h->d_src, x, ld, b, ld, n,
+    spk::k_residual_norms<<<grid, 256, 0, h->stream>>>(h->d_acsr, h->d_rowptr, h->d_col, nullptr, x, ld, b, ld, n,
                                                        (int)nrhs, sums);
     CU(h, cudaGetLastError());
     double host[2 * SPK_NOALLOC_MAX_RHS];
@@ -2625,7 +2654,7 @@ void spk_destroy(spk_handle* h) {
     if (h->own) cudaStreamSynchronize(h->own);
     for (Plan& P : h->plan) free_plan(P);
     void* ptrs[] = {h->d_xs, h->d_rows, h->d_runid, h->d_run_tgt, h->d_run_start, h->d_run_rel,
-                    h->d_rel, h->d_ipiv, h->d_bmap, h->d_info, h->d_slot, h->d_aval,
+                    h->d_rel, h->d_ipiv, h->d_bmap, h->d_info, h->d_slot, h->d_aval, h->d_acsr,
                     h->d_rowptr, h->d_col, h->d_src, h->d_ccolptr, h->d_crow, h->d_ccol, h->d_rperm, h->d_rinvp, h->d_wb,
                     h->d_wy, h->d_wx, h->d_rhs, h->d_x, h->d_r, h->d_sums, h->gm_V, h->gm_Z, h->gm_w, h->gm_c};
     for (void* p : ptrs)

@@ -1622,6 +1622,91 @@ __global__ void __launch_bounds__(256) k_block_inv(const T* fac, const int* ipiv
     }
 }
 
+// The same operators for blocks of at most W <= 32 columns, a warp per
+// block, four per CTA (launches by width class W = 4, 8, 16, 32): the block
+// in shared memory, lane j forms column j of Minv (P e_j through the
+// forward steps of the pieces, the multipliers of row i left of its piece
+// taken from its source row, as stage_lower stages them), lane i row i of
+// Uinv (e_i through the backward steps, scaled by 1 / U(j, j)).  The
+// operations of k_block_inv<T, 32>, in the same order, without a CTA per
+// block for blocks of a few columns.
+constexpr int BI_WARPS = 4;
+template <typename T, int W>
+__global__ void __launch_bounds__(32 * BI_WARPS) k_block_inv_small(const T* fac, const int* ipiv, T* inv2, Sched S,
+                                                                    const int* blk_front, const int* entries,
+                                                                    int count) {
+    constexpr int LD = W + 1;
+    __shared__ T sD[BI_WARPS][W * LD];   // D(r, c) at [c * LD + r]
+    __shared__ T srd[BI_WARPS][W];
+    __shared__ int sq[BI_WARPS][W + 1], sgm[BI_WARPS][W], spa[BI_WARPS][W];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int idx = blockIdx.x * BI_WARPS + warp;
+    if (idx >= count) return;   // whole warp; no CTA barrier below
+    const int blk = entries[idx];
+    const DFront F = S.fronts[blk_front[blk]];
+    const int c0 = S.blk_c0[blk], bw = S.blk_c1[blk] - c0;
+    const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
+    const T* blkp = fac + F.loff + (ll)c0 * F.ld + c0;
+    T* D = sD[warp];
+    T* rd = srd[warp];
+    int* q0 = sq[warp];
+    int* gm = sgm[warp];
+    int* pa = spa[warp];
+    for (int k = lane; k <= np; k += 32) q0[k] = S.xsuper[p0 + k] - F.f - c0;
+    for (int j = 0; j < bw; ++j)
+        if (lane < bw) D[j * LD + lane] = blkp[(ll)j * F.ld + lane];
+    if (lane < bw) rd[lane] = T(1) / blkp[(ll)lane * F.ld + lane];
+    __syncwarp();
+    const int* ipb = ipiv + F.f + c0;
+    for (int pc = lane; pc < np; pc += 32) {   // block_gather_map, a lane per piece
+        const int a = q0[pc], b = q0[pc + 1];
+        for (int i = a; i < b; ++i) {
+            gm[i] = i;
+            pa[i] = a;
+        }
+        for (int k = a; k < b; ++k) {
+            const int kp = a + ipb[k];
+            const int t = gm[k];
+            gm[k] = gm[kp];
+            gm[kp] = t;
+        }
+    }
+    __syncwarp();
+    T* out = inv2 + S.blk_inv2[blk];
+    {   // Minv(:, lane)
+        T y[W];
+#pragma unroll
+        for (int i = 0; i < W; ++i) y[i] = (lane < bw && i < bw && gm[i] == lane) ? T(1) : T(0);
+#pragma unroll
+        for (int i = 1; i < W; ++i)
+            if (i < bw) {
+                const int gi = gm[i], ai = pa[i];
+#pragma unroll
+                for (int k = 0; k < i; ++k) y[i] -= D[k * LD + (k < ai ? gi : i)] * y[k];
+            }
+        if (lane < bw)
+#pragma unroll
+            for (int i = 0; i < W; ++i)
+                if (i < bw) out[(ll)lane * bw + i] = y[i];
+    }
+    {   // Uinv(lane, :)
+        T x[W];
+#pragma unroll
+        for (int j = 0; j < W; ++j) x[j] = (j == lane && lane < bw) ? T(1) : T(0);
+#pragma unroll
+        for (int j = 0; j < W; ++j)
+            if (j < bw) {
+#pragma unroll
+                for (int k = 0; k < j; ++k) x[j] -= x[k] * D[j * LD + k];
+                x[j] *= rd[j];
+            }
+        if (lane < bw)
+#pragma unroll
+            for (int j = 0; j < W; ++j)
+                if (j < bw) out[(ll)bw * bw + (ll)j * bw + lane] = x[j];
+    }
+}
+
 // ---------------------------------------------------------------------------
 // 64 x 64 register-tiled block product, 256 threads, 4 x 4 outputs each.
 // sA[k][i] (k < kc, i < 64), sB[k][j]; thread (tx, ty) owns rows tx+16a and
@@ -3244,6 +3329,14 @@ __global__ void k_grad_pattern(const int* __restrict__ row, const int* __restric
 // ---------------------------------------------------------------------------
 
 // Zero-initialised factor storage += A's values at their slots (_inmatrix!).
+// A's values in CSR order (aval in CSC order, src the CSC index of each CSR
+// position), so that the residuals read each row's values contiguously.
+__global__ void __launch_bounds__(256) k_gather_csr(const double* __restrict__ aval, const ll* __restrict__ src,
+                                                    double* __restrict__ acsr, ll nnz) {
+    for (ll k = blockIdx.x * (ll)blockDim.x + threadIdx.x; k < nnz; k += (ll)gridDim.x * blockDim.x)
+        acsr[k] = aval[src[k]];
+}
+
 template <typename T>
 __global__ void k_scatter_values(const double* __restrict__ aval, const ll* __restrict__ slot, T* fac, ll nnz) {
     ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x;
@@ -3347,7 +3440,8 @@ __global__ void __launch_bounds__(256) k_residual(const double* __restrict__ ava
 // at V + j * n * nrhs.  Every right-hand side has its own Krylov space.
 // ---------------------------------------------------------------------------
 
-// w = A z (FP64, rows of A gathered from CSC order through src).
+// w = A z (FP64, rows of A; values in CSR order, or gathered from CSC order
+// through src).
 __global__ void __launch_bounds__(256) k_gm_spmv(const double* __restrict__ aval, const int* __restrict__ rowptr,
                                                  const int* __restrict__ col, const ll* __restrict__ src,
                                                  const double* __restrict__ z, double* __restrict__ w, int n, int nrhs) {
@@ -3355,7 +3449,7 @@ __global__ void __launch_bounds__(256) k_gm_spmv(const double* __restrict__ aval
         for (int r0 = 0; r0 < nrhs; r0 += RES_RG) {
             double acc[RES_RG] = {0.0, 0.0, 0.0, 0.0};
             for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
-                const double a = aval[src[k]];
+                const double a = aval[src ? src[k] : k];
                 const int c = col[k];
 #pragma unroll
                 for (int q = 0; q < RES_RG; ++q)
