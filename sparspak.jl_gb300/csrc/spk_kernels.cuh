@@ -2970,6 +2970,42 @@ __global__ void __cluster_dims__(NC, 1, 1) __launch_bounds__(FC_THREADS, 1)
 // end; wider fronts keep a lane per column and shuffle x.  Same operations as
 // k_fwd / k_bwd_u12 / k_bwd.
 constexpr int LEAF_M = 128;
+
+// Warp reduce-scatter: N (16 or 32) values per lane, summed over the 32
+// lanes; each step keeps the half of the values picked by a lane bit and
+// adds the partner's copy of it (N/2 + N/4 + ... shuffles instead of
+// 5 N).  Lane l ends with the sum of value l * N / 32 (for N = 16 lanes l
+// and l ^ 1 hold the same one).
+template <int N, int OFF, typename T>
+__device__ __forceinline__ void rs_halve(T* v, int lane) {
+    const bool hi = (lane & OFF) != 0;
+#pragma unroll
+    for (int i = 0; i < N / 2; ++i) {
+        const T keep = hi ? v[i + N / 2] : v[i];
+        const T send = hi ? v[i] : v[i + N / 2];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, OFF);
+    }
+}
+template <int N, typename T>
+__device__ __forceinline__ T warp_reduce_scatter(T (&v)[N]) {
+    static_assert(N == 16 || N == 32, "16 or 32 values");
+    const int lane = threadIdx.x & 31;
+    if constexpr (N == 32) {
+        rs_halve<32, 16>(v, lane);
+        rs_halve<16, 8>(v, lane);
+        rs_halve<8, 4>(v, lane);
+        rs_halve<4, 2>(v, lane);
+        rs_halve<2, 1>(v, lane);
+    } else {
+        rs_halve<16, 16>(v, lane);
+        rs_halve<8, 8>(v, lane);
+        rs_halve<4, 4>(v, lane);
+        rs_halve<2, 2>(v, lane);
+        v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+    }
+    return v[0];
+}
+
 template <typename T, bool FWD, int W>
 __global__ void __launch_bounds__(256) k_solve_leaf(const T* fac, const T* inv2, T* in, T* out, const T* xs, int n,
                                                      int nrhs, Sched S, Launch L) {
@@ -3012,15 +3048,18 @@ __global__ void __launch_bounds__(256) k_solve_leaf(const T* fac, const T* inv2,
 #pragma unroll
                         for (int r = 0; r < RG; ++r) pw[j][r] += uv[j] * xv[r];
                 }
+                constexpr int NV = W * RG;   // 16 or 32: value j * RG + r
+                T flat[NV];
 #pragma unroll
                 for (int j = 0; j < W; ++j)
 #pragma unroll
-                    for (int r = 0; r < RG; ++r) {
-                        T t = pw[j][r];
+                    for (int r = 0; r < RG; ++r) flat[j * RG + r] = pw[j][r];
+                const T t = warp_reduce_scatter<NV>(flat);   // lane l: value l * NV / 32
 #pragma unroll
-                        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(FULL, t, o);
-                        if (lane == j) acc[r] = t;
-                    }
+                for (int r = 0; r < RG; ++r) {
+                    const T vr = __shfl_sync(FULL, t, ((lane * RG + r) * 32 / NV) & 31);
+                    if (lane < bw) acc[r] = vr;
+                }
             } else {
                 const T* u = fac + F.uoff + (ll)lane * F.m;
                 for (int i0 = 0; i0 < F.m; i0 += 32) {
