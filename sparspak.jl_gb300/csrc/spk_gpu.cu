@@ -650,8 +650,9 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc, bool sym
         }
     }
     {
-        // k_block_inv work: blocks up to 32 wide, one entry per block; wider
-        // ones by line width 64 / 128, entries blk * 4 + kind * 2 + tile.
+        // Solve-operator work: blocks up to 32 wide, one entry per block
+        // (k_block_inv_small, by width class); wider ones by line width
+        // 64 / 128 (k_block_inv), entries blk * 4 + kind * 2 + tile.
         // Group 0 (fronts below the last two levels) can run beside the top
         // of the factorisation, group 1 after it.
         const int lim[3] = {32, 64, 128};

@@ -1557,11 +1557,11 @@ __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, co
 // written column-major (bw x bw, Minv then Uinv) at inv2[blk_inv2[blk]], so
 // that a triangular-solve step of a block is one product.  They are the
 // panel sweeps applied to the identity: column j of Minv is the U-panel
-// sweep of e_j, row i of Uinv the L-panel sweep of e_i.  `entries` lists
-// the work: for W == 32 one CTA per block (lines 0..31 Minv columns, 32..63
-// Uinv rows); otherwise entry = blk * 4 + kind * 2 + tile (kind 0 Minv,
-// 1 Uinv; 64 lines per tile).  Dynamic shared memory: 2 * W * SLD(W) T's
-// for W == 32, else W * SLD(W).
+// sweep of e_j, row i of Uinv the L-panel sweep of e_i.  This kernel takes
+// the blocks of more than 32 columns (W = 64, 128); `entries` lists the
+// work, entry = blk * 4 + kind * 2 + tile (kind 0 Minv, 1 Uinv; 64 lines per
+// tile).  Dynamic shared memory: W * SLD(W) T's.  Narrower blocks:
+// k_block_inv_small.
 template <typename T, int W>
 __global__ void __launch_bounds__(256) k_block_inv(const T* fac, const int* ipiv, T* inv2, Sched S,
                                                     const int* blk_front, const int* entries) {
@@ -1569,16 +1569,15 @@ __global__ void __launch_bounds__(256) k_block_inv(const T* fac, const int* ipiv
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ T rd[W];
     __shared__ int q0[W + 1], gmap[W], pa[W];
+    static_assert(W > 32, "blocks of at most 32 columns: k_block_inv_small");
     const int e = entries[blockIdx.x];
-    const int blk = (W == 32) ? e : (e >> 2);
-    const int kind = (W == 32) ? 2 : ((e >> 1) & 1);
-    const int l0 = (W == 32) ? 0 : (e & 1) * 64;
+    const int blk = e >> 2, kind = (e >> 1) & 1, l0 = (e & 1) * 64;
     const DFront F = S.fronts[blk_front[blk]];
     const int c0 = S.blk_c0[blk], c1 = S.blk_c1[blk], bw = c1 - c0;
     const int p0 = S.blk_p0[blk], np = S.blk_np[blk];
     const T* blkp = fac + F.loff + (ll)c0 * F.ld + c0;
     T* sL = reinterpret_cast<T*>(smem_raw);
-    T* sU = (W == 32) ? sL + W * SLD<T, W>::value : sL;
+    T* sU = sL;   // one kind per entry
     const int tid = threadIdx.x, line = tid >> 2, q = tid & 3;
     if (kind != 1) {
         for (int k = tid; k <= np; k += 256) q0[k] = S.xsuper[p0 + k] - F.f - c0;
@@ -1589,8 +1588,8 @@ __global__ void __launch_bounds__(256) k_block_inv(const T* fac, const int* ipiv
     }
     if (kind != 0) stage_upper<T, W>(sU, rd, blkp, F.ld, bw);
     __syncthreads();
-    const bool doM = (kind == 2) ? line < 32 : kind == 0;
-    const int idx = (kind == 2) ? (line & 31) : l0 + line;
+    const bool doM = kind == 0;
+    const int idx = l0 + line;
     if (__all_sync(0xffffffffu, idx >= bw)) return;   // the whole warp is past the block
     T v[CQ];
     T* out = inv2 + S.blk_inv2[blk];
@@ -1628,8 +1627,8 @@ __global__ void __launch_bounds__(256) k_block_inv(const T* fac, const int* ipiv
 // forward steps of the pieces, the multipliers of row i left of its piece
 // taken from its source row, as stage_lower stages them), lane i row i of
 // Uinv (e_i through the backward steps, scaled by 1 / U(j, j)).  The
-// operations of k_block_inv<T, 32>, in the same order, without a CTA per
-// block for blocks of a few columns.
+// operations of the sweeps k_block_inv applies, in the same order, without
+// a CTA per block for blocks of a few columns.
 constexpr int BI_WARPS = 4;
 template <typename T, int W>
 __global__ void __launch_bounds__(32 * BI_WARPS) k_block_inv_small(const T* fac, const int* ipiv, T* inv2, Sched S,
