@@ -1546,7 +1546,7 @@ static int residual_device(spk_handle* h, const double* b, i64 ldb, const double
                            double* relres, bool transpose = false, std::vector<double>* sq = nullptr) {
     const int n = (int)h->n;
     CU(h, cudaMemsetAsync(h->d_sums, 0, sizeof(double) * 2 * (size_t)nrhs, h->stream));
-    dim3 grid((n + 255) / 256);
+    dim3 grid(std::min((n + 255) / 256, 8 * h->nsm));   // grid-stride rows: few partial sums per norm
     {
         LaunchScope ls(h, SPK_K_RESIDUAL, 2.0 * h->nnz * nrhs, (double)h->nnz * (8 + 4 + 8) + 8.0 * h->nnz * nrhs +
                                                                   24.0 * n * nrhs);
@@ -2282,7 +2282,7 @@ int spk_residual_noalloc(spk_handle* h, const double* b, const double* x, int64_
     if ((rc = noalloc_scratch(h, &sums))) return rc;
     const int n = (int)h->n;
     CU(h, cudaMemsetAsync(sums, 0, sizeof(double) * 2 * (size_t)nrhs, h->stream));
-    dim3 grid((n + 255) / 256);
+    dim3 grid(std::min((n + 255) / 256, 8 * h->nsm));
     spk::k_residual_norms<<<grid, 256, 0, h->stream>>>(h->d_acsr, h->d_rowptr, h->d_col, nullptr, x, ld, b, ld, n,
                                                        (int)nrhs, sums);
     CU(h, cudaGetLastError());

@@ -3441,13 +3441,13 @@ __global__ void __launch_bounds__(256) k_residual(const double* __restrict__ ava
                                                   const double* __restrict__ x, ll ldx, const double* __restrict__ b,
                                                   ll ldb, double* __restrict__ r, int n, int nrhs,
                                                   double* __restrict__ sums) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     for (int r0 = 0; r0 < nrhs; r0 += RES_RG) {
         const int nr = min(RES_RG, nrhs - r0);
         double rr[RES_RG], bb[RES_RG];
 #pragma unroll
         for (int q = 0; q < RES_RG; ++q) rr[q] = bb[q] = 0.0;
-        if (i < n) {
+        // grid-stride over the rows: one partial sum per CTA and right-hand side
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
             double s[RES_RG];
 #pragma unroll
             for (int q = 0; q < RES_RG; ++q) s[q] = 0.0;
@@ -3463,8 +3463,8 @@ __global__ void __launch_bounds__(256) k_residual(const double* __restrict__ ava
                 if (q < nr) {
                     const double bi = b[(ll)(r0 + q) * ldb + i], ri = bi - s[q];
                     r[(ll)(r0 + q) * n + i] = ri;
-                    rr[q] = ri * ri;
-                    bb[q] = bi * bi;
+                    rr[q] += ri * ri;
+                    bb[q] += bi * bi;
                 }
         }
         residual_sums(rr, bb, r0, nr, sums);
@@ -3561,13 +3561,12 @@ __global__ void __launch_bounds__(256) k_residual_norms(const double* __restrict
                                                         const double* __restrict__ x, ll ldx,
                                                         const double* __restrict__ b, ll ldb, int n, int nrhs,
                                                         double* __restrict__ sums) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     for (int r0 = 0; r0 < nrhs; r0 += RES_RG) {
         const int nr = min(RES_RG, nrhs - r0);
         double rr[RES_RG], bb[RES_RG];
 #pragma unroll
         for (int q = 0; q < RES_RG; ++q) rr[q] = bb[q] = 0.0;
-        if (i < n) {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
             double s[RES_RG];
 #pragma unroll
             for (int q = 0; q < RES_RG; ++q) s[q] = 0.0;
@@ -3582,8 +3581,8 @@ __global__ void __launch_bounds__(256) k_residual_norms(const double* __restrict
             for (int q = 0; q < RES_RG; ++q)
                 if (q < nr) {
                     const double bi = b[(ll)(r0 + q) * ldb + i], ri = bi - s[q];
-                    rr[q] = ri * ri;
-                    bb[q] = bi * bi;
+                    rr[q] += ri * ri;
+                    bb[q] += bi * bi;
                 }
         }
         residual_sums(rr, bb, r0, nr, sums);
