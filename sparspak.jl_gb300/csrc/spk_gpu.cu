@@ -1370,11 +1370,19 @@ template <typename T, bool FWD>
 static cudaError_t launch_solve_leaf(int c, int count, cudaStream_t st, const T* fac, const T* inv, T* in, T* out,
                                      const T* xs, int n, int nrhs, const spk::Sched& S, const spk::Launch& la) {
     const int grid = (count + 7) / 8;
+    if (nrhs == 1) {   // one right-hand side: passes of one
+        switch (c) {
+        case 0: return launch_chained(spk::k_solve_leaf<T, FWD, 4, 1>, grid, 256, 0, st, fac, inv, in, out, xs, n, nrhs, S, la);
+        case 1: return launch_chained(spk::k_solve_leaf<T, FWD, 8, 1>, grid, 256, 0, st, fac, inv, in, out, xs, n, nrhs, S, la);
+        case 2: return launch_chained(spk::k_solve_leaf<T, FWD, 16, 1>, grid, 256, 0, st, fac, inv, in, out, xs, n, nrhs, S, la);
+        default: return launch_chained(spk::k_solve_leaf<T, FWD, 32, 1>, grid, 256, 0, st, fac, inv, in, out, xs, n, nrhs, S, la);
+        }
+    }
     switch (c) {
-    case 0: return launch_chained(spk::k_solve_leaf<T, FWD, 4>, grid, 256, 0, st, fac, inv, in, out, xs, n, nrhs, S, la);
-    case 1: return launch_chained(spk::k_solve_leaf<T, FWD, 8>, grid, 256, 0, st, fac, inv, in, out, xs, n, nrhs, S, la);
-    case 2: return launch_chained(spk::k_solve_leaf<T, FWD, 16>, grid, 256, 0, st, fac, inv, in, out, xs, n, nrhs, S, la);
-    default: return launch_chained(spk::k_solve_leaf<T, FWD, 32>, grid, 256, 0, st, fac, inv, in, out, xs, n, nrhs, S, la);
+    case 0: return launch_chained(spk::k_solve_leaf<T, FWD, 4, 4>, grid, 256, 0, st, fac, inv, in, out, xs, n, nrhs, S, la);
+    case 1: return launch_chained(spk::k_solve_leaf<T, FWD, 8, 4>, grid, 256, 0, st, fac, inv, in, out, xs, n, nrhs, S, la);
+    case 2: return launch_chained(spk::k_solve_leaf<T, FWD, 16, 4>, grid, 256, 0, st, fac, inv, in, out, xs, n, nrhs, S, la);
+    default: return launch_chained(spk::k_solve_leaf<T, FWD, 32, 4>, grid, 256, 0, st, fac, inv, in, out, xs, n, nrhs, S, la);
     }
 }
 

@@ -2970,11 +2970,12 @@ __global__ void __cluster_dims__(NC, 1, 1) __launch_bounds__(FC_THREADS, 1)
 // k_fwd / k_bwd_u12 / k_bwd.
 constexpr int LEAF_M = 128;
 
-// Warp reduce-scatter: N (16 or 32) values per lane, summed over the 32
-// lanes; each step keeps the half of the values picked by a lane bit and
-// adds the partner's copy of it (N/2 + N/4 + ... shuffles instead of
-// 5 N).  Lane l ends with the sum of value l * N / 32 (for N = 16 lanes l
-// and l ^ 1 hold the same one).
+// Warp reduce-scatter: N (a power of 2, at most 32) values per lane, summed
+// over the 32 lanes; each step keeps the half of the values picked by a
+// lane bit and adds the partner's copy of it, and once one value is left
+// the remaining lane bits are summed by a butterfly (N/2 + N/4 + ... + the
+// rest shuffles instead of 5 N).  Lane l ends with the sum of value
+// l * N / 32.
 template <int N, int OFF, typename T>
 __device__ __forceinline__ void rs_halve(T* v, int lane) {
     const bool hi = (lane & OFF) != 0;
@@ -2985,30 +2986,29 @@ __device__ __forceinline__ void rs_halve(T* v, int lane) {
         v[i] = keep + __shfl_xor_sync(0xffffffffu, send, OFF);
     }
 }
+template <int N, int OFF, typename T>
+__device__ __forceinline__ void rs_rec(T* v, int lane) {
+    if constexpr (OFF > 0) {
+        if constexpr (N > 1) {
+            rs_halve<N, OFF>(v, lane);
+            rs_rec<N / 2, OFF / 2>(v, lane);
+        } else {
+            v[0] += __shfl_xor_sync(0xffffffffu, v[0], OFF);
+            rs_rec<1, OFF / 2>(v, lane);
+        }
+    }
+}
 template <int N, typename T>
 __device__ __forceinline__ T warp_reduce_scatter(T (&v)[N]) {
-    static_assert(N == 16 || N == 32, "16 or 32 values");
-    const int lane = threadIdx.x & 31;
-    if constexpr (N == 32) {
-        rs_halve<32, 16>(v, lane);
-        rs_halve<16, 8>(v, lane);
-        rs_halve<8, 4>(v, lane);
-        rs_halve<4, 2>(v, lane);
-        rs_halve<2, 1>(v, lane);
-    } else {
-        rs_halve<16, 16>(v, lane);
-        rs_halve<8, 8>(v, lane);
-        rs_halve<4, 4>(v, lane);
-        rs_halve<2, 2>(v, lane);
-        v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
-    }
+    static_assert(N >= 1 && N <= 32 && (N & (N - 1)) == 0, "a power of 2, at most 32 values");
+    rs_rec<N, 16>(v, threadIdx.x & 31);
     return v[0];
 }
 
-template <typename T, bool FWD, int W>
+template <typename T, bool FWD, int W, int RG>
 __global__ void __launch_bounds__(256) k_solve_leaf(const T* fac, const T* inv2, T* in, T* out, const T* xs, int n,
                                                      int nrhs, Sched S, Launch L) {
-    constexpr int RG = 4;   // right-hand sides per pass
+    // RG: right-hand sides per pass (1 for a single one, else 4)
     const unsigned FULL = 0xffffffffu;
     griddep_launch();
     const int lane = threadIdx.x & 31, idx = blockIdx.x * 8 + (threadIdx.x >> 5);
@@ -3047,7 +3047,7 @@ __global__ void __launch_bounds__(256) k_solve_leaf(const T* fac, const T* inv2,
 #pragma unroll
                         for (int r = 0; r < RG; ++r) pw[j][r] += uv[j] * xv[r];
                 }
-                constexpr int NV = W * RG;   // 16 or 32: value j * RG + r
+                constexpr int NV = W * RG;   // value j * RG + r
                 T flat[NV];
 #pragma unroll
                 for (int j = 0; j < W; ++j)
