@@ -3020,6 +3020,23 @@ __global__ void __launch_bounds__(256) k_solve_leaf(const T* fac, const T* inv2,
     griddep_wait();
     for (int r0 = 0; r0 < nrhs; r0 += RG) {
         const int nr = min(RG, nrhs - r0);
+        // narrow fronts: the loads that do not depend on the solve first (the
+        // operator column, forward this lane's L21 row among the first 32
+        // rows), so that a front waits for fewer round trips; wider ones
+        // keep them where they are used (registers)
+        constexpr bool EARLY = W <= 8;
+        T mv[W];   // op(lane, k), op(j, k) at Mi[k * bw + j]
+        auto load_mv = [&] {
+#pragma unroll
+            for (int k = 0; k < W; ++k)
+                mv[k] = (k < bw && lane < bw && (FWD || k >= lane)) ? Mi[(ll)k * bw + lane] : T(0);
+        };
+        if constexpr (EARLY) load_mv();
+        T lv0[FWD && EARLY ? W : 1];
+        if constexpr (FWD && EARLY) {
+#pragma unroll
+            for (int k = 0; k < W; ++k) lv0[k] = (k < bw && lane < F.m) ? fac[F.loff + (ll)k * F.ld + F.nf + lane] : T(0);
+        }
         T v[RG];
 #pragma unroll
         for (int r = 0; r < RG; ++r) v[r] = (lane < bw && r < nr) ? in[(ll)(r0 + r) * n + F.f + lane] : T(0);
@@ -3083,9 +3100,7 @@ __global__ void __launch_bounds__(256) k_solve_leaf(const T* fac, const T* inv2,
 #pragma unroll
             for (int r = 0; r < RG; ++r) v[r] -= acc[r];
         }
-        T mv[W];   // op(lane, k), op(j, k) at Mi[k * bw + j]
-#pragma unroll
-        for (int k = 0; k < W; ++k) mv[k] = (k < bw && lane < bw && (FWD || k >= lane)) ? Mi[(ll)k * bw + lane] : T(0);
+        if constexpr (!EARLY) load_mv();
         T y[RG];   // lane j: sum_k op(j, k) v_k
 #pragma unroll
         for (int r = 0; r < RG; ++r) y[r] = T(0);
@@ -3103,9 +3118,14 @@ __global__ void __launch_bounds__(256) k_solve_leaf(const T* fac, const T* inv2,
         if constexpr (FWD) {   // b[R_F] -= L21 y_F (L21 column k contiguous in Lf)
             for (int i0 = 0; i0 < F.m; i0 += 32) {
                 const int i = i0 + lane;
-                T lv[W];   // this lane's row of L21
+                T lv[W];   // this lane's row of L21 (the first chunk's came in early)
 #pragma unroll
-                for (int k = 0; k < W; ++k) lv[k] = (k < bw && i < F.m) ? fac[F.loff + (ll)k * F.ld + F.nf + i] : T(0);
+                for (int k = 0; k < W; ++k) {
+                    if constexpr (EARLY) {
+                        if (i0 == 0) { lv[k] = lv0[k]; continue; }
+                    }
+                    lv[k] = (k < bw && i < F.m) ? fac[F.loff + (ll)k * F.ld + F.nf + i] : T(0);
+                }
                 T acc[RG];
 #pragma unroll
                 for (int r = 0; r < RG; ++r) acc[r] = T(0);
