@@ -339,6 +339,14 @@ int spk_measure_peaks(double* fp32_tflops, double* fp64_tflops, double* dmma_tfl
  *                        default 4) are solved by one 16-CTA cluster each
  *                        (all block steps in one launch); smaller ones by a
  *                        launch per block step.  Keeps the factors.
+ *  SPK_OPT_PANEL_SPLIT   1 (default): in the float forms, a block step
+ *                        whose trailing update is all on the tensor cores
+ *                        launches its panel in two parts: the lines the next
+ *                        block's diagonal block is updated from (the first
+ *                        128 rows below the block and columns right of it)
+ *                        on the launch stream, the others beside them on the
+ *                        look-ahead stream; 0: one panel launch.  The same
+ *                        arithmetic either way.
  */
 #define SPK_OPT_LEAF_QUEUE 0
 #define SPK_OPT_WAIT_BUDGET 1
@@ -348,6 +356,7 @@ int spk_measure_peaks(double* fp32_tflops, double* fp64_tflops, double* dmma_tfl
 #define SPK_OPT_TC_WIDE 5
 #define SPK_OPT_LU_PIECES 6
 #define SPK_OPT_SOLVE_CLUSTER_MINB 7
+#define SPK_OPT_PANEL_SPLIT 8
 int spk_set_option(spk_handle* h, int option, int64_t value);
 int spk_get_option(spk_handle* h, int option, int64_t* value);
 

@@ -57,6 +57,9 @@ struct LevelPlan {
     // btrail_tc0: tile 0 of each packed front's trailing update (it holds the
     // next block's diagonal block); btrail_tc: its tiles 1..
     std::vector<LaunchRec> blu, bpanel, btrail, btrail_tc0, btrail_tc, fwd, bwd;
+    // bpanel split in two parts: the near tiles (the first 128 rows below the
+    // block and columns right of it, which tile 0 reads) and the far ones
+    std::vector<LaunchRec> bpanel_near, bpanel_far;
     std::vector<char> blu_pc;   // every piece of the step's blocks is at most 32 columns (k_block_lu_pc)
     // Solves: fronts with many blocks by one cluster launch each direction
     // (front_big, one tile per front), the others by block steps
@@ -213,6 +216,7 @@ struct spk_handle {
     int tc_wide = 1;                       // SPK_OPT_TC_WIDE: Schur tiles of 128 x 256
     int lu_pieces = 0;                     // SPK_OPT_LU_PIECES: block LU by pieces (slower on GB300, see header)
     int fc_minb = spk::FC_MINB;            // SPK_OPT_SOLVE_CLUSTER_MINB: blocks of a front for the cluster solve
+    int panel_split = 1;                   // SPK_OPT_PANEL_SPLIT: near / far panel tiles on two streams
     std::string err;
 
     // launch accounting and optional per-class event timing
@@ -720,6 +724,8 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc, bool sym
         L.blu.resize(maxb);
         L.blu_pc.assign(maxb, 1);
         L.bpanel.resize(maxb);
+        L.bpanel_near.resize(maxb);
+        L.bpanel_far.resize(maxb);
         L.btrail.resize(maxb);
         L.btrail_tc0.resize(maxb);
         L.btrail_tc.resize(maxb);
@@ -847,6 +853,26 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc, bool sym
                         if (h->xs[q + 1] - h->xs[q] > 32) L.blu_pc[t] = 0;
                 }
             add_launch(&P, L.bpanel[t], ids, tp, fp, wp);
+            {   // the near and far parts (spk::panel_tile): two line tiles each side
+                std::vector<int> tn(nid), tfar(nid);
+                std::vector<double> fn(nid), wn(nid), ffar(nid), wfar(nid);
+                for (size_t k = 0; k < nid; ++k) {
+                    tn[k] = tfar[k] = 0;
+                    fn[k] = wn[k] = ffar[k] = wfar[k] = 0.0;
+                    if (tp[k] <= 0) continue;
+                    const HFront& F = h->fronts[ids[k]];
+                    const int c1 = P.blk_c1[P.block0[ids[k]] + t], lpt = panel_lines(tc, wide[t]);
+                    tn[k] = std::min(2, cdiv(F.nf + F.m - c1, lpt)) + (sym ? 0 : std::min(2, cdiv(F.nf - c1, lpt)));
+                    tfar[k] = tp[k] - tn[k];
+                    const double a = (double)tn[k] / tp[k];
+                    fn[k] = fp[k] * a;
+                    wn[k] = wp[k] * a;
+                    ffar[k] = fp[k] - fn[k];
+                    wfar[k] = wp[k] - wn[k];
+                }
+                add_launch(&P, L.bpanel_near[t], ids, tn, fn, wn);
+                add_launch(&P, L.bpanel_far[t], ids, tfar, ffar, wfar);
+            }
             int bwl = 1;
             for (size_t k = 0; k < nid; ++k)
                 if (t < P.nblocks[ids[k]]) {
@@ -1270,18 +1296,35 @@ static int factor_launches(spk_handle* h, int fs_nrhs = 0) {
                 CU(h, cudaStreamWaitEvent(h->stream, h->evB, 0));
                 pending = false;
             }
-            if (P.bpanel[t].tiles > 0) {
-                LaunchScope ls(h, SPK_K_PANEL, P.bpanel[t].flops, P.bpanel[t].words * sizeof(T));
-                const spk::Launch la = launch_of(PL, P.bpanel[t]);
+            // Panel split (float forms looking ahead, a step whose trailing
+            // update is all on the tensor cores): the near tiles on the launch
+            // stream ahead of tile 0, the far ones on the side stream beside
+            // them, ahead of the rest of the trailing update.
+            bool split = false;
+            if constexpr (std::is_same<T, float>::value)
+                split = ahead && h->panel_split && P.btrail[t].tiles == 0 && P.btrail_tc[t].tiles > 0 &&
+                        P.bpanel_far[t].tiles > 0 && P.bpanel_near[t].tiles > 0;
+            auto panel = [&](const LaunchRec& rec, int part, cudaStream_t st) {
+                if (rec.tiles <= 0) return;
+                LaunchScope ls(h, SPK_K_PANEL, rec.flops, rec.words * sizeof(T));
+                const spk::Launch la = launch_of(PL, rec);
                 if (bw <= 32)
-                    spk::k_block_panel<T, 32><<<P.bpanel[t].tiles, 256, sweep_smem<T, 32>(1), h->stream>>>(
-                        fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack, bf16);
+                    spk::k_block_panel<T, 32><<<rec.tiles, 256, sweep_smem<T, 32>(1), st>>>(
+                        fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack, bf16, part);
                 else if (bw <= 64)
-                    spk::k_block_panel<T, 64><<<P.bpanel[t].tiles, 256, sweep_smem<T, 64>(1), h->stream>>>(
-                        fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack, bf16);
+                    spk::k_block_panel<T, 64><<<rec.tiles, 256, sweep_smem<T, 64>(1), st>>>(
+                        fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack, bf16, part);
                 else
-                    spk::k_block_panel<T, BM><<<P.bpanel[t].tiles, panel_threads<T, BM>(), panel_smem<T, BM>(), h->stream>>>(
-                        fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack, bf16);
+                    spk::k_block_panel<T, BM><<<rec.tiles, panel_threads<T, BM>(), panel_smem<T, BM>(), st>>>(
+                        fac, h->d_ipiv, h->d_bmap, S, la, (int)t, storage<T>(h).pack, bf16, part);
+            };
+            if (split) {   // the side stream: after this block LU (and the last trailing update)
+                CU(h, cudaEventRecord(h->evP, h->stream));
+                CU(h, cudaStreamWaitEvent(h->side, h->evP, 0));
+                panel(P.bpanel_near[t], 1, h->stream);
+                panel(P.bpanel_far[t], 2, h->side);
+            } else {
+                panel(P.bpanel[t], 0, h->stream);
             }
             if (P.btrail[t].tiles > 0) {
                 LaunchScope ls(h, SPK_K_TRAIL, P.btrail[t].flops, P.btrail[t].words * sizeof(T));
@@ -1300,7 +1343,7 @@ static int factor_launches(spk_handle* h, int fs_nrhs = 0) {
                         const int reserve = std::max(P.btrail_tc0[t].tiles,
                                                      t + 1 < P.blu.size() ? P.blu[t + 1].tiles : 0);
                         grid = std::max(std::min(nt, h->nsm - reserve), std::min(nt, h->nsm / 2));
-                        CU(h, cudaEventRecord(h->evP, h->stream));
+                        CU(h, cudaEventRecord(h->evP, h->stream));   // with a split: the near tiles done
                         CU(h, cudaStreamWaitEvent(h->side, h->evP, 0));
                         st = h->side;
                     }
@@ -1818,11 +1861,15 @@ int spk_create(int64_t n, int64_t nsuper, const int64_t* xsuper, const int64_t* 
             h->device = dev;
             if (cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || h->nsm < 1)
                 h->nsm = 1;
-            e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking);
-            if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+            // the launch stream (the factorisation's block chain, captured
+            // from it) ahead of the look-ahead streams when SMs free up
+            int lo = 0, hi = 0;
+            if (cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess) lo = hi = 0;
+            e = cudaStreamCreateWithPriority(&h->own, cudaStreamNonBlocking, hi);
+            if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, lo);
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->evP, cudaEventDisableTiming);
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->evB, cudaEventDisableTiming);
-            if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side2, cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&h->side2, cudaStreamNonBlocking, lo);
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->evP2, cudaEventDisableTiming);
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->evI, cudaEventDisableTiming);
             if (e != cudaSuccess) rc = set_err(h, SPK_ECUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
@@ -2067,6 +2114,11 @@ int spk_set_option(spk_handle* h, int option, int64_t value) {
         h->lu_pieces = (int)value;
         drop_factor_graphs(h);
         return SPK_OK;
+    case SPK_OPT_PANEL_SPLIT:
+        if (value != 0 && value != 1) break;
+        h->panel_split = (int)value;
+        drop_factor_graphs(h);
+        return SPK_OK;
     case SPK_OPT_TC_SCHUR_M:
     case SPK_OPT_TC_TRAIL_ROWS:
     case SPK_OPT_TC_WIDE: {
@@ -2098,6 +2150,7 @@ int spk_get_option(spk_handle* h, int option, int64_t* value) {
     case SPK_OPT_TC_WIDE: *value = h->tc_wide; return SPK_OK;
     case SPK_OPT_LU_PIECES: *value = h->lu_pieces; return SPK_OK;
     case SPK_OPT_SOLVE_CLUSTER_MINB: *value = h->fc_minb; return SPK_OK;
+    case SPK_OPT_PANEL_SPLIT: *value = h->panel_split; return SPK_OK;
     default: return set_err(h, SPK_EARG, "spk_get_option: unknown option");
     }
 }

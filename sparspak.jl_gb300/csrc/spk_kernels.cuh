@@ -1443,9 +1443,21 @@ __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, cons
 // ([c1, nf)) and from 0 (U12).
 // Dynamic shared memory: W * SLD(W) T's (plus the line tile of
 // block_panel128).
+// Panel tiles of one launch part: 0 every tile; 1 the near ones (the first
+// two line tiles of the rows below the block and of the front columns right
+// of it: the lines the next block's diagonal region is updated from); 2 the
+// others.  Tiles of 64 lines: L rows first (nL tiles), then front columns
+// (nUa), then U12 columns.
+__device__ __forceinline__ int panel_tile(int part, int tile, int nL, int nUa, bool sym) {
+    if (part == 0) return tile;
+    const int aL = min(2, nL), aU = sym ? 0 : min(2, nUa);
+    if (part == 1) return tile < aL ? tile : nL + (tile - aL);
+    return tile < nL - aL ? aL + tile : nL + aU + (tile - (nL - aL));
+}
+
 template <typename T, int W>
 __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, const int* bmap, Sched S, Launch L,
-                                                      int step, unsigned char* pack, int bf16) {
+                                                      int step, unsigned char* pack, int bf16, int part) {
     constexpr int CQ = W / 4;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sT = reinterpret_cast<T*>(smem_raw);
@@ -1457,6 +1469,10 @@ __global__ void __launch_bounds__(256) k_block_panel(T* fac, const int* ipiv, co
     locate(L, blockIdx.x, fid, tile);
     const DFront F = S.fronts[fid];
     const int blk = F.block0 + step;
+    {
+        const int c1 = S.blk_c1[blk];
+        tile = panel_tile(part, tile, cdiv(F.ld - c1, 64), cdiv(F.nf - c1, 64), S.sym != 0);
+    }
     if constexpr (std::is_same<T, float>::value && W == 128) {
         block_panel128(fac, bmap, S, F, blk, tile, pack, sT, sT + 128 * SLD<float, 128>::value, rd, gmap, pa, bf16,
                        &smax, sdg);

@@ -17,6 +17,11 @@ option autotuner, through the C ABI.
   oracle's pivots in both, FP64 factors within 1e-12.
 * The cluster-solve threshold (SPK_OPT_SOLVE_CLUSTER_MINB) changes only the
   solves' launch lists: the factors are kept, and the solutions agree.
+* The panel split (SPK_OPT_PANEL_SPLIT: a block step's near panel tiles on
+  the launch stream, the far ones beside them on the look-ahead stream) does
+  the same arithmetic as one panel launch: the factors agree to FP32
+  rounding (only the Schur scatter-add order differs) in the FP32, BF16 and
+  SPD forms, and both refine to 1e-12.
 * spk_autotune chooses options from its set, leaves A assembled, and the
   factor that follows refines to 1e-12.
 """
@@ -181,6 +186,27 @@ def test_block_lu_by_pieces_vs_columns(prec):
         it, rr = eng.refine(np.asfortranarray(b), x, prec, 1e-12, 30)
         assert rr <= 1e-12 and relres(A, x, b) <= 1e-12
     print(f"{prec}: by pieces vs column groups, factors differ by {rel(got[1], got[0]):.1e}")
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16s", "fp32+spd"])
+def test_panel_split_matches_one_launch(prec):
+    A = S.gallery.laplacian((36, 36, 36), shift=1e-3)
+    n = A.shape[0]
+    base, _, form = prec.partition("+")
+    s = _solver(A, S.nd_grid(36, 36, 36), precision=base, spd=form == "spd")
+    b = S.gallery.random_rhs(n, 2, seed=9)
+    lnz = {}
+    for split in (1, 0):
+        eng = _factor_with(s, A, panel_split=split)
+        lnz[split] = s.slvr.lnz.copy()
+        x = np.zeros_like(b, order="F")
+        it, rr = eng.refine(np.asfortranarray(b), x, prec, 1e-12, 100)
+        assert rr <= 1e-12 and relres(A, x, b) <= 1e-12, (split, rr, it)
+    d = rel(lnz[1], lnz[0])
+    print(f"{prec}: panel split vs one launch, factors differ by {d:.1e}")
+    assert d < (5e-3 if base == "bf16s" else 1e-5)
+    with pytest.raises(S.ErrorException):
+        eng.set_option("panel_split", 2)
 
 
 def test_solve_cluster_threshold_keeps_factors():
