@@ -449,7 +449,7 @@ __device__ __forceinline__ void lu_group_factor(T (&a)[RPT][4], int g, int bw, c
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         const int k = 4 * g + j;
-        if (k >= bw) break;
+        if (k >= bw) continue;
         const int a0 = cpa[k], b = cpb[k];
         Key best = 0;
         int brow = 0;
@@ -460,13 +460,13 @@ __device__ __forceinline__ void lu_group_factor(T (&a)[RPT][4], int g, int bw, c
             if (ii == 0 || kv > best) { best = kv; brow = R; }
         }
         const int kp = warp_first_max_row(best, brow);
-        const int lk = k / RPT, ik = k % RPT, lp = kp / RPT, ip = kp % RPT;
+        const int lk = (4 * g) / RPT + j / RPT, ik = j % RPT, lp = kp / RPT, ip = kp % RPT;   // k = 4g + j
         const T pv = __shfl_sync(FULL, lu_pick(a, ip, j), lp);
         const bool scale = pv != T(0);
         if (scale && kp != k) {   // swap rows k and kp over the group's columns >= a0
 #pragma unroll
             for (int jj = 0; jj < 4; ++jj) {
-                const T vk = __shfl_sync(FULL, lu_pick(a, ik, jj), lk);
+                const T vk = __shfl_sync(FULL, a[ik][jj], lk);
                 const T vp = __shfl_sync(FULL, lu_pick(a, ip, jj), lp);
                 if (4 * g + jj >= a0) {
 #pragma unroll
@@ -488,7 +488,7 @@ __device__ __forceinline__ void lu_group_factor(T (&a)[RPT][4], int g, int bw, c
         }
 #pragma unroll
         for (int jj = j + 1; jj < 4; ++jj) {   // rank-1 update of the group's later columns
-            const T u = __shfl_sync(FULL, lu_pick(a, ik, jj), lk);
+            const T u = __shfl_sync(FULL, a[ik][jj], lk);
 #pragma unroll
             for (int ii = 0; ii < RPT; ++ii)
                 if (r0 + ii > k) a[ii][jj] -= a[ii][j] * u;
@@ -511,15 +511,15 @@ __device__ __forceinline__ void lu_group_update(T (&a)[RPT][4], int g, int bw, c
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         const int k = 4 * g + j;
-        if (k >= bw) break;
+        if (k >= bw) continue;
         const int kp = skp[j];
         const T pv = spv[j];
-        const int lk = k / RPT, ik = k % RPT;
+        const int lk = (4 * g) / RPT + j / RPT, ik = j % RPT;   // k = 4g + j
         if (pv != T(0) && kp != k) {   // all columns here are after k, hence >= a0
             const int lp = kp / RPT, ip = kp % RPT;
 #pragma unroll
             for (int jj = 0; jj < 4; ++jj) {
-                const T vk = __shfl_sync(FULL, lu_pick(a, ik, jj), lk);
+                const T vk = __shfl_sync(FULL, a[ik][jj], lk);
                 const T vp = __shfl_sync(FULL, lu_pick(a, ip, jj), lp);
 #pragma unroll
                 for (int ii = 0; ii < RPT; ++ii) {
@@ -533,7 +533,7 @@ __device__ __forceinline__ void lu_group_update(T (&a)[RPT][4], int g, int bw, c
         for (int ii = 0; ii < RPT; ++ii) l[ii] = lb[j * (32 * RPT) + r0 + ii];
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
-            const T u = __shfl_sync(FULL, lu_pick(a, ik, jj), lk);
+            const T u = __shfl_sync(FULL, a[ik][jj], lk);
 #pragma unroll
             for (int ii = 0; ii < RPT; ++ii)
                 if (r0 + ii > k) a[ii][jj] -= l[ii] * u;
@@ -551,13 +551,13 @@ __device__ __forceinline__ void lu_group_swap_left(T (&a)[RPT][4], int g, int bw
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         const int k = 4 * g + j;
-        if (k >= bw) break;
+        if (k >= bw) continue;
         const int kp = skp[j], a0 = sa0[j];
         if (spv[j] == T(0) || kp == k || 4 * w + 3 < a0) continue;   // uniform in the warp
-        const int lk = k / RPT, ik = k % RPT, lp = kp / RPT, ip = kp % RPT;
+        const int lk = (4 * g) / RPT + j / RPT, ik = j % RPT, lp = kp / RPT, ip = kp % RPT;   // k = 4g + j
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
-            const T vk = __shfl_sync(FULL, lu_pick(a, ik, jj), lk);
+            const T vk = __shfl_sync(FULL, a[ik][jj], lk);
             const T vp = __shfl_sync(FULL, lu_pick(a, ip, jj), lp);
             if (4 * w + jj >= a0) {
 #pragma unroll
