@@ -347,6 +347,15 @@ int spk_measure_peaks(double* fp32_tflops, double* fp64_tflops, double* dmma_tfl
  *                        on the launch stream, the others beside them on the
  *                        look-ahead stream; 0: one panel launch.  The same
  *                        arithmetic either way.
+ *  SPK_OPT_SCHUR_SPLIT   1 (default): in the float forms, the tiles of a
+ *                        level's tensor-core Schur complements whose target
+ *                        fronts (the owner of the smaller of row and column)
+ *                        are factored two or more levels up run on a third
+ *                        stream on half the SMs, beside the next level's
+ *                        factorisation, and are awaited two levels on,
+ *                        before any of their targets is factored; 0: all
+ *                        tiles before the next level.  Atomic scatter-adds either way (the sums
+ *                        come in another order: FP32 rounding).
  */
 #define SPK_OPT_LEAF_QUEUE 0
 #define SPK_OPT_WAIT_BUDGET 1
@@ -357,6 +366,7 @@ int spk_measure_peaks(double* fp32_tflops, double* fp64_tflops, double* dmma_tfl
 #define SPK_OPT_LU_PIECES 6
 #define SPK_OPT_SOLVE_CLUSTER_MINB 7
 #define SPK_OPT_PANEL_SPLIT 8
+#define SPK_OPT_SCHUR_SPLIT 9
 int spk_set_option(spk_handle* h, int option, int64_t value);
 int spk_get_option(spk_handle* h, int option, int64_t* value);
 

@@ -54,6 +54,9 @@ struct Timed {
 // the forward block steps, and backward the U12 product and block steps.
 struct LevelPlan {
     LaunchRec schur, schur_tc, bwdu;
+    // schur_tc in two parts: the tiles whose targets the next level factors
+    // (near) and the others (far, beside the next level's factorisation)
+    LaunchRec schur_tc_near, schur_tc_far;
     // btrail_tc0: tile 0 of each packed front's trailing update (it holds the
     // next block's diagonal block); btrail_tc: its tiles 1..
     std::vector<LaunchRec> blu, bpanel, btrail, btrail_tc0, btrail_tc, fwd, bwd;
@@ -100,6 +103,9 @@ struct Plan {
     int inv_split = 0;                    // group 0: blocks of fronts below this level (final before it starts)
     ll inv2_size = 0;
     std::vector<int> block0, nblocks;     // per front
+    // per front: update-row tiles holding the rows that fronts of the next
+    // level own (spk::schur_part_tile; DFront::sq)
+    std::vector<int> schur_q;
     std::vector<LevelPlan> levels;
     std::vector<int> sched_ids, sched_prefix;
     // The leaf queue (k_leaf_queue): the fronts factored whole (by a warp)
@@ -204,6 +210,11 @@ struct spk_handle {
     // the operators done).
     cudaStream_t side2 = nullptr;
     cudaEvent_t evP2 = nullptr, evI = nullptr;
+    // The far tiles of a level's tensor-core Schur complements run on side3
+    // beside the next level (evS: the level done; evF[l % 2]: level l's far
+    // tiles done, awaited before level l + 2 starts).
+    cudaStream_t side3 = nullptr;
+    cudaEvent_t evS = nullptr, evF[2] = {nullptr, nullptr};
     bool fc16 = false;   // front solves by clusters of 16 CTAs
     cudaEvent_t evP = nullptr, evB = nullptr;
     int device = -1;
@@ -217,6 +228,7 @@ struct spk_handle {
     int lu_pieces = 0;                     // SPK_OPT_LU_PIECES: block LU by pieces (slower on GB300, see header)
     int fc_minb = spk::FC_MINB;            // SPK_OPT_SOLVE_CLUSTER_MINB: blocks of a front for the cluster solve
     int panel_split = 1;                   // SPK_OPT_PANEL_SPLIT: near / far panel tiles on two streams
+    int schur_split = 1;                   // SPK_OPT_SCHUR_SPLIT: far Schur tiles beside the next level
     std::string err;
 
     // launch accounting and optional per-class event timing
@@ -691,6 +703,14 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc, bool sym
             P.inv_off[g][3] = (int)P.inv_ids.size();
         }
     }
+    P.schur_q.assign(nfr, 0);
+    for (int i = 0; i < nfr; ++i) {   // the last row a front of the next level owns
+        const HFront& F = h->fronts[i];
+        int p = 0;
+        for (int k = 0; k < F.m; ++k)
+            if (h->fronts[h->col_front[h->rows[F.rows_off + k]]].level <= F.level + 1) p = k + 1;
+        P.schur_q[i] = cdiv(p, spk::umma::TM);
+    }
     const int nlev = h->nlevels;
     std::vector<std::vector<int>> at(nlev);
     for (int i = 0; i < nfr; ++i) at[h->fronts[i].level].push_back(i);
@@ -920,6 +940,25 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc, bool sym
         }
         add_launch(&P, L.schur, ids, tsch, fs, ws);
         add_launch(&P, L.schur_tc, ids, tsch_tc, fs, ws);
+        {   // its near and far parts, flops and words by tile share
+            std::vector<int> tn(nid), tfar(nid);
+            std::vector<double> fn(nid), wn(nid), ffar(nid), wfar(nid);
+            for (size_t k = 0; k < nid; ++k) {
+                tn[k] = tfar[k] = 0;
+                fn[k] = wn[k] = ffar[k] = wfar[k] = 0.0;
+                if (tsch_tc[k] <= 0) continue;
+                const int ntc = cdiv(h->fronts[ids[k]].m, spk::umma::TM), q = P.schur_q[ids[k]];
+                tn[k] = spk::schur_part_count(1, ntc, P.schur_nh, q, sym);
+                tfar[k] = spk::schur_part_count(2, ntc, P.schur_nh, q, sym);
+                const double a = (double)tn[k] / tsch_tc[k];
+                fn[k] = fs[k] * a;
+                wn[k] = ws[k] * a;
+                ffar[k] = fs[k] - fn[k];
+                wfar[k] = ws[k] - wn[k];
+            }
+            add_launch(&P, L.schur_tc_near, ids, tn, fn, wn);
+            add_launch(&P, L.schur_tc_far, ids, tfar, ffar, wfar);
+        }
         add_launch(&P, L.bwdu, ids, tbu, fu, wu);
         for (size_t k = 0; k < nid; ++k)
             if (leaf[k]) tbu[k] = 0;
@@ -984,7 +1023,7 @@ static int ensure_plan(spk_handle* h) {
         d.run0 = F.run0;
         d.block0 = P.block0[i];
         d.nblocks = P.nblocks[i];
-        d.pad = 0;
+        d.sq = P.schur_q[i];
     }
     int rc;
     if ((rc = upload(h, &P.d_fronts, df))) return rc;
@@ -1249,8 +1288,13 @@ static int factor_launches(spk_handle* h, int fs_nrhs = 0) {
             fac, h->d_ipiv, h->d_info, S, PL.d_q_order, PL.d_q_parent, PL.nq, PL.d_q_next, PL.d_q_deps, budget,
             h->stall_test, h->d_info + 2);
     }
+    bool far_pending[2] = {false, false};   // far Schur tiles of level l in flight on side3 (slot l % 2)
     for (size_t lvl = 0; lvl < PL.levels.size(); ++lvl) {
         const LevelPlan& P = PL.levels[lvl];
+        if (far_pending[lvl & 1]) {   // level lvl - 2's far tiles target this level and above
+            CU(h, cudaStreamWaitEvent(h->stream, h->evF[lvl & 1], 0));
+            far_pending[lvl & 1] = false;
+        }
         const bool fs_here = fs_nrhs > 0 && (size_t)lvl == fused_split<T>(h) && lvl > 0;
         if (ahead && (int)lvl == PL.inv_split && (PL.inv_off[0][3] > PL.inv_off[0][0] || fs_here)) {
             // group 0's blocks are final: their operators beside the last levels
@@ -1350,7 +1394,7 @@ static int factor_launches(spk_handle* h, int fs_nrhs = 0) {
                     LaunchScope ls(h, SPK_K_TC_TRAIL, P.btrail_tc[t].flops, P.btrail_tc[t].words * sizeof(T));
                     auto kern = bf16 ? spk::k_tc_update<spk::TC_TRAIL, true> : spk::k_tc_update<spk::TC_TRAIL, false>;
                     kern<<<grid, spk::TC_THREADS, spk::umma::PSMEM, st>>>(
-                        fac, storage<T>(h).pack, S, launch_of(PL, P.btrail_tc[t]), (int)t, nt, 1, h->d_info + 1);
+                        fac, storage<T>(h).pack, S, launch_of(PL, P.btrail_tc[t]), (int)t, nt, 1, 0, h->d_info + 1);
                     if (ahead) {
                         CU(h, cudaEventRecord(h->evB, h->side));
                         pending = true;
@@ -1362,7 +1406,7 @@ static int factor_launches(spk_handle* h, int fs_nrhs = 0) {
                     const int nt = P.btrail_tc0[t].tiles;
                     auto kern = bf16 ? spk::k_tc_update<spk::TC_TRAIL, true> : spk::k_tc_update<spk::TC_TRAIL, false>;
                     kern<<<std::min(nt, h->nsm), spk::TC_THREADS, spk::umma::PSMEM, h->stream>>>(
-                        fac, storage<T>(h).pack, S, launch_of(PL, P.btrail_tc0[t]), (int)t, nt, 0, h->d_info + 1);
+                        fac, storage<T>(h).pack, S, launch_of(PL, P.btrail_tc0[t]), (int)t, nt, 0, 0, h->d_info + 1);
                 }
             }
         }
@@ -1375,22 +1419,39 @@ static int factor_launches(spk_handle* h, int fs_nrhs = 0) {
             spk::k_schur<T><<<P.schur.tiles, 256, 0, h->stream>>>(fac, S, launch_of(PL, P.schur));
         }
         if constexpr (std::is_same<T, float>::value) {
-            if (P.schur_tc.tiles > 0) {
-                LaunchScope ls(h, SPK_K_TC_SCHUR, P.schur_tc.flops, P.schur_tc.words * sizeof(T));
-                const int nt = P.schur_tc.tiles;
-                const spk::Launch la = launch_of(PL, P.schur_tc);
+            auto schur_tc = [&](const LaunchRec& rec, int part, int grid, cudaStream_t st) {
+                if (rec.tiles <= 0) return;
+                LaunchScope ls(h, SPK_K_TC_SCHUR, rec.flops, rec.words * sizeof(T));
+                const int nt = rec.tiles;
+                const spk::Launch la = launch_of(PL, rec);
                 if (PL.schur_nh == 2) {   // 128 x 256 tiles
                     auto kern = bf16 ? spk::k_tc_update<spk::TC_SCHUR, true, 2> : spk::k_tc_update<spk::TC_SCHUR, false, 2>;
-                    kern<<<std::min(nt, h->nsm), spk::TC_THREADS, spk::umma::PGeo<2>::SMEM, h->stream>>>(
-                        fac, storage<T>(h).pack, S, la, 0, nt, 0, h->d_info + 1);
+                    kern<<<std::min(nt, grid), spk::TC_THREADS, spk::umma::PGeo<2>::SMEM, st>>>(
+                        fac, storage<T>(h).pack, S, la, 0, nt, 0, part, h->d_info + 1);
                 } else {
                     auto kern = bf16 ? spk::k_tc_update<spk::TC_SCHUR, true> : spk::k_tc_update<spk::TC_SCHUR, false>;
-                    kern<<<std::min(nt, h->nsm), spk::TC_THREADS, spk::umma::PSMEM, h->stream>>>(
-                        fac, storage<T>(h).pack, S, la, 0, nt, 0, h->d_info + 1);
+                    kern<<<std::min(nt, grid), spk::TC_THREADS, spk::umma::PSMEM, st>>>(
+                        fac, storage<T>(h).pack, S, la, 0, nt, 0, part, h->d_info + 1);
                 }
+            };
+            // Far tiles (targets two or more levels up) on side3, on half the
+            // SMs, beside the near tiles and the next level; every scatter is
+            // an atomic add, so they may overlap the other levels' updates of
+            // the same fronts.
+            if (ahead && h->schur_split && P.schur_tc_far.tiles > 0) {
+                CU(h, cudaEventRecord(h->evS, h->stream));
+                schur_tc(P.schur_tc_near, 1, h->nsm, h->stream);
+                CU(h, cudaStreamWaitEvent(h->side3, h->evS, 0));
+                schur_tc(P.schur_tc_far, 2, std::max(1, h->nsm / 2), h->side3);
+                CU(h, cudaEventRecord(h->evF[lvl & 1], h->side3));
+                far_pending[lvl & 1] = true;
+            } else {
+                schur_tc(P.schur_tc, 0, h->nsm, h->stream);
             }
         }
     }
+    for (int k = 0; k < 2; ++k)   // join side3 (nothing is left to target, but the graph must rejoin)
+        if (far_pending[k]) CU(h, cudaStreamWaitEvent(h->stream, h->evF[k], 0));
     if (pending_inv) CU(h, cudaStreamWaitEvent(h->stream, h->evI, 0));
     else launch_inv(0, h->stream);
     launch_inv(1, h->stream);
@@ -1872,6 +1933,9 @@ int spk_create(int64_t n, int64_t nsuper, const int64_t* xsuper, const int64_t* 
             if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&h->side2, cudaStreamNonBlocking, lo);
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->evP2, cudaEventDisableTiming);
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->evI, cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&h->side3, cudaStreamNonBlocking, lo);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->evS, cudaEventDisableTiming);
+            for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&h->evF[k], cudaEventDisableTiming);
             if (e != cudaSuccess) rc = set_err(h, SPK_ECUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
             h->stream = h->own;
         }
@@ -2119,6 +2183,11 @@ int spk_set_option(spk_handle* h, int option, int64_t value) {
         h->panel_split = (int)value;
         drop_factor_graphs(h);
         return SPK_OK;
+    case SPK_OPT_SCHUR_SPLIT:
+        if (value != 0 && value != 1) break;
+        h->schur_split = (int)value;
+        drop_factor_graphs(h);
+        return SPK_OK;
     case SPK_OPT_TC_SCHUR_M:
     case SPK_OPT_TC_TRAIL_ROWS:
     case SPK_OPT_TC_WIDE: {
@@ -2151,6 +2220,7 @@ int spk_get_option(spk_handle* h, int option, int64_t* value) {
     case SPK_OPT_LU_PIECES: *value = h->lu_pieces; return SPK_OK;
     case SPK_OPT_SOLVE_CLUSTER_MINB: *value = h->fc_minb; return SPK_OK;
     case SPK_OPT_PANEL_SPLIT: *value = h->panel_split; return SPK_OK;
+    case SPK_OPT_SCHUR_SPLIT: *value = h->schur_split; return SPK_OK;
     default: return set_err(h, SPK_EARG, "spk_get_option: unknown option");
     }
 }
@@ -2733,12 +2803,17 @@ void spk_destroy(spk_handle* h) {
     drop_solve_graphs(h);
     if (h->side) cudaStreamSynchronize(h->side);
     if (h->side2) cudaStreamSynchronize(h->side2);
+    if (h->side3) cudaStreamSynchronize(h->side3);
     if (h->evP) cudaEventDestroy(h->evP);
     if (h->evB) cudaEventDestroy(h->evB);
     if (h->evP2) cudaEventDestroy(h->evP2);
     if (h->evI) cudaEventDestroy(h->evI);
+    if (h->evS) cudaEventDestroy(h->evS);
+    for (cudaEvent_t e : h->evF)
+        if (e) cudaEventDestroy(e);
     if (h->side) cudaStreamDestroy(h->side);
     if (h->side2) cudaStreamDestroy(h->side2);
+    if (h->side3) cudaStreamDestroy(h->side3);
     if (h->own) cudaStreamDestroy(h->own);
     delete h;
 }

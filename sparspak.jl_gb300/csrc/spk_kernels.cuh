@@ -52,7 +52,7 @@ struct DFront {
     int run0;      // first run of the front in run_*[]
     int block0;    // first block of the front (in the plan's block arrays)
     int nblocks;
-    int pad;
+    int sq;        // update-row tiles (128 rows) holding the rows that fronts of the next level own (schur_part_tile)
 };
 
 // A run is a maximal stretch of R_F lying in the columns of one ancestor
@@ -1762,6 +1762,43 @@ __host__ __device__ __forceinline__ int lower_tiles_w(int nr, int w) {
     return n;
 }
 
+// The Schur complement tiles of a tensor-core front in two parts: the near
+// part (1) holds every tile with an entry whose target front - the owner of
+// the smaller of its row and column, rows sorted ascending - is factored at
+// the next level, i.e. a row tile or a column below q (the first q row
+// tiles hold every row such a front owns); the far part (2) the others,
+// whose targets are factored two or more levels up.  Tiles of the whole
+// update (part 0): t = g n2 + rt, column group g of nh tiles and row tile
+// rt; in the SPD form the lower tiles of group g (rows nh g .. n2 - 1) in
+// that order, where the near part is the groups below cdiv(q, nh).
+__host__ __device__ __forceinline__ int schur_part_count(int part, int n2, int nh, int q, bool sym) {
+    const int ng = cdiv(n2, nh);
+    q = min(q, n2);
+    const int gq = min(cdiv(q, nh), ng);
+    const int all = sym ? lower_tiles_w(n2, nh) : ng * n2;
+    int far;
+    if (sym) {
+        int near = 0;
+        for (int j = 0; j < gq; ++j) near += n2 - nh * j;
+        far = all - near;
+    } else {
+        far = (ng - gq) * (n2 - q);
+    }
+    return part == 0 ? all : part == 1 ? all - far : far;
+}
+__host__ __device__ __forceinline__ int schur_part_tile(int part, int e, int n2, int nh, int q, bool sym) {
+    if (part == 0) return e;
+    q = min(q, n2);
+    const int gq = min(cdiv(q, nh), cdiv(n2, nh));
+    if (sym) return part == 1 ? e : schur_part_count(1, n2, nh, q, true) + e;
+    if (part == 1) {
+        if (e < gq * n2) return e;
+        e -= gq * n2;
+        return (gq + e / q) * n2 + e % q;
+    }
+    return (gq + e / (n2 - q)) * n2 + q + e % (n2 - q);
+}
+
 template <typename T, bool rows_fast>
 __device__ __forceinline__ void mma_tile(const T* sA, const T* sB, int kc, T acc[4][4]) {
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -2179,7 +2216,8 @@ __global__ void __launch_bounds__(256) k_schur(T* fac, Sched S, Launch L) {
 // A launch covers local tiles tile_base.. of each front in its list (the
 // trailing update is launched as tile 0, which holds the next block's
 // diagonal block, and tiles 1.., so that the next block LU can start before
-// the rest of the update is done).
+// the rest of the update is done).  SCHUR launches of part 1 / 2 cover the
+// near / far tiles of each front (schur_part_tile), part 0 all of them.
 // Persistent: CTA b takes tiles b, b + gridDim.x, ...  Warp 0 lane 0 issues
 // the bulk copies, warp 1 lane 0 the MMAs, and the TC_EPI epilogue warps
 // (from warp 4; warp w reads TMEM lanes 32 (w % 4).. and the 32 accumulator
@@ -2196,7 +2234,8 @@ struct TcTile {
 };
 
 template <int MODE, int NH = 1>
-__device__ __forceinline__ TcTile tc_decode(const Sched& S, const Launch& L, int step, int tile, int tile_base) {
+__device__ __forceinline__ TcTile tc_decode(const Sched& S, const Launch& L, int step, int tile, int tile_base,
+                                           int part) {
     TcTile T;
     int fid, t;
     locate(L, tile, fid, t);
@@ -2223,6 +2262,7 @@ __device__ __forceinline__ TcTile tc_decode(const Sched& S, const Launch& L, int
         T.nh = 1;
     } else {
         T.n1 = 0;
+        t = schur_part_tile(part, t, n2, NH, T.F.sq, S.sym != 0);
         int g;
         if (S.sym) {
             lower_tile_w(t, n2, NH, T.rt, g);
@@ -2277,7 +2317,7 @@ struct ChunkWalk {
 
 template <int MODE, bool BF, int NH = 1>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const unsigned char* pack, Sched S, Launch L,
-                                                              int step, int ntiles, int tile_base, int* err) {
+                                                              int step, int ntiles, int tile_base, int part, int* err) {
     static_assert(MODE == TC_SCHUR || NH == 1, "wide tiles are for the Schur complements");
     using G = umma::PGeo<NH>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -2313,7 +2353,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
             int s = 0;
             uint32_t ph = 0;
             for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-                const TcTile T = tc_decode<MODE, NH>(S, L, step, tile, tile_base);
+                const TcTile T = tc_decode<MODE, NH>(S, L, step, tile, tile_base, part);
                 ChunkWalk<MODE, BF> w(S, T, step);
                 int b, c, kc;
                 while (w.next(S, b, c, kc)) {
@@ -2344,7 +2384,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
             int acc = 0;
             uint32_t aph = 0;
             for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-                const TcTile T = tc_decode<MODE, NH>(S, L, step, tile, tile_base);
+                const TcTile T = tc_decode<MODE, NH>(S, L, step, tile, tile_base, part);
                 umma::wait_bounded(&cx.tempty[acc], aph ^ 1, vdead, err);
                 umma::fence_after();
                 ChunkWalk<MODE, BF> w(S, T, step);
@@ -2392,7 +2432,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(float* fac, const u
         int acc = 0;
         uint32_t aph = 0;
         for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-            const TcTile T = tc_decode<MODE, NH>(S, L, step, tile, tile_base);
+            const TcTile T = tc_decode<MODE, NH>(S, L, step, tile, tile_base, part);
             const DFront& F = T.F;
             if (MODE == TC_SCHUR) {
                 asm volatile("bar.sync 1, %0;" ::"n"(32 * TC_EPI) : "memory");   // previous tile's scatter done

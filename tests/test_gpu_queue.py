@@ -22,6 +22,10 @@ option autotuner, through the C ABI.
   the same arithmetic as one panel launch: the factors agree to FP32
   rounding (only the Schur scatter-add order differs) in the FP32, BF16 and
   SPD forms, and both refine to 1e-12.
+* The Schur split (SPK_OPT_SCHUR_SPLIT: the Schur tiles whose targets are
+  factored two or more levels up run on a third stream beside the next
+  level) gives the same factors to FP32 rounding (atomic scatter-adds in
+  another order) in the FP32, BF16 and SPD forms, and both refine to 1e-12.
 * spk_autotune chooses options from its set, leaves A assembled, and the
   factor that follows refines to 1e-12.
 """
@@ -207,6 +211,29 @@ def test_panel_split_matches_one_launch(prec):
     assert d < (5e-3 if base == "bf16s" else 1e-5)
     with pytest.raises(S.ErrorException):
         eng.set_option("panel_split", 2)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16s", "fp32+spd"])
+def test_schur_split_matches_one_launch(prec):
+    A = S.gallery.laplacian((40, 40, 40), shift=1e-3)
+    n = A.shape[0]
+    base, _, form = prec.partition("+")
+    s = _solver(A, S.nd_grid(40, 40, 40), precision=base, spd=form == "spd")
+    b = S.gallery.random_rhs(n, 2, seed=12)
+    lnz, xs = {}, {}
+    for split in (1, 0):
+        eng = _factor_with(s, A, schur_split=split)
+        lnz[split] = s.slvr.lnz.copy()
+        x = np.zeros_like(b, order="F")
+        it, rr = eng.refine(np.asfortranarray(b), x, prec, 1e-12, 100)
+        assert rr <= 1e-12 and relres(A, x, b) <= 1e-12, (split, rr, it)
+        xs[split] = x
+    d = rel(lnz[1], lnz[0])
+    print(f"{prec}: Schur split vs one launch, factors differ by {d:.1e}")
+    assert d < (5e-3 if base == "bf16s" else 1e-5)
+    assert rel(xs[1], xs[0]) < 1e-10
+    with pytest.raises(S.ErrorException):
+        eng.set_option("schur_split", 2)
 
 
 def test_solve_cluster_threshold_keeps_factors():
