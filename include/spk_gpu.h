@@ -351,11 +351,15 @@ int spk_measure_peaks(double* fp32_tflops, double* fp64_tflops, double* dmma_tfl
  *                        level's tensor-core Schur complements whose target
  *                        fronts (the owner of the smaller of row and column)
  *                        are factored two or more levels up run on a third
- *                        stream on half the SMs, beside the next level's
- *                        factorisation, and are awaited two levels on,
- *                        before any of their targets is factored; 0: all
- *                        tiles before the next level.  Atomic scatter-adds either way (the sums
- *                        come in another order: FP32 rounding).
+ *                        stream on SPK_OPT_SCHUR_FAR_SMS SMs, beside the
+ *                        next level's factorisation, and are awaited two
+ *                        levels on, before any of their targets is
+ *                        factored; 0: all tiles before the next level.
+ *                        Atomic scatter-adds either way (the sums come in
+ *                        another order: FP32 rounding).
+ *  SPK_OPT_SCHUR_FAR_SMS CTAs (one per SM) of those far tiles (0, the
+ *                        default: seven eighths of the SMs; the launch
+ *                        stream's kernels take SMs first as they free up).
  */
 #define SPK_OPT_LEAF_QUEUE 0
 #define SPK_OPT_WAIT_BUDGET 1
@@ -367,6 +371,7 @@ int spk_measure_peaks(double* fp32_tflops, double* fp64_tflops, double* dmma_tfl
 #define SPK_OPT_SOLVE_CLUSTER_MINB 7
 #define SPK_OPT_PANEL_SPLIT 8
 #define SPK_OPT_SCHUR_SPLIT 9
+#define SPK_OPT_SCHUR_FAR_SMS 10
 int spk_set_option(spk_handle* h, int option, int64_t value);
 int spk_get_option(spk_handle* h, int option, int64_t* value);
 

@@ -229,6 +229,7 @@ struct spk_handle {
     int fc_minb = spk::FC_MINB;            // SPK_OPT_SOLVE_CLUSTER_MINB: blocks of a front for the cluster solve
     int panel_split = 1;                   // SPK_OPT_PANEL_SPLIT: near / far panel tiles on two streams
     int schur_split = 1;                   // SPK_OPT_SCHUR_SPLIT: far Schur tiles beside the next level
+    int schur_far_sms = 0;                 // SPK_OPT_SCHUR_FAR_SMS: their CTAs (0: seven eighths of the SMs)
     std::string err;
 
     // launch accounting and optional per-class event timing
@@ -1289,6 +1290,7 @@ static int factor_launches(spk_handle* h, int fs_nrhs = 0) {
             h->stall_test, h->d_info + 2);
     }
     bool far_pending[2] = {false, false};   // far Schur tiles of level l in flight on side3 (slot l % 2)
+    const int far_sms = h->schur_far_sms > 0 ? std::min(h->schur_far_sms, h->nsm) : std::max(1, h->nsm * 7 / 8);
     for (size_t lvl = 0; lvl < PL.levels.size(); ++lvl) {
         const LevelPlan& P = PL.levels[lvl];
         if (far_pending[lvl & 1]) {   // level lvl - 2's far tiles target this level and above
@@ -1434,7 +1436,7 @@ static int factor_launches(spk_handle* h, int fs_nrhs = 0) {
                         fac, storage<T>(h).pack, S, la, 0, nt, 0, part, h->d_info + 1);
                 }
             };
-            // Far tiles (targets two or more levels up) on side3, on half the
+            // Far tiles (targets two or more levels up) on side3, on far_sms
             // SMs, beside the near tiles and the next level; every scatter is
             // an atomic add, so they may overlap the other levels' updates of
             // the same fronts.
@@ -1442,7 +1444,7 @@ static int factor_launches(spk_handle* h, int fs_nrhs = 0) {
                 CU(h, cudaEventRecord(h->evS, h->stream));
                 schur_tc(P.schur_tc_near, 1, h->nsm, h->stream);
                 CU(h, cudaStreamWaitEvent(h->side3, h->evS, 0));
-                schur_tc(P.schur_tc_far, 2, std::max(1, h->nsm / 2), h->side3);
+                schur_tc(P.schur_tc_far, 2, far_sms, h->side3);
                 CU(h, cudaEventRecord(h->evF[lvl & 1], h->side3));
                 far_pending[lvl & 1] = true;
             } else {
@@ -2188,6 +2190,11 @@ int spk_set_option(spk_handle* h, int option, int64_t value) {
         h->schur_split = (int)value;
         drop_factor_graphs(h);
         return SPK_OK;
+    case SPK_OPT_SCHUR_FAR_SMS:
+        if (value < 0 || value > 4096) break;
+        h->schur_far_sms = (int)value;
+        drop_factor_graphs(h);
+        return SPK_OK;
     case SPK_OPT_TC_SCHUR_M:
     case SPK_OPT_TC_TRAIL_ROWS:
     case SPK_OPT_TC_WIDE: {
@@ -2221,6 +2228,7 @@ int spk_get_option(spk_handle* h, int option, int64_t* value) {
     case SPK_OPT_SOLVE_CLUSTER_MINB: *value = h->fc_minb; return SPK_OK;
     case SPK_OPT_PANEL_SPLIT: *value = h->panel_split; return SPK_OK;
     case SPK_OPT_SCHUR_SPLIT: *value = h->schur_split; return SPK_OK;
+    case SPK_OPT_SCHUR_FAR_SMS: *value = h->schur_far_sms; return SPK_OK;
     default: return set_err(h, SPK_EARG, "spk_get_option: unknown option");
     }
 }
