@@ -360,6 +360,13 @@ int spk_measure_peaks(double* fp32_tflops, double* fp64_tflops, double* dmma_tfl
  *  SPK_OPT_SCHUR_FAR_SMS CTAs (one per SM) of those far tiles (0, the
  *                        default: seven eighths of the SMs; the launch
  *                        stream's kernels take SMs first as they free up).
+ *  SPK_OPT_SOLVE_CHUNK   1 (default): a root front (no rows below it) of more
+ *                        than 16 blocks is solved in chunks of at most 16
+ *                        consecutive blocks, one cluster launch each, the
+ *                        chunks linked by a product over all SMs (forward
+ *                        the L rows below a chunk, backward the U rows
+ *                        above it); 0: one cluster launch.  Keeps the
+ *                        factors.
  */
 #define SPK_OPT_LEAF_QUEUE 0
 #define SPK_OPT_WAIT_BUDGET 1
@@ -372,6 +379,7 @@ int spk_measure_peaks(double* fp32_tflops, double* fp64_tflops, double* dmma_tfl
 #define SPK_OPT_PANEL_SPLIT 8
 #define SPK_OPT_SCHUR_SPLIT 9
 #define SPK_OPT_SCHUR_FAR_SMS 10
+#define SPK_OPT_SOLVE_CHUNK 11
 int spk_set_option(spk_handle* h, int option, int64_t value);
 int spk_get_option(spk_handle* h, int option, int64_t* value);
 

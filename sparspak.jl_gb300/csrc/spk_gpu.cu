@@ -71,6 +71,14 @@ struct LevelPlan {
     // leaf_q: the leaf queue's fronts of this level, for when the queue is off
     LaunchRec leaf_factor[spk::LF_CLASSES], leaf_q[spk::LF_CLASSES];
     LaunchRec front_big, front_l21;   // front_l21: tiles of k_fwd_l21 for the front_big fronts
+    // Root fronts of more than spk::FC_CHUNK blocks: solved in chunks of
+    // consecutive blocks (a cluster launch each, on a pseudo front - the
+    // front's storage, the chunk's blocks), linked by k_front_gemv.
+    struct SolveChunk {
+        int front, lo, hi;   // front-local columns [lo, hi)
+        LaunchRec rec;       // the cluster launch on the pseudo front
+    };
+    std::vector<SolveChunk> chunks;
     // Small fronts (one block of at most 32 columns, m <= spk::LEAF_M) by
     // k_solve_leaf, a warp per front; bwdu_small: U12 products of the others.
     LaunchRec front_leaf[spk::LF_CLASSES], bwdu_small;   // front_leaf by width class (k_solve_leaf<W>)
@@ -106,6 +114,9 @@ struct Plan {
     // per front: update-row tiles holding the rows that fronts of the next
     // level own (spk::schur_part_tile; DFront::sq)
     std::vector<int> schur_q;
+    // pseudo fronts of the chunked solves (LevelPlan::SolveChunk): front,
+    // first block, blocks; device front ids from the number of fronts on
+    std::vector<int> pf_front, pf_b0, pf_nb;
     std::vector<LevelPlan> levels;
     std::vector<int> sched_ids, sched_prefix;
     // The leaf queue (k_leaf_queue): the fronts factored whole (by a warp)
@@ -230,6 +241,7 @@ struct spk_handle {
     int panel_split = 1;                   // SPK_OPT_PANEL_SPLIT: near / far panel tiles on two streams
     int schur_split = 1;                   // SPK_OPT_SCHUR_SPLIT: far Schur tiles beside the next level
     int schur_far_sms = 0;                 // SPK_OPT_SCHUR_FAR_SMS: their CTAs (0: seven eighths of the SMs)
+    int solve_chunk = 1;                   // SPK_OPT_SOLVE_CHUNK: root fronts solved in chunks of blocks
     std::string err;
 
     // launch accounting and optional per-class event timing
@@ -778,10 +790,30 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc, bool sym
                 const HFront& F = h->fronts[ids[k]];
                 const int nb = P.nblocks[ids[k]];
                 big[k] = nb >= h->fc_minb && nb <= spk::FC * spk::FC_OWN;
-                tbig[k] = big[k] ? 1 : 0;
+                const bool chunked = big[k] && h->solve_chunk && F.m == 0 && nb > spk::FC_CHUNK;
+                tbig[k] = big[k] && !chunked ? 1 : 0;
                 const double nf = F.nf;
                 fbig[k] = 2.0 * nf * nf;   // per right-hand side, both directions alike
                 wbig[k] = nf * nf;
+                if (chunked) {   // equal chunks of at most FC_CHUNK blocks
+                    const int nch = cdiv(nb, spk::FC_CHUNK);
+                    for (int c = 0, b = 0; c < nch; ++c) {
+                        const int len = (nb - b) / (nch - c);
+                        LevelPlan::SolveChunk ch;
+                        ch.front = ids[k];
+                        ch.lo = P.blk_c0[P.block0[ids[k]] + b];
+                        ch.hi = P.blk_c1[P.block0[ids[k]] + b + len - 1];
+                        const int pid = nfr + (int)P.pf_front.size();
+                        P.pf_front.push_back(ids[k]);
+                        P.pf_b0.push_back(P.block0[ids[k]] + b);
+                        P.pf_nb.push_back(len);
+                        const double w = ch.hi - ch.lo;
+                        add_launch(&P, ch.rec, std::vector<int>{pid}, std::vector<int>{1},
+                                   std::vector<double>{2.0 * w * w}, std::vector<double>{w * w});
+                        L.chunks.push_back(ch);
+                        b += len;
+                    }
+                }
             }
             add_launch(&P, L.front_big, ids, tbig, fbig, wbig);
             for (size_t k = 0; k < nid; ++k) {
@@ -1025,6 +1057,12 @@ static int ensure_plan(spk_handle* h) {
         d.block0 = P.block0[i];
         d.nblocks = P.nblocks[i];
         d.sq = P.schur_q[i];
+    }
+    for (size_t k = 0; k < P.pf_front.size(); ++k) {   // pseudo fronts of the chunked solves
+        spk::DFront d = df[P.pf_front[k]];
+        d.block0 = P.pf_b0[k];
+        d.nblocks = P.pf_nb[k];
+        df.push_back(d);
     }
     int rc;
     if ((rc = upload(h, &P.d_fronts, df))) return rc;
@@ -1528,6 +1566,27 @@ static int solve_fwd_levels(spk_handle* h, int nrhs, size_t l0, size_t l1, cudaS
             CU(h, launch_chained(spk::k_fwd_l21<T>, P.front_l21.tiles, 256, 0, st, fac, b, (const T*)y, n, nrhs,
                                  S, launch_of(PL, P.front_l21)));
         }
+        for (size_t c = 0; c < P.chunks.size(); ++c) {   // chunked root fronts, chunks in order
+            const LevelPlan::SolveChunk& ch = P.chunks[c];
+            {
+                LaunchScope ls(h, SPK_K_FWD, ch.rec.flops * nrhs, ch.rec.words * sizeof(T));
+                if (h->fc16)
+                    spk::k_front_solve<T, true, 16><<<16, spk::FC_THREADS, fc_smem, st>>>(fac, inv, b, y, n, nrhs, S,
+                                                                                         launch_of(PL, ch.rec));
+                else
+                    spk::k_front_solve<T, true, spk::FC><<<spk::FC, spk::FC_THREADS, fc_smem, st>>>(
+                        fac, inv, b, y, n, nrhs, S, launch_of(PL, ch.rec));
+            }
+            if (c + 1 < P.chunks.size() && P.chunks[c + 1].front == ch.front) {   // rows below the chunk
+                const HFront& F = h->fronts[ch.front];
+                const int r0 = ch.hi, r1 = F.nf;
+                LaunchScope ls(h, SPK_K_FWD, 2.0 * (r1 - r0) * (ch.hi - ch.lo) * nrhs,
+                               (double)(r1 - r0) * (ch.hi - ch.lo) * sizeof(T));
+                const int grid = spk::cdiv(r1 - r0, spk::L21_ROWS) * spk::cdiv(ch.hi - ch.lo, spk::L21_COLS);
+                spk::k_front_gemv<T><<<grid, 256, 0, st>>>(fac, b, (const T*)y, n, nrhs, F.loff, F.nf + F.m,
+                                                          (int)F.f, r0, r1, ch.lo, ch.hi);
+            }
+        }
         for (size_t t = 0; t < P.fwd_small.size(); ++t)
             if (P.fwd_small[t].tiles > 0) {
                 LaunchScope ls(h, SPK_K_FWD, P.fwd_small[t].flops * nrhs, P.fwd_small[t].words * sizeof(T));
@@ -1573,6 +1632,27 @@ static int solve_bwd_levels(spk_handle* h, int nrhs, cudaStream_t st) {
                 spk::k_front_solve<T, false, spk::FC><<<spk::FC * P.front_big.tiles, spk::FC_THREADS, fc_smem,
                                                         st>>>(fac, inv, y, x, n, nrhs, S,
                                                                      launch_of(PL, P.front_big));
+        }
+        for (size_t c = P.chunks.size(); c-- > 0;) {   // chunked root fronts, chunks in reverse
+            const LevelPlan::SolveChunk& ch = P.chunks[c];
+            {
+                LaunchScope ls(h, SPK_K_BWD, ch.rec.flops * nrhs, ch.rec.words * sizeof(T));
+                if (h->fc16)
+                    spk::k_front_solve<T, false, 16><<<16, spk::FC_THREADS, fc_smem, st>>>(fac, inv, y, x, n, nrhs,
+                                                                                          S, launch_of(PL, ch.rec));
+                else
+                    spk::k_front_solve<T, false, spk::FC><<<spk::FC, spk::FC_THREADS, fc_smem, st>>>(
+                        fac, inv, y, x, n, nrhs, S, launch_of(PL, ch.rec));
+            }
+            if (c > 0 && P.chunks[c - 1].front == ch.front) {   // rows above the chunk
+                const HFront& F = h->fronts[ch.front];
+                const int r0 = 0, r1 = ch.lo;
+                LaunchScope ls(h, SPK_K_BWD, 2.0 * (r1 - r0) * (ch.hi - ch.lo) * nrhs,
+                               (double)(r1 - r0) * (ch.hi - ch.lo) * sizeof(T));
+                const int grid = spk::cdiv(r1 - r0, spk::L21_ROWS) * spk::cdiv(ch.hi - ch.lo, spk::L21_COLS);
+                spk::k_front_gemv<T><<<grid, 256, 0, st>>>(fac, y, (const T*)x, n, nrhs, F.loff, F.nf + F.m,
+                                                          (int)F.f, r0, r1, ch.lo, ch.hi);
+            }
         }
         for (size_t t = 0; t < P.bwd_small.size(); ++t)
             if (P.bwd_small[t].tiles > 0) {
@@ -2195,6 +2275,13 @@ int spk_set_option(spk_handle* h, int option, int64_t value) {
         h->schur_far_sms = (int)value;
         drop_factor_graphs(h);
         return SPK_OK;
+    case SPK_OPT_SOLVE_CHUNK:
+        if (value != 0 && value != 1) break;
+        if (h->solve_chunk != (int)value) {
+            h->solve_chunk = (int)value;
+            reset_plans_keep_factors(h);
+        }
+        return SPK_OK;
     case SPK_OPT_TC_SCHUR_M:
     case SPK_OPT_TC_TRAIL_ROWS:
     case SPK_OPT_TC_WIDE: {
@@ -2229,6 +2316,7 @@ int spk_get_option(spk_handle* h, int option, int64_t* value) {
     case SPK_OPT_PANEL_SPLIT: *value = h->panel_split; return SPK_OK;
     case SPK_OPT_SCHUR_SPLIT: *value = h->schur_split; return SPK_OK;
     case SPK_OPT_SCHUR_FAR_SMS: *value = h->schur_far_sms; return SPK_OK;
+    case SPK_OPT_SOLVE_CHUNK: *value = h->solve_chunk; return SPK_OK;
     default: return set_err(h, SPK_EARG, "spk_get_option: unknown option");
     }
 }

@@ -3244,6 +3244,48 @@ __global__ void __launch_bounds__(256) k_fwd_l21(const T* fac, T* b, const T* y,
     }
 }
 
+// A root front (no rows below it) of more blocks than a cluster solves well
+// in one launch is solved in chunks of consecutive blocks, a cluster launch
+// each; between two of them every SM takes part in the rectangular product
+// that links them: out[f + r] -= sum_c A(r, c) in[f + c] over rows
+// [r0, r1) and columns [c0, c1) of the front (A(r, c) = fac[loff + c ld +
+// r]; forward the L rows below the chunk, backward the U rows above it).
+// Tiles of L21_ROWS rows x L21_COLS columns, atomics as k_fwd_l21.
+constexpr int FC_CHUNK = 16;   // blocks per chunk at most
+template <typename T>
+__global__ void __launch_bounds__(256) k_front_gemv(const T* fac, T* out, const T* in, int n, int nrhs, ll loff, int ld,
+                                                    int f, int r0, int r1, int c0, int c1) {
+    __shared__ T sv[L21_COLS * FC_RG];
+    const int nrt = cdiv(r1 - r0, L21_ROWS);
+    const int i0 = r0 + (int)(blockIdx.x % nrt) * L21_ROWS, k0 = c0 + (int)(blockIdx.x / nrt) * L21_COLS;
+    const int nk = min(L21_COLS, c1 - k0), i = i0 + threadIdx.x;
+    const bool ok = i < r1;
+    const T* a = fac + loff + (ll)k0 * ld + (ok ? i : 0);
+    for (int q0 = 0; q0 < nrhs; q0 += FC_RG) {
+        const int nr = min(FC_RG, nrhs - q0);
+        if (q0 > 0) __syncthreads();
+        for (int e = threadIdx.x; e < L21_COLS * FC_RG; e += blockDim.x) {
+            const int k = e % L21_COLS, r = e / L21_COLS;
+            sv[e] = (k < nk && r < nr) ? in[(ll)(q0 + r) * n + f + k0 + k] : T(0);
+        }
+        __syncthreads();
+        T acc[FC_RG];
+#pragma unroll
+        for (int r = 0; r < FC_RG; ++r) acc[r] = T(0);
+        if (ok) {
+#pragma unroll 16
+            for (int k = 0; k < nk; ++k) {
+                const T av = a[(ll)k * ld];
+#pragma unroll
+                for (int r = 0; r < FC_RG; ++r) acc[r] += av * sv[r * L21_COLS + k];
+            }
+#pragma unroll
+            for (int r = 0; r < FC_RG; ++r)
+                if (r < nr) atomicAdd(&out[(ll)(q0 + r) * n + f + i], -acc[r]);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Transposed solves, A^T x = b with the same factors (no reference kernel:
 // the reference's `transposetriangularsolve` is commented out,

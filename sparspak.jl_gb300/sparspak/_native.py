@@ -71,7 +71,7 @@ SPK_ETIMEOUT = -8
 # spk_set_option / spk_get_option
 OPTIONS = {"leaf_queue": 0, "wait_budget": 1, "stall_test": 2, "tc_schur_m": 3, "tc_trail_rows": 4, "tc_wide": 5,
            "lu_pieces": 6, "solve_cluster_minb": 7, "panel_split": 8,
-           "schur_split": 9, "schur_far_sms": 10}
+           "schur_split": 9, "schur_far_sms": 10, "solve_chunk": 11}
 SPK_HOST, SPK_DEVICE = 0, 1
 KERNEL_CLASSES = ["assemble", "getrf", "panel", "trail", "schur", "fwd", "bwd", "permute", "residual", "blockinv",
                   "tc_trail", "tc_schur"]

@@ -26,6 +26,11 @@ option autotuner, through the C ABI.
   factored two or more levels up run on a third stream beside the next
   level) gives the same factors to FP32 rounding (atomic scatter-adds in
   another order) in the FP32, BF16 and SPD forms, and both refine to 1e-12.
+* Chunked root-front solves (SPK_OPT_SOLVE_CHUNK: a root front of more
+  than 16 blocks in chunks of at most 16, linked by a product over all SMs)
+  change only the solves' launch lists: the solutions agree with the single
+  cluster launch to 1e-12 (FP64) and refine to 1e-12 (FP32), forward and
+  backward, one and several right-hand sides.
 * spk_autotune chooses options from its set, leaves A assembled, and the
   factor that follows refines to 1e-12.
 """
@@ -234,6 +239,35 @@ def test_schur_split_matches_one_launch(prec):
     assert rel(xs[1], xs[0]) < 1e-10
     with pytest.raises(S.ErrorException):
         eng.set_option("schur_split", 2)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp64+spd"])
+def test_chunked_root_solve_matches_one_cluster(prec):
+    # 48^3: the root separator (2304 columns) is 18 blocks of 128 (FP32) or
+    # 36 of 64 (FP64), more than one cluster's 16
+    A = S.gallery.laplacian((48, 48, 48), shift=1e-3)
+    n = A.shape[0]
+    base, _, form = prec.partition("+")
+    s = _solver(A, S.nd_grid(48, 48, 48), precision=base, spd=form == "spd")
+    eng = _factor_with(s, A)
+    for nrhs in (1, 5):
+        b = S.gallery.random_rhs(n, nrhs, seed=20 + nrhs)
+        xs = {}
+        for ch in (1, 0):
+            eng.set_option("solve_chunk", ch)   # no new factorisation
+            if base == "fp64":
+                xs[ch] = eng.solve(np.array(b, order="F"), prec)
+                assert relres(A, xs[ch], b) <= 1e-12, (ch, nrhs)
+            else:
+                x = np.zeros_like(b, order="F")
+                it, rr = eng.refine(np.asfortranarray(b), x, prec, 1e-12, 30)
+                assert rr <= 1e-12 and relres(A, x, b) <= 1e-12, (ch, nrhs, rr)
+                xs[ch] = x
+        d = rel(xs[1], xs[0])
+        print(f"{prec} nrhs={nrhs}: chunked vs one cluster, solutions differ by {d:.1e}")
+        assert d < 1e-10
+    with pytest.raises(S.ErrorException):
+        eng.set_option("solve_chunk", 2)
 
 
 def test_solve_cluster_threshold_keeps_factors():
