@@ -506,8 +506,22 @@ def run_ours(args):
     def fwd_err(x):
         return float(np.max(np.abs(x - x_fp64)) / np.max(np.abs(x_fp64)))
 
-    def traffic_of(cls):
-        """DRAM bytes per launch of the class's FP32 kernels from the committed ncu summary (40^3 capture)."""
+    def traffic_of(cls, alg_per_launch=None):
+        """DRAM bytes per launch of the class's FP32 kernels from the committed ncu summaries: the block-LU
+        class from sampled 64^3 launches (DRAM / algorithmic bytes of a one-block launch, scaled by the
+        blocks a launch processes), the others from the 40^3 capture."""
+        p64 = os.path.join(ROOT, "profiles", "dram_traffic_k_block_lu_laplace3d64.md")
+        if cls == "getrf" and alg_per_launch and os.path.exists(p64):
+            ratio = None
+            for line in open(p64):
+                if line.startswith("therefore ") and "x the algorithmic bytes" in line:
+                    ratio = float(line.split()[1].rstrip("x"))
+            if ratio:
+                return ratio * alg_per_launch, (
+                    f"64^3: ncu dram__bytes_read.sum + dram__bytes_write.sum of sampled one-block k_block_lu "
+                    f"launches is {ratio:.2f}x their algorithmic bytes "
+                    f"(profiles/dram_traffic_k_block_lu_laplace3d64.md); scaled by the algorithmic bytes per "
+                    f"launch of the class (the same ratio taken for its small-front kernels)")
         names = {"getrf": ("k_block_lu<float>", "k_block_lu_small<float>", "k_leaf_factor<float>"),
                  "panel": ("k_block_panel<float",),
                  "trail": ("k_block_trail<float>",), "schur": ("k_schur<float>",),
@@ -551,13 +565,13 @@ def run_ours(args):
             achieved = d["bytes"] / (d["ms"] * 1e-3) / 1e9
             roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                     "peak_kind": f"{pk_kind} HBM copy bandwidth"}
-        traffic, tnote = traffic_of(cls)
+        alg = (d["flops"] if roof["bound"] == "tensor" else d["bytes"]) / max(d["launches"], 1)
+        traffic, tnote = traffic_of(cls, d["bytes"] / max(d["launches"], 1))
         roof.update({"frac": roof["achieved"] / roof["peak"], "traffic": traffic, "traffic_unit": "bytes/launch",
                      "traffic_note": tnote,
                      "kernel": S._native.KERNEL_NAMES[cls] + f" ({kind})", "launches": d["launches"],
                      "ms_per_launch": d["ms"] / max(d["launches"], 1),
-                     "algorithmic_per_launch": (d["flops"] if roof["bound"] == "tensor" else d["bytes"])
-                     / max(d["launches"], 1)})
+                     "algorithmic_per_launch": alg})
         return roof
 
     roof = roofline_of(dom, live)

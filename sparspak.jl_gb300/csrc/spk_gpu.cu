@@ -865,7 +865,7 @@ static void build_plan(const spk_handle* h, Plan& P, int bmax, bool tc, bool sym
                 const int ld = F.nf + F.m;
                 tl[k] = leafF[k] ? 0 : 1;
                 fl[k] = 2.0 * bw * bw * bw;
-                wl[k] = 4.0 * bw * bw;
+                wl[k] = 2.0 * bw * bw + 2.0 * bw;   // the block read and written once, its pivots and row sources
                 const int lpt = panel_lines(tc, wide[t]);
                 // the SPD form launches the L-panel tiles only (they also write the U side)
                 tp[k] = leafF[k] ? 0 : cdiv(ld - c1, lpt) + (sym ? 0 : cdiv(F.nf - c1, lpt) + cdiv(F.m, lpt));
