@@ -1448,7 +1448,7 @@ __device__ __forceinline__ void block_panel128(float* fac, const int* bmap, cons
 // of it: the lines the next block's diagonal region is updated from); 2 the
 // others.  Tiles of 64 lines: L rows first (nL tiles), then front columns
 // (nUa), then U12 columns.
-__device__ __forceinline__ int panel_tile(int part, int tile, int nL, int nUa, bool sym) {
+__host__ __device__ __forceinline__ int panel_tile(int part, int tile, int nL, int nUa, bool sym) {
     if (part == 0) return tile;
     const int aL = min(2, nL), aU = sym ? 0 : min(2, nUa);
     if (part == 1) return tile < aL ? tile : nL + (tile - aL);
