@@ -3205,7 +3205,7 @@ __global__ void __launch_bounds__(256) k_solve_leaf(const T* fac, const T* inv2,
 // Tiles of 256 R_F rows x 128 front columns; a thread takes one row
 // (L21 column k contiguous in Lf), y_F of the tile's columns in shared
 // memory, partial sums added to b with atomics.
-constexpr int L21_ROWS = 256, L21_COLS = 128;
+constexpr int L21_ROWS = 256, L21_COLS = 64;   // 64 columns: twice the CTAs and loads in flight of 128
 template <typename T>
 __global__ void __launch_bounds__(256) k_fwd_l21(const T* fac, T* b, const T* y, int n, int nrhs, Sched S, Launch L) {
     __shared__ T sy[L21_COLS * FC_RG];
