@@ -120,7 +120,7 @@ def test_convection_diffusion_pivots_identity():
     A = S.gallery.convection_diffusion(k=10)
     s, o = run_both(A, S.nd_grid(10, 10, 10, leaf=16))
     check_factors(s, o)
-    # an M-matrix (diagonally dominant by columns): every in-block pivot is the diagonal
+    # an M-matrix: every in-block pivot is the diagonal
     b = s.slvr
     ident = np.concatenate([np.arange(1, b.xsuper[k + 1] - b.xsuper[k] + 1) for k in range(b.nsuper)])
     assert np.array_equal(b.ipiv, ident)
