@@ -44,3 +44,24 @@ def test_gpu_lib_reports_no_device_cleanly():
                         ctypes.byref(h))
     assert rc == N.SPK_ECUDA
     assert "CUDA" in lib.spk_last_error(None).decode() or "device" in lib.spk_last_error(None).decode()
+
+
+def _defines(prefix):
+    text = open(os.path.join(ROOT, "include", "spk_gpu.h")).read()
+    return {m.group(1): int(m.group(2)) for m in re.finditer(rf"#define ({prefix}[A-Z0-9_]+) (-?\d+)", text)}
+
+
+def test_python_constants_match_the_header():
+    # the option codes, status codes and kernel classes the Python mirror
+    # passes through the C ABI are the header's
+    from sparspak import _native as N
+
+    opts = _defines("SPK_OPT_")
+    assert {("SPK_OPT_" + k.upper()): v for k, v in N.OPTIONS.items()} == opts
+    status = _defines("SPK_E")
+    for name, v in status.items():
+        assert getattr(N, name) == v, name
+    classes = {k: v for k, v in _defines("SPK_K_").items() if k != "SPK_K_COUNT"}
+    assert len(N.KERNEL_CLASSES) == len(classes) == _defines("SPK_K_")["SPK_K_COUNT"]
+    for name, v in classes.items():
+        assert N.KERNEL_CLASSES[v] == name[len("SPK_K_"):].lower(), name
